@@ -1,0 +1,306 @@
+"""Benchmark of the GB300 KNP backend on the large sparse plain configuration.
+
+Workload (one GPU): 1,000,000 BLIFAT neurons (reference defaults), fixed fan-in 1000 from uniform
+random presynaptic sources (1e9 delta synapses; int32 index, FP32 weight k/256 with k in [-16, 48],
+u8 delay in 1..20), Bernoulli background drive p = 0.005 per neuron per step through a one-to-one
+projection (w = 1.0, delay 1). A step is one simulation step of the whole network. The synapse
+arrays (9 GB) are far larger than L2, so no L2 flush is needed between steps.
+
+value      synaptic events/s with the background schedule already in HBM, CUDA-event timed.
+e2e        the same metric through the C ABI with host buffers: every step the host sends the
+           step's background spikes (pinned host -> device) and reads the population's spikes back.
+roofline   the dominant kernel phase (projection scatter), algorithmic bytes 9 B per synaptic event
+           + 8 B per presynaptic spike row, divided by its CUDA-event time measured here.
+cpu_baseline / --impl reference: the CPU oracle (restated single-threaded backend step) on a
+           bounded sample: the same configuration at 1/100 scale.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "synaptic events/s per GB300, plain vs batched BF16 form, at ≤0.1% spike mismatch"
+UNIT = "events/s"
+SEED = 2
+N = 1_000_000
+FAN_IN = 1000
+P_BG = 0.005
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler (SM clock, max clock, throttle reasons) running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() in ("active", "0x1") or v == "1":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_large(b, n=N, fan_in=FAN_IN):
+    from knp_gb300 import network as Nw
+    from knp_gb300 import types as T
+
+    pop_uid, rec_uid, bg_uid, chan_uid = (T.uid_from_int(SEED * 100 + i) for i in (1, 2, 3, 4))
+    pop = Nw.Population(pop_uid, T.BLIFAT, T.blifat_defaults(n))
+    ar = np.arange(n, dtype=np.uint32)
+    bg = Nw.Projection(bg_uid, T.DELTA, T.NULL_UID, pop_uid, ar, ar.copy(), np.ones(n, np.float32),
+                       np.ones(n, np.uint32))
+    b.load_populations([pop])
+    b.load_projections([bg])
+    b.generate_fixed_fan_in_projection(rec_uid, pop_uid, pop_uid, n, n, fan_in, -16, 48, 1, 20, SEED,
+                                       Nw.LARGE_SEED_STREAM)
+    b.subscribe(bg_uid, [chan_uid])
+    return pop_uid, chan_uid
+
+
+def cpu_baseline_sample(target_s: float = 15.0):
+    """Restated single-threaded oracle on the large sparse config at 1/100 scale (10k neurons,
+    fan-in 1000): events/s of its step loop."""
+    from knp_gb300 import network as Nw
+    from oracle import oracle as orc
+
+    n = 10_000
+    steps = 200
+    net, sched = Nw.large_sparse_network(seed=SEED, n=n, fan_in=FAN_IN, steps=steps)
+    o = orc.OracleNet("restated")
+    o.load(net)
+    t0 = time.perf_counter()
+    done = 0
+    for t in range(steps):
+        idx = sched[0].at(t)
+        if idx.size:
+            o.send_spikes(sched[0].sender, idx, t)
+        o.step()
+        done += 1
+        if time.perf_counter() - t0 > target_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": o.events / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"large sparse config at 1/100 scale ({n} neurons, fan-in {FAN_IN}), {done} steps, "
+                      f"{o.events} events, {dt:.1f} s, restated single-threaded backend step"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cb = cpu_baseline_sample(target_s=max(5.0, min(60.0, 2.0 * args.steps)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+            "config": {"workload": "large_sparse_plain at 1/100 scale on the host CPU",
+                       "neurons": 10_000, "fan_in": FAN_IN, "p_background": P_BG},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--profile-steps", type=int, default=50)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    from knp_gb300 import backend as B
+    from knp_gb300 import network as Nw
+
+    b = B.GB300Backend(local)
+    t_build = time.perf_counter()
+    pop_uid, chan_uid = build_large(b)
+    b._init()
+    total_steps = args.warmup + args.steps + args.profile_steps
+    b.generate_bernoulli_schedule(chan_uid, N, P_BG, 0, total_steps, seed=SEED + 1000 * rank)
+    t_build = time.perf_counter() - t_build
+
+    b.step(args.warmup)
+    b.synchronize()
+    if dist is not None:
+        dist.barrier()
+    ev0, sp0, _ = b.counters()
+    with Clocks(local) as clk:
+        ms = b.step_timed(args.steps)
+    ev1, sp1, _ = b.counters()
+    t = ms / 1e3
+    if dist is not None:
+        import torch
+
+        tt = torch.tensor([t], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+        ee = torch.tensor([float(ev1 - ev0)], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(ee)
+        events_all = float(ee.item())
+    else:
+        events_all = float(ev1 - ev0)
+    events = ev1 - ev0
+    spikes = sp1 - sp0
+    value = events_all / t
+
+    # Live per-phase timing of the same steps (kernels launched one by one, CUDA events between phases).
+    e0, s0, _ = b.counters()
+    ph = b.profile_phases(args.profile_steps)
+    e1, s1, _ = b.counters()
+    p_events = (e1 - e0) / args.profile_steps
+    p_spikes = (s1 - s0) / args.profile_steps
+    hbm, src = peaks()
+    proj_ms = ph[1] / args.profile_steps
+    pop_ms = ph[0] / args.profile_steps
+    # Spike rows walked per step: population spikes through the recurrent projection + background
+    # spikes through the one-to-one projection (each a row_ptr pair).
+    bg_per_step = P_BG * N
+    proj_bytes = 9.0 * p_events + 8.0 * (p_spikes + bg_per_step)
+    pop_bytes = 32.0 * N
+    dominant = "projection" if proj_ms >= pop_ms else "population"
+    a_bytes, a_ms = (proj_bytes, proj_ms) if dominant == "projection" else (pop_bytes, pop_ms)
+    achieved = a_bytes / (a_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": f"{dominant} phase", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                "phase_ms_per_step": {"population": pop_ms, "projection": proj_ms,
+                                      "stdp": ph[2] / args.profile_steps, "step_end": ph[3] / args.profile_steps},
+                "algorithmic_bytes_per_step": {"projection": proj_bytes, "population": pop_bytes},
+                "whole_step_hbm_frac": (proj_bytes + pop_bytes) / (ms / args.steps / 1e3) / 1e9 / hbm}
+
+    # End to end through the C ABI with host buffers.
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        start = b.get_step()
+        sched = Nw.bernoulli_schedule(chan_uid, SEED + 7, N, args.e2e_steps, P_BG, step0=start)
+        b.record_spikes(pop_uid, True)
+        b.synchronize()
+        ea, _, _ = b.counters()
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for k in range(args.e2e_steps):
+            idx = sched.at(k)
+            b.send_spikes(chan_uid, idx, start + k)
+            h2d += idx.nbytes
+            b.step(1)
+            out = b.spikes(pop_uid, start + k)
+            d2h += out.nbytes
+        b.synchronize()
+        te = time.perf_counter() - t0
+        eb, _, _ = b.counters()
+        e2e = {"value": (eb - ea) / te, "unit": UNIT, "h2d_bytes_per_step": h2d / args.e2e_steps,
+               "d2h_bytes_per_step": d2h / args.e2e_steps, "steps": args.e2e_steps,
+               "ms_per_step": te / args.e2e_steps * 1e3}
+        b.record_spikes(pop_uid, False)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded counter-based generator)",
+            "config": {"workload": "large_sparse_plain", "neurons": N, "fan_in": FAN_IN, "synapses": N * FAN_IN,
+                       "delays": "1..20", "weights": "k/256, k in [-16,48]", "p_background": P_BG,
+                       "l2": "inputs larger than L2 (9 GB synapse arrays), no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "neuron_updates_per_s": N * world * args.steps / t,
+            "firing_rate": spikes / (N * args.steps),
+            "events_per_step": events / args.steps,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 4 * args.steps,
+            "clocks": clk.summary(),
+            "build_s": t_build,
+        }
+        print(json.dumps(line))
+    b.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

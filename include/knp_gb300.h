@@ -1,0 +1,251 @@
+/*
+ * knp_gb300 — C ABI of the GB300 (sm_103a) KNP backend: BLIFAT and synaptic-resource-STDP BLIFAT
+ * populations, delta-synapse and additive-STDP delta-synapse projections.
+ *
+ * Every entry point replaces one operation of the KNP backend plugin interface
+ * knp::core::Backend (knp/core-library/include/knp/core/backend.h) as the single-threaded CPU
+ * backend implements it (knp/backends/cpu/cpu-single-threaded-backend/...). The reference interface is
+ * C++ (std::shared_ptr<Backend>, variants of Population<Neuron>/Projection<Synapse>, messages on a
+ * MessageBus); this ABI carries the same data as plain pointers and sizes:
+ *   - populations as arrays of knp_blifat_neuron (+ knp_resource_stdp_state) structs,
+ *   - projections as synapse arrays (pre index, post index, weight, delay, output type, STDP taus),
+ *   - SpikeMessages as (sender UID, send time, index array),
+ *   - SynapticImpactMessages to a population as (sender, receiver, is_forcing, impact arrays).
+ * All buffers are caller-owned host memory unless a name says "device". Every call returns 0 on
+ * success or a negative knp_gb300_status; knp_gb300_last_error() describes the last failure of the
+ * calling thread. A backend handle is used by one thread at a time (as a reference backend is: one
+ * step at a time, no reentrancy).
+ */
+#ifndef KNP_GB300_H
+#define KNP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "knp_gb300_types.h"
+
+#if defined(__GNUC__)
+#define KNP_GB300_API __attribute__((visibility("default")))
+#else
+#define KNP_GB300_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct knp_gb300_backend knp_gb300_backend;
+
+typedef enum knp_gb300_status
+{
+    KNP_GB300_OK = 0,
+    KNP_GB300_E_INVALID = -1,      /* bad argument, unknown UID, unsupported type */
+    KNP_GB300_E_STATE = -2,        /* call not allowed in the current state (e.g. load after init) */
+    KNP_GB300_E_CUDA = -3,         /* CUDA runtime error */
+    KNP_GB300_E_DEVICE_FLAG = -4,  /* a kernel reported an error through the device error word */
+    KNP_GB300_E_NOMEM = -5         /* device allocation failed */
+} knp_gb300_status;
+
+/** Accumulator mode of a population's input ring. */
+typedef enum knp_gb300_accumulator
+{
+    KNP_GB300_ACC_AUTO = 0,  /* FP32 when every incoming weight is a dyadic k/256 with bounded sums, else FIXED64 */
+    KNP_GB300_ACC_FP32 = 1,  /* FP32 atomics: exact for dyadic weights, otherwise order-dependent rounding */
+    KNP_GB300_ACC_FIXED64 = 2 /* int64 fixed point (2^-40): order-independent, exact for |w| >= 2^-17 */
+} knp_gb300_accumulator;
+
+/** Message text of the last failed call on this thread (never NULL). */
+KNP_GB300_API const char *knp_gb300_last_error(void);
+
+/** Library version string. */
+KNP_GB300_API const char *knp_gb300_version(void);
+
+/**
+ * Create a backend on CUDA device `device`.
+ * Replaces: SingleThreadedCPUBackend::create()
+ *   (knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:48-52) reached through the exported
+ *   alias create_knp_backend (:340) and BackendLoader::load (knp/base-framework/impl/backend_loader.cpp:57-68).
+ */
+KNP_GB300_API int knp_gb300_create(int device, knp_gb300_backend **out);
+
+/** Destroy a backend and free its device memory. Replaces: Backend::~Backend (backend.h:70). */
+KNP_GB300_API int knp_gb300_destroy(knp_gb300_backend *b);
+
+/**
+ * Load a BLIFAT (kind KNP_NEURON_BLIFAT) or resource-STDP BLIFAT (KNP_NEURON_RESOURCE_STDP_BLIFAT,
+ * `ext` required) population of `n` neurons. Neuron order is the population's index order.
+ * Replaces: load_populations / load_all_populations for Population<BLIFATNeuron> and
+ *   Population<SynapticResourceSTDPBLIFATNeuron> (cpu-single-threaded-backend/include/knp/backends/
+ *   cpu-single-threaded/backend.h:199; core backend.h:146; impl/backend.cpp:144-186).
+ */
+KNP_GB300_API int knp_gb300_load_blifat_population(
+    knp_gb300_backend *b, knp_uid uid, int kind, uint32_t n, const knp_blifat_neuron *neurons,
+    const knp_resource_stdp_state *ext);
+
+/**
+ * Load a projection of `n_syn` synapses given in the reference's synapse order: synapse i is
+ * (weight[i], delay[i], out_type[i]) from presynaptic neuron pre[i] to postsynaptic neuron post[i].
+ * kind: KNP_SYNAPSE_DELTA or KNP_SYNAPSE_ADDITIVE_STDP_DELTA (tau_plus/tau_minus required, uniform
+ * per projection). out_type may be NULL (all EXCITATORY). pre_uid may be the all-zero UID (the
+ * projection then receives spikes only through knp_gb300_subscribe). KNP_OUT_BLOCKING is rejected:
+ * its last-writer-wins effect depends on message order. Replaces: load_projections /
+ * load_all_projections for Projection<DeltaSynapse> and Projection<AdditiveSTDPDeltaSynapse>
+ * (backend.h:206; core backend.h:137; impl/backend.cpp:158-178).
+ */
+KNP_GB300_API int knp_gb300_load_projection(
+    knp_gb300_backend *b, knp_uid uid, int kind, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn,
+    const uint32_t *pre, const uint32_t *post, const float *weight, const uint32_t *delay,
+    const uint8_t *out_type, const float *tau_plus, const float *tau_minus);
+
+/**
+ * Generate, on the device, a delta projection with fixed fan-in: synapse i has post = i % n_post,
+ * pre = uniform [0, n_pre), weight = k/256 with k uniform in [k_lo, k_hi], delay uniform in
+ * [d_lo, d_hi], drawn from the counter-based generator keyed by (seed, stream). Equivalent to
+ * knp_gb300_load_projection with the arrays of knp_gb300/network.py:fixed_fan_in_pre, without
+ * materialising them on the host. Replaces: Projection construction from the FixedNumberPre
+ * generator (knp/base-framework/include/knp/framework/projection/synapse_generators.h:410-457).
+ */
+KNP_GB300_API int knp_gb300_generate_fixed_fan_in_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint32_t n_pre, uint32_t n_post,
+    uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream);
+
+/**
+ * Register `pop_uid` in an STDP projection's stdp_populations_ map with processing type
+ * KNP_STDP_ONLY or KNP_STDP_AND_SPIKE. Replaces: writing
+ * Projection<STDP<...>>::get_shared_parameters().stdp_populations_ (knp/core-library/include/knp/core/projection.h:133-164).
+ */
+KNP_GB300_API int knp_gb300_set_stdp_population(knp_gb300_backend *b, knp_uid proj_uid, knp_uid pop_uid, int processing);
+
+/**
+ * Subscribe `receiver` (a projection: to SpikeMessages; a population: to SynapticImpactMessages) to
+ * messages of `sender` (a population of this backend or an external channel UID).
+ * Replaces: Backend::subscribe<MessageType> (core backend.h:222-226).
+ */
+KNP_GB300_API int knp_gb300_subscribe(knp_gb300_backend *b, knp_uid receiver, knp_uid sender);
+
+/** Force the accumulator mode of a population (before init). */
+KNP_GB300_API int knp_gb300_set_accumulator(knp_gb300_backend *b, knp_uid pop_uid, int mode);
+
+/**
+ * Enable or disable per-step spike recording of a population (SpikeMessages that an output
+ * channel or observer subscribed to this population would receive).
+ * Replaces: an external endpoint subscribing to the population's SpikeMessages
+ *   (knp/base-framework/impl/model_loader.cpp:100-120; knp/tests/backend/single_thread_cpu_test.cpp:76).
+ */
+KNP_GB300_API int knp_gb300_record_spikes(knp_gb300_backend *b, knp_uid pop_uid, int enable);
+
+/**
+ * Build device structures (CSR, rings, subscriptions) and capture the step graph.
+ * Replaces: Backend::_init (core backend.h:314) = cpu::init (knp/backends/cpu/cpu-library/include/
+ *   knp/backends/cpu-library/init.h:93-110) as called by SingleThreadedCPUBackend::_init (impl/backend.cpp:207-214).
+ */
+KNP_GB300_API int knp_gb300_init(knp_gb300_backend *b);
+
+/**
+ * Send an external SpikeMessage {sender, send_time, indexes[n]}; it is delivered at the next step to
+ * every projection subscribed to `sender`. Replaces: MessageEndpoint::send_message of a SpikeMessage
+ *   by an input channel (knp/base-framework/include/knp/framework/io/input_channel.h:99-120).
+ */
+KNP_GB300_API int knp_gb300_send_spikes(knp_gb300_backend *b, knp_uid sender, uint64_t send_time, uint32_t n, const uint32_t *idx);
+
+/**
+ * Upload a whole external spike schedule for `sender` to device memory: step t (t in
+ * [first_step, first_step + n_steps)) sends idx[offsets[t - first_step] : offsets[t - first_step + 1]].
+ * Replaces: an input channel's per-step SpikeMessages, staged on the device ahead of time.
+ */
+KNP_GB300_API int knp_gb300_load_spike_schedule(
+    knp_gb300_backend *b, knp_uid sender, uint64_t first_step, uint64_t n_steps, const int64_t *offsets,
+    const uint32_t *idx);
+
+/**
+ * Generate on the device a Bernoulli schedule for `sender`: source s spikes at step t iff the
+ * counter-based generator (seed, stream, t * n_sources + s) is below probability p.
+ */
+KNP_GB300_API int knp_gb300_generate_bernoulli_schedule(
+    knp_gb300_backend *b, knp_uid sender, uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps,
+    uint64_t seed, uint64_t stream);
+
+/**
+ * Send an external SynapticImpactMessage to population `receiver` (impacts post_idx[i], value[i],
+ * out_type[i] (NULL = EXCITATORY)); applied at the next step, after impacts of the backend's own
+ * projections. Replaces: MessageEndpoint::send_message of a SynapticImpactMessage
+ *   (knp/tests/framework/lif_test.cpp:78-86).
+ */
+KNP_GB300_API int knp_gb300_send_impacts(
+    knp_gb300_backend *b, knp_uid sender, knp_uid receiver, int is_forcing, uint32_t n, const uint32_t *post_idx,
+    const float *value, const uint8_t *out_type);
+
+/**
+ * Advance `n_steps` steps. Replaces: `n_steps` calls of Backend::_step (core backend.h:321;
+ *   cpu-single-threaded-backend/impl/backend.cpp:89-141), as driven by Backend::start (core impl/backend.cpp:116-141).
+ */
+KNP_GB300_API int knp_gb300_step(knp_gb300_backend *b, uint64_t n_steps);
+
+/** Current step number. Replaces: Backend::get_step (core backend.h:290). */
+KNP_GB300_API int knp_gb300_get_step(const knp_gb300_backend *b, uint64_t *step);
+
+/**
+ * Spike indexes (ascending) that population `pop` emitted at step `step`, which must be among the
+ * steps run since recording was enabled and not yet discarded. Writes min(count, cap) indexes and
+ * the full count to *n. Replaces: receiving the population's SpikeMessage of that step on a
+ * subscribed endpoint (single_thread_cpu_test.cpp:85, tests_messaging_common.h:48-56).
+ */
+KNP_GB300_API int knp_gb300_read_spikes(
+    knp_gb300_backend *b, knp_uid pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n);
+
+/** Discard recorded spikes of steps before `step` (frees log space). */
+KNP_GB300_API int knp_gb300_discard_spikes(knp_gb300_backend *b, uint64_t step);
+
+/**
+ * Read back a BLIFAT population's neurons (and, for resource-STDP BLIFAT, `ext`, may be NULL).
+ * Replaces: get_network_data population range (core backend.h:420;
+ *   cpu-single-threaded-backend/impl/get_network.cpp:80-93).
+ */
+KNP_GB300_API int knp_gb300_read_blifat_population(
+    knp_gb300_backend *b, knp_uid pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext);
+
+/** Read back projection weights in the order the synapses were loaded. Replaces: get_network_data projection range. */
+KNP_GB300_API int knp_gb300_read_weights(knp_gb300_backend *b, knp_uid proj, float *out);
+
+/** Number of synapses of a loaded projection. */
+KNP_GB300_API int knp_gb300_projection_size(const knp_gb300_backend *b, knp_uid proj, uint64_t *n);
+
+/**
+ * Unlock / lock projection weights. Replaces: start_learning / stop_learning
+ * (cpu-single-threaded-backend/include/.../backend.h:315-332). As in the reference, additive-STDP
+ * weight updates ignore the lock (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/impl/
+ * projections/training/stdp/additive_stdp.h:173-196); the flag is kept for get/set symmetry.
+ */
+KNP_GB300_API int knp_gb300_start_learning(knp_gb300_backend *b);
+KNP_GB300_API int knp_gb300_stop_learning(knp_gb300_backend *b);
+
+/**
+ * Cumulative counters since init: synaptic events (impacts created), spikes emitted by all
+ * populations, and neuron updates. Any pointer may be NULL.
+ */
+KNP_GB300_API int knp_gb300_counters(knp_gb300_backend *b, uint64_t *events, uint64_t *spikes, uint64_t *neuron_updates);
+
+/**
+ * Time `n_steps` steps with CUDA events on the backend's stream and return the elapsed
+ * milliseconds (device time). The steps run exactly as knp_gb300_step runs them.
+ */
+KNP_GB300_API int knp_gb300_step_timed(knp_gb300_backend *b, uint64_t n_steps, float *ms);
+
+/**
+ * Run `n_steps` steps with the kernels launched one by one (no graph) and CUDA events between the
+ * step phases; ms[0..3] receive the summed device time of the population kernels, the projection
+ * kernels, the STDP kernels and the end-of-step kernel. Results equal knp_gb300_step's.
+ */
+KNP_GB300_API int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms);
+
+/** Block until all queued device work of the backend has finished. */
+KNP_GB300_API int knp_gb300_synchronize(knp_gb300_backend *b);
+
+/** CUDA stream the backend launches on (a cudaStream_t), for callers that order their own work after it. */
+KNP_GB300_API int knp_gb300_stream(knp_gb300_backend *b, void **stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KNP_GB300_H */

@@ -1,0 +1,278 @@
+// extern "C" layer of include/knp_gb300.h over the host runtime: argument checks, exception to
+// status-code translation, thread-local error text.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/knp_gb300.h"
+#include "engine.h"
+
+struct knp_gb300_backend
+{
+    knp_gb300::Backend impl;
+    explicit knp_gb300_backend(int device) : impl(device) {}
+};
+
+namespace
+{
+thread_local std::string g_error;
+
+template <class F>
+int guarded(F &&f)
+{
+    try
+    {
+        f();
+        g_error.clear();
+        return KNP_GB300_OK;
+    }
+    catch (const knp_gb300::Error &e)
+    {
+        g_error = e.what();
+        return e.code();
+    }
+    catch (const std::bad_alloc &)
+    {
+        g_error = "host allocation failed";
+        return KNP_GB300_E_NOMEM;
+    }
+    catch (const std::exception &e)
+    {
+        g_error = e.what();
+        return KNP_GB300_E_INVALID;
+    }
+}
+
+int null_handle()
+{
+    g_error = "null backend handle";
+    return KNP_GB300_E_INVALID;
+}
+
+knp_gb300::Uid U(const knp_uid &u) { return knp_gb300::Uid(u); }
+}  // namespace
+
+extern "C" {
+
+const char *knp_gb300_last_error(void) { return g_error.c_str(); }
+
+const char *knp_gb300_version(void) { return "knp_gb300 0.1.0 (sm_103a)"; }
+
+int knp_gb300_create(int device, knp_gb300_backend **out)
+{
+    if (!out) return null_handle();
+    *out = nullptr;
+    return guarded([&] { *out = new knp_gb300_backend(device); });
+}
+
+int knp_gb300_destroy(knp_gb300_backend *b)
+{
+    if (!b) return null_handle();
+    return guarded([&] { delete b; });
+}
+
+int knp_gb300_load_blifat_population(
+    knp_gb300_backend *b, knp_uid uid, int kind, uint32_t n, const knp_blifat_neuron *neurons,
+    const knp_resource_stdp_state *ext)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.load_blifat(U(uid), kind, n, neurons, ext); });
+}
+
+int knp_gb300_load_projection(
+    knp_gb300_backend *b, knp_uid uid, int kind, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre,
+    const uint32_t *post, const float *weight, const uint32_t *delay, const uint8_t *out_type, const float *tau_plus,
+    const float *tau_minus)
+{
+    if (!b) return null_handle();
+    return guarded(
+        [&]
+        {
+            b->impl.load_projection(U(uid), kind, U(pre_uid), U(post_uid), n_syn, pre, post, weight, delay, out_type,
+                                    tau_plus, tau_minus);
+        });
+}
+
+int knp_gb300_generate_fixed_fan_in_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint32_t n_pre, uint32_t n_post,
+    uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream)
+{
+    if (!b) return null_handle();
+    return guarded(
+        [&]
+        {
+            b->impl.generate_fixed_fan_in(U(uid), U(pre_uid), U(post_uid), n_pre, n_post, fan_in, k_lo, k_hi, d_lo,
+                                          d_hi, seed, stream);
+        });
+}
+
+int knp_gb300_set_stdp_population(knp_gb300_backend *b, knp_uid proj_uid, knp_uid pop_uid, int processing)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.set_stdp_population(U(proj_uid), U(pop_uid), processing); });
+}
+
+int knp_gb300_subscribe(knp_gb300_backend *b, knp_uid receiver, knp_uid sender)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.subscribe(U(receiver), U(sender)); });
+}
+
+int knp_gb300_set_accumulator(knp_gb300_backend *b, knp_uid pop_uid, int mode)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.set_accumulator(U(pop_uid), mode); });
+}
+
+int knp_gb300_record_spikes(knp_gb300_backend *b, knp_uid pop_uid, int enable)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.record_spikes(U(pop_uid), enable != 0); });
+}
+
+int knp_gb300_init(knp_gb300_backend *b)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.init(); });
+}
+
+int knp_gb300_send_spikes(knp_gb300_backend *b, knp_uid sender, uint64_t send_time, uint32_t n, const uint32_t *idx)
+{
+    if (!b) return null_handle();
+    if (n && !idx)
+    {
+        g_error = "null index array";
+        return KNP_GB300_E_INVALID;
+    }
+    return guarded([&] { b->impl.send_spikes(U(sender), send_time, n, idx); });
+}
+
+int knp_gb300_load_spike_schedule(
+    knp_gb300_backend *b, knp_uid sender, uint64_t first_step, uint64_t n_steps, const int64_t *offsets,
+    const uint32_t *idx)
+{
+    if (!b) return null_handle();
+    if (!offsets)
+    {
+        g_error = "null offsets";
+        return KNP_GB300_E_INVALID;
+    }
+    return guarded([&] { b->impl.load_schedule(U(sender), first_step, n_steps, offsets, idx); });
+}
+
+int knp_gb300_generate_bernoulli_schedule(
+    knp_gb300_backend *b, knp_uid sender, uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps,
+    uint64_t seed, uint64_t stream)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.generate_bernoulli(U(sender), n_sources, p, first_step, n_steps, seed, stream); });
+}
+
+int knp_gb300_send_impacts(
+    knp_gb300_backend *b, knp_uid sender, knp_uid receiver, int is_forcing, uint32_t n, const uint32_t *post_idx,
+    const float *value, const uint8_t *out_type)
+{
+    if (!b) return null_handle();
+    if (n && (!post_idx || !value))
+    {
+        g_error = "null impact array";
+        return KNP_GB300_E_INVALID;
+    }
+    return guarded([&] { b->impl.send_impacts(U(sender), U(receiver), is_forcing != 0, n, post_idx, value, out_type); });
+}
+
+int knp_gb300_step(knp_gb300_backend *b, uint64_t n_steps)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.step(n_steps); });
+}
+
+int knp_gb300_get_step(const knp_gb300_backend *b, uint64_t *step)
+{
+    if (!b || !step) return null_handle();
+    *step = b->impl.current_step();
+    return KNP_GB300_OK;
+}
+
+int knp_gb300_read_spikes(knp_gb300_backend *b, knp_uid pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n)
+{
+    if (!b || !n) return null_handle();
+    if (cap && !out)
+    {
+        g_error = "null output array";
+        return KNP_GB300_E_INVALID;
+    }
+    return guarded([&] { b->impl.read_spikes(U(pop), step, cap, out, n); });
+}
+
+int knp_gb300_discard_spikes(knp_gb300_backend *b, uint64_t step)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.discard_spikes(step); });
+}
+
+int knp_gb300_read_blifat_population(
+    knp_gb300_backend *b, knp_uid pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext)
+{
+    if (!b || !out) return null_handle();
+    return guarded([&] { b->impl.read_blifat(U(pop), out, ext); });
+}
+
+int knp_gb300_read_weights(knp_gb300_backend *b, knp_uid proj, float *out)
+{
+    if (!b || !out) return null_handle();
+    return guarded([&] { b->impl.read_weights(U(proj), out); });
+}
+
+int knp_gb300_projection_size(const knp_gb300_backend *b, knp_uid proj, uint64_t *n)
+{
+    if (!b || !n) return null_handle();
+    return guarded([&] { *n = b->impl.projection_size(U(proj)); });
+}
+
+int knp_gb300_start_learning(knp_gb300_backend *b)
+{
+    if (!b) return null_handle();
+    b->impl.set_learning(true);
+    return KNP_GB300_OK;
+}
+
+int knp_gb300_stop_learning(knp_gb300_backend *b)
+{
+    if (!b) return null_handle();
+    b->impl.set_learning(false);
+    return KNP_GB300_OK;
+}
+
+int knp_gb300_counters(knp_gb300_backend *b, uint64_t *events, uint64_t *spikes, uint64_t *neuron_updates)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.counters(events, spikes, neuron_updates); });
+}
+
+int knp_gb300_step_timed(knp_gb300_backend *b, uint64_t n_steps, float *ms)
+{
+    if (!b || !ms) return null_handle();
+    return guarded([&] { *ms = b->impl.step_timed(n_steps); });
+}
+
+int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms)
+{
+    if (!b || !ms) return null_handle();
+    return guarded([&] { b->impl.profile_phases(n_steps, ms); });
+}
+
+int knp_gb300_synchronize(knp_gb300_backend *b)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.synchronize(); });
+}
+
+int knp_gb300_stream(knp_gb300_backend *b, void **stream)
+{
+    if (!b || !stream) return null_handle();
+    *stream = static_cast<void *>(b->impl.stream());
+    return KNP_GB300_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1427 @@
+// Host runtime of the GB300 KNP backend (see engine.h).
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <numeric>
+
+namespace knp_gb300
+{
+
+#define KNP_CUDA(call)                                                                                          \
+    do                                                                                                          \
+    {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                \
+        if (e_ != cudaSuccess)                                                                                  \
+            throw Error(e_ == cudaErrorMemoryAllocation ? KNP_GB300_E_NOMEM : KNP_GB300_E_CUDA,                 \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                    \
+    } while (0)
+
+namespace
+{
+
+uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+
+float to_f(double x) { return static_cast<float>(x); }
+
+bool is_dyadic(float w)
+{
+    const double k = static_cast<double>(w) * 256.0;
+    return std::floor(k) == k && std::fabs(k) < 16777216.0;
+}
+
+// The reference's stdp_w for d >= 0 (additive_stdp.h:50-55 with a_plus = a_minus = 1), evaluated
+// with the host libm exactly as the reference evaluates it; 0 beyond the returned length.
+std::vector<float> stdp_table(float tau_plus, float tau_minus)
+{
+    std::vector<float> t;
+    for (uint64_t d = 0;; ++d)
+    {
+        const float wd = static_cast<float>(d);
+        const float v = wd > 0 ? 1.0F * std::exp(-wd / tau_plus) : 1.0F * std::exp(wd / tau_minus);
+        if (v == 0.0F && d > 0) break;
+        t.push_back(v);
+        if (t.size() > (1u << 24)) break;
+    }
+    return t;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------- DeviceArena
+
+DeviceArena::~DeviceArena()
+{
+    for (void *p : ptrs_) cudaFree(p);
+}
+
+void *DeviceArena::alloc(size_t bytes, bool zero)
+{
+    if (bytes == 0) bytes = 16;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+        throw Error(KNP_GB300_E_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " +
+                                           cudaGetErrorString(e));
+    if (zero) KNP_CUDA(cudaMemset(p, 0, bytes));
+    ptrs_.push_back(p);
+    bytes_ += bytes;
+    return p;
+}
+
+void DeviceArena::release(void *p)
+{
+    auto it = std::find(ptrs_.begin(), ptrs_.end(), p);
+    if (it != ptrs_.end())
+    {
+        cudaFree(p);
+        ptrs_.erase(it);
+    }
+}
+
+// ----------------------------------------------------------------------------------- Backend
+
+Backend::Backend(int device) : device_(device)
+{
+    int n = 0;
+    KNP_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) throw Error(KNP_GB300_E_INVALID, "no CUDA device " + std::to_string(device));
+    KNP_CUDA(cudaSetDevice(device));
+    KNP_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
+    KNP_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    KNP_CUDA(cudaEventCreateWithFlags(&pinned_free_, cudaEventDisableTiming));
+    ctl_ = arena_.make<Control>(1);
+}
+
+Backend::~Backend()
+{
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (graph1_) cudaGraphExecDestroy(graph1_);
+    if (graphK_) cudaGraphExecDestroy(graphK_);
+    for (auto &c : channels_)
+        if (c->owns_generated && c->idx) cudaFree(c->idx);
+    if (pinned_) cudaFreeHost(pinned_);
+    if (pinned_free_) cudaEventDestroy(pinned_free_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Backend::require_not_init(const char *what) const
+{
+    if (initialized_) throw Error(KNP_GB300_E_STATE, std::string(what) + " is not allowed after init");
+}
+
+void Backend::require_init(const char *what) const
+{
+    if (!initialized_) throw Error(KNP_GB300_E_STATE, std::string(what) + " requires init");
+}
+
+PopulationSlot *Backend::find_pop(const Uid &u)
+{
+    for (auto &p : pops_)
+        if (p->uid == u) return p.get();
+    return nullptr;
+}
+
+ProjectionSlot *Backend::find_proj(const Uid &u)
+{
+    for (auto &p : projs_)
+        if (p->uid == u) return p.get();
+    return nullptr;
+}
+
+const ProjectionSlot *Backend::find_proj(const Uid &u) const
+{
+    for (auto &p : projs_)
+        if (p->uid == u) return p.get();
+    return nullptr;
+}
+
+Channel *Backend::find_channel(const Uid &u)
+{
+    for (auto &c : channels_)
+        if (c->uid == u) return c.get();
+    return nullptr;
+}
+
+Channel &Backend::channel(const Uid &u)
+{
+    if (Channel *c = find_channel(u)) return *c;
+    auto c = std::make_unique<Channel>();
+    c->uid = u;
+    c->dev = arena_.make<ChannelDev>(1);
+    channels_.push_back(std::move(c));
+    return *channels_.back();
+}
+
+void Backend::load_blifat(
+    const Uid &uid, int kind, uint32_t n, const knp_blifat_neuron *neurons, const knp_resource_stdp_state *ext)
+{
+    require_not_init("load_blifat_population");
+    if (kind != KNP_NEURON_BLIFAT && kind != KNP_NEURON_RESOURCE_STDP_BLIFAT)
+        throw Error(KNP_GB300_E_INVALID, "unsupported neuron kind " + std::to_string(kind));
+    if (kind == KNP_NEURON_RESOURCE_STDP_BLIFAT && !ext)
+        throw Error(KNP_GB300_E_INVALID, "a resource-STDP population needs its knp_resource_stdp_state array");
+    if (!neurons && n) throw Error(KNP_GB300_E_INVALID, "null neuron array");
+    if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    auto p = std::make_unique<PopulationSlot>();
+    p->uid = uid;
+    p->kind = kind;
+    p->n = n;
+    p->n_pad = round_up(std::max<uint32_t>(n, 1), 4);
+    p->init_blifat.assign(neurons, neurons + n);
+    if (ext) p->init_res.assign(ext, ext + n);
+    pops_.push_back(std::move(p));
+}
+
+void Backend::load_projection(
+    const Uid &uid, int kind, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn, const uint32_t *pre,
+    const uint32_t *post, const float *w, const uint32_t *delay, const uint8_t *type, const float *tau_plus,
+    const float *tau_minus)
+{
+    require_not_init("load_projection");
+    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA)
+        throw Error(KNP_GB300_E_INVALID, "unsupported synapse kind " + std::to_string(kind));
+    if (n_syn && (!pre || !post || !w || !delay)) throw Error(KNP_GB300_E_INVALID, "null synapse array");
+    if (n_syn > 0xFFFFFFFFull) throw Error(KNP_GB300_E_INVALID, "more than 2^32-1 synapses in one projection");
+    if (kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && n_syn && (!tau_plus || !tau_minus))
+        throw Error(KNP_GB300_E_INVALID, "an additive-STDP projection needs tau_plus and tau_minus");
+    if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    auto p = std::make_unique<ProjectionSlot>();
+    p->uid = uid;
+    p->kind = kind;
+    p->pre_uid = pre_uid;
+    p->post_uid = post_uid;
+    p->n_syn = n_syn;
+    p->pre.assign(pre, pre + n_syn);
+    p->post.assign(post, post + n_syn);
+    p->weight.assign(w, w + n_syn);
+    p->delay.assign(delay, delay + n_syn);
+    if (type)
+    {
+        p->type.assign(type, type + n_syn);
+        for (uint8_t t : p->type)
+        {
+            if (t == KNP_OUT_BLOCKING)
+                throw Error(KNP_GB300_E_INVALID,
+                            "BLOCKING synapses are not supported: their effect depends on message order");
+            if (t > KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
+        }
+        if (std::all_of(p->type.begin(), p->type.end(), [&](uint8_t t) { return t == p->type[0]; }) && n_syn)
+        {
+            // Uniform type: keep only the value.
+            const uint8_t t0 = p->type[0];
+            p->type.assign(1, t0);
+        }
+    }
+    for (uint64_t i = 0; i < n_syn; ++i)
+        if (p->delay[i] > 255)
+            throw Error(KNP_GB300_E_INVALID, "synapse delay above 255 steps is not supported");
+    if (kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && n_syn)
+    {
+        p->tau_plus.assign(tau_plus, tau_plus + n_syn);
+        p->tau_minus.assign(tau_minus, tau_minus + n_syn);
+        for (uint64_t i = 0; i < n_syn; ++i)
+            if (p->tau_plus[i] != p->tau_plus[0] || p->tau_minus[i] != p->tau_minus[0])
+                throw Error(KNP_GB300_E_INVALID, "STDP time constants must be uniform within a projection");
+    }
+    projs_.push_back(std::move(p));
+}
+
+void Backend::generate_fixed_fan_in(
+    const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint32_t n_pre, uint32_t n_post, uint32_t fan_in,
+    int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream)
+{
+    require_not_init("generate_fixed_fan_in_projection");
+    const uint64_t n_syn = static_cast<uint64_t>(n_post) * fan_in;
+    if (n_syn > 0xFFFFFFFFull) throw Error(KNP_GB300_E_INVALID, "more than 2^32-1 synapses in one projection");
+    if (k_lo > k_hi || d_lo > d_hi || d_hi > 255 || n_pre == 0)
+        throw Error(KNP_GB300_E_INVALID, "bad generator ranges");
+    if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    auto p = std::make_unique<ProjectionSlot>();
+    p->uid = uid;
+    p->kind = KNP_SYNAPSE_DELTA;
+    p->pre_uid = pre_uid;
+    p->post_uid = post_uid;
+    p->n_syn = n_syn;
+    p->generated = true;
+    p->gen = {n_pre, n_post, fan_in, k_lo, k_hi, d_lo, d_hi, seed, stream};
+    projs_.push_back(std::move(p));
+}
+
+void Backend::set_stdp_population(const Uid &proj, const Uid &pop, int processing)
+{
+    require_not_init("set_stdp_population");
+    ProjectionSlot *p = find_proj(proj);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown projection");
+    if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) throw Error(KNP_GB300_E_INVALID, "not an STDP projection");
+    if (processing != KNP_STDP_ONLY && processing != KNP_STDP_AND_SPIKE)
+        throw Error(KNP_GB300_E_INVALID, "bad STDP processing type");
+    p->stdp_pops[pop] = processing;
+}
+
+void Backend::subscribe(const Uid &receiver, const Uid &sender)
+{
+    require_not_init("subscribe");
+    subs_.emplace_back(receiver, sender);
+}
+
+void Backend::set_accumulator(const Uid &pop, int mode)
+{
+    require_not_init("set_accumulator");
+    PopulationSlot *p = find_pop(pop);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown population");
+    if (mode < KNP_GB300_ACC_AUTO || mode > KNP_GB300_ACC_FIXED64) throw Error(KNP_GB300_E_INVALID, "bad mode");
+    p->acc_request = mode;
+}
+
+void Backend::record_spikes(const Uid &pop, bool enable)
+{
+    PopulationSlot *p = find_pop(pop);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown population");
+    if (initialized_)
+    {
+        drain_recordings();
+        if (enable && !p->log)
+        {
+            const uint64_t per = std::max<uint64_t>(p->n, 1);
+            const uint64_t steps = std::max<uint64_t>(1, std::min<uint64_t>(hist_steps_, (1ull << 26) / per));
+            p->log_cap = steps * per;
+            p->log = arena_.make<uint32_t>(p->log_cap, false);
+            p->log_fill = arena_.make<unsigned long long>(1);
+            p->bdev.log_fill = p->ldev.log_fill = p->log_fill;
+            p->bdev.log_cap = p->ldev.log_cap = p->log_cap;
+            any_recording_ = true;
+        }
+        p->record = enable;
+        p->record_from = step_;
+        p->bdev.log = enable ? p->log : nullptr;
+        p->ldev.log = enable ? p->log : nullptr;
+        capture_graphs();
+        return;
+    }
+    p->record = enable;
+}
+
+// ------------------------------------------------------------------------------------- init
+
+void Backend::wire()
+{
+    // cpu::init (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/init.h:93-110).
+    for (auto &p : projs_)
+    {
+        for (auto &[u, _] : p->stdp_pops)
+            if (!u.is_null()) p->spike_senders.insert(u);
+        if (!p->pre_uid.is_null()) p->spike_senders.insert(p->pre_uid);
+        if (!p->post_uid.is_null())
+            if (PopulationSlot *q = find_pop(p->post_uid)) q->impact_senders.insert(p->uid);
+    }
+    for (auto &[recv, send] : subs_)
+    {
+        if (ProjectionSlot *p = find_proj(recv))
+            p->spike_senders.insert(send);
+        else if (PopulationSlot *q = find_pop(recv))
+            q->impact_senders.insert(send);
+        else
+            throw Error(KNP_GB300_E_INVALID, "subscription receiver is neither a population nor a projection");
+    }
+    for (auto &q : pops_)
+        for (const Uid &s : q->impact_senders)
+            if (!find_proj(s)) q->has_external_impacts = true;
+}
+
+void Backend::build_population(PopulationSlot &p)
+{
+    const uint32_t n = p.n, np = p.n_pad;
+    // Incoming projections decide ring length, accumulator mode and the live input channels.
+    uint32_t slots = 1;
+    bool dyadic = true, stdp_in = false, g_in = false, d_in = false, forcing_exc = false;
+    for (auto &pr : projs_)
+    {
+        if (!(pr->post_uid == p.uid)) continue;
+        slots = std::max(slots, pr->max_delay);
+        dyadic = dyadic && pr->dyadic;
+        stdp_in = stdp_in || pr->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA;
+        const bool has_type = !pr->type.empty();
+        auto any_type = [&](uint8_t t)
+        { return has_type ? std::find(pr->type.begin(), pr->type.end(), t) != pr->type.end() : t == 0; };
+        g_in = g_in || any_type(KNP_OUT_INHIBITORY_CONDUCTANCE);
+        d_in = d_in || any_type(KNP_OUT_DOPAMINE);
+        if (pr->kind == KNP_SYNAPSE_DELTA && any_type(KNP_OUT_EXCITATORY)) forcing_exc = true;
+    }
+    if (p.has_external_impacts) g_in = d_in = forcing_exc = true;
+    bool fixed = false;
+    if (p.kind != KNP_NEURON_LIF)
+    {
+        if (p.acc_request == KNP_GB300_ACC_FIXED64)
+            fixed = true;
+        else if (p.acc_request == KNP_GB300_ACC_AUTO)
+            fixed = !dyadic || stdp_in;
+    }
+
+    RingView &rg = p.ring;
+    rg.n = n;
+    rg.pitch = np;
+    rg.slots = slots;
+    rg.fixed = fixed ? 1 : 0;
+    const size_t cells = static_cast<size_t>(slots) * np;
+    if (fixed)
+        rg.v64 = arena_.make<long long>(cells);
+    else
+        rg.v32 = arena_.make<float>(cells);
+    const bool res = p.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT;
+    if (p.kind != KNP_NEURON_LIF)
+    {
+        if (g_in) rg.g = arena_.make<float>(cells);
+        if (d_in) rg.dopa = arena_.make<float>(cells);
+        if (res && forcing_exc)
+        {
+            rg.words = (np + 31) / 32;
+            rg.forced = arena_.make<uint32_t>(static_cast<size_t>(slots) * rg.words);
+        }
+    }
+
+    // Spike list, count, recording log.
+    uint32_t *spikes = arena_.make<uint32_t>(np);
+    uint32_t *count = counters_ + p.counter_index;
+    if (p.record)
+    {
+        const uint64_t per = std::max<uint64_t>(n, 1);
+        const uint64_t steps = std::max<uint64_t>(1, std::min<uint64_t>(hist_steps_, (1ull << 26) / per));
+        p.log_cap = steps * per;
+        p.log = arena_.make<uint32_t>(p.log_cap, false);
+        p.log_fill = arena_.make<unsigned long long>(1);
+        any_recording_ = true;
+        p.record_from = 0;
+    }
+
+    if (p.kind == KNP_NEURON_LIF)
+    {
+        LifDev &d = p.ldev;
+        d.n = n;
+        d.n_pad = np;
+        d.V = arena_.make<float>(np);
+        d.refract = arena_.make<uint32_t>(np);
+        std::vector<float> V(np, 0.f);
+        std::vector<uint32_t> rc(np, 0);
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            V[i] = p.init_lif[i].potential;
+            rc[i] = p.init_lif[i].refract_counter;
+        }
+        KNP_CUDA(cudaMemcpy(d.V, V.data(), np * 4, cudaMemcpyHostToDevice));
+        KNP_CUDA(cudaMemcpy(d.refract, rc.data(), np * 4, cudaMemcpyHostToDevice));
+        auto pf = [&](auto get) -> ParamF
+        {
+            ParamF r{nullptr, n ? get(p.init_lif[0]) : 0.f};
+            bool uni = true;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = get(p.init_lif[i]) == r.u;
+            if (!uni)
+            {
+                std::vector<float> a(np, 0.f);
+                for (uint32_t i = 0; i < n; ++i) a[i] = get(p.init_lif[i]);
+                float *dp = arena_.make<float>(np);
+                KNP_CUDA(cudaMemcpy(dp, a.data(), np * 4, cudaMemcpyHostToDevice));
+                r.a = dp;
+            }
+            return r;
+        };
+        d.leak = pf([](const knp_lif_neuron &x) { return x.leak_coefficient; });
+        d.thr = pf([](const knp_lif_neuron &x) { return x.activation_threshold; });
+        d.v_reset = pf([](const knp_lif_neuron &x) { return x.potential_reset_value; });
+        {
+            ParamU r{nullptr, n ? p.init_lif[0].refract_period : 0u};
+            bool uni = true;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = p.init_lif[i].refract_period == r.u;
+            if (!uni)
+            {
+                std::vector<uint32_t> a(np, 0);
+                for (uint32_t i = 0; i < n; ++i) a[i] = p.init_lif[i].refract_period;
+                uint32_t *dp = arena_.make<uint32_t>(np);
+                KNP_CUDA(cudaMemcpy(dp, a.data(), np * 4, cudaMemcpyHostToDevice));
+                r.a = dp;
+            }
+            d.refract_period = r;
+        }
+        d.spikes = spikes;
+        d.spike_count = count;
+        d.log = p.record ? p.log : nullptr;
+        d.log_fill = p.log_fill;
+        d.log_cap = p.log_cap;
+        d.ring = rg;
+        return;
+    }
+
+    const auto &nn = p.init_blifat;
+    BlifatDev &d = p.bdev;
+    d.n = n;
+    d.n_pad = np;
+    auto any = [&](auto pred)
+    {
+        for (uint32_t i = 0; i < n; ++i)
+            if (pred(nn[i])) return true;
+        return false;
+    };
+    uint32_t f = 0;
+    if (any([](const knp_blifat_neuron &x) { return x.potential_decay != 0.0; })) f |= kLiveVRead;
+    if (any([](const knp_blifat_neuron &x)
+            { return x.dynamic_threshold != 0.0 || x.threshold_decay != 0.0 || x.threshold_increment != 0.0; }))
+        f |= kLiveThrDyn;
+    if (any([](const knp_blifat_neuron &x)
+            {
+                return x.postsynaptic_trace != 0.0 || x.postsynaptic_trace_decay != 0.0 ||
+                       x.postsynaptic_trace_increment != 0.0;
+            }))
+        f |= kLiveTrace;
+    if (g_in || any([](const knp_blifat_neuron &x)
+                    { return x.inhibitory_conductance != 0.0 || x.inhibitory_conductance_decay != 0.0; }))
+        f |= kLiveG;
+    if (any([](const knp_blifat_neuron &x) { return x.bursting_period != 0 || x.bursting_phase != 0; })) f |= kLiveBurst;
+    if (any([](const knp_blifat_neuron &x) { return x.total_blocking_period != std::numeric_limits<int64_t>::max(); }))
+        f |= kLiveBlock;
+    if (any([](const knp_blifat_neuron &x)
+            {
+                return x.absolute_refractory_period != 0 ||
+                       x.n_time_steps_since_last_firing != std::numeric_limits<uint64_t>::max();
+            }))
+        f |= kLiveRefract;
+    if (d_in) f |= kLiveDopa;
+    if (f & (kLiveBlock | kLiveVRead | kLiveBurst)) f |= kLiveVPre;
+    if (res)
+    {
+        f |= kResource | kLiveAddThr;
+        for (uint32_t i = 0; i < n; ++i)
+            if (!(std::fabs(p.init_res[i].free_synaptic_resource) < p.init_res[i].synaptic_resource_threshold))
+                f |= kLiveRenorm;
+    }
+    if (any([](const knp_blifat_neuron &x) { return x.additional_threshold != 0.0; })) f |= kLiveAddThr;
+    d.flags = f;
+
+    auto upload_f = [&](auto get) -> float *
+    {
+        std::vector<float> a(np, 0.f);
+        for (uint32_t i = 0; i < n; ++i) a[i] = get(i);
+        float *dp = arena_.make<float>(np);
+        KNP_CUDA(cudaMemcpy(dp, a.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+        return dp;
+    };
+    auto upload_u = [&](auto get) -> uint32_t *
+    {
+        std::vector<uint32_t> a(np, 0);
+        for (uint32_t i = 0; i < n; ++i) a[i] = get(i);
+        uint32_t *dp = arena_.make<uint32_t>(np);
+        KNP_CUDA(cudaMemcpy(dp, a.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        return dp;
+    };
+    auto param_f = [&](auto get) -> ParamF
+    {
+        ParamF r{nullptr, n ? to_f(get(nn[0])) : 0.f};
+        bool uni = true;
+        for (uint32_t i = 1; i < n && uni; ++i) uni = to_f(get(nn[i])) == r.u;
+        if (!uni) r.a = upload_f([&](uint32_t i) { return to_f(get(nn[i])); });
+        return r;
+    };
+    auto param_u = [&](auto get) -> ParamU
+    {
+        ParamU r{nullptr, n ? static_cast<uint32_t>(get(nn[0])) : 0u};
+        bool uni = true;
+        for (uint32_t i = 1; i < n && uni; ++i) uni = static_cast<uint32_t>(get(nn[i])) == r.u;
+        if (!uni) r.a = upload_u([&](uint32_t i) { return static_cast<uint32_t>(get(nn[i])); });
+        return r;
+    };
+    using N = knp_blifat_neuron;
+    d.thr = param_f([](const N &x) { return x.activation_threshold; });
+    d.thr_decay = param_f([](const N &x) { return x.threshold_decay; });
+    d.thr_inc = param_f([](const N &x) { return x.threshold_increment; });
+    d.trace_decay = param_f([](const N &x) { return x.postsynaptic_trace_decay; });
+    d.trace_inc = param_f([](const N &x) { return x.postsynaptic_trace_increment; });
+    d.g_decay = param_f([](const N &x) { return x.inhibitory_conductance_decay; });
+    d.v_decay = param_f([](const N &x) { return x.potential_decay; });
+    d.reflexive = param_f([](const N &x) { return x.reflexive_weight; });
+    d.e_inh = param_f([](const N &x) { return x.reversal_inhibitory_potential; });
+    d.v_reset = param_f([](const N &x) { return x.potential_reset_value; });
+    d.v_min = param_f([](const N &x) { return x.min_potential; });
+    d.t_ref = param_u([](const N &x) { return x.absolute_refractory_period; });
+    d.burst_period = param_u([](const N &x) { return x.bursting_period; });
+
+    d.V = upload_f([&](uint32_t i) { return to_f(nn[i].potential); });
+    d.V_pre = (f & kLiveVPre) ? upload_f([&](uint32_t i) { return to_f(nn[i].pre_impact_potential); }) : nullptr;
+    d.thr_dyn = (f & kLiveThrDyn) ? upload_f([&](uint32_t i) { return to_f(nn[i].dynamic_threshold); }) : nullptr;
+    d.trace = (f & kLiveTrace) ? upload_f([&](uint32_t i) { return to_f(nn[i].postsynaptic_trace); }) : nullptr;
+    d.g = (f & kLiveG) ? upload_f([&](uint32_t i) { return to_f(nn[i].inhibitory_conductance); }) : nullptr;
+    d.dopa = ((f & kLiveDopa) || res) ? upload_f([&](uint32_t i) { return to_f(nn[i].dopamine_value); }) : nullptr;
+    d.add_thr = (f & kLiveAddThr) ? upload_f([&](uint32_t i) { return to_f(nn[i].additional_threshold); }) : nullptr;
+    d.n_since = upload_u(
+        [&](uint32_t i) -> uint32_t
+        {
+            if (!(f & kLiveRefract)) return 0u;  // step of the last spike (lazy tracking)
+            const uint64_t v = nn[i].n_time_steps_since_last_firing;
+            if (v == std::numeric_limits<uint64_t>::max()) return 0xFFFFFFFFu;
+            return v >= 0xFFFFFFFEull ? 0xFFFFFFFEu : static_cast<uint32_t>(v);
+        });
+    d.burst_phase = (f & kLiveBurst) ? upload_u([&](uint32_t i) { return nn[i].bursting_phase; }) : nullptr;
+    if (f & kLiveBlock)
+    {
+        std::vector<long long> a(np, 0);
+        for (uint32_t i = 0; i < n; ++i) a[i] = nn[i].total_blocking_period;
+        d.blocking = arena_.make<long long>(np);
+        KNP_CUDA(cudaMemcpy(d.blocking, a.data(), np * 8, cudaMemcpyHostToDevice));
+    }
+    if (res)
+    {
+        ResourceDev &r = d.res;
+        const auto &rr = p.init_res;
+        auto up64 = [&](auto get)
+        {
+            std::vector<unsigned long long> a(np, 0);
+            for (uint32_t i = 0; i < n; ++i) a[i] = get(rr[i]);
+            auto *dp = arena_.make<unsigned long long>(np);
+            KNP_CUDA(cudaMemcpy(dp, a.data(), np * 8, cudaMemcpyHostToDevice));
+            return dp;
+        };
+        using R = knp_resource_stdp_state;
+        r.isi_status = reinterpret_cast<int32_t *>(upload_u([&](uint32_t i) { return static_cast<uint32_t>(rr[i].isi_status); }));
+        r.last_step = up64([](const R &x) { return x.last_step; });
+        r.last_spike_step = up64([](const R &x) { return x.last_spike_step; });
+        r.first_isi_spike = up64([](const R &x) { return x.first_isi_spike; });
+        r.stability = upload_f([&](uint32_t i) { return rr[i].stability; });
+        r.free_resource = upload_f([&](uint32_t i) { return rr[i].free_synaptic_resource; });
+        {
+            std::vector<uint8_t> a(np, 0);
+            for (uint32_t i = 0; i < n; ++i) a[i] = rr[i].is_being_forced ? 1 : 0;
+            r.is_forced = arena_.make<uint8_t>(np);
+            KNP_CUDA(cudaMemcpy(r.is_forced, a.data(), np, cudaMemcpyHostToDevice));
+        }
+        auto rpf = [&](auto get) -> ParamF
+        {
+            ParamF x{nullptr, n ? get(rr[0]) : 0.f};
+            bool uni = true;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = get(rr[i]) == x.u;
+            if (!uni) x.a = upload_f([&](uint32_t i) { return get(rr[i]); });
+            return x;
+        };
+        r.add_thr_coef = rpf([](const R &x) { return x.synapse_sum_threshold_coefficient; });
+        r.resource_threshold = rpf([](const R &x) { return x.synaptic_resource_threshold; });
+        r.stability_change_param = rpf([](const R &x) { return x.stability_change_parameter; });
+        r.stability_change_at_isi = rpf([](const R &x) { return x.stability_change_at_isi; });
+        {
+            ParamU x{nullptr, n ? rr[0].isi_max : 0u};
+            bool uni = true;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = rr[i].isi_max == x.u;
+            if (!uni) x.a = upload_u([&](uint32_t i) { return rr[i].isi_max; });
+            r.isi_max = x;
+        }
+    }
+    d.spikes = spikes;
+    d.spike_count = count;
+    d.log = p.record ? p.log : nullptr;
+    d.log_fill = p.log_fill;
+    d.log_cap = p.log_cap;
+    d.ring = rg;
+}
+
+void Backend::build_projection(ProjectionSlot &p)
+{
+    PopulationSlot *post = find_pop(p.post_uid);
+    const uint64_t S = p.n_syn;
+    // Rows: presynaptic indexes 0..max(pre).
+    uint32_t *d_key = nullptr;
+    uint32_t *d_post = nullptr, *d_delay = nullptr;
+    float *d_w = nullptr;
+    uint8_t *d_type = nullptr;
+    if (p.generated)
+    {
+        p.n_rows = p.gen.n_pre;
+        d_key = arena_.make<uint32_t>(S, false);
+        launch_gen_fixed_fan_in_keys(S, p.gen.n_pre, stream_key(p.gen.seed, p.gen.stream + 1), d_key, stream_);
+    }
+    else
+    {
+        uint32_t max_pre = 0;
+        for (uint32_t v : p.pre) max_pre = std::max(max_pre, v + 1);
+        p.n_rows = max_pre;
+        d_key = arena_.make<uint32_t>(S, false);
+        d_post = arena_.make<uint32_t>(S, false);
+        d_delay = arena_.make<uint32_t>(S, false);
+        d_w = arena_.make<float>(S, false);
+        KNP_CUDA(cudaMemcpyAsync(d_key, p.pre.data(), S * 4, cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaMemcpyAsync(d_post, p.post.data(), S * 4, cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaMemcpyAsync(d_delay, p.delay.data(), S * 4, cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaMemcpyAsync(d_w, p.weight.data(), S * 4, cudaMemcpyHostToDevice, stream_));
+        if (p.type.size() > 1)
+        {
+            d_type = arena_.make<uint8_t>(S, false);
+            KNP_CUDA(cudaMemcpyAsync(d_type, p.type.data(), S, cudaMemcpyHostToDevice, stream_));
+        }
+    }
+    p.row_ptr = arena_.make<long long>(static_cast<size_t>(p.n_rows) + 1);
+    uint32_t *perm = arena_.make<uint32_t>(S, false);
+    size_t temp_need = 0;
+    KNP_CUDA(build_csr(S, p.n_rows, d_key, perm, p.row_ptr, nullptr, 0, &temp_need, stream_));
+    void *temp = arena_.alloc(temp_need, false);
+    KNP_CUDA(build_csr(S, p.n_rows, d_key, perm, p.row_ptr, temp, temp_need, &temp_need, stream_));
+    p.col = arena_.make<int32_t>(S, false);
+    p.w = arena_.make<float>(S, false);
+    p.delay_d = arena_.make<uint8_t>(S, false);
+    if (p.generated)
+    {
+        launch_gen_fixed_fan_in_gather(S, perm, p.gen.n_post, p.gen.k_lo, p.gen.k_hi, p.gen.d_lo, p.gen.d_hi,
+                                       stream_key(p.gen.seed, p.gen.stream + 2), stream_key(p.gen.seed, p.gen.stream + 3),
+                                       p.col, p.w, p.delay_d, stream_);
+    }
+    else
+    {
+        if (d_type) p.type_d = arena_.make<uint8_t>(S, false);
+        launch_gather_synapses(S, perm, d_post, d_w, d_delay, d_type, p.col, p.w, p.delay_d, p.type_d, stream_);
+    }
+    KNP_CUDA(cudaGetLastError());
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    arena_.release(temp);
+    arena_.release(d_key);
+    if (d_post) arena_.release(d_post);
+    if (d_delay) arena_.release(d_delay);
+    if (d_w) arena_.release(d_w);
+    if (d_type) arena_.release(d_type);
+    if (p.generated)
+        arena_.release(perm);  // weights of a generated projection are regenerated, not permuted
+    else
+        p.perm = perm;
+
+    ProjectionDev &d = p.dev;
+    d.row_ptr = p.row_ptr;
+    d.n_rows = p.n_rows;
+    d.col = p.col;
+    d.w = p.w;
+    d.delay = p.delay_d;
+    d.type = p.type_d;
+    d.uniform_type = p.type.size() == 1 ? p.type[0] : 0;
+    d.forcing = p.kind == KNP_SYNAPSE_DELTA ? 1 : 0;  // is_forced(): stdp_dispatcher.h:54-58, additive_stdp.h:199-203
+    if (post) d.ring = post->ring;
+    // Spike sources: every subscribed sender, except STDP-only populations whose messages the
+    // projection empties before propagating them (additive_stdp.h:162-166).
+    d.n_src = 0;
+    for (const Uid &s : p.spike_senders)
+    {
+        auto it = p.stdp_pops.find(s);
+        if (it != p.stdp_pops.end() && it->second == KNP_STDP_ONLY) continue;
+        SpikeSource src{};
+        if (PopulationSlot *q = find_pop(s))
+        {
+            src.idx = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+            src.count = counters_ + q->counter_index;
+        }
+        else
+        {
+            src.channel = channel(s).dev;
+        }
+        if (d.n_src >= kMaxSources) throw Error(KNP_GB300_E_INVALID, "too many spike sources for one projection");
+        d.src[d.n_src++] = src;
+    }
+    if (!post) d.n_src = 0;  // no target population on this backend: impacts go nowhere
+}
+
+void Backend::build_stdp(ProjectionSlot &p)
+{
+    if (p.kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p.n_syn == 0) return;
+    const float tp = p.tau_plus[0], tm = p.tau_minus[0];
+    const float period_f = tp + tm;
+    uint32_t period = 0;
+    while (static_cast<float>(period) < period_f) ++period;  // smallest n with n >= tau+ + tau- (float compare)
+    if (period == 0) period = 0;
+    uint32_t n_cols = 0;
+    for (uint32_t v : p.post) n_cols = std::max(n_cols, v + 1);
+    StdpDev &s = p.stdp;
+    s.n_cols = n_cols;
+    s.period = period;
+    s.pre_hist = arena_.make<uint32_t>(static_cast<size_t>(n_cols) * std::max<uint32_t>(period, 1));
+    s.post_hist = arena_.make<uint32_t>(static_cast<size_t>(n_cols) * std::max<uint32_t>(period, 1));
+    s.pre_cnt = arena_.make<uint32_t>(n_cols);
+    s.post_cnt = arena_.make<uint32_t>(n_cols);
+    s.touched = arena_.make<uint32_t>(n_cols);
+    s.touched_stamp = arena_.make<unsigned long long>(n_cols);
+    s.w = p.w;
+    // Column index: CSR positions grouped by postsynaptic neuron (stable).
+    std::vector<uint32_t> perm(p.n_syn);
+    KNP_CUDA(cudaMemcpy(perm.data(), p.perm, p.n_syn * 4, cudaMemcpyDeviceToHost));
+    std::vector<long long> col_ptr(static_cast<size_t>(n_cols) + 1, 0);
+    for (uint64_t e = 0; e < p.n_syn; ++e) ++col_ptr[p.post[perm[e]] + 1];
+    for (uint32_t c = 0; c < n_cols; ++c) col_ptr[c + 1] += col_ptr[c];
+    std::vector<uint64_t> col_pos(p.n_syn);
+    std::vector<long long> fill(col_ptr.begin(), col_ptr.end() - 1);
+    for (uint64_t e = 0; e < p.n_syn; ++e) col_pos[fill[p.post[perm[e]]]++] = e;
+    auto *cp = arena_.make<long long>(col_ptr.size());
+    auto *cpos = arena_.make<uint64_t>(col_pos.size());
+    KNP_CUDA(cudaMemcpy(cp, col_ptr.data(), col_ptr.size() * 8, cudaMemcpyHostToDevice));
+    KNP_CUDA(cudaMemcpy(cpos, col_pos.data(), col_pos.size() * 8, cudaMemcpyHostToDevice));
+    s.col_ptr = cp;
+    s.col_pos = cpos;
+    std::vector<float> table = stdp_table(tp, tm);
+    auto *tb = arena_.make<float>(table.size());
+    KNP_CUDA(cudaMemcpy(tb, table.data(), table.size() * 4, cudaMemcpyHostToDevice));
+    s.table = tb;
+    s.table_len = static_cast<uint32_t>(table.size());
+    // Append sources: STDP populations in population load order (the order their SpikeMessages
+    // arrive in one step).
+    for (auto &q : pops_)
+    {
+        auto it = p.stdp_pops.find(q->uid);
+        if (it == p.stdp_pops.end()) continue;
+        SpikeSource src{};
+        src.idx = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+        src.count = counters_ + q->counter_index;
+        p.stdp_sources.emplace_back(src, it->second == KNP_STDP_AND_SPIKE ? 1 : 0);
+    }
+}
+
+void Backend::init()
+{
+    require_not_init("init");
+    KNP_CUDA(cudaSetDevice(device_));
+    for (auto &p : projs_)
+    {
+        if (!p->post_uid.is_null() && !find_pop(p->post_uid))
+            throw Error(KNP_GB300_E_INVALID, "projection targets a population that is not loaded");
+        PopulationSlot *post = find_pop(p->post_uid);
+        if (post && post->kind == KNP_NEURON_LIF)
+            for (uint8_t t : p->type)
+                if (t > KNP_OUT_INHIBITORY_CURRENT)
+                    throw Error(KNP_GB300_E_INVALID, "LIF neurons accept only excitatory and inhibitory-current impacts");
+        if (p->generated)
+        {
+            p->max_delay = p->gen.d_hi;
+            const double kmax = std::max(std::abs(p->gen.k_lo), std::abs(p->gen.k_hi));
+            p->dyadic = static_cast<double>(p->gen.fan_in) * kmax / 256.0 < 32768.0;
+            if (post && p->gen.n_post > post->n)
+                throw Error(KNP_GB300_E_INVALID, "postsynaptic index out of the target population");
+            continue;
+        }
+        uint32_t md = 1;
+        for (uint32_t d : p->delay) md = std::max(md, d);
+        p->max_delay = md;
+        bool dy = true;
+        for (float w : p->weight) dy = dy && is_dyadic(w);
+        if (dy && post)
+        {
+            std::vector<double> colsum(post->n, 0.0);
+            for (uint64_t i = 0; i < p->n_syn; ++i)
+                if (p->post[i] < post->n) colsum[p->post[i]] += std::fabs(p->weight[i]);
+            for (double v : colsum) dy = dy && v < 32768.0;
+        }
+        p->dyadic = dy;
+        if (post)
+            for (uint32_t v : p->post)
+                if (v >= post->n) throw Error(KNP_GB300_E_INVALID, "postsynaptic index out of the target population");
+    }
+    wire();
+    // Per-step counters: population spike counts, then STDP touched counts.
+    n_spike_counters_ = static_cast<uint32_t>(pops_.size());
+    n_counters_ = n_spike_counters_;
+    for (auto &p : projs_)
+        if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) ++n_counters_;
+    counters_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
+    hist_ = arena_.make<uint32_t>(static_cast<size_t>(hist_steps_) * std::max<uint32_t>(n_spike_counters_, 1));
+    hist_base_ = arena_.make<unsigned long long>(1);
+    for (uint32_t i = 0; i < pops_.size(); ++i) pops_[i]->counter_index = i;
+    neurons_total_ = 0;
+    for (auto &q : pops_)
+    {
+        build_population(*q);
+        neurons_total_ += q->n;
+    }
+    for (auto &p : projs_)
+    {
+        build_projection(*p);
+        if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) build_stdp(*p);
+    }
+    uint32_t ci = n_spike_counters_;
+    for (auto &p : projs_)
+        if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) p->stdp.touched_count = counters_ + ci++;
+    // Host copies of the synapse arrays are no longer needed, except what readback and STDP use.
+    for (auto &p : projs_)
+    {
+        std::vector<uint32_t>().swap(p->pre);
+        std::vector<uint32_t>().swap(p->delay);
+        std::vector<float>().swap(p->weight);
+        if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) std::vector<uint32_t>().swap(p->post);
+    }
+    initialized_ = true;
+    capture_graphs();
+}
+
+// ------------------------------------------------------------------------------------ stepping
+
+void Backend::enqueue_step()
+{
+    for (auto &q : pops_)
+    {
+        if (q->kind == KNP_NEURON_LIF)
+            launch_lif(q->ldev, ctl_, stream_);
+        else
+            launch_blifat(q->bdev, ctl_, stream_);
+    }
+    for (auto &p : projs_)
+    {
+        if (p->dev.n_src == 0) continue;
+        uint64_t bound = 0;
+        for (int k = 0; k < p->dev.n_src; ++k)
+        {
+            const SpikeSource &s = p->dev.src[k];
+            bound += s.channel ? p->n_rows : p->n_rows;
+        }
+        const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((bound + 7) / 8, 8ull * sm_count_));
+        launch_projection(p->dev, ctl_, static_cast<int>(blocks), stream_);
+    }
+    for (auto &p : projs_)
+    {
+        if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
+        for (auto &[src, both] : p->stdp_sources) launch_stdp_append(p->stdp, src, both, ctl_, stream_);
+        launch_stdp_modify(p->stdp, ctl_, stream_);
+    }
+    StepEnd e{counters_, n_counters_, n_spike_counters_, hist_, hist_base_, hist_steps_};
+    launch_step_end(e, ctl_, stream_);
+}
+
+void Backend::capture_graphs()
+{
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    if (graph1_) cudaGraphExecDestroy(graph1_);
+    if (graphK_) cudaGraphExecDestroy(graphK_);
+    graph1_ = graphK_ = nullptr;
+    for (int which = 0; which < 2; ++which)
+    {
+        cudaGraph_t g = nullptr;
+        KNP_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        const uint64_t k = which ? kGraphSteps : 1;
+        for (uint64_t i = 0; i < k; ++i) enqueue_step();
+        KNP_CUDA(cudaStreamEndCapture(stream_, &g));
+        cudaGraphExec_t ex = nullptr;
+        KNP_CUDA(cudaGraphInstantiate(&ex, g, 0));
+        cudaGraphDestroy(g);
+        (which ? graphK_ : graph1_) = ex;
+    }
+}
+
+uint64_t Backend::steps_before_drain() const
+{
+    uint64_t room = hist_steps_ - (step_ - hist_base_host_);
+    for (auto &q : pops_)
+        if (q->record && q->log)
+            room = std::min<uint64_t>(room, q->log_cap / std::max<uint32_t>(q->n, 1) - (step_ - hist_base_host_));
+    return room;
+}
+
+void Backend::stage_host_inputs()
+{
+    // Pinned staging: wait until the previous staging copy has been consumed.
+    KNP_CUDA(cudaEventSynchronize(pinned_free_));
+    size_t need = 0;
+    for (auto &c : channels_)
+        if (c->has_pending) need += sizeof(ChannelDev) + 16 + c->pending.size() * 4 + 64;
+    for (auto &m : pending_impacts_) need += m.post.size() * 9 + 64;
+    if (need > pinned_bytes_)
+    {
+        if (pinned_) KNP_CUDA(cudaFreeHost(pinned_));
+        pinned_bytes_ = std::max<size_t>(need * 2, 1 << 16);
+        KNP_CUDA(cudaHostAlloc(&pinned_, pinned_bytes_, cudaHostAllocDefault));
+    }
+    char *hp = static_cast<char *>(pinned_);
+    size_t off = 0;
+    auto stage = [&](const void *src, size_t bytes) -> char *
+    {
+        off = (off + 15) & ~size_t(15);
+        char *dst = hp + off;
+        std::memcpy(dst, src, bytes);
+        off += bytes;
+        return dst;
+    };
+    for (auto &c : channels_)
+    {
+        if (!c->has_pending) continue;
+        const uint64_t n = c->pending.size();
+        if (n > c->cap_idx || c->cap_steps < 1 || c->scheduled || c->owns_generated)
+        {
+            KNP_CUDA(cudaStreamSynchronize(stream_));
+            if (c->idx && !c->owns_generated) arena_.release(c->idx);
+            if (c->idx && c->owns_generated) cudaFree(c->idx);
+            if (c->offsets) arena_.release(c->offsets);
+            c->cap_idx = std::max<uint64_t>(n * 2, 1024);
+            c->cap_steps = 1;
+            c->idx = arena_.make<uint32_t>(c->cap_idx, false);
+            c->offsets = arena_.make<long long>(2);
+            c->owns_generated = false;
+        }
+        const long long offs[2] = {0, static_cast<long long>(n)};
+        c->host = ChannelDev{step_, 1, c->offsets, c->idx};
+        c->scheduled = false;
+        char *a = stage(offs, sizeof(offs));
+        KNP_CUDA(cudaMemcpyAsync(c->offsets, a, sizeof(offs), cudaMemcpyHostToDevice, stream_));
+        if (n)
+        {
+            char *b = stage(c->pending.data(), n * 4);
+            KNP_CUDA(cudaMemcpyAsync(c->idx, b, n * 4, cudaMemcpyHostToDevice, stream_));
+        }
+        char *h = stage(&c->host, sizeof(ChannelDev));
+        KNP_CUDA(cudaMemcpyAsync(c->dev, h, sizeof(ChannelDev), cudaMemcpyHostToDevice, stream_));
+        c->pending.clear();
+        c->has_pending = false;
+    }
+    for (auto &m : pending_impacts_)
+    {
+        PopulationSlot *q = find_pop(m.receiver);
+        const uint32_t n = static_cast<uint32_t>(m.post.size());
+        if (!q || !n) continue;
+        // Device staging for impacts: allocated per message batch and released after the step.
+        uint32_t *dpost = arena_.make<uint32_t>(n, false);
+        float *dval = arena_.make<float>(n, false);
+        uint8_t *dtype = arena_.make<uint8_t>(n, false);
+        KNP_CUDA(cudaMemcpyAsync(dpost, stage(m.post.data(), n * 4), n * 4, cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaMemcpyAsync(dval, stage(m.value.data(), n * 4), n * 4, cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaMemcpyAsync(dtype, stage(m.type.data(), n), n, cudaMemcpyHostToDevice, stream_));
+        const RingView &rg = q->kind == KNP_NEURON_LIF ? q->ldev.ring : q->bdev.ring;
+        launch_apply_impacts(rg, dpost, dval, dtype, m.forcing ? 1 : 0, n, ctl_, stream_);
+        KNP_CUDA(cudaGetLastError());
+        KNP_CUDA(cudaStreamSynchronize(stream_));
+        arena_.release(dpost);
+        arena_.release(dval);
+        arena_.release(dtype);
+    }
+    pending_impacts_.clear();
+    KNP_CUDA(cudaEventRecord(pinned_free_, stream_));
+}
+
+void Backend::step(uint64_t n)
+{
+    require_init("step");
+    KNP_CUDA(cudaSetDevice(device_));
+    while (n > 0)
+    {
+        bool host_inputs = !pending_impacts_.empty();
+        for (auto &c : channels_) host_inputs = host_inputs || c->has_pending;
+        if (any_recording_ && steps_before_drain() == 0) drain_recordings();
+        if (host_inputs)
+        {
+            stage_host_inputs();
+            KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
+            ++step_;
+            --n;
+            continue;
+        }
+        uint64_t k = n;
+        if (any_recording_) k = std::min<uint64_t>(k, steps_before_drain());
+        uint64_t done = 0;
+        while (k - done >= kGraphSteps)
+        {
+            KNP_CUDA(cudaGraphLaunch(graphK_, stream_));
+            done += kGraphSteps;
+        }
+        while (done < k)
+        {
+            KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
+            ++done;
+        }
+        step_ += k;
+        n -= k;
+    }
+}
+
+float Backend::step_timed(uint64_t n)
+{
+    cudaEvent_t a, b;
+    KNP_CUDA(cudaEventCreate(&a));
+    KNP_CUDA(cudaEventCreate(&b));
+    KNP_CUDA(cudaEventRecord(a, stream_));
+    step(n);
+    KNP_CUDA(cudaEventRecord(b, stream_));
+    KNP_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    KNP_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    check_device_error();
+    return ms;
+}
+
+void Backend::profile_phases(uint64_t n, float *ms)
+{
+    require_init("profile_phases");
+    KNP_CUDA(cudaSetDevice(device_));
+    if (any_recording_) drain_recordings();
+    bool host_inputs = !pending_impacts_.empty();
+    for (auto &c : channels_) host_inputs = host_inputs || c->has_pending;
+    if (host_inputs) throw Error(KNP_GB300_E_STATE, "profile_phases does not stage host messages");
+    cudaEvent_t ev[5];
+    for (auto &e : ev) KNP_CUDA(cudaEventCreate(&e));
+    double acc[4] = {0, 0, 0, 0};
+    for (uint64_t i = 0; i < n; ++i)
+    {
+        if (any_recording_ && steps_before_drain() == 0) drain_recordings();
+        KNP_CUDA(cudaEventRecord(ev[0], stream_));
+        for (auto &q : pops_)
+        {
+            if (q->kind == KNP_NEURON_LIF)
+                launch_lif(q->ldev, ctl_, stream_);
+            else
+                launch_blifat(q->bdev, ctl_, stream_);
+        }
+        KNP_CUDA(cudaEventRecord(ev[1], stream_));
+        for (auto &p : projs_)
+        {
+            if (p->dev.n_src == 0) continue;
+            const uint64_t bound = static_cast<uint64_t>(p->dev.n_src) * p->n_rows;
+            const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((bound + 7) / 8, 8ull * sm_count_));
+            launch_projection(p->dev, ctl_, static_cast<int>(blocks), stream_);
+        }
+        KNP_CUDA(cudaEventRecord(ev[2], stream_));
+        for (auto &p : projs_)
+        {
+            if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
+            for (auto &[src, both] : p->stdp_sources) launch_stdp_append(p->stdp, src, both, ctl_, stream_);
+            launch_stdp_modify(p->stdp, ctl_, stream_);
+        }
+        KNP_CUDA(cudaEventRecord(ev[3], stream_));
+        StepEnd e{counters_, n_counters_, n_spike_counters_, hist_, hist_base_, hist_steps_};
+        launch_step_end(e, ctl_, stream_);
+        KNP_CUDA(cudaEventRecord(ev[4], stream_));
+        KNP_CUDA(cudaEventSynchronize(ev[4]));
+        for (int k = 0; k < 4; ++k)
+        {
+            float m = 0.f;
+            KNP_CUDA(cudaEventElapsedTime(&m, ev[k], ev[k + 1]));
+            acc[k] += m;
+        }
+        ++step_;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 4; ++k) ms[k] = static_cast<float>(acc[k]);
+    check_device_error();
+}
+
+void Backend::check_device_error()
+{
+    Control c{};
+    KNP_CUDA(cudaMemcpyAsync(&c, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, stream_));
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    if (c.error)
+        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(c.error) +
+                                                 (c.error & kErrLogOverflow ? " (spike recording overflow)" : ""));
+}
+
+void Backend::drain_recordings()
+{
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    const uint64_t steps = step_ - hist_base_host_;
+    if (steps)
+    {
+        std::vector<uint32_t> hist(steps * n_spike_counters_);
+        KNP_CUDA(cudaMemcpy(hist.data(), hist_, hist.size() * 4, cudaMemcpyDeviceToHost));
+        for (auto &q : pops_)
+        {
+            if (!q->record || !q->log) continue;
+            unsigned long long fill = 0;
+            KNP_CUDA(cudaMemcpy(&fill, q->log_fill, 8, cudaMemcpyDeviceToHost));
+            std::vector<uint32_t> data(fill);
+            if (fill) KNP_CUDA(cudaMemcpy(data.data(), q->log, fill * 4, cudaMemcpyDeviceToHost));
+            uint64_t off = 0;
+            for (uint64_t s = 0; s < steps; ++s)
+            {
+                const uint32_t c = hist[s * n_spike_counters_ + q->counter_index];
+                const uint64_t step = hist_base_host_ + s;
+                if (off + c > fill) throw Error(KNP_GB300_E_DEVICE_FLAG, "spike recording log is inconsistent");
+                if (step >= q->record_from)
+                {
+                    std::vector<uint32_t> v(data.begin() + off, data.begin() + off + c);
+                    std::sort(v.begin(), v.end());
+                    q->recorded[step] = std::move(v);
+                }
+                off += c;
+            }
+            KNP_CUDA(cudaMemset(q->log_fill, 0, 8));
+        }
+    }
+    hist_base_host_ = step_;
+    unsigned long long hb = step_;
+    KNP_CUDA(cudaMemcpy(hist_base_, &hb, 8, cudaMemcpyHostToDevice));
+    check_device_error();
+}
+
+void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n)
+{
+    require_init("read_spikes");
+    PopulationSlot *q = find_pop(pop);
+    if (!q) throw Error(KNP_GB300_E_INVALID, "unknown population");
+    if (!q->record) throw Error(KNP_GB300_E_STATE, "spike recording is not enabled for this population");
+    if (step >= step_) throw Error(KNP_GB300_E_INVALID, "step has not been run yet");
+    if (step >= hist_base_host_) drain_recordings();
+    auto it = q->recorded.find(step);
+    if (it == q->recorded.end()) throw Error(KNP_GB300_E_INVALID, "spikes of this step were not recorded or were discarded");
+    *n = static_cast<uint32_t>(it->second.size());
+    std::copy_n(it->second.begin(), std::min<size_t>(cap, it->second.size()), out);
+}
+
+void Backend::discard_spikes(uint64_t before)
+{
+    for (auto &q : pops_) q->recorded.erase(q->recorded.begin(), q->recorded.lower_bound(before));
+}
+
+// ------------------------------------------------------------------------------------ messages
+
+void Backend::send_spikes(const Uid &sender, uint64_t, uint32_t n, const uint32_t *idx)
+{
+    require_init("send_spikes");
+    Channel *c = find_channel(sender);
+    if (!c)
+    {
+        // No projection subscribed to this sender: the message reaches nobody (as on the bus).
+        return;
+    }
+    if (c->scheduled && step_ >= c->host.first_step && step_ - c->host.first_step < c->host.n_steps)
+        throw Error(KNP_GB300_E_STATE, "this sender's device spike schedule covers the next step");
+    c->pending.insert(c->pending.end(), idx, idx + n);
+    c->has_pending = true;
+}
+
+void Backend::load_schedule(
+    const Uid &sender, uint64_t first_step, uint64_t n_steps, const int64_t *offsets, const uint32_t *idx)
+{
+    require_init("load_spike_schedule");
+    Channel *c = find_channel(sender);
+    if (!c) throw Error(KNP_GB300_E_INVALID, "no projection is subscribed to this sender");
+    if (offsets[0] != 0) throw Error(KNP_GB300_E_INVALID, "schedule offsets must start at 0");
+    for (uint64_t t = 0; t < n_steps; ++t)
+        if (offsets[t + 1] < offsets[t]) throw Error(KNP_GB300_E_INVALID, "schedule offsets must be non-decreasing");
+    const uint64_t total = static_cast<uint64_t>(offsets[n_steps]);
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    if (c->idx && c->owns_generated) cudaFree(c->idx);
+    else if (c->idx) arena_.release(c->idx);
+    if (c->offsets) arena_.release(c->offsets);
+    c->idx = arena_.make<uint32_t>(std::max<uint64_t>(total, 1), false);
+    c->offsets = arena_.make<long long>(n_steps + 1, false);
+    c->owns_generated = false;
+    c->cap_idx = total;
+    c->cap_steps = n_steps;
+    KNP_CUDA(cudaMemcpy(c->offsets, offsets, (n_steps + 1) * 8, cudaMemcpyHostToDevice));
+    if (total) KNP_CUDA(cudaMemcpy(c->idx, idx, total * 4, cudaMemcpyHostToDevice));
+    c->host = ChannelDev{first_step, n_steps, c->offsets, c->idx};
+    KNP_CUDA(cudaMemcpy(c->dev, &c->host, sizeof(ChannelDev), cudaMemcpyHostToDevice));
+    c->scheduled = true;
+}
+
+void Backend::generate_bernoulli(
+    const Uid &sender, uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps, uint64_t seed,
+    uint64_t stream)
+{
+    require_init("generate_bernoulli_schedule");
+    Channel *c = find_channel(sender);
+    if (!c) throw Error(KNP_GB300_E_INVALID, "no projection is subscribed to this sender");
+    if (n_steps > 65535) throw Error(KNP_GB300_E_INVALID, "at most 65535 steps per generated schedule");
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    if (c->idx && c->owns_generated) cudaFree(c->idx);
+    else if (c->idx) arena_.release(c->idx);
+    if (c->offsets) arena_.release(c->offsets);
+    c->offsets = arena_.make<long long>(n_steps + 1, false);
+    uint32_t *idx = nullptr;
+    uint64_t total = 0;
+    const double pc = std::min(std::max(p, 0.0), 1.0);
+    const unsigned long long thr = static_cast<unsigned long long>(pc * 9007199254740992.0);
+    KNP_CUDA(gen_bernoulli_schedule(n_sources, thr, stream_key(seed, stream), first_step, n_steps, c->offsets, &idx,
+                                    &total, stream_));
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    c->idx = idx;
+    c->owns_generated = true;
+    c->cap_idx = total;
+    c->cap_steps = n_steps;
+    c->host = ChannelDev{first_step, n_steps, c->offsets, c->idx};
+    KNP_CUDA(cudaMemcpy(c->dev, &c->host, sizeof(ChannelDev), cudaMemcpyHostToDevice));
+    c->scheduled = true;
+}
+
+void Backend::send_impacts(
+    const Uid &sender, const Uid &receiver, bool forcing, uint32_t n, const uint32_t *post, const float *value,
+    const uint8_t *type)
+{
+    require_init("send_impacts");
+    PopulationSlot *q = find_pop(receiver);
+    if (!q) throw Error(KNP_GB300_E_INVALID, "unknown receiver population");
+    if (!q->impact_senders.count(sender)) return;  // not subscribed: the message reaches nobody
+    PendingImpacts m{receiver, forcing, {}, {}, {}};
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        if (post[i] >= q->n) throw Error(KNP_GB300_E_INVALID, "impact postsynaptic index out of range");
+        const uint8_t t = type ? type[i] : 0;
+        if (t == KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "BLOCKING impacts are not supported");
+        if (t > KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
+        if (q->kind == KNP_NEURON_LIF && t > KNP_OUT_INHIBITORY_CURRENT)
+            throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
+        m.post.push_back(post[i]);
+        m.value.push_back(value[i]);
+        m.type.push_back(t);
+    }
+    pending_impacts_.push_back(std::move(m));
+}
+
+// ------------------------------------------------------------------------------------ readback
+
+void Backend::read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext)
+{
+    PopulationSlot *q = find_pop(pop);
+    if (!q || q->kind == KNP_NEURON_LIF) throw Error(KNP_GB300_E_INVALID, "unknown BLIFAT population");
+    const uint32_t n = q->n;
+    std::copy(q->init_blifat.begin(), q->init_blifat.end(), out);
+    if (ext && !q->init_res.empty()) std::copy(q->init_res.begin(), q->init_res.end(), ext);
+    if (!initialized_) return;
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    const BlifatDev &d = q->bdev;
+    const uint32_t f = d.flags;
+    const uint64_t T = step_;
+    auto getf = [&](const float *p)
+    {
+        std::vector<float> v(n);
+        if (n) KNP_CUDA(cudaMemcpy(v.data(), p, n * 4, cudaMemcpyDeviceToHost));
+        return v;
+    };
+    auto getu = [&](const uint32_t *p)
+    {
+        std::vector<uint32_t> v(n);
+        if (n) KNP_CUDA(cudaMemcpy(v.data(), p, n * 4, cudaMemcpyDeviceToHost));
+        return v;
+    };
+    if (T == 0) return;
+    auto V = getf(d.V);
+    for (uint32_t i = 0; i < n; ++i) out[i].potential = V[i];
+    if (f & kLiveVPre)
+    {
+        auto v = getf(d.V_pre);
+        for (uint32_t i = 0; i < n; ++i) out[i].pre_impact_potential = v[i];
+    }
+    else
+        for (uint32_t i = 0; i < n; ++i) out[i].pre_impact_potential = 0.0;
+    if (f & kLiveThrDyn)
+    {
+        auto v = getf(d.thr_dyn);
+        for (uint32_t i = 0; i < n; ++i) out[i].dynamic_threshold = v[i];
+    }
+    if (f & kLiveTrace)
+    {
+        auto v = getf(d.trace);
+        for (uint32_t i = 0; i < n; ++i) out[i].postsynaptic_trace = v[i];
+    }
+    if (f & kLiveG)
+    {
+        auto v = getf(d.g);
+        for (uint32_t i = 0; i < n; ++i) out[i].inhibitory_conductance = v[i];
+    }
+    if (d.dopa)
+    {
+        auto v = getf(d.dopa);
+        for (uint32_t i = 0; i < n; ++i) out[i].dopamine_value = v[i];
+    }
+    if (d.add_thr)
+    {
+        auto v = getf(d.add_thr);
+        for (uint32_t i = 0; i < n; ++i) out[i].additional_threshold = v[i];
+    }
+    {
+        auto v = getu(d.n_since);
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            if (f & kLiveRefract)
+                out[i].n_time_steps_since_last_firing =
+                    v[i] == 0xFFFFFFFFu ? std::numeric_limits<uint64_t>::max() : static_cast<uint64_t>(v[i]);
+            else
+                out[i].n_time_steps_since_last_firing = (T - 1) - v[i];
+        }
+    }
+    if (f & kLiveBurst)
+    {
+        auto v = getu(d.burst_phase);
+        for (uint32_t i = 0; i < n; ++i) out[i].bursting_phase = v[i];
+    }
+    if (f & kLiveBlock)
+    {
+        std::vector<long long> v(n);
+        if (n) KNP_CUDA(cudaMemcpy(v.data(), d.blocking, n * 8, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < n; ++i) out[i].total_blocking_period = v[i];
+    }
+    else
+        for (uint32_t i = 0; i < n; ++i) out[i].total_blocking_period = std::numeric_limits<int64_t>::max() - T;
+    if (ext && (f & kResource))
+    {
+        const ResourceDev &r = d.res;
+        auto st = getu(reinterpret_cast<const uint32_t *>(r.isi_status));
+        auto stab = getf(r.stability);
+        auto fr = getf(r.free_resource);
+        std::vector<unsigned long long> ls(n), lss(n), fis(n);
+        std::vector<uint8_t> forced(n);
+        if (n)
+        {
+            KNP_CUDA(cudaMemcpy(ls.data(), r.last_step, n * 8, cudaMemcpyDeviceToHost));
+            KNP_CUDA(cudaMemcpy(lss.data(), r.last_spike_step, n * 8, cudaMemcpyDeviceToHost));
+            KNP_CUDA(cudaMemcpy(fis.data(), r.first_isi_spike, n * 8, cudaMemcpyDeviceToHost));
+            KNP_CUDA(cudaMemcpy(forced.data(), r.is_forced, n, cudaMemcpyDeviceToHost));
+        }
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            ext[i].isi_status = static_cast<int32_t>(st[i]);
+            ext[i].stability = stab[i];
+            ext[i].free_synaptic_resource = fr[i];
+            ext[i].last_step = ls[i];
+            ext[i].last_spike_step = lss[i];
+            ext[i].first_isi_spike = fis[i];
+            ext[i].is_being_forced = forced[i];
+        }
+    }
+}
+
+void Backend::read_weights(const Uid &proj, float *out)
+{
+    ProjectionSlot *p = find_proj(proj);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown projection");
+    if (!initialized_)
+    {
+        if (p->generated) throw Error(KNP_GB300_E_STATE, "generated projection weights exist only after init");
+        std::copy(p->weight.begin(), p->weight.end(), out);
+        return;
+    }
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    std::vector<float> w(p->n_syn);
+    if (p->n_syn) KNP_CUDA(cudaMemcpy(w.data(), p->w, p->n_syn * 4, cudaMemcpyDeviceToHost));
+    if (p->generated)
+    {
+        // Generated projections are read back in CSR order (row by presynaptic neuron).
+        std::copy(w.begin(), w.end(), out);
+        return;
+    }
+    std::vector<uint32_t> perm(p->n_syn);
+    if (p->n_syn) KNP_CUDA(cudaMemcpy(perm.data(), p->perm, p->n_syn * 4, cudaMemcpyDeviceToHost));
+    for (uint64_t e = 0; e < p->n_syn; ++e) out[perm[e]] = w[e];
+}
+
+uint64_t Backend::projection_size(const Uid &proj) const
+{
+    const ProjectionSlot *p = find_proj(proj);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown projection");
+    return p->n_syn;
+}
+
+void Backend::counters(uint64_t *events, uint64_t *spikes, uint64_t *updates)
+{
+    Control c{};
+    if (initialized_)
+    {
+        KNP_CUDA(cudaMemcpyAsync(&c, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, stream_));
+        KNP_CUDA(cudaStreamSynchronize(stream_));
+    }
+    if (events) *events = c.events_total;
+    if (spikes) *spikes = c.spikes_total;
+    if (updates) *updates = neurons_total_ * step_;
+}
+
+void Backend::synchronize()
+{
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    check_device_error();
+}
+
+}  // namespace knp_gb300

@@ -1,0 +1,247 @@
+// Host runtime of the GB300 KNP backend: owns device memory, builds the device network at init,
+// records the step as a CUDA graph, stages external messages and drains spike recordings.
+//
+// The step order is the single-threaded backend's (knp/backends/cpu/cpu-single-threaded-backend/
+// impl/backend.cpp:89-141): all populations (consume this step's ring slot, emit spikes), then all
+// projections (scatter this step's spikes into future ring slots), then additive-STDP updates
+// (after the scatter, as modify_weights follows impact construction in delta_impl.h:63-111), then the
+// end-of-step kernel. Internal SpikeMessages / SynapticImpactMessages never leave the device.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/knp_gb300.h"
+#include "kernels.h"
+
+namespace knp_gb300
+{
+
+class Error : public std::runtime_error
+{
+public:
+    Error(int code, const std::string &msg) : std::runtime_error(msg), code_(code) {}
+    int code() const { return code_; }
+
+private:
+    int code_;
+};
+
+struct Uid
+{
+    knp_uid v{};
+    Uid() = default;
+    explicit Uid(const knp_uid &u) : v(u) {}
+    bool operator<(const Uid &o) const { return std::memcmp(v.bytes, o.v.bytes, 16) < 0; }
+    bool operator==(const Uid &o) const { return std::memcmp(v.bytes, o.v.bytes, 16) == 0; }
+    bool is_null() const
+    {
+        for (auto b : v.bytes)
+            if (b) return false;
+        return true;
+    }
+};
+
+// Owner of device allocations made for one backend.
+class DeviceArena
+{
+public:
+    ~DeviceArena();
+    void *alloc(size_t bytes, bool zero = true);
+    template <class T>
+    T *make(size_t n, bool zero = true)
+    {
+        return static_cast<T *>(alloc(n * sizeof(T), zero));
+    }
+    void release(void *p);
+    size_t bytes() const { return bytes_; }
+
+private:
+    std::vector<void *> ptrs_;
+    size_t bytes_ = 0;
+};
+
+struct PopulationSlot
+{
+    Uid uid;
+    int kind = KNP_NEURON_BLIFAT;
+    uint32_t n = 0, n_pad = 0;
+    std::vector<knp_blifat_neuron> init_blifat;
+    std::vector<knp_resource_stdp_state> init_res;
+    std::vector<knp_lif_neuron> init_lif;
+    int acc_request = KNP_GB300_ACC_AUTO;
+    bool record = false;
+    std::set<Uid> impact_senders;
+    // device
+    BlifatDev bdev{};
+    LifDev ldev{};
+    RingView ring{};
+    uint32_t counter_index = 0;
+    uint32_t *log = nullptr;
+    unsigned long long *log_fill = nullptr;  // device
+    unsigned long long log_cap = 0;
+    bool has_external_impacts = false;
+    // recorded spikes drained to the host: per step, ascending indexes
+    std::map<uint64_t, std::vector<uint32_t>> recorded;
+    uint64_t record_from = 0;
+};
+
+struct ProjectionSlot
+{
+    Uid uid;
+    int kind = KNP_SYNAPSE_DELTA;
+    Uid pre_uid, post_uid;
+    uint64_t n_syn = 0;
+    // host copy until init
+    std::vector<uint32_t> pre, post, delay;
+    std::vector<float> weight, tau_plus, tau_minus;
+    std::vector<uint8_t> type;
+    bool generated = false;
+    struct
+    {
+        uint32_t n_pre, n_post, fan_in;
+        int32_t k_lo, k_hi;
+        uint32_t d_lo, d_hi;
+        uint64_t seed, stream;
+    } gen{};
+    std::map<Uid, int> stdp_pops;
+    std::set<Uid> spike_senders;
+    uint32_t max_delay = 1;
+    bool dyadic = true;  // every weight is k/256 with bounded column sums
+    // device
+    uint32_t n_rows = 0;
+    long long *row_ptr = nullptr;
+    int32_t *col = nullptr;
+    float *w = nullptr;
+    uint8_t *delay_d = nullptr;
+    uint8_t *type_d = nullptr;
+    uint32_t *perm = nullptr;  // CSR position -> loaded synapse index (null for generated projections)
+    ProjectionDev dev{};
+    StdpDev stdp{};
+    std::vector<std::pair<SpikeSource, int>> stdp_sources;  // (source, both lists)
+};
+
+struct Channel
+{
+    Uid uid;
+    ChannelDev host{};
+    ChannelDev *dev = nullptr;  // device descriptor read by kernels
+    // device data
+    long long *offsets = nullptr;
+    uint32_t *idx = nullptr;
+    uint64_t cap_idx = 0, cap_steps = 0;
+    bool scheduled = false;        // a device schedule is loaded
+    bool owns_generated = false;   // idx allocated by the device generator (cudaFree on replace)
+    std::vector<uint32_t> pending;  // host-sent spikes for the next step
+    bool has_pending = false;
+};
+
+struct PendingImpacts
+{
+    Uid receiver;
+    bool forcing;
+    std::vector<uint32_t> post;
+    std::vector<float> value;
+    std::vector<uint8_t> type;
+};
+
+class Backend
+{
+public:
+    explicit Backend(int device);
+    ~Backend();
+
+    void load_blifat(const Uid &uid, int kind, uint32_t n, const knp_blifat_neuron *neurons,
+                     const knp_resource_stdp_state *ext);
+    void load_projection(const Uid &uid, int kind, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn,
+                         const uint32_t *pre, const uint32_t *post, const float *w, const uint32_t *delay,
+                         const uint8_t *type, const float *tau_plus, const float *tau_minus);
+    void generate_fixed_fan_in(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint32_t n_pre, uint32_t n_post,
+                               uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed,
+                               uint64_t stream);
+    void set_stdp_population(const Uid &proj, const Uid &pop, int processing);
+    void subscribe(const Uid &receiver, const Uid &sender);
+    void set_accumulator(const Uid &pop, int mode);
+    void record_spikes(const Uid &pop, bool enable);
+    void init();
+
+    void send_spikes(const Uid &sender, uint64_t send_time, uint32_t n, const uint32_t *idx);
+    void load_schedule(const Uid &sender, uint64_t first_step, uint64_t n_steps, const int64_t *offsets,
+                       const uint32_t *idx);
+    void generate_bernoulli(const Uid &sender, uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps,
+                            uint64_t seed, uint64_t stream);
+    void send_impacts(const Uid &sender, const Uid &receiver, bool forcing, uint32_t n, const uint32_t *post,
+                      const float *value, const uint8_t *type);
+
+    void step(uint64_t n);
+    float step_timed(uint64_t n);
+    void profile_phases(uint64_t n, float *ms);
+    uint64_t current_step() const { return step_; }
+    void read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n);
+    void discard_spikes(uint64_t before);
+    void read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext);
+    void read_weights(const Uid &proj, float *out);
+    uint64_t projection_size(const Uid &proj) const;
+    void counters(uint64_t *events, uint64_t *spikes, uint64_t *updates);
+    void synchronize();
+    void set_learning(bool on) { learning_ = on; }
+    cudaStream_t stream() const { return stream_; }
+
+private:
+    PopulationSlot *find_pop(const Uid &u);
+    ProjectionSlot *find_proj(const Uid &u);
+    const ProjectionSlot *find_proj(const Uid &u) const;
+    Channel *find_channel(const Uid &u);
+    Channel &channel(const Uid &u);
+    void require_not_init(const char *what) const;
+    void require_init(const char *what) const;
+
+    void build_population(PopulationSlot &p);
+    void build_projection(ProjectionSlot &p);
+    void build_stdp(ProjectionSlot &p);
+    void wire();
+    void enqueue_step();
+    void capture_graphs();
+    void stage_host_inputs();
+    void drain_recordings();
+    void check_device_error();
+    void ensure_record_capacity(uint64_t n_steps);
+    uint64_t steps_before_drain() const;
+
+    int device_ = 0;
+    int sm_count_ = 0;
+    cudaStream_t stream_ = nullptr;
+    DeviceArena arena_;
+    bool initialized_ = false;
+    bool learning_ = true;
+    uint64_t step_ = 0;  // host mirror of Control::step
+    std::vector<std::unique_ptr<PopulationSlot>> pops_;
+    std::vector<std::unique_ptr<ProjectionSlot>> projs_;
+    std::vector<std::unique_ptr<Channel>> channels_;
+    std::vector<std::pair<Uid, Uid>> subs_;
+    std::vector<PendingImpacts> pending_impacts_;
+    Control *ctl_ = nullptr;
+    uint32_t *counters_ = nullptr;  // per-step counters
+    uint32_t n_counters_ = 0, n_spike_counters_ = 0;
+    uint32_t *hist_ = nullptr;
+    unsigned long long *hist_base_ = nullptr;
+    uint32_t hist_steps_ = 4096;
+    uint64_t hist_base_host_ = 0;
+    uint64_t neurons_total_ = 0;
+    uint64_t updates_before_init_ = 0;
+    cudaGraphExec_t graph1_ = nullptr, graphK_ = nullptr;
+    static constexpr uint64_t kGraphSteps = 16;
+    // pinned staging for host-sent messages
+    void *pinned_ = nullptr;
+    size_t pinned_bytes_ = 0;
+    cudaEvent_t pinned_free_ = nullptr;
+    bool any_recording_ = false;
+};
+
+}  // namespace knp_gb300

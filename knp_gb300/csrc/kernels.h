@@ -1,0 +1,248 @@
+// Device data layout of the GB300 KNP backend and the host-side launchers of its kernels.
+//
+// Layout in HBM (one backend):
+//   population  SoA arrays of n_pad = round_up(n, 4) entries (float4-aligned), one per live state
+//               field; parameters either broadcast (uniform across the population) or SoA arrays.
+//   input ring  [slots][n_pad] accumulators of postsynaptic input, slot = step mod slots, with
+//               slots = the largest delay into the population. FP32 (exact for dyadic weights) or
+//               int64 fixed point with 40 fractional bits (order-independent). Optional rings for
+//               conductance / dopamine input and a forcing bitmap for resource-STDP neurons.
+//   projection  presynaptic-major CSR: row_ptr int64[n_pre + 1], col int32[S], weight fp32[S],
+//               delay u8[S], optional per-synapse output type u8[S]; STDP projections add a
+//               postsynaptic-major index (col_ptr, CSR positions) and per-column spike histories.
+//   spikes      per population a spike list (u32[n]) + count, written by the population kernel
+//               with warp-ballot compaction, consumed by projection kernels in the same step.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace knp_gb300
+{
+
+constexpr int kFxShift = 40;  // fixed-point input: value * 2^40 in int64
+constexpr int kMaxSources = 8;
+
+// Bits of Control::error.
+enum DeviceError : uint32_t
+{
+    kErrLogOverflow = 1u << 0,
+    kErrHistory = 1u << 1,
+};
+
+// Device-resident step control block (one per backend).
+struct Control
+{
+    unsigned long long step;          // step being executed
+    unsigned long long events_total;  // synaptic events (impacts created) since init
+    unsigned long long spikes_total;  // spikes since init
+    unsigned int error;               // sticky DeviceError bits
+    unsigned int pad;
+};
+
+struct RingView
+{
+    uint32_t n;      // neurons
+    uint32_t pitch;  // elements per slot row (multiple of 4)
+    uint32_t slots;  // ring length
+    int fixed;       // 0: v32, 1: v64
+    float *v32;
+    long long *v64;
+    float *g;          // conductance input, or null
+    float *dopa;       // dopamine input, or null
+    uint32_t *forced;  // forcing bitmap [slots][words], or null
+    uint32_t words;
+};
+
+// Liveness flags of a BLIFAT population: a field that is not live keeps a value that follows from
+// its initial value alone and is neither read nor written per step.
+enum BlifatFlags : uint32_t
+{
+    kLiveVRead = 1u << 0,     // potential carries over between steps (potential_decay != 0 somewhere)
+    kLiveThrDyn = 1u << 1,    // dynamic threshold
+    kLiveTrace = 1u << 2,     // postsynaptic trace
+    kLiveG = 1u << 3,         // inhibitory conductance
+    kLiveBurst = 1u << 4,     // bursting phase
+    kLiveBlock = 1u << 5,     // total blocking period
+    kLiveRefract = 1u << 6,   // steps since last firing must be tracked per neuron
+    kLiveDopa = 1u << 7,      // dopamine input
+    kLiveVPre = 1u << 8,      // store pre-impact potential
+    kResource = 1u << 9,      // synaptic-resource-STDP neuron bookkeeping
+    kLiveRenorm = 1u << 10,   // free-resource renormalisation can fire
+    kLiveAddThr = 1u << 11,   // additional threshold differs from 0 somewhere
+};
+
+// One parameter: a broadcast value, or a per-neuron array when `a` is not null.
+struct ParamF
+{
+    const float *a;
+    float u;
+};
+struct ParamU
+{
+    const uint32_t *a;
+    uint32_t u;
+};
+
+struct ResourceDev
+{
+    // state
+    int32_t *isi_status;
+    unsigned long long *last_step, *last_spike_step, *first_isi_spike;
+    float *stability, *free_resource;
+    uint8_t *is_forced;  // is_being_forced_ of the last step
+    // parameters
+    ParamF add_thr_coef, resource_threshold, stability_change_param, stability_change_at_isi;
+    ParamU isi_max;
+};
+
+struct BlifatDev
+{
+    uint32_t n, n_pad;
+    uint32_t flags;
+    // state
+    float *V, *V_pre, *thr_dyn, *trace, *g, *dopa, *add_thr;
+    uint32_t *n_since, *burst_phase;
+    long long *blocking;
+    // parameters
+    ParamF thr, thr_decay, thr_inc, trace_decay, trace_inc, g_decay, v_decay, reflexive, e_inh, v_reset, v_min;
+    ParamU t_ref, burst_period;
+    ResourceDev res;
+    // outputs
+    uint32_t *spikes;
+    uint32_t *spike_count;  // this step
+    uint32_t *log;          // spike recording, or null
+    unsigned long long *log_fill;
+    unsigned long long log_cap;
+    RingView ring;
+};
+
+struct LifDev
+{
+    uint32_t n, n_pad;
+    float *V;
+    uint32_t *refract;
+    ParamF leak, thr, v_reset;
+    ParamU refract_period;
+    uint32_t *spikes;
+    uint32_t *spike_count;
+    uint32_t *log;
+    unsigned long long *log_fill;
+    unsigned long long log_cap;
+    RingView ring;
+};
+
+// External spike schedule of one sender channel (device-resident window).
+struct ChannelDev
+{
+    unsigned long long first_step;
+    unsigned long long n_steps;
+    const long long *offsets;  // n_steps + 1
+    const uint32_t *idx;
+};
+
+// A spike source of a projection: a population's spike list of this step, or a channel.
+struct SpikeSource
+{
+    const uint32_t *idx;          // population spike list (null for a channel)
+    const uint32_t *count;        // population spike count
+    const ChannelDev *channel;    // channel descriptor (null for a population)
+};
+
+struct ProjectionDev
+{
+    const long long *row_ptr;
+    uint32_t n_rows;
+    const int32_t *col;
+    float *w;
+    const uint8_t *delay;
+    const uint8_t *type;  // per-synapse output type, or null (uniform_type)
+    int uniform_type;
+    int forcing;  // impacts of this projection carry is_forcing (plain delta projections)
+    RingView ring;
+    int n_src;
+    SpikeSource src[kMaxSources];
+};
+
+// Additive-STDP state of one projection (per postsynaptic column).
+struct StdpDev
+{
+    uint32_t n_cols;
+    uint32_t period;  // list capacity and trigger count: smallest integer >= tau_plus + tau_minus
+    uint32_t *pre_hist, *post_hist;  // [n_cols][period] step numbers
+    uint32_t *pre_cnt, *post_cnt;    // [n_cols]
+    uint32_t *touched;               // [n_cols] columns appended this step
+    uint32_t *touched_count;         // this step
+    unsigned long long *touched_stamp;  // [n_cols] step + 1 of the last append
+    const long long *col_ptr;        // [n_cols + 1] into col_pos
+    const uint64_t *col_pos;         // CSR positions of the column's synapses
+    float *w;                        // CSR weights
+    const float *table;              // stdp_w(d) for d in [0, table_len)
+    uint32_t table_len;
+};
+
+// Per-step reset of this step's counters (launched at the end of every step for the next one).
+struct StepEnd
+{
+    uint32_t *zero_u32;       // per-step counters to zero
+    uint32_t n_zero_u32;
+    uint32_t n_spike_counts;  // the first n_spike_counts counters are population spike counts
+    uint32_t *hist;           // per-step copy of the spike counts: hist[(step - *hist_base) * n_spike_counts + k]
+    const unsigned long long *hist_base;
+    uint32_t hist_steps;      // capacity in steps
+};
+
+// ---------------------------------------------------------------- launchers (stream-ordered)
+void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s);
+void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
+void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
+void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
+void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
+void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
+void launch_apply_impacts(
+    const RingView &ring, const uint32_t *post, const float *value, const uint8_t *type, int forcing, uint32_t n,
+    Control *ctl, cudaStream_t s);
+
+// Network construction on the device.
+cudaError_t build_csr(
+    uint64_t n_syn, uint32_t n_rows, const uint32_t *d_row_key, uint32_t *d_perm_out, long long *d_row_ptr,
+    void *d_temp, size_t temp_bytes, size_t *temp_needed, cudaStream_t s);
+void launch_iota_u32(uint32_t *out, uint64_t n, cudaStream_t s);
+void launch_gather_synapses(
+    uint64_t n_syn, const uint32_t *perm, const uint32_t *post, const float *w, const uint32_t *delay,
+    const uint8_t *type, int32_t *col_out, float *w_out, uint8_t *delay_out, uint8_t *type_out, cudaStream_t s);
+void launch_gen_fixed_fan_in_keys(
+    uint64_t n_syn, uint32_t n_pre, unsigned long long key_pre, uint32_t *pre_out, cudaStream_t s);
+void launch_gen_fixed_fan_in_gather(
+    uint64_t n_syn, const uint32_t *perm, uint32_t n_post, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi,
+    unsigned long long key_w, unsigned long long key_d, int32_t *col_out, float *w_out, uint8_t *delay_out,
+    cudaStream_t s);
+cudaError_t gen_bernoulli_schedule(
+    uint32_t n_sources, unsigned long long threshold, unsigned long long key, unsigned long long first_step,
+    uint64_t n_steps, long long *d_offsets, uint32_t **d_idx, uint64_t *n_idx, cudaStream_t s);
+
+// Counter-based generator shared with knp_gb300/network.py (SplitMix64 finaliser).
+__host__ __device__ inline unsigned long long mix64(unsigned long long x)
+{
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__host__ __device__ inline unsigned long long stream_key(unsigned long long seed, unsigned long long stream)
+{
+    return mix64(seed * 0x9E3779B97F4A7C15ull + stream);
+}
+__host__ __device__ inline unsigned long long rand64(unsigned long long key, unsigned long long ctr)
+{
+    return mix64(key ^ (ctr * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull));
+}
+__host__ __device__ inline long long uniform_int(unsigned long long key, unsigned long long ctr, long long lo, long long hi)
+{
+    const unsigned long long r = rand64(key, ctr) >> 32;
+    const unsigned long long span = static_cast<unsigned long long>(hi - lo + 1);
+    return static_cast<long long>((r * span) >> 32) + lo;
+}
+
+}  // namespace knp_gb300

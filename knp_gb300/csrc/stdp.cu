@@ -1,0 +1,170 @@
+// Additive STDP kernels and the end-of-step kernel.
+//
+// The reference rule (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/impl/projections/
+// training/stdp/additive_stdp.h) keeps two spike-time lists per synapse and, every step, scans all
+// synapses:
+//   init_projection (:117-170)  a SpikeMessage from an STDP population appends its send time to the
+//       postsynaptic list (and, for STDPAndSpike, the presynaptic list) of every synapse found
+//       by_postsynaptic for each spiking index, while the list is shorter than tau+ + tau-;
+//   modify_weights (:173-196)   when both lists reach tau+ + tau-, weight += sum over (t_f in pre,
+//       t_n in post) of stdp_w(float(t_n - t_f)) with unsigned differences, then both lists clear.
+// Every synapse of one postsynaptic column receives the same appends, so the GB300 layout keeps one
+// pair of lists per column and touches only the columns appended this step. stdp_w(d) is 1 for
+// d = 0, expf(-d / tau+) for d > 0 and 0 for t_n < t_f (the unsigned difference wraps to a huge
+// value); its values for d in [0, table_len) come from the host, computed with the same libm call as
+// the reference, and the sum is accumulated in the reference's order in FP32.
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace knp_gb300
+{
+namespace
+{
+
+__global__ void stdp_append_kernel(StdpDev d, SpikeSource src, int both_lists, Control *ctl)
+{
+    const unsigned long long t = ctl->step;
+    const uint32_t *idx;
+    uint32_t cnt;
+    if (src.channel)
+    {
+        const ChannelDev &c = *src.channel;
+        if (t >= c.first_step && t - c.first_step < c.n_steps)
+        {
+            const unsigned long long k = t - c.first_step;
+            idx = c.idx + c.offsets[k];
+            cnt = static_cast<uint32_t>(c.offsets[k + 1] - c.offsets[k]);
+        }
+        else
+        {
+            return;
+        }
+    }
+    else
+    {
+        idx = src.idx;
+        cnt = *src.count;
+    }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
+    {
+        const uint32_t col = idx[k];
+        if (col >= d.n_cols) continue;
+        const uint32_t tt = static_cast<uint32_t>(t);
+        uint32_t c = d.post_cnt[col];
+        if (c < d.period)
+        {
+            d.post_hist[static_cast<size_t>(col) * d.period + c] = tt;
+            d.post_cnt[col] = c + 1;
+        }
+        if (both_lists)
+        {
+            c = d.pre_cnt[col];
+            if (c < d.period)
+            {
+                d.pre_hist[static_cast<size_t>(col) * d.period + c] = tt;
+                d.pre_cnt[col] = c + 1;
+            }
+        }
+        if (d.touched_stamp[col] != t + 1)
+        {
+            d.touched_stamp[col] = t + 1;
+            d.touched[atomicAdd(d.touched_count, 1u)] = col;
+        }
+    }
+}
+
+// One warp per touched column.
+__global__ void stdp_modify_kernel(StdpDev d, Control *ctl)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t n = *d.touched_count;
+    for (uint32_t k = warp; k < n; k += n_warps)
+    {
+        const uint32_t col = d.touched[k];
+        if (d.pre_cnt[col] < d.period || d.post_cnt[col] < d.period) continue;
+        float wj = 0.0f;
+        if (lane == 0)
+        {
+            const uint32_t *pre = d.pre_hist + static_cast<size_t>(col) * d.period;
+            const uint32_t *post = d.post_hist + static_cast<size_t>(col) * d.period;
+            for (uint32_t a = 0; a < d.period; ++a)
+            {
+                const uint32_t tf = pre[a];
+                for (uint32_t b = 0; b < d.period; ++b)
+                {
+                    const uint32_t tn = post[b];
+                    if (tn < tf) continue;  // term is exactly +0
+                    const uint32_t diff = tn - tf;
+                    if (diff < d.table_len) wj = __fadd_rn(wj, d.table[diff]);
+                }
+            }
+        }
+        wj = __shfl_sync(0xffffffffu, wj, 0);
+        const long long a = d.col_ptr[col], b = d.col_ptr[col + 1];
+        for (long long e = a + lane; e < b; e += 32)
+        {
+            const uint64_t pos = d.col_pos[e];
+            d.w[pos] = __fadd_rn(d.w[pos], wj);
+        }
+        __syncwarp();
+        if (lane == 0)
+        {
+            d.pre_cnt[col] = 0;
+            d.post_cnt[col] = 0;
+        }
+    }
+}
+
+__global__ void step_end_kernel(StepEnd e, uint32_t n_spike_counts, Control *ctl)
+{
+    __shared__ unsigned long long spikes;
+    if (threadIdx.x == 0) spikes = 0;
+    __syncthreads();
+    const unsigned long long rel = ctl->step - *e.hist_base;
+    if (rel >= e.hist_steps && threadIdx.x == 0) atomicOr(&ctl->error, kErrLogOverflow);
+    for (uint32_t k = threadIdx.x; k < e.n_zero_u32; k += blockDim.x)
+    {
+        if (k < n_spike_counts)
+        {
+            const uint32_t c = e.zero_u32[k];
+            atomicAdd(&spikes, static_cast<unsigned long long>(c));
+            if (rel < e.hist_steps) e.hist[rel * n_spike_counts + k] = c;
+        }
+        e.zero_u32[k] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        ctl->spikes_total += spikes;
+        ctl->step += 1;
+    }
+}
+
+}  // namespace
+
+void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s)
+{
+    const int threads = 256;
+    const int blocks = static_cast<int>((d.n_cols + threads - 1) / threads);
+    stdp_append_kernel<<<blocks > 0 ? blocks : 1, threads, 0, s>>>(d, src, both_lists, ctl);
+}
+
+void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s)
+{
+    const int threads = 256;
+    int blocks = static_cast<int>((static_cast<uint64_t>(d.n_cols) * 32 + threads - 1) / threads);
+    if (blocks > 1216) blocks = 1216;
+    stdp_modify_kernel<<<blocks > 0 ? blocks : 1, threads, 0, s>>>(d, ctl);
+}
+
+// Zeroes this step's counters (adding the population spike counts to the spike total) and advances
+// the device step number.
+void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s)
+{
+    step_end_kernel<<<1, 256, 0, s>>>(e, e.n_spike_counts, ctl);
+}
+
+}  // namespace knp_gb300

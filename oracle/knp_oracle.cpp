@@ -1,0 +1,751 @@
+// TEST INFRASTRUCTURE — CPU restatement of the KNP single-threaded backend step (the oracle).
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU arms load this library; the GB300 product
+// path never calls it. It restates, with FP64 neuron state and the reference's own container
+// structure (unordered_map future-impact queue, per-spike synapse lookup, impact vectors copied
+// through a FIFO bus), the following reference code (paths inside the KNP project):
+//
+//   step loop       knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:89-141
+//   subscriptions   knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/init.h:46-110
+//   bus order       knp/core-library/impl/message_bus_cpu_impl/message_bus_cpu_impl.cpp:41-88 (route = pop_back)
+//                   + message_endpoint_cpu_impl.h:62-76 (receive = pop_back): the two LIFOs give FIFO
+//   population      cpu-library/populations_old.h:104-121 (any), :195-217 (resource STDP)
+//   BLIFAT          cpu-library/impl/populations/blifat/blifat_impl.h:31-168
+//   resource STDP   cpu-library/impl/populations/blifat/blifat_stdp.h:35-172, impl/populations/training/stdp.h:88-186
+//   LIF             cpu-library/impl/populations/lif/lif_impl.h:33-86
+//   projection      cpu-library/projections.h:58-84, impl/projections/delta/delta_impl.h:54-114
+//   additive STDP   cpu-library/impl/projections/training/stdp/additive_stdp.h:42-196
+//
+// Synapses of one presynaptic (or postsynaptic) neuron are visited in ascending synapse index. The
+// reference visits them in Boost.MultiIndex hashed-index order (knp/core-library/impl/projection.cpp:168-188);
+// that order only changes FP64 rounding of impact sums, never the set of impacts.
+#include "knp_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+namespace
+{
+
+thread_local std::string g_error;
+
+struct Uid
+{
+    knp_uid v;
+    bool operator==(const Uid &o) const { return std::memcmp(v.bytes, o.v.bytes, 16) == 0; }
+    bool is_null() const
+    {
+        for (auto b : v.bytes)
+            if (b) return false;
+        return true;
+    }
+};
+
+struct UidHash
+{
+    size_t operator()(const Uid &u) const
+    {
+        uint64_t a, b;
+        std::memcpy(&a, u.v.bytes, 8);
+        std::memcpy(&b, u.v.bytes + 8, 8);
+        return static_cast<size_t>(a * 0x9E3779B97F4A7C15ull ^ b);
+    }
+};
+
+struct SpikeMessage
+{
+    Uid sender;
+    uint64_t send_time;
+    std::vector<uint32_t> idx;
+};
+
+struct Impact
+{
+    uint64_t connection_index;
+    float value;
+    uint8_t type;
+    uint32_t pre;
+    uint32_t post;
+};
+
+struct ImpactMessage
+{
+    Uid sender;
+    uint64_t send_time;
+    Uid pre_uid;
+    Uid post_uid;
+    bool is_forcing;
+    std::vector<Impact> impacts;
+};
+
+struct Population
+{
+    Uid uid;
+    int kind;
+    std::vector<knp_blifat_neuron> blifat;
+    std::vector<knp_resource_stdp_state> res;
+    std::vector<knp_lif_neuron> lif;
+    std::vector<uint32_t> last_spikes;
+    std::unordered_set<Uid, UidHash> impact_senders;  // impact-message subscription
+    std::vector<ImpactMessage> inbox;
+    size_t size() const { return kind == KNP_NEURON_LIF ? lif.size() : blifat.size(); }
+};
+
+struct Synapse
+{
+    float weight;
+    uint32_t delay;
+    uint8_t type;
+    float tau_plus;
+    float tau_minus;
+    std::vector<uint64_t> pre_times;
+    std::vector<uint64_t> post_times;
+    uint32_t pre;
+    uint32_t post;
+};
+
+struct Projection
+{
+    Uid uid;
+    int kind;
+    Uid pre_uid;
+    Uid post_uid;
+    std::vector<Synapse> syn;
+    std::vector<std::vector<size_t>> by_pre;
+    std::vector<std::vector<size_t>> by_post;
+    std::unordered_map<Uid, int, UidHash> stdp_pops;
+    std::unordered_set<Uid, UidHash> spike_senders;  // spike-message subscription
+    std::vector<SpikeMessage> inbox;
+    std::unordered_map<uint64_t, ImpactMessage> future;  // MessageQueue (message_queue.h:34)
+
+    const std::vector<size_t> &find_by_pre(uint32_t i) const
+    {
+        static const std::vector<size_t> none;
+        return i < by_pre.size() ? by_pre[i] : none;
+    }
+    const std::vector<size_t> &find_by_post(uint32_t i) const
+    {
+        static const std::vector<size_t> none;
+        return i < by_post.size() ? by_post[i] : none;
+    }
+};
+
+}  // namespace
+
+struct or_net
+{
+    std::vector<std::unique_ptr<Population>> pops;
+    std::vector<std::unique_ptr<Projection>> projs;
+    std::vector<std::pair<Uid, Uid>> extra_subs;  // receiver, sender
+    std::vector<SpikeMessage> ext_spikes;
+    std::vector<ImpactMessage> ext_impacts;
+    uint64_t step = 0;
+    uint64_t events = 0;
+    bool initialized = false;
+
+    Population *find_pop(const Uid &u) const
+    {
+        for (auto &p : pops)
+            if (p->uid == u) return p.get();
+        return nullptr;
+    }
+    Projection *find_proj(const Uid &u) const
+    {
+        for (auto &p : projs)
+            if (p->uid == u) return p.get();
+        return nullptr;
+    }
+};
+
+namespace
+{
+
+int fail(const std::string &msg)
+{
+    g_error = msg;
+    return -1;
+}
+
+// ---------------------------------------------------------------- BLIFAT (blifat_impl.h:31-168)
+
+void blifat_pre_impact(knp_blifat_neuron &n)
+{
+    ++n.n_time_steps_since_last_firing;
+    n.dynamic_threshold *= n.threshold_decay;
+    n.postsynaptic_trace *= n.postsynaptic_trace_decay;
+    n.inhibitory_conductance *= n.inhibitory_conductance_decay;
+    n.potential *= n.potential_decay;
+    if (1 == n.bursting_phase)
+    {
+        --n.bursting_phase;
+        n.potential += n.reflexive_weight;
+    }
+    n.pre_impact_potential = n.potential;
+}
+
+// Resource-STDP variant (blifat_impl.h:50-65): resets dopamine and forcing, and does not decrement
+// the bursting phase.
+void resource_blifat_pre_impact(knp_blifat_neuron &n, knp_resource_stdp_state &r)
+{
+    ++n.n_time_steps_since_last_firing;
+    n.dynamic_threshold *= n.threshold_decay;
+    n.postsynaptic_trace *= n.postsynaptic_trace_decay;
+    n.inhibitory_conductance *= n.inhibitory_conductance_decay;
+    n.dopamine_value = 0.0;
+    r.is_being_forced = 0;
+    n.potential *= n.potential_decay;
+    if (1 == n.bursting_phase) n.potential += n.reflexive_weight;
+    n.pre_impact_potential = n.potential;
+}
+
+void blifat_impact(knp_blifat_neuron &n, const Impact &imp)
+{
+    switch (imp.type)
+    {
+        case KNP_OUT_EXCITATORY:
+            n.potential += imp.value;
+            break;
+        case KNP_OUT_INHIBITORY_CURRENT:
+            n.potential -= imp.value;
+            break;
+        case KNP_OUT_INHIBITORY_CONDUCTANCE:
+            n.inhibitory_conductance += imp.value;
+            break;
+        case KNP_OUT_DOPAMINE:
+            n.dopamine_value += imp.value;
+            break;
+        case KNP_OUT_BLOCKING:
+            n.total_blocking_period = static_cast<int64_t>(imp.value);
+            break;
+        default:
+            throw std::runtime_error("Unhandled synapse type.");
+    }
+}
+
+bool blifat_post_impact(knp_blifat_neuron &n)
+{
+    if (n.total_blocking_period <= 0) n.potential = n.pre_impact_potential;
+    if (n.total_blocking_period < 0)
+    {
+        ++n.total_blocking_period;
+        if (n.total_blocking_period == 0) n.total_blocking_period = std::numeric_limits<int64_t>::max();
+    }
+    else if (n.total_blocking_period > 0)
+    {
+        n.total_blocking_period -= 1;
+    }
+    if (n.inhibitory_conductance < 1.0)
+        n.potential -= (n.potential - n.reversal_inhibitory_potential) * n.inhibitory_conductance;
+    else
+        n.potential = n.reversal_inhibitory_potential;
+
+    const bool spike = (n.n_time_steps_since_last_firing > n.absolute_refractory_period) &&
+                       (n.potential >= n.activation_threshold + n.dynamic_threshold + n.additional_threshold);
+    if (spike)
+    {
+        n.dynamic_threshold += n.threshold_increment;
+        n.postsynaptic_trace += n.postsynaptic_trace_increment;
+        n.potential = n.potential_reset_value;
+        n.bursting_phase = n.bursting_period;
+        n.n_time_steps_since_last_firing = 0;
+    }
+    if (n.potential < n.min_potential) n.potential = n.min_potential;
+    return spike;
+}
+
+// ------------------------------------------- resource-STDP neuron training (blifat_stdp.h:35-172)
+// The GB300 backend supports no SynapticResourceSTDPDeltaSynapse projection, so the list of
+// "working projections" (populations_old.h:207-209) is always empty and only the neuron-side
+// bookkeeping runs: ISI status, stability, additional threshold, dopamine-driven stability and the
+// free-resource renormalisation.
+
+int update_isi(knp_resource_stdp_state &r, const knp_blifat_neuron &n, uint64_t step)  // training/stdp.h:88-126
+{
+    if (r.is_being_forced)
+    {
+        r.isi_status = KNP_ISI_IS_FORCED;
+        return r.isi_status;
+    }
+    switch (r.isi_status)
+    {
+        case KNP_ISI_NOT_IN_PERIOD:
+        case KNP_ISI_IS_FORCED:
+            r.isi_status = KNP_ISI_PERIOD_STARTED;
+            r.first_isi_spike = step;
+            break;
+        case KNP_ISI_PERIOD_STARTED:
+            // Unsigned difference, as in the reference.
+            if (r.last_step - step < r.isi_max) r.isi_status = KNP_ISI_PERIOD_CONTINUED;
+            break;
+        case KNP_ISI_PERIOD_CONTINUED:
+            if (r.last_step - step >= r.isi_max || n.dopamine_value != 0)
+            {
+                r.isi_status = KNP_ISI_PERIOD_STARTED;
+                r.first_isi_spike = step;
+            }
+            break;
+        default:
+            throw std::runtime_error("Not supported ISI status.");
+    }
+    r.last_step = step;
+    return r.isi_status;
+}
+
+void train_resource_population(Population &pop, const std::vector<uint32_t> &spikes, uint64_t step)
+{
+    // process_spiking_neurons_impl (blifat_stdp.h:35-103) with no connected synapses.
+    for (uint32_t i : spikes)
+    {
+        auto &n = pop.blifat[i];
+        auto &r = pop.res[i];
+        r.last_spike_step = step;
+        update_isi(r, n, step);
+        if (KNP_ISI_PERIOD_STARTED == r.isi_status) r.stability -= r.stability_change_at_isi;
+        n.additional_threshold = 0.0;
+        n.additional_threshold *= r.synapse_sum_threshold_coefficient;
+    }
+    // do_dopamine_plasticity_impl (blifat_stdp.h:106-155).
+    for (size_t i = 0; i < pop.blifat.size(); ++i)
+    {
+        auto &n = pop.blifat[i];
+        auto &r = pop.res[i];
+        if (n.dopamine_value > 0.0 || (n.dopamine_value < 0.0 && r.isi_status != KNP_ISI_IS_FORCED))
+        {
+            if (r.is_being_forced || n.dopamine_value < 0)
+            {
+                r.stability -= n.dopamine_value * r.stability_change_parameter;
+                r.stability = std::max(r.stability, 0.0F);
+            }
+            else
+            {
+                const double dopamine_constant = 2.0;
+                const double difference = std::fabs(step - r.first_isi_spike - r.isi_max);
+                r.stability += r.stability_change_parameter * n.dopamine_value *
+                               std::max(dopamine_constant - difference / r.isi_max, -1.0);
+            }
+        }
+    }
+    // renormalize_resource (training/stdp.h:152-186).
+    for (size_t i = 0; i < pop.blifat.size(); ++i)
+    {
+        auto &r = pop.res[i];
+        if (step - r.last_step <= r.isi_max && r.isi_status != KNP_ISI_IS_FORCED) continue;
+        if (std::fabs(r.free_synaptic_resource) < r.synaptic_resource_threshold) continue;
+        r.free_synaptic_resource = 0.0F;
+    }
+}
+
+// ----------------------------------------------------------------------- LIF (lif_impl.h:33-86)
+
+void lif_pre_impact(knp_lif_neuron &n)
+{
+    if (0 == n.refract_counter) n.potential *= n.leak_coefficient;
+}
+
+void lif_impact(knp_lif_neuron &n, const Impact &imp)
+{
+    switch (imp.type)
+    {
+        case KNP_OUT_EXCITATORY:
+            if (0 == n.refract_counter) n.potential += imp.value;
+            break;
+        case KNP_OUT_INHIBITORY_CURRENT:
+            if (0 == n.refract_counter) n.potential -= imp.value;
+            break;
+        default:
+            throw std::runtime_error("Unhandled synapse type.");
+    }
+}
+
+bool lif_post_impact(knp_lif_neuron &n)
+{
+    if (0 == n.refract_counter)
+    {
+        if (n.potential > n.activation_threshold)
+        {
+            n.potential = n.potential_reset_value;
+            n.refract_counter = n.refract_period;
+            return true;
+        }
+    }
+    else
+    {
+        --n.refract_counter;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ one population step
+
+void check_impacts(const Population &pop, const std::vector<ImpactMessage> &msgs)
+{
+    for (auto &m : msgs)
+        for (auto &imp : m.impacts)
+            if (imp.post >= pop.size()) throw std::runtime_error("Impact postsynaptic index out of range.");
+}
+
+// calculate_any_population / calculate_resource_stdp_population (populations_old.h:104-121, 195-217).
+void calculate_population(Population &pop, uint64_t step)
+{
+    std::vector<ImpactMessage> msgs = std::move(pop.inbox);
+    pop.inbox.clear();
+    check_impacts(pop, msgs);
+    pop.last_spikes.clear();
+    if (pop.kind == KNP_NEURON_LIF)
+    {
+        for (auto &n : pop.lif) lif_pre_impact(n);
+        for (auto &m : msgs)
+            for (auto &imp : m.impacts) lif_impact(pop.lif[imp.post], imp);
+        for (uint32_t i = 0; i < pop.lif.size(); ++i)
+            if (lif_post_impact(pop.lif[i])) pop.last_spikes.push_back(i);
+        return;
+    }
+    const bool res = pop.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT;
+    for (size_t i = 0; i < pop.blifat.size(); ++i)
+    {
+        if (res)
+            resource_blifat_pre_impact(pop.blifat[i], pop.res[i]);
+        else
+            blifat_pre_impact(pop.blifat[i]);
+    }
+    for (auto &m : msgs)
+        for (auto &imp : m.impacts)
+        {
+            blifat_impact(pop.blifat[imp.post], imp);
+            if (res && imp.type == KNP_OUT_EXCITATORY) pop.res[imp.post].is_being_forced |= m.is_forcing ? 1u : 0u;
+        }
+    for (uint32_t i = 0; i < pop.blifat.size(); ++i)
+        if (blifat_post_impact(pop.blifat[i])) pop.last_spikes.push_back(i);
+    if (res) train_resource_population(pop, pop.last_spikes, step);
+}
+
+// --------------------------------------------------------- additive STDP (additive_stdp.h:42-196)
+
+// STDPFormula::stdp_w with a_plus = a_minus = 1 (additive_stdp.h:50-55, :187). The argument is the
+// unsigned step difference converted to float, as in stdp_delta_w (:72): a negative difference wraps
+// to a huge positive value, whose term is exp(-huge) = 0.
+float stdp_w(float tau_plus, float tau_minus, float weight_diff)
+{
+    return weight_diff > 0 ? 1.0F * std::exp(-weight_diff / tau_plus) : 1.0F * std::exp(weight_diff / tau_minus);
+}
+
+float stdp_delta_w(const Synapse &s)
+{
+    float w_j = 0;
+    for (uint64_t t_f : s.pre_times)
+        for (uint64_t t_n : s.post_times) w_j += stdp_w(s.tau_plus, s.tau_minus, static_cast<float>(t_n - t_f));
+    return w_j;
+}
+
+// init_projection (additive_stdp.h:117-170): fill spike-time lists from messages of STDP populations.
+void stdp_init_projection(Projection &proj, std::vector<SpikeMessage> &msgs)
+{
+    for (auto &msg : msgs)
+    {
+        auto it = proj.stdp_pops.find(msg.sender);
+        if (it == proj.stdp_pops.end()) continue;
+        const int type = it->second;
+        auto append = [&](bool post_list)
+        {
+            for (uint32_t j : msg.idx)
+                for (size_t si : proj.find_by_post(j))
+                {
+                    Synapse &s = proj.syn[si];
+                    auto &q = post_list ? s.post_times : s.pre_times;
+                    if (q.size() < s.tau_minus + s.tau_plus) q.push_back(msg.send_time);
+                }
+        };
+        append(true);
+        if (type == KNP_STDP_AND_SPIKE) append(false);
+        if (type == KNP_STDP_ONLY) msg.idx.clear();
+    }
+}
+
+// modify_weights (additive_stdp.h:173-196).
+void stdp_modify_weights(Projection &proj)
+{
+    for (auto &s : proj.syn)
+    {
+        const float period = s.tau_plus + s.tau_minus;
+        if (s.pre_times.size() >= period && s.post_times.size() >= period)
+        {
+            s.weight += stdp_delta_w(s);
+            s.pre_times.clear();
+            s.post_times.clear();
+        }
+    }
+}
+
+// ----------------------------------------------------------------- one projection step
+
+// projections::calculate_projection + delta::calculate_projection_impl (projections.h:58-84,
+// delta_impl.h:54-114). Returns true and fills `out` if an impact message is due this step.
+bool calculate_projection(or_net &net, Projection &proj, uint64_t step, ImpactMessage &out)
+{
+    std::vector<SpikeMessage> msgs = std::move(proj.inbox);
+    proj.inbox.clear();
+    const bool stdp = proj.kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA;
+    if (stdp) stdp_init_projection(proj, msgs);
+    for (auto &msg : msgs)
+        for (uint32_t spiked : msg.idx)
+            for (size_t si : proj.find_by_pre(spiked))
+            {
+                const Synapse &s = proj.syn[si];
+                // The message is sent on step N - 1 and received on step N.
+                const uint64_t future_step = s.delay + step - 1;
+                Impact imp{si, s.weight, s.type, s.pre, s.post};
+                ++net.events;
+                auto it = proj.future.find(future_step);
+                if (it != proj.future.end())
+                {
+                    it->second.impacts.push_back(imp);
+                }
+                else
+                {
+                    // is_forced(): true for plain delta projections, false for additive STDP
+                    // (stdp_dispatcher.h:54-58, additive_stdp.h:199-203).
+                    ImpactMessage m{proj.uid, step, proj.pre_uid, proj.post_uid, !stdp, {imp}};
+                    proj.future.emplace(future_step, std::move(m));
+                }
+            }
+    if (stdp) stdp_modify_weights(proj);
+    auto it = proj.future.find(step);
+    if (it == proj.future.end()) return false;
+    out = std::move(it->second);
+    proj.future.erase(it);
+    return true;
+}
+
+template <class F>
+int guarded(F &&f)
+{
+    try
+    {
+        return f();
+    }
+    catch (const std::exception &e)
+    {
+        return fail(e.what());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *or_last_error(void) { return g_error.c_str(); }
+
+or_net *or_create(void) { return new or_net(); }
+
+void or_destroy(or_net *net) { delete net; }
+
+int or_add_blifat_population(
+    or_net *net, knp_uid uid, int kind, uint32_t n, const knp_blifat_neuron *neurons,
+    const knp_resource_stdp_state *ext)
+{
+    if (kind != KNP_NEURON_BLIFAT && kind != KNP_NEURON_RESOURCE_STDP_BLIFAT) return fail("bad neuron kind");
+    if (kind == KNP_NEURON_RESOURCE_STDP_BLIFAT && !ext) return fail("resource-STDP population needs ext state");
+    auto p = std::make_unique<Population>();
+    p->uid = Uid{uid};
+    p->kind = kind;
+    p->blifat.assign(neurons, neurons + n);
+    if (ext) p->res.assign(ext, ext + n);
+    net->pops.push_back(std::move(p));
+    return 0;
+}
+
+int or_add_lif_population(or_net *net, knp_uid uid, uint32_t n, const knp_lif_neuron *neurons)
+{
+    auto p = std::make_unique<Population>();
+    p->uid = Uid{uid};
+    p->kind = KNP_NEURON_LIF;
+    p->lif.assign(neurons, neurons + n);
+    net->pops.push_back(std::move(p));
+    return 0;
+}
+
+int or_add_projection(
+    or_net *net, knp_uid uid, int kind, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn,
+    const uint32_t *pre_idx, const uint32_t *post_idx, const float *weight, const uint32_t *delay,
+    const uint8_t *out_type, const float *tau_plus, const float *tau_minus)
+{
+    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) return fail("bad synapse kind");
+    auto p = std::make_unique<Projection>();
+    p->uid = Uid{uid};
+    p->kind = kind;
+    p->pre_uid = Uid{pre_uid};
+    p->post_uid = Uid{post_uid};
+    p->syn.resize(n_syn);
+    uint32_t max_pre = 0, max_post = 0;
+    for (uint64_t i = 0; i < n_syn; ++i)
+    {
+        Synapse &s = p->syn[i];
+        s.weight = weight[i];
+        s.delay = delay[i];
+        s.type = out_type ? out_type[i] : KNP_OUT_EXCITATORY;
+        s.tau_plus = tau_plus ? tau_plus[i] : 10.0F;
+        s.tau_minus = tau_minus ? tau_minus[i] : 10.0F;
+        s.pre = pre_idx[i];
+        s.post = post_idx[i];
+        max_pre = std::max(max_pre, s.pre + 1);
+        max_post = std::max(max_post, s.post + 1);
+    }
+    p->by_pre.resize(max_pre);
+    p->by_post.resize(max_post);
+    for (uint64_t i = 0; i < n_syn; ++i)
+    {
+        p->by_pre[p->syn[i].pre].push_back(i);
+        p->by_post[p->syn[i].post].push_back(i);
+    }
+    net->projs.push_back(std::move(p));
+    return 0;
+}
+
+int or_set_stdp_population(or_net *net, knp_uid proj_uid, knp_uid pop_uid, int processing)
+{
+    Projection *p = net->find_proj(Uid{proj_uid});
+    if (!p) return fail("unknown projection");
+    if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) return fail("not an STDP projection");
+    p->stdp_pops[Uid{pop_uid}] = processing;
+    return 0;
+}
+
+int or_subscribe(or_net *net, knp_uid receiver, knp_uid sender)
+{
+    net->extra_subs.emplace_back(Uid{receiver}, Uid{sender});
+    if (net->initialized)
+    {
+        if (Projection *p = net->find_proj(Uid{receiver})) p->spike_senders.insert(Uid{sender});
+        if (Population *q = net->find_pop(Uid{receiver})) q->impact_senders.insert(Uid{sender});
+    }
+    return 0;
+}
+
+int or_init(or_net *net)
+{
+    // cpu::init (init.h:93-110) + subscribe_stdp_projection (init.h:46-82).
+    for (auto &p : net->projs)
+    {
+        for (auto &[pop_uid, _] : p->stdp_pops)
+            if (!pop_uid.is_null()) p->spike_senders.insert(pop_uid);
+        if (!p->pre_uid.is_null()) p->spike_senders.insert(p->pre_uid);
+        if (!p->post_uid.is_null())
+            if (Population *q = net->find_pop(p->post_uid)) q->impact_senders.insert(p->uid);
+    }
+    for (auto &[recv, send] : net->extra_subs)
+    {
+        if (Projection *p = net->find_proj(recv)) p->spike_senders.insert(send);
+        if (Population *q = net->find_pop(recv)) q->impact_senders.insert(send);
+    }
+    net->initialized = true;
+    return 0;
+}
+
+int or_send_spikes(or_net *net, knp_uid sender, uint64_t send_time, uint32_t n, const uint32_t *idx)
+{
+    net->ext_spikes.push_back(SpikeMessage{Uid{sender}, send_time, std::vector<uint32_t>(idx, idx + n)});
+    return 0;
+}
+
+int or_send_impacts(
+    or_net *net, knp_uid sender, knp_uid receiver_pop, int is_forcing, uint32_t n, const uint32_t *post_idx,
+    const float *value, const uint8_t *out_type)
+{
+    ImpactMessage m{Uid{sender}, net->step, Uid{knp_uid{}}, Uid{receiver_pop}, is_forcing != 0, {}};
+    for (uint32_t i = 0; i < n; ++i)
+        m.impacts.push_back(Impact{0, value[i], out_type ? out_type[i] : uint8_t(KNP_OUT_EXCITATORY), 0, post_idx[i]});
+    net->ext_impacts.push_back(std::move(m));
+    return 0;
+}
+
+// SingleThreadedCPUBackend::_step (backend.cpp:89-141): route, populations, route, projections, route.
+int or_step(or_net *net)
+{
+    return guarded(
+        [&]
+        {
+            if (!net->initialized) throw std::runtime_error("or_init was not called");
+            const uint64_t step = net->step;
+            // Route #1: external messages sent before this step.
+            for (auto &m : net->ext_spikes)
+                for (auto &p : net->projs)
+                    if (p->spike_senders.count(m.sender)) p->inbox.push_back(m);
+            for (auto &m : net->ext_impacts)
+                for (auto &q : net->pops)
+                    if (q->impact_senders.count(m.sender)) q->inbox.push_back(m);
+            net->ext_spikes.clear();
+            net->ext_impacts.clear();
+            // Populations, in load order; their spike messages are routed after all of them ran.
+            std::vector<SpikeMessage> sent;
+            for (auto &q : net->pops)
+            {
+                calculate_population(*q, step);
+                if (!q->last_spikes.empty()) sent.push_back(SpikeMessage{q->uid, step, q->last_spikes});
+            }
+            for (auto &m : sent)  // Route #2.
+                for (auto &p : net->projs)
+                    if (p->spike_senders.count(m.sender)) p->inbox.push_back(m);
+            // Projections, in load order.
+            std::vector<ImpactMessage> out;
+            for (auto &p : net->projs)
+            {
+                ImpactMessage m;
+                if (calculate_projection(*net, *p, step, m)) out.push_back(std::move(m));
+            }
+            for (auto &m : out)  // Route #3: delivered to populations for the next step.
+                for (auto &q : net->pops)
+                    if (q->impact_senders.count(m.sender)) q->inbox.push_back(m);
+            ++net->step;
+            return 0;
+        });
+}
+
+uint64_t or_get_step(const or_net *net) { return net->step; }
+
+int or_read_spikes(const or_net *net, knp_uid pop, uint32_t cap, uint32_t *out, uint32_t *n)
+{
+    const Population *q = net->find_pop(Uid{pop});
+    if (!q) return fail("unknown population");
+    *n = static_cast<uint32_t>(q->last_spikes.size());
+    if (q->last_spikes.size() > cap) return fail("spike buffer too small");
+    std::copy(q->last_spikes.begin(), q->last_spikes.end(), out);
+    return 0;
+}
+
+int or_read_blifat(const or_net *net, knp_uid pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext)
+{
+    const Population *q = net->find_pop(Uid{pop});
+    if (!q || q->kind == KNP_NEURON_LIF) return fail("unknown BLIFAT population");
+    std::copy(q->blifat.begin(), q->blifat.end(), out);
+    if (ext && !q->res.empty()) std::copy(q->res.begin(), q->res.end(), ext);
+    return 0;
+}
+
+int or_read_lif(const or_net *net, knp_uid pop, knp_lif_neuron *out)
+{
+    const Population *q = net->find_pop(Uid{pop});
+    if (!q || q->kind != KNP_NEURON_LIF) return fail("unknown LIF population");
+    std::copy(q->lif.begin(), q->lif.end(), out);
+    return 0;
+}
+
+int or_read_weights(const or_net *net, knp_uid proj, float *out)
+{
+    const Projection *p = net->find_proj(Uid{proj});
+    if (!p) return fail("unknown projection");
+    for (size_t i = 0; i < p->syn.size(); ++i) out[i] = p->syn[i].weight;
+    return 0;
+}
+
+uint64_t or_event_count(const or_net *net) { return net->events; }
+
+}  // extern "C"

@@ -1,0 +1,55 @@
+"""Writes tests/golden/spike_digests.json from the reference-header oracle (oracle/_ref/libknp_ref.so:
+the KNP reference's own per-neuron / per-synapse headers, built by `make -C oracle ref` where the
+KNP sources are present). Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Each case stores, per step, the spike count and the CRC32 of the ascending spike indexes of the
+network's first population, the total synaptic event count, and CRC32s of final projection weights.
+"""
+import json
+import os
+import sys
+import zlib
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from knp_gb300 import network as N  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+CASES = [
+    ("smallest_delta", "smallest_network", {"kind": "delta"}, 20, [0, 1]),
+    ("smallest_stdp", "smallest_network", {"kind": "stdp"}, 20, [0, 1]),
+    ("smallest_stdp_resource", "smallest_network", {"kind": "stdp_resource_neuron"}, 20, [0, 1]),
+    ("small_seed1_1000", "small_network", {"seed": 1, "steps": 1000}, 1000, []),
+    ("large_sparse_n2000", "large_sparse_network", {"seed": 2, "n": 2000, "fan_in": 200, "steps": 100}, 100, []),
+    ("stdp_3samples", "stdp_network", {"seed": 3, "samples": 3, "steps_per_sample": 100}, 300, [0, 1]),
+]
+
+
+def digest(trains):
+    return [[int(s.size), zlib.crc32(np.ascontiguousarray(s, np.uint32).tobytes())] for s in trains]
+
+
+def main():
+    orc.build("reference", knp_ref=os.environ.get("KNP_REF", "/root/reference"))
+    out = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "cases": []}
+    for name, builder, kwargs, steps, wproj in CASES:
+        net, sched = getattr(N, builder)(**kwargs)
+        res, o = orc.run(net, sched, steps, which="reference")
+        pop = net.populations[0].uid
+        case = {"name": name, "builder": builder, "kwargs": kwargs, "steps": steps,
+                "digest": digest(res[pop]), "events": o.events}
+        if wproj:
+            case["weights_crc"] = {str(k): zlib.crc32(o.weights(net.projections[k].uid).tobytes()) for k in wproj}
+        out["cases"].append(case)
+        print(name, "spikes", sum(s.size for s in res[pop]), "events", o.events)
+    with open(os.path.join(ROOT, "tests", "golden", "spike_digests.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,38 @@
+"""CPU checks of the C ABI library: it builds for sm_103a, loads without a GPU, and exports every
+entry point that include/knp_gb300.h declares (no compute call is made here)."""
+import ctypes
+import subprocess
+
+import pytest
+
+from knp_gb300 import _capi
+from knp_gb300 import build as kb
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    return kb.build()
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    declared = _capi.exported_symbols()
+    assert len(declared) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    lib = ctypes.CDLL(lib_path)
+    for s in declared:
+        assert getattr(lib, s)
+
+
+def test_binding_loads_and_reports_errors_without_gpu(lib_path):
+    lib = _capi.lib()
+    assert b"sm_103a" in lib.knp_gb300_version()
+    # Null handles are rejected before any CUDA call.
+    assert lib.knp_gb300_step(None, 1) == -1
+    assert b"null" in lib.knp_gb300_last_error()
+
+
+def test_library_is_built_for_sm_103a_only():
+    assert kb.GENCODE == ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,138 @@
+"""CPU tests: the oracle against the reference's golden vectors and known answers, the restated
+oracle against the reference-header oracle (where the KNP sources were available to build it), and
+the generators / fixtures that both sides share."""
+import json
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+from knp_gb300 import network as N
+from knp_gb300 import types as T
+from oracle import oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN_DIR = os.path.join(HERE, "golden")
+GOLDEN = [1, 6, 7, 11, 12, 13, 16, 17, 18, 19]
+
+
+def load_golden(name):
+    with open(os.path.join(GOLDEN_DIR, name)) as f:
+        return json.load(f)
+
+
+def spike_digest(trains):
+    """Per-step (count, crc32 of the ascending uint32 indexes)."""
+    return [[int(s.size), zlib.crc32(np.ascontiguousarray(s, np.uint32).tobytes())] for s in trains]
+
+
+@pytest.mark.parametrize("kind", ["delta", "stdp", "stdp_resource_neuron"])
+def test_oracle_smallest_network_golden(oracle_lib, kind):
+    """knp/tests/backend/single_thread_cpu_test.cpp:54-264 expected spike steps."""
+    net, sched = N.smallest_network(kind)
+    out, o = orc.run(net, sched, 20)
+    pop = net.populations[0].uid
+    assert [t for t, s in enumerate(out[pop]) if s.size] == GOLDEN
+    if kind != "delta":
+        assert o.weights(net.projections[1].uid)[0] != 1.0
+
+
+def _run_lif(neuron, steps, impacts=()):
+    """knp/tests/framework/lif_test.cpp:60-100: one LIF neuron, one external impact per step."""
+    pop_uid, in_uid = T.uid_from_int(501), T.uid_from_int(502)
+    pop = N.Population(pop_uid, T.LIF, neuron.copy())
+    net = N.Network([pop], [], [(pop_uid, in_uid)])
+    o = orc.OracleNet("restated")
+    o.load(net)
+    pots, spikes = [], []
+    for t in range(steps):
+        if t < len(impacts):
+            o.send_impacts(in_uid, pop_uid, [0], [impacts[t]], [T.EXCITATORY], True)
+        pots.append(float(o.lif(pop_uid)["potential"][0]))
+        o.step()
+        if o.spikes(pop_uid).size:
+            spikes.append(t)
+    return pots, spikes
+
+
+def test_oracle_lif_known_answers(oracle_lib):
+    """Expected potentials and spike steps of lif_test.cpp:103-177."""
+    n = T.lif_defaults(1)
+    n["activation_threshold"] = 101.0
+    n["leak_coefficient"] = 0.25
+    n["potential"] = 100.0
+    pots, spikes = _run_lif(n, 10)
+    assert pots == [100.0 * 0.25 ** k for k in range(10)] and spikes == []
+    n = T.lif_defaults(1)
+    n["leak_coefficient"] = 0.5
+    n["potential"] = 3.0
+    assert _run_lif(n, 3) == ([3.0, 0.0, 0.0], [0])
+    n = T.lif_defaults(1)
+    n["leak_coefficient"] = 0.5
+    n["activation_threshold"] = 6.0
+    assert _run_lif(n, 6, [5, 5, 2, 3, 8]) == ([0.0, 5.0, 0.0, 2.0, 4.0, 0.0], [1, 4])
+    n["refract_period"] = 2
+    assert _run_lif(n, 7, [5, 5, 10, 10, 5, 5]) == ([0.0, 5.0, 0.0, 0.0, 0.0, 5.0, 0.0], [1, 5])
+
+
+def test_oracle_against_golden_fixtures(oracle_lib):
+    """Spike digests written by tests/golden/make_golden.py from the reference-header oracle."""
+    for case in load_golden("spike_digests.json")["cases"]:
+        net, sched = N.__dict__[case["builder"]](**case["kwargs"])
+        out, o = orc.run(net, sched, case["steps"])
+        pop = net.populations[0].uid
+        assert spike_digest(out[pop]) == case["digest"], case["name"]
+        if "weights_crc" in case:
+            for k, crc in case["weights_crc"].items():
+                w = o.weights(net.projections[int(k)].uid)
+                assert zlib.crc32(w.tobytes()) == crc, (case["name"], k)
+        assert o.events == case["events"], case["name"]
+
+
+@pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
+@pytest.mark.parametrize("seed", [11, 12])
+def test_restated_oracle_matches_reference_headers(oracle_lib, seed):
+    net, sched = N.small_network(seed=seed, n=300, n_in=50, steps=300, p_in=0.1)
+    a, oa = orc.run(net, sched, 300, which="restated")
+    b, ob = orc.run(net, sched, 300, which="reference")
+    pop = net.populations[0].uid
+    assert spike_digest(a[pop]) == spike_digest(b[pop])
+    assert oa.blifat(pop)[0].tobytes() == ob.blifat(pop)[0].tobytes()
+    assert oa.events == ob.events
+
+
+@pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
+def test_restated_oracle_matches_reference_headers_stdp(oracle_lib):
+    net, sched = N.stdp_network(seed=3, n_in=100, n=60, samples=6, steps_per_sample=50)
+    a, oa = orc.run(net, sched, 300, which="restated")
+    b, ob = orc.run(net, sched, 300, which="reference")
+    pop = net.populations[0].uid
+    assert spike_digest(a[pop]) == spike_digest(b[pop])
+    for pr in net.projections:
+        assert oa.weights(pr.uid).tobytes() == ob.weights(pr.uid).tobytes()
+    sa, ea = oa.blifat(pop)
+    sb, eb = ob.blifat(pop)
+    assert sa.tobytes() == sb.tobytes() and ea.tobytes() == eb.tobytes()
+
+
+def test_generator_is_counter_based():
+    """Any slice of a generated projection equals the same slice of the whole."""
+    k = [N.stream_key(4, s) for s in (1, 2, 3)]
+    full = N.fixed_fan_in_pre(*k, 500, 500, 10, -16, 48, 1, 20)
+    part = N.fixed_fan_in_pre(*k, 500, 500, 10, -16, 48, 1, 20, start=1234, count=100)
+    for a, b in zip(full, part):
+        np.testing.assert_array_equal(a[1234:1334], b)
+    pre, post, w, d = full
+    assert pre.max() < 500 and d.min() >= 1 and d.max() <= 20
+    assert np.all((w * 256) == np.round(w * 256)) and w.min() >= -16 / 256 and w.max() <= 48 / 256
+    np.testing.assert_array_equal(post, np.arange(5000) % 500)
+
+
+def test_struct_layouts():
+    assert T.BLIFAT_DTYPE.itemsize == 192
+    assert T.RESOURCE_DTYPE.itemsize == 72
+    assert T.LIF_DTYPE.itemsize == 24
+    d = T.blifat_defaults(2)
+    assert d["n_time_steps_since_last_firing"][0] == np.iinfo(np.uint64).max
+    assert d["total_blocking_period"][0] == np.iinfo(np.int64).max
