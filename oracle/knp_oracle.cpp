@@ -23,12 +23,17 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
 #include <limits>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <unordered_set>
 #include <vector>
@@ -139,10 +144,73 @@ struct Projection
     }
 };
 
+// Fixed-size worker pool with post/join, standing in for the reference's Boost.Asio thread pool
+// (knp/backends/cpu/thread_pool/include/knp/backends/thread_pool/thread_pool.h:36-77).
+class ThreadPool
+{
+public:
+    explicit ThreadPool(int n)
+    {
+        for (int i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
+    }
+    ~ThreadPool()
+    {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &w : workers_) w.join();
+    }
+    void post(std::function<void()> f)
+    {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            q_.push_back(std::move(f));
+            ++pending_;
+        }
+        cv_.notify_one();
+    }
+    void join()
+    {
+        std::unique_lock<std::mutex> l(m_);
+        done_.wait(l, [this] { return pending_ == 0; });
+    }
+    int size() const { return static_cast<int>(workers_.size()); }
+
+private:
+    void loop()
+    {
+        for (;;)
+        {
+            std::function<void()> f;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [this] { return stop_ || !q_.empty(); });
+                if (stop_ && q_.empty()) return;
+                f = std::move(q_.front());
+                q_.pop_front();
+            }
+            f();
+            {
+                std::lock_guard<std::mutex> l(m_);
+                if (--pending_ == 0) done_.notify_all();
+            }
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::deque<std::function<void()>> q_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    size_t pending_ = 0;
+    bool stop_ = false;
+};
+
 }  // namespace
 
 struct or_net
 {
+    std::unique_ptr<ThreadPool> pool;
     std::vector<std::unique_ptr<Population>> pops;
     std::vector<std::unique_ptr<Projection>> projs;
     std::vector<std::pair<Uid, Uid>> extra_subs;  // receiver, sender
@@ -702,6 +770,168 @@ int or_step(or_net *net)
                 if (calculate_projection(*net, *p, step, m)) out.push_back(std::move(m));
             }
             for (auto &m : out)  // Route #3: delivered to populations for the next step.
+                for (auto &q : net->pops)
+                    if (q->impact_senders.count(m.sender)) q->inbox.push_back(m);
+            ++net->step;
+            return 0;
+        });
+}
+
+// MultiThreadedCPUBackend::_step (knp/backends/cpu/cpu-multi-threaded-backend/impl/backend.cpp:310-323),
+// restated for timing the reference's multi-threaded CPU path: populations in parts of 1000 neurons
+// (:77-200), one impact task per population (:101-118); every delta projection scans all of its
+// synapses in parts of 1000 against the neuron->count map of its FIRST spike message only (:250-295,
+// delta_impl.h:117-175) and merges impacts (weight x count) under one mutex. The MT backend has no
+// additive STDP, and its spike order within a step is not deterministic.
+int or_step_mt(or_net *net, int threads)
+{
+    return guarded(
+        [&]
+        {
+            if (!net->initialized) throw std::runtime_error("or_init was not called");
+            if (threads < 1) threads = 1;
+            if (!net->pool || net->pool->size() != threads) net->pool = std::make_unique<ThreadPool>(threads);
+            ThreadPool &pool = *net->pool;
+            const uint64_t step = net->step;
+            const size_t part = 1000;
+            std::mutex merge;
+            for (auto &m : net->ext_spikes)
+                for (auto &p : net->projs)
+                    if (p->spike_senders.count(m.sender)) p->inbox.push_back(m);
+            for (auto &m : net->ext_impacts)
+                for (auto &q : net->pops)
+                    if (q->impact_senders.count(m.sender)) q->inbox.push_back(m);
+            net->ext_spikes.clear();
+            net->ext_impacts.clear();
+            std::vector<std::vector<ImpactMessage>> msgs(net->pops.size());
+            for (size_t k = 0; k < net->pops.size(); ++k)
+            {
+                Population &q = *net->pops[k];
+                msgs[k] = std::move(q.inbox);
+                q.inbox.clear();
+                q.last_spikes.clear();
+                check_impacts(q, msgs[k]);
+                const size_t n = q.size();
+                for (size_t a = 0; a < n; a += part)
+                    pool.post(
+                        [&q, a, n, part]
+                        {
+                            const size_t b = std::min(a + part, n);
+                            for (size_t i = a; i < b; ++i)
+                            {
+                                if (q.kind == KNP_NEURON_LIF)
+                                    lif_pre_impact(q.lif[i]);
+                                else if (q.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT)
+                                    resource_blifat_pre_impact(q.blifat[i], q.res[i]);
+                                else
+                                    blifat_pre_impact(q.blifat[i]);
+                            }
+                        });
+            }
+            pool.join();
+            for (size_t k = 0; k < net->pops.size(); ++k)
+                pool.post(
+                    [&, k]
+                    {
+                        Population &q = *net->pops[k];
+                        for (auto &m : msgs[k])
+                            for (auto &imp : m.impacts)
+                            {
+                                if (q.kind == KNP_NEURON_LIF)
+                                {
+                                    lif_impact(q.lif[imp.post], imp);
+                                    continue;
+                                }
+                                blifat_impact(q.blifat[imp.post], imp);
+                                if (q.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT && imp.type == KNP_OUT_EXCITATORY)
+                                    q.res[imp.post].is_being_forced |= m.is_forcing ? 1u : 0u;
+                            }
+                    });
+            pool.join();
+            for (auto &qp : net->pops)
+            {
+                Population &q = *qp;
+                const size_t n = q.size();
+                for (size_t a = 0; a < n; a += part)
+                    pool.post(
+                        [&q, a, n, part, &merge]
+                        {
+                            std::vector<uint32_t> local;
+                            const size_t b = std::min(a + part, n);
+                            for (size_t i = a; i < b; ++i)
+                            {
+                                const bool s = q.kind == KNP_NEURON_LIF ? lif_post_impact(q.lif[i])
+                                                                        : blifat_post_impact(q.blifat[i]);
+                                if (s) local.push_back(static_cast<uint32_t>(i));
+                            }
+                            std::lock_guard<std::mutex> l(merge);
+                            q.last_spikes.insert(q.last_spikes.end(), local.begin(), local.end());
+                        });
+            }
+            pool.join();
+            std::vector<SpikeMessage> sent;
+            for (auto &q : net->pops)
+            {
+                if (q->kind == KNP_NEURON_RESOURCE_STDP_BLIFAT) train_resource_population(*q, q->last_spikes, step);
+                if (!q->last_spikes.empty()) sent.push_back(SpikeMessage{q->uid, step, q->last_spikes});
+            }
+            for (auto &m : sent)
+                for (auto &p : net->projs)
+                    if (p->spike_senders.count(m.sender)) p->inbox.push_back(m);
+            std::vector<std::unordered_map<uint64_t, size_t>> converted;
+            converted.reserve(net->projs.size());
+            std::vector<uint64_t> events(net->projs.size(), 0);
+            for (size_t k = 0; k < net->projs.size(); ++k)
+            {
+                Projection &p = *net->projs[k];
+                std::vector<SpikeMessage> in = std::move(p.inbox);
+                p.inbox.clear();
+                if (in.empty()) continue;
+                converted.emplace_back();
+                auto &counts = converted.back();
+                for (uint32_t i : in[0].idx) ++counts[i];
+                const size_t S = p.syn.size();
+                for (size_t a = 0; a < S; a += part)
+                    pool.post(
+                        [&p, &counts, &merge, &events, k, a, S, part, step]
+                        {
+                            std::vector<std::pair<uint64_t, Impact>> container;
+                            const size_t b = std::min(a + part, S);
+                            for (size_t si = a; si < b; ++si)
+                            {
+                                const Synapse &s = p.syn[si];
+                                auto it = counts.find(s.pre);
+                                if (it == counts.end()) continue;
+                                container.emplace_back(s.delay + step - 1,
+                                                       Impact{si, s.weight * static_cast<float>(it->second), s.type,
+                                                              s.pre, s.post});
+                            }
+                            std::lock_guard<std::mutex> l(merge);
+                            events[k] += container.size();
+                            for (auto &[key, imp] : container)
+                            {
+                                auto f = p.future.find(key);
+                                if (f != p.future.end())
+                                    f->second.impacts.push_back(imp);
+                                else
+                                    p.future.emplace(key, ImpactMessage{p.uid, step, p.post_uid, p.pre_uid, true, {imp}});
+                            }
+                        });
+            }
+            pool.join();
+            std::vector<ImpactMessage> out;
+            for (size_t k = 0; k < net->projs.size(); ++k)
+            {
+                Projection &p = *net->projs[k];
+                net->events += events[k];
+                auto it = p.future.find(step);
+                if (it != p.future.end())
+                {
+                    out.push_back(std::move(it->second));
+                    p.future.erase(it);
+                }
+            }
+            for (auto &m : out)
                 for (auto &q : net->pops)
                     if (q->impact_senders.count(m.sender)) q->inbox.push_back(m);
             ++net->step;

@@ -67,6 +67,13 @@ int or_send_impacts(
 
 /** One backend step. */
 int or_step(or_net *net);
+
+/**
+ * One step of the reference's multi-threaded CPU backend structure on `threads` workers (for timing
+ * the reference's multi-threaded path; its semantics differ from the single-threaded oracle: only
+ * the first spike message per projection per step, impacts = weight x spike count, no additive STDP).
+ */
+int or_step_mt(or_net *net, int threads);
 uint64_t or_get_step(const or_net *net);
 
 /** Spike indexes a population emitted in the last step (ascending), count in *n. */

@@ -74,6 +74,8 @@ def _load(which: str):
             "or_read_weights": ([p, U, p], ctypes.c_int),
             "or_event_count": ([p], ctypes.c_uint64),
         }
+        if which == "restated":
+            sig["or_step_mt"] = ([p, ctypes.c_int], ctypes.c_int)
         for name, (args, res) in sig.items():
             f = getattr(lib, name)
             f.argtypes = args
@@ -156,6 +158,10 @@ class OracleNet:
 
     def step(self):
         self._chk(self.lib.or_step(self.h))
+
+    def step_mt(self, threads: int):
+        """One step with the reference multi-threaded backend's structure (timing only)."""
+        self._chk(self.lib.or_step_mt(self.h, threads))
 
     @property
     def step_count(self) -> int:
