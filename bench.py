@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--profile-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
+    ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -194,10 +196,11 @@ def main():
 
     b = B.GB300Backend(local)
     t_build = time.perf_counter()
-    pop_uid, chan_uid = build_large(b)
+    n_neurons = args.neurons
+    pop_uid, chan_uid = build_large(b, n=n_neurons, fan_in=args.fan_in)
     b._init()
     total_steps = args.warmup + args.steps + args.profile_steps
-    b.generate_bernoulli_schedule(chan_uid, N, P_BG, 0, total_steps, seed=SEED + 1000 * rank)
+    b.generate_bernoulli_schedule(chan_uid, n_neurons, P_BG, 0, total_steps, seed=SEED + 1000 * rank)
     t_build = time.perf_counter() - t_build
 
     b.step(args.warmup)
@@ -225,6 +228,7 @@ def main():
     value = events_all / t
 
     # Live per-phase timing of the same steps (kernels launched one by one, CUDA events between phases).
+    args.profile_steps = max(args.profile_steps, 1)
     e0, s0, _ = b.counters()
     ph = b.profile_phases(args.profile_steps)
     e1, s1, _ = b.counters()
@@ -235,9 +239,9 @@ def main():
     pop_ms = ph[0] / args.profile_steps
     # Spike rows walked per step: population spikes through the recurrent projection + background
     # spikes through the one-to-one projection (each a row_ptr pair).
-    bg_per_step = P_BG * N
+    bg_per_step = P_BG * n_neurons
     proj_bytes = 9.0 * p_events + 8.0 * (p_spikes + bg_per_step)
-    pop_bytes = 32.0 * N
+    pop_bytes = 32.0 * n_neurons
     dominant = "projection" if proj_ms >= pop_ms else "population"
     a_bytes, a_ms = (proj_bytes, proj_ms) if dominant == "projection" else (pop_bytes, pop_ms)
     achieved = a_bytes / (a_ms / 1e3) / 1e9
@@ -252,7 +256,7 @@ def main():
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
         start = b.get_step()
-        sched = Nw.bernoulli_schedule(chan_uid, SEED + 7, N, args.e2e_steps, P_BG, step0=start)
+        sched = Nw.bernoulli_schedule(chan_uid, SEED + 7, n_neurons, args.e2e_steps, P_BG, step0=start)
         b.record_spikes(pop_uid, True)
         b.synchronize()
         ea, _, _ = b.counters()
@@ -282,12 +286,13 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded counter-based generator)",
-            "config": {"workload": "large_sparse_plain", "neurons": N, "fan_in": FAN_IN, "synapses": N * FAN_IN,
+            "config": {"workload": "large_sparse_plain", "neurons": n_neurons, "fan_in": args.fan_in,
+                       "synapses": n_neurons * args.fan_in,
                        "delays": "1..20", "weights": "k/256, k in [-16,48]", "p_background": P_BG,
                        "l2": "inputs larger than L2 (9 GB synapse arrays), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "neuron_updates_per_s": N * world * args.steps / t,
-            "firing_rate": spikes / (N * args.steps),
+            "neuron_updates_per_s": n_neurons * world * args.steps / t,
+            "firing_rate": spikes / (n_neurons * args.steps),
             "events_per_step": events / args.steps,
             "roofline": roofline,
             "cpu_baseline": cpu,
