@@ -149,16 +149,45 @@ def cpu_baseline_sample(target_s: float = 15.0):
                       f"{o.events} events, {dt:.1f} s, restated single-threaded backend step"}
 
 
+def reference_mt_sample(target_s: float = 30.0):
+    """The reference multi-threaded CPU backend's step structure (restated in the oracle library:
+    1000-neuron parts, O(S) synapse scan per step in 1000-synapse parts) on all host threads, on
+    the large sparse config at 1/100 scale: events/s of its step loop."""
+    from knp_gb300 import network as Nw
+    from oracle import oracle as orc
+
+    n = 10_000
+    steps = 200
+    threads = os.cpu_count() or 1
+    net, sched = Nw.large_sparse_network(seed=SEED, n=n, fan_in=FAN_IN, steps=steps)
+    o = orc.OracleNet("restated")
+    o.load(net)
+    t0 = time.perf_counter()
+    done = 0
+    for t in range(steps):
+        idx = sched[0].at(t)
+        if idx.size:
+            o.send_spikes(sched[0].sender, idx, t)
+        o.step_mt(threads)
+        done += 1
+        if time.perf_counter() - t0 > target_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": o.events / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"large sparse config at 1/100 scale ({n} neurons, fan-in {FAN_IN}), {done} steps, "
+                      f"{o.events} events, {dt:.1f} s, restated multi-threaded backend step on {threads} threads"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = cpu_baseline_sample(target_s=max(5.0, min(60.0, 2.0 * args.steps)))
+    cb = reference_mt_sample(target_s=max(5.0, min(60.0, 0.5 * args.steps)))
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
-            "config": {"workload": "large_sparse_plain at 1/100 scale on the host CPU",
-                       "neurons": 10_000, "fan_in": FAN_IN, "p_background": P_BG},
+            "config": {"workload": "large_sparse_plain at 1/100 scale on the host CPU (reference multi-threaded "
+                                   "backend structure)", "neurons": 10_000, "fan_in": FAN_IN, "p_background": P_BG},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -175,6 +204,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
+    ap.add_argument("--pull-threshold", type=float, default=0.1,
+                    help="spike share above which a step is gathered instead of scattered (-1: scatter only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -198,6 +229,9 @@ def main():
     t_build = time.perf_counter()
     n_neurons = args.neurons
     pop_uid, chan_uid = build_large(b, n=n_neurons, fan_in=args.fan_in)
+    from knp_gb300 import types as T
+
+    b.set_pull_threshold(T.uid_from_int(SEED * 100 + 2), args.pull_threshold)
     b._init()
     total_steps = args.warmup + args.steps + args.profile_steps
     b.generate_bernoulli_schedule(chan_uid, n_neurons, P_BG, 0, total_steps, seed=SEED + 1000 * rank)
@@ -290,7 +324,8 @@ def main():
                        "synapses": n_neurons * args.fan_in,
                        "delays": "1..20", "weights": "k/256, k in [-16,48]", "p_background": P_BG,
                        "l2": "inputs larger than L2 (9 GB synapse arrays), no flush",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "pull_threshold": args.pull_threshold},
             "neuron_updates_per_s": n_neurons * world * args.steps / t,
             "firing_rate": spikes / (n_neurons * args.steps),
             "events_per_step": events / args.steps,

@@ -83,6 +83,17 @@ KNP_GB300_API int knp_gb300_load_blifat_population(
     const knp_resource_stdp_state *ext);
 
 /**
+ * Load a LIF population (reference semantics of lif_impl.h:33-86: leak and impacts only outside the
+ * refractory period, spike iff potential > threshold, reset to a value). Used by the batched form
+ * and its FP32 comparison path. Replaces: load_populations for Population<LIFNeuron>
+ * (cpu-single-threaded-backend/impl/backend.cpp:255-260).
+ */
+KNP_GB300_API int knp_gb300_load_lif_population(knp_gb300_backend *b, knp_uid uid, uint32_t n, const knp_lif_neuron *neurons);
+
+/** Read back a LIF population's neurons. Replaces: get_network_data population range for LIF. */
+KNP_GB300_API int knp_gb300_read_lif_population(knp_gb300_backend *b, knp_uid pop, knp_lif_neuron *out);
+
+/**
  * Load a projection of `n_syn` synapses given in the reference's synapse order: synapse i is
  * (weight[i], delay[i], out_type[i]) from presynaptic neuron pre[i] to postsynaptic neuron post[i].
  * kind: KNP_SYNAPSE_DELTA or KNP_SYNAPSE_ADDITIVE_STDP_DELTA (tau_plus/tau_minus required, uniform
@@ -125,6 +136,16 @@ KNP_GB300_API int knp_gb300_subscribe(knp_gb300_backend *b, knp_uid receiver, kn
 
 /** Force the accumulator mode of a population (before init). */
 KNP_GB300_API int knp_gb300_set_accumulator(knp_gb300_backend *b, knp_uid pop_uid, int mode);
+
+/**
+ * Direction choice of a delta projection: a step in which at least `fraction` x (presynaptic
+ * neurons) spike is delivered by the gather kernel (synapses sorted by delay and target, no global
+ * atomics) instead of the scatter kernel; results are identical. Default 0.1; a negative fraction
+ * keeps every step on the scatter path. The gather form is built at init for delta projections of
+ * at least 2^20 synapses fed by one population into an FP32 input ring. No reference counterpart:
+ * the reference's delivery loop (delta_impl.h:65-107) is a scatter only.
+ */
+KNP_GB300_API int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid proj_uid, double fraction);
 
 /**
  * Enable or disable per-step spike recording of a population (SpikeMessages that an output
@@ -237,6 +258,53 @@ KNP_GB300_API int knp_gb300_step_timed(knp_gb300_backend *b, uint64_t n_steps, f
  * kernels, the STDP kernels and the end-of-step kernel. Results equal knp_gb300_step's.
  */
 KNP_GB300_API int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms);
+
+/*
+ * Differentiation form (no reference counterpart: KNP has no gradient-based training). LIF layer
+ * recurrence over T steps for BN = batch x neurons independent neurons, device buffers laid out
+ * [T][BN] (I, S, dS, dI) and [ceil(T/K)][BN] (ckpt):
+ *   U_t = beta V_{t-1} + I_t,  S_t = H(U_t - theta) (strict '>'),  V_t = U_t - theta S_t,  V_{-1} = 0.
+ * The forward stores the membrane state entering every K-th step (K <= 16); the backward recomputes
+ * each K-step segment from its checkpoint and returns dI = dL/dI from dS = dL/dS using the
+ * fast-sigmoid surrogate dS/dU = (k/2) / (1 + k|U - theta|)^2. relaxed != 0 replaces H by the
+ * fast sigmoid (1 + kx/(1+k|x|))/2 in the forward, whose exact derivative the backward then is.
+ * `stream` is a cudaStream_t (NULL: legacy default stream). Launches only; returns before completion.
+ */
+KNP_GB300_API int knp_gb300_lif_scan_forward(
+    const float *I, float *S, float *ckpt, int T, int64_t BN, float beta, float theta, int K, int relaxed, float k,
+    void *stream);
+KNP_GB300_API int knp_gb300_lif_scan_backward(
+    const float *I, const float *ckpt, const float *dS, float *dI, int T, int64_t BN, float beta, float theta, int K,
+    int relaxed, float k, void *stream);
+
+/*
+ * Batched / precision form (no reference counterpart). D[M x N] (FP32, row-major) = A[M x K] *
+ * B[N x K]^T with BF16 operands (row-major, K contiguous, device memory) on the tcgen05 tensor
+ * cores, accumulator in tensor memory. *d_err (device) receives bit 0 if a completion wait timed
+ * out. Launch only.
+ */
+KNP_GB300_API int knp_gb300_bf16_gemm_tn(
+    const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, void *stream);
+
+/*
+ * Batched / precision form (no reference counterpart: the reference steps one network at a time).
+ * `batch` independent samples of a feed-forward LIF network with n_layers all-to-all delay-1
+ * layers (sizes[0] inputs -> sizes[1] -> ... -> sizes[n_layers], each <= 4096; reference LIF
+ * semantics lif_impl.h:33-86 with per-layer leak / threshold / reset / refractory period, NULL =
+ * reference defaults 1, 1, 0, 0) run in one persistent cooperative kernel on the tcgen05 tensor cores:
+ * every step each layer's input is the previous layer's 0/1 spike matrix (BF16, exact) times its BF16
+ * weights (device, d_weights[l] = [sizes[l + 1]][sizes[l]] row-major) with FP32 accumulation in tensor
+ * memory. Sample b runs steps[b] (host array) steps; its input i spikes at step t iff
+ * rand64(stream_key(seed, 5), (t * batch + b) * sizes[0] + i) >> 11 < d_rates[b][i] * 2^53 (the
+ * generator of knp_gb300/network.py). Outputs: d_counts[batch][sizes[n_layers]] (device, int32) output
+ * spike counts; optional d_record (device, uint32) with every layer's spike bitmap of every step,
+ * laid out [max(steps)][layer 0..n_layers][batch][ceil(sizes[l] / 32)]; *events (host) synaptic events
+ * (spikes x fan-out of their layer); *ms (host) device time of the run. Synchronous.
+ */
+KNP_GB300_API int knp_gb300_batched_lif_run(
+    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *d_rates,
+    uint64_t seed, int32_t *d_counts, uint32_t *d_record, uint64_t *events, float *ms, void *stream);
 
 /** Block until all queued device work of the backend has finished. */
 KNP_GB300_API int knp_gb300_synchronize(knp_gb300_backend *b);

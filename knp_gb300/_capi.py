@@ -46,12 +46,15 @@ def lib():
         "knp_gb300_create": ([c_int, ctypes.POINTER(p)], c_int),
         "knp_gb300_destroy": ([p], c_int),
         "knp_gb300_load_blifat_population": ([p, U, c_int, u32, p, p], c_int),
+        "knp_gb300_load_lif_population": ([p, U, u32, p], c_int),
+        "knp_gb300_read_lif_population": ([p, U, p], c_int),
         "knp_gb300_load_projection": ([p, U, c_int, U, U, u64, p, p, p, p, p, p, p], c_int),
         "knp_gb300_generate_fixed_fan_in_projection": ([p, U, U, U, u32, u32, u32, i32, i32, u32, u32, u64, u64], c_int),
         "knp_gb300_set_stdp_population": ([p, U, U, c_int], c_int),
         "knp_gb300_subscribe": ([p, U, U], c_int),
         "knp_gb300_set_accumulator": ([p, U, c_int], c_int),
         "knp_gb300_record_spikes": ([p, U, c_int], c_int),
+        "knp_gb300_set_pull_threshold": ([p, U, ctypes.c_double], c_int),
         "knp_gb300_init": ([p], c_int),
         "knp_gb300_send_spikes": ([p, U, u64, u32, p], c_int),
         "knp_gb300_load_spike_schedule": ([p, U, u64, u64, p, p], c_int),
@@ -69,6 +72,13 @@ def lib():
         "knp_gb300_counters": ([p, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64)], c_int),
         "knp_gb300_step_timed": ([p, u64, ctypes.POINTER(ctypes.c_float)], c_int),
         "knp_gb300_profile_phases": ([p, u64, ctypes.POINTER(ctypes.c_float)], c_int),
+        "knp_gb300_lif_scan_forward": ([p, p, p, c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_int, c_int,
+                                        ctypes.c_float, p], c_int),
+        "knp_gb300_lif_scan_backward": ([p, p, p, p, c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_int,
+                                         c_int, ctypes.c_float, p], c_int),
+        "knp_gb300_bf16_gemm_tn": ([p, p, p, c_int, c_int, c_int, p, p], c_int),
+        "knp_gb300_batched_lif_run": ([c_int, p, p, p, p, p, p, u32, p, p, u64, p, p, ctypes.POINTER(u64),
+                                       ctypes.POINTER(ctypes.c_float), p], c_int),
         "knp_gb300_synchronize": ([p], c_int),
         "knp_gb300_stream": ([p, ctypes.POINTER(p)], c_int),
     }

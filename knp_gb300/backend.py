@@ -24,7 +24,7 @@ from . import _capi
 from . import network as N
 from . import types as T
 
-SUPPORTED_NEURONS = ["BLIFATNeuron", "SynapticResourceSTDPBLIFATNeuron"]
+SUPPORTED_NEURONS = ["BLIFATNeuron", "SynapticResourceSTDPBLIFATNeuron", "LIFNeuron"]
 SUPPORTED_SYNAPSES = ["DeltaSynapse", "AdditiveSTDPDeltaSynapse"]
 
 
@@ -81,6 +81,12 @@ class GB300Backend:
     # ------------------------------------------------------------------ loading (backend.h:137-160)
     def load_populations(self, populations):
         for pop in populations:
+            if pop.kind == T.LIF:
+                neurons = np.ascontiguousarray(pop.neurons, dtype=T.LIF_DTYPE)
+                self._chk(self._lib.knp_gb300_load_lif_population(self._h, T.to_c_uid(pop.uid), pop.size,
+                                                                  _ptr(neurons)))
+                self._pops[pop.uid] = pop
+                continue
             if pop.kind not in (T.BLIFAT, T.RESOURCE_STDP_BLIFAT):
                 raise TypeError("Type is not supported.")
             neurons = np.ascontiguousarray(pop.neurons, dtype=T.BLIFAT_DTYPE)
@@ -131,6 +137,11 @@ class GB300Backend:
 
     def set_accumulator(self, pop_uid: bytes, mode: int):
         self._chk(self._lib.knp_gb300_set_accumulator(self._h, T.to_c_uid(pop_uid), mode))
+
+    def set_pull_threshold(self, proj_uid: bytes, fraction: float):
+        """Spike share above which a step of this projection is gathered instead of scattered
+        (negative: always scatter)."""
+        self._chk(self._lib.knp_gb300_set_pull_threshold(self._h, T.to_c_uid(proj_uid), float(fraction)))
 
     def record_spikes(self, pop_uid: bytes, enable: bool = True):
         self._chk(self._lib.knp_gb300_record_spikes(self._h, T.to_c_uid(pop_uid), int(enable)))
@@ -254,6 +265,11 @@ class GB300Backend:
         self._chk(self._lib.knp_gb300_read_blifat_population(self._h, T.to_c_uid(uid), _ptr(out), _ptr(ext)))
         return out, ext
 
+    def read_lif(self, uid: bytes) -> np.ndarray:
+        out = np.empty(self._pops[uid].size, T.LIF_DTYPE)
+        self._chk(self._lib.knp_gb300_read_lif_population(self._h, T.to_c_uid(uid), _ptr(out)))
+        return out
+
     def read_weights(self, uid: bytes) -> np.ndarray:
         n = ctypes.c_uint64(0)
         self._chk(self._lib.knp_gb300_projection_size(self._h, T.to_c_uid(uid), ctypes.byref(n)))
@@ -266,6 +282,9 @@ class GB300Backend:
         weights (get_network.cpp:80-93)."""
         pops, projs = [], []
         for uid, pop in self._pops.items():
+            if pop.kind == T.LIF:
+                pops.append(N.Population(uid, pop.kind, self.read_lif(uid)))
+                continue
             neurons, ext = self.read_population(uid)
             pops.append(N.Population(uid, pop.kind, neurons, ext))
         for uid, pr in self._projs.items():

@@ -1,0 +1,154 @@
+"""Batched / precision form: many independent LIF network samples on the tcgen05 tensor cores.
+
+``run`` drives ``knp_gb300_batched_lif_run`` (knp_gb300/csrc/batched.cu): B samples of a
+feed-forward LIF network with all-to-all delay-1 layers, uneven lengths T_b, Bernoulli inputs with
+per-(sample, input) rates, BF16 weights (FP32 master values rounded to BF16), FP32 accumulation.
+``plain_network`` builds the same computation as one block-diagonal network for the plain backend
+(FP32 input rings, the same BF16-valued weights), which is what the batched form is compared with.
+The reference has no batched execution; these forms have no counterpart there.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi
+from . import network as N
+from . import types as T
+
+
+@dataclass
+class BatchedConfig:
+    sizes: tuple
+    weights: list  # float32 arrays [n_out, n_in], BF16-representable values
+    rates: np.ndarray  # float32 [B, n_0]
+    steps: np.ndarray  # uint32 [B]
+    seed: int
+    leak: tuple = None
+    threshold: tuple = None
+    reset: tuple = None
+    refract: tuple = None
+
+    @property
+    def batch(self) -> int:
+        return int(self.steps.shape[0])
+
+
+def bf16_round(x: np.ndarray) -> np.ndarray:
+    """Round FP32 values to the nearest BF16 (ties to even), returned as FP32."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def dense_config(seed: int = 4, batch: int = 256, sizes=(784, 1000, 1000, 10), t_lo: int = 50, t_hi: int = 200,
+                 rate_max: float = 0.2) -> BatchedConfig:
+    """Batched dense config: weights N(0, 1/fan_in) rounded to BF16, threshold 1, per-input rates
+    uniform in [0, rate_max], per-sample lengths uniform in [t_lo, t_hi]."""
+    rng = np.random.default_rng(seed)
+    ws = [bf16_round(rng.normal(0.0, 1.0 / np.sqrt(a), size=(b, a)).astype(np.float32))
+          for a, b in zip(sizes[:-1], sizes[1:])]
+    rates = (rng.random((batch, sizes[0])) * rate_max).astype(np.float32)
+    steps = rng.integers(t_lo, t_hi + 1, size=batch).astype(np.uint32)
+    return BatchedConfig(tuple(sizes), ws, rates, steps, seed)
+
+
+def input_spikes(cfg: BatchedConfig, b: int, t: int) -> np.ndarray:
+    """Input indexes of sample b at step t: the counter-based draw the kernel makes."""
+    n0 = cfg.sizes[0]
+    key = N.stream_key(cfg.seed, N.S_INPUT)
+    ctr = (np.uint64(t) * np.uint64(cfg.batch) + np.uint64(b)) * np.uint64(n0) + np.arange(n0, dtype=np.uint64)
+    thr = (cfg.rates[b].astype(np.float64) * float(1 << 53)).astype(np.uint64)
+    return np.nonzero((N.rand64(key, ctr) >> np.uint64(11)) < thr)[0].astype(np.uint32)
+
+
+def run(cfg: BatchedConfig, record: bool = False, device: int = 0):
+    """Run the batch on the GPU. Returns (counts [B, n_L], record or None, events, ms). With
+    ``record`` the per-step spike bitmaps of every layer come back as a dict
+    {layer: uint32 [T_max, B, words]}."""
+    import torch
+
+    dev = torch.device(f"cuda:{device}")
+    L = len(cfg.sizes) - 1
+    wts = [torch.from_numpy(np.ascontiguousarray(w)).to(dev).to(torch.bfloat16).contiguous() for w in cfg.weights]
+    rates = torch.from_numpy(np.ascontiguousarray(cfg.rates, np.float32)).to(dev)
+    counts = torch.zeros((cfg.batch, cfg.sizes[-1]), dtype=torch.int32, device=dev)
+    words = [(n + 31) // 32 for n in cfg.sizes]
+    t_max = int(cfg.steps.max())
+    stride = sum(cfg.batch * w for w in words)
+    rec = torch.zeros(t_max * stride, dtype=torch.int32, device=dev) if record else None
+    sizes = (ctypes.c_uint32 * (L + 1))(*cfg.sizes)
+    wptr = (ctypes.c_void_p * L)(*[w.data_ptr() for w in wts])
+
+    def fl(v, default):
+        return (ctypes.c_float * L)(*(v if v is not None else [default] * L))
+
+    refract = (ctypes.c_uint32 * L)(*(cfg.refract if cfg.refract is not None else [0] * L))
+    steps = (ctypes.c_uint32 * cfg.batch)(*[int(x) for x in cfg.steps])
+    events = ctypes.c_uint64(0)
+    ms = ctypes.c_float(0)
+    lib = _capi.lib()
+    _capi.check(lib.knp_gb300_batched_lif_run(
+        L, sizes, wptr, fl(cfg.leak, 1.0), fl(cfg.threshold, 1.0), fl(cfg.reset, 0.0), refract, cfg.batch, steps,
+        ctypes.c_void_p(rates.data_ptr()), cfg.seed, ctypes.c_void_p(counts.data_ptr()),
+        ctypes.c_void_p(rec.data_ptr()) if rec is not None else None, ctypes.byref(events), ctypes.byref(ms),
+        ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    out_rec = None
+    if rec is not None:
+        r = rec.cpu().numpy().view(np.uint32).reshape(t_max, stride)
+        out_rec, off = {}, 0
+        for layer, w in enumerate(words):
+            out_rec[layer] = r[:, off:off + cfg.batch * w].reshape(t_max, cfg.batch, w)
+            off += cfg.batch * w
+    return counts.cpu().numpy(), out_rec, int(events.value), float(ms.value)
+
+
+def spikes_from_bits(words_row: np.ndarray, n: int) -> np.ndarray:
+    """Ascending indexes of the set bits of one bitmap row."""
+    bits = np.unpackbits(words_row.astype("<u4").view(np.uint8), bitorder="little")[:n]
+    return np.nonzero(bits)[0].astype(np.uint32)
+
+
+def plain_network(cfg: BatchedConfig, samples=None):
+    """The same samples as one block-diagonal network for the plain backend (LIF populations,
+    delay-1 projections with the same weights as FP32, inputs as one external channel). Sample s of
+    the selection occupies neurons [s * n_l, (s + 1) * n_l) of layer l. Returns (network, schedule)."""
+    samples = list(range(cfg.batch)) if samples is None else list(samples)
+    S = len(samples)
+    L = len(cfg.sizes) - 1
+    pops = []
+    for l in range(1, L + 1):
+        a = T.lif_defaults(S * cfg.sizes[l])
+        if cfg.leak is not None:
+            a["leak_coefficient"] = cfg.leak[l - 1]
+        if cfg.threshold is not None:
+            a["activation_threshold"] = cfg.threshold[l - 1]
+        if cfg.reset is not None:
+            a["potential_reset_value"] = cfg.reset[l - 1]
+        if cfg.refract is not None:
+            a["refract_period"] = cfg.refract[l - 1]
+        pops.append(N.Population(T.uid_from_int(800 + l), T.LIF, a))
+    chan = T.uid_from_int(899)
+    projs = []
+    for l in range(1, L + 1):
+        n_in, n_out = cfg.sizes[l - 1], cfg.sizes[l]
+        w = cfg.weights[l - 1]  # [n_out, n_in]
+        jj, ii = np.meshgrid(np.arange(n_out, dtype=np.uint32), np.arange(n_in, dtype=np.uint32), indexing="ij")
+        pre = np.concatenate([s * n_in + ii.ravel() for s in range(S)]).astype(np.uint32)
+        post = np.concatenate([s * n_out + jj.ravel() for s in range(S)]).astype(np.uint32)
+        wt = np.tile(w.ravel(), S).astype(np.float32)
+        pre_uid = T.NULL_UID if l == 1 else pops[l - 2].uid
+        projs.append(N.Projection(T.uid_from_int(850 + l), T.DELTA, pre_uid, pops[l - 1].uid, pre, post, wt,
+                                  np.ones(pre.size, np.uint32)))
+    net = N.Network(pops, projs, [(projs[0].uid, chan)])
+    t_max = int(cfg.steps[samples].max())
+    offs = np.zeros(t_max + 1, np.int64)
+    chunks = []
+    for t in range(t_max):
+        parts = [s * cfg.sizes[0] + input_spikes(cfg, b, t) for s, b in enumerate(samples) if t < cfg.steps[b]]
+        idx = np.concatenate(parts).astype(np.uint32) if parts else np.zeros(0, np.uint32)
+        chunks.append(idx)
+        offs[t + 1] = offs[t] + idx.size
+    return net, N.SpikeSchedule(chan, offs, np.concatenate(chunks) if chunks else np.zeros(0, np.uint32))

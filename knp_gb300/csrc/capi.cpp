@@ -7,6 +7,26 @@
 #include "../../include/knp_gb300.h"
 #include "engine.h"
 
+namespace knp_gb300
+{
+int lif_scan_forward(
+    const float *I, float *S, float *ckpt, int T, long long BN, float beta, float theta, int K, int relaxed, float k,
+    cudaStream_t s);
+int lif_scan_backward(
+    const float *I, const float *ckpt, const float *dS, float *dI, int T, long long BN, float beta, float theta, int K,
+    int relaxed, float k, cudaStream_t s);
+}  // namespace knp_gb300
+
+namespace knp_gb300
+{
+int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, cudaStream_t s);
+int batched_lif_run(
+    int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *rates,
+    unsigned long long key, int *counts, uint32_t *record, unsigned long long *events_out, float *ms,
+    cudaStream_t s, const char **why);
+}  // namespace knp_gb300
+
 struct knp_gb300_backend
 {
     knp_gb300::Backend impl;
@@ -79,6 +99,18 @@ int knp_gb300_load_blifat_population(
     return guarded([&] { b->impl.load_blifat(U(uid), kind, n, neurons, ext); });
 }
 
+int knp_gb300_load_lif_population(knp_gb300_backend *b, knp_uid uid, uint32_t n, const knp_lif_neuron *neurons)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.load_lif(U(uid), n, neurons); });
+}
+
+int knp_gb300_read_lif_population(knp_gb300_backend *b, knp_uid pop, knp_lif_neuron *out)
+{
+    if (!b || !out) return null_handle();
+    return guarded([&] { b->impl.read_lif(U(pop), out); });
+}
+
 int knp_gb300_load_projection(
     knp_gb300_backend *b, knp_uid uid, int kind, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre,
     const uint32_t *post, const float *weight, const uint32_t *delay, const uint8_t *out_type, const float *tau_plus,
@@ -122,6 +154,12 @@ int knp_gb300_set_accumulator(knp_gb300_backend *b, knp_uid pop_uid, int mode)
 {
     if (!b) return null_handle();
     return guarded([&] { b->impl.set_accumulator(U(pop_uid), mode); });
+}
+
+int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid proj_uid, double fraction)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.set_pull_threshold(U(proj_uid), fraction); });
 }
 
 int knp_gb300_record_spikes(knp_gb300_backend *b, knp_uid pop_uid, int enable)
@@ -260,6 +298,70 @@ int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms)
 {
     if (!b || !ms) return null_handle();
     return guarded([&] { b->impl.profile_phases(n_steps, ms); });
+}
+
+int knp_gb300_lif_scan_forward(
+    const float *I, float *S, float *ckpt, int T, int64_t BN, float beta, float theta, int K, int relaxed, float k,
+    void *stream)
+{
+    if (!I || !S || !ckpt)
+    {
+        g_error = "null buffer";
+        return KNP_GB300_E_INVALID;
+    }
+    const int rc = knp_gb300::lif_scan_forward(I, S, ckpt, T, BN, beta, theta, K, relaxed, k,
+                                               static_cast<cudaStream_t>(stream));
+    if (rc) g_error = rc == -1 ? "bad sizes (T >= 1, BN >= 1, 1 <= K <= 16)" : "kernel launch failed";
+    return rc;
+}
+
+int knp_gb300_lif_scan_backward(
+    const float *I, const float *ckpt, const float *dS, float *dI, int T, int64_t BN, float beta, float theta, int K,
+    int relaxed, float k, void *stream)
+{
+    if (!I || !ckpt || !dS || !dI)
+    {
+        g_error = "null buffer";
+        return KNP_GB300_E_INVALID;
+    }
+    const int rc = knp_gb300::lif_scan_backward(I, ckpt, dS, dI, T, BN, beta, theta, K, relaxed, k,
+                                                static_cast<cudaStream_t>(stream));
+    if (rc) g_error = rc == -1 ? "bad sizes (T >= 1, BN >= 1, 1 <= K <= 16)" : "kernel launch failed";
+    return rc;
+}
+
+int knp_gb300_bf16_gemm_tn(
+    const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, void *stream)
+{
+    const int rc = knp_gb300::bf16_gemm_tn(A, B, D, M, N, K, d_err, static_cast<cudaStream_t>(stream));
+    if (rc) g_error = rc == -1 ? "bad GEMM arguments" : "kernel launch failed";
+    return rc == 0 ? KNP_GB300_OK : (rc == -1 ? KNP_GB300_E_INVALID : KNP_GB300_E_CUDA);
+}
+
+int knp_gb300_batched_lif_run(
+    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *d_rates,
+    uint64_t seed, int32_t *d_counts, uint32_t *d_record, uint64_t *events, float *ms, void *stream)
+{
+    const char *why = "";
+    unsigned long long ev = 0;
+    const int rc = knp_gb300::batched_lif_run(
+        n_layers, sizes, d_weights, leak, threshold, reset, refract, batch, steps, d_rates,
+        knp_gb300::stream_key(seed, 5), d_counts, d_record, &ev, ms, static_cast<cudaStream_t>(stream), &why);
+    if (events) *events = ev;
+    if (rc == 0) return KNP_GB300_OK;
+    g_error = why;
+    switch (rc)
+    {
+        case -1:
+            return KNP_GB300_E_INVALID;
+        case -4:
+            return KNP_GB300_E_DEVICE_FLAG;
+        case -5:
+            return KNP_GB300_E_NOMEM;
+        default:
+            return KNP_GB300_E_CUDA;
+    }
 }
 
 int knp_gb300_synchronize(knp_gb300_backend *b)

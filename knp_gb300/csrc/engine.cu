@@ -176,6 +176,20 @@ void Backend::load_blifat(
     pops_.push_back(std::move(p));
 }
 
+void Backend::load_lif(const Uid &uid, uint32_t n, const knp_lif_neuron *neurons)
+{
+    require_not_init("load_lif_population");
+    if (!neurons && n) throw Error(KNP_GB300_E_INVALID, "null neuron array");
+    if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    auto p = std::make_unique<PopulationSlot>();
+    p->uid = uid;
+    p->kind = KNP_NEURON_LIF;
+    p->n = n;
+    p->n_pad = round_up(std::max<uint32_t>(n, 1), 4);
+    p->init_lif.assign(neurons, neurons + n);
+    pops_.push_back(std::move(p));
+}
+
 void Backend::load_projection(
     const Uid &uid, int kind, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn, const uint32_t *pre,
     const uint32_t *post, const float *w, const uint32_t *delay, const uint8_t *type, const float *tau_plus,
@@ -775,6 +789,78 @@ void Backend::build_stdp(ProjectionSlot &p)
     }
 }
 
+cudaError_t set_gather_smem(size_t bytes);
+
+int Backend::gather_grid(const ProjectionSlot &p) const
+{
+    return static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(p.dev.pull.n_tiles, sm_count_)));
+}
+
+// The gather form is built for large delta projections fed by one population into an FP32 ring,
+// when the device has room for a second (8 B / synapse) copy of the synapses.
+void Backend::build_pull(ProjectionSlot &p)
+{
+    PopulationSlot *post = find_pop(p.post_uid);
+    if (p.pull_fraction < 0 || p.kind != KNP_SYNAPSE_DELTA || !post || p.n_syn < (1u << 20)) return;
+    if (p.dev.n_src != 1 || p.dev.src[0].channel) return;
+    const RingView &rg = post->ring;
+    if (rg.fixed || (rg.forced && p.dev.forcing)) return;
+    if (p.dev.type || (p.dev.uniform_type != KNP_OUT_EXCITATORY && p.dev.uniform_type != KNP_OUT_INHIBITORY_CURRENT))
+        return;
+    if (p.n_rows > (1u << (32 - kPullTileBits))) return;
+    if (static_cast<uint64_t>(p.max_delay) * post->n >= 0xFFFFFFFFull) return;
+    PullDev g{};
+    g.words = round_up((p.n_rows + 31) / 32, 4);
+    g.max_delay = p.max_delay;
+    g.hist_slots = p.max_delay + 1;
+    g.n_tiles = (post->n + kPullTile - 1) / kPullTile;
+    const int grid = static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(g.n_tiles, sm_count_)));
+    const size_t smem = gather_smem_bytes(g, grid);
+    int smem_max = 0;
+    KNP_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+    if (smem > static_cast<size_t>(smem_max)) return;
+    size_t free_b = 0, total_b = 0;
+    KNP_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (free_b < p.n_syn * 30 + (1ull << 30)) return;
+    uint32_t *packed = nullptr;
+    float *w = nullptr;
+    long long *seg = nullptr;
+    const bool negate = p.dev.uniform_type == KNP_OUT_INHIBITORY_CURRENT;
+    KNP_CUDA(build_pull_layout(p.n_syn, p.n_rows, post->n, p.row_ptr, p.col, p.w, p.delay_d, negate, g, &packed, &w,
+                               &seg, stream_));
+    arena_.adopt(packed, p.n_syn * 4);
+    arena_.adopt(w, p.n_syn * 4);
+    arena_.adopt(seg, (static_cast<size_t>(g.max_delay) * g.n_tiles + 1) * 8);
+    g.bitmap = arena_.make<uint32_t>(static_cast<size_t>(g.hist_slots) * g.words);
+    g.pulled = arena_.make<uint32_t>(g.hist_slots);
+    g.threshold = static_cast<uint32_t>(std::max(1.0, std::ceil(p.pull_fraction * p.n_rows)));
+    KNP_CUDA(set_gather_smem(std::max<size_t>(smem, 48 * 1024)));
+    p.dev.pull = g;
+    p.pull = true;
+}
+
+void Backend::set_pull_threshold(const Uid &proj, double fraction)
+{
+    ProjectionSlot *p = find_proj(proj);
+    if (!p) throw Error(KNP_GB300_E_INVALID, "unknown projection");
+    if (initialized_)
+    {
+        if (!p->pull)
+        {
+            if (fraction >= 0) throw Error(KNP_GB300_E_STATE, "this projection has no gather form");
+            return;
+        }
+        KNP_CUDA(cudaStreamSynchronize(stream_));
+        p->pull_fraction = fraction;
+        // A negative fraction disables pulling: no step reaches a threshold above every spike count.
+        p->dev.pull.threshold =
+            fraction < 0 ? 0xFFFFFFFFu : static_cast<uint32_t>(std::max(1.0, std::ceil(fraction * p->n_rows)));
+        capture_graphs();
+        return;
+    }
+    p->pull_fraction = fraction;
+}
+
 void Backend::init()
 {
     require_not_init("init");
@@ -834,6 +920,7 @@ void Backend::init()
     {
         build_projection(*p);
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) build_stdp(*p);
+        build_pull(*p);
     }
     uint32_t ci = n_spike_counters_;
     for (auto &p : projs_)
@@ -873,6 +960,8 @@ void Backend::enqueue_step()
         const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((bound + 7) / 8, 8ull * sm_count_));
         launch_projection(p->dev, ctl_, static_cast<int>(blocks), stream_);
     }
+    for (auto &p : projs_)
+        if (p->pull) launch_gather(p->dev, ctl_, gather_grid(*p), stream_);
     for (auto &p : projs_)
     {
         if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
@@ -1073,6 +1162,8 @@ void Backend::profile_phases(uint64_t n, float *ms)
             const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((bound + 7) / 8, 8ull * sm_count_));
             launch_projection(p->dev, ctl_, static_cast<int>(blocks), stream_);
         }
+        for (auto &p : projs_)
+            if (p->pull) launch_gather(p->dev, ctl_, gather_grid(*p), stream_);
         KNP_CUDA(cudaEventRecord(ev[2], stream_));
         for (auto &p : projs_)
         {
@@ -1371,6 +1462,25 @@ void Backend::read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_s
             ext[i].first_isi_spike = fis[i];
             ext[i].is_being_forced = forced[i];
         }
+    }
+}
+
+void Backend::read_lif(const Uid &pop, knp_lif_neuron *out)
+{
+    PopulationSlot *q = find_pop(pop);
+    if (!q || q->kind != KNP_NEURON_LIF) throw Error(KNP_GB300_E_INVALID, "unknown LIF population");
+    const uint32_t n = q->n;
+    std::copy(q->init_lif.begin(), q->init_lif.end(), out);
+    if (!initialized_ || n == 0) return;
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    std::vector<float> V(n);
+    std::vector<uint32_t> rc(n);
+    KNP_CUDA(cudaMemcpy(V.data(), q->ldev.V, n * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(rc.data(), q->ldev.refract, n * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        out[i].potential = V[i];
+        out[i].refract_counter = rc[i];
     }
 }
 

@@ -60,6 +60,11 @@ public:
         return static_cast<T *>(alloc(n * sizeof(T), zero));
     }
     void release(void *p);
+    void adopt(void *p, size_t bytes)  // take ownership of a cudaMalloc'd buffer
+    {
+        ptrs_.push_back(p);
+        bytes_ += bytes;
+    }
     size_t bytes() const { return bytes_; }
 
 private:
@@ -122,6 +127,8 @@ struct ProjectionSlot
     uint8_t *delay_d = nullptr;
     uint8_t *type_d = nullptr;
     uint32_t *perm = nullptr;  // CSR position -> loaded synapse index (null for generated projections)
+    double pull_fraction = 0.1;  // pull a step when its spikes reach this share of presynaptic neurons (<0: never)
+    bool pull = false;           // the gather layout was built
     ProjectionDev dev{};
     StdpDev stdp{};
     std::vector<std::pair<SpikeSource, int>> stdp_sources;  // (source, both lists)
@@ -168,6 +175,7 @@ public:
     void set_stdp_population(const Uid &proj, const Uid &pop, int processing);
     void subscribe(const Uid &receiver, const Uid &sender);
     void set_accumulator(const Uid &pop, int mode);
+    void set_pull_threshold(const Uid &proj, double fraction);
     void record_spikes(const Uid &pop, bool enable);
     void init();
 
@@ -186,6 +194,8 @@ public:
     void read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n);
     void discard_spikes(uint64_t before);
     void read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext);
+    void load_lif(const Uid &uid, uint32_t n, const knp_lif_neuron *neurons);
+    void read_lif(const Uid &pop, knp_lif_neuron *out);
     void read_weights(const Uid &proj, float *out);
     uint64_t projection_size(const Uid &proj) const;
     void counters(uint64_t *events, uint64_t *spikes, uint64_t *updates);
@@ -205,6 +215,8 @@ private:
     void build_population(PopulationSlot &p);
     void build_projection(ProjectionSlot &p);
     void build_stdp(ProjectionSlot &p);
+    void build_pull(ProjectionSlot &p);
+    int gather_grid(const ProjectionSlot &p) const;
     void wire();
     void enqueue_step();
     void capture_graphs();

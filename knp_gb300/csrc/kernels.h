@@ -151,8 +151,34 @@ struct SpikeSource
     const ChannelDev *channel;    // channel descriptor (null for a population)
 };
 
+// Gather ("pull") form of a projection. A step whose spike count reaches `threshold` is not
+// scattered: its spikes go to a bitmap slot instead, and the gather kernel adds, for every target,
+// the weights of its synapses whose presynaptic neuron spiked d steps before the target step.
+// Synapses are stored sorted by (delay, postsynaptic neuron): for delay d and postsynaptic tile
+// tau (kPullTile neurons) the segment is [seg_ptr[(d-1) * n_tiles + tau], ... + 1); each entry is a
+// packed (pre << kPullTileBits | post - tile base) and a weight (negated for inhibitory current).
+constexpr int kPullTileBits = 9;
+constexpr int kPullTile = 1 << kPullTileBits;
+
+struct PullDev
+{
+    uint32_t *bitmap;       // [hist_slots][words] spikes of pulled steps
+    uint32_t *pulled;       // [hist_slots] 1 if that step was pulled
+    uint32_t hist_slots;    // max_delay + 1
+    uint32_t words;         // ceil(n_rows / 32)
+    uint32_t threshold;     // minimum spike count for pulling a step
+    uint32_t max_delay;
+    uint32_t n_tiles;
+    uint32_t n_post;
+    const long long *seg_ptr;  // [max_delay * n_tiles + 1]
+    const uint32_t *packed;
+    const float *w;
+    uint64_t padded_entries;  // entries of packed / w (segments padded to multiples of 4)
+};
+
 struct ProjectionDev
 {
+    PullDev pull;  // pull.bitmap == nullptr: scatter only
     const long long *row_ptr;
     uint32_t n_rows;
     const int32_t *col;
@@ -201,6 +227,12 @@ void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStrea
 void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
 void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
+void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
+size_t gather_smem_bytes(const PullDev &p, int grid);
+cudaError_t build_pull_layout(
+    uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
+    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, long long **seg_out,
+    cudaStream_t s);
 void launch_apply_impacts(
     const RingView &ring, const uint32_t *post, const float *value, const uint8_t *type, int forcing, uint32_t n,
     Control *ctl, cudaStream_t s);

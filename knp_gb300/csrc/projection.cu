@@ -108,6 +108,40 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
     if (threadIdx.x == 0) block_events = 0;
     __syncthreads();
     unsigned long long events = 0;
+    if (p.pull.bitmap)
+    {
+        // Direction choice for this step's spikes (the same in every block: it depends only on the
+        // spike count). A pulled step only records its spikes; gather_kernel delivers them.
+        const bool pull = total >= p.pull.threshold;
+        const uint32_t sl = static_cast<uint32_t>(t % p.pull.hist_slots);
+        if (blockIdx.x == 0 && threadIdx.x == 0) p.pull.pulled[sl] = pull ? 1u : 0u;
+        if (pull)
+        {
+            uint32_t *bm = p.pull.bitmap + static_cast<size_t>(sl) * p.pull.words;
+            const uint32_t stride = gridDim.x * blockDim.x;
+            for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
+            {
+                uint32_t jj = j;
+                int k = 0;
+                while (jj >= cnt[k])
+                {
+                    jj -= cnt[k];
+                    ++k;
+                }
+                const uint32_t pre = idx[k][jj];
+                if (pre >= p.n_rows) continue;
+                atomicOr(bm + (pre >> 5), 1u << (pre & 31));
+                events += static_cast<unsigned long long>(p.row_ptr[pre + 1] - p.row_ptr[pre]);
+            }
+            // Per-thread counts: reduce over the warp, then the block.
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) events += __shfl_down_sync(0xffffffffu, events, o);
+            if (lane == 0 && events) atomicAdd(&block_events, events);
+            __syncthreads();
+            if (threadIdx.x == 0 && block_events) atomicAdd(&ctl->events_total, block_events);
+            return;
+        }
+    }
     for (uint32_t j = warp; j < total; j += n_warps)
     {
         uint32_t jj = j;

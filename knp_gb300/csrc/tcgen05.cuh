@@ -1,0 +1,124 @@
+// Minimal inline-PTX layer for 5th-generation tensor cores (tcgen05) on sm_103a: tensor-memory
+// allocation, shared-memory matrix descriptors, BF16 MMA with FP32 accumulation in tensor memory,
+// completion through an mbarrier, and tensor-memory loads. Every wait is bounded: it gives up after
+// a fixed number of polls and reports failure, so a kernel can set an error flag and finish.
+#pragma once
+
+#include <cstdint>
+
+namespace knp_gb300
+{
+namespace tc
+{
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+// Shared-memory matrix descriptor for a K-major operand in the canonical layout without swizzle:
+// the tile is made of 8-row x 16-byte core matrices stored as 128 contiguous bytes (row r of the
+// core matrix at byte 16 r); core matrices adjacent along K are `lbo` bytes apart, adjacent along
+// M (or N) `sbo` bytes apart. Element (r, k) of a BF16 tile is at
+//   (r / 8) * sbo + (k / 8) * lbo + (r % 8) * 16 + (k % 8) * 2.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= 1ull << 46;  // descriptor version of tcgen05; base offset 0, no swizzle
+    return d;
+}
+
+__device__ __forceinline__ uint32_t core_offset(uint32_t r, uint32_t k, uint32_t lbo, uint32_t sbo)
+{
+    return (r >> 3) * sbo + (k >> 3) * lbo + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: A and B BF16, D FP32, both operands K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n)
+{
+    return (1u << 4)                                    // D format F32
+           | (1u << 7)                                  // A format BF16
+           | (1u << 10)                                 // B format BF16
+           | (static_cast<uint32_t>(n >> 3) << 17)      // N / 8
+           | (static_cast<uint32_t>(m >> 4) << 24);     // M / 16
+}
+
+// Allocate `ncols` (power of two, >= 32) tensor-memory columns; one full warp executes it and the
+// base address lands in *slot (shared memory).
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Make generic-proxy shared-memory writes visible to the tensor core (async proxy).
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// D[tmem] (+)= A * B^T for one K = 16 slice; issued by a single thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                        uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// The mbarrier at `mbar` receives one arrival when every previously issued tcgen05.mma of this
+// thread has completed.
+__device__ __forceinline__ void commit(uint64_t *mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Wait for phase `parity` of the mbarrier to complete; false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit)
+{
+    const uint32_t a = smem_u32(mbar);
+    for (uint32_t i = 0; i < limit; ++i)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Thread t of warp w (w = warp index within its warpgroup) reads tensor-memory lane 32 w + t,
+// 16 consecutive 32-bit columns starting at `taddr`'s column.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+}  // namespace knp_gb300

@@ -1,0 +1,98 @@
+"""Batched / precision form: tcgen05 BF16 GEMM (FP32 accumulation in tensor memory) against a
+PyTorch FP32 reference of the same BF16 operands (tolerance: relative 1e-5, FP32 summation order)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _gemm(a, b):
+    from knp_gb300 import _capi
+
+    M, K = a.shape
+    N = b.shape[0]
+    d = torch.full((M, N), float("nan"), device="cuda", dtype=torch.float32)
+    err = torch.zeros(1, device="cuda", dtype=torch.int32)
+    rc = _capi.lib().knp_gb300_bf16_gemm_tn(
+        ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(d.data_ptr()), M, N, K,
+        ctypes.c_void_p(err.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, _capi.lib().knp_gb300_last_error()
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    return d
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 64, 16), (200, 100, 784), (256, 1000, 1000), (37, 10, 1000)])
+def test_bf16_gemm_tn(M, N, K):
+    g = torch.Generator(device="cpu").manual_seed(M * 7 + N + K)
+    a = (torch.rand(M, K, generator=g) < 0.2).to(torch.bfloat16).cuda()  # 0/1 spike matrix
+    b = (torch.randn(N, K, generator=g) / K ** 0.5).to(torch.bfloat16).cuda()
+    ref = a.float() @ b.float().t()
+    d = _gemm(a, b)
+    torch.testing.assert_close(d, ref, rtol=1e-5, atol=1e-5)
+
+
+def test_bf16_gemm_tn_dense_values():
+    g = torch.Generator(device="cpu").manual_seed(5)
+    a = torch.randn(130, 96, generator=g).to(torch.bfloat16).cuda()
+    b = torch.randn(48, 96, generator=g).to(torch.bfloat16).cuda()
+    torch.testing.assert_close(_gemm(a, b), a.float() @ b.float().t(), rtol=1e-5, atol=1e-4)
+
+
+def _batched_spikes(cfg, rec, layer, b, t):
+    from knp_gb300 import batched as BT
+
+    return BT.spikes_from_bits(rec[layer][t, b], cfg.sizes[layer])
+
+
+def test_batched_lif_matches_plain_fp32_path():
+    """Batched tcgen05 form against the FP32 plain path on the same samples (block-diagonal network,
+    same BF16-valued weights, FP32 input rings): every layer's spikes agree on at least 99.9% of
+    (sample, neuron, step) and the input spikes agree exactly."""
+    from knp_gb300 import backend as B
+    from knp_gb300 import batched as BT
+    from knp_gb300 import types as T
+
+    cfg = BT.dense_config(seed=9, batch=24, sizes=(64, 96, 96, 10), t_lo=10, t_hi=30, rate_max=0.3)
+    counts, rec, events, ms = BT.run(cfg, record=True)
+    net, sched = BT.plain_network(cfg)
+    t_max = int(cfg.steps.max())
+    out, b = B.run(net, [sched], t_max, accumulator=T.ACC_FP32)
+    # Input layer: identical draws.
+    for s in range(cfg.batch):
+        for t in range(int(cfg.steps[s])):
+            np.testing.assert_array_equal(_batched_spikes(cfg, rec, 0, s, t), BT.input_spikes(cfg, s, t))
+    total = mism = 0
+    for l in range(1, len(cfg.sizes)):
+        n = cfg.sizes[l]
+        uid = net.populations[l - 1].uid
+        for t in range(t_max):
+            plain = out[uid][t]
+            for s in range(cfg.batch):
+                if t >= cfg.steps[s]:
+                    continue
+                g = _batched_spikes(cfg, rec, l, s, t)
+                p = plain[(plain >= s * n) & (plain < (s + 1) * n)] - s * n
+                mism += np.setxor1d(g, p).size
+                total += n
+    assert mism <= 1e-3 * total, (mism, total)
+    # Output counts are the last layer's recorded spikes.
+    L = len(cfg.sizes) - 1
+    for s in range(cfg.batch):
+        c = np.zeros(cfg.sizes[L], np.int64)
+        for t in range(int(cfg.steps[s])):
+            c[_batched_spikes(cfg, rec, L, s, t)] += 1
+        np.testing.assert_array_equal(counts[s], c)
+    assert events > 0 and ms > 0
+
+
+def test_batched_lif_full_config_runs():
+    """The full batched dense config (256 samples, 784-1000-1000-10, T in [50, 200])."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(seed=4)
+    counts, _, events, ms = BT.run(cfg)
+    assert counts.shape == (256, 10) and events > 0 and ms > 0

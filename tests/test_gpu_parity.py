@@ -94,6 +94,65 @@ def test_large_sparse_reduced_scale():
     assert b.counters()[0] == oo.events
 
 
+@pytest.mark.parametrize("fraction", [0.0, 0.05, 0.3, -1.0])
+def test_gather_direction_bit_exact(fraction):
+    """Steps delivered by the gather kernel (spike share >= fraction; 0 = every step with a spike,
+    -1 = never) give the same spike trains as the oracle, through the ramp into saturated firing."""
+    from knp_gb300 import backend as B
+    from oracle import oracle as orc
+
+    net, sched = N.large_sparse_network(seed=2, n=5000, fan_in=1000, steps=70)
+    rec = net.projections[1]
+    b = B.GB300Backend()
+    b.load_network(net)
+    b.set_pull_threshold(rec.uid, fraction)
+    b._init()
+    for t in range(70):
+        idx = sched[0].at(t)
+        if idx.size:
+            b.send_spikes(sched[0].sender, idx, t)
+        b.step(1)
+    o, oo = orc.run(net, sched, 70)
+    pop = net.populations[0].uid
+    for t in range(70):
+        np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t], err_msg=f"step {t}")
+    assert b.counters()[0] == oo.events
+    assert_same_state(b, oo, pop)
+
+
+def test_gather_inhibitory_projection():
+    """Uniform INHIBITORY_CURRENT projection in gather form (weights negated in the layout)."""
+    from knp_gb300 import backend as B
+    from oracle import oracle as orc
+
+    n, fan = 2000, 600
+    pop = N.Population(T.uid_from_int(41), T.BLIFAT, T.blifat_defaults(n))
+    chan = T.uid_from_int(49)
+    k = [N.stream_key(9, s) for s in (1, 2, 3)]
+    pre, post, w, d = N.fixed_fan_in_pre(*k, n, n, fan, 0, 64, 1, 6)
+    exc = N.Projection(T.uid_from_int(42), T.DELTA, pop.uid, pop.uid, pre, post, w, d)
+    k2 = [N.stream_key(10, s) for s in (1, 2, 3)]
+    pre2, post2, w2, d2 = N.fixed_fan_in_pre(*k2, n, n, fan, 0, 32, 1, 6)
+    inh = N.Projection(T.uid_from_int(43), T.DELTA, pop.uid, pop.uid, pre2, post2, w2, d2,
+                       out_type=np.full(pre2.size, T.INHIBITORY_CURRENT, np.uint8))
+    ar = np.arange(n, dtype=np.uint32)
+    bg = N.Projection(T.uid_from_int(44), T.DELTA, T.NULL_UID, pop.uid, ar, ar.copy(), np.ones(n, np.float32),
+                      np.ones(n, np.uint32))
+    net = N.Network([pop], [bg, exc, inh], [(bg.uid, chan)])
+    sched = N.bernoulli_schedule(chan, 6, n, 60, 0.05)
+    b = B.GB300Backend()
+    b.load_network(net)
+    b.set_pull_threshold(exc.uid, 0.0)
+    b.set_pull_threshold(inh.uid, 0.0)
+    b._init()
+    b.load_spike_schedule(sched)
+    b.step(60)
+    o, oo = orc.run(net, [sched], 60)
+    for t in range(60):
+        np.testing.assert_array_equal(b.spikes(pop.uid, t), o[pop.uid][t], err_msg=f"step {t}")
+    assert b.counters()[0] == oo.events
+
+
 def test_device_generated_projection_matches_host_arrays():
     """The device-side fixed fan-in generator builds exactly the synapses of network.fixed_fan_in_pre."""
     from knp_gb300 import backend as B
@@ -225,6 +284,73 @@ def test_stdp_only_and_multiple_sources():
     g, b, o, oo = run_both(net, [sched], 80)
     assert_same_spikes(g, o)
     np.testing.assert_array_equal(b.read_weights(plastic.uid), oo.weights(plastic.uid))
+
+
+def _gpu_lif_run(neuron, steps, impacts=()):
+    """knp/tests/framework/lif_test.cpp:60-100 through the C ABI: one LIF neuron, one external
+    impact per step, potential read before every step."""
+    from knp_gb300 import backend as B
+
+    pop_uid, in_uid = T.uid_from_int(601), T.uid_from_int(602)
+    b = B.GB300Backend()
+    b.load_network(N.Network([N.Population(pop_uid, T.LIF, neuron.copy())], [], [(pop_uid, in_uid)]))
+    b._init()
+    pots, spikes = [], []
+    for t in range(steps):
+        if t < len(impacts):
+            b.send_impacts(in_uid, pop_uid, [0], [impacts[t]], [T.EXCITATORY])
+        pots.append(float(b.read_lif(pop_uid)["potential"][0]))
+        b.step(1)
+        if b.spikes(pop_uid, t).size:
+            spikes.append(t)
+    return pots, spikes
+
+
+def test_lif_known_answers():
+    """Expected potentials and spike steps of lif_test.cpp:103-177."""
+    n = T.lif_defaults(1)
+    n["activation_threshold"] = 101.0
+    n["leak_coefficient"] = 0.25
+    n["potential"] = 100.0
+    assert _gpu_lif_run(n, 10) == ([100.0 * 0.25 ** k for k in range(10)], [])
+    n = T.lif_defaults(1)
+    n["leak_coefficient"] = 0.5
+    n["potential"] = 3.0
+    assert _gpu_lif_run(n, 3) == ([3.0, 0.0, 0.0], [0])
+    n = T.lif_defaults(1)
+    n["leak_coefficient"] = 0.5
+    n["activation_threshold"] = 6.0
+    assert _gpu_lif_run(n, 6, [5, 5, 2, 3, 8]) == ([0.0, 5.0, 0.0, 2.0, 4.0, 0.0], [1, 4])
+    n["refract_period"] = 2
+    assert _gpu_lif_run(n, 7, [5, 5, 10, 10, 5, 5]) == ([0.0, 5.0, 0.0, 0.0, 0.0, 5.0, 0.0], [1, 5])
+
+
+def test_lif_network_against_oracle():
+    """Feed-forward LIF layers (dyadic weights, refractory period 1, threshold 2) against the oracle.
+    Leak stays 1 (the reference default) so that FP32 sums are exact whatever their order: the
+    reference adds impacts one by one, the ring adds their pre-summed value."""
+    n_in, n1, n2 = 100, 300, 50
+    l1 = T.lif_defaults(n1)
+    l1["refract_period"] = 1
+    l2 = T.lif_defaults(n2)
+    l2["activation_threshold"] = 2.0
+    p1 = N.Population(T.uid_from_int(611), T.LIF, l1)
+    p2 = N.Population(T.uid_from_int(612), T.LIF, l2)
+    chan = T.uid_from_int(619)
+    k = [N.stream_key(13, s) for s in (1, 2, 3)]
+    i = np.arange(n_in * n1, dtype=np.uint64)
+    a = N.Projection(T.uid_from_int(613), T.DELTA, T.NULL_UID, p1.uid, (i % n_in).astype(np.uint32),
+                     (i // n_in).astype(np.uint32), N.dyadic_weights(k[1], i, -32, 64), np.ones(i.size, np.uint32))
+    j = np.arange(n1 * n2, dtype=np.uint64)
+    b_ = N.Projection(T.uid_from_int(614), T.DELTA, p1.uid, p2.uid, (j % n1).astype(np.uint32),
+                      (j // n1).astype(np.uint32), N.dyadic_weights(k[2], j, -16, 32),
+                      N.uniform_int(k[0], j, 1, 3).astype(np.uint32))
+    net = N.Network([p1, p2], [a, b_], [(a.uid, chan)])
+    sched = N.bernoulli_schedule(chan, 14, n_in, 80, 0.1)
+    g, b, o, oo = run_both(net, [sched], 80)
+    assert_same_spikes(g, o)
+    for p in (p1, p2):
+        np.testing.assert_array_equal(b.read_lif(p.uid), oo.lif(p.uid))
 
 
 def test_errors_are_reported():
