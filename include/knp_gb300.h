@@ -187,6 +187,31 @@ KNP_GB300_API int knp_gb300_generate_bernoulli_schedule(
     uint64_t seed, uint64_t stream);
 
 /**
+ * Allocation-free variant of knp_gb300_generate_bernoulli_schedule, for callers that cannot
+ * allocate GPU memory when they need a schedule (code running while another component owns the
+ * device memory pool, allocators that forbid cudaMalloc/cudaFree in the calling phase or thread,
+ * plugins that may only use buffers their host hands them). No reference counterpart.
+ *
+ * Writes the schedule of `n_sources` Bernoulli(p) sources for steps [first_step, first_step +
+ * n_steps) into caller-owned DEVICE buffers: d_offsets[n_steps + 1] and d_idx[capacity]; step
+ * first_step + t sends d_idx[d_offsets[t] : d_offsets[t + 1]] (ascending), the same spikes the
+ * allocating generator produces for (seed, stream). *n_idx (host) receives the number of spikes.
+ * It calls no cudaMalloc, cudaFree or allocating library routine: its scratch is one fixed device
+ * array of 2^18 + 1 int64 counters that every GPU loading the library keeps until process exit, so
+ * n_steps * ceil(n_sources / 4096) must not exceed 262144 and n_steps 65535 (else
+ * KNP_GB300_E_INVALID). If capacity is too small it returns KNP_GB300_E_INVALID with the needed
+ * count in *n_idx and writes nothing to d_idx. The first call on a device looks up the scratch
+ * array's device address with that device current; make that first call before any stream capture.
+ * Every call shares the scratch and finds the previous call's contents (each call rewrites every
+ * counter it reads); calls that overlap on the GPU race and must be serialised by the caller. The
+ * call waits for its own stream (`stream`, a cudaStream_t; NULL: legacy default stream) once, to read
+ * the spike count, and returns with the index writes queued on that stream.
+ */
+KNP_GB300_API int knp_gb300_generate_bernoulli_schedule_noalloc(
+    uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps, uint64_t seed, uint64_t stream_id,
+    int64_t *d_offsets, uint32_t *d_idx, uint64_t capacity, uint64_t *n_idx, void *stream);
+
+/**
  * Send an external SynapticImpactMessage to population `receiver` (impacts post_idx[i], value[i],
  * out_type[i] (NULL = EXCITATORY)); applied at the next step, after impacts of the backend's own
  * projections. Replaces: MessageEndpoint::send_message of a SynapticImpactMessage

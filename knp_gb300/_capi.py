@@ -60,6 +60,8 @@ def lib():
         "knp_gb300_load_spike_schedule": ([p, U, u64, u64, p, p], c_int),
         "knp_gb300_generate_bernoulli_schedule": ([p, U, u32, ctypes.c_double, u64, u64, u64, u64], c_int),
         "knp_gb300_send_impacts": ([p, U, U, c_int, u32, p, p, p], c_int),
+        "knp_gb300_generate_bernoulli_schedule_noalloc": ([u32, ctypes.c_double, u64, u64, u64, u64, p, p, u64,
+                                                           ctypes.POINTER(u64), p], c_int),
         "knp_gb300_step": ([p, u64], c_int),
         "knp_gb300_get_step": ([p, ctypes.POINTER(u64)], c_int),
         "knp_gb300_read_spikes": ([p, U, u64, u32, p, ctypes.POINTER(u32)], c_int),

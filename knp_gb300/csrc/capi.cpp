@@ -19,6 +19,13 @@ int lif_scan_backward(
 
 namespace knp_gb300
 {
+int bernoulli_schedule_noalloc(
+    uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps, uint64_t seed, uint64_t stream,
+    long long *d_offsets, uint32_t *d_idx, uint64_t capacity, uint64_t *n_idx, cudaStream_t s, const char **why);
+}  // namespace knp_gb300
+
+namespace knp_gb300
+{
 int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, cudaStream_t s);
 int batched_lif_run(
     int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
@@ -328,6 +335,19 @@ int knp_gb300_lif_scan_backward(
                                                 static_cast<cudaStream_t>(stream));
     if (rc) g_error = rc == -1 ? "bad sizes (T >= 1, BN >= 1, 1 <= K <= 16)" : "kernel launch failed";
     return rc;
+}
+
+int knp_gb300_generate_bernoulli_schedule_noalloc(
+    uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps, uint64_t seed, uint64_t stream_id,
+    int64_t *d_offsets, uint32_t *d_idx, uint64_t capacity, uint64_t *n_idx, void *stream)
+{
+    const char *why = "";
+    const int rc = knp_gb300::bernoulli_schedule_noalloc(
+        n_sources, p, first_step, n_steps, seed, stream_id, reinterpret_cast<long long *>(d_offsets), d_idx, capacity,
+        n_idx, static_cast<cudaStream_t>(stream), &why);
+    if (rc == 0) return KNP_GB300_OK;
+    g_error = why;
+    return rc == -3 ? KNP_GB300_E_CUDA : KNP_GB300_E_INVALID;
 }
 
 int knp_gb300_bf16_gemm_tn(
