@@ -178,6 +178,129 @@ def reference_mt_sample(target_s: float = 30.0):
                       f"{o.events} events, {dt:.1f} s, restated multi-threaded backend step on {threads} threads"}
 
 
+def _flush_l2(dev):
+    """Write a buffer larger than L2 (129 MB) so that the next timed run starts with a cold cache."""
+    import torch
+
+    buf = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    buf.fill_(1.0)
+    del buf
+
+
+def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
+    """Batched dense config (256 LIF samples, 784-1000-1000-10, T uniform in [50, 200], delay-1
+    all-to-all layers, BF16 weights, FP32 accumulation) on the tcgen05 batched form, beside the
+    plain FP32 backend path running the same samples as one block-diagonal network. Both count a
+    synaptic event as a spike times the fan-out of its layer. Spike mismatch: share of (sample,
+    neuron, step) of layers 1..3 where the two forms disagree, over each sample's own steps."""
+    import torch
+
+    from knp_gb300 import backend as B
+    from knp_gb300 import batched as BT
+    from knp_gb300 import types as T
+
+    dev = torch.device(f"cuda:{device}")
+    cfg = BT.dense_config(seed=4)
+    for _ in range(warmup):
+        BT.run(cfg, device=device)
+    times, events = [], 0
+    for _ in range(reps):
+        _flush_l2(dev)
+        torch.cuda.synchronize(dev)
+        _, _, events, ms = BT.run(cfg, device=device)
+        times.append(ms)
+    ms_b = statistics.median(times)
+    _, rec, _, _ = BT.run(cfg, record=True, device=device)
+
+    # Plain FP32 path on the same samples.
+    t_build = time.perf_counter()
+    net, sched = BT.plain_network(cfg)
+    b = B.GB300Backend(device)
+    b.load_network(net)
+    for p in net.populations:
+        b.set_accumulator(p.uid, T.ACC_FP32)
+    b._init()
+    b.load_spike_schedule(sched)
+    del net
+    t_build = time.perf_counter() - t_build
+    t_max = int(cfg.steps.max())
+    e0, _, _ = b.counters()
+    _flush_l2(dev)
+    ms_p = b.step_timed(t_max)
+    e1, _, _ = b.counters()
+    ev_p = e1 - e0
+
+    # Spike mismatch between the two forms.
+    live = np.arange(t_max)[:, None] < cfg.steps[None, :].astype(np.int64)  # [t, sample]
+    mism = total = 0
+    pops = [p for p in b._pops]
+    for layer in range(1, len(cfg.sizes)):
+        n = cfg.sizes[layer]
+        words = (n + 31) // 32
+        uid = pops[layer - 1]
+        for t in range(t_max):
+            idx = b.spikes(uid, t).astype(np.int64)
+            bm = np.zeros((cfg.batch, words), np.uint32)
+            s, j = idx // n, idx % n
+            np.bitwise_or.at(bm, (s, j >> 5), (np.uint32(1) << (j & 31).astype(np.uint32)))
+            diff = (bm ^ rec[layer][t]) & np.where(live[t][:, None], np.uint32(0xFFFFFFFF), np.uint32(0))
+            mism += int(np.unpackbits(diff.view(np.uint8)).sum())
+            total += int(live[t].sum()) * n
+    b.close()
+    flops = 2.0 * float(sum(int(cfg.steps.sum()) * a * c for a, c in zip(cfg.sizes[:-1], cfg.sizes[1:])))
+    return {
+        "workload": "batched_dense: 256 LIF samples 784-1000-1000-10, T in [50,200], inputs rate U[0,0.2], "
+                    "weights N(0,1/fan_in) as BF16, FP32 accumulation, one persistent launch",
+        "value": events / (ms_b / 1e3), "unit": UNIT, "ms_per_run": ms_b, "events_per_run": events,
+        "plain_fp32_path": {"value": ev_p / (ms_p / 1e3), "unit": UNIT, "ms_per_run": ms_p, "events_per_run": ev_p,
+                            "build_s": t_build},
+        "speedup_vs_plain": (events / ms_b) / (ev_p / ms_p),
+        "spike_mismatch": mism / max(total, 1), "compared": total,
+        "tensor": {"dense_flops_per_run": flops, "achieved_tflops": flops / (ms_b / 1e3) / 1e12},
+        "dtype": "bf16 x bf16 -> fp32", "l2": "flushed (256 MB write) before each timed run",
+    }
+
+
+def bptt_measure(device: int, iters: int = 10, warmup: int = 3):
+    """Surrogate-gradient BPTT training step (LIF 784-512-512-10, batch 128, T 32, decay 0.9,
+    threshold 1, fast-sigmoid slope 25, membrane checkpoint every 8 steps): forward + backward +
+    SGD update of the FP32 master weights, CUDA-event timed on torch's current stream."""
+    import torch
+
+    from knp_gb300 import bptt
+
+    dev = torch.device(f"cuda:{device}")
+    torch.cuda.set_device(dev)
+    x, labels = bptt.make_batch(T=32, B=128, seed=11, device=dev)
+    model = bptt.SpikingMLP(sizes=(784, 512, 512, 10), checkpoint=8, seed=12, device=dev)
+    opt = torch.optim.SGD(model.parameters(), lr=1e-3)
+
+    def it():
+        opt.zero_grad(set_to_none=True)
+        loss = bptt.loss_fn(model(x), labels)
+        loss.backward()
+        opt.step()
+        return loss
+
+    for _ in range(warmup):
+        it()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        loss = it()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / iters
+    layers = [(784, 512), (512, 512), (512, 10)]
+    tb = 32 * 128
+    # Forward GEMMs, recomputed input GEMMs in the backward, weight and input gradients.
+    flops = 2.0 * tb * sum(a * c for a, c in layers) * 4
+    return {"workload": "bptt: LIF 784-512-512-10, batch 128, T 32, checkpoint 8", "ms_per_iter": ms,
+            "gemm_flops_per_iter": flops, "achieved_tflops": flops / (ms / 1e3) / 1e12,
+            "loss": float(loss.item())}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -202,6 +325,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--profile-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched dense and BPTT measurements")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     ap.add_argument("--pull-threshold", type=float, default=0.1,
@@ -314,6 +438,12 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample()
+    b.close()
+
+    batched = bp = None
+    if rank == 0 and not args.no_forms:
+        batched = batched_dense_measure(local)
+        bp = bptt_measure(local)
 
     if rank == 0:
         line = {
@@ -332,12 +462,15 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 4 * args.steps,
+            # Per step: the population kernel, one scatter kernel per projection (recurrent and
+            # background), the gather kernel of the recurrent projection, the end-of-step kernel.
+            "gpu_launches": 5 * args.steps,
             "clocks": clk.summary(),
             "build_s": t_build,
+            "batched_dense": batched,
+            "bptt": bp,
         }
         print(json.dumps(line))
-    b.close()
     if dist is not None:
         dist.destroy_process_group()
 

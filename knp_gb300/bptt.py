@@ -135,14 +135,17 @@ class _SpikeFn64(torch.autograd.Function):
         return g * (0.5 * ctx.k) / (d * d), None, None
 
 
-def reference_forward64(x, weights, beta=0.9, theta=1.0, relaxed=False, k=K_SLOPE):
-    """The same network in float64 with torch autograd (loop over steps, no checkpointing)."""
-    s_all = x.to(torch.float64)
+def reference_forward(x, weights, beta=0.9, theta=1.0, relaxed=False, k=K_SLOPE):
+    """The same network with torch autograd (loop over steps, no checkpointing), computed in the
+    dtype of ``weights[0]``: float64 for the reference answer, float32 for a plain FP32
+    implementation whose error against float64 calibrates the tolerance of the relaxed form."""
+    dt = weights[0].dtype
+    s_all = x.to(dt)
     T = s_all.shape[0]
     for w in weights:
-        wb = w.to(torch.float64)
+        wb = w.to(dt)
         outs = []
-        V = torch.zeros(s_all.shape[1], wb.shape[1], dtype=torch.float64, device=x.device)
+        V = torch.zeros(s_all.shape[1], wb.shape[1], dtype=dt, device=x.device)
         for t in range(T):
             U = beta * V + s_all[t] @ wb
             s = _SpikeFn64.apply(U - theta, relaxed, k)

@@ -173,7 +173,7 @@ struct PullDev
     const long long *seg_ptr;  // [max_delay * n_tiles + 1]
     const uint32_t *packed;
     const float *w;
-    uint64_t padded_entries;  // entries of packed / w (segments padded to multiples of 4)
+    uint64_t padded_entries;  // entries of packed / w (segments padded to multiples of 8)
 };
 
 struct ProjectionDev

@@ -23,7 +23,7 @@ namespace
 {
 
 constexpr int kGatherThreads = 1024;
-constexpr int kUnroll = 4;  // 16-byte key + weight loads in flight per lane (16 synapses)
+constexpr int kUnroll = 2;  // groups of 8 synapses in flight per lane (16 synapses)
 
 __global__ void row_of_kernel(const long long *row_ptr, uint32_t n_rows, uint32_t *row_of)
 {
@@ -76,7 +76,7 @@ __global__ void pull_seg_kernel(
 
 // One warp per segment: copy the segment's synapses (sorted positions [seg[s], seg[s+1])) to
 // padded positions [pseg[s], pseg[s+1]) as packed (pre << 9 | post mod 512) + weight, and fill the
-// padding (up to 3 entries, so that every segment starts on a 16-byte boundary) with sentinels.
+// padding (up to 7 entries, so that every segment starts on a 32-byte boundary) with key 0 / weight 0.
 __global__ void pull_fill_kernel(
     uint64_t n_seg, const long long *seg, const long long *pseg, const uint32_t *order, const uint32_t *row_of,
     const int32_t *col, const float *w, bool negate, uint32_t *packed, float *w_out)
@@ -98,7 +98,7 @@ __global__ void pull_fill_kernel(
             }
             else
             {
-                packed[pa + i] = 0xFFFFFFFFu;
+                packed[pa + i] = 0u;
                 w_out[pa + i] = 0.0f;
             }
         }
@@ -155,47 +155,51 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
         for (uint32_t tile = t0; tile < t1; ++tile)
         {
             const size_t si = static_cast<size_t>(d - 1) * g.n_tiles + tile;
-            // Segments start and end on 4-entry boundaries: a lane takes 4 consecutive synapses
-            // with one 16-byte load of keys and one of weights.
-            const long long qa = g.seg_ptr[si] >> 2, qb = g.seg_ptr[si + 1] >> 2;
+            // Segments start and end on 8-entry boundaries: a lane takes 8 consecutive synapses
+            // with two 16-byte loads of keys and two of weights. Padding entries (and lanes past the
+            // segment) are key 0 / weight 0: presynaptic neuron 0, target 0, contributing nothing.
+            const long long oa = g.seg_ptr[si] >> 3, ob = g.seg_ptr[si + 1] >> 3;
             float *acc_t = acc + static_cast<size_t>(tile - t0) * kPullTile;
             const uint4 *pk = reinterpret_cast<const uint4 *>(g.packed);
             const float4 *pw = reinterpret_cast<const float4 *>(g.w);
-            for (long long base = qa + warp_base; base < qb; base += static_cast<long long>(blockDim.x) * kUnroll)
+            for (long long base = oa + warp_base; base < ob; base += static_cast<long long>(blockDim.x) * kUnroll)
             {
-                uint4 key[kUnroll];
-                float4 w[kUnroll];
+                uint4 key[kUnroll][2];
+                float4 w[kUnroll][2];
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u)
                 {
-                    const long long q = base + static_cast<long long>(u) * blockDim.x + lane;
-                    key[u] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-                    w[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (q < qb)
+                    const long long o = base + static_cast<long long>(u) * blockDim.x + lane;
+                    key[u][0] = key[u][1] = make_uint4(0u, 0u, 0u, 0u);
+                    w[u][0] = w[u][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (o < ob)
                     {
-                        key[u] = __ldcs(pk + q);
-                        w[u] = __ldcs(pw + q);
+                        key[u][0] = __ldcs(pk + 2 * o);
+                        key[u][1] = __ldcs(pk + 2 * o + 1);
+                        w[u][0] = __ldcs(pw + 2 * o);
+                        w[u][1] = __ldcs(pw + 2 * o + 1);
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < kUnroll; ++u)
                 {
-                    // Runs of equal targets inside the lane's 4 entries: every run but the last is
+                    // Runs of equal targets inside the lane's 8 entries: every run but the last is
                     // added at once; the last joins the warp-wide merge across lanes.
-                    const uint32_t kk[4] = {key[u].x, key[u].y, key[u].z, key[u].w};
-                    const float ww[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
-                    uint32_t cur = 0xFFFFFFFFu;
+                    const uint32_t kk[8] = {key[u][0].x, key[u][0].y, key[u][0].z, key[u][0].w,
+                                            key[u][1].x, key[u][1].y, key[u][1].z, key[u][1].w};
+                    const float ww[8] = {w[u][0].x, w[u][0].y, w[u][0].z, w[u][0].w,
+                                         w[u][1].x, w[u][1].y, w[u][1].z, w[u][1].w};
+                    uint32_t cur = kk[0] & (kPullTile - 1);
                     float sum = 0.0f;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                    for (int i = 0; i < 8; ++i)
                     {
-                        if (kk[i] == 0xFFFFFFFFu) continue;
                         const uint32_t pre = kk[i] >> kPullTileBits;
                         const uint32_t jl = kk[i] & (kPullTile - 1);
                         const float v = ((bm[pre >> 5] >> (pre & 31)) & 1u) ? ww[i] : 0.0f;
                         if (jl != cur)
                         {
-                            if (cur != 0xFFFFFFFFu && sum != 0.0f) atomicAdd(acc_t + cur, sum);
+                            if (sum != 0.0f) atomicAdd(acc_t + cur, sum);
                             cur = jl;
                             sum = v;
                         }
@@ -306,12 +310,12 @@ cudaError_t build_pull_layout(
     KNP_TRY(cudaGetLastError());
     KNP_TRY(cudaStreamSynchronize(s));
     {
-        // Pad every segment to a multiple of 4 entries (16-byte aligned starts for vector loads).
+        // Pad every segment to a multiple of 8 entries (32-byte aligned starts for vector loads).
         const size_t n_seg = static_cast<size_t>(D) * n_tiles;
         std::vector<long long> raw(n_seg + 1), pad(n_seg + 1, 0);
         err = cudaMemcpy(raw.data(), seg_raw, raw.size() * sizeof(long long), cudaMemcpyDeviceToHost);
         if (err != cudaSuccess) goto done;
-        for (size_t i = 0; i < n_seg; ++i) pad[i + 1] = pad[i] + ((raw[i + 1] - raw[i] + 3) & ~3ll);
+        for (size_t i = 0; i < n_seg; ++i) pad[i + 1] = pad[i] + ((raw[i + 1] - raw[i] + 7) & ~7ll);
         err = cudaMemcpy(*seg_out, pad.data(), pad.size() * sizeof(long long), cudaMemcpyHostToDevice);
         if (err != cudaSuccess) goto done;
         const size_t padded = static_cast<size_t>(pad[n_seg]) * sizeof(uint32_t) + 16;

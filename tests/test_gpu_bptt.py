@@ -29,7 +29,7 @@ def _ref_grads(model, x, labels, relaxed, dtype=torch.float64):
     from knp_gb300 import bptt
 
     ws = [bptt.bf16_values(w.detach()).to(dtype).requires_grad_(True) for w in model.weights]
-    counts = bptt.reference_forward64(x.to(dtype), ws, model.beta, model.theta, relaxed, model.k)
+    counts = bptt.reference_forward(x.to(dtype), ws, model.beta, model.theta, relaxed, model.k)
     loss = torch.nn.functional.cross_entropy(counts, labels)
     loss.backward()
     return counts.detach(), loss.detach(), [w.grad.to(torch.float64) for w in ws]
@@ -68,7 +68,7 @@ def test_bptt_finite_differences_relaxed():
     ws64 = [bptt.bf16_values(w.detach()).to(torch.float64) for w in model.weights]
 
     def loss64(ws):
-        c = bptt.reference_forward64(x, ws, model.beta, model.theta, True, model.k)
+        c = bptt.reference_forward(x, ws, model.beta, model.theta, True, model.k)
         return torch.nn.functional.cross_entropy(c, labels).item()
 
     gen = torch.Generator().manual_seed(0)
