@@ -326,6 +326,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched dense and BPTT measurements")
+    ap.add_argument("--form", default="all", choices=["all", "batched", "bptt"],
+                    help="measure only the batched dense form or only the BPTT step (profiling runs)")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     ap.add_argument("--pull-threshold", type=float, default=0.1,
@@ -334,6 +336,12 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.form != "all":
+        # One form alone (profiling runs): prints that form's measurement as one JSON line.
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        out = batched_dense_measure(local) if args.form == "batched" else bptt_measure(local)
+        print(json.dumps({"form": args.form, **out}))
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -418,21 +426,24 @@ def main():
         b.record_spikes(pop_uid, True)
         b.synchronize()
         ea, _, _ = b.counters()
-        h2d = d2h = 0
+        h2d = d2h = n_out = 0
         t0 = time.perf_counter()
         for k in range(args.e2e_steps):
             idx = sched.at(k)
             b.send_spikes(chan_uid, idx, start + k)
             h2d += idx.nbytes
             b.step(1)
-            out = b.spikes(pop_uid, start + k)
-            d2h += out.nbytes
+            out = b.spikes(pop_uid, start + k)  # ascending indexes, as in the reference's SpikeMessage
+            b.discard_spikes(start + k + 1)
+            # What crosses to the host is the step's spike bitmap (one bit per neuron), expanded there.
+            d2h += (n_neurons + 31) // 32 * 4
+            n_out += out.size
         b.synchronize()
         te = time.perf_counter() - t0
         eb, _, _ = b.counters()
         e2e = {"value": (eb - ea) / te, "unit": UNIT, "h2d_bytes_per_step": h2d / args.e2e_steps,
                "d2h_bytes_per_step": d2h / args.e2e_steps, "steps": args.e2e_steps,
-               "ms_per_step": te / args.e2e_steps * 1e3}
+               "ms_per_step": te / args.e2e_steps * 1e3, "spikes_returned_per_step": n_out / args.e2e_steps}
         b.record_spikes(pop_uid, False)
 
     cpu = None

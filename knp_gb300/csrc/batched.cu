@@ -158,7 +158,7 @@ namespace knp_gb300
 namespace
 {
 
-constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
+constexpr int kBM = 128, kBN = 32, kBK = 128, kABufs = 2, kMaxLayers = 4, kMaxItems = 512;
 constexpr int kBatchThreads = 256;
 
 struct BatchedNet
@@ -173,12 +173,10 @@ struct BatchedNet
     uint32_t batch;
     const uint32_t *perm;   // slot -> sample
     const uint32_t *steps;  // T per slot, non-increasing
-    const float *rates;     // [batch][size[0]] by sample
+    const unsigned long long *rate_thr;  // [batch][size[0]] by sample: rate * 2^53, the draw's threshold
     unsigned long long key;
     uint32_t t_max;
     uint32_t *bits[kMaxLayers + 1][2];  // [batch][words[l]] per step parity
-    float *V[kMaxLayers];               // [batch][size[l]] by slot, l = 1..L stored at index l - 1
-    uint32_t *rc[kMaxLayers];
     int *counts;                         // [batch][size[L]] by sample
     uint32_t *record;                    // [t_max][sum_l batch * words[l]] by sample, or null
     unsigned long long rec_off[kMaxLayers + 1];
@@ -237,11 +235,18 @@ __device__ __forceinline__ uint32_t active_slots(const uint32_t *steps, uint32_t
     return lo;
 }
 
+// Per (sample, input): the 53-bit threshold that the input draw is compared with.
+__global__ void rate_threshold_kernel(const float *rates, unsigned long long *thr, size_t n)
+{
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) thr[i] = static_cast<unsigned long long>(static_cast<double>(rates[i]) * 9007199254740992.0);
+}
+
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[kABufs];
     __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
     const uint32_t item = blockIdx.x;
@@ -250,8 +255,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t n0 = net.item_n[item] * kBN;
     const uint32_t K = net.size[layer - 1], Kp = net.kpad[layer], N = net.size[layer];
     const uint32_t wk = net.words[layer - 1], wn = net.words[layer];
+    const uint32_t bm_stride = wk | 1u;  // odd row stride: 32 consecutive rows hit 32 banks
+    // Shared memory: weight tile [kBN x Kp], kABufs A chunks [kBM x kBK], spike bitmap rows [kBM x bm_stride].
     uint8_t *sW = smem;
     uint8_t *sA = smem + static_cast<size_t>(kBN) * Kp * 2;
+    uint32_t *sBM = reinterpret_cast<uint32_t *>(sA + static_cast<size_t>(kABufs) * kBM * kBK * 2);
     const uint32_t sbo_w = (Kp / 8) * 128, sbo_a = (kBK / 8) * 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -266,15 +274,38 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
     if (warp == 0) tc::tmem_alloc(&tmem_slot, 32);
-    if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kABufs; ++i) tc::mbar_init(&mbar[i], 1);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
     const uint32_t fan_out = layer < net.n_layers ? net.size[layer + 1] : 0u;
-    uint32_t phase = 0;
+    const uint32_t n_chunks = (Kp + kBK - 1) / kBK;
+    uint32_t uses[kABufs];  // commits made on each A buffer's mbarrier so far
+#pragma unroll
+    for (int i = 0; i < kABufs; ++i) uses[i] = 0;
     bool ok = true;
+
+    // Epilogue ownership, fixed for the run: thread (warp, lane) owns row 32 (warp % 4) + lane of the
+    // tile and columns 16 (warp / 4) .. +15, so it keeps their LIF state in registers.
+    const uint32_t er = 32u * (warp & 3) + lane;
+    const uint32_t erow = m0 + er;
+    const uint32_t cb = 16u * (warp >> 2);
+    float V[16];
+    uint32_t RC[16];
+    int CNT[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+    {
+        V[i] = 0.f;
+        RC[i] = 0u;
+        CNT[i] = 0;
+    }
+    const int li = layer - 1;
+    const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
+    const uint32_t per = net.refract[li];
 
     for (uint32_t t = 0; t < net.t_max && ok; ++t)
     {
@@ -286,84 +317,108 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         __syncthreads();
         if (m0 < b_act)
         {
-            for (uint32_t k0 = 0; k0 < Kp && ok; k0 += kBK)
+            // This tile's rows of the previous layer's spike bitmap (step t - 1), one coalesced pass.
+            for (uint32_t u = threadIdx.x; u < kBM * wk; u += blockDim.x)
             {
+                const uint32_t r = u / wk, w = u % wk, row = m0 + r;
+                sBM[r * bm_stride + w] = row < net.batch ? src[static_cast<size_t>(row) * wk + w] : 0u;
+            }
+            __syncthreads();
+            uint32_t issued = 0;
+            for (uint32_t c = 0; c < n_chunks && ok; ++c)
+            {
+                const uint32_t buf = c % kABufs;
+                uint8_t *a = sA + static_cast<size_t>(buf) * kBM * kBK * 2;
+                if (c >= kABufs)
+                {
+                    // The MMAs that last read this buffer (chunk c - kABufs) must have completed.
+                    const bool waited = tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1u, kWaitLimit);
+                    tc::fence_after_sync();
+                    if (!waited) ok = false;
+                }
+                const uint32_t k0 = c * kBK;
                 const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - k0);
+                // Expand 0/1 bits to BF16 (1.0 = 0x3F80): unit (row r, 8-input group g); rows vary
+                // fastest so that 8 consecutive lanes fill one 128-byte core matrix.
                 for (uint32_t u = threadIdx.x; u < kBM * (kc / 8); u += blockDim.x)
                 {
-                    const uint32_t r = u / (kc / 8), g = u % (kc / 8), row = m0 + r, k = k0 + g * 8;
-                    uint32_t byte = 0;
-                    if (row < net.batch && k < K) byte = (src[static_cast<size_t>(row) * wk + (k >> 5)] >> (k & 31)) & 0xFFu;
+                    const uint32_t r = u % kBM, g = u / kBM, k = k0 + g * 8;
+                    const uint32_t byte = (sBM[r * bm_stride + (k >> 5)] >> (k & 31)) & 0xFFu;
                     uint32_t h[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
-                        h[e] = (((byte >> (2 * e)) & 1u) ? 0x3F80u : 0u) | (((byte >> (2 * e + 1)) & 1u) ? 0x3F800000u : 0u);
-                    *reinterpret_cast<uint4 *>(sA + tc::core_offset(r, g * 8, 128, sbo_a)) = make_uint4(h[0], h[1], h[2], h[3]);
+                        h[e] = (((byte >> (2 * e)) & 1u) ? 0x3F80u : 0u) |
+                               (((byte >> (2 * e + 1)) & 1u) ? 0x3F800000u : 0u);
+                    *reinterpret_cast<uint4 *>(a + tc::core_offset(r, g * 8, 128, sbo_a)) =
+                        make_uint4(h[0], h[1], h[2], h[3]);
                 }
                 tc::fence_async_smem();
-                __syncthreads();
+                ok = __syncthreads_and(ok ? 1 : 0) != 0;
+                if (!ok) break;
                 if (threadIdx.x == 0)
                 {
                     tc::fence_after_sync();
                     for (uint32_t j = 0; j < kc / 16; ++j)
                     {
-                        const uint64_t da = tc::smem_desc(tc::smem_u32(sA) + j * 256, 128, sbo_a);
+                        const uint64_t da = tc::smem_desc(tc::smem_u32(a) + j * 256, 128, sbo_a);
                         const uint64_t db = tc::smem_desc(tc::smem_u32(sW) + (k0 / 8 + 2 * j) * 128, 128, sbo_w);
-                        tc::mma_bf16(tmem, da, db, idesc, (k0 > 0 || j > 0) ? 1u : 0u);
+                        tc::mma_bf16(tmem, da, db, idesc, (c > 0 || j > 0) ? 1u : 0u);
                     }
-                    tc::commit(&mbar);
+                    tc::commit(&mbar[buf]);
                 }
-                const bool waited = tc::mbar_wait(&mbar, phase, kWaitLimit);
-                phase ^= 1u;
-                tc::fence_after_sync();
-                ok = __syncthreads_and(waited ? 1 : 0) != 0;
+                ++uses[buf];
+                ++issued;
             }
-            // Epilogue: warps 0-3 take columns 0-15, warps 4-7 columns 16-31 of rows 32 (warp % 4) + lane.
-            const uint32_t r = 32u * (warp & 3) + lane;
-            const uint32_t row = m0 + r;
-            const uint32_t cb = 16u * (warp >> 2);
-            float acc[16];
-            tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + cb, acc);
-            uint32_t mask = 0;
-            if (row < b_act && ok)
+            // Wait for the commits not waited for yet (the last min(issued, kABufs) chunks), also
+            // after a failed wait, so that no MMA is in flight when the kernel leaves.
             {
-                const int li = layer - 1;
-                const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
-                const uint32_t per = net.refract[li];
-                float *Vr = net.V[li] + static_cast<size_t>(row) * N;
-                uint32_t *Rr = net.rc[li] + static_cast<size_t>(row) * N;
-#pragma unroll
-                for (int i = 0; i < 16; ++i)
+                bool waited = true;
+                for (uint32_t c = (issued > kABufs ? issued - kABufs : 0); c < issued; ++c)
                 {
-                    const uint32_t n = n0 + cb + i;
-                    if (n >= N) break;
-                    float v = Vr[n];
-                    uint32_t c = Rr[n];
-                    if (c == 0u)
+                    const uint32_t buf = c % kABufs;
+                    waited = tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1u, kWaitLimit) && waited;
+                }
+                tc::fence_after_sync();
+                ok = waited && ok;
+            }
+            ok = __syncthreads_and(ok ? 1 : 0) != 0;
+            uint32_t mask = 0;
+            if (ok)
+            {
+                float acc[16];
+                tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + cb, acc);
+                if (erow < b_act)
+                {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
                     {
-                        v = __fadd_rn(__fmul_rn(v, leak), acc[i]);
-                        if (v > thr)
+                        if (n0 + cb + i >= N) break;
+                        // lif_impl.h:33-86: leak and input only outside the refractory period;
+                        // strict '>'; reset to a value.
+                        if (RC[i] == 0u)
                         {
-                            v = rst;
-                            c = per;
-                            mask |= 1u << (cb + i);
+                            const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
+                            if (v > thr)
+                            {
+                                V[i] = rst;
+                                RC[i] = per;
+                                mask |= 1u << (cb + i);
+                                ++CNT[i];
+                            }
+                            else
+                            {
+                                V[i] = v;
+                            }
+                        }
+                        else
+                        {
+                            --RC[i];
                         }
                     }
-                    else
-                    {
-                        --c;
-                    }
-                    Vr[n] = v;
-                    Rr[n] = c;
-                }
-                if (mask && layer == net.n_layers)
-                {
-                    const uint32_t smp = net.perm[row];
-                    for (int i = 0; i < 16; ++i)
-                        if (mask & (1u << (cb + i))) atomicAdd(net.counts + static_cast<size_t>(smp) * N + n0 + cb + i, 1);
                 }
             }
-            if (mask) atomicOr(&sbits[r], mask);
+            if (mask) atomicOr(&sbits[er], mask);
+            tc::fence_before_sync();
             __syncthreads();
             if (threadIdx.x < kBM)
             {
@@ -378,7 +433,6 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     if (bw && fan_out) atomicAdd(&s_events, static_cast<unsigned long long>(__popc(bw)) * fan_out);
                 }
             }
-            tc::fence_before_sync();
         }
         // Input spikes of step t (layer 0), shared by all CTAs.
         {
@@ -397,11 +451,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     {
                         const uint32_t i = wi * 32 + e;
                         if (i >= n_in) break;
-                        const float rate = net.rates[static_cast<size_t>(smp) * n_in + i];
-                        const unsigned long long thr =
-                            static_cast<unsigned long long>(static_cast<double>(rate) * 9007199254740992.0);
+                        const unsigned long long thr64 = net.rate_thr[static_cast<size_t>(smp) * n_in + i];
                         const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
-                        if ((rand64(net.key, ctr) >> 11) < thr) word |= 1u << e;
+                        if ((rand64(net.key, ctr) >> 11) < thr64) word |= 1u << e;
                     }
                     if (net.record) net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
                     if (word) atomicAdd(&s_events, static_cast<unsigned long long>(__popc(word)) * net.size[1]);
@@ -414,6 +466,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         __threadfence();
         if (!grid_sync(net.barrier, gridDim.x, 1u << 26)) ok = false;
         tc::fence_after_sync();
+    }
+    // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
+    if (layer == net.n_layers && erow < net.batch)
+    {
+        const uint32_t smp = net.perm[erow];
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+            if (n0 + cb + i < N) net.counts[static_cast<size_t>(smp) * N + n0 + cb + i] = CNT[i];
     }
     if (!ok && threadIdx.x == 0) atomicOr(net.err, 1u);
     tc::fence_before_sync();
@@ -469,7 +529,8 @@ int batched_lif_run(
                 net.item_n[n_items] = static_cast<uint16_t>(n);
                 ++n_items;
             }
-        smem = std::max<size_t>(smem, static_cast<size_t>(kBN) * net.kpad[l] * 2 + kBM * kBK * 2);
+        smem = std::max<size_t>(smem, static_cast<size_t>(kBN) * net.kpad[l] * 2 + kABufs * kBM * kBK * 2 +
+                                          kBM * (net.words[l - 1] | 1u) * 4);
     }
     net.n_items = n_items;
     int device = 0, sms = 0, per_sm = 0;
@@ -497,7 +558,6 @@ int batched_lif_run(
     net.t_max = st[0];
     net.batch = batch;
     net.key = key;
-    net.rates = rates;
     net.counts = counts;
     for (int l = 0; l < n_layers; ++l)
     {
@@ -523,11 +583,10 @@ int batched_lif_run(
     for (int l = 0; l <= n_layers && ok; ++l)
         for (int p = 0; p < 2 && ok; ++p)
             ok = (net.bits[l][p] = static_cast<uint32_t *>(dalloc(static_cast<size_t>(batch) * net.words[l] * 4)));
-    for (int l = 0; l < n_layers && ok; ++l)
-    {
-        ok = (net.V[l] = static_cast<float *>(dalloc(static_cast<size_t>(batch) * net.size[l + 1] * 4))) &&
-             (net.rc[l] = static_cast<uint32_t *>(dalloc(static_cast<size_t>(batch) * net.size[l + 1] * 4)));
-    }
+    unsigned long long *d_thr =
+        static_cast<unsigned long long *>(dalloc(static_cast<size_t>(batch) * sizes[0] * sizeof(unsigned long long)));
+    ok = ok && d_thr;
+    net.rate_thr = d_thr;
     net.events = static_cast<unsigned long long *>(dalloc(8));
     net.err = static_cast<unsigned int *>(dalloc(4));
     net.barrier = static_cast<unsigned int *>(dalloc(8));
@@ -554,6 +613,8 @@ int batched_lif_run(
         }
         net.rec_stride = off;
         if (record) cudaMemsetAsync(record, 0, static_cast<size_t>(net.t_max) * off * 4, s);
+        const size_t n_thr = static_cast<size_t>(batch) * sizes[0];
+        rate_threshold_kernel<<<static_cast<unsigned>((n_thr + 255) / 256), 256, 0, s>>>(rates, d_thr, n_thr);
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);

@@ -104,6 +104,7 @@ Backend::~Backend()
     for (auto &c : channels_)
         if (c->owns_generated && c->idx) cudaFree(c->idx);
     if (pinned_) cudaFreeHost(pinned_);
+    if (rec_host_) cudaFreeHost(rec_host_);
     if (pinned_free_) cudaEventDestroy(pinned_free_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -298,21 +299,16 @@ void Backend::record_spikes(const Uid &pop, bool enable)
     if (initialized_)
     {
         drain_recordings();
-        if (enable && !p->log)
+        if (enable && !p->rec_bits)
         {
-            const uint64_t per = std::max<uint64_t>(p->n, 1);
-            const uint64_t steps = std::max<uint64_t>(1, std::min<uint64_t>(hist_steps_, (1ull << 26) / per));
-            p->log_cap = steps * per;
-            p->log = arena_.make<uint32_t>(p->log_cap, false);
-            p->log_fill = arena_.make<unsigned long long>(1);
-            p->bdev.log_fill = p->ldev.log_fill = p->log_fill;
-            p->bdev.log_cap = p->ldev.log_cap = p->log_cap;
-            any_recording_ = true;
+            alloc_recording(*p);
+            p->bdev.rec_words = p->ldev.rec_words = p->rec_words;
+            p->bdev.rec_slots = p->ldev.rec_slots = p->rec_slots;
         }
         p->record = enable;
         p->record_from = step_;
-        p->bdev.log = enable ? p->log : nullptr;
-        p->ldev.log = enable ? p->log : nullptr;
+        p->bdev.rec_bits = enable ? p->rec_bits : nullptr;
+        p->ldev.rec_bits = enable ? p->rec_bits : nullptr;
         capture_graphs();
         return;
     }
@@ -402,12 +398,7 @@ void Backend::build_population(PopulationSlot &p)
     uint32_t *count = counters_ + p.counter_index;
     if (p.record)
     {
-        const uint64_t per = std::max<uint64_t>(n, 1);
-        const uint64_t steps = std::max<uint64_t>(1, std::min<uint64_t>(hist_steps_, (1ull << 26) / per));
-        p.log_cap = steps * per;
-        p.log = arena_.make<uint32_t>(p.log_cap, false);
-        p.log_fill = arena_.make<unsigned long long>(1);
-        any_recording_ = true;
+        alloc_recording(p);
         p.record_from = 0;
     }
 
@@ -461,9 +452,9 @@ void Backend::build_population(PopulationSlot &p)
         }
         d.spikes = spikes;
         d.spike_count = count;
-        d.log = p.record ? p.log : nullptr;
-        d.log_fill = p.log_fill;
-        d.log_cap = p.log_cap;
+        d.rec_bits = p.record ? p.rec_bits : nullptr;
+        d.rec_words = p.rec_words;
+        d.rec_slots = p.rec_slots;
         d.ring = rg;
         return;
     }
@@ -630,9 +621,9 @@ void Backend::build_population(PopulationSlot &p)
     }
     d.spikes = spikes;
     d.spike_count = count;
-    d.log = p.record ? p.log : nullptr;
-    d.log_fill = p.log_fill;
-    d.log_cap = p.log_cap;
+    d.rec_bits = p.record ? p.rec_bits : nullptr;
+    d.rec_words = p.rec_words;
+    d.rec_slots = p.rec_slots;
     d.ring = rg;
 }
 
@@ -907,8 +898,6 @@ void Backend::init()
     for (auto &p : projs_)
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) ++n_counters_;
     counters_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
-    hist_ = arena_.make<uint32_t>(static_cast<size_t>(hist_steps_) * std::max<uint32_t>(n_spike_counters_, 1));
-    hist_base_ = arena_.make<unsigned long long>(1);
     for (uint32_t i = 0; i < pops_.size(); ++i) pops_[i]->counter_index = i;
     neurons_total_ = 0;
     for (auto &q : pops_)
@@ -968,7 +957,7 @@ void Backend::enqueue_step()
         for (auto &[src, both] : p->stdp_sources) launch_stdp_append(p->stdp, src, both, ctl_, stream_);
         launch_stdp_modify(p->stdp, ctl_, stream_);
     }
-    StepEnd e{counters_, n_counters_, n_spike_counters_, hist_, hist_base_, hist_steps_};
+    StepEnd e{counters_, n_counters_, n_spike_counters_};
     launch_step_end(e, ctl_, stream_);
 }
 
@@ -994,10 +983,9 @@ void Backend::capture_graphs()
 
 uint64_t Backend::steps_before_drain() const
 {
-    uint64_t room = hist_steps_ - (step_ - hist_base_host_);
+    uint64_t room = ~0ull;
     for (auto &q : pops_)
-        if (q->record && q->log)
-            room = std::min<uint64_t>(room, q->log_cap / std::max<uint32_t>(q->n, 1) - (step_ - hist_base_host_));
+        if (q->record && q->rec_bits) room = std::min<uint64_t>(room, q->rec_slots - (step_ - drained_to_));
     return room;
 }
 
@@ -1172,7 +1160,7 @@ void Backend::profile_phases(uint64_t n, float *ms)
             launch_stdp_modify(p->stdp, ctl_, stream_);
         }
         KNP_CUDA(cudaEventRecord(ev[3], stream_));
-        StepEnd e{counters_, n_counters_, n_spike_counters_, hist_, hist_base_, hist_steps_};
+        StepEnd e{counters_, n_counters_, n_spike_counters_};
         launch_step_end(e, ctl_, stream_);
         KNP_CUDA(cudaEventRecord(ev[4], stream_));
         KNP_CUDA(cudaEventSynchronize(ev[4]));
@@ -1199,41 +1187,66 @@ void Backend::check_device_error()
                                                  (c.error & kErrLogOverflow ? " (spike recording overflow)" : ""));
 }
 
+void Backend::alloc_recording(PopulationSlot &p)
+{
+    // Up to 4096 steps between drains, at most 64 MB of bitmaps per population.
+    p.rec_words = std::max<uint32_t>((p.n + 31) / 32, 1);
+    p.rec_slots = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(4096, (16ull << 20) / p.rec_words)));
+    p.rec_bits = arena_.make<uint32_t>(static_cast<size_t>(p.rec_words) * p.rec_slots);
+    any_recording_ = true;
+}
+
+// Copies the recorded bitmaps of steps [drained_to_, step_) to the host and turns each into its
+// ascending spike indexes (the order of the reference's SpikeMessage, populations_old.h:104-118).
 void Backend::drain_recordings()
 {
-    KNP_CUDA(cudaStreamSynchronize(stream_));
-    const uint64_t steps = step_ - hist_base_host_;
+    const uint64_t steps = step_ - drained_to_;
     if (steps)
     {
-        std::vector<uint32_t> hist(steps * n_spike_counters_);
-        KNP_CUDA(cudaMemcpy(hist.data(), hist_, hist.size() * 4, cudaMemcpyDeviceToHost));
+        size_t need = 0;
+        for (auto &q : pops_)
+            if (q->record && q->rec_bits) need = std::max<size_t>(need, static_cast<size_t>(steps) * q->rec_words);
+        if (need > rec_host_words_)
+        {
+            KNP_CUDA(cudaStreamSynchronize(stream_));
+            if (rec_host_) KNP_CUDA(cudaFreeHost(rec_host_));
+            rec_host_ = nullptr;
+            size_t cap = 0;
+            for (auto &q : pops_)
+                if (q->rec_bits) cap = std::max<size_t>(cap, static_cast<size_t>(q->rec_slots) * q->rec_words);
+            KNP_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&rec_host_), cap * 4, cudaHostAllocDefault));
+            rec_host_words_ = cap;
+        }
         for (auto &q : pops_)
         {
-            if (!q->record || !q->log) continue;
-            unsigned long long fill = 0;
-            KNP_CUDA(cudaMemcpy(&fill, q->log_fill, 8, cudaMemcpyDeviceToHost));
-            std::vector<uint32_t> data(fill);
-            if (fill) KNP_CUDA(cudaMemcpy(data.data(), q->log, fill * 4, cudaMemcpyDeviceToHost));
-            uint64_t off = 0;
-            for (uint64_t s = 0; s < steps; ++s)
+            if (!q->record || !q->rec_bits) continue;
+            // The steps occupy ring slots drained_to_ % slots ... (step_ - 1) % slots: one or two spans.
+            const uint64_t first = drained_to_ % q->rec_slots;
+            const uint64_t span1 = std::min<uint64_t>(steps, q->rec_slots - first);
+            const size_t W = q->rec_words;
+            KNP_CUDA(cudaMemcpyAsync(rec_host_, q->rec_bits + first * W, span1 * W * 4, cudaMemcpyDeviceToHost,
+                                     stream_));
+            if (span1 < steps)
+                KNP_CUDA(cudaMemcpyAsync(rec_host_ + span1 * W, q->rec_bits, (steps - span1) * W * 4,
+                                         cudaMemcpyDeviceToHost, stream_));
+            KNP_CUDA(cudaStreamSynchronize(stream_));
+            for (uint64_t k = 0; k < steps; ++k)
             {
-                const uint32_t c = hist[s * n_spike_counters_ + q->counter_index];
-                const uint64_t step = hist_base_host_ + s;
-                if (off + c > fill) throw Error(KNP_GB300_E_DEVICE_FLAG, "spike recording log is inconsistent");
-                if (step >= q->record_from)
-                {
-                    std::vector<uint32_t> v(data.begin() + off, data.begin() + off + c);
-                    std::sort(v.begin(), v.end());
-                    q->recorded[step] = std::move(v);
-                }
-                off += c;
+                const uint64_t step = drained_to_ + k;
+                if (step < q->record_from) continue;
+                const uint32_t *bits = rec_host_ + k * W;
+                size_t c = 0;
+                for (size_t w = 0; w < W; ++w) c += static_cast<size_t>(__builtin_popcount(bits[w]));
+                std::vector<uint32_t> v;
+                v.reserve(c);
+                for (size_t w = 0; w < W; ++w)
+                    for (uint32_t x = bits[w]; x; x &= x - 1)
+                        v.push_back(static_cast<uint32_t>(w * 32 + __builtin_ctz(x)));
+                q->recorded[step] = std::move(v);
             }
-            KNP_CUDA(cudaMemset(q->log_fill, 0, 8));
         }
     }
-    hist_base_host_ = step_;
-    unsigned long long hb = step_;
-    KNP_CUDA(cudaMemcpy(hist_base_, &hb, 8, cudaMemcpyHostToDevice));
+    drained_to_ = step_;
     check_device_error();
 }
 
@@ -1244,7 +1257,7 @@ void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t 
     if (!q) throw Error(KNP_GB300_E_INVALID, "unknown population");
     if (!q->record) throw Error(KNP_GB300_E_STATE, "spike recording is not enabled for this population");
     if (step >= step_) throw Error(KNP_GB300_E_INVALID, "step has not been run yet");
-    if (step >= hist_base_host_) drain_recordings();
+    if (step >= drained_to_) drain_recordings();
     auto it = q->recorded.find(step);
     if (it == q->recorded.end()) throw Error(KNP_GB300_E_INVALID, "spikes of this step were not recorded or were discarded");
     *n = static_cast<uint32_t>(it->second.size());

@@ -88,9 +88,9 @@ struct PopulationSlot
     LifDev ldev{};
     RingView ring{};
     uint32_t counter_index = 0;
-    uint32_t *log = nullptr;
-    unsigned long long *log_fill = nullptr;  // device
-    unsigned long long log_cap = 0;
+    // spike recording: ring of rec_slots per-step bitmaps on the device (see BlifatDev)
+    uint32_t *rec_bits = nullptr;
+    uint32_t rec_words = 0, rec_slots = 0;
     bool has_external_impacts = false;
     // recorded spikes drained to the host: per step, ascending indexes
     std::map<uint64_t, std::vector<uint32_t>> recorded;
@@ -223,7 +223,7 @@ private:
     void stage_host_inputs();
     void drain_recordings();
     void check_device_error();
-    void ensure_record_capacity(uint64_t n_steps);
+    void alloc_recording(PopulationSlot &p);
     uint64_t steps_before_drain() const;
 
     int device_ = 0;
@@ -241,10 +241,10 @@ private:
     Control *ctl_ = nullptr;
     uint32_t *counters_ = nullptr;  // per-step counters
     uint32_t n_counters_ = 0, n_spike_counters_ = 0;
-    uint32_t *hist_ = nullptr;
-    unsigned long long *hist_base_ = nullptr;
-    uint32_t hist_steps_ = 4096;
-    uint64_t hist_base_host_ = 0;
+    uint64_t drained_to_ = 0;  // recorded steps before this one have been copied to the host
+    // pinned host buffer that recorded bitmaps are drained through
+    uint32_t *rec_host_ = nullptr;
+    size_t rec_host_words_ = 0;
     uint64_t neurons_total_ = 0;
     uint64_t updates_before_init_ = 0;
     cudaGraphExec_t graph1_ = nullptr, graphK_ = nullptr;

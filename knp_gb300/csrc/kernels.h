@@ -113,9 +113,10 @@ struct BlifatDev
     // outputs
     uint32_t *spikes;
     uint32_t *spike_count;  // this step
-    uint32_t *log;          // spike recording, or null
-    unsigned long long *log_fill;
-    unsigned long long log_cap;
+    // Spike recording, or null: a ring of rec_slots per-step bitmaps of rec_words words each; step t
+    // writes slot t % rec_slots completely (bit i of word i / 32 = neuron i fired).
+    uint32_t *rec_bits;
+    uint32_t rec_words, rec_slots;
     RingView ring;
 };
 
@@ -128,9 +129,8 @@ struct LifDev
     ParamU refract_period;
     uint32_t *spikes;
     uint32_t *spike_count;
-    uint32_t *log;
-    unsigned long long *log_fill;
-    unsigned long long log_cap;
+    uint32_t *rec_bits;  // spike recording ring, as for BlifatDev
+    uint32_t rec_words, rec_slots;
     RingView ring;
 };
 
@@ -215,9 +215,6 @@ struct StepEnd
     uint32_t *zero_u32;       // per-step counters to zero
     uint32_t n_zero_u32;
     uint32_t n_spike_counts;  // the first n_spike_counts counters are population spike counts
-    uint32_t *hist;           // per-step copy of the spike counts: hist[(step - *hist_base) * n_spike_counts + k]
-    const unsigned long long *hist_base;
-    uint32_t hist_steps;      // capacity in steps
 };
 
 // ---------------------------------------------------------------- launchers (stream-ordered)

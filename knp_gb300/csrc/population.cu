@@ -41,16 +41,26 @@ __device__ __forceinline__ float &at(float4 &v, int k) { return reinterpret_cast
 __device__ __forceinline__ uint32_t &at(uint4 &v, int k) { return reinterpret_cast<uint32_t *>(&v)[k]; }
 
 // Append this thread's spikes (bit k of mask = neuron i0 + k) to list[*count ...] with one atomic
-// per block; indexes stay ascending within a block. Optionally also appends to a recording log.
+// per block; indexes stay ascending within a block. With a recording slot `rec` (rec_words words),
+// also writes the step's spike bitmap: the 8 lanes of an aligned lane group cover 32 consecutive
+// neurons, so OR-ing their 4-bit masks gives one whole word, stored by the group's first lane.
+// Every thread of the block calls this (threads past the population with mask 0).
 __device__ __forceinline__ void emit_spikes(
-    uint32_t mask, uint32_t i0, uint32_t *list, uint32_t *count, uint32_t *log, unsigned long long *log_fill,
-    unsigned long long log_cap, Control *ctl)
+    uint32_t mask, uint32_t i0, uint32_t *list, uint32_t *count, uint32_t *rec, uint32_t rec_words)
 {
     __shared__ uint32_t warp_tot[kBlock / 32];
     __shared__ uint32_t block_base;
-    __shared__ unsigned long long log_base;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    if (rec)
+    {
+        uint32_t v = mask << (4 * (lane & 7));
+        v |= __shfl_xor_sync(0xffffffffu, v, 1);
+        v |= __shfl_xor_sync(0xffffffffu, v, 2);
+        v |= __shfl_xor_sync(0xffffffffu, v, 4);
+        const uint32_t word = i0 >> 5;
+        if ((lane & 7) == 0 && word < rec_words) rec[word] = v;
+    }
     const uint32_t c = __popc(mask);
     uint32_t incl = c;
 #pragma unroll
@@ -71,22 +81,19 @@ __device__ __forceinline__ void emit_spikes(
             run += x;
         }
         block_base = run ? atomicAdd(count, run) : 0u;
-        log_base = (run && log) ? atomicAdd(log_fill, static_cast<unsigned long long>(run)) : 0ull;
-        if (run && log && log_base + run > log_cap) atomicOr(&ctl->error, kErrLogOverflow);
     }
     __syncthreads();
     if (!c) return;
-    const uint32_t off = warp_tot[warp] + incl - c;
-    uint32_t pos = block_base + off;
-    unsigned long long lpos = log_base + off;
+    uint32_t pos = block_base + warp_tot[warp] + incl - c;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        if (mask & (1u << k))
-        {
-            list[pos++] = i0 + k;
-            if (log && lpos < log_cap) log[lpos] = i0 + k;
-            ++lpos;
-        }
+        if (mask & (1u << k)) list[pos++] = i0 + k;
+}
+
+__device__ __forceinline__ uint32_t *record_slot(uint32_t *rec_bits, uint32_t rec_words, uint32_t rec_slots,
+                                                 unsigned long long t)
+{
+    return rec_bits ? rec_bits + static_cast<size_t>(t % rec_slots) * rec_words : nullptr;
 }
 
 struct NeuronState
@@ -374,7 +381,8 @@ __global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ct
         (void)ns_old;
         if (f & kLiveBurst) st4u(p.burst_phase, i0, phase);
     }
-    emit_spikes(mask, i0, p.spikes, p.spike_count, p.log, p.log_fill, p.log_cap, ctl);
+    emit_spikes(mask, i0, p.spikes, p.spike_count, record_slot(p.rec_bits, p.rec_words, p.rec_slots, t),
+                p.rec_words);
 }
 
 __global__ void __launch_bounds__(kBlock) lif_kernel(LifDev p, Control *ctl)
@@ -421,7 +429,8 @@ __global__ void __launch_bounds__(kBlock) lif_kernel(LifDev p, Control *ctl)
         st4(p.V, i0, V);
         st4u(p.refract, i0, rc);
     }
-    emit_spikes(mask, i0, p.spikes, p.spike_count, p.log, p.log_fill, p.log_cap, ctl);
+    emit_spikes(mask, i0, p.spikes, p.spike_count, record_slot(p.rec_bits, p.rec_words, p.rec_slots, t),
+                p.rec_words);
 }
 
 __global__ void apply_impacts_kernel(

@@ -123,16 +123,9 @@ __global__ void step_end_kernel(StepEnd e, uint32_t n_spike_counts, Control *ctl
     __shared__ unsigned long long spikes;
     if (threadIdx.x == 0) spikes = 0;
     __syncthreads();
-    const unsigned long long rel = ctl->step - *e.hist_base;
-    if (rel >= e.hist_steps && threadIdx.x == 0) atomicOr(&ctl->error, kErrLogOverflow);
     for (uint32_t k = threadIdx.x; k < e.n_zero_u32; k += blockDim.x)
     {
-        if (k < n_spike_counts)
-        {
-            const uint32_t c = e.zero_u32[k];
-            atomicAdd(&spikes, static_cast<unsigned long long>(c));
-            if (rel < e.hist_steps) e.hist[rel * n_spike_counts + k] = c;
-        }
+        if (k < n_spike_counts) atomicAdd(&spikes, static_cast<unsigned long long>(e.zero_u32[k]));
         e.zero_u32[k] = 0;
     }
     __syncthreads();

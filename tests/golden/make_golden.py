@@ -6,6 +6,11 @@ KNP sources are present). Run from the repository root:
 
 Each case stores, per step, the spike count and the CRC32 of the ascending spike indexes of the
 network's first population, the total synaptic event count, and CRC32s of final projection weights.
+
+`python tests/golden/make_golden.py --full` also writes tests/golden/stdp_full.json for the full STDP
+learning config (200 samples x 100 steps; about two minutes of CPU): per sample the spike count and
+a CRC32 over that sample's per-step digests, the final plastic weights' CRC32, and every 613th final
+weight (for the relative-error check).
 """
 import json
 import os
@@ -34,8 +39,37 @@ def digest(trains):
     return [[int(s.size), zlib.crc32(np.ascontiguousarray(s, np.uint32).tobytes())] for s in trains]
 
 
+def sample_digest(trains, steps_per_sample):
+    """Per sample: [spike count, CRC32 of the concatenated per-step (count, CRC32) pairs]."""
+    d = np.asarray(digest(trains), np.uint64).astype(np.uint32)
+    out = []
+    for s0 in range(0, len(trains), steps_per_sample):
+        blk = d[s0:s0 + steps_per_sample]
+        out.append([int(blk[:, 0].sum()), zlib.crc32(np.ascontiguousarray(blk).tobytes())])
+    return out
+
+
+def full_stdp():
+    kwargs = {"seed": 3, "samples": 200, "steps_per_sample": 100}
+    net, sched = N.stdp_network(**kwargs)
+    steps = 200 * 100
+    res, o = orc.run(net, sched, steps, which="reference")
+    pop = net.populations[0].uid
+    w = o.weights(net.projections[0].uid)
+    case = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "builder": "stdp_network",
+            "kwargs": kwargs, "steps": steps, "events": o.events,
+            "samples": sample_digest(res[pop], 100), "weights_crc": zlib.crc32(w.tobytes()),
+            "weights_stride": 613, "weights_sampled": [float(x) for x in w[::613]]}
+    with open(os.path.join(ROOT, "tests", "golden", "stdp_full.json"), "w") as f:
+        json.dump(case, f, separators=(",", ":"))
+    print("stdp_full", "spikes", sum(s.size for s in res[pop]), "events", o.events)
+
+
 def main():
     orc.build("reference", knp_ref=os.environ.get("KNP_REF", "/root/reference"))
+    if "--full" in sys.argv:
+        full_stdp()
+        return
     out = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "cases": []}
     for name, builder, kwargs, steps, wproj in CASES:
         net, sched = getattr(N, builder)(**kwargs)

@@ -207,6 +207,34 @@ def test_stdp_reduced():
     assert_same_state(b, oo, net.populations[0].uid)
 
 
+def test_stdp_full_config_against_fixture():
+    """The full STDP learning config (200 samples x 100 steps, 784 -> 800 additive STDP + lateral
+    inhibition) against tests/golden/stdp_full.json, written from the reference-header oracle: every
+    sample's spike digest, the event count, the final plastic weights bit-exact (CRC32) and, as the
+    config's stated bar, every sampled weight within 1e-5 relative."""
+    import json
+    import os
+    import zlib
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stdp_full.json")) as f:
+        case = json.load(f)
+    net, sched = N.__dict__[case["builder"]](**case["kwargs"])
+    B = _gpu()
+    g, b = B.run(net, sched, case["steps"], device_schedule=True)
+    pop = net.populations[0].uid
+    d = np.asarray([[s.size, zlib.crc32(np.ascontiguousarray(s, np.uint32).tobytes())] for s in g[pop]],
+                   np.uint64).astype(np.uint32)
+    samples = [[int(d[s:s + 100, 0].sum()), zlib.crc32(np.ascontiguousarray(d[s:s + 100]).tobytes())]
+               for s in range(0, case["steps"], 100)]
+    assert samples == case["samples"]
+    w = b.read_weights(net.projections[0].uid)
+    ws = w[::case["weights_stride"]].astype(np.float64)
+    ref = np.asarray(case["weights_sampled"], np.float64)
+    np.testing.assert_allclose(ws, ref, rtol=1e-5, atol=0)
+    assert zlib.crc32(w.tobytes()) == case["weights_crc"]
+    assert b.counters()[0] == case["events"]
+
+
 def test_external_impacts_and_channels():
     """External SynapticImpactMessages of every supported type into a BLIFAT population with
     non-default dynamics; potentials within 1e-5 relative of the FP64 oracle."""

@@ -90,6 +90,22 @@ def test_oracle_against_golden_fixtures(oracle_lib):
         assert o.events == case["events"], case["name"]
 
 
+def sample_digest(trains, steps_per_sample):
+    """Per sample: [spike count, CRC32 of the concatenated per-step (count, CRC32) pairs]."""
+    d = np.asarray(spike_digest(trains), np.uint64).astype(np.uint32)
+    return [[int(d[s:s + steps_per_sample, 0].sum()), zlib.crc32(np.ascontiguousarray(d[s:s + steps_per_sample]).tobytes())]
+            for s in range(0, len(trains), steps_per_sample)]
+
+
+def test_oracle_against_full_stdp_fixture(oracle_lib):
+    """The first 4 samples of the full STDP learning config (fixture written from the
+    reference-header oracle over all 200 samples) reproduce with the restated oracle."""
+    case = load_golden("stdp_full.json")
+    net, sched = N.__dict__[case["builder"]](**case["kwargs"])
+    out, _ = orc.run(net, sched, 400)
+    assert sample_digest(out[net.populations[0].uid], 100) == case["samples"][:4]
+
+
 @pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
 @pytest.mark.parametrize("seed", [11, 12])
 def test_restated_oracle_matches_reference_headers(oracle_lib, seed):
