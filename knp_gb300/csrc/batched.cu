@@ -158,7 +158,10 @@ namespace knp_gb300
 namespace
 {
 
-constexpr int kBM = 128, kBN = 32, kBK = 128, kABufs = 2, kMaxLayers = 4, kMaxItems = 512;
+constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
+constexpr int kRoundChunks = 2;                   // K chunks expanded between two block barriers
+constexpr int kABufs = 2 * kRoundChunks;          // A chunk buffers: two rounds in flight
+constexpr int kInCache = 8;                       // input words per warp whose draw thresholds stay in registers
 constexpr int kBatchThreads = 256;
 
 struct BatchedNet
@@ -171,8 +174,8 @@ struct BatchedNet
     float leak[kMaxLayers], thr[kMaxLayers], reset[kMaxLayers];
     uint32_t refract[kMaxLayers];
     uint32_t batch;
-    const uint32_t *perm;   // slot -> sample
-    const uint32_t *steps;  // T per slot, non-increasing
+    const uint32_t *perm;  // slot -> sample
+    const uint32_t *act;   // [t_max]: slots still running at step t (slots sorted by decreasing T)
     const unsigned long long *rate_thr;  // [batch][size[0]] by sample: rate * 2^53, the draw's threshold
     unsigned long long key;
     uint32_t t_max;
@@ -220,21 +223,6 @@ __device__ __forceinline__ bool grid_sync(unsigned int *bar, unsigned int n_bloc
     return ok_s != 0;
 }
 
-__device__ __forceinline__ uint32_t active_slots(const uint32_t *steps, uint32_t batch, uint32_t t)
-{
-    // steps is non-increasing: count of slots with steps > t.
-    uint32_t lo = 0, hi = batch;
-    while (lo < hi)
-    {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (steps[mid] > t)
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
 // Per (sample, input): the 53-bit threshold that the input draw is compared with.
 __global__ void rate_threshold_kernel(const float *rates, unsigned long long *thr, size_t n)
 {
@@ -242,11 +230,18 @@ __global__ void rate_threshold_kernel(const float *rates, unsigned long long *th
     if (i < n) thr[i] = static_cast<unsigned long long>(static_cast<double>(rates[i]) * 9007199254740992.0);
 }
 
+__device__ __forceinline__ void cp_async4(uint32_t *dst, const uint32_t *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t mbar[kABufs];
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
     const uint32_t item = blockIdx.x;
@@ -275,7 +270,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     }
     if (warp == 0) tc::tmem_alloc(&tmem_slot, 32);
     if (threadIdx.x == 0)
-        for (int i = 0; i < kABufs; ++i) tc::mbar_init(&mbar[i], 1);
+    {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        s_events = 0;
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -283,10 +282,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
     const uint32_t fan_out = layer < net.n_layers ? net.size[layer + 1] : 0u;
     const uint32_t n_chunks = (Kp + kBK - 1) / kBK;
-    uint32_t uses[kABufs];  // commits made on each A buffer's mbarrier so far
-#pragma unroll
-    for (int i = 0; i < kABufs; ++i) uses[i] = 0;
+    uint32_t uses[2] = {0, 0};  // commits made on each round mbarrier so far
     bool ok = true;
+    unsigned long long my_events = 0;
 
     // Epilogue ownership, fixed for the run: thread (warp, lane) owns row 32 (warp % 4) + lane of the
     // tile and columns 16 (warp / 4) .. +15, so it keeps their LIF state in registers.
@@ -307,42 +305,71 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
     const uint32_t per = net.refract[li];
 
+    // Input words this warp draws every step (u = warp id + j * warps in grid) and, for the first
+    // kInCache of them, this lane's draw threshold and sample, kept in registers for the run.
+    const uint32_t n_in = net.size[0], w0 = net.words[0];
+    const uint64_t in_total = static_cast<uint64_t>(net.batch) * w0;
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * wpb + warp, nw = static_cast<uint64_t>(gridDim.x) * wpb;
+    unsigned long long in_thr[kInCache];
+    uint32_t in_smp[kInCache];
+#pragma unroll
+    for (int j = 0; j < kInCache; ++j)
+    {
+        const uint64_t u = gw + j * nw;
+        in_thr[j] = 0;
+        in_smp[j] = 0;
+        if (u < in_total)
+        {
+            const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
+            in_smp[j] = net.perm[slot];
+            if (i < n_in) in_thr[j] = net.rate_thr[static_cast<size_t>(in_smp[j]) * n_in + i];
+        }
+    }
+
+    uint32_t b_next = net.act[0];
     for (uint32_t t = 0; t < net.t_max && ok; ++t)
     {
-        const uint32_t b_act = active_slots(net.steps, net.batch, t);
+        const uint32_t b_act = b_next;
+        if (t + 1 < net.t_max) b_next = net.act[t + 1];  // used next step; the load overlaps this one
         const uint32_t *src = net.bits[layer - 1][(t + 1) & 1];
         uint32_t *dst = net.bits[layer][t & 1];
-        if (threadIdx.x == 0) s_events = 0;
         if (threadIdx.x < kBM) sbits[threadIdx.x] = 0;
-        __syncthreads();
         if (m0 < b_act)
         {
-            // This tile's rows of the previous layer's spike bitmap (step t - 1), one coalesced pass.
+            // This tile's rows of the previous layer's spike bitmap (step t - 1): asynchronous 4-byte
+            // copies, all in flight at once.
             for (uint32_t u = threadIdx.x; u < kBM * wk; u += blockDim.x)
             {
                 const uint32_t r = u / wk, w = u % wk, row = m0 + r;
-                sBM[r * bm_stride + w] = row < net.batch ? src[static_cast<size_t>(row) * wk + w] : 0u;
+                if (row < net.batch)
+                    cp_async4(sBM + r * bm_stride + w, src + static_cast<size_t>(row) * wk + w);
+                else
+                    sBM[r * bm_stride + w] = 0u;
             }
+            cp_async_wait_all();
             __syncthreads();
-            uint32_t issued = 0;
-            for (uint32_t c = 0; c < n_chunks && ok; ++c)
+            uint32_t rounds = 0;
+            for (uint32_t c0 = 0; c0 < n_chunks && ok; c0 += kRoundChunks, ++rounds)
             {
-                const uint32_t buf = c % kABufs;
-                uint8_t *a = sA + static_cast<size_t>(buf) * kBM * kBK * 2;
-                if (c >= kABufs)
+                const uint32_t c1 = min(c0 + kRoundChunks, n_chunks);
+                const uint32_t pr = rounds & 1u;
+                if (rounds >= 2)
                 {
-                    // The MMAs that last read this buffer (chunk c - kABufs) must have completed.
-                    const bool waited = tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1u, kWaitLimit);
+                    // The MMAs of round `rounds - 2` read these buffers; they must have completed.
+                    const bool waited = tc::mbar_wait(&mbar[pr], (uses[pr] - 1) & 1u, kWaitLimit);
                     tc::fence_after_sync();
                     if (!waited) ok = false;
                 }
-                const uint32_t k0 = c * kBK;
-                const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - k0);
-                // Expand 0/1 bits to BF16 (1.0 = 0x3F80): unit (row r, 8-input group g); rows vary
-                // fastest so that 8 consecutive lanes fill one 128-byte core matrix.
-                for (uint32_t u = threadIdx.x; u < kBM * (kc / 8); u += blockDim.x)
+                // Expand 0/1 bits to BF16 (1.0 = 0x3F80): unit (row r, 8-input group g of the round);
+                // rows vary fastest so that 8 consecutive lanes fill one 128-byte core matrix.
+                const uint32_t groups = (min(c1 * kBK, Kp) - c0 * kBK) / 8;
+                for (uint32_t u = threadIdx.x; u < kBM * groups; u += blockDim.x)
                 {
-                    const uint32_t r = u % kBM, g = u / kBM, k = k0 + g * 8;
+                    const uint32_t r = u % kBM, gg = u / kBM;
+                    const uint32_t k = c0 * kBK + gg * 8;
+                    const uint32_t c = k / kBK, g = (k % kBK) / 8;
+                    uint8_t *a = sA + static_cast<size_t>(c % kABufs) * kBM * kBK * 2;
                     const uint32_t byte = (sBM[r * bm_stride + (k >> 5)] >> (k & 31)) & 0xFFu;
                     uint32_t h[4];
 #pragma unroll
@@ -358,26 +385,27 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 if (threadIdx.x == 0)
                 {
                     tc::fence_after_sync();
-                    for (uint32_t j = 0; j < kc / 16; ++j)
+                    for (uint32_t c = c0; c < c1; ++c)
                     {
-                        const uint64_t da = tc::smem_desc(tc::smem_u32(a) + j * 256, 128, sbo_a);
-                        const uint64_t db = tc::smem_desc(tc::smem_u32(sW) + (k0 / 8 + 2 * j) * 128, 128, sbo_w);
-                        tc::mma_bf16(tmem, da, db, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                        const uint8_t *a = sA + static_cast<size_t>(c % kABufs) * kBM * kBK * 2;
+                        const uint32_t k0 = c * kBK, kc = min(static_cast<uint32_t>(kBK), Kp - k0);
+                        for (uint32_t j = 0; j < kc / 16; ++j)
+                        {
+                            const uint64_t da = tc::smem_desc(tc::smem_u32(a) + j * 256, 128, sbo_a);
+                            const uint64_t db = tc::smem_desc(tc::smem_u32(sW) + (k0 / 8 + 2 * j) * 128, 128, sbo_w);
+                            tc::mma_bf16(tmem, da, db, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                        }
                     }
-                    tc::commit(&mbar[buf]);
+                    tc::commit(&mbar[pr]);
                 }
-                ++uses[buf];
-                ++issued;
+                ++uses[pr];
             }
-            // Wait for the commits not waited for yet (the last min(issued, kABufs) chunks), also
-            // after a failed wait, so that no MMA is in flight when the kernel leaves.
+            // Wait for the commits not waited for yet (the last min(rounds, 2) rounds), also after a
+            // failed wait, so that no MMA is in flight when the kernel leaves.
             {
                 bool waited = true;
-                for (uint32_t c = (issued > kABufs ? issued - kABufs : 0); c < issued; ++c)
-                {
-                    const uint32_t buf = c % kABufs;
-                    waited = tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1u, kWaitLimit) && waited;
-                }
+                for (uint32_t q = (rounds > 2 ? rounds - 2 : 0); q < rounds; ++q)
+                    waited = tc::mbar_wait(&mbar[q & 1u], (uses[q & 1u] - 1) & 1u, kWaitLimit) && waited;
                 tc::fence_after_sync();
                 ok = waited && ok;
             }
@@ -430,39 +458,60 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     if (net.record && rw < b_act)
                         net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[rw]) * wn +
                                    (n0 >> 5)] = bw;
-                    if (bw && fan_out) atomicAdd(&s_events, static_cast<unsigned long long>(__popc(bw)) * fan_out);
+                    my_events += static_cast<unsigned long long>(__popc(bw)) * fan_out;
                 }
             }
         }
-        // Input spikes of step t (layer 0), shared by all CTAs.
+        // Input spikes of step t (layer 0), spread over every warp of the grid: a warp makes one
+        // 32-input word per iteration, one draw per lane, combined by a ballot.
         {
-            const uint32_t n_in = net.size[0], w0 = net.words[0];
-            const uint64_t total = static_cast<uint64_t>(net.batch) * w0;
             uint32_t *d0 = net.bits[0][t & 1];
-            for (uint64_t u = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; u < total;
-                 u += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+            uint32_t j = 0;
+            for (uint64_t u = gw; u < in_total; u += nw, ++j)
             {
                 const uint32_t slot = static_cast<uint32_t>(u / w0), wi = static_cast<uint32_t>(u % w0);
-                uint32_t word = 0;
+                const uint32_t i = wi * 32 + lane;
+                bool bit = false;
+                uint32_t smp = 0;
                 if (slot < b_act)
                 {
-                    const uint32_t smp = net.perm[slot];
-                    for (int e = 0; e < 32; ++e)
+                    unsigned long long thr64;
+                    if (j < kInCache)
                     {
-                        const uint32_t i = wi * 32 + e;
-                        if (i >= n_in) break;
-                        const unsigned long long thr64 = net.rate_thr[static_cast<size_t>(smp) * n_in + i];
-                        const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
-                        if ((rand64(net.key, ctr) >> 11) < thr64) word |= 1u << e;
+                        // Registers indexed by a loop counter: select with a fixed unrolled scan.
+                        thr64 = 0;
+#pragma unroll
+                        for (int q = 0; q < kInCache; ++q)
+                            if (q == static_cast<int>(j))
+                            {
+                                thr64 = in_thr[q];
+                                smp = in_smp[q];
+                            }
                     }
-                    if (net.record) net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
-                    if (word) atomicAdd(&s_events, static_cast<unsigned long long>(__popc(word)) * net.size[1]);
+                    else
+                    {
+                        smp = net.perm[slot];
+                        thr64 = i < n_in ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull;
+                    }
+                    if (i < n_in)
+                    {
+                        const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
+                        bit = (rand64(net.key, ctr) >> 11) < thr64;
+                    }
                 }
-                d0[u] = word;
+                const uint32_t word = __ballot_sync(0xffffffffu, bit);
+                if (lane == 0)
+                {
+                    d0[u] = word;
+                    if (slot < b_act)
+                    {
+                        if (net.record)
+                            net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
+                        my_events += static_cast<unsigned long long>(__popc(word)) * net.size[1];
+                    }
+                }
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
         __threadfence();
         if (!grid_sync(net.barrier, gridDim.x, 1u << 26)) ok = false;
         tc::fence_after_sync();
@@ -475,9 +524,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         for (int i = 0; i < 16; ++i)
             if (n0 + cb + i < N) net.counts[static_cast<size_t>(smp) * N + n0 + cb + i] = CNT[i];
     }
+    if (my_events) atomicAdd(&s_events, my_events);
     if (!ok && threadIdx.x == 0) atomicOr(net.err, 1u);
     tc::fence_before_sync();
     __syncthreads();
+    if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
     if (warp == 0) tc::tmem_dealloc(tmem, 32);
 }
 
@@ -533,9 +584,15 @@ int batched_lif_run(
                                           kBM * (net.words[l - 1] | 1u) * 4);
     }
     net.n_items = n_items;
-    int device = 0, sms = 0, per_sm = 0;
+    int device = 0, sms = 0, per_sm = 0, smem_max = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (smem > static_cast<size_t>(smem_max))
+    {
+        *why = "a layer's weight tile and staging buffers exceed the shared memory of one CTA (fan-in too large)";
+        return -1;
+    }
     cudaError_t err = cudaFuncSetAttribute(batched_lif_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(smem));
     if (err == cudaSuccess)
@@ -578,8 +635,8 @@ int batched_lif_run(
     };
     bool ok = true;
     uint32_t *d_perm = static_cast<uint32_t *>(dalloc(batch * 4));
-    uint32_t *d_steps = static_cast<uint32_t *>(dalloc(batch * 4));
-    ok = ok && d_perm && d_steps;
+    uint32_t *d_act = static_cast<uint32_t *>(dalloc(static_cast<size_t>(net.t_max) * 4));
+    ok = ok && d_perm && d_act;
     for (int l = 0; l <= n_layers && ok; ++l)
         for (int p = 0; p < 2 && ok; ++p)
             ok = (net.bits[l][p] = static_cast<uint32_t *>(dalloc(static_cast<size_t>(batch) * net.words[l] * 4)));
@@ -600,10 +657,17 @@ int batched_lif_run(
     else
     {
         cudaMemcpyAsync(d_perm, perm.data(), batch * 4, cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(d_steps, st.data(), batch * 4, cudaMemcpyHostToDevice, s);
+        // act[t] = slots with T > t (slots are sorted by decreasing T).
+        std::vector<uint32_t> act(net.t_max);
+        for (uint32_t t = 0, a = batch; t < net.t_max; ++t)
+        {
+            while (a > 0 && st[a - 1] <= t) --a;
+            act[t] = a;
+        }
+        cudaMemcpyAsync(d_act, act.data(), act.size() * 4, cudaMemcpyHostToDevice, s);
         cudaMemsetAsync(counts, 0, static_cast<size_t>(batch) * net.size[n_layers] * 4, s);
         net.perm = d_perm;
-        net.steps = d_steps;
+        net.act = d_act;
         net.record = record;
         unsigned long long off = 0;
         for (int l = 0; l <= n_layers; ++l)

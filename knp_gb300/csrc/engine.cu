@@ -378,7 +378,10 @@ void Backend::build_population(PopulationSlot &p)
     rg.fixed = fixed ? 1 : 0;
     const size_t cells = static_cast<size_t>(slots) * np;
     if (fixed)
+    {
         rg.v64 = arena_.make<long long>(cells);
+        rg.v64lo = arena_.make<long long>(cells);
+    }
     else
         rg.v32 = arena_.make<float>(cells);
     const bool res = p.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT;

@@ -5,8 +5,10 @@
 //               field; parameters either broadcast (uniform across the population) or SoA arrays.
 //   input ring  [slots][n_pad] accumulators of postsynaptic input, slot = step mod slots, with
 //               slots = the largest delay into the population. FP32 (exact for dyadic weights) or
-//               int64 fixed point with 40 fractional bits (order-independent). Optional rings for
-//               conductance / dopamine input and a forcing bitmap for resource-STDP neurons.
+//               two-word fixed point (order-independent, exact for every FP32 weight that is a
+//               multiple of 2^-48 while the sum stays below 2^54): a high word in units of 2^-8 and
+//               a low word in units of 2^-48 per neuron. Optional rings for conductance / dopamine
+//               input and a forcing bitmap for resource-STDP neurons.
 //   projection  presynaptic-major CSR: row_ptr int64[n_pre + 1], col int32[S], weight fp32[S],
 //               delay u8[S], optional per-synapse output type u8[S]; STDP projections add a
 //               postsynaptic-major index (col_ptr, CSR positions) and per-column spike histories.
@@ -22,7 +24,7 @@
 namespace knp_gb300
 {
 
-constexpr int kFxShift = 40;  // fixed-point input: value * 2^40 in int64
+constexpr int kFxLoBits = 40;  // fixed-point input: value = hi * 2^-8 + lo * 2^-48
 constexpr int kMaxSources = 8;
 
 // Bits of Control::error.
@@ -47,9 +49,10 @@ struct RingView
     uint32_t n;      // neurons
     uint32_t pitch;  // elements per slot row (multiple of 4)
     uint32_t slots;  // ring length
-    int fixed;       // 0: v32, 1: v64
+    int fixed;       // 0: v32, 1: v64 + v64lo
     float *v32;
-    long long *v64;
+    long long *v64;    // fixed point, sums of high words (units of 2^-8)
+    long long *v64lo;  // fixed point, sums of low words (units of 2^-48, each addend in [0, 2^40])
     float *g;          // conductance input, or null
     float *dopa;       // dopamine input, or null
     uint32_t *forced;  // forcing bitmap [slots][words], or null
@@ -253,6 +256,128 @@ cudaError_t gen_bernoulli_schedule(
     uint64_t n_steps, long long *d_offsets, uint32_t **d_idx, uint64_t *n_idx, cudaStream_t s);
 
 // Counter-based generator shared with knp_gb300/network.py (SplitMix64 finaliser).
+// ---------------------------------------------------------------- two-word fixed point
+// An FP32 value w = s * m * 2^e (m < 2^24) is W = w * 2^48 = H * 2^40 + L with 0 <= L < 2^40: exact
+// when w is a multiple of 2^-48 (every FP32 value of magnitude >= 2^-24 is), else rounded to the
+// nearest multiple; |w| >= 2^54 saturates. Sums of H and of L over any order give the same exact
+// total, which fx_normalize brings back to H * 2^40 + L form.
+__host__ __device__ inline void fx_split(float w, long long &hi, long long &lo)
+{
+    uint32_t b;
+    static_assert(sizeof(float) == sizeof(uint32_t), "32-bit float");
+#ifdef __CUDA_ARCH__
+    b = __float_as_uint(w);
+#else
+    __builtin_memcpy(&b, &w, 4);
+#endif
+    const int ex = static_cast<int>((b >> 23) & 0xFFu);
+    unsigned long long m = b & 0x7FFFFFu;
+    int e = -149;
+    if (ex != 0)
+    {
+        m |= 0x800000u;
+        e = ex - 150;
+    }
+    const unsigned long long mask = (1ull << kFxLoBits) - 1;
+    const int s = e + 48;  // W = m * 2^s
+    unsigned long long H = 0, L = 0;
+    if (s >= 0)
+    {
+        if (s <= kFxLoBits)
+        {
+            const unsigned long long v = m << s;  // < 2^64
+            H = v >> kFxLoBits;
+            L = v & mask;
+        }
+        else if (s - kFxLoBits <= 38)
+        {
+            H = m << (s - kFxLoBits);
+        }
+        else
+        {
+            H = 1ull << 62;
+        }
+    }
+    else if (s > -26)
+    {
+        // Below 2^-48: round m * 2^s to nearest, ties to even.
+        const int r = -s;
+        const unsigned long long q = m >> r, rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+        L = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    }
+    if (b >> 31)
+    {
+        if (L)
+        {
+            hi = -static_cast<long long>(H) - 1;
+            lo = static_cast<long long>((1ull << kFxLoBits) - L);
+        }
+        else
+        {
+            hi = -static_cast<long long>(H);
+            lo = 0;
+        }
+    }
+    else
+    {
+        hi = static_cast<long long>(H);
+        lo = static_cast<long long>(L);
+    }
+}
+
+// Bring (hi, lo) with lo >= 0 back to 0 <= lo < 2^40.
+__host__ __device__ inline void fx_normalize(long long &hi, long long &lo)
+{
+    hi += lo >> kFxLoBits;
+    lo &= (1ll << kFxLoBits) - 1;
+}
+
+#ifdef __CUDACC__
+// Correctly rounded FP32 value of hi * 2^-8 + lo * 2^-48 (0 <= lo < 2^40).
+__device__ __forceinline__ float fx_to_float(long long hi, long long lo)
+{
+    const bool neg = hi < 0;
+    unsigned long long H = static_cast<unsigned long long>(hi), L = static_cast<unsigned long long>(lo);
+    if (neg)
+    {
+        if (L)
+        {
+            H = ~H;  // -hi - 1
+            L = (1ull << kFxLoBits) - L;
+        }
+        else
+        {
+            H = 0ull - H;
+        }
+    }
+    // Magnitude H * 2^40 + L as the 128-bit integer u1:u0.
+    const unsigned long long u1 = H >> (64 - kFxLoBits), u0 = (H << kFxLoBits) | L;
+    float f;
+    if (u1 == 0)
+    {
+        f = __fmul_rn(__ull2float_rn(u0), 3.5527136788005009e-15f);  // 2^-48
+    }
+    else
+    {
+        const int lz = __clzll(static_cast<long long>(u1));
+        const int sh = 64 - lz;  // bits of u0 below the 64-bit window
+        const unsigned long long top = (u1 << lz) | (sh == 64 ? 0ull : (u0 >> sh));
+        const unsigned long long sticky = (sh == 64 ? u0 : (u0 & ((1ull << sh) - 1))) != 0 ? 1ull : 0ull;
+        f = __fmul_rn(__ull2float_rn(top | sticky), __int_as_float((127 + sh - 48) << 23));
+    }
+    return neg ? -f : f;
+}
+
+// Adds an FP32 impact to a two-word fixed-point accumulator.
+__device__ __forceinline__ void fx_atomic_add(long long *hi, long long *lo, size_t o, float w)
+{
+    long long h, l;
+    fx_split(w, h, l);
+    if (h) atomicAdd(reinterpret_cast<unsigned long long *>(hi + o), static_cast<unsigned long long>(h));
+    if (l) atomicAdd(reinterpret_cast<unsigned long long *>(lo + o), static_cast<unsigned long long>(l));
+}
+#endif
+
 __host__ __device__ inline unsigned long long mix64(unsigned long long x)
 {
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;

@@ -18,20 +18,10 @@ namespace knp_gb300
 namespace
 {
 
-constexpr float kFxScale = 1099511627776.0f;  // 2^40
-constexpr float kFxInv = 9.094947017729282e-13f;  // 2^-40
 constexpr int kBlock = 256;
 
 __device__ __forceinline__ float pf(const ParamF &p, uint32_t i) { return p.a ? p.a[i] : p.u; }
 __device__ __forceinline__ uint32_t pu(const ParamU &p, uint32_t i) { return p.a ? p.a[i] : p.u; }
-
-// Exact fixed-point image of x when |x| < 2^22 (the low bits below 2^-40 are rounded).
-__device__ __forceinline__ bool to_fx(float x, long long &out)
-{
-    if (!(fabsf(x) < 4194304.0f)) return false;
-    out = __float2ll_rn(__fmul_rn(x, kFxScale));
-    return true;
-}
 
 __device__ __forceinline__ float4 ld4(const float *p, uint32_t i) { return *reinterpret_cast<const float4 *>(p + i); }
 __device__ __forceinline__ void st4(float *p, uint32_t i, float4 v) { *reinterpret_cast<float4 *>(p + i) = v; }
@@ -104,11 +94,11 @@ struct NeuronState
 };
 
 // One BLIFAT neuron for one step. `acc` is this step's summed EXCITATORY - INHIBITORY_CURRENT input
-// (FP32 ring) and `acc64` the same in fixed point (fixed ring).
+// (FP32 ring) and (acc_hi, acc_lo) the same in two-word fixed point (fixed ring).
 template <bool kFixed>
 __device__ __forceinline__ bool blifat_step(
-    const BlifatDev &p, uint32_t i, unsigned long long t, NeuronState &s, float acc, long long acc64, float g_in,
-    float d_in)
+    const BlifatDev &p, uint32_t i, unsigned long long t, NeuronState &s, float acc, long long acc_hi,
+    long long acc_lo, float g_in, float d_in)
 {
     const uint32_t f = p.flags;
     const bool res = f & kResource;
@@ -126,22 +116,25 @@ __device__ __forceinline__ bool blifat_step(
     }
     s.V_pre = s.V;
     // ---- impacts (blifat_impl.h:68-107), pre-summed per channel
-    long long vfx = 0;
+    // Fixed point: the exact potential as vh * 2^-8 + vl * 2^-48; the spike test compares it with the
+    // threshold exactly, and the stored potential is its correctly rounded FP32 value.
+    long long vh = 0, vl = 0;
     bool fx_ok = false;
     if (kFixed)
     {
-        if (s.V_pre == 0.0f)
+        vh = acc_hi;
+        vl = acc_lo;
+        fx_normalize(vh, vl);
+        if (s.V_pre != 0.0f)
         {
-            vfx = acc64;
-            fx_ok = true;
+            long long ph, pl;
+            fx_split(s.V_pre, ph, pl);
+            vh += ph;
+            vl += pl;
+            fx_normalize(vh, vl);
         }
-        else
-        {
-            long long pfx;
-            fx_ok = to_fx(s.V_pre, pfx);
-            vfx = pfx + acc64;
-        }
-        s.V = fx_ok ? __fmul_rn(__ll2float_rn(vfx), kFxInv) : __fadd_rn(s.V_pre, __fmul_rn(__ll2float_rn(acc64), kFxInv));
+        fx_ok = true;
+        s.V = fx_to_float(vh, vl);
     }
     else
     {
@@ -179,11 +172,16 @@ __device__ __forceinline__ bool blifat_step(
     const float thr_total = __fadd_rn(__fadd_rn(pf(p.thr, i), s.thr_dyn), s.add_thr);
     const bool ref_ok = (f & kLiveRefract) ? (s.ns > pu(p.t_ref, i)) : (t > 0);
     bool above;
-    long long thr_fx;
-    if (kFixed && fx_ok && to_fx(thr_total, thr_fx))
-        above = vfx >= thr_fx;
+    if (kFixed && fx_ok)
+    {
+        long long th, tl;
+        fx_split(thr_total, th, tl);
+        above = vh > th || (vh == th && vl >= tl);
+    }
     else
+    {
         above = s.V >= thr_total;
+    }
     const bool spike = ref_ok && above;
     if (spike)
     {
@@ -285,17 +283,21 @@ __global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ct
         const uint32_t slot = static_cast<uint32_t>(t % rg.slots);
         const size_t ro = static_cast<size_t>(slot) * rg.pitch + i0;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        long long acc64[4] = {0, 0, 0, 0};
+        long long acc_hi[4] = {0, 0, 0, 0}, acc_lo[4] = {0, 0, 0, 0};
         if (kFixed)
         {
             longlong2 *a = reinterpret_cast<longlong2 *>(rg.v64 + ro);
-            const longlong2 x = a[0], y = a[1];
-            acc64[0] = x.x;
-            acc64[1] = x.y;
-            acc64[2] = y.x;
-            acc64[3] = y.y;
-            a[0] = make_longlong2(0, 0);
-            a[1] = make_longlong2(0, 0);
+            longlong2 *b = reinterpret_cast<longlong2 *>(rg.v64lo + ro);
+            const longlong2 x = a[0], y = a[1], xl = b[0], yl = b[1];
+            acc_hi[0] = x.x;
+            acc_hi[1] = x.y;
+            acc_hi[2] = y.x;
+            acc_hi[3] = y.y;
+            acc_lo[0] = xl.x;
+            acc_lo[1] = xl.y;
+            acc_lo[2] = yl.x;
+            acc_lo[3] = yl.y;
+            a[0] = a[1] = b[0] = b[1] = make_longlong2(0, 0);
         }
         else
         {
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ct
             s.ns = at(ns, k);
             s.phase = at(phase, k);
             s.block = (f & kLiveBlock) ? p.blocking[i] : 0;
-            const bool spike = blifat_step<kFixed>(p, i, t, s, at(acc, k), acc64[k], at(gin, k), at(din, k));
+            const bool spike = blifat_step<kFixed>(p, i, t, s, at(acc, k), acc_hi[k], acc_lo[k], at(gin, k), at(din, k));
             if (spike) mask |= 1u << k;
             if (f & kResource)
                 resource_step(p, i, t, spike, (forced_bits >> k) & 1u, s.dopa, s.add_thr);
@@ -448,8 +450,7 @@ __global__ void apply_impacts_kernel(
     {
         if (ty == 1) w = -w;
         if (ring.fixed)
-            atomicAdd(reinterpret_cast<unsigned long long *>(ring.v64 + o),
-                      static_cast<unsigned long long>(__float2ll_rn(__fmul_rn(w, kFxScale))));
+            fx_atomic_add(ring.v64, ring.v64lo, o, w);
         else
             atomicAdd(ring.v32 + o, w);
         if (ty == 0 && forcing && ring.forced)

@@ -5,7 +5,7 @@
 // knp/backends/cpu-library/impl/projections/delta/delta_impl.h:54-114): an impact created at step t
 // through delay d is sent at step t + d - 1 and applied by the population at step t + d; delay 0
 // lands on step t - 1, which has already been sent, so it is counted as an event and never applied.
-// Sums of impacts are order-independent (FP32 for dyadic weights, or 2^-40 fixed point), so the
+// Sums of impacts are order-independent (FP32 for dyadic weights, or two-word fixed point), so the
 // warp/atomic order of the scatter does not change results.
 //
 // Work distribution: persistent grid; each warp takes whole spike rows (row-major over the
@@ -20,7 +20,6 @@ namespace knp_gb300
 namespace
 {
 
-constexpr float kFxScale = 1099511627776.0f;  // 2^40
 
 __device__ __forceinline__ void resolve_source(
     const SpikeSource &s, unsigned long long t, const uint32_t *&idx, uint32_t &cnt)
@@ -60,8 +59,7 @@ __device__ __forceinline__ void deliver(
     {
         if (!kUniformExc && ty == 1) w = -w;
         if (kFixed)
-            atomicAdd(reinterpret_cast<unsigned long long *>(p.ring.v64 + o),
-                      static_cast<unsigned long long>(__float2ll_rn(__fmul_rn(w, kFxScale))));
+            fx_atomic_add(p.ring.v64, p.ring.v64lo, o, w);
         else
             atomicAdd(p.ring.v32 + o, w);
         if ((kUniformExc || ty == 0) && p.forcing && p.ring.forced)
