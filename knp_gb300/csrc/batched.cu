@@ -148,28 +148,40 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
 //
 // Each step is a BF16 GEMM of the 0/1 spike matrix (exact in BF16) against BF16 weights with FP32
 // accumulation in tensor memory. One CTA owns (layer, 128-sample tile, 32-neuron tile); its weight
-// tile stays in shared memory for the whole run. Spike matrices live in global memory as bitmaps
-// (double-buffered by step parity) and are expanded to BF16 0/1 in shared memory, 128 inputs at a
-// time. Samples are processed sorted by decreasing T, so finished samples leave whole M-tiles idle
-// ("compaction" by order). Steps are separated by a grid barrier; the kernel is launched
-// cooperatively (every CTA resident) and every wait is bounded.
+// tile stays in shared memory and its neurons' LIF state in registers for the whole run.
+//
+// Spike matrices are kept in global memory already in the layout the tensor cores read: for each
+// layer, step parity and 128-sample tile, the consumer's K range is cut into 128-input chunks of
+// 32 KB each in the canonical no-swizzle K-major form (8 x 16-byte core matrices). A producer CTA
+// writes its 128 x 32 block of 0/1 BF16 spikes there (512 16-byte stores), so a consumer needs no
+// conversion: a loader thread streams the chunks into a 4-stage shared-memory ring with bulk copies
+// (cp.async.bulk, completion on mbarriers), two issuer threads run the MMAs of alternate chunks
+// into separate accumulators, and the other warps draw the next step's input spikes meanwhile.
+// Samples are processed sorted by decreasing T, so finished samples leave whole M-tiles idle.
+// Steps are separated by a grid barrier; the kernel is launched cooperatively (every CTA resident)
+// and every wait is bounded.
 namespace knp_gb300
 {
 namespace
 {
 
 constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
-constexpr int kRoundChunks = 2;                   // K chunks expanded between two block barriers
-constexpr int kABufs = 2 * kRoundChunks;          // A chunk buffers: two rounds in flight
-constexpr int kInCache = 8;                       // input words per warp whose draw thresholds stay in registers
+constexpr int kIssuers = 2;                           // issuer q runs the MMAs of chunks c with c % 2 == q
+constexpr int kABufs = 5;                             // A chunk ring stages
+constexpr uint32_t kChunkBytes = kBM * kBK * 2;       // one 128 x 128 BF16 chunk
+constexpr uint32_t kSboA = (kBK / 8) * 128;           // row-group stride of a chunk (16 core matrices)
+constexpr int kLoaderWarp = kIssuers;                 // lane 0 of this warp streams the chunks
+constexpr int kFirstDrawWarp = kLoaderWarp + 1;       // warps from here on draw the input spikes
+constexpr int kInCache = 12;                          // input words per drawing warp with cached thresholds
 constexpr int kBatchThreads = 256;
 
 struct BatchedNet
 {
     int n_layers;
     uint32_t size[kMaxLayers + 1];
-    uint32_t words[kMaxLayers + 1];  // ceil(size / 32)
-    uint32_t kpad[kMaxLayers + 1];   // kpad[l] = size[l - 1] rounded up to 16
+    uint32_t words[kMaxLayers + 1];   // ceil(size / 32)
+    uint32_t kpad[kMaxLayers + 1];    // kpad[l] = size[l - 1] rounded up to 16 (layer l's K)
+    uint32_t chunks[kMaxLayers + 1];  // chunks[l] = ceil(kpad[l] / 128)
     const __nv_bfloat16 *w[kMaxLayers];
     float leak[kMaxLayers], thr[kMaxLayers], reset[kMaxLayers];
     uint32_t refract[kMaxLayers];
@@ -179,44 +191,45 @@ struct BatchedNet
     const unsigned long long *rate_thr;  // [batch][size[0]] by sample: rate * 2^53, the draw's threshold
     unsigned long long key;
     uint32_t t_max;
-    uint32_t *bits[kMaxLayers + 1][2];  // [batch][words[l]] per step parity
-    int *counts;                         // [batch][size[L]] by sample
-    uint32_t *record;                    // [t_max][sum_l batch * words[l]] by sample, or null
+    // spk[l][p]: spikes of layer l (l < n_layers) at steps of parity p, as layer l + 1's A operand:
+    // [m tile][chunks[l + 1]][kChunkBytes].
+    uint8_t *spk[kMaxLayers][2];
+    int *counts;           // [batch][size[L]] by sample
+    uint32_t *record;      // [t_max][sum_l batch * words[l]] by sample, or null
     unsigned long long rec_off[kMaxLayers + 1];
     unsigned long long rec_stride;
     unsigned long long *events;
     unsigned int *err;
-    unsigned int *barrier;  // [0] arrivals, [1] generation
+    unsigned int *barrier;  // arrival counter of the grid barrier
     uint32_t n_items;
     uint16_t item_layer[kMaxItems];
     uint16_t item_m[kMaxItems];
     uint16_t item_n[kMaxItems];  // 32-neuron tile index
 };
 
-__device__ __forceinline__ bool grid_sync(unsigned int *bar, unsigned int n_blocks, uint32_t limit)
+// Grid barrier on a counter that only grows: arrival k (0-based) belongs to barrier k / n_blocks,
+// which completes when the counter reaches (k / n_blocks + 1) * n_blocks. One release add per CTA,
+// acquire polls (bounded) until then.
+__device__ __forceinline__ bool grid_sync(unsigned int *count, unsigned int n_blocks, uint32_t limit)
 {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0)
     {
-        volatile unsigned int *gen = bar + 1;
-        const unsigned int g = *gen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
-        int ok = 1;
-        if (arrived == n_blocks)
+        unsigned int old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
+        const unsigned int target = (old / n_blocks + 1) * n_blocks;
+        int ok = 0;
+        for (uint32_t i = 0; i < limit; ++i)
         {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+            unsigned int cur;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
+            if (static_cast<int>(cur - target) >= 0)
+            {
+                ok = 1;
+                break;
+            }
         }
-        else
-        {
-            uint32_t i = 0;
-            while (*gen == g && i < limit) ++i;
-            ok = *gen != g;
-        }
-        __threadfence();
         ok_s = ok;
     }
     __syncthreads();
@@ -230,32 +243,60 @@ __global__ void rate_threshold_kernel(const float *rates, unsigned long long *th
     if (i < n) thr[i] = static_cast<unsigned long long>(static_cast<double>(rates[i]) * 9007199254740992.0);
 }
 
-__device__ __forceinline__ void cp_async4(uint32_t *dst, const uint32_t *src)
+// Bulk copy global -> shared (both 16-byte aligned, size a multiple of 16) completing on `mbar`.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
 {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_u32(dst)), "l"(src) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     tc::smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(tc::smem_u32(mbar))
+                 : "memory");
 }
 
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(mbar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// The low 8 bits of x as eight BF16 values 0 or 1.0 (0x3F80), bit i -> element i.
+__device__ __forceinline__ uint4 bf16_bits(uint32_t x)
+{
+    uint4 v;
+    v.x = ((x & 1u) ? 0x3F80u : 0u) | ((x & 2u) ? 0x3F800000u : 0u);
+    v.y = ((x & 4u) ? 0x3F80u : 0u) | ((x & 8u) ? 0x3F800000u : 0u);
+    v.z = ((x & 16u) ? 0x3F80u : 0u) | ((x & 32u) ? 0x3F800000u : 0u);
+    v.w = ((x & 64u) ? 0x3F80u : 0u) | ((x & 128u) ? 0x3F800000u : 0u);
+    return v;
+}
+
+// Byte offset of element (row r, input k) of a layer's spike matrix inside one 128-sample tile.
+__device__ __forceinline__ uint32_t spk_offset(uint32_t r, uint32_t k)
+{
+    return (k / kBK) * kChunkBytes + (r >> 3) * kSboA + ((k % kBK) >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
 
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t full[kABufs];   // chunk in stage b has landed (loader's expect_tx)
+    __shared__ __align__(8) uint64_t empty[kABufs];  // MMAs that read stage b have completed (commit)
+    __shared__ __align__(8) uint64_t done[kIssuers]; // all of an issuer's MMAs of a step have completed
     __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
     const uint32_t item = blockIdx.x;
     const int layer = net.item_layer[item];  // 1..L
-    const uint32_t m0 = net.item_m[item] * kBM;
+    const uint32_t m_tile = net.item_m[item];
+    const uint32_t m0 = m_tile * kBM;
     const uint32_t n0 = net.item_n[item] * kBN;
     const uint32_t K = net.size[layer - 1], Kp = net.kpad[layer], N = net.size[layer];
-    const uint32_t wk = net.words[layer - 1], wn = net.words[layer];
-    const uint32_t bm_stride = wk | 1u;  // odd row stride: 32 consecutive rows hit 32 banks
-    // Shared memory: weight tile [kBN x Kp], kABufs A chunks [kBM x kBK], spike bitmap rows [kBM x bm_stride].
+    const uint32_t wn = net.words[layer];
+    const uint32_t n_chunks = net.chunks[layer];
+    // Shared memory: weight tile [kBN x Kp] (K-major core matrices), kABufs chunk stages.
     uint8_t *sW = smem;
     uint8_t *sA = smem + static_cast<size_t>(kBN) * Kp * 2;
-    uint32_t *sBM = reinterpret_cast<uint32_t *>(sA + static_cast<size_t>(kABufs) * kBM * kBK * 2);
-    const uint32_t sbo_w = (Kp / 8) * 128, sbo_a = (kBK / 8) * 128;
+    const uint32_t sbo_w = (Kp / 8) * 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     // Weight tile rows n0..n0+31 (zero beyond N), inputs 0..Kp (zero beyond K).
@@ -268,11 +309,16 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             tmp[e] = (n < N && k + e < K) ? net.w[layer - 1][static_cast<size_t>(n) * K + k + e] : __float2bfloat16(0.0f);
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, 32);
+    // Tensor memory: issuer q accumulates into columns [32 q, 32 q + 32).
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, 32 * kIssuers);
     if (threadIdx.x == 0)
     {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
+        for (int b = 0; b < kABufs; ++b)
+        {
+            tc::mbar_init(&full[b], 1);
+            tc::mbar_init(&empty[b], 1);
+        }
+        for (int q = 0; q < kIssuers; ++q) tc::mbar_init(&done[q], 1);
         s_events = 0;
     }
     tc::fence_before_sync();
@@ -281,8 +327,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
     const uint32_t fan_out = layer < net.n_layers ? net.size[layer + 1] : 0u;
-    const uint32_t n_chunks = (Kp + kBK - 1) / kBK;
-    uint32_t uses[2] = {0, 0};  // commits made on each round mbarrier so far
+    // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
+    // adding byte offsets / 16 to the start-address field.
+    const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
+    const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
+    uint32_t seq = 0;        // chunks streamed by this CTA in earlier steps (stage = seq % kABufs)
+    uint32_t act_steps = 0;  // steps this CTA has computed (phase of done[])
     bool ok = true;
     unsigned long long my_events = 0;
 
@@ -305,12 +355,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
     const uint32_t per = net.refract[li];
 
-    // Input words this warp draws every step (u = warp id + j * warps in grid) and, for the first
-    // kInCache of them, this lane's draw threshold and sample, kept in registers for the run.
+    // Input words drawn by this warp every step (drawing warps only: u = draw warp id + j * draw
+    // warps in grid) and, for the first kInCache of them, this lane's threshold and sample.
     const uint32_t n_in = net.size[0], w0 = net.words[0];
     const uint64_t in_total = static_cast<uint64_t>(net.batch) * w0;
-    const uint32_t wpb = blockDim.x >> 5;
-    const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * wpb + warp, nw = static_cast<uint64_t>(gridDim.x) * wpb;
+    const uint32_t dpb = (blockDim.x >> 5) - kFirstDrawWarp;
+    const bool drawer = warp >= kFirstDrawWarp;
+    const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * dpb + (warp - kFirstDrawWarp),
+                   nw = static_cast<uint64_t>(gridDim.x) * dpb;
     unsigned long long in_thr[kInCache];
     uint32_t in_smp[kInCache];
 #pragma unroll
@@ -319,102 +371,123 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint64_t u = gw + j * nw;
         in_thr[j] = 0;
         in_smp[j] = 0;
-        if (u < in_total)
+        if (drawer && u < in_total)
         {
             const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
             in_smp[j] = net.perm[slot];
             if (i < n_in) in_thr[j] = net.rate_thr[static_cast<size_t>(in_smp[j]) * n_in + i];
         }
     }
+    const size_t spk0_tile = static_cast<size_t>(net.chunks[1]) * kChunkBytes;
 
     uint32_t b_next = net.act[0];
     for (uint32_t t = 0; t < net.t_max && ok; ++t)
     {
         const uint32_t b_act = b_next;
         if (t + 1 < net.t_max) b_next = net.act[t + 1];  // used next step; the load overlaps this one
-        const uint32_t *src = net.bits[layer - 1][(t + 1) & 1];
-        uint32_t *dst = net.bits[layer][t & 1];
+        const bool active = m0 < b_act;
         if (threadIdx.x < kBM) sbits[threadIdx.x] = 0;
-        if (m0 < b_act)
+        if (active)
         {
-            // This tile's rows of the previous layer's spike bitmap (step t - 1): asynchronous 4-byte
-            // copies, all in flight at once.
-            for (uint32_t u = threadIdx.x; u < kBM * wk; u += blockDim.x)
+            const uint8_t *src = net.spk[layer - 1][(t + 1) & 1] + static_cast<size_t>(m_tile) * n_chunks * kChunkBytes;
+            if (warp == kLoaderWarp && lane == 0)
             {
-                const uint32_t r = u / wk, w = u % wk, row = m0 + r;
-                if (row < net.batch)
-                    cp_async4(sBM + r * bm_stride + w, src + static_cast<size_t>(row) * wk + w);
-                else
-                    sBM[r * bm_stride + w] = 0u;
-            }
-            cp_async_wait_all();
-            __syncthreads();
-            uint32_t rounds = 0;
-            for (uint32_t c0 = 0; c0 < n_chunks && ok; c0 += kRoundChunks, ++rounds)
-            {
-                const uint32_t c1 = min(c0 + kRoundChunks, n_chunks);
-                const uint32_t pr = rounds & 1u;
-                if (rounds >= 2)
+                // Loader: the chunks were written by other CTAs before the grid barrier (generic
+                // proxy); the bulk copies read them through the async proxy.
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                for (uint32_t c = 0; c < n_chunks; ++c)
                 {
-                    // The MMAs of round `rounds - 2` read these buffers; they must have completed.
-                    const bool waited = tc::mbar_wait(&mbar[pr], (uses[pr] - 1) & 1u, kWaitLimit);
-                    tc::fence_after_sync();
-                    if (!waited) ok = false;
+                    const uint32_t sq = seq + c, b = sq % kABufs;
+                    if (sq >= kABufs && !tc::mbar_wait(&empty[b], (sq / kABufs - 1) & 1u, kWaitLimit)) ok = false;
+                    mbar_arrive_expect_tx(&full[b], kChunkBytes);
+                    bulk_load(sA + static_cast<size_t>(b) * kChunkBytes, src + static_cast<size_t>(c) * kChunkBytes,
+                              kChunkBytes, &full[b]);
                 }
-                // Expand 0/1 bits to BF16 (1.0 = 0x3F80): unit (row r, 8-input group g of the round);
-                // rows vary fastest so that 8 consecutive lanes fill one 128-byte core matrix.
-                const uint32_t groups = (min(c1 * kBK, Kp) - c0 * kBK) / 8;
-                for (uint32_t u = threadIdx.x; u < kBM * groups; u += blockDim.x)
+            }
+            else if (warp < kIssuers && lane == 0)
+            {
+                // Issuer q: chunks q, q + 2, ... into its accumulator, then one commit for the step.
+                for (uint32_t c = warp; c < n_chunks; c += kIssuers)
                 {
-                    const uint32_t r = u % kBM, gg = u / kBM;
-                    const uint32_t k = c0 * kBK + gg * 8;
-                    const uint32_t c = k / kBK, g = (k % kBK) / 8;
-                    uint8_t *a = sA + static_cast<size_t>(c % kABufs) * kBM * kBK * 2;
-                    const uint32_t byte = (sBM[r * bm_stride + (k >> 5)] >> (k & 31)) & 0xFFu;
-                    uint32_t h[4];
+                    const uint32_t sq = seq + c, b = sq % kABufs;
+                    if (!tc::mbar_wait(&full[b], (sq / kABufs) & 1u, kWaitLimit)) ok = false;
+                    tc::fence_after_sync();
+                    const uint64_t da = dA0 + b * (kChunkBytes >> 4);
+                    const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
+                    const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - c * kBK);
+                    for (uint32_t j = 0; j < kc / 16; ++j)
+                        tc::mma_bf16(tmem + 32u * warp, da + j * 16, db + j * 16, idesc,
+                                     (c >= static_cast<uint32_t>(kIssuers) || j > 0) ? 1u : 0u);
+                    tc::commit(&empty[b]);
+                }
+                tc::commit(&done[warp]);
+            }
+        }
+        // Input spikes of step t (layer 0), drawn by the drawing warps of every CTA: a warp makes one
+        // 32-input word per item, one draw per lane. Each lane writes its BF16 0/1 into layer 1's A
+        // layout; the ballot gives the word for the record and the event count.
+        if (drawer)
+        {
+            uint8_t *d0 = net.spk[0][t & 1];
+            auto draw = [&](uint64_t u, unsigned long long thr64, uint32_t smp)
+            {
+                const uint32_t slot = static_cast<uint32_t>(u / w0), wi = static_cast<uint32_t>(u % w0);
+                const uint32_t i = wi * 32 + lane;
+                bool bit = false;
+                if (slot < b_act && i < n_in)
+                {
+                    const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
+                    bit = (rand64(net.key, ctr) >> 11) < thr64;
+                }
+                if (i < net.kpad[1])
+                    *reinterpret_cast<uint16_t *>(d0 + (slot / kBM) * spk0_tile + spk_offset(slot % kBM, i)) =
+                        bit ? 0x3F80u : 0u;
+                const uint32_t word = __ballot_sync(0xffffffffu, bit);
+                if (lane == 0 && slot < b_act)
+                {
+                    if (net.record)
+                        net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
+                    my_events += static_cast<unsigned long long>(__popc(word)) * net.size[1];
+                }
+            };
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        h[e] = (((byte >> (2 * e)) & 1u) ? 0x3F80u : 0u) |
-                               (((byte >> (2 * e + 1)) & 1u) ? 0x3F800000u : 0u);
-                    *reinterpret_cast<uint4 *>(a + tc::core_offset(r, g * 8, 128, sbo_a)) =
-                        make_uint4(h[0], h[1], h[2], h[3]);
-                }
-                tc::fence_async_smem();
-                ok = __syncthreads_and(ok ? 1 : 0) != 0;
-                if (!ok) break;
-                if (threadIdx.x == 0)
-                {
-                    tc::fence_after_sync();
-                    for (uint32_t c = c0; c < c1; ++c)
-                    {
-                        const uint8_t *a = sA + static_cast<size_t>(c % kABufs) * kBM * kBK * 2;
-                        const uint32_t k0 = c * kBK, kc = min(static_cast<uint32_t>(kBK), Kp - k0);
-                        for (uint32_t j = 0; j < kc / 16; ++j)
-                        {
-                            const uint64_t da = tc::smem_desc(tc::smem_u32(a) + j * 256, 128, sbo_a);
-                            const uint64_t db = tc::smem_desc(tc::smem_u32(sW) + (k0 / 8 + 2 * j) * 128, 128, sbo_w);
-                            tc::mma_bf16(tmem, da, db, idesc, (c > 0 || j > 0) ? 1u : 0u);
-                        }
-                    }
-                    tc::commit(&mbar[pr]);
-                }
-                ++uses[pr];
-            }
-            // Wait for the commits not waited for yet (the last min(rounds, 2) rounds), also after a
-            // failed wait, so that no MMA is in flight when the kernel leaves.
+            for (int j = 0; j < kInCache; ++j)
             {
-                bool waited = true;
-                for (uint32_t q = (rounds > 2 ? rounds - 2 : 0); q < rounds; ++q)
-                    waited = tc::mbar_wait(&mbar[q & 1u], (uses[q & 1u] - 1) & 1u, kWaitLimit) && waited;
-                tc::fence_after_sync();
-                ok = waited && ok;
+                const uint64_t u = gw + j * nw;
+                if (u < in_total) draw(u, in_thr[j], in_smp[j]);
             }
-            ok = __syncthreads_and(ok ? 1 : 0) != 0;
+            for (uint64_t u = gw + kInCache * nw; u < in_total; u += nw)
+            {
+                const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
+                const uint32_t smp = net.perm[slot];
+                draw(u, i < n_in ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp);
+            }
+        }
+        if (active)
+        {
+            // Every issuer commits done[] once per computed step; waiting for both means no MMA of
+            // this step is in flight.
+            bool waited = true;
+            for (int q = 0; q < kIssuers; ++q)
+                waited = tc::mbar_wait(&done[q], act_steps & 1u, kWaitLimit) && waited;
+            tc::fence_after_sync();
+            ok = __syncthreads_and((waited && ok) ? 1 : 0) != 0;
+            ++act_steps;
+            seq += n_chunks;
             uint32_t mask = 0;
             if (ok)
             {
+                // Sum of the issuers' accumulators (issuer q holds the chunks c with c % 2 == q).
                 float acc[16];
                 tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + cb, acc);
+                for (int q = 1; q < kIssuers; ++q)
+                {
+                    if (static_cast<uint32_t>(q) >= n_chunks) break;
+                    float part[16];
+                    tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + 32u * q + cb, part);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) acc[i] = __fadd_rn(acc[i], part[i]);
+                }
                 if (erow < b_act)
                 {
 #pragma unroll
@@ -445,74 +518,26 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     }
                 }
             }
+            // This thread's 16 spikes as the next layer's A operand (two 16-byte stores).
+            if (layer < net.n_layers && erow < net.batch)
+            {
+                uint8_t *d = net.spk[layer][t & 1] + static_cast<size_t>(m_tile) * net.chunks[layer + 1] * kChunkBytes;
+                const uint32_t k = n0 + cb;
+                *reinterpret_cast<uint4 *>(d + spk_offset(er, k)) = bf16_bits(mask >> cb);
+                *reinterpret_cast<uint4 *>(d + spk_offset(er, k + 8)) = bf16_bits(mask >> (cb + 8));
+            }
             if (mask) atomicOr(&sbits[er], mask);
+            my_events += static_cast<unsigned long long>(__popc(mask)) * fan_out;
             tc::fence_before_sync();
             __syncthreads();
-            if (threadIdx.x < kBM)
+            if (net.record && threadIdx.x < kBM)
             {
                 const uint32_t rr = threadIdx.x, rw = m0 + rr;
-                if (rw < net.batch)
-                {
-                    const uint32_t bw = sbits[rr];
-                    dst[static_cast<size_t>(rw) * wn + (n0 >> 5)] = bw;
-                    if (net.record && rw < b_act)
-                        net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[rw]) * wn +
-                                   (n0 >> 5)] = bw;
-                    my_events += static_cast<unsigned long long>(__popc(bw)) * fan_out;
-                }
+                if (rw < b_act)
+                    net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[rw]) * wn +
+                               (n0 >> 5)] = sbits[rr];
             }
         }
-        // Input spikes of step t (layer 0), spread over every warp of the grid: a warp makes one
-        // 32-input word per iteration, one draw per lane, combined by a ballot.
-        {
-            uint32_t *d0 = net.bits[0][t & 1];
-            uint32_t j = 0;
-            for (uint64_t u = gw; u < in_total; u += nw, ++j)
-            {
-                const uint32_t slot = static_cast<uint32_t>(u / w0), wi = static_cast<uint32_t>(u % w0);
-                const uint32_t i = wi * 32 + lane;
-                bool bit = false;
-                uint32_t smp = 0;
-                if (slot < b_act)
-                {
-                    unsigned long long thr64;
-                    if (j < kInCache)
-                    {
-                        // Registers indexed by a loop counter: select with a fixed unrolled scan.
-                        thr64 = 0;
-#pragma unroll
-                        for (int q = 0; q < kInCache; ++q)
-                            if (q == static_cast<int>(j))
-                            {
-                                thr64 = in_thr[q];
-                                smp = in_smp[q];
-                            }
-                    }
-                    else
-                    {
-                        smp = net.perm[slot];
-                        thr64 = i < n_in ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull;
-                    }
-                    if (i < n_in)
-                    {
-                        const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
-                        bit = (rand64(net.key, ctr) >> 11) < thr64;
-                    }
-                }
-                const uint32_t word = __ballot_sync(0xffffffffu, bit);
-                if (lane == 0)
-                {
-                    d0[u] = word;
-                    if (slot < b_act)
-                    {
-                        if (net.record)
-                            net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
-                        my_events += static_cast<unsigned long long>(__popc(word)) * net.size[1];
-                    }
-                }
-            }
-        }
-        __threadfence();
         if (!grid_sync(net.barrier, gridDim.x, 1u << 26)) ok = false;
         tc::fence_after_sync();
     }
@@ -525,11 +550,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (n0 + cb + i < N) net.counts[static_cast<size_t>(smp) * N + n0 + cb + i] = CNT[i];
     }
     if (my_events) atomicAdd(&s_events, my_events);
-    if (!ok && threadIdx.x == 0) atomicOr(net.err, 1u);
+    if (!ok)
+    {
+        if (threadIdx.x == 0) atomicOr(net.err, 1u);
+        // After a failed wait: let any MMA and bulk copy still in flight finish (bounded) before the
+        // tensor memory and shared memory are released.
+        if (threadIdx.x == 0)
+            for (int q = 0; q < kIssuers; ++q) tc::mbar_wait(&done[q], (act_steps + 1) & 1u, kWaitLimit);
+        if (warp == kLoaderWarp && lane == 0)
+            for (uint32_t sq = (seq > kABufs ? seq - kABufs : 0); sq < seq; ++sq)
+                tc::mbar_wait(&full[sq % kABufs], (sq / kABufs) & 1u, kWaitLimit);
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
-    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+    if (warp == 0) tc::tmem_dealloc(tmem, 32 * kIssuers);
 }
 
 }  // namespace
@@ -559,7 +594,11 @@ int batched_lif_run(
         }
         net.size[l] = sizes[l];
         net.words[l] = (sizes[l] + 31) / 32;
-        if (l > 0) net.kpad[l] = (sizes[l - 1] + 15) / 16 * 16;
+        if (l > 0)
+        {
+            net.kpad[l] = (sizes[l - 1] + 15) / 16 * 16;
+            net.chunks[l] = (net.kpad[l] + kBK - 1) / kBK;
+        }
     }
     // Work items: (layer, 128-sample tile, 32-neuron tile).
     const uint32_t m_tiles = (batch + kBM - 1) / kBM;
@@ -580,15 +619,14 @@ int batched_lif_run(
                 net.item_n[n_items] = static_cast<uint16_t>(n);
                 ++n_items;
             }
-        smem = std::max<size_t>(smem, static_cast<size_t>(kBN) * net.kpad[l] * 2 + kABufs * kBM * kBK * 2 +
-                                          kBM * (net.words[l - 1] | 1u) * 4);
+        smem = std::max<size_t>(smem, static_cast<size_t>(kBN) * net.kpad[l] * 2 + kABufs * kChunkBytes);
     }
     net.n_items = n_items;
     int device = 0, sms = 0, per_sm = 0, smem_max = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    if (smem > static_cast<size_t>(smem_max))
+    if (smem + 2048 > static_cast<size_t>(smem_max))  // 2 KB: the kernel's static shared memory
     {
         *why = "a layer's weight tile and staging buffers exceed the shared memory of one CTA (fan-in too large)";
         return -1;
@@ -637,9 +675,10 @@ int batched_lif_run(
     uint32_t *d_perm = static_cast<uint32_t *>(dalloc(batch * 4));
     uint32_t *d_act = static_cast<uint32_t *>(dalloc(static_cast<size_t>(net.t_max) * 4));
     ok = ok && d_perm && d_act;
-    for (int l = 0; l <= n_layers && ok; ++l)
+    for (int l = 0; l < n_layers && ok; ++l)
         for (int p = 0; p < 2 && ok; ++p)
-            ok = (net.bits[l][p] = static_cast<uint32_t *>(dalloc(static_cast<size_t>(batch) * net.words[l] * 4)));
+            ok = (net.spk[l][p] = static_cast<uint8_t *>(
+                      dalloc(static_cast<size_t>(m_tiles) * net.chunks[l + 1] * kChunkBytes))) != nullptr;
     unsigned long long *d_thr =
         static_cast<unsigned long long *>(dalloc(static_cast<size_t>(batch) * sizes[0] * sizeof(unsigned long long)));
     ok = ok && d_thr;
@@ -705,7 +744,7 @@ int batched_lif_run(
         }
         else if (kerr)
         {
-            *why = "a tensor-core completion wait or the grid barrier timed out";
+            *why = "a tensor-core completion wait, a bulk copy wait or the grid barrier timed out";
             rc = -4;
         }
     }
