@@ -182,6 +182,87 @@ def test_device_generated_projection_matches_host_arrays():
     np.testing.assert_array_equal(np.sort(b.read_weights(rec.uid)), np.sort(rec.weight))
 
 
+def _full_size_run(threshold, n, fan, seed, steps, keep):
+    """The large sparse config at full size, synapses and background generated on the device, with
+    the given gather threshold. Returns (per-step spike digests, spike masks of the last `keep`
+    steps, final potentials, event count)."""
+    import zlib
+
+    from knp_gb300 import backend as B
+
+    pop_uid, rec_uid, bg_uid, chan_uid = (T.uid_from_int(seed * 100 + i) for i in (1, 2, 3, 4))
+    pop = N.Population(pop_uid, T.BLIFAT, T.blifat_defaults(n))
+    ar = np.arange(n, dtype=np.uint32)
+    bg = N.Projection(bg_uid, T.DELTA, T.NULL_UID, pop_uid, ar, ar.copy(), np.ones(n, np.float32),
+                      np.ones(n, np.uint32))
+    b = B.GB300Backend()
+    b.load_populations([pop])
+    b.load_projections([bg])
+    b.generate_fixed_fan_in_projection(rec_uid, pop_uid, pop_uid, n, n, fan, -16, 48, 1, 20, seed,
+                                       N.LARGE_SEED_STREAM)
+    b.subscribe(bg_uid, [chan_uid])
+    b.record_spikes(pop_uid)
+    b.set_pull_threshold(rec_uid, threshold)
+    b._init()
+    b.generate_bernoulli_schedule(chan_uid, n, 0.005, 0, steps, seed=seed + 5)
+    b.step(steps)
+    digests, masks = [], {}
+    for t in range(steps):
+        s = b.spikes(pop_uid, t)
+        digests.append((s.size, zlib.crc32(s.tobytes())))
+        if t >= steps - keep:
+            m = np.zeros(n, bool)
+            m[s] = True
+            masks[t] = m
+    v = b.read_population(pop_uid)[0]["potential"].copy()
+    events = b.counters()[0]
+    b.close()
+    return digests, masks, v, events
+
+
+def test_large_sparse_full_size_properties():
+    """The large sparse config at its full size (1M neurons, 1e9 synapses), where the oracle cannot
+    run, through size-independent properties:
+    - the scatter-only and the mixed scatter/gather runs give identical spike trains and event
+      counts over the ramp into saturated firing;
+    - for 256 sampled neurons and every step, the exact input sum recomputed on the host from the
+      counter-based synapse generator and the recorded spikes (every presynaptic spike at t - d
+      through each of the neuron's 1000 synapses, plus its background spike at t - 1) decides the
+      neuron's spike (sum >= 1.0, step > 0), and at the last step equals its stored potential when
+      it did not fire (reset to 0 when it did)."""
+    n, fan, seed, steps = 1_000_000, 1000, 2, 40
+    d_a, _, _, ev_a = _full_size_run(-1.0, n, fan, seed, steps, 0)
+    d_b, masks, v, ev_b = _full_size_run(0.1, n, fan, seed, steps, steps)
+    assert d_a == d_b
+    assert ev_a == ev_b
+    assert d_b[-1][0] > n // 2  # saturated by the last step
+    s = N.LARGE_SEED_STREAM
+    keys = [N.stream_key(seed, s + k) for k in (N.S_PRE, N.S_WEIGHT, N.S_DELAY)]
+    rng = np.random.default_rng(11)
+    targets = np.sort(rng.choice(n, 256, replace=False)).astype(np.uint64)
+    tg = targets.astype(np.int64)
+    i = (targets[:, None] + np.arange(fan, dtype=np.uint64)[None, :] * np.uint64(n)).ravel()
+    pre = N.uniform_int(keys[0], i, 0, n - 1).astype(np.int64).reshape(256, fan)
+    w = N.dyadic_weights(keys[1], i, -16, 48).astype(np.float64).reshape(256, fan)
+    d = N.uniform_int(keys[2], i, 1, 20).astype(np.int64).reshape(256, fan)
+    src = N.stream_key(seed + 5, N.S_INPUT)
+    bg_thr = np.uint64(int(0.005 * float(1 << 53)))
+    hist = np.stack([masks[t] for t in range(steps)])  # [step, neuron]
+    mixed = 0
+    for t in range(1, steps):
+        ts = t - d  # step of each synapse's presynaptic spike
+        fired = np.where(ts >= 0, hist[np.maximum(ts, 0), pre], False)
+        bg_prev = (N.rand64(src, np.uint64(t - 1) * np.uint64(n) + targets) >> np.uint64(11)) < bg_thr
+        total = np.where(fired, w, 0.0).sum(axis=1) + bg_prev.astype(np.float64)
+        spiked = hist[t, tg]
+        np.testing.assert_array_equal(spiked, total >= 1.0, err_msg=f"step {t}")
+        mixed += 0 < spiked.sum() < spiked.size
+    assert mixed > 0  # some checked steps had both firing and silent sampled neurons
+    vt = v[tg].astype(np.float64)
+    np.testing.assert_array_equal(vt[~spiked], total[~spiked])
+    np.testing.assert_array_equal(vt[spiked], 0.0)
+
+
 def test_device_bernoulli_schedule_matches_host():
     from knp_gb300 import backend as B
 
