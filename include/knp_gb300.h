@@ -331,6 +331,37 @@ KNP_GB300_API int knp_gb300_batched_lif_run(
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *d_rates,
     uint64_t seed, int32_t *d_counts, uint32_t *d_record, uint64_t *events, float *ms, void *stream);
 
+/*
+ * Batched form, prepared once and run as one CUDA-graph launch (no reference counterpart). The
+ * arguments are those of knp_gb300_batched_lif_run plus:
+ *   sample_sizes  optional host array [(n_layers + 1) * batch], layer-major: sample b's size of layer
+ *                 l (<= sizes[l]); inputs and neurons beyond it do not exist for that sample (never
+ *                 spike, carry no events). NULL: every sample has the full sizes (uneven network
+ *                 instances over shared weights, or inputs of uneven width).
+ *   autotune      non-zero: each operand ring depth that fits (3..5 chunks of 32 KB) is run twice at
+ *                 creation and the fastest kept; the depth does not change any result.
+ * The device buffers (weights, rates, counts, record) must stay valid for the plan's life; their
+ * contents are read / written by every knp_gb300_batched_plan_run, so rates and weights may be
+ * rewritten between runs. One run: memsets of the run's state, the input-threshold kernel and the
+ * persistent cooperative kernel, launched as one graph on `stream`; synchronous. Runs of one plan
+ * must not overlap (they share the plan's device state).
+ */
+typedef struct knp_gb300_batched_plan knp_gb300_batched_plan;
+
+KNP_GB300_API int knp_gb300_batched_plan_create(
+    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
+    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, void *stream,
+    knp_gb300_batched_plan **plan);
+
+/** Runs the prepared batch once: *events (host) synaptic events, *ms device time of the graph launch. */
+KNP_GB300_API int knp_gb300_batched_plan_run(knp_gb300_batched_plan *plan, uint64_t *events, float *ms);
+
+/** The ring depth in use and, after autotuning, the time of each depth tried (tune_ms[3] for depths 3, 4, 5; 0 = not tried). */
+KNP_GB300_API int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, float *tune_ms);
+
+KNP_GB300_API void knp_gb300_batched_plan_destroy(knp_gb300_batched_plan *plan);
+
 /** Block until all queued device work of the backend has finished. */
 KNP_GB300_API int knp_gb300_synchronize(knp_gb300_backend *b);
 

@@ -1,8 +1,10 @@
 """Batched / precision form: many independent LIF network samples on the tcgen05 tensor cores.
 
-``run`` drives ``knp_gb300_batched_lif_run`` (knp_gb300/csrc/batched.cu): B samples of a
-feed-forward LIF network with all-to-all delay-1 layers, uneven lengths T_b, Bernoulli inputs with
-per-(sample, input) rates, BF16 weights (FP32 master values rounded to BF16), FP32 accumulation.
+``BatchedPlan`` drives ``knp_gb300_batched_plan_*`` (knp_gb300/csrc/batched.cu): B samples of a
+feed-forward LIF network with all-to-all delay-1 layers, uneven lengths T_b and optionally uneven
+layer sizes per sample, Bernoulli inputs with per-(sample, input) rates, BF16 weights (FP32 master
+values rounded to BF16), FP32 accumulation; prepared once and run as one CUDA-graph launch. ``run``
+is the one-shot form.
 ``plain_network`` builds the same computation as one block-diagonal network for the plain backend
 (FP32 input rings, the same BF16-valued weights), which is what the batched form is compared with.
 The reference has no batched execution; these forms have no counterpart there.
@@ -30,6 +32,7 @@ class BatchedConfig:
     threshold: tuple = None
     reset: tuple = None
     refract: tuple = None
+    sample_sizes: np.ndarray = None  # uint32 [n_layers + 1, B]: sample b's size of layer l (<= sizes[l])
 
     @property
     def batch(self) -> int:
@@ -56,53 +59,118 @@ def dense_config(seed: int = 4, batch: int = 256, sizes=(784, 1000, 1000, 10), t
 
 
 def input_spikes(cfg: BatchedConfig, b: int, t: int) -> np.ndarray:
-    """Input indexes of sample b at step t: the counter-based draw the kernel makes."""
+    """Input indexes of sample b at step t: the counter-based draw the kernel makes (inputs beyond the
+    sample's input width never spike)."""
     n0 = cfg.sizes[0]
     key = N.stream_key(cfg.seed, N.S_INPUT)
     ctr = (np.uint64(t) * np.uint64(cfg.batch) + np.uint64(b)) * np.uint64(n0) + np.arange(n0, dtype=np.uint64)
     thr = (cfg.rates[b].astype(np.float64) * float(1 << 53)).astype(np.uint64)
-    return np.nonzero((N.rand64(key, ctr) >> np.uint64(11)) < thr)[0].astype(np.uint32)
+    idx = np.nonzero((N.rand64(key, ctr) >> np.uint64(11)) < thr)[0].astype(np.uint32)
+    if cfg.sample_sizes is not None:
+        idx = idx[idx < cfg.sample_sizes[0][b]]
+    return idx
 
 
-def run(cfg: BatchedConfig, record: bool = False, device: int = 0):
-    """Run the batch on the GPU. Returns (counts [B, n_L], record or None, events, ms). With
+def uneven_config(seed: int = 8, batch: int = 40, sizes=(96, 128, 64, 10), t_lo: int = 10, t_hi: int = 30,
+                  rate_max: float = 0.3) -> BatchedConfig:
+    """Dense config whose samples are network instances of uneven size: sample b keeps a random
+    prefix of every layer (at least half of it, the output layer whole) over shared weights."""
+    cfg = dense_config(seed=seed, batch=batch, sizes=sizes, t_lo=t_lo, t_hi=t_hi, rate_max=rate_max)
+    rng = np.random.default_rng(seed + 1000)
+    ss = np.zeros((len(sizes), batch), np.uint32)
+    for layer, n in enumerate(sizes):
+        ss[layer] = n if layer == len(sizes) - 1 else rng.integers(n // 2, n + 1, size=batch)
+    cfg.sample_sizes = ss
+    return cfg
+
+
+class BatchedPlan:
+    """A batch prepared on the device (knp_gb300_batched_plan_create) and run as one CUDA-graph
+    launch per ``run()``; with ``autotune`` the operand ring depth is chosen by timing each depth."""
+
+    def __init__(self, cfg: BatchedConfig, record: bool = False, autotune: bool = False, device: int = 0):
+        import torch
+
+        self.cfg = cfg
+        self._lib = _capi.lib()
+        dev = torch.device(f"cuda:{device}")
+        L = len(cfg.sizes) - 1
+        self._w = [torch.from_numpy(np.ascontiguousarray(w)).to(dev).to(torch.bfloat16).contiguous()
+                   for w in cfg.weights]
+        self._rates = torch.from_numpy(np.ascontiguousarray(cfg.rates, np.float32)).to(dev)
+        self._counts = torch.zeros((cfg.batch, cfg.sizes[-1]), dtype=torch.int32, device=dev)
+        self._words = [(n + 31) // 32 for n in cfg.sizes]
+        self._t_max = int(cfg.steps.max())
+        self._stride = sum(cfg.batch * w for w in self._words)
+        self._rec = torch.zeros(self._t_max * self._stride, dtype=torch.int32, device=dev) if record else None
+        self._stream = torch.cuda.current_stream(dev)
+
+        def fl(v, default):
+            return (ctypes.c_float * L)(*(v if v is not None else [default] * L))
+
+        sizes = (ctypes.c_uint32 * (L + 1))(*cfg.sizes)
+        wptr = (ctypes.c_void_p * L)(*[w.data_ptr() for w in self._w])
+        refract = (ctypes.c_uint32 * L)(*(cfg.refract if cfg.refract is not None else [0] * L))
+        steps = (ctypes.c_uint32 * cfg.batch)(*[int(x) for x in cfg.steps])
+        ss = None
+        if cfg.sample_sizes is not None:
+            flat = np.ascontiguousarray(cfg.sample_sizes, np.uint32).ravel()
+            ss = (ctypes.c_uint32 * flat.size)(*flat.tolist())
+        self._h = ctypes.c_void_p()
+        _capi.check(self._lib.knp_gb300_batched_plan_create(
+            L, sizes, wptr, fl(cfg.leak, 1.0), fl(cfg.threshold, 1.0), fl(cfg.reset, 0.0), refract, cfg.batch, steps,
+            ss, ctypes.c_void_p(self._rates.data_ptr()), cfg.seed, ctypes.c_void_p(self._counts.data_ptr()),
+            ctypes.c_void_p(self._rec.data_ptr()) if self._rec is not None else None, int(autotune),
+            ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self._h)))
+
+    def run(self):
+        """One graph launch; returns (synaptic events, device ms)."""
+        events = ctypes.c_uint64(0)
+        ms = ctypes.c_float(0)
+        _capi.check(self._lib.knp_gb300_batched_plan_run(self._h, ctypes.byref(events), ctypes.byref(ms)))
+        return int(events.value), float(ms.value)
+
+    def info(self):
+        """(ring depth in use, {depth: ms of the autotuning run})."""
+        st = ctypes.c_int(0)
+        t = (ctypes.c_float * 3)()
+        _capi.check(self._lib.knp_gb300_batched_plan_info(self._h, ctypes.byref(st), t))
+        return st.value, {d: float(t[d - 3]) for d in (3, 4, 5) if t[d - 3] > 0}
+
+    def counts(self) -> np.ndarray:
+        return self._counts.cpu().numpy()
+
+    def record(self):
+        """Per-step spike bitmaps of every layer: {layer: uint32 [T_max, B, words]}."""
+        r = self._rec.cpu().numpy().view(np.uint32).reshape(self._t_max, self._stride)
+        out, off = {}, 0
+        for layer, w in enumerate(self._words):
+            out[layer] = r[:, off:off + self.cfg.batch * w].reshape(self._t_max, self.cfg.batch, w)
+            off += self.cfg.batch * w
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.knp_gb300_batched_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run(cfg: BatchedConfig, record: bool = False, device: int = 0, autotune: bool = False):
+    """Run the batch once on the GPU. Returns (counts [B, n_L], record or None, events, ms). With
     ``record`` the per-step spike bitmaps of every layer come back as a dict
     {layer: uint32 [T_max, B, words]}."""
-    import torch
-
-    dev = torch.device(f"cuda:{device}")
-    L = len(cfg.sizes) - 1
-    wts = [torch.from_numpy(np.ascontiguousarray(w)).to(dev).to(torch.bfloat16).contiguous() for w in cfg.weights]
-    rates = torch.from_numpy(np.ascontiguousarray(cfg.rates, np.float32)).to(dev)
-    counts = torch.zeros((cfg.batch, cfg.sizes[-1]), dtype=torch.int32, device=dev)
-    words = [(n + 31) // 32 for n in cfg.sizes]
-    t_max = int(cfg.steps.max())
-    stride = sum(cfg.batch * w for w in words)
-    rec = torch.zeros(t_max * stride, dtype=torch.int32, device=dev) if record else None
-    sizes = (ctypes.c_uint32 * (L + 1))(*cfg.sizes)
-    wptr = (ctypes.c_void_p * L)(*[w.data_ptr() for w in wts])
-
-    def fl(v, default):
-        return (ctypes.c_float * L)(*(v if v is not None else [default] * L))
-
-    refract = (ctypes.c_uint32 * L)(*(cfg.refract if cfg.refract is not None else [0] * L))
-    steps = (ctypes.c_uint32 * cfg.batch)(*[int(x) for x in cfg.steps])
-    events = ctypes.c_uint64(0)
-    ms = ctypes.c_float(0)
-    lib = _capi.lib()
-    _capi.check(lib.knp_gb300_batched_lif_run(
-        L, sizes, wptr, fl(cfg.leak, 1.0), fl(cfg.threshold, 1.0), fl(cfg.reset, 0.0), refract, cfg.batch, steps,
-        ctypes.c_void_p(rates.data_ptr()), cfg.seed, ctypes.c_void_p(counts.data_ptr()),
-        ctypes.c_void_p(rec.data_ptr()) if rec is not None else None, ctypes.byref(events), ctypes.byref(ms),
-        ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
-    out_rec = None
-    if rec is not None:
-        r = rec.cpu().numpy().view(np.uint32).reshape(t_max, stride)
-        out_rec, off = {}, 0
-        for layer, w in enumerate(words):
-            out_rec[layer] = r[:, off:off + cfg.batch * w].reshape(t_max, cfg.batch, w)
-            off += cfg.batch * w
-    return counts.cpu().numpy(), out_rec, int(events.value), float(ms.value)
+    plan = BatchedPlan(cfg, record=record, autotune=autotune, device=device)
+    try:
+        events, ms = plan.run()
+        return plan.counts(), (plan.record() if record else None), events, ms
+    finally:
+        plan.close()
 
 
 def spikes_from_bits(words_row: np.ndarray, n: int) -> np.ndarray:
@@ -129,6 +197,11 @@ def plain_network(cfg: BatchedConfig, samples=None):
             a["potential_reset_value"] = cfg.reset[l - 1]
         if cfg.refract is not None:
             a["refract_period"] = cfg.refract[l - 1]
+        if cfg.sample_sizes is not None:
+            # Neurons beyond a sample's layer size do not exist for it: they never fire.
+            pos = np.arange(S * cfg.sizes[l]) % cfg.sizes[l]
+            own = np.repeat(np.asarray([cfg.sample_sizes[l][b] for b in samples]), cfg.sizes[l])
+            a["activation_threshold"] = np.where(pos < own, a["activation_threshold"], np.float32(np.inf))
         pops.append(N.Population(T.uid_from_int(800 + l), T.LIF, a))
     chan = T.uid_from_int(899)
     projs = []

@@ -5,6 +5,7 @@
 // tcgen05 encodings and as a library GEMM of spike matrices.
 #include <algorithm>
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -167,7 +168,7 @@ namespace
 
 constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
 constexpr int kIssuers = 2;                           // issuer q runs the MMAs of chunks c with c % 2 == q
-constexpr int kABufs = 5;                             // A chunk ring stages
+constexpr int kMinStages = 3, kMaxStages = 5;        // operand ring depths the autotuner tries
 constexpr uint32_t kChunkBytes = kBM * kBK * 2;       // one 128 x 128 BF16 chunk
 constexpr uint32_t kSboA = (kBK / 8) * 128;           // row-group stride of a chunk (16 core matrices)
 constexpr int kLoaderWarp = kIssuers;                 // lane 0 of this warp streams the chunks
@@ -189,6 +190,9 @@ struct BatchedNet
     const uint32_t *perm;  // slot -> sample
     const uint32_t *act;   // [t_max]: slots still running at step t (slots sorted by decreasing T)
     const unsigned long long *rate_thr;  // [batch][size[0]] by sample: rate * 2^53, the draw's threshold
+    // Optional per-sample layer sizes ([batch] by sample, <= size[l]); neurons and inputs beyond a
+    // sample's size do not exist for it (never spike). Null: every sample has the full sizes.
+    const uint32_t *sample_size[kMaxLayers + 1];
     unsigned long long key;
     uint32_t t_max;
     // spk[l][p]: spikes of layer l (l < n_layers) at steps of parity p, as layer l + 1's A operand:
@@ -276,12 +280,13 @@ __device__ __forceinline__ uint32_t spk_offset(uint32_t r, uint32_t k)
     return (k / kBK) * kChunkBytes + (r >> 3) * kSboA + ((k % kBK) >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
 }
 
+template <int kStages>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t full[kABufs];   // chunk in stage b has landed (loader's expect_tx)
-    __shared__ __align__(8) uint64_t empty[kABufs];  // MMAs that read stage b have completed (commit)
+    __shared__ __align__(8) uint64_t full[kStages];   // chunk in stage b has landed (loader's expect_tx)
+    __shared__ __align__(8) uint64_t empty[kStages];  // MMAs that read stage b have completed (commit)
     __shared__ __align__(8) uint64_t done[kIssuers]; // all of an issuer's MMAs of a step have completed
     __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t K = net.size[layer - 1], Kp = net.kpad[layer], N = net.size[layer];
     const uint32_t wn = net.words[layer];
     const uint32_t n_chunks = net.chunks[layer];
-    // Shared memory: weight tile [kBN x Kp] (K-major core matrices), kABufs chunk stages.
+    // Shared memory: weight tile [kBN x Kp] (K-major core matrices), kStages chunk stages.
     uint8_t *sW = smem;
     uint8_t *sA = smem + static_cast<size_t>(kBN) * Kp * 2;
     const uint32_t sbo_w = (Kp / 8) * 128;
@@ -313,7 +318,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     if (warp == 0) tc::tmem_alloc(&tmem_slot, 32 * kIssuers);
     if (threadIdx.x == 0)
     {
-        for (int b = 0; b < kABufs; ++b)
+        for (int b = 0; b < kStages; ++b)
         {
             tc::mbar_init(&full[b], 1);
             tc::mbar_init(&empty[b], 1);
@@ -326,12 +331,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
-    const uint32_t fan_out = layer < net.n_layers ? net.size[layer + 1] : 0u;
     // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
     // adding byte offsets / 16 to the start-address field.
     const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
     const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
-    uint32_t seq = 0;        // chunks streamed by this CTA in earlier steps (stage = seq % kABufs)
+    uint32_t seq = 0;        // chunks streamed by this CTA in earlier steps (stage = seq % kStages)
     uint32_t act_steps = 0;  // steps this CTA has computed (phase of done[])
     bool ok = true;
     unsigned long long my_events = 0;
@@ -354,6 +358,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const int li = layer - 1;
     const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
     const uint32_t per = net.refract[li];
+    // This thread's sample: its own neuron count and its next layer's (the fan-out of its spikes).
+    const uint32_t e_smp = erow < net.batch ? net.perm[erow] : 0u;
+    const uint32_t my_n = (net.sample_size[layer] && erow < net.batch) ? net.sample_size[layer][e_smp] : N;
+    const uint32_t my_fan_out =
+        layer < net.n_layers ? ((net.sample_size[layer + 1] && erow < net.batch) ? net.sample_size[layer + 1][e_smp]
+                                                                                  : net.size[layer + 1])
+                             : 0u;
 
     // Input words drawn by this warp every step (drawing warps only: u = draw warp id + j * draw
     // warps in grid) and, for the first kInCache of them, this lane's threshold and sample.
@@ -375,7 +386,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         {
             const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
             in_smp[j] = net.perm[slot];
-            if (i < n_in) in_thr[j] = net.rate_thr[static_cast<size_t>(in_smp[j]) * n_in + i];
+            if (i < n_in && (!net.sample_size[0] || i < net.sample_size[0][in_smp[j]]))
+                in_thr[j] = net.rate_thr[static_cast<size_t>(in_smp[j]) * n_in + i];
         }
     }
     const size_t spk0_tile = static_cast<size_t>(net.chunks[1]) * kChunkBytes;
@@ -397,8 +409,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 asm volatile("fence.proxy.async.global;" ::: "memory");
                 for (uint32_t c = 0; c < n_chunks; ++c)
                 {
-                    const uint32_t sq = seq + c, b = sq % kABufs;
-                    if (sq >= kABufs && !tc::mbar_wait(&empty[b], (sq / kABufs - 1) & 1u, kWaitLimit)) ok = false;
+                    const uint32_t sq = seq + c, b = sq % kStages;
+                    if (sq >= kStages && !tc::mbar_wait(&empty[b], (sq / kStages - 1) & 1u, kWaitLimit)) ok = false;
                     mbar_arrive_expect_tx(&full[b], kChunkBytes);
                     bulk_load(sA + static_cast<size_t>(b) * kChunkBytes, src + static_cast<size_t>(c) * kChunkBytes,
                               kChunkBytes, &full[b]);
@@ -409,8 +421,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 // Issuer q: chunks q, q + 2, ... into its accumulator, then one commit for the step.
                 for (uint32_t c = warp; c < n_chunks; c += kIssuers)
                 {
-                    const uint32_t sq = seq + c, b = sq % kABufs;
-                    if (!tc::mbar_wait(&full[b], (sq / kABufs) & 1u, kWaitLimit)) ok = false;
+                    const uint32_t sq = seq + c, b = sq % kStages;
+                    if (!tc::mbar_wait(&full[b], (sq / kStages) & 1u, kWaitLimit)) ok = false;
                     tc::fence_after_sync();
                     const uint64_t da = dA0 + b * (kChunkBytes >> 4);
                     const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
@@ -447,7 +459,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 {
                     if (net.record)
                         net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
-                    my_events += static_cast<unsigned long long>(__popc(word)) * net.size[1];
+                    my_events += static_cast<unsigned long long>(__popc(word)) *
+                                 (net.sample_size[1] ? net.sample_size[1][smp] : net.size[1]);
                 }
             };
 #pragma unroll
@@ -460,7 +473,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             {
                 const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
                 const uint32_t smp = net.perm[slot];
-                draw(u, i < n_in ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp);
+                const bool exists = i < n_in && (!net.sample_size[0] || i < net.sample_size[0][smp]);
+                draw(u, exists ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp);
             }
         }
         if (active)
@@ -493,7 +507,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
                     {
-                        if (n0 + cb + i >= N) break;
+                        if (n0 + cb + i >= my_n) break;
                         // lif_impl.h:33-86: leak and input only outside the refractory period;
                         // strict '>'; reset to a value.
                         if (RC[i] == 0u)
@@ -527,7 +541,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 *reinterpret_cast<uint4 *>(d + spk_offset(er, k + 8)) = bf16_bits(mask >> (cb + 8));
             }
             if (mask) atomicOr(&sbits[er], mask);
-            my_events += static_cast<unsigned long long>(__popc(mask)) * fan_out;
+            my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
             tc::fence_before_sync();
             __syncthreads();
             if (net.record && threadIdx.x < kBM)
@@ -558,8 +572,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         if (threadIdx.x == 0)
             for (int q = 0; q < kIssuers; ++q) tc::mbar_wait(&done[q], (act_steps + 1) & 1u, kWaitLimit);
         if (warp == kLoaderWarp && lane == 0)
-            for (uint32_t sq = (seq > kABufs ? seq - kABufs : 0); sq < seq; ++sq)
-                tc::mbar_wait(&full[sq % kABufs], (sq / kABufs) & 1u, kWaitLimit);
+            for (uint32_t sq = (seq > kStages ? seq - kStages : 0); sq < seq; ++sq)
+                tc::mbar_wait(&full[sq % kStages], (sq / kStages) & 1u, kWaitLimit);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -569,21 +583,151 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
 
 }  // namespace
 
-// Runs a whole batch. Host arrays: sizes[n_layers + 1], leak/threshold/reset/refract[n_layers],
-// steps[batch]; device arrays: weights[l] (BF16 [sizes[l + 1]][sizes[l]]), rates [batch][sizes[0]],
-// counts [batch][sizes[n_layers]] (zeroed here), record (optional, see knp_gb300.h).
-int batched_lif_run(
-    int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
-    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *rates,
-    unsigned long long key, int *counts, uint32_t *record, unsigned long long *events_out, float *ms,
-    cudaStream_t s, const char **why)
+// A batch prepared once and run as one CUDA-graph launch (memsets of the run's state, the input
+// threshold kernel and the cooperative persistent kernel). Reusable: every run starts from zero
+// state, so repeated runs of the same plan give identical results.
+struct BatchedPlan
 {
+    BatchedNet net{};
+    cudaStream_t caller = nullptr;  // the caller's stream: a run starts after its queued work
+    cudaStream_t stream = nullptr;  // the plan's own stream (graphs cannot be captured on the legacy stream)
+    cudaEvent_t ready = nullptr;
+    std::vector<void *> allocs;
+    std::vector<std::pair<void *, size_t>> zero;  // cleared at the start of every run
+    const float *rates = nullptr;
+    unsigned long long *d_thr = nullptr;
+    size_t n_thr = 0;
+    size_t w_bytes = 0;  // largest weight tile (shared memory besides the ring)
+    uint32_t n_items = 0;
+    cudaGraphExec_t exec = nullptr;
+    int stages = 0;
+    float tune_ms[kMaxStages + 1] = {};
+
+    ~BatchedPlan()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (stream) cudaStreamSynchronize(stream);
+        for (void *p : allocs) cudaFree(p);
+        if (ready) cudaEventDestroy(ready);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace
+{
+
+const void *kernel_for(int stages)
+{
+    switch (stages)
+    {
+        case 3:
+            return reinterpret_cast<const void *>(batched_lif_kernel<3>);
+        case 4:
+            return reinterpret_cast<const void *>(batched_lif_kernel<4>);
+        default:
+            return reinterpret_cast<const void *>(batched_lif_kernel<5>);
+    }
+}
+
+// Whether a ring of `stages` chunks fits (shared memory, every CTA resident at once).
+bool variant_fits(const BatchedPlan &p, int stages)
+{
+    int device = 0, sms = 0, smem_max = 0, per_sm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    const size_t smem = p.w_bytes + static_cast<size_t>(stages) * kChunkBytes;
+    if (smem + 2048 > static_cast<size_t>(smem_max)) return false;  // 2 KB: the kernel's static shared memory
+    const void *k = kernel_for(stages);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
+        return false;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBatchThreads, smem) != cudaSuccess) return false;
+    return static_cast<long long>(per_sm) * sms >= p.n_items;
+}
+
+// Captures one run with a ring of `stages` chunks into p.exec.
+cudaError_t capture(BatchedPlan &p, int stages)
+{
+    if (p.exec)
+    {
+        cudaGraphExecDestroy(p.exec);
+        p.exec = nullptr;
+    }
+    cudaStream_t s = p.stream;
+    cudaError_t err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) return err;
+    for (auto &z : p.zero) cudaMemsetAsync(z.first, 0, z.second, s);
+    rate_threshold_kernel<<<static_cast<unsigned>((p.n_thr + 255) / 256), 256, 0, s>>>(p.rates, p.d_thr, p.n_thr);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(p.n_items);
+    cfg.blockDim = dim3(kBatchThreads);
+    cfg.dynamicSmemBytes = p.w_bytes + static_cast<size_t>(stages) * kChunkBytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void *args[] = {&p.net};
+    const cudaError_t lerr = cudaLaunchKernelExC(&cfg, kernel_for(stages), args);
+    cudaGraph_t g = nullptr;
+    err = cudaStreamEndCapture(s, &g);
+    if (lerr != cudaSuccess) err = lerr;
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&p.exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (err == cudaSuccess) p.stages = stages;
+    return err;
+}
+
+cudaError_t launch_timed(BatchedPlan &p, float *ms)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // Order the run after the caller's queued work (weights, rates written on its stream).
+    cudaEventRecord(p.ready, p.caller);
+    cudaStreamWaitEvent(p.stream, p.ready, 0);
+    cudaEventRecord(e0, p.stream);
+    cudaError_t err = cudaGraphLaunch(p.exec, p.stream);
+    cudaEventRecord(e1, p.stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (err == cudaSuccess) cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return err;
+}
+
+}  // namespace
+
+// Prepares a batch. Host arrays: sizes[n_layers + 1], leak/threshold/reset/refract[n_layers],
+// steps[batch], sample_sizes[(n_layers + 1) * batch] (layer-major, optional); device arrays:
+// weights[l] (BF16 [sizes[l + 1]][sizes[l]]), rates [batch][sizes[0]], counts [batch][sizes[n_layers]]
+// and record (optional; layouts in knp_gb300.h). With `autotune`, each operand ring depth that fits
+// is run twice and the fastest kept; every depth computes the same results.
+int batched_plan_create(
+    int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
+    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, cudaStream_t s,
+    BatchedPlan **out, const char **why)
+{
+    *out = nullptr;
     if (n_layers < 1 || n_layers > kMaxLayers || batch == 0 || !sizes || !weights || !steps || !rates || !counts)
     {
         *why = "bad arguments";
         return -1;
     }
-    BatchedNet net{};
+    std::unique_ptr<BatchedPlan> plan(new BatchedPlan());
+    BatchedPlan &p = *plan;
+    BatchedNet &net = p.net;
+    p.caller = s;
+    if (cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p.ready, cudaEventDisableTiming) != cudaSuccess)
+    {
+        *why = "could not create the plan's stream";
+        return -3;
+    }
     net.n_layers = n_layers;
     for (int l = 0; l <= n_layers; ++l)
     {
@@ -600,49 +744,48 @@ int batched_lif_run(
             net.chunks[l] = (net.kpad[l] + kBK - 1) / kBK;
         }
     }
+    for (uint32_t b = 0; b < batch; ++b)
+    {
+        if (steps[b] == 0 || steps[b] > 1000000)
+        {
+            *why = "per-sample step counts must be in [1, 1000000]";
+            return -1;
+        }
+        if (sample_sizes)
+            for (int l = 0; l <= n_layers; ++l)
+                if (sample_sizes[static_cast<size_t>(l) * batch + b] > sizes[l])
+                {
+                    *why = "a sample's layer size exceeds the layer size";
+                    return -1;
+                }
+    }
     // Work items: (layer, 128-sample tile, 32-neuron tile).
     const uint32_t m_tiles = (batch + kBM - 1) / kBM;
-    uint32_t n_items = 0;
-    size_t smem = 0;
     for (int l = 1; l <= n_layers; ++l)
     {
         for (uint32_t m = 0; m < m_tiles; ++m)
             for (uint32_t n = 0; n < net.words[l]; ++n)
             {
-                if (n_items >= kMaxItems)
+                if (p.n_items >= kMaxItems)
                 {
                     *why = "too many (layer, sample tile, neuron tile) work items";
                     return -1;
                 }
-                net.item_layer[n_items] = static_cast<uint16_t>(l);
-                net.item_m[n_items] = static_cast<uint16_t>(m);
-                net.item_n[n_items] = static_cast<uint16_t>(n);
-                ++n_items;
+                net.item_layer[p.n_items] = static_cast<uint16_t>(l);
+                net.item_m[p.n_items] = static_cast<uint16_t>(m);
+                net.item_n[p.n_items] = static_cast<uint16_t>(n);
+                ++p.n_items;
             }
-        smem = std::max<size_t>(smem, static_cast<size_t>(kBN) * net.kpad[l] * 2 + kABufs * kChunkBytes);
+        p.w_bytes = std::max<size_t>(p.w_bytes, static_cast<size_t>(kBN) * net.kpad[l] * 2);
     }
-    net.n_items = n_items;
-    int device = 0, sms = 0, per_sm = 0, smem_max = 0;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    if (smem + 2048 > static_cast<size_t>(smem_max))  // 2 KB: the kernel's static shared memory
+    net.n_items = p.n_items;
+    int best = 0;
+    for (int st = kMaxStages; st >= kMinStages && !best; --st)
+        if (variant_fits(p, st)) best = st;
+    if (!best)
     {
-        *why = "a layer's weight tile and staging buffers exceed the shared memory of one CTA (fan-in too large)";
-        return -1;
-    }
-    cudaError_t err = cudaFuncSetAttribute(batched_lif_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem));
-    if (err == cudaSuccess)
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_lif_kernel, kBatchThreads, smem);
-    if (err != cudaSuccess)
-    {
-        *why = cudaGetErrorString(err);
-        return -3;
-    }
-    if (static_cast<long long>(per_sm) * sms < n_items)
-    {
-        *why = "the batch needs more resident CTAs than the device holds";
+        *why = "the batch does not fit: a layer's weight tile and operand ring exceed one CTA's shared memory "
+               "(fan-in too large) or the work items exceed the resident CTAs";
         return -1;
     }
     // Samples sorted by decreasing length.
@@ -654,6 +797,7 @@ int batched_lif_run(
     net.batch = batch;
     net.key = key;
     net.counts = counts;
+    net.record = record;
     for (int l = 0; l < n_layers; ++l)
     {
         net.w[l] = static_cast<const __nv_bfloat16 *>(weights[l]);
@@ -662,94 +806,135 @@ int batched_lif_run(
         net.reset[l] = reset ? reset[l] : 0.0f;
         net.refract[l] = refract ? refract[l] : 0u;
     }
-    std::vector<void *> allocs;
     auto dalloc = [&](size_t bytes) -> void *
     {
-        void *p = nullptr;
-        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
-        allocs.push_back(p);
-        cudaMemsetAsync(p, 0, bytes ? bytes : 16, s);
-        return p;
+        void *q = nullptr;
+        if (cudaMalloc(&q, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        p.allocs.push_back(q);
+        return q;
     };
-    bool ok = true;
-    uint32_t *d_perm = static_cast<uint32_t *>(dalloc(batch * 4));
-    uint32_t *d_act = static_cast<uint32_t *>(dalloc(static_cast<size_t>(net.t_max) * 4));
-    ok = ok && d_perm && d_act;
+    auto upload = [&](const void *src, size_t bytes) -> void *
+    {
+        void *q = dalloc(bytes);
+        if (q && cudaMemcpy(q, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+        return q;
+    };
+    // act[t] = slots with T > t (slots are sorted by decreasing T).
+    std::vector<uint32_t> act(net.t_max);
+    for (uint32_t t = 0, a = batch; t < net.t_max; ++t)
+    {
+        while (a > 0 && st[a - 1] <= t) --a;
+        act[t] = a;
+    }
+    bool ok = (net.perm = static_cast<const uint32_t *>(upload(perm.data(), batch * 4))) != nullptr;
+    ok = ok && (net.act = static_cast<const uint32_t *>(upload(act.data(), act.size() * 4))) != nullptr;
+    if (sample_sizes)
+        for (int l = 0; l <= n_layers && ok; ++l)
+            ok = (net.sample_size[l] = static_cast<const uint32_t *>(
+                      upload(sample_sizes + static_cast<size_t>(l) * batch, batch * 4))) != nullptr;
     for (int l = 0; l < n_layers && ok; ++l)
-        for (int p = 0; p < 2 && ok; ++p)
-            ok = (net.spk[l][p] = static_cast<uint8_t *>(
-                      dalloc(static_cast<size_t>(m_tiles) * net.chunks[l + 1] * kChunkBytes))) != nullptr;
-    unsigned long long *d_thr =
-        static_cast<unsigned long long *>(dalloc(static_cast<size_t>(batch) * sizes[0] * sizeof(unsigned long long)));
-    ok = ok && d_thr;
-    net.rate_thr = d_thr;
-    net.events = static_cast<unsigned long long *>(dalloc(8));
-    net.err = static_cast<unsigned int *>(dalloc(4));
-    net.barrier = static_cast<unsigned int *>(dalloc(8));
-    ok = ok && net.events && net.err && net.barrier;
-    int rc = 0;
+        for (int q = 0; q < 2 && ok; ++q)
+        {
+            const size_t bytes = static_cast<size_t>(m_tiles) * net.chunks[l + 1] * kChunkBytes;
+            ok = (net.spk[l][q] = static_cast<uint8_t *>(dalloc(bytes))) != nullptr;
+            p.zero.emplace_back(net.spk[l][q], bytes);
+        }
+    p.n_thr = static_cast<size_t>(batch) * sizes[0];
+    ok = ok && (p.d_thr = static_cast<unsigned long long *>(dalloc(p.n_thr * 8))) != nullptr;
+    net.rate_thr = p.d_thr;
+    p.rates = rates;
+    ok = ok && (net.events = static_cast<unsigned long long *>(dalloc(8))) != nullptr;
+    ok = ok && (net.err = static_cast<unsigned int *>(dalloc(4))) != nullptr;
+    ok = ok && (net.barrier = static_cast<unsigned int *>(dalloc(8))) != nullptr;
     if (!ok)
     {
         *why = "device allocation failed";
-        rc = -5;
+        return -5;
     }
-    else
+    p.zero.emplace_back(counts, static_cast<size_t>(batch) * net.size[n_layers] * 4);
+    p.zero.emplace_back(net.events, 8);
+    p.zero.emplace_back(net.err, 4);
+    p.zero.emplace_back(net.barrier, 8);
+    unsigned long long off = 0;
+    for (int l = 0; l <= n_layers; ++l)
     {
-        cudaMemcpyAsync(d_perm, perm.data(), batch * 4, cudaMemcpyHostToDevice, s);
-        // act[t] = slots with T > t (slots are sorted by decreasing T).
-        std::vector<uint32_t> act(net.t_max);
-        for (uint32_t t = 0, a = batch; t < net.t_max; ++t)
+        net.rec_off[l] = off;
+        off += static_cast<unsigned long long>(batch) * net.words[l];
+    }
+    net.rec_stride = off;
+    if (record) p.zero.emplace_back(record, static_cast<size_t>(net.t_max) * off * 4);
+
+    cudaError_t err = cudaSuccess;
+    if (autotune)
+    {
+        float best_ms = 0.f;
+        for (int stg = kMinStages; stg <= kMaxStages; ++stg)
         {
-            while (a > 0 && st[a - 1] <= t) --a;
-            act[t] = a;
-        }
-        cudaMemcpyAsync(d_act, act.data(), act.size() * 4, cudaMemcpyHostToDevice, s);
-        cudaMemsetAsync(counts, 0, static_cast<size_t>(batch) * net.size[n_layers] * 4, s);
-        net.perm = d_perm;
-        net.act = d_act;
-        net.record = record;
-        unsigned long long off = 0;
-        for (int l = 0; l <= n_layers; ++l)
-        {
-            net.rec_off[l] = off;
-            off += static_cast<unsigned long long>(batch) * net.words[l];
-        }
-        net.rec_stride = off;
-        if (record) cudaMemsetAsync(record, 0, static_cast<size_t>(net.t_max) * off * 4, s);
-        const size_t n_thr = static_cast<size_t>(batch) * sizes[0];
-        rate_threshold_kernel<<<static_cast<unsigned>((n_thr + 255) / 256), 256, 0, s>>>(rates, d_thr, n_thr);
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, s);
-        void *args[] = {&net};
-        err = cudaLaunchCooperativeKernel(reinterpret_cast<void *>(batched_lif_kernel), dim3(n_items),
-                                          dim3(kBatchThreads), args, smem, s);
-        cudaEventRecord(e1, s);
-        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-        float t = 0.f;
-        cudaEventElapsedTime(&t, e0, e1);
-        if (ms) *ms = t;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        unsigned long long ev = 0;
-        unsigned int kerr = 0;
-        if (err == cudaSuccess) err = cudaMemcpy(&ev, net.events, 8, cudaMemcpyDeviceToHost);
-        if (err == cudaSuccess) err = cudaMemcpy(&kerr, net.err, 4, cudaMemcpyDeviceToHost);
-        if (events_out) *events_out = ev;
-        if (err != cudaSuccess)
-        {
-            *why = cudaGetErrorString(err);
-            rc = -3;
-        }
-        else if (kerr)
-        {
-            *why = "a tensor-core completion wait, a bulk copy wait or the grid barrier timed out";
-            rc = -4;
+            if (!variant_fits(p, stg)) continue;
+            err = capture(p, stg);
+            float t = 0.f;
+            for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) err = launch_timed(p, &t);
+            if (err != cudaSuccess) break;
+            p.tune_ms[stg] = t;
+            if (!best_ms || t < best_ms)
+            {
+                best_ms = t;
+                best = stg;
+            }
         }
     }
-    cudaStreamSynchronize(s);
-    for (void *p : allocs) cudaFree(p);
+    if (err == cudaSuccess && p.stages != best) err = capture(p, best);
+    if (err != cudaSuccess)
+    {
+        *why = cudaGetErrorString(err);
+        return -3;
+    }
+    *out = plan.release();
+    return 0;
+}
+
+int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, const char **why)
+{
+    cudaError_t err = launch_timed(*p, ms);
+    unsigned long long ev = 0;
+    unsigned int kerr = 0;
+    if (err == cudaSuccess) err = cudaMemcpy(&ev, p->net.events, 8, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(&kerr, p->net.err, 4, cudaMemcpyDeviceToHost);
+    if (events_out) *events_out = ev;
+    if (err != cudaSuccess)
+    {
+        *why = cudaGetErrorString(err);
+        return -3;
+    }
+    if (kerr)
+    {
+        *why = "a tensor-core completion wait, a bulk copy wait or the grid barrier timed out";
+        return -4;
+    }
+    return 0;
+}
+
+void batched_plan_info(const BatchedPlan *p, int *stages, float *tune_ms)
+{
+    if (stages) *stages = p->stages;
+    if (tune_ms)
+        for (int i = kMinStages; i <= kMaxStages; ++i) tune_ms[i - kMinStages] = p->tune_ms[i];
+}
+
+void batched_plan_destroy(BatchedPlan *p) { delete p; }
+
+// One-shot form: prepare, run once, release.
+int batched_lif_run(
+    int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *rates,
+    unsigned long long key, int *counts, uint32_t *record, unsigned long long *events_out, float *ms,
+    cudaStream_t s, const char **why)
+{
+    BatchedPlan *p = nullptr;
+    int rc = batched_plan_create(n_layers, sizes, weights, leak, threshold, reset, refract, batch, steps, nullptr,
+                                 rates, key, counts, record, 0, s, &p, why);
+    if (rc == 0) rc = batched_plan_run(p, events_out, ms, why);
+    if (p) batched_plan_destroy(p);
     return rc;
 }
 

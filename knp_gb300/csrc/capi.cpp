@@ -32,7 +32,21 @@ int batched_lif_run(
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *rates,
     unsigned long long key, int *counts, uint32_t *record, unsigned long long *events_out, float *ms,
     cudaStream_t s, const char **why);
+struct BatchedPlan;
+int batched_plan_create(
+    int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
+    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, cudaStream_t s,
+    BatchedPlan **out, const char **why);
+int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, const char **why);
+void batched_plan_info(const BatchedPlan *p, int *stages, float *tune_ms);
+void batched_plan_destroy(BatchedPlan *p);
 }  // namespace knp_gb300
+
+struct knp_gb300_batched_plan
+{
+    knp_gb300::BatchedPlan *impl;
+};
 
 struct knp_gb300_backend
 {
@@ -358,17 +372,8 @@ int knp_gb300_bf16_gemm_tn(
     return rc == 0 ? KNP_GB300_OK : (rc == -1 ? KNP_GB300_E_INVALID : KNP_GB300_E_CUDA);
 }
 
-int knp_gb300_batched_lif_run(
-    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
-    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *d_rates,
-    uint64_t seed, int32_t *d_counts, uint32_t *d_record, uint64_t *events, float *ms, void *stream)
+static int batched_status(int rc, const char *why)
 {
-    const char *why = "";
-    unsigned long long ev = 0;
-    const int rc = knp_gb300::batched_lif_run(
-        n_layers, sizes, d_weights, leak, threshold, reset, refract, batch, steps, d_rates,
-        knp_gb300::stream_key(seed, 5), d_counts, d_record, &ev, ms, static_cast<cudaStream_t>(stream), &why);
-    if (events) *events = ev;
     if (rc == 0) return KNP_GB300_OK;
     g_error = why;
     switch (rc)
@@ -382,6 +387,73 @@ int knp_gb300_batched_lif_run(
         default:
             return KNP_GB300_E_CUDA;
     }
+}
+
+int knp_gb300_batched_lif_run(
+    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const float *d_rates,
+    uint64_t seed, int32_t *d_counts, uint32_t *d_record, uint64_t *events, float *ms, void *stream)
+{
+    const char *why = "";
+    unsigned long long ev = 0;
+    const int rc = knp_gb300::batched_lif_run(
+        n_layers, sizes, d_weights, leak, threshold, reset, refract, batch, steps, d_rates,
+        knp_gb300::stream_key(seed, 5), d_counts, d_record, &ev, ms, static_cast<cudaStream_t>(stream), &why);
+    if (events) *events = ev;
+    return batched_status(rc, why);
+}
+
+int knp_gb300_batched_plan_create(
+    int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
+    const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
+    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, void *stream,
+    knp_gb300_batched_plan **plan)
+{
+    if (!plan)
+    {
+        g_error = "plan is null";
+        return KNP_GB300_E_INVALID;
+    }
+    *plan = nullptr;
+    const char *why = "";
+    knp_gb300::BatchedPlan *p = nullptr;
+    const int rc = knp_gb300::batched_plan_create(
+        n_layers, sizes, d_weights, leak, threshold, reset, refract, batch, steps, sample_sizes, d_rates,
+        knp_gb300::stream_key(seed, 5), d_counts, d_record, autotune, static_cast<cudaStream_t>(stream), &p, &why);
+    if (rc == 0) *plan = new knp_gb300_batched_plan{p};
+    return batched_status(rc, why);
+}
+
+int knp_gb300_batched_plan_run(knp_gb300_batched_plan *plan, uint64_t *events, float *ms)
+{
+    if (!plan || !plan->impl)
+    {
+        g_error = "plan is null";
+        return KNP_GB300_E_INVALID;
+    }
+    const char *why = "";
+    unsigned long long ev = 0;
+    const int rc = knp_gb300::batched_plan_run(plan->impl, &ev, ms, &why);
+    if (events) *events = ev;
+    return batched_status(rc, why);
+}
+
+int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, float *tune_ms)
+{
+    if (!plan || !plan->impl)
+    {
+        g_error = "plan is null";
+        return KNP_GB300_E_INVALID;
+    }
+    knp_gb300::batched_plan_info(plan->impl, stages, tune_ms);
+    return KNP_GB300_OK;
+}
+
+void knp_gb300_batched_plan_destroy(knp_gb300_batched_plan *plan)
+{
+    if (!plan) return;
+    knp_gb300::batched_plan_destroy(plan->impl);
+    delete plan;
 }
 
 int knp_gb300_synchronize(knp_gb300_backend *b)

@@ -96,3 +96,76 @@ def test_batched_lif_full_config_runs():
     cfg = BT.dense_config(seed=4)
     counts, _, events, ms = BT.run(cfg)
     assert counts.shape == (256, 10) and events > 0 and ms > 0
+
+
+def _compare_with_plain(cfg, rec, counts):
+    """Spike mismatch of the batched form against the plain FP32 path on the same samples."""
+    from knp_gb300 import backend as B
+    from knp_gb300 import batched as BT
+    from knp_gb300 import types as T
+
+    net, sched = BT.plain_network(cfg)
+    t_max = int(cfg.steps.max())
+    out, b = B.run(net, [sched], t_max, accumulator=T.ACC_FP32)
+    for s in range(cfg.batch):
+        for t in range(int(cfg.steps[s])):
+            np.testing.assert_array_equal(_batched_spikes(cfg, rec, 0, s, t), BT.input_spikes(cfg, s, t))
+    total = mism = 0
+    for layer in range(1, len(cfg.sizes)):
+        n = cfg.sizes[layer]
+        uid = net.populations[layer - 1].uid
+        for t in range(t_max):
+            plain = out[uid][t]
+            for s in range(cfg.batch):
+                if t >= cfg.steps[s]:
+                    continue
+                g = _batched_spikes(cfg, rec, layer, s, t)
+                p = plain[(plain >= s * n) & (plain < (s + 1) * n)] - s * n
+                mism += np.setxor1d(g, p).size
+                total += n
+    return mism, total
+
+
+def test_batched_plan_graph_runs_repeat_exactly():
+    """A plan (one CUDA-graph launch per run, autotuned ring depth) gives identical counts, spike
+    records and event counts on every run, and the same results as the one-shot form."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(seed=10, batch=130, sizes=(200, 160, 96, 10), t_lo=20, t_hi=40, rate_max=0.3)
+    plan = BT.BatchedPlan(cfg, record=True, autotune=True)
+    try:
+        stages, tuned = plan.info()
+        assert stages in (3, 4, 5) and stages in tuned
+        ev1, ms1 = plan.run()
+        c1, r1 = plan.counts(), plan.record()
+        ev2, ms2 = plan.run()
+        c2, r2 = plan.counts(), plan.record()
+    finally:
+        plan.close()
+    assert ev1 == ev2 and ev1 > 0 and ms1 > 0 and ms2 > 0
+    np.testing.assert_array_equal(c1, c2)
+    for layer in r1:
+        np.testing.assert_array_equal(r1[layer], r2[layer])
+    c3, r3, ev3, _ = BT.run(cfg, record=True)
+    assert ev3 == ev1
+    np.testing.assert_array_equal(c3, c1)
+    for layer in r1:
+        np.testing.assert_array_equal(r3[layer], r1[layer])
+
+
+def test_batched_uneven_instance_sizes_match_plain_fp32_path():
+    """Samples that are network instances of uneven size (per-sample layer widths over shared
+    weights) against the plain FP32 path with the missing neurons silenced: at most 0.1% mismatch,
+    identical inputs, and no spike from a neuron beyond its sample's size."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.uneven_config(seed=8, batch=40)
+    counts, rec, events, ms = BT.run(cfg, record=True)
+    for layer in range(1, len(cfg.sizes)):
+        for s in range(cfg.batch):
+            for t in range(int(cfg.steps[s])):
+                g = _batched_spikes(cfg, rec, layer, s, t)
+                assert g.size == 0 or g.max() < cfg.sample_sizes[layer][s]
+    mism, total = _compare_with_plain(cfg, rec, counts)
+    assert mism <= 1e-3 * total, (mism, total)
+    assert events > 0 and ms > 0
