@@ -178,6 +178,21 @@ def reference_mt_sample(target_s: float = 30.0):
                       f"{o.events} events, {dt:.1f} s, restated multi-threaded backend step on {threads} threads"}
 
 
+def replica_totals(t_s: float, events: int, device: str = "cpu"):
+    """Whole-job numbers of N independent replicas (one per GPU, no data-path collective): the
+    slowest replica's time and the events of all replicas. One process: the inputs unchanged."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(t_s), float(events)
+    tt = torch.tensor([float(t_s)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    ee = torch.tensor([float(events)], device=device, dtype=torch.float64)
+    dist.all_reduce(ee)
+    return float(tt.item()), float(ee.item())
+
+
 def _flush_l2(dev):
     """Write a buffer larger than L2 (129 MB) so that the next timed run starts with a cold cache."""
     import torch
@@ -383,18 +398,7 @@ def main():
     with Clocks(local) as clk:
         ms = b.step_timed(args.steps)
     ev1, sp1, _ = b.counters()
-    t = ms / 1e3
-    if dist is not None:
-        import torch
-
-        tt = torch.tensor([t], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-        ee = torch.tensor([float(ev1 - ev0)], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(ee)
-        events_all = float(ee.item())
-    else:
-        events_all = float(ev1 - ev0)
+    t, events_all = replica_totals(ms / 1e3, ev1 - ev0, f"cuda:{local}" if dist is not None else "cpu")
     events = ev1 - ev0
     spikes = sp1 - sp0
     value = events_all / t

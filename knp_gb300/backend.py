@@ -252,7 +252,7 @@ class GB300Backend:
             out = np.empty(cnt.value, np.uint32)
             self._chk(self._lib.knp_gb300_read_spikes(self._h, T.to_c_uid(pop), step, out.size, _ptr(out),
                                                       ctypes.byref(cnt)))
-        return out[: cnt.value].copy()
+        return out[: cnt.value]
 
     def discard_spikes(self, before_step: int):
         self._chk(self._lib.knp_gb300_discard_spikes(self._h, before_step))

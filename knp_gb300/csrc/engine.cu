@@ -1199,8 +1199,9 @@ void Backend::alloc_recording(PopulationSlot &p)
     any_recording_ = true;
 }
 
-// Copies the recorded bitmaps of steps [drained_to_, step_) to the host and turns each into its
-// ascending spike indexes (the order of the reference's SpikeMessage, populations_old.h:104-118).
+// Copies the recorded bitmaps of steps [drained_to_, step_) to the host (per step: the bitmap and
+// its spike count); read_spikes expands a step's bitmap into ascending spike indexes, the order of
+// the reference's SpikeMessage (populations_old.h:104-118).
 void Backend::drain_recordings()
 {
     const uint64_t steps = step_ - drained_to_;
@@ -1238,14 +1239,10 @@ void Backend::drain_recordings()
                 const uint64_t step = drained_to_ + k;
                 if (step < q->record_from) continue;
                 const uint32_t *bits = rec_host_ + k * W;
-                size_t c = 0;
-                for (size_t w = 0; w < W; ++w) c += static_cast<size_t>(__builtin_popcount(bits[w]));
-                std::vector<uint32_t> v;
-                v.reserve(c);
-                for (size_t w = 0; w < W; ++w)
-                    for (uint32_t x = bits[w]; x; x &= x - 1)
-                        v.push_back(static_cast<uint32_t>(w * 32 + __builtin_ctz(x)));
-                q->recorded[step] = std::move(v);
+                RecordedStep &r = q->recorded[step];
+                r.bits.assign(bits, bits + W);
+                r.count = 0;
+                for (size_t w = 0; w < W; ++w) r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
             }
         }
     }
@@ -1263,8 +1260,12 @@ void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t 
     if (step >= drained_to_) drain_recordings();
     auto it = q->recorded.find(step);
     if (it == q->recorded.end()) throw Error(KNP_GB300_E_INVALID, "spikes of this step were not recorded or were discarded");
-    *n = static_cast<uint32_t>(it->second.size());
-    std::copy_n(it->second.begin(), std::min<size_t>(cap, it->second.size()), out);
+    // Ascending indexes straight from the step's bitmap into the caller's buffer.
+    const RecordedStep &r = it->second;
+    *n = r.count;
+    uint32_t k = 0;
+    for (size_t w = 0; w < r.bits.size() && k < cap; ++w)
+        for (uint32_t x = r.bits[w]; x && k < cap; x &= x - 1) out[k++] = static_cast<uint32_t>(w * 32 + __builtin_ctz(x));
 }
 
 void Backend::discard_spikes(uint64_t before)

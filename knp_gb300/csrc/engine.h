@@ -72,6 +72,12 @@ private:
     size_t bytes_ = 0;
 };
 
+struct RecordedStep
+{
+    std::vector<uint32_t> bits;  // bit i of word i / 32: neuron i fired
+    uint32_t count = 0;
+};
+
 struct PopulationSlot
 {
     Uid uid;
@@ -92,8 +98,8 @@ struct PopulationSlot
     uint32_t *rec_bits = nullptr;
     uint32_t rec_words = 0, rec_slots = 0;
     bool has_external_impacts = false;
-    // recorded spikes drained to the host: per step, ascending indexes
-    std::map<uint64_t, std::vector<uint32_t>> recorded;
+    // recorded spikes drained to the host: per step, the spike bitmap and its count
+    std::map<uint64_t, RecordedStep> recorded;
     uint64_t record_from = 0;
 };
 
