@@ -818,12 +818,14 @@ void Backend::build_pull(ProjectionSlot &p)
     if (free_b < p.n_syn * 30 + (1ull << 30)) return;
     uint32_t *packed = nullptr;
     float *w = nullptr;
+    uint16_t *w16 = nullptr;
     long long *seg = nullptr;
     const bool negate = p.dev.uniform_type == KNP_OUT_INHIBITORY_CURRENT;
     KNP_CUDA(build_pull_layout(p.n_syn, p.n_rows, post->n, p.row_ptr, p.col, p.w, p.delay_d, negate, g, &packed, &w,
-                               &seg, stream_));
+                               &w16, &seg, stream_));
     arena_.adopt(packed, p.n_syn * 4);
-    arena_.adopt(w, p.n_syn * 4);
+    if (w) arena_.adopt(w, p.n_syn * 4);
+    if (w16) arena_.adopt(w16, p.n_syn * 2);
     arena_.adopt(seg, (static_cast<size_t>(g.max_delay) * g.n_tiles + 1) * 8);
     g.bitmap = arena_.make<uint32_t>(static_cast<size_t>(g.hist_slots) * g.words);
     g.pulled = arena_.make<uint32_t>(g.hist_slots);

@@ -175,7 +175,8 @@ struct PullDev
     uint32_t n_post;
     const long long *seg_ptr;  // [max_delay * n_tiles + 1]
     const uint32_t *packed;
-    const float *w;
+    const float *w;           // FP32 weights, or null when w16 holds them
+    const uint16_t *w16;      // FP16 bit patterns, used when every weight is exactly an FP16 value
     uint64_t padded_entries;  // entries of packed / w (segments padded to multiples of 8)
 };
 
@@ -229,10 +230,12 @@ void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 size_t gather_smem_bytes(const PullDev &p, int grid);
+// On return exactly one of *w_out (FP32) and *w16_out (FP16, when every weight is exactly an FP16
+// value) is non-null; the caller owns it, *packed_out and *seg_out.
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
-    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, long long **seg_out,
-    cudaStream_t s);
+    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, uint16_t **w16_out,
+    long long **seg_out, cudaStream_t s);
 void launch_apply_impacts(
     const RingView &ring, const uint32_t *post, const float *value, const uint8_t *type, int forcing, uint32_t n,
     Control *ctl, cudaStream_t s);

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cuda_fp16.h>
 
 #include "kernels.h"
 
@@ -23,7 +24,8 @@ namespace
 {
 
 constexpr int kGatherThreads = 1024;
-constexpr int kUnroll = 2;  // groups of 8 synapses in flight per lane (16 synapses)
+constexpr int kLaneRun = 8;   // consecutive synapses per lane (segments are padded to multiples of it)
+constexpr int kUnroll = 2;    // groups of kLaneRun synapses in flight per lane
 
 __global__ void row_of_kernel(const long long *row_ptr, uint32_t n_rows, uint32_t *row_of)
 {
@@ -105,6 +107,23 @@ __global__ void pull_fill_kernel(
     }
 }
 
+// flag |= 1 if some weight is not exactly an FP16 value.
+__global__ void half_exact_kernel(const float *w, uint64_t n, unsigned int *flag)
+{
+    bool bad = false;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        bad = bad || !(__half2float(__float2half_rn(w[i])) == w[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
+__global__ void to_half_kernel(const float *w, uint64_t n, uint16_t *out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        out[i] = __half_as_ushort(__float2half_rn(w[i]));
+}
+
 __device__ __forceinline__ void reduce_runs(uint32_t jl, float val, float *acc)
 {
     const unsigned full = 0xffffffffu;
@@ -123,6 +142,8 @@ __device__ __forceinline__ void reduce_runs(uint32_t jl, float val, float *acc)
     if (tail && jl != 0xFFFFFFFFu && val != 0.0f) atomicAdd(acc + jl, val);
 }
 
+// kHalf: weights stored as FP16 (exact); one 16-byte load gives a lane's 8 weights.
+template <bool kHalf>
 __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev p, Control *ctl)
 {
     extern __shared__ uint4 smem_u4[];
@@ -155,13 +176,15 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
         for (uint32_t tile = t0; tile < t1; ++tile)
         {
             const size_t si = static_cast<size_t>(d - 1) * g.n_tiles + tile;
-            // Segments start and end on 8-entry boundaries: a lane takes 8 consecutive synapses
-            // with two 16-byte loads of keys and two of weights. Padding entries (and lanes past the
-            // segment) are key 0 / weight 0: presynaptic neuron 0, target 0, contributing nothing.
-            const long long oa = g.seg_ptr[si] >> 3, ob = g.seg_ptr[si + 1] >> 3;
+            // Segments start and end on 8-entry boundaries: a lane takes 8 consecutive synapses per
+            // group (two 16-byte loads of keys; one of FP16 or two of FP32 weights), two groups in
+            // flight. Padding entries (and lanes past the segment) are key 0 / weight 0: presynaptic
+            // neuron 0, target 0, contributing nothing.
+            const long long oa = g.seg_ptr[si] / kLaneRun, ob = g.seg_ptr[si + 1] / kLaneRun;
             float *acc_t = acc + static_cast<size_t>(tile - t0) * kPullTile;
             const uint4 *pk = reinterpret_cast<const uint4 *>(g.packed);
             const float4 *pw = reinterpret_cast<const float4 *>(g.w);
+            const uint4 *ph = reinterpret_cast<const uint4 *>(g.w16);
             for (long long base = oa + warp_base; base < ob; base += static_cast<long long>(blockDim.x) * kUnroll)
             {
                 uint4 key[kUnroll][2];
@@ -176,8 +199,20 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
                     {
                         key[u][0] = __ldcs(pk + 2 * o);
                         key[u][1] = __ldcs(pk + 2 * o + 1);
-                        w[u][0] = __ldcs(pw + 2 * o);
-                        w[u][1] = __ldcs(pw + 2 * o + 1);
+                        if (kHalf)
+                        {
+                            const uint4 h = __ldcs(ph + o);
+                            const __half2 *h2 = reinterpret_cast<const __half2 *>(&h);
+                            const float2 a = __half22float2(h2[0]), b = __half22float2(h2[1]);
+                            const float2 c = __half22float2(h2[2]), e = __half22float2(h2[3]);
+                            w[u][0] = make_float4(a.x, a.y, b.x, b.y);
+                            w[u][1] = make_float4(c.x, c.y, e.x, e.y);
+                        }
+                        else
+                        {
+                            w[u][0] = __ldcs(pw + 2 * o);
+                            w[u][1] = __ldcs(pw + 2 * o + 1);
+                        }
                     }
                 }
 #pragma unroll
@@ -257,21 +292,30 @@ size_t gather_smem_bytes(const PullDev &p, int grid)
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s)
 {
     const size_t smem = gather_smem_bytes(p.pull, grid);
-    gather_kernel<<<grid, kGatherThreads, smem, s>>>(p, ctl);
+    if (p.pull.w16)
+        gather_kernel<true><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+    else
+        gather_kernel<false><<<grid, kGatherThreads, smem, s>>>(p, ctl);
 }
 
 cudaError_t set_gather_smem(size_t bytes)
 {
-    return cudaFuncSetAttribute(gather_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    cudaError_t err =
+        cudaFuncSetAttribute(gather_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (err != cudaSuccess) return err;
+    return cudaFuncSetAttribute(gather_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(bytes));
 }
 
 // Builds the sorted (delay, postsynaptic) layout from a projection's CSR. Allocates the outputs
 // with cudaMalloc (the caller owns them) and its temporaries with cudaMallocAsync.
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
-    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, long long **seg_out,
-    cudaStream_t s)
+    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, uint16_t **w16_out,
+    long long **seg_out, cudaStream_t s)
 {
+    *w16_out = nullptr;
+    unsigned int *flag = nullptr;
     const uint32_t D = out.max_delay;
     const uint32_t n_tiles = (n_post + kPullTile - 1) / kPullTile;
     out.n_tiles = n_tiles;
@@ -315,7 +359,8 @@ cudaError_t build_pull_layout(
         std::vector<long long> raw(n_seg + 1), pad(n_seg + 1, 0);
         err = cudaMemcpy(raw.data(), seg_raw, raw.size() * sizeof(long long), cudaMemcpyDeviceToHost);
         if (err != cudaSuccess) goto done;
-        for (size_t i = 0; i < n_seg; ++i) pad[i + 1] = pad[i] + ((raw[i + 1] - raw[i] + 7) & ~7ll);
+        for (size_t i = 0; i < n_seg; ++i)
+            pad[i + 1] = pad[i] + ((raw[i + 1] - raw[i] + kLaneRun - 1) / kLaneRun) * kLaneRun;
         err = cudaMemcpy(*seg_out, pad.data(), pad.size() * sizeof(long long), cudaMemcpyHostToDevice);
         if (err != cudaSuccess) goto done;
         const size_t padded = static_cast<size_t>(pad[n_seg]) * sizeof(uint32_t) + 16;
@@ -332,7 +377,31 @@ cudaError_t build_pull_layout(
     out.seg_ptr = *seg_out;
     out.packed = *packed_out;
     out.w = *w_out;
+    out.w16 = nullptr;
+    {
+        // Lossless 16-bit weights when every weight is exactly an FP16 value (6 instead of 8 bytes
+        // per synapse streamed by the gather).
+        const uint64_t n_pad = out.padded_entries;
+        KNP_TRY(cudaMallocAsync(&flag, sizeof(unsigned int), s));
+        KNP_TRY(cudaMemsetAsync(flag, 0, sizeof(unsigned int), s));
+        half_exact_kernel<<<grid_for(n_pad), 256, 0, s>>>(*w_out, n_pad, flag);
+        unsigned int h_flag = 1;
+        KNP_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        KNP_TRY(cudaStreamSynchronize(s));
+        if (h_flag == 0)
+        {
+            KNP_TRY(cudaMalloc(w16_out, n_pad * sizeof(uint16_t) + 16));
+            to_half_kernel<<<grid_for(n_pad), 256, 0, s>>>(*w_out, n_pad, *w16_out);
+            KNP_TRY(cudaGetLastError());
+            KNP_TRY(cudaStreamSynchronize(s));
+            cudaFree(*w_out);
+            *w_out = nullptr;
+            out.w = nullptr;
+            out.w16 = *w16_out;
+        }
+    }
 done:
+    if (flag) cudaFreeAsync(flag, s);
     if (seg_raw) cudaFreeAsync(seg_raw, s);
     if (tmp) cudaFreeAsync(tmp, s);
     if (row_of) cudaFreeAsync(row_of, s);

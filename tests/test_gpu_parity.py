@@ -153,6 +153,37 @@ def test_gather_inhibitory_projection():
     assert b.counters()[0] == oo.events
 
 
+@pytest.mark.parametrize("k_range", [(-16, 48), (-3001, 3001)])
+def test_gather_weight_storage(k_range):
+    """The gather layout stores weights as FP16 when every weight is exactly an FP16 value (k/256 with
+    |k| < 2048) and as FP32 otherwise (k/256 up to ~11.7 needs 12 significant bits); both give the
+    oracle's spike trains bit for bit."""
+    from knp_gb300 import backend as B
+    from oracle import oracle as orc
+
+    n, fan = 5000, 220  # >= 2^20 synapses: the projection gets a gather layout
+    pop = N.Population(T.uid_from_int(61), T.BLIFAT, T.blifat_defaults(n))
+    chan = T.uid_from_int(69)
+    k = [N.stream_key(12, s) for s in (1, 2, 3)]
+    pre, post, w, d = N.fixed_fan_in_pre(*k, n, n, fan, k_range[0], k_range[1], 1, 8)
+    rec = N.Projection(T.uid_from_int(62), T.DELTA, pop.uid, pop.uid, pre, post, w, d)
+    ar = np.arange(n, dtype=np.uint32)
+    bg = N.Projection(T.uid_from_int(63), T.DELTA, T.NULL_UID, pop.uid, ar, ar.copy(), np.ones(n, np.float32),
+                      np.ones(n, np.uint32))
+    net = N.Network([pop], [bg, rec], [(bg.uid, chan)])
+    sched = N.bernoulli_schedule(chan, 13, n, 50, 0.02)
+    b = B.GB300Backend()
+    b.load_network(net)
+    b.set_pull_threshold(rec.uid, 0.0)
+    b._init()
+    b.load_spike_schedule(sched)
+    b.step(50)
+    o, oo = orc.run(net, [sched], 50)
+    for t in range(50):
+        np.testing.assert_array_equal(b.spikes(pop.uid, t), o[pop.uid][t], err_msg=f"step {t}")
+    assert b.counters()[0] == oo.events
+
+
 def test_device_generated_projection_matches_host_arrays():
     """The device-side fixed fan-in generator builds exactly the synapses of network.fixed_fan_in_pre."""
     from knp_gb300 import backend as B
