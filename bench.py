@@ -36,6 +36,7 @@ SEED = 2
 N = 1_000_000
 FAN_IN = 1000
 P_BG = 0.005
+GATHER_DRAM_BYTES_PER_SYNAPSE = (0.962e9 + 3.4e6) / 2e8
 
 
 def peaks():
@@ -422,7 +423,13 @@ def main():
     a_bytes, a_ms = (proj_bytes, proj_ms) if dominant == "projection" else (pop_bytes, pop_ms)
     achieved = a_bytes / (a_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": f"{dominant} phase", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                "frac": achieved / hbm, "peak_source": src,
+                # DRAM bytes (read + write) of one saturated gather launch, measured with ncu on the
+                # same configuration at 200k neurons (0.962 GB read + 3.4 MB written for 2e8
+                # synapses), scaled by the synapse count; a step of the timed region that scatters
+                # moves far less.
+                "traffic": GATHER_DRAM_BYTES_PER_SYNAPSE * n_neurons * args.fan_in,
+                "traffic_per": "saturated gathered step (ncu at 200k neurons, scaled by synapses)",
                 "phase_ms_per_step": {"population": pop_ms, "projection": proj_ms,
                                       "stdp": ph[2] / args.profile_steps, "step_end": ph[3] / args.profile_steps},
                 "algorithmic_bytes_per_step": {"projection": proj_bytes, "population": pop_bytes},
