@@ -787,11 +787,12 @@ cudaError_t set_gather_smem(size_t bytes);
 
 int Backend::gather_grid(const ProjectionSlot &p) const
 {
-    return static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(p.dev.pull.n_tiles, sm_count_)));
+    return static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(p.dev.pull.n_windows, sm_count_)));
 }
 
 // The gather form is built for large delta projections fed by one population into an FP32 ring,
-// when the device has room for a second (8 B / synapse) copy of the synapses.
+// when the device has room for a second (6 or 8 B / synapse) copy of the synapses and the build's
+// temporaries.
 void Backend::build_pull(ProjectionSlot &p)
 {
     PopulationSlot *post = find_pop(p.post_uid);
@@ -801,32 +802,25 @@ void Backend::build_pull(ProjectionSlot &p)
     if (rg.fixed || (rg.forced && p.dev.forcing)) return;
     if (p.dev.type || (p.dev.uniform_type != KNP_OUT_EXCITATORY && p.dev.uniform_type != KNP_OUT_INHIBITORY_CURRENT))
         return;
-    if (p.n_rows > (1u << (32 - kPullTileBits))) return;
     if (static_cast<uint64_t>(p.max_delay) * post->n >= 0xFFFFFFFFull) return;
     PullDev g{};
     g.words = round_up((p.n_rows + 31) / 32, 4);
     g.max_delay = p.max_delay;
     g.hist_slots = p.max_delay + 1;
-    g.n_tiles = (post->n + kPullTile - 1) / kPullTile;
-    const int grid = static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(g.n_tiles, sm_count_)));
+    g.n_windows = (post->n + kPullWindow - 1) / kPullWindow;
+    const int grid = static_cast<int>(std::max<uint32_t>(1, std::min<uint32_t>(g.n_windows, sm_count_)));
     const size_t smem = gather_smem_bytes(g, grid);
     int smem_max = 0;
     KNP_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
     if (smem > static_cast<size_t>(smem_max)) return;
     size_t free_b = 0, total_b = 0;
     KNP_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    if (free_b < p.n_syn * 30 + (1ull << 30)) return;
-    uint32_t *packed = nullptr;
-    float *w = nullptr;
-    uint16_t *w16 = nullptr;
-    long long *seg = nullptr;
+    if (free_b < p.n_syn * 36 + static_cast<size_t>(p.max_delay) * post->n * 16 + (1ull << 30)) return;
     const bool negate = p.dev.uniform_type == KNP_OUT_INHIBITORY_CURRENT;
-    KNP_CUDA(build_pull_layout(p.n_syn, p.n_rows, post->n, p.row_ptr, p.col, p.w, p.delay_d, negate, g, &packed, &w,
-                               &w16, &seg, stream_));
-    arena_.adopt(packed, p.n_syn * 4);
-    if (w) arena_.adopt(w, p.n_syn * 4);
-    if (w16) arena_.adopt(w16, p.n_syn * 2);
-    arena_.adopt(seg, (static_cast<size_t>(g.max_delay) * g.n_tiles + 1) * 8);
+    PullBuffers bufs;
+    KNP_CUDA(build_pull_layout(p.n_syn, p.n_rows, post->n, p.row_ptr, p.col, p.w, p.delay_d, negate, g, bufs, stream_));
+    for (int i = 0; i < 6; ++i)
+        if (bufs.ptr[i]) arena_.adopt(bufs.ptr[i], bufs.bytes[i]);
     g.bitmap = arena_.make<uint32_t>(static_cast<size_t>(g.hist_slots) * g.words);
     g.pulled = arena_.make<uint32_t>(g.hist_slots);
     g.threshold = static_cast<uint32_t>(std::max(1.0, std::ceil(p.pull_fraction * p.n_rows)));

@@ -157,27 +157,42 @@ struct SpikeSource
 // Gather ("pull") form of a projection. A step whose spike count reaches `threshold` is not
 // scattered: its spikes go to a bitmap slot instead, and the gather kernel adds, for every target,
 // the weights of its synapses whose presynaptic neuron spiked d steps before the target step.
-// Synapses are stored sorted by (delay, postsynaptic neuron): for delay d and postsynaptic tile
-// tau (kPullTile neurons) the segment is [seg_ptr[(d-1) * n_tiles + tau], ... + 1); each entry is a
-// packed (pre << kPullTileBits | post - tile base) and a weight (negated for inhibitory current).
-constexpr int kPullTileBits = 9;
-constexpr int kPullTile = 1 << kPullTileBits;
+// Layout (sliced ELL): for each delay d and each window of kPullWindow consecutive targets, the
+// targets are ordered by decreasing number of synapses with delay d (perm: sorted position -> target
+// offset in the window) and cut into slices of kPullSlice. Slice q holds its 32 targets' synapses
+// column-major: entry k of the slice's lane L (its L-th target) is at slice_ptr[q] + 32 k + L, and
+// every lane's list is padded with zero entries (presynaptic 0, weight 0) to slice_len[q], the
+// longest list of the slice. A lane therefore owns one target for a whole slice: no atomics, and
+// each warp load reads 32 consecutive entries. Slices are indexed q = ((d - 1) * n_windows + window)
+// * kPullSlicesPerWindow + slice-in-window.
+constexpr int kPullWindow = 256;
+constexpr int kPullSlice = 32;
+constexpr int kPullSlicesPerWindow = kPullWindow / kPullSlice;
 
 struct PullDev
 {
     uint32_t *bitmap;       // [hist_slots][words] spikes of pulled steps
     uint32_t *pulled;       // [hist_slots] 1 if that step was pulled
     uint32_t hist_slots;    // max_delay + 1
-    uint32_t words;         // ceil(n_rows / 32)
+    uint32_t words;         // ceil(n_rows / 32), rounded up to 4
     uint32_t threshold;     // minimum spike count for pulling a step
     uint32_t max_delay;
-    uint32_t n_tiles;
+    uint32_t n_windows;     // ceil(n_post / kPullWindow)
     uint32_t n_post;
-    const long long *seg_ptr;  // [max_delay * n_tiles + 1]
-    const uint32_t *packed;
-    const float *w;           // FP32 weights, or null when w16 holds them
-    const uint16_t *w16;      // FP16 bit patterns, used when every weight is exactly an FP16 value
-    uint64_t padded_entries;  // entries of packed / w (segments padded to multiples of 8)
+    const long long *slice_ptr;  // [max_delay * n_windows * kPullSlicesPerWindow + 1] first entry of each slice
+    const uint32_t *slice_len;   // [max_delay * n_windows * kPullSlicesPerWindow] entries per lane
+    const uint8_t *perm;         // [max_delay * n_windows * kPullWindow] target offset in its window
+    const uint32_t *packed;      // presynaptic neuron of each entry
+    const float *w;              // FP32 weights (negated for inhibitory current), or null when w16 holds them
+    const uint16_t *w16;         // FP16 bit patterns, used when every weight is exactly an FP16 value
+    uint64_t padded_entries;     // entries of packed / w
+};
+
+// Device buffers of a gather layout (cudaMalloc'd; the caller takes ownership), with their sizes.
+struct PullBuffers
+{
+    void *ptr[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t bytes[6] = {0, 0, 0, 0, 0, 0};
 };
 
 struct ProjectionDev
@@ -230,12 +245,11 @@ void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 size_t gather_smem_bytes(const PullDev &p, int grid);
-// On return exactly one of *w_out (FP32) and *w16_out (FP16, when every weight is exactly an FP16
-// value) is non-null; the caller owns it, *packed_out and *seg_out.
+// Builds the gather layout of a projection from its CSR (weights stored as FP16 when every weight
+// is exactly an FP16 value, else FP32) and fills `out`; the buffers go to `bufs`.
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
-    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, uint16_t **w16_out,
-    long long **seg_out, cudaStream_t s);
+    const uint8_t *delay, bool negate, PullDev &out, PullBuffers &bufs, cudaStream_t s);
 void launch_apply_impacts(
     const RingView &ring, const uint32_t *post, const float *value, const uint8_t *type, int forcing, uint32_t n,
     Control *ctl, cudaStream_t s);

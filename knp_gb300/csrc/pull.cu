@@ -3,17 +3,18 @@
 // The scatter kernel costs one global atomic per synaptic event, which limits a step in which a
 // large share of the presynaptic neurons fire. For such a step the scatter kernel only records the
 // spikes in a bitmap slot; the gather kernel, run at the end of every step for the next step t,
-// walks the synapses sorted by (delay d, postsynaptic neuron), and for every delay whose step t - d
-// was recorded stages that bitmap in shared memory and adds the weights of the synapses whose
-// presynaptic bit is set. Contributions are reduced per target with a warp-segmented scan and one
-// shared-memory atomic per run of equal targets, then added once to the target's input-ring slot of
-// step t. The sums are the same impacts the scatter would have delivered at step t (delay
-// convention of delta_impl.h:78-79), added in another order, which is exact for the FP32 ring
-// (dyadic weights); populations with the fixed-point ring never use this form.
+// reads for every delay whose step t - d was recorded the synapses of that delay in the sliced ELL
+// layout of kernels.h: each lane owns one target of a slice and sums, down its list, the weights of
+// the synapses whose presynaptic bit is set (bitmap staged in shared memory), then adds the sum to
+// the target's accumulator; the accumulators are added once to the targets' input-ring slot of step
+// t. The sums are the same impacts the scatter would have delivered at step t (delay convention of
+// delta_impl.h:78-79), added in another order, which is exact for the FP32 ring (dyadic weights);
+// populations with the fixed-point ring never use this form.
 #include <cstdint>
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 #include <cuda_fp16.h>
 
 #include "kernels.h"
@@ -24,8 +25,7 @@ namespace
 {
 
 constexpr int kGatherThreads = 1024;
-constexpr int kLaneRun = 8;   // consecutive synapses per lane (segments are padded to multiples of it)
-constexpr int kUnroll = 2;    // groups of kLaneRun synapses in flight per lane
+constexpr int kDepth = 16;  // list entries per lane in flight
 
 __global__ void row_of_kernel(const long long *row_ptr, uint32_t n_rows, uint32_t *row_of)
 {
@@ -36,74 +36,97 @@ __global__ void row_of_kernel(const long long *row_ptr, uint32_t n_rows, uint32_
         for (long long e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32) row_of[e] = r;
 }
 
+// key = (d - 1) * n_post + post, or the sentinel max_delay * n_post for delay 0 (never delivered);
+// count[key]++ for the delivered ones.
 __global__ void pull_key_kernel(
     uint64_t n, const int32_t *col, const uint8_t *delay, uint32_t n_post, uint32_t max_delay, uint32_t *key,
-    uint32_t *val)
+    uint32_t *val, uint32_t *count)
 {
     for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < n;
          e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
     {
         const uint32_t d = delay[e];
-        // Delay-0 synapses never deliver; they sort after every segment.
-        key[e] = d == 0 ? max_delay * n_post : (d - 1) * n_post + static_cast<uint32_t>(col[e]);
+        const uint32_t k = d == 0 ? max_delay * n_post : (d - 1) * n_post + static_cast<uint32_t>(col[e]);
+        key[e] = k;
         val[e] = static_cast<uint32_t>(e);
+        if (d != 0) atomicAdd(count + k, 1u);
     }
 }
 
-// seg[i] for i = (d - 1) * n_tiles + tile: first sorted position whose key >= (d - 1) * n_post + tile * kPullTile.
-__global__ void pull_seg_kernel(
-    const uint32_t *keys, uint64_t n, uint32_t n_post, uint32_t n_tiles, uint32_t max_delay, long long *seg)
+// One block of kPullWindow threads per (delay, window): order the window's targets by decreasing
+// synapse count (ties by target), write perm (sorted position -> target offset), inv (target offset
+// -> sorted position) and each slice's longest list.
+__global__ void pull_window_kernel(
+    const uint32_t *count, uint32_t n_post, uint32_t n_windows, uint8_t *perm, uint8_t *inv, uint32_t *slice_len)
 {
-    const uint64_t total = static_cast<uint64_t>(max_delay) * n_tiles;
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i <= total;
+    __shared__ uint32_t key[kPullWindow];
+    __shared__ uint32_t cnt[kPullWindow];
+    const uint32_t dw = blockIdx.x;  // (d - 1) * n_windows + window
+    const uint32_t d0 = dw / n_windows, win = dw % n_windows;
+    const uint32_t t = threadIdx.x;
+    const uint32_t j = win * kPullWindow + t;
+    const uint32_t c = j < n_post ? count[static_cast<size_t>(d0) * n_post + j] : 0u;
+    cnt[t] = c;
+    // Descending by count, then ascending by target: sort (min(c, 2^24 - 1) << 8 | 255 - t) descending.
+    key[t] = (min(c, 0xFFFFFFu) << 8) | (kPullWindow - 1 - t);
+    __syncthreads();
+    // Bitonic sort, descending.
+    for (uint32_t size = 2; size <= kPullWindow; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1)
+        {
+            const uint32_t partner = t ^ stride;
+            if (partner > t)
+            {
+                const bool desc = (t & size) == 0;
+                const uint32_t a = key[t], b = key[partner];
+                if (desc ? a < b : a > b)
+                {
+                    key[t] = b;
+                    key[partner] = a;
+                }
+            }
+            __syncthreads();
+        }
+    const uint32_t tt = kPullWindow - 1 - (key[t] & 0xFFu);  // target offset at sorted position t
+    perm[static_cast<size_t>(dw) * kPullWindow + t] = static_cast<uint8_t>(tt);
+    inv[static_cast<size_t>(dw) * kPullWindow + tt] = static_cast<uint8_t>(t);
+    // Longest list of each slice (sorted positions [32 s, 32 s + 32)).
+    uint32_t m = cnt[tt];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((t & 31) == 0) slice_len[static_cast<size_t>(dw) * kPullSlicesPerWindow + t / 32] = m;
+}
+
+__global__ void slice_entries_kernel(const uint32_t *slice_len, uint64_t n, long long *entries)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-    {
-        uint64_t target;
-        if (i == total)
-            target = static_cast<uint64_t>(max_delay) * n_post;
-        else
-            target = (i / n_tiles) * static_cast<uint64_t>(n_post) + (i % n_tiles) * kPullTile;
-        uint64_t lo = 0, hi = n;
-        while (lo < hi)
-        {
-            const uint64_t mid = (lo + hi) >> 1;
-            if (keys[mid] < target)
-                lo = mid + 1;
-            else
-                hi = mid;
-        }
-        seg[i] = static_cast<long long>(lo);
-    }
+        entries[i] = static_cast<long long>(slice_len[i]) * kPullSlice;
 }
 
-// One warp per segment: copy the segment's synapses (sorted positions [seg[s], seg[s+1])) to
-// padded positions [pseg[s], pseg[s+1]) as packed (pre << 9 | post mod 512) + weight, and fill the
-// padding (up to 7 entries, so that every segment starts on a 32-byte boundary) with key 0 / weight 0.
+// Places every delivered synapse (sorted by key, so a target's synapses of one delay are
+// consecutive from first[key]) at its slice entry.
 __global__ void pull_fill_kernel(
-    uint64_t n_seg, const long long *seg, const long long *pseg, const uint32_t *order, const uint32_t *row_of,
-    const int32_t *col, const float *w, bool negate, uint32_t *packed, float *w_out)
+    uint64_t n, const uint32_t *keys, const uint32_t *order, const long long *first, const uint8_t *inv,
+    const long long *slice_ptr, const uint32_t *row_of, const float *w, bool negate, uint32_t n_post,
+    uint32_t n_windows, uint32_t max_delay, uint32_t *packed, float *w_out)
 {
-    const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
-    const uint64_t n_warps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    for (uint64_t sg = warp; sg < n_seg; sg += n_warps)
+    const uint32_t sentinel = max_delay * n_post;
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < n;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x)
     {
-        const long long a = seg[sg], b = seg[sg + 1], pa = pseg[sg], pb = pseg[sg + 1];
-        for (long long i = lane; i < pb - pa; i += 32)
-        {
-            if (i < b - a)
-            {
-                const uint32_t e = order[a + i];
-                packed[pa + i] = (row_of[e] << kPullTileBits) | (static_cast<uint32_t>(col[e]) & (kPullTile - 1));
-                const float x = w[e];
-                w_out[pa + i] = negate ? -x : x;
-            }
-            else
-            {
-                packed[pa + i] = 0u;
-                w_out[pa + i] = 0.0f;
-            }
-        }
+        const uint32_t k = keys[p];
+        if (k >= sentinel) continue;
+        const uint32_t d0 = k / n_post, j = k % n_post;
+        const uint32_t dw = d0 * n_windows + j / kPullWindow;
+        const uint32_t pos = inv[static_cast<size_t>(dw) * kPullWindow + j % kPullWindow];
+        const size_t q = static_cast<size_t>(dw) * kPullSlicesPerWindow + pos / kPullSlice;
+        const long long rank = static_cast<long long>(p) - first[k];
+        const long long at = slice_ptr[q] + rank * kPullSlice + (pos % kPullSlice);
+        const uint32_t e = order[p];
+        packed[at] = row_of[e];
+        const float x = w[e];
+        w_out[at] = negate ? -x : x;
     }
 }
 
@@ -124,39 +147,21 @@ __global__ void to_half_kernel(const float *w, uint64_t n, uint16_t *out)
         out[i] = __half_as_ushort(__float2half_rn(w[i]));
 }
 
-__device__ __forceinline__ void reduce_runs(uint32_t jl, float val, float *acc)
-{
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const uint32_t prev = __shfl_up_sync(full, jl, 1);
-    const bool head = lane == 0 || jl != prev;
-    const unsigned hm = __ballot_sync(full, head);
-    const int my_head = 31 - __clz(hm & (full >> (31 - lane)));
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        const float v = __shfl_up_sync(full, val, o);
-        if (lane - o >= my_head) val = __fadd_rn(val, v);
-    }
-    const bool tail = lane == 31 || ((hm >> (lane + 1)) & 1u);
-    if (tail && jl != 0xFFFFFFFFu && val != 0.0f) atomicAdd(acc + jl, val);
-}
-
-// kHalf: weights stored as FP16 (exact); one 16-byte load gives a lane's 8 weights.
+// kHalf: weights stored as FP16 (exact).
 template <bool kHalf>
 __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev p, Control *ctl)
 {
     extern __shared__ uint4 smem_u4[];
+    __shared__ uint32_t s_next;  // next slice of the current delay to hand out
     const PullDev &g = p.pull;
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem_u4);
     float *acc = reinterpret_cast<float *>(bm + g.words);
     const uint32_t G = gridDim.x;
-    const uint32_t t0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * g.n_tiles / G);
-    const uint32_t t1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * g.n_tiles / G);
-    const uint32_t n_acc = (t1 - t0) * kPullTile;
+    const uint32_t w0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * g.n_windows / G);
+    const uint32_t w1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * g.n_windows / G);
+    const uint32_t n_acc = (w1 - w0) * kPullWindow;
     const unsigned long long tn = ctl->step + 1;  // the step whose input this gather completes
     const int lane = threadIdx.x & 31;
-    const uint32_t warp_base = threadIdx.x & ~31u;
 
     bool any = false;
     for (uint32_t d = 1; d <= g.max_delay && d <= tn; ++d)
@@ -172,80 +177,45 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
         __syncthreads();  // the previous bitmap is no longer read
         const uint4 *src = reinterpret_cast<const uint4 *>(g.bitmap + static_cast<size_t>(sl) * g.words);
         for (uint32_t i = threadIdx.x; i < g.words / 4; i += blockDim.x) smem_u4[i] = src[i];
+        if (threadIdx.x == 0) s_next = 0;
         __syncthreads();
-        for (uint32_t tile = t0; tile < t1; ++tile)
+        const size_t q0 = (static_cast<size_t>(d - 1) * g.n_windows + w0) * kPullSlicesPerWindow;
+        const uint32_t n_q = (w1 - w0) * kPullSlicesPerWindow;
+        // Slices are handed out one at a time (lists differ in length: longest first within a window).
+        for (;;)
         {
-            const size_t si = static_cast<size_t>(d - 1) * g.n_tiles + tile;
-            // Segments start and end on 8-entry boundaries: a lane takes 8 consecutive synapses per
-            // group (two 16-byte loads of keys; one of FP16 or two of FP32 weights), two groups in
-            // flight. Padding entries (and lanes past the segment) are key 0 / weight 0: presynaptic
-            // neuron 0, target 0, contributing nothing.
-            const long long oa = g.seg_ptr[si] / kLaneRun, ob = g.seg_ptr[si + 1] / kLaneRun;
-            float *acc_t = acc + static_cast<size_t>(tile - t0) * kPullTile;
-            const uint4 *pk = reinterpret_cast<const uint4 *>(g.packed);
-            const float4 *pw = reinterpret_cast<const float4 *>(g.w);
-            const uint4 *ph = reinterpret_cast<const uint4 *>(g.w16);
-            for (long long base = oa + warp_base; base < ob; base += static_cast<long long>(blockDim.x) * kUnroll)
+            uint32_t qi = 0;
+            if (lane == 0) qi = atomicAdd(&s_next, 1u);
+            qi = __shfl_sync(0xffffffffu, qi, 0);
+            if (qi >= n_q) break;
+            const size_t q = q0 + qi;
+            const uint32_t len = g.slice_len[q];
+            if (len == 0) continue;
+            const long long base = g.slice_ptr[q] + lane;
+            float sum = 0.0f;
+            for (uint32_t k0 = 0; k0 < len; k0 += kDepth)
             {
-                uint4 key[kUnroll][2];
-                float4 w[kUnroll][2];
+                uint32_t pre[kDepth];
+                float w[kDepth];
 #pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
+                for (int i = 0; i < kDepth; ++i)
                 {
-                    const long long o = base + static_cast<long long>(u) * blockDim.x + lane;
-                    key[u][0] = key[u][1] = make_uint4(0u, 0u, 0u, 0u);
-                    w[u][0] = w[u][1] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (o < ob)
+                    pre[i] = 0u;
+                    w[i] = 0.0f;
+                    if (k0 + i < len)
                     {
-                        key[u][0] = __ldcs(pk + 2 * o);
-                        key[u][1] = __ldcs(pk + 2 * o + 1);
-                        if (kHalf)
-                        {
-                            const uint4 h = __ldcs(ph + o);
-                            const __half2 *h2 = reinterpret_cast<const __half2 *>(&h);
-                            const float2 a = __half22float2(h2[0]), b = __half22float2(h2[1]);
-                            const float2 c = __half22float2(h2[2]), e = __half22float2(h2[3]);
-                            w[u][0] = make_float4(a.x, a.y, b.x, b.y);
-                            w[u][1] = make_float4(c.x, c.y, e.x, e.y);
-                        }
-                        else
-                        {
-                            w[u][0] = __ldcs(pw + 2 * o);
-                            w[u][1] = __ldcs(pw + 2 * o + 1);
-                        }
+                        const long long e = base + static_cast<long long>(k0 + i) * kPullSlice;
+                        pre[i] = __ldcs(g.packed + e);
+                        w[i] = kHalf ? __half2float(__ushort_as_half(__ldcs(g.w16 + e))) : __ldcs(g.w + e);
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                {
-                    // Runs of equal targets inside the lane's 8 entries: every run but the last is
-                    // added at once; the last joins the warp-wide merge across lanes.
-                    const uint32_t kk[8] = {key[u][0].x, key[u][0].y, key[u][0].z, key[u][0].w,
-                                            key[u][1].x, key[u][1].y, key[u][1].z, key[u][1].w};
-                    const float ww[8] = {w[u][0].x, w[u][0].y, w[u][0].z, w[u][0].w,
-                                         w[u][1].x, w[u][1].y, w[u][1].z, w[u][1].w};
-                    uint32_t cur = kk[0] & (kPullTile - 1);
-                    float sum = 0.0f;
-#pragma unroll
-                    for (int i = 0; i < 8; ++i)
-                    {
-                        const uint32_t pre = kk[i] >> kPullTileBits;
-                        const uint32_t jl = kk[i] & (kPullTile - 1);
-                        const float v = ((bm[pre >> 5] >> (pre & 31)) & 1u) ? ww[i] : 0.0f;
-                        if (jl != cur)
-                        {
-                            if (sum != 0.0f) atomicAdd(acc_t + cur, sum);
-                            cur = jl;
-                            sum = v;
-                        }
-                        else
-                        {
-                            sum = __fadd_rn(sum, v);
-                        }
-                    }
-                    reduce_runs(cur, sum, acc_t);
-                }
+                for (int i = 0; i < kDepth; ++i)
+                    if ((bm[pre[i] >> 5] >> (pre[i] & 31)) & 1u) sum = __fadd_rn(sum, w[i]);
             }
+            // This lane's target: one owner per (delay, target), so a plain add.
+            const uint32_t t = g.perm[q * kPullSlice + lane];
+            if (sum != 0.0f) acc[(qi / kPullSlicesPerWindow) * kPullWindow + t] += sum;
         }
     }
     __syncthreads();
@@ -255,7 +225,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
         float *ring = p.ring.v32 + static_cast<size_t>(slot) * p.ring.pitch;
         for (uint32_t i = threadIdx.x; i < n_acc; i += blockDim.x)
         {
-            const uint32_t j = t0 * kPullTile + i;
+            const uint32_t j = w0 * kPullWindow + i;
             if (j < g.n_post && acc[i] != 0.0f) ring[j] = __fadd_rn(ring[j], acc[i]);
         }
     }
@@ -263,9 +233,9 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
     // tn - hist_slots, which no gather reads any more.
     const uint32_t sl_next = static_cast<uint32_t>(tn % g.hist_slots);
     uint32_t *dst = g.bitmap + static_cast<size_t>(sl_next) * g.words;
-    const uint32_t w0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * g.words / G);
-    const uint32_t w1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * g.words / G);
-    for (uint32_t i = w0 + threadIdx.x; i < w1; i += blockDim.x) dst[i] = 0u;
+    const uint32_t b0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * g.words / G);
+    const uint32_t b1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * g.words / G);
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) dst[i] = 0u;
 }
 
 int grid_for(uint64_t n)
@@ -285,8 +255,8 @@ int bits_for(uint64_t max_key)
 
 size_t gather_smem_bytes(const PullDev &p, int grid)
 {
-    const uint64_t tiles_per_block = (p.n_tiles + grid - 1) / grid;
-    return static_cast<size_t>(p.words) * 4 + tiles_per_block * kPullTile * 4;
+    const uint64_t windows_per_block = (p.n_windows + grid - 1) / grid;
+    return static_cast<size_t>(p.words) * 4 + windows_per_block * kPullWindow * 4;
 }
 
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s)
@@ -307,29 +277,42 @@ cudaError_t set_gather_smem(size_t bytes)
                                 static_cast<int>(bytes));
 }
 
-// Builds the sorted (delay, postsynaptic) layout from a projection's CSR. Allocates the outputs
-// with cudaMalloc (the caller owns them) and its temporaries with cudaMallocAsync.
+// Builds the sliced ELL layout from a projection's CSR: sort synapses by (delay, target), count the
+// lists, order each window's targets by list length, size and place the slices, then store the
+// weights as FP16 if every one is exactly an FP16 value. Outputs are cudaMalloc'd (the caller owns
+// them through `bufs`); temporaries use cudaMallocAsync.
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
-    const uint8_t *delay, bool negate, PullDev &out, uint32_t **packed_out, float **w_out, uint16_t **w16_out,
-    long long **seg_out, cudaStream_t s)
+    const uint8_t *delay, bool negate, PullDev &out, PullBuffers &bufs, cudaStream_t s)
 {
-    *w16_out = nullptr;
-    unsigned int *flag = nullptr;
     const uint32_t D = out.max_delay;
-    const uint32_t n_tiles = (n_post + kPullTile - 1) / kPullTile;
-    out.n_tiles = n_tiles;
+    const uint32_t n_win = (n_post + kPullWindow - 1) / kPullWindow;
+    out.n_windows = n_win;
     out.n_post = n_post;
-    uint32_t *row_of = nullptr, *k_in = nullptr, *k_out = nullptr, *v_in = nullptr, *v_out = nullptr;
-    long long *seg_raw = nullptr;
+    const uint64_t n_keys = static_cast<uint64_t>(D) * n_post;
+    const uint64_t n_dw = static_cast<uint64_t>(D) * n_win;
+    const uint64_t n_slices = n_dw * kPullSlicesPerWindow;
+    uint32_t *row_of = nullptr, *k_in = nullptr, *k_out = nullptr, *v_in = nullptr, *v_out = nullptr,
+             *count = nullptr;
+    long long *first = nullptr, *entries = nullptr;
+    uint8_t *inv = nullptr;
+    unsigned int *flag = nullptr;
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     const size_t bytes = n_syn * sizeof(uint32_t) + 16;
+    uint32_t *packed = nullptr, *slice_len = nullptr;
+    float *w32 = nullptr;
+    uint16_t *w16 = nullptr;
+    long long *slice_ptr = nullptr;
+    uint8_t *perm = nullptr;
+    uint64_t n_entries = 0;
+    unsigned int h_flag = 1;
+    long long total = 0;
     cudaError_t err;
-#define KNP_TRY(x)                     \
-    do                                 \
-    {                                  \
-        err = (x);                     \
+#define KNP_TRY(x)                         \
+    do                                     \
+    {                                      \
+        err = (x);                         \
         if (err != cudaSuccess) goto done; \
     } while (0)
     KNP_TRY(cudaMallocAsync(&row_of, bytes, s));
@@ -337,79 +320,116 @@ cudaError_t build_pull_layout(
     KNP_TRY(cudaMallocAsync(&k_out, bytes, s));
     KNP_TRY(cudaMallocAsync(&v_in, bytes, s));
     KNP_TRY(cudaMallocAsync(&v_out, bytes, s));
+    KNP_TRY(cudaMallocAsync(&count, (n_keys + 1) * sizeof(uint32_t), s));
+    KNP_TRY(cudaMemsetAsync(count, 0, (n_keys + 1) * sizeof(uint32_t), s));
     row_of_kernel<<<152 * 8, 256, 0, s>>>(row_ptr, n_rows, row_of);
-    pull_key_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, col, delay, n_post, D, k_in, v_in);
-    {
-        const int bits = bits_for(static_cast<uint64_t>(D) * n_post);
-        KNP_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in, k_out, v_in, v_out,
-                                                static_cast<int64_t>(n_syn), 0, bits, s));
-        KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
-        KNP_TRY(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k_in, k_out, v_in, v_out, static_cast<int64_t>(n_syn),
-                                                0, bits, s));
-    }
-    KNP_TRY(cudaMalloc(seg_out, (static_cast<size_t>(D) * n_tiles + 1) * sizeof(long long)));
-    KNP_TRY(cudaMallocAsync(&seg_raw, (static_cast<size_t>(D) * n_tiles + 1) * sizeof(long long), s));
-    pull_seg_kernel<<<grid_for(static_cast<uint64_t>(D) * n_tiles + 1), 256, 0, s>>>(k_out, n_syn, n_post, n_tiles, D,
-                                                                                   seg_raw);
+    pull_key_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, col, delay, n_post, D, k_in, v_in, count);
+    KNP_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in, k_out, v_in, v_out, static_cast<int64_t>(n_syn),
+                                            0, bits_for(n_keys), s));
+    KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
+    KNP_TRY(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k_in, k_out, v_in, v_out, static_cast<int64_t>(n_syn), 0,
+                                            bits_for(n_keys), s));
+    KNP_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+    // first[key]: sorted position of the key's first synapse (exclusive scan of the counts).
+    KNP_TRY(cudaMallocAsync(&first, (n_keys + 1) * sizeof(long long), s));
+    tmp_bytes = 0;
+    KNP_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, count, first, static_cast<int64_t>(n_keys + 1), s));
+    KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
+    KNP_TRY(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, count, first, static_cast<int64_t>(n_keys + 1), s));
+    KNP_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+    // Window orders and slice lengths.
+    KNP_TRY(cudaMalloc(&perm, n_dw * kPullWindow + 16));
+    KNP_TRY(cudaMallocAsync(&inv, n_dw * kPullWindow + 16, s));
+    KNP_TRY(cudaMalloc(&slice_len, n_slices * sizeof(uint32_t) + 16));
+    if (n_dw > 0)
+        pull_window_kernel<<<static_cast<unsigned>(n_dw), kPullWindow, 0, s>>>(count, n_post, n_win, perm, inv,
+                                                                               slice_len);
     KNP_TRY(cudaGetLastError());
+    // Slice offsets: exclusive scan of 32 x length.
+    KNP_TRY(cudaMallocAsync(&entries, (n_slices + 1) * sizeof(long long), s));
+    KNP_TRY(cudaMemsetAsync(entries, 0, (n_slices + 1) * sizeof(long long), s));
+    slice_entries_kernel<<<grid_for(n_slices), 256, 0, s>>>(slice_len, n_slices, entries);
+    KNP_TRY(cudaMalloc(&slice_ptr, (n_slices + 1) * sizeof(long long)));
+    tmp_bytes = 0;
+    KNP_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, entries, slice_ptr, static_cast<int64_t>(n_slices + 1),
+                                          s));
+    KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
+    KNP_TRY(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, entries, slice_ptr, static_cast<int64_t>(n_slices + 1), s));
+    KNP_TRY(cudaFreeAsync(tmp, s));
+    tmp = nullptr;
+    KNP_TRY(cudaMemcpyAsync(&total, slice_ptr + n_slices, sizeof(long long), cudaMemcpyDeviceToHost, s));
     KNP_TRY(cudaStreamSynchronize(s));
-    {
-        // Pad every segment to a multiple of 8 entries (32-byte aligned starts for vector loads).
-        const size_t n_seg = static_cast<size_t>(D) * n_tiles;
-        std::vector<long long> raw(n_seg + 1), pad(n_seg + 1, 0);
-        err = cudaMemcpy(raw.data(), seg_raw, raw.size() * sizeof(long long), cudaMemcpyDeviceToHost);
-        if (err != cudaSuccess) goto done;
-        for (size_t i = 0; i < n_seg; ++i)
-            pad[i + 1] = pad[i] + ((raw[i + 1] - raw[i] + kLaneRun - 1) / kLaneRun) * kLaneRun;
-        err = cudaMemcpy(*seg_out, pad.data(), pad.size() * sizeof(long long), cudaMemcpyHostToDevice);
-        if (err != cudaSuccess) goto done;
-        const size_t padded = static_cast<size_t>(pad[n_seg]) * sizeof(uint32_t) + 16;
-        err = cudaMalloc(packed_out, padded);
-        if (err != cudaSuccess) goto done;
-        err = cudaMalloc(w_out, padded);
-        if (err != cudaSuccess) goto done;
-        pull_fill_kernel<<<152 * 8, 256, 0, s>>>(n_seg, seg_raw, *seg_out, v_out, row_of, col, w, negate, *packed_out,
-                                                 *w_out);
-        out.padded_entries = static_cast<uint64_t>(pad[n_seg]);
-    }
+    n_entries = static_cast<uint64_t>(total);
+    // Entries: zero (padding: presynaptic 0, weight 0), then every delivered synapse in place.
+    KNP_TRY(cudaMalloc(&packed, n_entries * sizeof(uint32_t) + 16));
+    KNP_TRY(cudaMalloc(&w32, n_entries * sizeof(float) + 16));
+    KNP_TRY(cudaMemsetAsync(packed, 0, n_entries * sizeof(uint32_t) + 16, s));
+    KNP_TRY(cudaMemsetAsync(w32, 0, n_entries * sizeof(float) + 16, s));
+    pull_fill_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, k_out, v_out, first, inv, slice_ptr, row_of, w, negate,
+                                                    n_post, n_win, D, packed, w32);
     KNP_TRY(cudaGetLastError());
+    // Lossless 16-bit weights when every weight is exactly an FP16 value.
+    KNP_TRY(cudaMallocAsync(&flag, sizeof(unsigned int), s));
+    KNP_TRY(cudaMemsetAsync(flag, 0, sizeof(unsigned int), s));
+    half_exact_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, flag);
+    KNP_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     KNP_TRY(cudaStreamSynchronize(s));
-    out.seg_ptr = *seg_out;
-    out.packed = *packed_out;
-    out.w = *w_out;
-    out.w16 = nullptr;
+    if (h_flag == 0)
     {
-        // Lossless 16-bit weights when every weight is exactly an FP16 value (6 instead of 8 bytes
-        // per synapse streamed by the gather).
-        const uint64_t n_pad = out.padded_entries;
-        KNP_TRY(cudaMallocAsync(&flag, sizeof(unsigned int), s));
-        KNP_TRY(cudaMemsetAsync(flag, 0, sizeof(unsigned int), s));
-        half_exact_kernel<<<grid_for(n_pad), 256, 0, s>>>(*w_out, n_pad, flag);
-        unsigned int h_flag = 1;
-        KNP_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        KNP_TRY(cudaMalloc(&w16, n_entries * sizeof(uint16_t) + 16));
+        to_half_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, w16);
+        KNP_TRY(cudaGetLastError());
         KNP_TRY(cudaStreamSynchronize(s));
-        if (h_flag == 0)
-        {
-            KNP_TRY(cudaMalloc(w16_out, n_pad * sizeof(uint16_t) + 16));
-            to_half_kernel<<<grid_for(n_pad), 256, 0, s>>>(*w_out, n_pad, *w16_out);
-            KNP_TRY(cudaGetLastError());
-            KNP_TRY(cudaStreamSynchronize(s));
-            cudaFree(*w_out);
-            *w_out = nullptr;
-            out.w = nullptr;
-            out.w16 = *w16_out;
-        }
+        cudaFree(w32);
+        w32 = nullptr;
     }
+    out.slice_ptr = slice_ptr;
+    out.slice_len = slice_len;
+    out.perm = perm;
+    out.packed = packed;
+    out.w = w32;
+    out.w16 = w16;
+    out.padded_entries = n_entries;
+    bufs.ptr[0] = packed;
+    bufs.bytes[0] = n_entries * sizeof(uint32_t);
+    bufs.ptr[1] = w32;
+    bufs.bytes[1] = w32 ? n_entries * sizeof(float) : 0;
+    bufs.ptr[2] = w16;
+    bufs.bytes[2] = w16 ? n_entries * sizeof(uint16_t) : 0;
+    bufs.ptr[3] = slice_ptr;
+    bufs.bytes[3] = (n_slices + 1) * sizeof(long long);
+    bufs.ptr[4] = slice_len;
+    bufs.bytes[4] = n_slices * sizeof(uint32_t);
+    bufs.ptr[5] = perm;
+    bufs.bytes[5] = n_dw * kPullWindow;
+    packed = nullptr;
+    w32 = nullptr;
+    w16 = nullptr;
+    slice_ptr = nullptr;
+    slice_len = nullptr;
+    perm = nullptr;
 done:
     if (flag) cudaFreeAsync(flag, s);
-    if (seg_raw) cudaFreeAsync(seg_raw, s);
     if (tmp) cudaFreeAsync(tmp, s);
     if (row_of) cudaFreeAsync(row_of, s);
     if (k_in) cudaFreeAsync(k_in, s);
     if (k_out) cudaFreeAsync(k_out, s);
     if (v_in) cudaFreeAsync(v_in, s);
     if (v_out) cudaFreeAsync(v_out, s);
+    if (count) cudaFreeAsync(count, s);
+    if (first) cudaFreeAsync(first, s);
+    if (entries) cudaFreeAsync(entries, s);
+    if (inv) cudaFreeAsync(inv, s);
     cudaStreamSynchronize(s);
+    // On failure, buffers not handed to the caller are released.
+    if (packed) cudaFree(packed);
+    if (w32) cudaFree(w32);
+    if (w16) cudaFree(w16);
+    if (slice_ptr) cudaFree(slice_ptr);
+    if (slice_len) cudaFree(slice_len);
+    if (perm) cudaFree(perm);
 #undef KNP_TRY
     return err;
 }
