@@ -819,7 +819,7 @@ void Backend::build_pull(ProjectionSlot &p)
     const bool negate = p.dev.uniform_type == KNP_OUT_INHIBITORY_CURRENT;
     PullBuffers bufs;
     KNP_CUDA(build_pull_layout(p.n_syn, p.n_rows, post->n, p.row_ptr, p.col, p.w, p.delay_d, negate, g, bufs, stream_));
-    for (int i = 0; i < 6; ++i)
+    for (int i = 0; i < PullBuffers::kCount; ++i)
         if (bufs.ptr[i]) arena_.adopt(bufs.ptr[i], bufs.bytes[i]);
     g.bitmap = arena_.make<uint32_t>(static_cast<size_t>(g.hist_slots) * g.words);
     g.pulled = arena_.make<uint32_t>(g.hist_slots);

@@ -182,8 +182,10 @@ struct PullDev
     const long long *slice_ptr;  // [max_delay * n_windows * kPullSlicesPerWindow + 1] first entry of each slice
     const uint32_t *slice_len;   // [max_delay * n_windows * kPullSlicesPerWindow] entries per lane
     const uint8_t *perm;         // [max_delay * n_windows * kPullWindow] target offset in its window
-    const uint32_t *packed;      // presynaptic neuron of each entry
-    const float *w;              // FP32 weights (negated for inhibitory current), or null when w16 holds them
+    const uint32_t *packed;      // presynaptic neuron of each entry (| weight index << 24 with wtab)
+    const float *wtab;           // [256] weight dictionary (entry 0 is +0.0), used when the projection has at
+                                 // most 256 distinct weights and fewer than 2^24 presynaptic neurons; else null
+    const float *w;              // FP32 weights (negated for inhibitory current), or null
     const uint16_t *w16;         // FP16 bit patterns, used when every weight is exactly an FP16 value
     uint64_t padded_entries;     // entries of packed / w
 };
@@ -191,8 +193,9 @@ struct PullDev
 // Device buffers of a gather layout (cudaMalloc'd; the caller takes ownership), with their sizes.
 struct PullBuffers
 {
-    void *ptr[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    size_t bytes[6] = {0, 0, 0, 0, 0, 0};
+    static constexpr int kCount = 7;
+    void *ptr[kCount] = {};
+    size_t bytes[kCount] = {};
 };
 
 struct ProjectionDev
@@ -245,8 +248,10 @@ void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 size_t gather_smem_bytes(const PullDev &p, int grid);
-// Builds the gather layout of a projection from its CSR (weights stored as FP16 when every weight
-// is exactly an FP16 value, else FP32) and fills `out`; the buffers go to `bufs`.
+// Builds the gather layout of a projection from its CSR and fills `out`; the buffers go to `bufs`.
+// Weights are stored losslessly in the smallest form that holds them: an 8-bit index into a
+// 256-entry dictionary packed with the presynaptic neuron (at most 256 distinct weights), FP16 (every
+// weight exactly an FP16 value), else FP32.
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
     const uint8_t *delay, bool negate, PullDev &out, PullBuffers &bufs, cudaStream_t s);

@@ -15,6 +15,7 @@
 
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
+#include <cub/device/device_select.cuh>
 #include <cuda_fp16.h>
 
 #include "kernels.h"
@@ -130,6 +131,33 @@ __global__ void pull_fill_kernel(
     }
 }
 
+__global__ void float_bits_kernel(const float *w, uint64_t n, uint32_t *bits)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        bits[i] = __float_as_uint(w[i]);
+}
+
+// packed[i] |= (position of w[i]'s bit pattern in the ascending table) << 24.
+__global__ void dict_pack_kernel(const float *w, uint64_t n, const uint32_t *table, uint32_t n_table, uint32_t *packed)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const uint32_t b = __float_as_uint(w[i]);
+        uint32_t lo = 0, hi = n_table;
+        while (lo < hi)
+        {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (table[mid] < b)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        packed[i] |= lo << 24;
+    }
+}
+
 // flag |= 1 if some weight is not exactly an FP16 value.
 __global__ void half_exact_kernel(const float *w, uint64_t n, unsigned int *flag)
 {
@@ -147,13 +175,22 @@ __global__ void to_half_kernel(const float *w, uint64_t n, uint16_t *out)
         out[i] = __half_as_ushort(__float2half_rn(w[i]));
 }
 
-// kHalf: weights stored as FP16 (exact).
-template <bool kHalf>
+enum WeightForm
+{
+    kDict = 0,  // 8-bit dictionary index in the top bits of the packed entry
+    kHalf = 1,  // FP16
+    kFull = 2,  // FP32
+};
+
+template <int kForm>
 __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev p, Control *ctl)
 {
     extern __shared__ uint4 smem_u4[];
     __shared__ uint32_t s_next;  // next slice of the current delay to hand out
+    __shared__ float s_tab[256];
     const PullDev &g = p.pull;
+    if (kForm == kDict)
+        for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) s_tab[i] = g.wtab[i];
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem_u4);
     float *acc = reinterpret_cast<float *>(bm + g.words);
     const uint32_t G = gridDim.x;
@@ -206,12 +243,22 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
                     {
                         const long long e = base + static_cast<long long>(k0 + i) * kPullSlice;
                         pre[i] = __ldcs(g.packed + e);
-                        w[i] = kHalf ? __half2float(__ushort_as_half(__ldcs(g.w16 + e))) : __ldcs(g.w + e);
+                        if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(g.w16 + e)));
+                        if (kForm == kFull) w[i] = __ldcs(g.w + e);
                     }
                 }
 #pragma unroll
                 for (int i = 0; i < kDepth; ++i)
-                    if ((bm[pre[i] >> 5] >> (pre[i] & 31)) & 1u) sum = __fadd_rn(sum, w[i]);
+                {
+                    uint32_t pn = pre[i];
+                    float wi = w[i];
+                    if (kForm == kDict)
+                    {
+                        wi = s_tab[pn >> 24];
+                        pn &= 0xFFFFFFu;
+                    }
+                    if ((bm[pn >> 5] >> (pn & 31)) & 1u) sum = __fadd_rn(sum, wi);
+                }
             }
             // This lane's target: one owner per (delay, target), so a plain add.
             const uint32_t t = g.perm[q * kPullSlice + lane];
@@ -262,19 +309,23 @@ size_t gather_smem_bytes(const PullDev &p, int grid)
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s)
 {
     const size_t smem = gather_smem_bytes(p.pull, grid);
-    if (p.pull.w16)
-        gather_kernel<true><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+    if (p.pull.wtab)
+        gather_kernel<kDict><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+    else if (p.pull.w16)
+        gather_kernel<kHalf><<<grid, kGatherThreads, smem, s>>>(p, ctl);
     else
-        gather_kernel<false><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+        gather_kernel<kFull><<<grid, kGatherThreads, smem, s>>>(p, ctl);
 }
 
 cudaError_t set_gather_smem(size_t bytes)
 {
-    cudaError_t err =
-        cudaFuncSetAttribute(gather_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-    if (err != cudaSuccess) return err;
-    return cudaFuncSetAttribute(gather_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(bytes));
+    const int b = static_cast<int>(bytes);
+    cudaError_t err = cudaFuncSetAttribute(gather_kernel<kDict>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(gather_kernel<kHalf>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(gather_kernel<kFull>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return err;
 }
 
 // Builds the sliced ELL layout from a projection's CSR: sort synapses by (delay, target), count the
@@ -308,6 +359,10 @@ cudaError_t build_pull_layout(
     uint64_t n_entries = 0;
     unsigned int h_flag = 1;
     long long total = 0;
+    uint32_t *bits_in = nullptr, *bits_out = nullptr, *uniq = nullptr;
+    int64_t *n_uniq = nullptr;
+    int64_t h_uniq = 0;
+    float *wtab = nullptr;
     cudaError_t err;
 #define KNP_TRY(x)                         \
     do                                     \
@@ -370,25 +425,79 @@ cudaError_t build_pull_layout(
     pull_fill_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, k_out, v_out, first, inv, slice_ptr, row_of, w, negate,
                                                     n_post, n_win, D, packed, w32);
     KNP_TRY(cudaGetLastError());
-    // Lossless 16-bit weights when every weight is exactly an FP16 value.
-    KNP_TRY(cudaMallocAsync(&flag, sizeof(unsigned int), s));
-    KNP_TRY(cudaMemsetAsync(flag, 0, sizeof(unsigned int), s));
-    half_exact_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, flag);
-    KNP_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
-    KNP_TRY(cudaStreamSynchronize(s));
-    if (h_flag == 0)
+    // The sort and placement temporaries are no longer needed.
+    for (void **t : {reinterpret_cast<void **>(&row_of), reinterpret_cast<void **>(&k_in),
+                     reinterpret_cast<void **>(&k_out), reinterpret_cast<void **>(&v_in),
+                     reinterpret_cast<void **>(&v_out), reinterpret_cast<void **>(&count),
+                     reinterpret_cast<void **>(&first), reinterpret_cast<void **>(&entries),
+                     reinterpret_cast<void **>(&inv)})
     {
-        KNP_TRY(cudaMalloc(&w16, n_entries * sizeof(uint16_t) + 16));
-        to_half_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, w16);
-        KNP_TRY(cudaGetLastError());
+        KNP_TRY(cudaFreeAsync(*t, s));
+        *t = nullptr;
+    }
+    // Dictionary form: at most 256 distinct weight bit patterns (the padding's +0.0, the smallest
+    // pattern, becomes entry 0) and presynaptic indexes below 2^24.
+    if (n_rows <= (1u << 24) && n_entries > 0)
+    {
+        KNP_TRY(cudaMallocAsync(&bits_in, n_entries * sizeof(uint32_t), s));
+        KNP_TRY(cudaMallocAsync(&bits_out, n_entries * sizeof(uint32_t), s));
+        KNP_TRY(cudaMallocAsync(&uniq, n_entries * sizeof(uint32_t), s));
+        KNP_TRY(cudaMallocAsync(&n_uniq, sizeof(int64_t), s));
+        float_bits_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, bits_in);
+        tmp_bytes = 0;
+        KNP_TRY(cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, bits_in, bits_out, static_cast<int64_t>(n_entries), 0,
+                                               32, s));
+        KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
+        KNP_TRY(cub::DeviceRadixSort::SortKeys(tmp, tmp_bytes, bits_in, bits_out, static_cast<int64_t>(n_entries), 0,
+                                               32, s));
+        KNP_TRY(cudaFreeAsync(tmp, s));
+        tmp = nullptr;
+        tmp_bytes = 0;
+        KNP_TRY(cub::DeviceSelect::Unique(nullptr, tmp_bytes, bits_out, uniq, n_uniq, static_cast<int64_t>(n_entries),
+                                          s));
+        KNP_TRY(cudaMallocAsync(&tmp, tmp_bytes, s));
+        KNP_TRY(cub::DeviceSelect::Unique(tmp, tmp_bytes, bits_out, uniq, n_uniq, static_cast<int64_t>(n_entries), s));
+        KNP_TRY(cudaFreeAsync(tmp, s));
+        tmp = nullptr;
+        KNP_TRY(cudaMemcpyAsync(&h_uniq, n_uniq, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         KNP_TRY(cudaStreamSynchronize(s));
-        cudaFree(w32);
-        w32 = nullptr;
+        if (h_uniq > 0 && h_uniq <= 256)
+        {
+            KNP_TRY(cudaMalloc(&wtab, 256 * sizeof(float)));
+            KNP_TRY(cudaMemsetAsync(wtab, 0, 256 * sizeof(float), s));
+            KNP_TRY(cudaMemcpyAsync(wtab, uniq, static_cast<size_t>(h_uniq) * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                    s));
+            dict_pack_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, uniq, static_cast<uint32_t>(h_uniq),
+                                                                packed);
+            KNP_TRY(cudaGetLastError());
+            KNP_TRY(cudaStreamSynchronize(s));
+            cudaFree(w32);
+            w32 = nullptr;
+        }
+    }
+    // Lossless 16-bit weights when every weight is exactly an FP16 value.
+    if (w32)
+    {
+        KNP_TRY(cudaMallocAsync(&flag, sizeof(unsigned int), s));
+        KNP_TRY(cudaMemsetAsync(flag, 0, sizeof(unsigned int), s));
+        half_exact_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, flag);
+        KNP_TRY(cudaMemcpyAsync(&h_flag, flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        KNP_TRY(cudaStreamSynchronize(s));
+        if (h_flag == 0)
+        {
+            KNP_TRY(cudaMalloc(&w16, n_entries * sizeof(uint16_t) + 16));
+            to_half_kernel<<<grid_for(n_entries), 256, 0, s>>>(w32, n_entries, w16);
+            KNP_TRY(cudaGetLastError());
+            KNP_TRY(cudaStreamSynchronize(s));
+            cudaFree(w32);
+            w32 = nullptr;
+        }
     }
     out.slice_ptr = slice_ptr;
     out.slice_len = slice_len;
     out.perm = perm;
     out.packed = packed;
+    out.wtab = wtab;
     out.w = w32;
     out.w16 = w16;
     out.padded_entries = n_entries;
@@ -404,13 +513,20 @@ cudaError_t build_pull_layout(
     bufs.bytes[4] = n_slices * sizeof(uint32_t);
     bufs.ptr[5] = perm;
     bufs.bytes[5] = n_dw * kPullWindow;
+    bufs.ptr[6] = wtab;
+    bufs.bytes[6] = wtab ? 256 * sizeof(float) : 0;
     packed = nullptr;
     w32 = nullptr;
     w16 = nullptr;
     slice_ptr = nullptr;
     slice_len = nullptr;
     perm = nullptr;
+    wtab = nullptr;
 done:
+    if (bits_in) cudaFreeAsync(bits_in, s);
+    if (bits_out) cudaFreeAsync(bits_out, s);
+    if (uniq) cudaFreeAsync(uniq, s);
+    if (n_uniq) cudaFreeAsync(n_uniq, s);
     if (flag) cudaFreeAsync(flag, s);
     if (tmp) cudaFreeAsync(tmp, s);
     if (row_of) cudaFreeAsync(row_of, s);
@@ -430,6 +546,7 @@ done:
     if (slice_ptr) cudaFree(slice_ptr);
     if (slice_len) cudaFree(slice_len);
     if (perm) cudaFree(perm);
+    if (wtab) cudaFree(wtab);
 #undef KNP_TRY
     return err;
 }

@@ -153,11 +153,11 @@ def test_gather_inhibitory_projection():
     assert b.counters()[0] == oo.events
 
 
-@pytest.mark.parametrize("k_range", [(-16, 48), (-3001, 3001)])
+@pytest.mark.parametrize("k_range", [(-16, 48), (-1000, 1000), (-3001, 3001)])
 def test_gather_weight_storage(k_range):
-    """The gather layout stores weights as FP16 when every weight is exactly an FP16 value (k/256 with
-    |k| < 2048) and as FP32 otherwise (k/256 up to ~11.7 needs 12 significant bits); both give the
-    oracle's spike trains bit for bit."""
+    """The gather layout stores weights in the smallest lossless form: an 8-bit dictionary index
+    (65 distinct weights k/256, k in [-16, 48]), FP16 (2001 distinct weights, all exactly FP16) or FP32
+    (k/256 up to ~11.7 needs 12 significant bits); each gives the oracle's spike trains bit for bit."""
     from knp_gb300 import backend as B
     from oracle import oracle as orc
 
