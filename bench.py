@@ -36,7 +36,7 @@ SEED = 2
 N = 1_000_000
 FAN_IN = 1000
 P_BG = 0.005
-GATHER_DRAM_BYTES_PER_SYNAPSE = (0.962e9 + 3.4e6) / 2e8
+GATHER_DRAM_BYTES_PER_SYNAPSE = (677.2e6 + 3.05e6) / 2e8
 
 
 def peaks():
@@ -425,11 +425,15 @@ def main():
     roofline = {"bound": "hbm", "kernel": f"{dominant} phase", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": src,
                 # DRAM bytes (read + write) of one saturated gather launch, measured with ncu on the
-                # same configuration at 200k neurons (0.962 GB read + 3.4 MB written for 2e8
+                # same configuration at 200k neurons (677.2 MB read + 3.05 MB written for 2e8
                 # synapses), scaled by the synapse count; a step of the timed region that scatters
-                # moves far less.
+                # moves far less. The gather layout holds 4 B per synapse (presynaptic index and an
+                # 8-bit weight-dictionary index; target and delay are implied by the position), so
+                # the bytes actually moved are below the 9 B per event counted as algorithmic.
                 "traffic": GATHER_DRAM_BYTES_PER_SYNAPSE * n_neurons * args.fan_in,
                 "traffic_per": "saturated gathered step (ncu at 200k neurons, scaled by synapses)",
+                # The same traffic over the projection phase of the profiled (saturated) steps.
+                "traffic_frac": GATHER_DRAM_BYTES_PER_SYNAPSE * n_neurons * args.fan_in / (proj_ms / 1e3) / 1e9 / hbm,
                 "phase_ms_per_step": {"population": pop_ms, "projection": proj_ms,
                                       "stdp": ph[2] / args.profile_steps, "step_end": ph[3] / args.profile_steps},
                 "algorithmic_bytes_per_step": {"projection": proj_bytes, "population": pop_bytes},
