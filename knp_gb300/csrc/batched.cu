@@ -167,6 +167,7 @@ namespace
 {
 
 constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
+constexpr int kPairN = 2 * kBN;  // neurons of a CTA pair's MMA tile; each CTA finalises kBN of them
 constexpr int kIssuers = 2;                           // issuer q runs the MMAs of chunks c with c % 2 == q
 constexpr int kMinStages = 3, kMaxStages = 5;        // operand ring depths the autotuner tries
 constexpr uint32_t kChunkBytes = kBM * kBK * 2;       // one 128 x 128 BF16 chunk
@@ -205,10 +206,13 @@ struct BatchedNet
     unsigned long long *events;
     unsigned int *err;
     unsigned int *barrier;  // arrival counter of the grid barrier
+    float *xbuf;                  // [n_items][kBM][kBN]: partial sums a CTA hands to its pair partner
+    unsigned int *pair_flag;      // [n_items / 2]: arrivals of the pair exchange (2 per computed step)
     uint32_t n_items;
     uint16_t item_layer[kMaxItems];
     uint16_t item_m[kMaxItems];
-    uint16_t item_n[kMaxItems];  // 32-neuron tile index
+    uint16_t item_n[kMaxItems];  // kPairN-neuron tile index
+    uint8_t item_k[kMaxItems];   // K half: items 2i and 2i + 1 are the two halves of one tile
 };
 
 // Grid barrier on a counter that only grows: arrival k (0-based) belongs to barrier k / n_blocks,
@@ -238,6 +242,32 @@ __device__ __forceinline__ bool grid_sync(unsigned int *count, unsigned int n_bl
     }
     __syncthreads();
     return ok_s != 0;
+}
+
+// Exchange barrier of a CTA pair: both CTAs add 1 after writing their partial sums; a CTA goes on
+// once the counter reaches `target + 2` (bounded polls). Returns false on timeout (block-uniform).
+__device__ __forceinline__ bool pair_sync(unsigned int *flag, unsigned int target, uint32_t limit)
+{
+    __shared__ int pok_s;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(flag) : "memory");
+        int ok = 0;
+        for (uint32_t i = 0; i < limit; ++i)
+        {
+            unsigned int cur;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(flag) : "memory");
+            if (static_cast<int>(cur - (target + 2u)) >= 0)
+            {
+                ok = 1;
+                break;
+            }
+        }
+        pok_s = ok;
+    }
+    __syncthreads();
+    return pok_s != 0;
 }
 
 // Per (sample, input): the 53-bit threshold that the input draw is compared with.
@@ -294,28 +324,37 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const int layer = net.item_layer[item];  // 1..L
     const uint32_t m_tile = net.item_m[item];
     const uint32_t m0 = m_tile * kBM;
-    const uint32_t n0 = net.item_n[item] * kBN;
+    // The pair's tile is neurons np0 .. np0 + 63 over all K; this CTA multiplies K half kh of it and
+    // finalises neurons n0 .. n0 + 31 (half kh of the tile) after adding the partner's partial sums.
+    const uint32_t kh = net.item_k[item];
+    const uint32_t np0 = net.item_n[item] * kPairN;
+    const uint32_t n0 = np0 + kBN * kh;
     const uint32_t K = net.size[layer - 1], Kp = net.kpad[layer], N = net.size[layer];
     const uint32_t wn = net.words[layer];
-    const uint32_t n_chunks = net.chunks[layer];
-    // Shared memory: weight tile [kBN x Kp] (K-major core matrices), kStages chunk stages.
+    const uint32_t n_chunks_all = net.chunks[layer];
+    const uint32_t c_mid = (n_chunks_all + 1) / 2;
+    const uint32_t c_lo = kh ? c_mid : 0u, c_hi = kh ? n_chunks_all : c_mid;
+    const uint32_t n_chunks = c_hi - c_lo;  // this CTA's chunks
+    const uint32_t Kw = c_mid * kBK;        // K extent of the weight tile (the larger half)
+    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), kStages chunk stages.
     uint8_t *sW = smem;
-    uint8_t *sA = smem + static_cast<size_t>(kBN) * Kp * 2;
-    const uint32_t sbo_w = (Kp / 8) * 128;
+    uint8_t *sA = smem + static_cast<size_t>(kPairN) * Kw * 2;
+    const uint32_t sbo_w = (Kw / 8) * 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // Weight tile rows n0..n0+31 (zero beyond N), inputs 0..Kp (zero beyond K).
-    for (uint32_t u = threadIdx.x; u < kBN * (Kp / 8); u += blockDim.x)
+    // Weight tile rows np0..np0+63 (zero beyond N), inputs c_lo * 128 + [0, Kw) (zero beyond K).
+    for (uint32_t u = threadIdx.x; u < kPairN * (Kw / 8); u += blockDim.x)
     {
-        const uint32_t r = u / (Kp / 8), g = u % (Kp / 8), n = n0 + r, k = g * 8;
+        const uint32_t r = u / (Kw / 8), g = u % (Kw / 8), n = np0 + r, k = g * 8, kg = c_lo * kBK + k;
         __nv_bfloat16 tmp[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e)
-            tmp[e] = (n < N && k + e < K) ? net.w[layer - 1][static_cast<size_t>(n) * K + k + e] : __float2bfloat16(0.0f);
+            tmp[e] = (n < N && kg + e < K) ? net.w[layer - 1][static_cast<size_t>(n) * K + kg + e]
+                                           : __float2bfloat16(0.0f);
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
-    // Tensor memory: issuer q accumulates into columns [32 q, 32 q + 32).
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, 32 * kIssuers);
+    // Tensor memory: issuer q accumulates the 64-column tile into columns [64 q, 64 q + 64).
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, kPairN * kIssuers);
     if (threadIdx.x == 0)
     {
         for (int b = 0; b < kStages; ++b)
@@ -330,7 +369,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
-    constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
     // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
     // adding byte offsets / 16 to the start-address field.
     const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
@@ -401,7 +440,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         if (threadIdx.x < kBM) sbits[threadIdx.x] = 0;
         if (active)
         {
-            const uint8_t *src = net.spk[layer - 1][(t + 1) & 1] + static_cast<size_t>(m_tile) * n_chunks * kChunkBytes;
+            const uint8_t *src = net.spk[layer - 1][(t + 1) & 1] +
+                                 (static_cast<size_t>(m_tile) * n_chunks_all + c_lo) * kChunkBytes;
             if (warp == kLoaderWarp && lane == 0)
             {
                 // Loader: the chunks were written by other CTAs before the grid barrier (generic
@@ -418,7 +458,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             }
             else if (warp < kIssuers && lane == 0)
             {
-                // Issuer q: chunks q, q + 2, ... into its accumulator, then one commit for the step.
+                // Issuer q: chunks q, q + 2, ... of this half into its accumulator, then one commit
+                // for the step.
                 for (uint32_t c = warp; c < n_chunks; c += kIssuers)
                 {
                     const uint32_t sq = seq + c, b = sq % kStages;
@@ -426,9 +467,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     tc::fence_after_sync();
                     const uint64_t da = dA0 + b * (kChunkBytes >> 4);
                     const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
-                    const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - c * kBK);
+                    const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
                     for (uint32_t j = 0; j < kc / 16; ++j)
-                        tc::mma_bf16(tmem + 32u * warp, da + j * 16, db + j * 16, idesc,
+                        tc::mma_bf16(tmem + kPairN * warp, da + j * 16, db + j * 16, idesc,
                                      (c >= static_cast<uint32_t>(kIssuers) || j > 0) ? 1u : 0u);
                     tc::commit(&empty[b]);
                 }
@@ -489,18 +530,50 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             ++act_steps;
             seq += n_chunks;
             uint32_t mask = 0;
-            if (ok)
+            // This half's partial sums of 16 columns at tile column `col` (issuer 0 + issuer 1).
+            const uint32_t lane_base = (32u * (warp & 3)) << 16;
+            auto partial = [&](uint32_t col, float *v)
             {
-                // Sum of the issuers' accumulators (issuer q holds the chunks c with c % 2 == q).
-                float acc[16];
-                tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + cb, acc);
+                if (n_chunks == 0)
+                {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+                    return;
+                }
+                tc::tmem_ld16(tmem + lane_base + col, v);
                 for (int q = 1; q < kIssuers; ++q)
                 {
                     if (static_cast<uint32_t>(q) >= n_chunks) break;
                     float part[16];
-                    tc::tmem_ld16(tmem + ((32u * (warp & 3)) << 16) + 32u * q + cb, part);
+                    tc::tmem_ld16(tmem + lane_base + kPairN * q + col, part);
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) acc[i] = __fadd_rn(acc[i], part[i]);
+                    for (int i = 0; i < 16; ++i) v[i] = __fadd_rn(v[i], part[i]);
+                }
+            };
+            float acc[16];
+            // Hand the partner the columns it finalises, then add its partial to ours: the total is
+            // (K half 0) + (K half 1) on both sides.
+            if (ok)
+            {
+                partial(kBN * (1u - kh) + cb, acc);
+                float4 *xo = reinterpret_cast<float4 *>(net.xbuf + (static_cast<size_t>(item) * kBM + er) * kBN + cb);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) xo[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+            }
+            ok = pair_sync(net.pair_flag + item / 2, 2u * (act_steps - 1u), 1u << 26) && ok;
+            if (ok)
+            {
+                partial(kBN * kh + cb, acc);
+                const float4 *xi =
+                    reinterpret_cast<const float4 *>(net.xbuf + (static_cast<size_t>(item ^ 1u) * kBM + er) * kBN + cb);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                {
+                    const float4 p4 = __ldcg(xi + i);
+                    const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        acc[4 * i + e] = kh ? __fadd_rn(pv[e], acc[4 * i + e]) : __fadd_rn(acc[4 * i + e], pv[e]);
                 }
                 if (erow < b_act)
                 {
@@ -544,7 +617,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
             tc::fence_before_sync();
             __syncthreads();
-            if (net.record && threadIdx.x < kBM)
+            if (net.record && threadIdx.x < kBM && (n0 >> 5) < wn)  // the second half of a tile may lie past N
             {
                 const uint32_t rr = threadIdx.x, rw = m0 + rr;
                 if (rw < b_act)
@@ -578,7 +651,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
-    if (warp == 0) tc::tmem_dealloc(tmem, 32 * kIssuers);
+    if (warp == 0) tc::tmem_dealloc(tmem, kPairN * kIssuers);
 }
 
 }  // namespace
@@ -759,24 +832,28 @@ int batched_plan_create(
                     return -1;
                 }
     }
-    // Work items: (layer, 128-sample tile, 32-neuron tile).
+    // Work items: (layer, 128-sample tile, 64-neuron tile, K half), the two halves of a tile adjacent.
     const uint32_t m_tiles = (batch + kBM - 1) / kBM;
     for (int l = 1; l <= n_layers; ++l)
     {
+        const uint32_t n_tiles = (net.size[l] + kPairN - 1) / kPairN;
         for (uint32_t m = 0; m < m_tiles; ++m)
-            for (uint32_t n = 0; n < net.words[l]; ++n)
-            {
-                if (p.n_items >= kMaxItems)
+            for (uint32_t n = 0; n < n_tiles; ++n)
+                for (uint32_t h = 0; h < 2; ++h)
                 {
-                    *why = "too many (layer, sample tile, neuron tile) work items";
-                    return -1;
+                    if (p.n_items >= kMaxItems)
+                    {
+                        *why = "too many (layer, sample tile, neuron tile) work items";
+                        return -1;
+                    }
+                    net.item_layer[p.n_items] = static_cast<uint16_t>(l);
+                    net.item_m[p.n_items] = static_cast<uint16_t>(m);
+                    net.item_n[p.n_items] = static_cast<uint16_t>(n);
+                    net.item_k[p.n_items] = static_cast<uint8_t>(h);
+                    ++p.n_items;
                 }
-                net.item_layer[p.n_items] = static_cast<uint16_t>(l);
-                net.item_m[p.n_items] = static_cast<uint16_t>(m);
-                net.item_n[p.n_items] = static_cast<uint16_t>(n);
-                ++p.n_items;
-            }
-        p.w_bytes = std::max<size_t>(p.w_bytes, static_cast<size_t>(kBN) * net.kpad[l] * 2);
+        const uint32_t c_mid = (net.chunks[l] + 1) / 2;
+        p.w_bytes = std::max<size_t>(p.w_bytes, static_cast<size_t>(kPairN) * c_mid * kBK * 2);
     }
     net.n_items = p.n_items;
     int best = 0;
@@ -846,6 +923,9 @@ int batched_plan_create(
     ok = ok && (net.events = static_cast<unsigned long long *>(dalloc(8))) != nullptr;
     ok = ok && (net.err = static_cast<unsigned int *>(dalloc(4))) != nullptr;
     ok = ok && (net.barrier = static_cast<unsigned int *>(dalloc(8))) != nullptr;
+    ok = ok && (net.xbuf = static_cast<float *>(dalloc(static_cast<size_t>(p.n_items) * kBM * kBN * 4))) != nullptr;
+    ok = ok && (net.pair_flag = static_cast<unsigned int *>(dalloc(static_cast<size_t>(p.n_items / 2 + 1) * 4))) !=
+                   nullptr;
     if (!ok)
     {
         *why = "device allocation failed";
@@ -855,6 +935,7 @@ int batched_plan_create(
     p.zero.emplace_back(net.events, 8);
     p.zero.emplace_back(net.err, 4);
     p.zero.emplace_back(net.barrier, 8);
+    p.zero.emplace_back(net.pair_flag, static_cast<size_t>(p.n_items / 2 + 1) * 4);
     unsigned long long off = 0;
     for (int l = 0; l <= n_layers; ++l)
     {
