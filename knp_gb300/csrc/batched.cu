@@ -430,6 +430,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         }
     }
     const size_t spk0_tile = static_cast<size_t>(net.chunks[1]) * kChunkBytes;
+    const uint32_t kpad1 = net.kpad[1];
+    // This warp's input words: gw, gw + nw, ... below in_total (as (slot, word) pairs).
+    const uint32_t dr_items = (drawer && gw < in_total) ? static_cast<uint32_t>((in_total - 1 - gw) / nw + 1) : 0u;
+    const uint32_t dr_slot0 = drawer ? static_cast<uint32_t>(gw / w0) : 0u;
+    const uint32_t dr_wi0 = drawer ? static_cast<uint32_t>(gw % w0) : 0u;
+    const uint32_t dr_step_q = static_cast<uint32_t>(nw / w0), dr_step_r = static_cast<uint32_t>(nw % w0);
 
     uint32_t b_next = net.act[0];
     for (uint32_t t = 0; t < net.t_max && ok; ++t)
@@ -482,40 +488,63 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         if (drawer)
         {
             uint8_t *d0 = net.spk[0][t & 1];
-            auto draw = [&](uint64_t u, unsigned long long thr64, uint32_t smp)
+            const unsigned long long ctr_t = static_cast<unsigned long long>(t) * net.batch;
+            const unsigned long long rec_t = net.record ? t * net.rec_stride + net.rec_off[0] : 0ull;
+            auto emit = [&](uint32_t slot, uint32_t wi, bool bit, uint32_t smp)
             {
-                const uint32_t slot = static_cast<uint32_t>(u / w0), wi = static_cast<uint32_t>(u % w0);
                 const uint32_t i = wi * 32 + lane;
-                bool bit = false;
-                if (slot < b_act && i < n_in)
-                {
-                    const unsigned long long ctr = (static_cast<unsigned long long>(t) * net.batch + smp) * n_in + i;
-                    bit = (rand64(net.key, ctr) >> 11) < thr64;
-                }
-                if (i < net.kpad[1])
+                if (i < kpad1)
                     *reinterpret_cast<uint16_t *>(d0 + (slot / kBM) * spk0_tile + spk_offset(slot % kBM, i)) =
                         bit ? 0x3F80u : 0u;
                 const uint32_t word = __ballot_sync(0xffffffffu, bit);
                 if (lane == 0 && slot < b_act)
                 {
-                    if (net.record)
-                        net.record[t * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + wi] = word;
+                    if (net.record) net.record[rec_t + static_cast<size_t>(smp) * w0 + wi] = word;
                     my_events += static_cast<unsigned long long>(__popc(word)) *
                                  (net.sample_size[1] ? net.sample_size[1][smp] : net.size[1]);
                 }
             };
+            auto draw = [&](uint32_t slot, uint32_t wi, unsigned long long thr64, uint32_t smp) -> bool
+            {
+                const uint32_t i = wi * 32 + lane;
+                return slot < b_act && i < n_in && (rand64(net.key, (ctr_t + smp) * n_in + i) >> 11) < thr64;
+            };
+            // Word u = slot * w0 + wi advances by nw each item; (slot, wi) follow without division.
+            // The cached items' draws are independent: all drawn first, then written.
+            uint32_t slot = dr_slot0, wi = dr_wi0;
+            bool bits[kInCache];
+            uint32_t slots[kInCache], wis[kInCache];
 #pragma unroll
             for (int j = 0; j < kInCache; ++j)
             {
-                const uint64_t u = gw + j * nw;
-                if (u < in_total) draw(u, in_thr[j], in_smp[j]);
+                slots[j] = slot;
+                wis[j] = wi;
+                bits[j] = static_cast<uint32_t>(j) < dr_items && draw(slot, wi, in_thr[j], in_smp[j]);
+                wi += dr_step_r;
+                slot += dr_step_q;
+                if (wi >= w0)
+                {
+                    wi -= w0;
+                    ++slot;
+                }
             }
-            for (uint64_t u = gw + kInCache * nw; u < in_total; u += nw)
+#pragma unroll
+            for (int j = 0; j < kInCache; ++j)
+                if (static_cast<uint32_t>(j) < dr_items) emit(slots[j], wis[j], bits[j], in_smp[j]);
+            for (uint32_t j = kInCache; j < dr_items; ++j)
             {
-                const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
+                const uint32_t i = wi * 32 + lane;
                 const uint32_t smp = net.perm[slot];
                 const bool exists = i < n_in && (!net.sample_size[0] || i < net.sample_size[0][smp]);
-                draw(u, exists ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp);
+                emit(slot, wi, draw(slot, wi, exists ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp),
+                     smp);
+                wi += dr_step_r;
+                slot += dr_step_q;
+                if (wi >= w0)
+                {
+                    wi -= w0;
+                    ++slot;
+                }
             }
         }
         if (active)
