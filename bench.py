@@ -278,7 +278,8 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
         "spike_mismatch": mism / max(total, 1), "compared": total,
         "tensor": {"dense_flops_per_run": flops, "achieved_tflops": flops / (ms_b / 1e3) / 1e12},
         "dtype": "bf16 x bf16 -> fp32", "l2": "flushed (256 MB write) before each timed run",
-        "launch": "one CUDA graph per batch (state memsets, input thresholds, persistent cooperative kernel)",
+        "launch": "one CUDA graph per batch (state memsets, input thresholds, input spike bitmaps drawn ahead, "
+                  "persistent kernel of CTA-pair clusters)",
         "autotuned_ring_depth": stages, "autotune_ms": tuned,
     }
 

@@ -314,9 +314,9 @@ KNP_GB300_API int knp_gb300_bf16_gemm_tn(
 /*
  * Batched / precision form (no reference counterpart: the reference steps one network at a time).
  * `batch` independent samples of a feed-forward LIF network with n_layers all-to-all delay-1
- * layers (sizes[0] inputs -> sizes[1] -> ... -> sizes[n_layers], each <= 4096; reference LIF
+ * layers (sizes[0] inputs -> sizes[1] -> ... -> sizes[n_layers], each <= 4096, fan-in <= 2048; reference LIF
  * semantics lif_impl.h:33-86 with per-layer leak / threshold / reset / refractory period, NULL =
- * reference defaults 1, 1, 0, 0) run in one persistent cooperative kernel on the tcgen05 tensor cores:
+ * reference defaults 1, 1, 0, 0) run in a persistent kernel of CTA pairs on the tcgen05 tensor cores:
  * every step each layer's input is the previous layer's 0/1 spike matrix (BF16, exact) times its BF16
  * weights (device, d_weights[l] = [sizes[l + 1]][sizes[l]] row-major) with FP32 accumulation in tensor
  * memory. Sample b runs steps[b] (host array) steps; its input i spikes at step t iff
@@ -338,26 +338,30 @@ KNP_GB300_API int knp_gb300_batched_lif_run(
  *                 l (<= sizes[l]); inputs and neurons beyond it do not exist for that sample (never
  *                 spike, carry no events). NULL: every sample has the full sizes (uneven network
  *                 instances over shared weights, or inputs of uneven width).
- *   autotune      non-zero: each operand ring depth that fits (3..5 chunks of 32 KB) is run twice at
- *                 creation and the fastest kept; the depth does not change any result.
+ *   autotune      > 0: each operand ring depth that fits (2..4 chunks of 32 KB) is run twice at
+ *                 creation and the fastest kept; < 0: depth -autotune; 0: the deepest that fits. The
+ *                 depth does not change any result.
+ *   segment_steps non-zero: at most this many steps per persistent launch (0: as many as a 256 MB
+ *                 buffer of pre-drawn input spike bitmaps holds); segments do not change any result.
  * The device buffers (weights, rates, counts, record) must stay valid for the plan's life; their
  * contents are read / written by every knp_gb300_batched_plan_run, so rates and weights may be
- * rewritten between runs. One run: memsets of the run's state, the input-threshold kernel and the
- * persistent cooperative kernel, launched as one graph on `stream`; synchronous. Runs of one plan
- * must not overlap (they share the plan's device state).
+ * rewritten between runs. One run: memsets of the run's state, the input-threshold kernel and, per
+ * segment of steps, the input-drawing kernel and the persistent kernel (cluster launch of CTA pairs),
+ * launched as one graph on `stream`; synchronous. Runs of one plan must not overlap (they share the
+ * plan's device state).
  */
 typedef struct knp_gb300_batched_plan knp_gb300_batched_plan;
 
 KNP_GB300_API int knp_gb300_batched_plan_create(
     int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
-    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, void *stream,
-    knp_gb300_batched_plan **plan);
+    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, uint32_t segment_steps,
+    void *stream, knp_gb300_batched_plan **plan);
 
 /** Runs the prepared batch once: *events (host) synaptic events, *ms device time of the graph launch. */
 KNP_GB300_API int knp_gb300_batched_plan_run(knp_gb300_batched_plan *plan, uint64_t *events, float *ms);
 
-/** The ring depth in use and, after autotuning, the time of each depth tried (tune_ms[3] for depths 3, 4, 5; 0 = not tried). */
+/** The ring depth in use and, after autotuning, the time of each depth tried (tune_ms[3] for depths 2, 3, 4; 0 = not tried). */
 KNP_GB300_API int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, float *tune_ms);
 
 KNP_GB300_API void knp_gb300_batched_plan_destroy(knp_gb300_batched_plan *plan);

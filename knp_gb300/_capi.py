@@ -81,7 +81,7 @@ def lib():
         "knp_gb300_bf16_gemm_tn": ([p, p, p, c_int, c_int, c_int, p, p], c_int),
         "knp_gb300_batched_lif_run": ([c_int, p, p, p, p, p, p, u32, p, p, u64, p, p, ctypes.POINTER(u64),
                                        ctypes.POINTER(ctypes.c_float), p], c_int),
-        "knp_gb300_batched_plan_create": ([c_int, p, p, p, p, p, p, u32, p, p, p, u64, p, p, c_int, p,
+        "knp_gb300_batched_plan_create": ([c_int, p, p, p, p, p, p, u32, p, p, p, u64, p, p, c_int, u32, p,
                                            ctypes.POINTER(p)], c_int),
         "knp_gb300_batched_plan_run": ([p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_float)], c_int),
         "knp_gb300_batched_plan_info": ([p, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_float)], c_int),

@@ -86,9 +86,11 @@ def uneven_config(seed: int = 8, batch: int = 40, sizes=(96, 128, 64, 10), t_lo:
 
 class BatchedPlan:
     """A batch prepared on the device (knp_gb300_batched_plan_create) and run as one CUDA-graph
-    launch per ``run()``; with ``autotune`` the operand ring depth is chosen by timing each depth."""
+    launch per ``run()``; with ``autotune`` the operand ring depth is chosen by timing each depth,
+    ``stages`` fixes it (0: the deepest that fits)."""
 
-    def __init__(self, cfg: BatchedConfig, record: bool = False, autotune: bool = False, device: int = 0):
+    def __init__(self, cfg: BatchedConfig, record: bool = False, autotune: bool = False, device: int = 0,
+                 segment_steps: int = 0, stages: int = 0):
         import torch
 
         self.cfg = cfg
@@ -120,8 +122,9 @@ class BatchedPlan:
         _capi.check(self._lib.knp_gb300_batched_plan_create(
             L, sizes, wptr, fl(cfg.leak, 1.0), fl(cfg.threshold, 1.0), fl(cfg.reset, 0.0), refract, cfg.batch, steps,
             ss, ctypes.c_void_p(self._rates.data_ptr()), cfg.seed, ctypes.c_void_p(self._counts.data_ptr()),
-            ctypes.c_void_p(self._rec.data_ptr()) if self._rec is not None else None, int(autotune),
-            ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self._h)))
+            ctypes.c_void_p(self._rec.data_ptr()) if self._rec is not None else None,
+            -int(stages) if stages else int(bool(autotune)),
+            int(segment_steps), ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self._h)))
 
     def run(self):
         """One graph launch; returns (synaptic events, device ms)."""
@@ -135,7 +138,7 @@ class BatchedPlan:
         st = ctypes.c_int(0)
         t = (ctypes.c_float * 3)()
         _capi.check(self._lib.knp_gb300_batched_plan_info(self._h, ctypes.byref(st), t))
-        return st.value, {d: float(t[d - 3]) for d in (3, 4, 5) if t[d - 3] > 0}
+        return st.value, {d: float(t[d - 2]) for d in (2, 3, 4) if t[d - 2] > 0}
 
     def counts(self) -> np.ndarray:
         return self._counts.cpu().numpy()
@@ -161,11 +164,11 @@ class BatchedPlan:
             pass
 
 
-def run(cfg: BatchedConfig, record: bool = False, device: int = 0, autotune: bool = False):
+def run(cfg: BatchedConfig, record: bool = False, device: int = 0, autotune: bool = False, segment_steps: int = 0):
     """Run the batch once on the GPU. Returns (counts [B, n_L], record or None, events, ms). With
     ``record`` the per-step spike bitmaps of every layer come back as a dict
-    {layer: uint32 [T_max, B, words]}."""
-    plan = BatchedPlan(cfg, record=record, autotune=autotune, device=device)
+    {layer: uint32 [T_max, B, words]}; ``segment_steps`` caps the steps per persistent launch."""
+    plan = BatchedPlan(cfg, record=record, autotune=autotune, device=device, segment_steps=segment_steps)
     try:
         events, ms = plan.run()
         return plan.counts(), (plan.record() if record else None), events, ms

@@ -147,35 +147,43 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
 // whose spike of source i for sample b at step t is the counter-based Bernoulli draw
 // rand64(key, (t * B + b) * n_0 + i) >> 11 < rate[b][i] * 2^53. Sample b runs steps [0, T_b).
 //
-// Each step is a BF16 GEMM of the 0/1 spike matrix (exact in BF16) against BF16 weights with FP32
-// accumulation in tensor memory. One CTA owns (layer, 128-sample tile, 32-neuron tile); its weight
-// tile stays in shared memory and its neurons' LIF state in registers for the whole run.
+// Each step of a layer is a BF16 GEMM of the 0/1 spike matrix (exact in BF16) against BF16 weights
+// with FP32 accumulation in tensor memory. A CTA pair (a cluster of two) owns (layer, 128-sample
+// tile, 64-neuron tile): each CTA multiplies one half of the K range against its half of the weight
+// tile (resident in shared memory for the whole run), sends the partner the partial sums of the 32
+// neurons the partner finalises (st.async into the partner's shared memory) and finalises its own
+// 32 neurons, whose LIF state stays in registers.
 //
-// Spike matrices are kept in global memory already in the layout the tensor cores read: for each
-// layer, step parity and 128-sample tile, the consumer's K range is cut into 128-input chunks of
-// 32 KB each in the canonical no-swizzle K-major form (8 x 16-byte core matrices). A producer CTA
-// writes its 128 x 32 block of 0/1 BF16 spikes there (512 16-byte stores), so a consumer needs no
-// conversion: a loader thread streams the chunks into a 4-stage shared-memory ring with bulk copies
-// (cp.async.bulk, completion on mbarriers), two issuer threads run the MMAs of alternate chunks
-// into separate accumulators, and the other warps draw the next step's input spikes meanwhile.
-// Samples are processed sorted by decreasing T, so finished samples leave whole M-tiles idle.
-// Steps are separated by a grid barrier; the kernel is launched cooperatively (every CTA resident)
-// and every wait is bounded.
+// Spikes travel between layers as bitmaps (one 32-bit word per sample and 32 neurons) in a ring of
+// kRing steps per layer. A consumer expands its K half chunk by chunk into BF16 operand tiles in
+// shared memory (canonical no-swizzle K-major layout) while the tensor cores multiply the previous
+// chunk. There is no grid-wide barrier: per (layer, sample tile, ring slot) counters record how
+// many times the layer's CTAs have written the slot (`ready`) and how many times consumer CTAs have
+// read it (`consumed`), so a layer starts step t as soon as every CTA of the layer below has
+// published step t - 1, and overwrites a slot only after every consumer has read it (a layer runs
+// at most kRing - 2 steps ahead of its consumers). Counting per slot matters: CTAs of one layer are
+// not in lockstep, and a sum over all slots would let a fast CTA stand in for a slow one. Input spikes do not depend on the network, so
+// a separate kernel draws them ahead of the run (layer 0's slots hold every step of a segment; long
+// runs are cut into segments, the LIF state saved and restored between them). Samples are processed
+// sorted by decreasing T, so finished samples leave whole sample tiles idle. Every wait is bounded.
 namespace knp_gb300
 {
 namespace
 {
 
 constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
-constexpr int kPairN = 2 * kBN;  // neurons of a CTA pair's MMA tile; each CTA finalises kBN of them
-constexpr int kIssuers = 2;                           // issuer q runs the MMAs of chunks c with c % 2 == q
-constexpr int kMinStages = 3, kMaxStages = 5;        // operand ring depths the autotuner tries
-constexpr uint32_t kChunkBytes = kBM * kBK * 2;       // one 128 x 128 BF16 chunk
-constexpr uint32_t kSboA = (kBK / 8) * 128;           // row-group stride of a chunk (16 core matrices)
-constexpr int kLoaderWarp = kIssuers;                 // lane 0 of this warp streams the chunks
-constexpr int kFirstDrawWarp = kLoaderWarp + 1;       // warps from here on draw the input spikes
-constexpr int kInCache = 12;                          // input words per drawing warp with cached thresholds
+constexpr int kPairN = 2 * kBN;                 // neurons of a CTA pair's tile; each CTA finalises kBN
+constexpr int kMinStages = 2, kMaxStages = 4;  // operand ring depths the autotuner tries
+constexpr uint32_t kChunkBytes = kBM * kBK * 2;  // one 128 x 128 BF16 chunk
+constexpr uint32_t kSboA = (kBK / 8) * 128;      // row-group stride of a chunk (16 core matrices)
+constexpr uint32_t kChunkWords = kBK / 32;       // bitmap words per sample row and chunk
+constexpr uint32_t kMaxHalfChunks = 8;           // chunks of a K half (bounded by shared memory)
+constexpr uint32_t kRing = 8;                    // bitmap steps kept per layer
+constexpr uint32_t kXchBytes = kBM * kBN * 4;    // one exchange buffer: [kBM][kBN] FP32 partial sums
+constexpr uint32_t kPollLimit = 1u << 22;        // polls of a cross-CTA counter before giving up
+constexpr int kStateWords = 48;                  // V, refractory counter, spike count of 16 neurons
 constexpr int kBatchThreads = 256;
+constexpr size_t kInputSlotBudget = size_t(256) << 20;  // bytes of layer 0's slots per segment
 
 struct BatchedNet
 {
@@ -184,10 +192,12 @@ struct BatchedNet
     uint32_t words[kMaxLayers + 1];   // ceil(size / 32)
     uint32_t kpad[kMaxLayers + 1];    // kpad[l] = size[l - 1] rounded up to 16 (layer l's K)
     uint32_t chunks[kMaxLayers + 1];  // chunks[l] = ceil(kpad[l] / 128)
+    uint32_t wpad[kMaxLayers + 1];    // wpad[l] = 4 * chunks[l + 1]: words per sample row of layer l's slots
+    uint32_t n_cta[kMaxLayers + 1];   // CTAs of layer l per sample tile
     const __nv_bfloat16 *w[kMaxLayers];
     float leak[kMaxLayers], thr[kMaxLayers], reset[kMaxLayers];
     uint32_t refract[kMaxLayers];
-    uint32_t batch;
+    uint32_t batch, m_tiles;
     const uint32_t *perm;  // slot -> sample
     const uint32_t *act;   // [t_max]: slots still running at step t (slots sorted by decreasing T)
     const unsigned long long *rate_thr;  // [batch][size[0]] by sample: rate * 2^53, the draw's threshold
@@ -196,79 +206,26 @@ struct BatchedNet
     const uint32_t *sample_size[kMaxLayers + 1];
     unsigned long long key;
     uint32_t t_max;
-    // spk[l][p]: spikes of layer l (l < n_layers) at steps of parity p, as layer l + 1's A operand:
-    // [m tile][chunks[l + 1]][kChunkBytes].
-    uint8_t *spk[kMaxLayers][2];
-    int *counts;           // [batch][size[L]] by sample
-    uint32_t *record;      // [t_max][sum_l batch * words[l]] by sample, or null
+    // bits[l]: spikes of layer l as layer l + 1's input, [slot][m tile][kBM][wpad[l]] words (bit j of
+    // word w = neuron 32 w + j, words past words[l] zero). Layer 0: slot j of a segment starting at
+    // step t0 = input drawn at step t0 + j - 1 (nothing before step 0). Layers >= 1: kRing slots,
+    // slot (t + 1) % kRing written at step t.
+    uint32_t *bits[kMaxLayers];
+    unsigned int *ready;     // [kMaxLayers + 1][m_tiles][kRing]: writes of layer l's slot by its CTAs
+    unsigned int *consumed;  // [kMaxLayers + 1][m_tiles][kRing]: reads of layer l's slot by layer l + 1's CTAs
+    uint32_t *state;         // [n_items][kBatchThreads][kStateWords]: LIF state between segments
+    int *counts;             // [batch][size[L]] by sample
+    uint32_t *record;        // [t_max][sum_l batch * words[l]] by sample, or null
     unsigned long long rec_off[kMaxLayers + 1];
     unsigned long long rec_stride;
     unsigned long long *events;
     unsigned int *err;
-    unsigned int *barrier;  // arrival counter of the grid barrier
-    float *xbuf;                  // [n_items][kBM][kBN]: partial sums a CTA hands to its pair partner
-    unsigned int *pair_flag;      // [n_items / 2]: arrivals of the pair exchange (2 per computed step)
     uint32_t n_items;
     uint16_t item_layer[kMaxItems];
     uint16_t item_m[kMaxItems];
     uint16_t item_n[kMaxItems];  // kPairN-neuron tile index
-    uint8_t item_k[kMaxItems];   // K half: items 2i and 2i + 1 are the two halves of one tile
+    uint8_t item_k[kMaxItems];   // K half = rank in the cluster: items 2i and 2i + 1 are one tile
 };
-
-// Grid barrier on a counter that only grows: arrival k (0-based) belongs to barrier k / n_blocks,
-// which completes when the counter reaches (k / n_blocks + 1) * n_blocks. One release add per CTA,
-// acquire polls (bounded) until then.
-__device__ __forceinline__ bool grid_sync(unsigned int *count, unsigned int n_blocks, uint32_t limit)
-{
-    __shared__ int ok_s;
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        unsigned int old;
-        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(count) : "memory");
-        const unsigned int target = (old / n_blocks + 1) * n_blocks;
-        int ok = 0;
-        for (uint32_t i = 0; i < limit; ++i)
-        {
-            unsigned int cur;
-            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(count) : "memory");
-            if (static_cast<int>(cur - target) >= 0)
-            {
-                ok = 1;
-                break;
-            }
-        }
-        ok_s = ok;
-    }
-    __syncthreads();
-    return ok_s != 0;
-}
-
-// Exchange barrier of a CTA pair: both CTAs add 1 after writing their partial sums; a CTA goes on
-// once the counter reaches `target + 2` (bounded polls). Returns false on timeout (block-uniform).
-__device__ __forceinline__ bool pair_sync(unsigned int *flag, unsigned int target, uint32_t limit)
-{
-    __shared__ int pok_s;
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(flag) : "memory");
-        int ok = 0;
-        for (uint32_t i = 0; i < limit; ++i)
-        {
-            unsigned int cur;
-            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(flag) : "memory");
-            if (static_cast<int>(cur - (target + 2u)) >= 0)
-            {
-                ok = 1;
-                break;
-            }
-        }
-        pok_s = ok;
-    }
-    __syncthreads();
-    return pok_s != 0;
-}
 
 // Per (sample, input): the 53-bit threshold that the input draw is compared with.
 __global__ void rate_threshold_kernel(const float *rates, unsigned long long *thr, size_t n)
@@ -277,13 +234,43 @@ __global__ void rate_threshold_kernel(const float *rates, unsigned long long *th
     if (i < n) thr[i] = static_cast<unsigned long long>(static_cast<double>(rates[i]) * 9007199254740992.0);
 }
 
-// Bulk copy global -> shared (both 16-byte aligned, size a multiple of 16) completing on `mbar`.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+// Layer 0's slots of the segment [t0, t1): slot j = the input spikes drawn at step t0 + j - 1, one
+// thread per bitmap word (32 draws). Also writes layer 0's record and adds the synaptic events of
+// each step drawn; the last segment has one extra row of words (j = t1 - t0, the draws of step
+// t_max - 1) that no layer reads.
+__global__ void input_bits_kernel(BatchedNet net, uint32_t t0, uint32_t t1)
 {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     tc::smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(tc::smem_u32(mbar))
-                 : "memory");
+    const uint32_t wp = net.wpad[0], w0 = net.words[0], n_in = net.size[0];
+    const uint32_t span = t1 - t0 + (t1 == net.t_max ? 1u : 0u);
+    const size_t per_slot = static_cast<size_t>(net.m_tiles) * kBM * wp;
+    const size_t total = span * per_slot;
+    unsigned long long ev = 0;
+    for (size_t u = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; u < total;
+         u += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        const uint32_t j = static_cast<uint32_t>(u / per_slot);
+        const uint32_t rem = static_cast<uint32_t>(u - static_cast<size_t>(j) * per_slot);
+        const uint32_t row = rem / wp, w = rem - row * wp;  // row = m tile * kBM + slot row
+        const uint32_t t = t0 + j;                           // the step that consumes the draws of t - 1
+        uint32_t word = 0;
+        if (t >= 1 && w < w0 && row < net.act[t - 1])
+        {
+            const uint32_t s = t - 1, smp = net.perm[row];
+            const uint32_t lim = net.sample_size[0] ? min(n_in, net.sample_size[0][smp]) : n_in;
+            const unsigned long long base = (static_cast<unsigned long long>(s) * net.batch + smp) * n_in;
+            const unsigned long long *thr = net.rate_thr + static_cast<size_t>(smp) * n_in;
+            const uint32_t i0 = w * 32;
+            for (uint32_t b = 0; b < 32 && i0 + b < lim; ++b)
+                if ((rand64(net.key, base + i0 + b) >> 11) < thr[i0 + b]) word |= 1u << b;
+            if (net.record)
+                net.record[s * net.rec_stride + net.rec_off[0] + static_cast<size_t>(smp) * w0 + w] = word;
+            ev += static_cast<unsigned long long>(__popc(word)) *
+                  (net.sample_size[1] ? net.sample_size[1][smp] : net.size[1]);
+        }
+        if (j < t1 - t0) net.bits[0][u] = word;
+    }
+    for (int o = 16; o > 0; o >>= 1) ev += __shfl_down_sync(0xffffffffu, ev, o);
+    if ((threadIdx.x & 31) == 0 && ev) atomicAdd(net.events, ev);
 }
 
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
@@ -291,6 +278,23 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t b
     asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(mbar)),
                  "r"(bytes)
                  : "memory");
+}
+
+// Polls (acquire, bounded) until *counter >= target; false on timeout.
+__device__ __forceinline__ bool poll_at_least(const unsigned int *counter, unsigned int target)
+{
+    for (uint32_t i = 0; i < kPollLimit; ++i)
+    {
+        unsigned int cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(counter) : "memory");
+        if (static_cast<int>(cur - target) >= 0) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void release_add(unsigned int *counter)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
 }
 
 // The low 8 bits of x as eight BF16 values 0 or 1.0 (0x3F80), bit i -> element i.
@@ -304,22 +308,17 @@ __device__ __forceinline__ uint4 bf16_bits(uint32_t x)
     return v;
 }
 
-// Byte offset of element (row r, input k) of a layer's spike matrix inside one 128-sample tile.
-__device__ __forceinline__ uint32_t spk_offset(uint32_t r, uint32_t k)
-{
-    return (k / kBK) * kChunkBytes + (r >> 3) * kSboA + ((k % kBK) >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
-}
-
 template <int kStages>
-__global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net)
+__global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net, uint32_t t0, uint32_t t1)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t full[kStages];   // chunk in stage b has landed (loader's expect_tx)
-    __shared__ __align__(8) uint64_t empty[kStages];  // MMAs that read stage b have completed (commit)
-    __shared__ __align__(8) uint64_t done[kIssuers]; // all of an issuer's MMAs of a step have completed
+    __shared__ __align__(8) uint64_t empty[kStages];  // the MMAs that read stage b have completed (commit)
+    __shared__ __align__(8) uint64_t done;            // every MMA of the step has completed (commit)
+    __shared__ __align__(8) uint64_t xfull[2];        // the partner's partial sums of a step have landed
     __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
+    __shared__ int s_ready, s_room;
     const uint32_t item = blockIdx.x;
     const int layer = net.item_layer[item];  // 1..L
     const uint32_t m_tile = net.item_m[item];
@@ -334,11 +333,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t n_chunks_all = net.chunks[layer];
     const uint32_t c_mid = (n_chunks_all + 1) / 2;
     const uint32_t c_lo = kh ? c_mid : 0u, c_hi = kh ? n_chunks_all : c_mid;
-    const uint32_t n_chunks = c_hi - c_lo;  // this CTA's chunks
+    const uint32_t n_chunks = c_hi - c_lo;  // this CTA's chunks (<= kMaxHalfChunks)
     const uint32_t Kw = c_mid * kBK;        // K extent of the weight tile (the larger half)
-    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), kStages chunk stages.
+    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), kStages operand stages, two
+    // exchange buffers.
     uint8_t *sW = smem;
     uint8_t *sA = smem + static_cast<size_t>(kPairN) * Kw * 2;
+    uint8_t *sX = sA + static_cast<size_t>(kStages) * kChunkBytes;
     const uint32_t sbo_w = (Kw / 8) * 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -353,20 +354,18 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                                            : __float2bfloat16(0.0f);
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
-    // Tensor memory: issuer q accumulates the 64-column tile into columns [64 q, 64 q + 64).
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, kPairN * kIssuers);
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, kPairN);
     if (threadIdx.x == 0)
     {
-        for (int b = 0; b < kStages; ++b)
-        {
-            tc::mbar_init(&full[b], 1);
-            tc::mbar_init(&empty[b], 1);
-        }
-        for (int q = 0; q < kIssuers; ++q) tc::mbar_init(&done[q], 1);
+        for (int b = 0; b < kStages; ++b) tc::mbar_init(&empty[b], 1);
+        tc::mbar_init(&done, 1);
+        tc::mbar_init(&xfull[0], 1);
+        tc::mbar_init(&xfull[1], 1);
         s_events = 0;
     }
     tc::fence_before_sync();
     __syncthreads();
+    tc::cluster_sync();  // the partner's barriers are initialised before any st.async reaches them
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
@@ -374,10 +373,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     // adding byte offsets / 16 to the start-address field.
     const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
     const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
-    uint32_t seq = 0;        // chunks streamed by this CTA in earlier steps (stage = seq % kStages)
-    uint32_t act_steps = 0;  // steps this CTA has computed (phase of done[])
-    bool ok = true;
-    unsigned long long my_events = 0;
+    const uint32_t peer = tc::cluster_rank() ^ 1u;
+    const uint32_t x_peer = tc::mapa(tc::smem_u32(sX), peer);
+    const uint32_t xfull_peer[2] = {tc::mapa(tc::smem_u32(&xfull[0]), peer), tc::mapa(tc::smem_u32(&xfull[1]), peer)};
 
     // Epilogue ownership, fixed for the run: thread (warp, lane) owns row 32 (warp % 4) + lane of the
     // tile and columns 16 (warp / 4) .. +15, so it keeps their LIF state in registers.
@@ -387,12 +385,13 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     float V[16];
     uint32_t RC[16];
     int CNT[16];
+    uint32_t *saved = net.state + (static_cast<size_t>(item) * kBatchThreads + threadIdx.x) * kStateWords;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
     {
-        V[i] = 0.f;
-        RC[i] = 0u;
-        CNT[i] = 0;
+        V[i] = t0 ? __uint_as_float(saved[i]) : 0.f;
+        RC[i] = t0 ? saved[16 + i] : 0u;
+        CNT[i] = t0 ? static_cast<int>(saved[32 + i]) : 0;
     }
     const int li = layer - 1;
     const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
@@ -405,289 +404,237 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                                                                                   : net.size[layer + 1])
                              : 0u;
 
-    // Input words drawn by this warp every step (drawing warps only: u = draw warp id + j * draw
-    // warps in grid) and, for the first kInCache of them, this lane's threshold and sample.
-    const uint32_t n_in = net.size[0], w0 = net.words[0];
-    const uint64_t in_total = static_cast<uint64_t>(net.batch) * w0;
-    const uint32_t dpb = (blockDim.x >> 5) - kFirstDrawWarp;
-    const bool drawer = warp >= kFirstDrawWarp;
-    const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * dpb + (warp - kFirstDrawWarp),
-                   nw = static_cast<uint64_t>(gridDim.x) * dpb;
-    unsigned long long in_thr[kInCache];
-    uint32_t in_smp[kInCache];
-#pragma unroll
-    for (int j = 0; j < kInCache; ++j)
-    {
-        const uint64_t u = gw + j * nw;
-        in_thr[j] = 0;
-        in_smp[j] = 0;
-        if (drawer && u < in_total)
-        {
-            const uint32_t slot = static_cast<uint32_t>(u / w0), i = static_cast<uint32_t>(u % w0) * 32 + lane;
-            in_smp[j] = net.perm[slot];
-            if (i < n_in && (!net.sample_size[0] || i < net.sample_size[0][in_smp[j]]))
-                in_thr[j] = net.rate_thr[static_cast<size_t>(in_smp[j]) * n_in + i];
-        }
-    }
-    const size_t spk0_tile = static_cast<size_t>(net.chunks[1]) * kChunkBytes;
-    const uint32_t kpad1 = net.kpad[1];
-    // This warp's input words: gw, gw + nw, ... below in_total (as (slot, word) pairs).
-    const uint32_t dr_items = (drawer && gw < in_total) ? static_cast<uint32_t>((in_total - 1 - gw) / nw + 1) : 0u;
-    const uint32_t dr_slot0 = drawer ? static_cast<uint32_t>(gw / w0) : 0u;
-    const uint32_t dr_wi0 = drawer ? static_cast<uint32_t>(gw % w0) : 0u;
-    const uint32_t dr_step_q = static_cast<uint32_t>(nw / w0), dr_step_r = static_cast<uint32_t>(nw % w0);
+    // Input side: layer - 1's bitmap slots and, above layer 1, its publication / consumption counters.
+    const uint32_t m_tiles = net.m_tiles;
+    const uint32_t wp_in = net.wpad[layer - 1];
+    const uint32_t *in_bits = net.bits[layer - 1];
+    const size_t ctr_in = (static_cast<size_t>(layer - 1) * m_tiles + m_tile) * kRing;
+    const unsigned int *ready_in = layer > 1 ? net.ready + ctr_in : nullptr;
+    unsigned int *consumed_in = layer > 1 ? net.consumed + ctr_in : nullptr;
+    const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] : 0u;
+    // Output side (every layer but the last).
+    const bool producer = layer < net.n_layers;
+    uint32_t *out_bits = producer ? net.bits[layer] : nullptr;
+    const uint32_t wp_out = producer ? net.wpad[layer] : 0u;
+    const size_t ctr_out = (static_cast<size_t>(layer) * m_tiles + m_tile) * kRing;
+    unsigned int *ready_out = producer ? net.ready + ctr_out : nullptr;
+    const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
+    const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
+    // Expansion ownership: thread -> sample row xr, chunk words 2 xh and 2 xh + 1 (8-input groups
+    // 8 xh .. 8 xh + 7); a quarter warp covers 8 consecutive rows of one group (conflict-free stores).
+    const uint32_t xr = (threadIdx.x & 7u) + 8u * ((threadIdx.x >> 3) & 15u), xh = threadIdx.x >> 7;
+    const uint32_t x_off = (xr >> 3) * kSboA + (xr & 7u) * 16u + 8u * xh * 128u;
 
-    uint32_t b_next = net.act[0];
-    for (uint32_t t = 0; t < net.t_max && ok; ++t)
+    uint32_t seq = 0;        // chunks expanded by this CTA in earlier steps (stage = seq % kStages)
+    uint32_t act_steps = 0;  // steps this CTA has computed (phase of done, exchange buffer)
+    bool in_flight = false;  // MMAs committed to `done` whose completion has not been seen
+    bool ok = true;
+    unsigned long long my_events = 0;
+    uint32_t b_next = net.act[t0];
+    for (uint32_t t = t0; t < t1; ++t)
     {
         const uint32_t b_act = b_next;
-        if (t + 1 < net.t_max) b_next = net.act[t + 1];  // used next step; the load overlaps this one
-        const bool active = m0 < b_act;
+        if (m0 >= b_act) break;  // sample tiles finish in order: this one has no steps left
+        if (t + 1 < t1) b_next = net.act[t + 1];  // used next step; the load overlaps this one
+        // Layer - 1's spikes of step t - 1 (slot t % kRing, written at steps t - 1, t - 1 - kRing, ...)
+        // published by every one of its CTAs of this sample tile?
+        if (threadIdx.x == 0)
+            s_ready = (ready_in && t > 0) ? poll_at_least(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1)) : 1;
         if (threadIdx.x < kBM) sbits[threadIdx.x] = 0;
-        if (active)
+        __syncthreads();
+        if (!s_ready)
         {
-            const uint8_t *src = net.spk[layer - 1][(t + 1) & 1] +
-                                 (static_cast<size_t>(m_tile) * n_chunks_all + c_lo) * kChunkBytes;
-            if (warp == kLoaderWarp && lane == 0)
+            ok = false;
+            break;
+        }
+        const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
+        const uint32_t *rowp = in_bits + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
+                               static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords + 2u * xh;
+        uint2 wv[kMaxHalfChunks];
+#pragma unroll
+        for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
+            wv[c] = c < n_chunks ? __ldcg(reinterpret_cast<const uint2 *>(rowp + c * kChunkWords)) : make_uint2(0u, 0u);
+        // Chunk by chunk: expand the bitmap words into the stage (after the MMAs that last read it),
+        // then one thread issues the chunk's MMAs.
+#pragma unroll
+        for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
+        {
+            if (c >= n_chunks) break;
+            const uint32_t u = seq + c, b = u % kStages;
+            if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
+            uint8_t *dst = sA + static_cast<size_t>(b) * kChunkBytes + x_off;
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q)
+                *reinterpret_cast<uint4 *>(dst + q * 128u) = bf16_bits(wv[c].x >> (8u * q));
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q)
+                *reinterpret_cast<uint4 *>(dst + (4u + q) * 128u) = bf16_bits(wv[c].y >> (8u * q));
+            tc::fence_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0)
             {
-                // Loader: the chunks were written by other CTAs before the grid barrier (generic
-                // proxy); the bulk copies read them through the async proxy.
-                asm volatile("fence.proxy.async.global;" ::: "memory");
-                for (uint32_t c = 0; c < n_chunks; ++c)
-                {
-                    const uint32_t sq = seq + c, b = sq % kStages;
-                    if (sq >= kStages && !tc::mbar_wait(&empty[b], (sq / kStages - 1) & 1u, kWaitLimit)) ok = false;
-                    mbar_arrive_expect_tx(&full[b], kChunkBytes);
-                    bulk_load(sA + static_cast<size_t>(b) * kChunkBytes, src + static_cast<size_t>(c) * kChunkBytes,
-                              kChunkBytes, &full[b]);
-                }
-            }
-            else if (warp < kIssuers && lane == 0)
-            {
-                // Issuer q: chunks q, q + 2, ... of this half into its accumulator, then one commit
-                // for the step.
-                for (uint32_t c = warp; c < n_chunks; c += kIssuers)
-                {
-                    const uint32_t sq = seq + c, b = sq % kStages;
-                    if (!tc::mbar_wait(&full[b], (sq / kStages) & 1u, kWaitLimit)) ok = false;
-                    tc::fence_after_sync();
-                    const uint64_t da = dA0 + b * (kChunkBytes >> 4);
-                    const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
-                    const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
-                    for (uint32_t j = 0; j < kc / 16; ++j)
-                        tc::mma_bf16(tmem + kPairN * warp, da + j * 16, db + j * 16, idesc,
-                                     (c >= static_cast<uint32_t>(kIssuers) || j > 0) ? 1u : 0u);
-                    tc::commit(&empty[b]);
-                }
-                tc::commit(&done[warp]);
+                tc::fence_after_sync();
+                const uint64_t da = dA0 + b * (kChunkBytes >> 4);
+                const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
+                const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
+                for (uint32_t j = 0; j < kc / 16; ++j)
+                    tc::mma_bf16(tmem, da + j * 16, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                tc::commit(&empty[b]);
             }
         }
-        // Input spikes of step t (layer 0), drawn by the drawing warps of every CTA: a warp makes one
-        // 32-input word per item, one draw per lane. Each lane writes its BF16 0/1 into layer 1's A
-        // layout; the ballot gives the word for the record and the event count.
-        if (drawer)
+        seq += n_chunks;
+        in_flight = true;
+        if (threadIdx.x == 0)
         {
-            uint8_t *d0 = net.spk[0][t & 1];
-            const unsigned long long ctr_t = static_cast<unsigned long long>(t) * net.batch;
-            const unsigned long long rec_t = net.record ? t * net.rec_stride + net.rec_off[0] : 0ull;
-            auto emit = [&](uint32_t slot, uint32_t wi, bool bit, uint32_t smp)
-            {
-                const uint32_t i = wi * 32 + lane;
-                if (i < kpad1)
-                    *reinterpret_cast<uint16_t *>(d0 + (slot / kBM) * spk0_tile + spk_offset(slot % kBM, i)) =
-                        bit ? 0x3F80u : 0u;
-                const uint32_t word = __ballot_sync(0xffffffffu, bit);
-                if (lane == 0 && slot < b_act)
-                {
-                    if (net.record) net.record[rec_t + static_cast<size_t>(smp) * w0 + wi] = word;
-                    my_events += static_cast<unsigned long long>(__popc(word)) *
-                                 (net.sample_size[1] ? net.sample_size[1][smp] : net.size[1]);
-                }
-            };
-            auto draw = [&](uint32_t slot, uint32_t wi, unsigned long long thr64, uint32_t smp) -> bool
-            {
-                const uint32_t i = wi * 32 + lane;
-                return slot < b_act && i < n_in && (rand64(net.key, (ctr_t + smp) * n_in + i) >> 11) < thr64;
-            };
-            // Word u = slot * w0 + wi advances by nw each item; (slot, wi) follow without division.
-            // The cached items' draws are independent: all drawn first, then written.
-            uint32_t slot = dr_slot0, wi = dr_wi0;
-            bool bits[kInCache];
-            uint32_t slots[kInCache], wis[kInCache];
-#pragma unroll
-            for (int j = 0; j < kInCache; ++j)
-            {
-                slots[j] = slot;
-                wis[j] = wi;
-                bits[j] = static_cast<uint32_t>(j) < dr_items && draw(slot, wi, in_thr[j], in_smp[j]);
-                wi += dr_step_r;
-                slot += dr_step_q;
-                if (wi >= w0)
-                {
-                    wi -= w0;
-                    ++slot;
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kInCache; ++j)
-                if (static_cast<uint32_t>(j) < dr_items) emit(slots[j], wis[j], bits[j], in_smp[j]);
-            for (uint32_t j = kInCache; j < dr_items; ++j)
-            {
-                const uint32_t i = wi * 32 + lane;
-                const uint32_t smp = net.perm[slot];
-                const bool exists = i < n_in && (!net.sample_size[0] || i < net.sample_size[0][smp]);
-                emit(slot, wi, draw(slot, wi, exists ? net.rate_thr[static_cast<size_t>(smp) * n_in + i] : 0ull, smp),
-                     smp);
-                wi += dr_step_r;
-                slot += dr_step_q;
-                if (wi >= w0)
-                {
-                    wi -= w0;
-                    ++slot;
-                }
-            }
+            tc::commit(&done);
+            if (consumed_in) release_add(consumed_in + t % kRing);  // every thread's words of the slot are expanded
         }
-        if (active)
+        const bool waited = tc::mbar_wait(&done, act_steps & 1u, kWaitLimit);
+        tc::fence_after_sync();
+        ok = __syncthreads_and((waited && ok) ? 1 : 0) != 0;
+        if (!ok) break;
+        in_flight = false;
+        const uint32_t xp = act_steps & 1u, xphase = (act_steps >> 1) & 1u;
+        ++act_steps;
+
+        // This half's partial sums of 16 columns at tile column `col`.
+        const uint32_t lane_base = (32u * (warp & 3)) << 16;
+        auto partial = [&](uint32_t col, float *v)
         {
-            // Every issuer commits done[] once per computed step; waiting for both means no MMA of
-            // this step is in flight.
-            bool waited = true;
-            for (int q = 0; q < kIssuers; ++q)
-                waited = tc::mbar_wait(&done[q], act_steps & 1u, kWaitLimit) && waited;
-            tc::fence_after_sync();
-            ok = __syncthreads_and((waited && ok) ? 1 : 0) != 0;
-            ++act_steps;
-            seq += n_chunks;
-            uint32_t mask = 0;
-            // This half's partial sums of 16 columns at tile column `col` (issuer 0 + issuer 1).
-            const uint32_t lane_base = (32u * (warp & 3)) << 16;
-            auto partial = [&](uint32_t col, float *v)
+            if (n_chunks == 0)
             {
-                if (n_chunks == 0)
-                {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) v[i] = 0.0f;
-                    return;
-                }
-                tc::tmem_ld16(tmem + lane_base + col, v);
-                for (int q = 1; q < kIssuers; ++q)
-                {
-                    if (static_cast<uint32_t>(q) >= n_chunks) break;
-                    float part[16];
-                    tc::tmem_ld16(tmem + lane_base + kPairN * q + col, part);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) v[i] = __fadd_rn(v[i], part[i]);
-                }
-            };
-            float acc[16];
-            // Hand the partner the columns it finalises, then add its partial to ours: the total is
-            // (K half 0) + (K half 1) on both sides.
-            if (ok)
-            {
-                partial(kBN * (1u - kh) + cb, acc);
-                float4 *xo = reinterpret_cast<float4 *>(net.xbuf + (static_cast<size_t>(item) * kBM + er) * kBN + cb);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) xo[i] = make_float4(acc[4 * i], acc[4 * i + 1], acc[4 * i + 2], acc[4 * i + 3]);
+                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+                return;
             }
-            ok = pair_sync(net.pair_flag + item / 2, 2u * (act_steps - 1u), 1u << 26) && ok;
-            if (ok)
+            tc::tmem_ld16(tmem + lane_base + col, v);
+        };
+        // Hand the partner the columns it finalises (row er, 16-byte slot s of the row stored at
+        // s ^ (er % 8), so that 8 consecutive rows read different banks), then add its partial to
+        // ours: the total is (K half 0) + (K half 1) on both sides.
+        float acc[16];
+        if (threadIdx.x == 0) mbar_arrive_expect_tx(&xfull[xp], kXchBytes);
+        partial(kBN * (1u - kh) + cb, acc);
+        const uint32_t row_peer = x_peer + xp * kXchBytes + er * (kBN * 4u);
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i)
+            tc::st_async_v4(row_peer + ((((cb >> 2) + i) ^ (er & 7u)) << 4), acc[4 * i], acc[4 * i + 1], acc[4 * i + 2],
+                            acc[4 * i + 3], xfull_peer[xp]);
+        partial(kBN * kh + cb, acc);
+        const bool got = tc::mbar_wait_cluster(&xfull[xp], xphase, kWaitLimit);
+        uint32_t mask = 0;
+        if (got)
+        {
+            const uint8_t *row_own = sX + xp * kXchBytes + er * (kBN * 4u);
+#pragma unroll
+            for (uint32_t i = 0; i < 4; ++i)
             {
-                partial(kBN * kh + cb, acc);
-                const float4 *xi =
-                    reinterpret_cast<const float4 *>(net.xbuf + (static_cast<size_t>(item ^ 1u) * kBM + er) * kBN + cb);
+                const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((((cb >> 2) + i) ^ (er & 7u)) << 4));
+                const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+                for (int e = 0; e < 4; ++e)
+                    acc[4 * i + e] = kh ? __fadd_rn(pv[e], acc[4 * i + e]) : __fadd_rn(acc[4 * i + e], pv[e]);
+            }
+            if (erow < b_act)
+            {
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
                 {
-                    const float4 p4 = __ldcg(xi + i);
-                    const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        acc[4 * i + e] = kh ? __fadd_rn(pv[e], acc[4 * i + e]) : __fadd_rn(acc[4 * i + e], pv[e]);
-                }
-                if (erow < b_act)
-                {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i)
+                    if (n0 + cb + i >= my_n) break;
+                    // lif_impl.h:33-86: leak and input only outside the refractory period;
+                    // strict '>'; reset to a value.
+                    if (RC[i] == 0u)
                     {
-                        if (n0 + cb + i >= my_n) break;
-                        // lif_impl.h:33-86: leak and input only outside the refractory period;
-                        // strict '>'; reset to a value.
-                        if (RC[i] == 0u)
+                        const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
+                        if (v > thr)
                         {
-                            const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
-                            if (v > thr)
-                            {
-                                V[i] = rst;
-                                RC[i] = per;
-                                mask |= 1u << (cb + i);
-                                ++CNT[i];
-                            }
-                            else
-                            {
-                                V[i] = v;
-                            }
+                            V[i] = rst;
+                            RC[i] = per;
+                            mask |= 1u << (cb + i);
+                            ++CNT[i];
                         }
                         else
                         {
-                            --RC[i];
+                            V[i] = v;
                         }
+                    }
+                    else
+                    {
+                        --RC[i];
                     }
                 }
             }
-            // This thread's 16 spikes as the next layer's A operand (two 16-byte stores).
-            if (layer < net.n_layers && erow < net.batch)
-            {
-                uint8_t *d = net.spk[layer][t & 1] + static_cast<size_t>(m_tile) * net.chunks[layer + 1] * kChunkBytes;
-                const uint32_t k = n0 + cb;
-                *reinterpret_cast<uint4 *>(d + spk_offset(er, k)) = bf16_bits(mask >> cb);
-                *reinterpret_cast<uint4 *>(d + spk_offset(er, k + 8)) = bf16_bits(mask >> (cb + 8));
-            }
-            if (mask) atomicOr(&sbits[er], mask);
-            my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
-            tc::fence_before_sync();
-            __syncthreads();
-            if (net.record && threadIdx.x < kBM && (n0 >> 5) < wn)  // the second half of a tile may lie past N
-            {
-                const uint32_t rr = threadIdx.x, rw = m0 + rr;
-                if (rw < b_act)
-                    net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[rw]) * wn +
-                               (n0 >> 5)] = sbits[rr];
-            }
         }
-        if (!grid_sync(net.barrier, gridDim.x, 1u << 26)) ok = false;
-        tc::fence_after_sync();
+        if (mask) atomicOr(&sbits[er], mask);
+        my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
+        // Ring slot (t + 1) % kRing was read at steps t + 1 - kRing, t + 1 - 2 kRing, ...: every
+        // consumer must have read it that many times.
+        if (threadIdx.x == 0)
+            s_room = (producer && t + 1 >= kRing)
+                         ? poll_at_least(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1))
+                         : 1;
+        tc::fence_before_sync();
+        ok = __syncthreads_and((got && ok) ? 1 : 0) != 0;
+        if (!ok || !s_room)
+        {
+            ok = false;
+            break;
+        }
+        if (threadIdx.x < kBM && (n0 >> 5) < wn)  // the second half of a tile may lie past N
+        {
+            const uint32_t r = threadIdx.x, word = sbits[r];
+            if (producer)
+                out_bits[((static_cast<size_t>((t + 1) % kRing) * m_tiles + m_tile) * kBM + r) * wp_out + (n0 >> 5)] =
+                    word;
+            if (net.record && m0 + r < b_act)
+                net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[m0 + r]) * wn +
+                           (n0 >> 5)] = word;
+        }
+        if (producer)
+        {
+            __syncthreads();
+            if (threadIdx.x == 0) release_add(ready_out + (t + 1) % kRing);
+        }
     }
-    // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
-    if (layer == net.n_layers && erow < net.batch)
+    if (t1 < net.t_max)
     {
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+        {
+            saved[i] = __float_as_uint(V[i]);
+            saved[16 + i] = RC[i];
+            saved[32 + i] = static_cast<uint32_t>(CNT[i]);
+        }
+    }
+    else if (layer == net.n_layers && erow < net.batch)
+    {
+        // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
         const uint32_t smp = net.perm[erow];
 #pragma unroll
         for (int i = 0; i < 16; ++i)
             if (n0 + cb + i < N) net.counts[static_cast<size_t>(smp) * N + n0 + cb + i] = CNT[i];
     }
     if (my_events) atomicAdd(&s_events, my_events);
-    if (!ok)
+    if (!ok && threadIdx.x == 0)
     {
-        if (threadIdx.x == 0) atomicOr(net.err, 1u);
-        // After a failed wait: let any MMA and bulk copy still in flight finish (bounded) before the
-        // tensor memory and shared memory are released.
-        if (threadIdx.x == 0)
-            for (int q = 0; q < kIssuers; ++q) tc::mbar_wait(&done[q], (act_steps + 1) & 1u, kWaitLimit);
-        if (warp == kLoaderWarp && lane == 0)
-            for (uint32_t sq = (seq > kStages ? seq - kStages : 0); sq < seq; ++sq)
-                tc::mbar_wait(&full[sq % kStages], (sq / kStages) & 1u, kWaitLimit);
+        atomicOr(net.err, 1u);
+        // After a failed wait: let the MMAs still in flight finish (bounded) before the tensor memory
+        // and shared memory are released.
+        if (in_flight) tc::mbar_wait(&done, act_steps & 1u, kWaitLimit);
     }
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
-    if (warp == 0) tc::tmem_dealloc(tmem, kPairN * kIssuers);
+    tc::cluster_sync();  // neither CTA leaves while the other may still write into its shared memory
+    if (warp == 0) tc::tmem_dealloc(tmem, kPairN);
 }
 
 }  // namespace
 
-// A batch prepared once and run as one CUDA-graph launch (memsets of the run's state, the input
-// threshold kernel and the cooperative persistent kernel). Reusable: every run starts from zero
-// state, so repeated runs of the same plan give identical results.
+// A batch prepared once and run as one CUDA-graph launch: memsets of the run's state, the input
+// threshold kernel, then per segment of steps the input-drawing kernel and the persistent kernel
+// (cluster launch of CTA pairs, every CTA resident). Reusable: every run starts from zero state, so
+// repeated runs of the same plan give identical results.
 struct BatchedPlan
 {
     BatchedNet net{};
@@ -699,10 +646,12 @@ struct BatchedPlan
     const float *rates = nullptr;
     unsigned long long *d_thr = nullptr;
     size_t n_thr = 0;
-    size_t w_bytes = 0;  // largest weight tile (shared memory besides the ring)
+    size_t w_bytes = 0;  // largest weight tile (shared memory besides the ring and the exchange buffers)
     uint32_t n_items = 0;
+    uint32_t seg_steps = 0;  // steps per segment
     cudaGraphExec_t exec = nullptr;
     int stages = 0;
+    bool cooperative = true;  // cluster launch with the cooperative attribute (cleared if refused)
     float tune_ms[kMaxStages + 1] = {};
 
     ~BatchedPlan()
@@ -722,29 +671,49 @@ const void *kernel_for(int stages)
 {
     switch (stages)
     {
+        case 2:
+            return reinterpret_cast<const void *>(batched_lif_kernel<2>);
         case 3:
             return reinterpret_cast<const void *>(batched_lif_kernel<3>);
-        case 4:
-            return reinterpret_cast<const void *>(batched_lif_kernel<4>);
         default:
-            return reinterpret_cast<const void *>(batched_lif_kernel<5>);
+            return reinterpret_cast<const void *>(batched_lif_kernel<4>);
     }
 }
 
-// Whether a ring of `stages` chunks fits (shared memory, every CTA resident at once).
+size_t smem_bytes(const BatchedPlan &p, int stages)
+{
+    return p.w_bytes + static_cast<size_t>(stages) * kChunkBytes + 2 * kXchBytes;
+}
+
+// Whether a ring of `stages` chunks fits (shared memory, every CTA pair resident at once).
 bool variant_fits(const BatchedPlan &p, int stages)
 {
-    int device = 0, sms = 0, smem_max = 0, per_sm = 0;
+    int device = 0, smem_max = 0;
     cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-    const size_t smem = p.w_bytes + static_cast<size_t>(stages) * kChunkBytes;
+    const size_t smem = smem_bytes(p, stages);
     if (smem + 2048 > static_cast<size_t>(smem_max)) return false;  // 2 KB: the kernel's static shared memory
     const void *k = kernel_for(stages);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
         return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBatchThreads, smem) != cudaSuccess) return false;
-    return static_cast<long long>(per_sm) * sms >= p.n_items;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(p.n_items);
+    cfg.blockDim = dim3(kBatchThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return 2ll * clusters >= p.n_items;
 }
 
 // Captures one run with a ring of `stages` chunks into p.exec.
@@ -760,18 +729,33 @@ cudaError_t capture(BatchedPlan &p, int stages)
     if (err != cudaSuccess) return err;
     for (auto &z : p.zero) cudaMemsetAsync(z.first, 0, z.second, s);
     rate_threshold_kernel<<<static_cast<unsigned>((p.n_thr + 255) / 256), 256, 0, s>>>(p.rates, p.d_thr, p.n_thr);
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(p.n_items);
-    cfg.blockDim = dim3(kBatchThreads);
-    cfg.dynamicSmemBytes = p.w_bytes + static_cast<size_t>(stages) * kChunkBytes;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    void *args[] = {&p.net};
-    const cudaError_t lerr = cudaLaunchKernelExC(&cfg, kernel_for(stages), args);
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t lerr = cudaSuccess;
+    for (uint32_t t0 = 0; t0 < p.net.t_max && lerr == cudaSuccess; t0 += p.seg_steps)
+    {
+        uint32_t t1 = std::min(p.net.t_max, t0 + p.seg_steps);
+        const size_t words = (static_cast<size_t>(t1 - t0) + 1) * p.net.m_tiles * kBM * p.net.wpad[0];
+        const unsigned blocks = static_cast<unsigned>(std::min<size_t>((words + 255) / 256, static_cast<size_t>(sms) * 8));
+        input_bits_kernel<<<blocks, 256, 0, s>>>(p.net, t0, t1);
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(p.n_items);
+        cfg.blockDim = dim3(kBatchThreads);
+        cfg.dynamicSmemBytes = smem_bytes(p, stages);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[2];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeCooperative;
+        attr[1].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = p.cooperative ? 2 : 1;
+        void *args[] = {&p.net, &t0, &t1};
+        lerr = cudaLaunchKernelExC(&cfg, kernel_for(stages), args);
+    }
     cudaGraph_t g = nullptr;
     err = cudaStreamEndCapture(s, &g);
     if (lerr != cudaSuccess) err = lerr;
@@ -801,18 +785,49 @@ cudaError_t launch_timed(BatchedPlan &p, float *ms)
     return err;
 }
 
+// Whether this process's device accepted a cooperative cluster launch (-1: not tried yet).
+int g_coop_cluster = -1;
+
+// Captures the plan with `stages` and, if `timed` (or to find out whether the cooperative cluster
+// launch is accepted), runs it once. A refused cooperative launch is captured again as a plain
+// cluster launch; co-residency of every CTA pair is still checked by variant_fits.
+cudaError_t prepare(BatchedPlan &p, int stages, bool timed, float *ms)
+{
+    p.cooperative = g_coop_cluster != 0;
+    cudaError_t err = capture(p, stages);
+    if (err == cudaSuccess && (timed || g_coop_cluster < 0)) err = launch_timed(p, ms);
+    if (err == cudaSuccess)
+    {
+        if (p.cooperative) g_coop_cluster = 1;
+        return err;
+    }
+    if (p.cooperative && g_coop_cluster < 0 &&
+        (err == cudaErrorInvalidValue || err == cudaErrorNotSupported || err == cudaErrorInvalidConfiguration ||
+         err == cudaErrorCooperativeLaunchTooLarge))
+    {
+        cudaGetLastError();
+        g_coop_cluster = 0;
+        p.cooperative = false;
+        err = capture(p, stages);
+        if (err == cudaSuccess && timed) err = launch_timed(p, ms);
+    }
+    return err;
+}
+
 }  // namespace
 
 // Prepares a batch. Host arrays: sizes[n_layers + 1], leak/threshold/reset/refract[n_layers],
 // steps[batch], sample_sizes[(n_layers + 1) * batch] (layer-major, optional); device arrays:
 // weights[l] (BF16 [sizes[l + 1]][sizes[l]]), rates [batch][sizes[0]], counts [batch][sizes[n_layers]]
-// and record (optional; layouts in knp_gb300.h). With `autotune`, each operand ring depth that fits
-// is run twice and the fastest kept; every depth computes the same results.
+// and record (optional; layouts in knp_gb300.h). With `autotune` > 0, each operand ring depth that
+// fits is run twice and the fastest kept; < 0 uses depth -autotune; 0 the deepest that fits. Every
+// depth computes the same results. `segment_steps` > 0
+// caps the steps per persistent launch (0: as many as layer 0's slot budget allows).
 int batched_plan_create(
     int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
-    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, cudaStream_t s,
-    BatchedPlan **out, const char **why)
+    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, uint32_t segment_steps,
+    cudaStream_t s, BatchedPlan **out, const char **why)
 {
     *out = nullptr;
     if (n_layers < 1 || n_layers > kMaxLayers || batch == 0 || !sizes || !weights || !steps || !rates || !counts)
@@ -844,6 +859,12 @@ int batched_plan_create(
         {
             net.kpad[l] = (sizes[l - 1] + 15) / 16 * 16;
             net.chunks[l] = (net.kpad[l] + kBK - 1) / kBK;
+            net.wpad[l - 1] = net.chunks[l] * kChunkWords;
+            if ((net.chunks[l] + 1) / 2 > kMaxHalfChunks)
+            {
+                *why = "a layer's fan-in exceeds 2048";
+                return -1;
+            }
         }
     }
     for (uint32_t b = 0; b < batch; ++b)
@@ -861,11 +882,14 @@ int batched_plan_create(
                     return -1;
                 }
     }
-    // Work items: (layer, 128-sample tile, 64-neuron tile, K half), the two halves of a tile adjacent.
+    // Work items: (layer, 128-sample tile, 64-neuron tile, K half), the two halves of a tile adjacent
+    // (one cluster).
     const uint32_t m_tiles = (batch + kBM - 1) / kBM;
+    net.m_tiles = m_tiles;
     for (int l = 1; l <= n_layers; ++l)
     {
         const uint32_t n_tiles = (net.size[l] + kPairN - 1) / kPairN;
+        net.n_cta[l] = 2 * n_tiles;
         for (uint32_t m = 0; m < m_tiles; ++m)
             for (uint32_t n = 0; n < n_tiles; ++n)
                 for (uint32_t h = 0; h < 2; ++h)
@@ -891,8 +915,19 @@ int batched_plan_create(
     if (!best)
     {
         *why = "the batch does not fit: a layer's weight tile and operand ring exceed one CTA's shared memory "
-               "(fan-in too large) or the work items exceed the resident CTAs";
+               "(fan-in too large) or the CTA pairs exceed the resident clusters";
         return -1;
+    }
+    if (autotune < 0)
+    {
+        // A fixed ring depth (-autotune).
+        if (-autotune < kMinStages || -autotune > kMaxStages || !variant_fits(p, -autotune))
+        {
+            *why = "the requested operand ring depth is out of range or does not fit";
+            return -1;
+        }
+        best = -autotune;
+        autotune = 0;
     }
     // Samples sorted by decreasing length.
     std::vector<uint32_t> perm(batch), st(batch);
@@ -912,6 +947,10 @@ int batched_plan_create(
         net.reset[l] = reset ? reset[l] : 0.0f;
         net.refract[l] = refract ? refract[l] : 0u;
     }
+    // Segments: layer 0's slots of one segment stay within the budget.
+    const size_t slot_bytes = static_cast<size_t>(m_tiles) * kBM * net.wpad[0] * 4;
+    p.seg_steps = static_cast<uint32_t>(std::max<size_t>(1, std::min<size_t>(net.t_max, kInputSlotBudget / slot_bytes)));
+    if (segment_steps) p.seg_steps = std::min(p.seg_steps, segment_steps);
     auto dalloc = [&](size_t bytes) -> void *
     {
         void *q = nullptr;
@@ -938,23 +977,24 @@ int batched_plan_create(
         for (int l = 0; l <= n_layers && ok; ++l)
             ok = (net.sample_size[l] = static_cast<const uint32_t *>(
                       upload(sample_sizes + static_cast<size_t>(l) * batch, batch * 4))) != nullptr;
-    for (int l = 0; l < n_layers && ok; ++l)
-        for (int q = 0; q < 2 && ok; ++q)
-        {
-            const size_t bytes = static_cast<size_t>(m_tiles) * net.chunks[l + 1] * kChunkBytes;
-            ok = (net.spk[l][q] = static_cast<uint8_t *>(dalloc(bytes))) != nullptr;
-            p.zero.emplace_back(net.spk[l][q], bytes);
-        }
+    ok = ok && (net.bits[0] = static_cast<uint32_t *>(dalloc(p.seg_steps * slot_bytes))) != nullptr;
+    for (int l = 1; l < n_layers && ok; ++l)
+    {
+        const size_t bytes = static_cast<size_t>(kRing) * m_tiles * kBM * net.wpad[l] * 4;
+        ok = (net.bits[l] = static_cast<uint32_t *>(dalloc(bytes))) != nullptr;
+        p.zero.emplace_back(net.bits[l], bytes);
+    }
+    const size_t n_counters = static_cast<size_t>(kMaxLayers + 1) * m_tiles * kRing;
+    ok = ok && (net.ready = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
+    ok = ok && (net.consumed = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
+    ok = ok && (net.state = static_cast<uint32_t *>(
+                    dalloc(static_cast<size_t>(p.n_items) * kBatchThreads * kStateWords * 4))) != nullptr;
     p.n_thr = static_cast<size_t>(batch) * sizes[0];
     ok = ok && (p.d_thr = static_cast<unsigned long long *>(dalloc(p.n_thr * 8))) != nullptr;
     net.rate_thr = p.d_thr;
     p.rates = rates;
     ok = ok && (net.events = static_cast<unsigned long long *>(dalloc(8))) != nullptr;
     ok = ok && (net.err = static_cast<unsigned int *>(dalloc(4))) != nullptr;
-    ok = ok && (net.barrier = static_cast<unsigned int *>(dalloc(8))) != nullptr;
-    ok = ok && (net.xbuf = static_cast<float *>(dalloc(static_cast<size_t>(p.n_items) * kBM * kBN * 4))) != nullptr;
-    ok = ok && (net.pair_flag = static_cast<unsigned int *>(dalloc(static_cast<size_t>(p.n_items / 2 + 1) * 4))) !=
-                   nullptr;
     if (!ok)
     {
         *why = "device allocation failed";
@@ -963,8 +1003,8 @@ int batched_plan_create(
     p.zero.emplace_back(counts, static_cast<size_t>(batch) * net.size[n_layers] * 4);
     p.zero.emplace_back(net.events, 8);
     p.zero.emplace_back(net.err, 4);
-    p.zero.emplace_back(net.barrier, 8);
-    p.zero.emplace_back(net.pair_flag, static_cast<size_t>(p.n_items / 2 + 1) * 4);
+    p.zero.emplace_back(net.ready, n_counters * 4);
+    p.zero.emplace_back(net.consumed, n_counters * 4);
     unsigned long long off = 0;
     for (int l = 0; l <= n_layers; ++l)
     {
@@ -981,9 +1021,9 @@ int batched_plan_create(
         for (int stg = kMinStages; stg <= kMaxStages; ++stg)
         {
             if (!variant_fits(p, stg)) continue;
-            err = capture(p, stg);
             float t = 0.f;
-            for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) err = launch_timed(p, &t);
+            err = prepare(p, stg, true, &t);
+            if (err == cudaSuccess) err = launch_timed(p, &t);
             if (err != cudaSuccess) break;
             p.tune_ms[stg] = t;
             if (!best_ms || t < best_ms)
@@ -992,8 +1032,12 @@ int batched_plan_create(
                 best = stg;
             }
         }
+        if (err == cudaSuccess && p.stages != best) err = capture(p, best);
     }
-    if (err == cudaSuccess && p.stages != best) err = capture(p, best);
+    else
+    {
+        err = prepare(p, best, false, nullptr);
+    }
     if (err != cudaSuccess)
     {
         *why = cudaGetErrorString(err);
@@ -1018,7 +1062,7 @@ int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, 
     }
     if (kerr)
     {
-        *why = "a tensor-core completion wait, a bulk copy wait or the grid barrier timed out";
+        *why = "a tensor-core completion wait, the pair exchange or a layer's step counter wait timed out";
         return -4;
     }
     return 0;
@@ -1042,7 +1086,7 @@ int batched_lif_run(
 {
     BatchedPlan *p = nullptr;
     int rc = batched_plan_create(n_layers, sizes, weights, leak, threshold, reset, refract, batch, steps, nullptr,
-                                 rates, key, counts, record, 0, s, &p, why);
+                                 rates, key, counts, record, 0, 0, s, &p, why);
     if (rc == 0) rc = batched_plan_run(p, events_out, ms, why);
     if (p) batched_plan_destroy(p);
     return rc;

@@ -36,8 +36,8 @@ struct BatchedPlan;
 int batched_plan_create(
     int n_layers, const uint32_t *sizes, const void *const *weights, const float *leak, const float *threshold,
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
-    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, cudaStream_t s,
-    BatchedPlan **out, const char **why);
+    const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, uint32_t segment_steps,
+    cudaStream_t s, BatchedPlan **out, const char **why);
 int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, const char **why);
 void batched_plan_info(const BatchedPlan *p, int *stages, float *tune_ms);
 void batched_plan_destroy(BatchedPlan *p);
@@ -406,8 +406,8 @@ int knp_gb300_batched_lif_run(
 int knp_gb300_batched_plan_create(
     int n_layers, const uint32_t *sizes, const void *const *d_weights, const float *leak, const float *threshold,
     const float *reset, const uint32_t *refract, uint32_t batch, const uint32_t *steps, const uint32_t *sample_sizes,
-    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, void *stream,
-    knp_gb300_batched_plan **plan)
+    const float *d_rates, uint64_t seed, int32_t *d_counts, uint32_t *d_record, int autotune, uint32_t segment_steps,
+    void *stream, knp_gb300_batched_plan **plan)
 {
     if (!plan)
     {
@@ -419,7 +419,8 @@ int knp_gb300_batched_plan_create(
     knp_gb300::BatchedPlan *p = nullptr;
     const int rc = knp_gb300::batched_plan_create(
         n_layers, sizes, d_weights, leak, threshold, reset, refract, batch, steps, sample_sizes, d_rates,
-        knp_gb300::stream_key(seed, 5), d_counts, d_record, autotune, static_cast<cudaStream_t>(stream), &p, &why);
+        knp_gb300::stream_key(seed, 5), d_counts, d_record, autotune, segment_steps, static_cast<cudaStream_t>(stream),
+        &p, &why);
     if (rc == 0) *plan = new knp_gb300_batched_plan{p};
     return batched_status(rc, why);
 }

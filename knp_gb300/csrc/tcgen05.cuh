@@ -105,6 +105,56 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// As mbar_wait, with cluster-scope acquire: for phases completed by another CTA of the cluster
+// (st.async with complete_tx into this CTA's shared memory).
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *mbar, uint32_t parity, uint32_t limit)
+{
+    const uint32_t a = smem_u32(mbar);
+    for (uint32_t i = 0; i < limit; ++i)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Address of the same shared-memory location in CTA `rank` of this cluster.
+__device__ __forceinline__ uint32_t mapa(uint32_t addr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
+// 16-byte store into another CTA's shared memory; its mbarrier `remote_mbar` counts the bytes.
+__device__ __forceinline__ void st_async_v4(uint32_t remote_addr, float a, float b, float c, float d,
+                                            uint32_t remote_mbar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                     remote_addr),
+                 "f"(a), "f"(b), "f"(c), "f"(d), "r"(remote_mbar)
+                 : "memory");
+}
+
+// Every thread of every CTA in the cluster arrives, then waits for all of them.
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
 // Thread t of warp w (w = warp index within its warpgroup) reads tensor-memory lane 32 w + t,
 // 16 consecutive 32-bit columns starting at `taddr`'s column.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)

@@ -135,7 +135,7 @@ def test_batched_plan_graph_runs_repeat_exactly():
     plan = BT.BatchedPlan(cfg, record=True, autotune=True)
     try:
         stages, tuned = plan.info()
-        assert stages in (3, 4, 5) and stages in tuned
+        assert stages in (2, 3, 4) and stages in tuned
         ev1, ms1 = plan.run()
         c1, r1 = plan.counts(), plan.record()
         ev2, ms2 = plan.run()
@@ -169,3 +169,20 @@ def test_batched_uneven_instance_sizes_match_plain_fp32_path():
     mism, total = _compare_with_plain(cfg, rec, counts)
     assert mism <= 1e-3 * total, (mism, total)
     assert events > 0 and ms > 0
+
+
+def test_batched_segments_give_identical_results():
+    """Cutting the run into persistent launches of a few steps each (LIF state saved and restored
+    between launches, layer rings and step counters carried over, input spikes drawn per segment)
+    changes no spike, count or event."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(seed=12, batch=150, sizes=(120, 200, 64, 10), t_lo=5, t_hi=33, rate_max=0.3)
+    c1, r1, e1, _ = BT.run(cfg, record=True)
+    assert e1 > 0
+    for seg in (1, 7):
+        c2, r2, e2, _ = BT.run(cfg, record=True, segment_steps=seg)
+        assert e2 == e1
+        np.testing.assert_array_equal(c2, c1)
+        for layer in r1:
+            np.testing.assert_array_equal(r2[layer], r1[layer])
