@@ -181,8 +181,11 @@ constexpr uint32_t kMaxHalfChunks = 8;           // chunks of a K half (bounded 
 constexpr uint32_t kRing = 8;                    // bitmap steps kept per layer
 constexpr uint32_t kXchBytes = kBM * kBN * 4;    // one exchange buffer: [kBM][kBN] FP32 partial sums
 constexpr uint32_t kPollLimit = 1u << 22;        // polls of a cross-CTA counter before giving up
-constexpr int kStateWords = 48;                  // V, refractory counter, spike count of 16 neurons
-constexpr int kBatchThreads = 256;
+constexpr int kExpandWarps = 4, kEpilogueWarps = 4;  // warps 0-3 expand, 4-7 epilogue, 8 issues
+constexpr int kIssuerWarp = kExpandWarps + kEpilogueWarps;
+constexpr int kExpandThreads = 32 * kExpandWarps, kEpilogueThreads = 32 * kEpilogueWarps;
+constexpr int kBatchThreads = kExpandThreads + kEpilogueThreads + 32;
+constexpr int kStateWords = 3 * kBN;  // V, refractory counter, spike count of an epilogue thread's neurons
 constexpr size_t kInputSlotBudget = size_t(256) << 20;  // bytes of layer 0's slots per segment
 
 struct BatchedNet
@@ -213,7 +216,7 @@ struct BatchedNet
     uint32_t *bits[kMaxLayers];
     unsigned int *ready;     // [kMaxLayers + 1][m_tiles][kRing]: writes of layer l's slot by its CTAs
     unsigned int *consumed;  // [kMaxLayers + 1][m_tiles][kRing]: reads of layer l's slot by layer l + 1's CTAs
-    uint32_t *state;         // [n_items][kBatchThreads][kStateWords]: LIF state between segments
+    uint32_t *state;         // [n_items][kEpilogueThreads][kStateWords]: LIF state between segments
     int *counts;             // [batch][size[L]] by sample
     uint32_t *record;        // [t_max][sum_l batch * words[l]] by sample, or null
     unsigned long long rec_off[kMaxLayers + 1];
@@ -308,17 +311,23 @@ __device__ __forceinline__ uint4 bf16_bits(uint32_t x)
     return v;
 }
 
+// Roles of the 9 warps: warps 0-3 expand the input bitmaps into the operand ring (one sample row
+// per thread), warps 4-7 run the epilogue (one sample row and the CTA's 32 neurons per thread; warp
+// 4 + w reads tensor-memory lanes 32 w .. 32 w + 31), lane 0 of warp 8 issues the MMAs. Two
+// accumulators in tensor memory let the MMAs of step s + 1 run while the epilogue of step s
+// exchanges partial sums and updates the neurons.
 template <int kStages>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net, uint32_t t0, uint32_t t1)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t full[kStages];   // stage b expanded (kExpandThreads arrivals)
     __shared__ __align__(8) uint64_t empty[kStages];  // the MMAs that read stage b have completed (commit)
-    __shared__ __align__(8) uint64_t done;            // every MMA of the step has completed (commit)
+    __shared__ __align__(8) uint64_t acc_full[2];     // every MMA into accumulator a has completed (commit)
+    __shared__ __align__(8) uint64_t acc_empty[2];    // the epilogue has read accumulator a (kEpilogueThreads)
     __shared__ __align__(8) uint64_t xfull[2];        // the partner's partial sums of a step have landed
-    __shared__ uint32_t sbits[kBM];
     __shared__ unsigned long long s_events;
-    __shared__ int s_ready, s_room;
+    __shared__ int s_fail;  // some role gave up on a wait (each group reads it through one thread)
     const uint32_t item = blockIdx.x;
     const int layer = net.item_layer[item];  // 1..L
     const uint32_t m_tile = net.item_m[item];
@@ -354,279 +363,290 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                                            : __float2bfloat16(0.0f);
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, kPairN);
+    if (warp == kIssuerWarp) tc::tmem_alloc(&tmem_slot, 2 * kPairN);
     if (threadIdx.x == 0)
     {
-        for (int b = 0; b < kStages; ++b) tc::mbar_init(&empty[b], 1);
-        tc::mbar_init(&done, 1);
-        tc::mbar_init(&xfull[0], 1);
-        tc::mbar_init(&xfull[1], 1);
+        for (int b = 0; b < kStages; ++b)
+        {
+            tc::mbar_init(&full[b], kExpandThreads);
+            tc::mbar_init(&empty[b], 1);
+        }
+        for (int a = 0; a < 2; ++a)
+        {
+            tc::mbar_init(&acc_full[a], 1);
+            tc::mbar_init(&acc_empty[a], kEpilogueThreads);
+            tc::mbar_init(&xfull[a], 1);
+        }
         s_events = 0;
+        s_fail = 0;
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::cluster_sync();  // the partner's barriers are initialised before any st.async reaches them
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
-    constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
-    // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
-    // adding byte offsets / 16 to the start-address field.
-    const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
-    const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
-    const uint32_t peer = tc::cluster_rank() ^ 1u;
-    const uint32_t x_peer = tc::mapa(tc::smem_u32(sX), peer);
-    const uint32_t xfull_peer[2] = {tc::mapa(tc::smem_u32(&xfull[0]), peer), tc::mapa(tc::smem_u32(&xfull[1]), peer)};
-
-    // Epilogue ownership, fixed for the run: thread (warp, lane) owns row 32 (warp % 4) + lane of the
-    // tile and columns 16 (warp / 4) .. +15, so it keeps their LIF state in registers.
-    const uint32_t er = 32u * (warp & 3) + lane;
-    const uint32_t erow = m0 + er;
-    const uint32_t cb = 16u * (warp >> 2);
-    float V[16];
-    uint32_t RC[16];
-    int CNT[16];
-    uint32_t *saved = net.state + (static_cast<size_t>(item) * kBatchThreads + threadIdx.x) * kStateWords;
-#pragma unroll
-    for (int i = 0; i < 16; ++i)
-    {
-        V[i] = t0 ? __uint_as_float(saved[i]) : 0.f;
-        RC[i] = t0 ? saved[16 + i] : 0u;
-        CNT[i] = t0 ? static_cast<int>(saved[32 + i]) : 0;
-    }
-    const int li = layer - 1;
-    const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
-    const uint32_t per = net.refract[li];
-    // This thread's sample: its own neuron count and its next layer's (the fan-out of its spikes).
-    const uint32_t e_smp = erow < net.batch ? net.perm[erow] : 0u;
-    const uint32_t my_n = (net.sample_size[layer] && erow < net.batch) ? net.sample_size[layer][e_smp] : N;
-    const uint32_t my_fan_out =
-        layer < net.n_layers ? ((net.sample_size[layer + 1] && erow < net.batch) ? net.sample_size[layer + 1][e_smp]
-                                                                                  : net.size[layer + 1])
-                             : 0u;
-
-    // Input side: layer - 1's bitmap slots and, above layer 1, its publication / consumption counters.
     const uint32_t m_tiles = net.m_tiles;
-    const uint32_t wp_in = net.wpad[layer - 1];
-    const uint32_t *in_bits = net.bits[layer - 1];
     const size_t ctr_in = (static_cast<size_t>(layer - 1) * m_tiles + m_tile) * kRing;
-    const unsigned int *ready_in = layer > 1 ? net.ready + ctr_in : nullptr;
-    unsigned int *consumed_in = layer > 1 ? net.consumed + ctr_in : nullptr;
-    const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] : 0u;
-    // Output side (every layer but the last).
-    const bool producer = layer < net.n_layers;
-    uint32_t *out_bits = producer ? net.bits[layer] : nullptr;
-    const uint32_t wp_out = producer ? net.wpad[layer] : 0u;
     const size_t ctr_out = (static_cast<size_t>(layer) * m_tiles + m_tile) * kRing;
-    unsigned int *ready_out = producer ? net.ready + ctr_out : nullptr;
-    const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
-    const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
-    // Expansion ownership: thread -> sample row xr, chunk words 2 xh and 2 xh + 1 (8-input groups
-    // 8 xh .. 8 xh + 7); a quarter warp covers 8 consecutive rows of one group (conflict-free stores).
-    const uint32_t xr = (threadIdx.x & 7u) + 8u * ((threadIdx.x >> 3) & 15u), xh = threadIdx.x >> 7;
-    const uint32_t x_off = (xr >> 3) * kSboA + (xr & 7u) * 16u + 8u * xh * 128u;
-
-    uint32_t seq = 0;        // chunks expanded by this CTA in earlier steps (stage = seq % kStages)
-    uint32_t act_steps = 0;  // steps this CTA has computed (phase of done, exchange buffer)
-    bool in_flight = false;  // MMAs committed to `done` whose completion has not been seen
-    bool ok = true;
+    const bool producer = layer < net.n_layers;
     unsigned long long my_events = 0;
-    uint32_t b_next = net.act[t0];
-    for (uint32_t t = t0; t < t1; ++t)
-    {
-        const uint32_t b_act = b_next;
-        if (m0 >= b_act) break;  // sample tiles finish in order: this one has no steps left
-        if (t + 1 < t1) b_next = net.act[t + 1];  // used next step; the load overlaps this one
-        // Layer - 1's spikes of step t - 1 (slot t % kRing, written at steps t - 1, t - 1 - kRing, ...)
-        // published by every one of its CTAs of this sample tile?
-        if (threadIdx.x == 0)
-            s_ready = (ready_in && t > 0) ? poll_at_least(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1)) : 1;
-        if (threadIdx.x < kBM) sbits[threadIdx.x] = 0;
-        __syncthreads();
-        if (!s_ready)
-        {
-            ok = false;
-            break;
-        }
-        const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
-        const uint32_t *rowp = in_bits + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
-                               static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords + 2u * xh;
-        uint2 wv[kMaxHalfChunks];
-#pragma unroll
-        for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
-            wv[c] = c < n_chunks ? __ldcg(reinterpret_cast<const uint2 *>(rowp + c * kChunkWords)) : make_uint2(0u, 0u);
-        // Chunk by chunk: expand the bitmap words into the stage (after the MMAs that last read it),
-        // then one thread issues the chunk's MMAs.
-#pragma unroll
-        for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
-        {
-            if (c >= n_chunks) break;
-            const uint32_t u = seq + c, b = u % kStages;
-            if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
-            uint8_t *dst = sA + static_cast<size_t>(b) * kChunkBytes + x_off;
-#pragma unroll
-            for (uint32_t q = 0; q < 4; ++q)
-                *reinterpret_cast<uint4 *>(dst + q * 128u) = bf16_bits(wv[c].x >> (8u * q));
-#pragma unroll
-            for (uint32_t q = 0; q < 4; ++q)
-                *reinterpret_cast<uint4 *>(dst + (4u + q) * 128u) = bf16_bits(wv[c].y >> (8u * q));
-            tc::fence_async_smem();
-            __syncthreads();
-            if (threadIdx.x == 0)
-            {
-                tc::fence_after_sync();
-                const uint64_t da = dA0 + b * (kChunkBytes >> 4);
-                const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
-                const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
-                for (uint32_t j = 0; j < kc / 16; ++j)
-                    tc::mma_bf16(tmem, da + j * 16, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
-                tc::commit(&empty[b]);
-            }
-        }
-        seq += n_chunks;
-        in_flight = true;
-        if (threadIdx.x == 0)
-        {
-            tc::commit(&done);
-            if (consumed_in) release_add(consumed_in + t % kRing);  // every thread's words of the slot are expanded
-        }
-        const bool waited = tc::mbar_wait(&done, act_steps & 1u, kWaitLimit);
-        tc::fence_after_sync();
-        ok = __syncthreads_and((waited && ok) ? 1 : 0) != 0;
-        if (!ok) break;
-        in_flight = false;
-        const uint32_t xp = act_steps & 1u, xphase = (act_steps >> 1) & 1u;
-        ++act_steps;
 
-        // This half's partial sums of 16 columns at tile column `col`.
+    if (warp < kExpandWarps)
+    {
+        // Expanders: per step, wait until every CTA of layer - 1 (this sample tile) has published
+        // step t - 1, load this row's words of the K half, and write each chunk as BF16 0/1 into a
+        // free stage (8 consecutive rows of one 8-input group per quarter warp: conflict-free).
+        const uint32_t xr = threadIdx.x;
+        const uint32_t wp_in = net.wpad[layer - 1];
+        const unsigned int *ready_in = layer > 1 ? net.ready + ctr_in : nullptr;
+        const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] : 0u;
+        const uint32_t x_off = (xr >> 3) * kSboA + (xr & 7u) * 16u;
+        uint32_t seq = 0;
+        bool ok = true;
+        for (uint32_t t = t0; t < t1; ++t)
+        {
+            if (m0 >= net.act[t]) break;  // sample tiles finish in order: no steps left
+            bool go = ok;
+            if (threadIdx.x == 0)
+                go = go && !s_fail &&
+                     (!ready_in || t == 0 || poll_at_least(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1)));
+            if (!tc::named_sync_and(1, kExpandThreads, go))  // the group's decision is uniform
+            {
+                s_fail = 1;
+                break;
+            }
+            const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
+            const uint4 *rowp = reinterpret_cast<const uint4 *>(
+                net.bits[layer - 1] + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
+                static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords);
+            uint4 wv[kMaxHalfChunks];
+#pragma unroll
+            for (uint32_t c = 0; c < kMaxHalfChunks; ++c) wv[c] = c < n_chunks ? __ldcg(rowp + c) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
+            {
+                if (c >= n_chunks) break;
+                const uint32_t u = seq + c, b = u % kStages;
+                if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
+                uint8_t *dst = sA + static_cast<size_t>(b) * kChunkBytes + x_off;
+                const uint32_t w4[4] = {wv[c].x, wv[c].y, wv[c].z, wv[c].w};
+#pragma unroll
+                for (uint32_t g = 0; g < 16; ++g)
+                    *reinterpret_cast<uint4 *>(dst + g * 128u) = bf16_bits(w4[g >> 2] >> (8u * (g & 3u)));
+                tc::fence_async_smem();
+                tc::mbar_arrive(&full[b]);
+            }
+            seq += n_chunks;
+        }
+    }
+    else if (warp < kExpandWarps + kEpilogueWarps)
+    {
+        // Epilogue: thread (warp 4 + w, lane) owns sample row er = 32 w + lane of the tile and the
+        // CTA's 32 neurons, keeping their LIF state in registers.
+        const uint32_t et = threadIdx.x - kExpandThreads;
+        const uint32_t er = et, erow = m0 + er;
         const uint32_t lane_base = (32u * (warp & 3)) << 16;
+        float V[kBN];
+        uint32_t RC[kBN];
+        int CNT[kBN];
+        uint32_t *saved = net.state + (static_cast<size_t>(item) * kEpilogueThreads + et) * kStateWords;
+#pragma unroll
+        for (int i = 0; i < kBN; ++i)
+        {
+            V[i] = t0 ? __uint_as_float(saved[i]) : 0.f;
+            RC[i] = t0 ? saved[kBN + i] : 0u;
+            CNT[i] = t0 ? static_cast<int>(saved[2 * kBN + i]) : 0;
+        }
+        const int li = layer - 1;
+        const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
+        const uint32_t per = net.refract[li];
+        // This row's sample: its own neuron count and its next layer's (the fan-out of its spikes).
+        const uint32_t e_smp = erow < net.batch ? net.perm[erow] : 0u;
+        const uint32_t my_n = (net.sample_size[layer] && erow < net.batch) ? net.sample_size[layer][e_smp] : N;
+        const uint32_t my_fan_out =
+            producer ? ((net.sample_size[layer + 1] && erow < net.batch) ? net.sample_size[layer + 1][e_smp]
+                                                                          : net.size[layer + 1])
+                     : 0u;
+        uint32_t *out_bits = producer ? net.bits[layer] : nullptr;
+        const uint32_t wp_out = producer ? net.wpad[layer] : 0u;
+        unsigned int *ready_out = producer ? net.ready + ctr_out : nullptr;
+        const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
+        const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
+        const uint32_t peer = tc::cluster_rank() ^ 1u;
+        const uint32_t x_peer = tc::mapa(tc::smem_u32(sX), peer);
+        const uint32_t xfull_peer[2] = {tc::mapa(tc::smem_u32(&xfull[0]), peer),
+                                        tc::mapa(tc::smem_u32(&xfull[1]), peer)};
         auto partial = [&](uint32_t col, float *v)
         {
             if (n_chunks == 0)
             {
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+                for (int i = 0; i < kBN; ++i) v[i] = 0.0f;
                 return;
             }
             tc::tmem_ld16(tmem + lane_base + col, v);
+            tc::tmem_ld16(tmem + lane_base + col + 16, v + 16);
         };
-        // Hand the partner the columns it finalises (row er, 16-byte slot s of the row stored at
-        // s ^ (er % 8), so that 8 consecutive rows read different banks), then add its partial to
-        // ours: the total is (K half 0) + (K half 1) on both sides.
-        float acc[16];
-        if (threadIdx.x == 0) mbar_arrive_expect_tx(&xfull[xp], kXchBytes);
-        partial(kBN * (1u - kh) + cb, acc);
-        const uint32_t row_peer = x_peer + xp * kXchBytes + er * (kBN * 4u);
-#pragma unroll
-        for (uint32_t i = 0; i < 4; ++i)
-            tc::st_async_v4(row_peer + ((((cb >> 2) + i) ^ (er & 7u)) << 4), acc[4 * i], acc[4 * i + 1], acc[4 * i + 2],
-                            acc[4 * i + 3], xfull_peer[xp]);
-        partial(kBN * kh + cb, acc);
-        const bool got = tc::mbar_wait_cluster(&xfull[xp], xphase, kWaitLimit);
-        uint32_t mask = 0;
-        if (got)
+        uint32_t s = 0;
+        for (uint32_t t = t0; t < t1; ++t)
         {
-            const uint8_t *row_own = sX + xp * kXchBytes + er * (kBN * 4u);
+            const uint32_t b_act = net.act[t];
+            if (m0 >= b_act) break;
+            // Ring slot (t + 1) % kRing was read at steps t + 1 - kRing, t + 1 - 2 kRing, ...: every
+            // consumer must have read it that many times before it is overwritten below.
+            bool room = true;
+            if (et == 0 && producer && t + 1 >= kRing)
+                room = poll_at_least(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1));
+            const uint32_t a = s & 1u, ph = (s >> 1) & 1u;
+            bool ok = tc::mbar_wait(&acc_full[a], ph, kWaitLimit);
+            tc::fence_after_sync();
+            // Hand the partner the columns it finalises (row er, 16-byte slot q of the row stored at
+            // q ^ (er % 8), so that 8 consecutive rows hit different banks), keep ours, release the
+            // accumulator, then add the partner's partial: (K half 0) + (K half 1) on both sides.
+            if (et == 0) mbar_arrive_expect_tx(&xfull[a], kXchBytes);
+            float acc[kBN];
+            partial(a * kPairN + kBN * (1u - kh), acc);
+            const uint32_t row_peer = x_peer + a * kXchBytes + er * (kBN * 4u);
 #pragma unroll
-            for (uint32_t i = 0; i < 4; ++i)
+            for (uint32_t q = 0; q < kBN / 4; ++q)
+                tc::st_async_v4(row_peer + ((q ^ (er & 7u)) << 4), acc[4 * q], acc[4 * q + 1], acc[4 * q + 2],
+                                acc[4 * q + 3], xfull_peer[a]);
+            partial(a * kPairN + kBN * kh, acc);
+            tc::fence_before_sync();
+            tc::mbar_arrive(&acc_empty[a]);
+            ok = tc::mbar_wait_cluster(&xfull[a], ph, kWaitLimit) && ok;
+            uint32_t mask = 0;
+            if (ok)
             {
-                const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((((cb >> 2) + i) ^ (er & 7u)) << 4));
-                const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+                const uint8_t *row_own = sX + a * kXchBytes + er * (kBN * 4u);
 #pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    acc[4 * i + e] = kh ? __fadd_rn(pv[e], acc[4 * i + e]) : __fadd_rn(acc[4 * i + e], pv[e]);
-            }
-            if (erow < b_act)
-            {
-#pragma unroll
-                for (int i = 0; i < 16; ++i)
+                for (uint32_t q = 0; q < kBN / 4; ++q)
                 {
-                    if (n0 + cb + i >= my_n) break;
-                    // lif_impl.h:33-86: leak and input only outside the refractory period;
-                    // strict '>'; reset to a value.
-                    if (RC[i] == 0u)
+                    const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((q ^ (er & 7u)) << 4));
+                    const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        acc[4 * q + e] = kh ? __fadd_rn(pv[e], acc[4 * q + e]) : __fadd_rn(acc[4 * q + e], pv[e]);
+                }
+                if (erow < b_act)
+                {
+#pragma unroll
+                    for (int i = 0; i < kBN; ++i)
                     {
-                        const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
-                        if (v > thr)
+                        if (n0 + i >= my_n) break;
+                        // lif_impl.h:33-86: leak and input only outside the refractory period;
+                        // strict '>'; reset to a value.
+                        if (RC[i] == 0u)
                         {
-                            V[i] = rst;
-                            RC[i] = per;
-                            mask |= 1u << (cb + i);
-                            ++CNT[i];
+                            const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
+                            if (v > thr)
+                            {
+                                V[i] = rst;
+                                RC[i] = per;
+                                mask |= 1u << i;
+                                ++CNT[i];
+                            }
+                            else
+                            {
+                                V[i] = v;
+                            }
                         }
                         else
                         {
-                            V[i] = v;
+                            --RC[i];
                         }
-                    }
-                    else
-                    {
-                        --RC[i];
                     }
                 }
             }
-        }
-        if (mask) atomicOr(&sbits[er], mask);
-        my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
-        // Ring slot (t + 1) % kRing was read at steps t + 1 - kRing, t + 1 - 2 kRing, ...: every
-        // consumer must have read it that many times.
-        if (threadIdx.x == 0)
-            s_room = (producer && t + 1 >= kRing)
-                         ? poll_at_least(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1))
-                         : 1;
-        tc::fence_before_sync();
-        ok = __syncthreads_and((got && ok) ? 1 : 0) != 0;
-        if (!ok || !s_room)
-        {
-            ok = false;
-            break;
-        }
-        if (threadIdx.x < kBM && (n0 >> 5) < wn)  // the second half of a tile may lie past N
-        {
-            const uint32_t r = threadIdx.x, word = sbits[r];
+            const bool go = ok && room && (et != 0 || !s_fail);
+            if (!tc::named_sync_and(2, kEpilogueThreads, go))  // the group's decision is uniform
+            {
+                s_fail = 1;
+                break;
+            }
+            ++s;
+            my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
+            if ((n0 >> 5) < wn)  // the second half of a tile may lie past N
+            {
+                if (producer)
+                    out_bits[((static_cast<size_t>((t + 1) % kRing) * m_tiles + m_tile) * kBM + er) * wp_out +
+                             (n0 >> 5)] = mask;
+                if (net.record && erow < b_act)
+                    net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(e_smp) * wn + (n0 >> 5)] =
+                        mask;
+            }
             if (producer)
-                out_bits[((static_cast<size_t>((t + 1) % kRing) * m_tiles + m_tile) * kBM + r) * wp_out + (n0 >> 5)] =
-                    word;
-            if (net.record && m0 + r < b_act)
-                net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(net.perm[m0 + r]) * wn +
-                           (n0 >> 5)] = word;
+            {
+                tc::named_sync_and(2, kEpilogueThreads, true);
+                if (et == 0) release_add(ready_out + (t + 1) % kRing);
+            }
         }
-        if (producer)
+        if (t1 < net.t_max)
         {
-            __syncthreads();
-            if (threadIdx.x == 0) release_add(ready_out + (t + 1) % kRing);
+#pragma unroll
+            for (int i = 0; i < kBN; ++i)
+            {
+                saved[i] = __float_as_uint(V[i]);
+                saved[kBN + i] = RC[i];
+                saved[2 * kBN + i] = static_cast<uint32_t>(CNT[i]);
+            }
+        }
+        else if (layer == net.n_layers && erow < net.batch)
+        {
+            // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
+#pragma unroll
+            for (int i = 0; i < kBN; ++i)
+                if (n0 + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + i] = CNT[i];
         }
     }
-    if (t1 < net.t_max)
+    else if (lane == 0)
     {
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
+        // Issuer: per step, once the epilogue has released accumulator s % 2 (step s - 2), the MMAs
+        // of each expanded stage, then one commit for the accumulator. The input slot has been read
+        // once every stage of the step is expanded.
+        constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
+        // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
+        // adding byte offsets / 16 to the start-address field.
+        const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
+        const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
+        unsigned int *consumed_in = layer > 1 ? net.consumed + ctr_in : nullptr;
+        uint32_t seq = 0, s = 0;
+        for (uint32_t t = t0; t < t1; ++t)
         {
-            saved[i] = __float_as_uint(V[i]);
-            saved[16 + i] = RC[i];
-            saved[32 + i] = static_cast<uint32_t>(CNT[i]);
+            if (m0 >= net.act[t] || s_fail) break;
+            const uint32_t a = s & 1u;
+            if (s >= 2 && !tc::mbar_wait(&acc_empty[a], ((s >> 1) - 1u) & 1u, kWaitLimit)) s_fail = 1;
+            tc::fence_after_sync();
+            for (uint32_t c = 0; c < n_chunks; ++c)
+            {
+                const uint32_t u = seq + c, b = u % kStages;
+                if (!tc::mbar_wait(&full[b], (u / kStages) & 1u, kWaitLimit)) s_fail = 1;
+                tc::fence_after_sync();
+                const uint64_t da = dA0 + b * (kChunkBytes >> 4);
+                const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
+                const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
+                for (uint32_t j = 0; j < kc / 16; ++j)
+                    tc::mma_bf16(tmem + a * kPairN, da + j * 16, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                tc::commit(&empty[b]);
+            }
+            seq += n_chunks;
+            tc::commit(&acc_full[a]);
+            if (consumed_in) release_add(consumed_in + t % kRing);
+            ++s;
         }
-    }
-    else if (layer == net.n_layers && erow < net.batch)
-    {
-        // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
-        const uint32_t smp = net.perm[erow];
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-            if (n0 + cb + i < N) net.counts[static_cast<size_t>(smp) * N + n0 + cb + i] = CNT[i];
+        // Let the MMAs still in flight finish (bounded) before the tensor memory is released.
+        if (s) tc::mbar_wait(&acc_full[(s - 1) & 1u], ((s - 1) >> 1) & 1u, kWaitLimit);
     }
     if (my_events) atomicAdd(&s_events, my_events);
-    if (!ok && threadIdx.x == 0)
-    {
-        atomicOr(net.err, 1u);
-        // After a failed wait: let the MMAs still in flight finish (bounded) before the tensor memory
-        // and shared memory are released.
-        if (in_flight) tc::mbar_wait(&done, act_steps & 1u, kWaitLimit);
-    }
     tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x == 0 && s_events) atomicAdd(net.events, s_events);
+    if (threadIdx.x == 0)
+    {
+        if (s_fail) atomicOr(net.err, 1u);
+        if (s_events) atomicAdd(net.events, s_events);
+    }
     tc::cluster_sync();  // neither CTA leaves while the other may still write into its shared memory
-    if (warp == 0) tc::tmem_dealloc(tmem, kPairN);
+    if (warp == kIssuerWarp) tc::tmem_dealloc(tmem, 2 * kPairN);
 }
 
 }  // namespace
@@ -988,7 +1008,7 @@ int batched_plan_create(
     ok = ok && (net.ready = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
     ok = ok && (net.consumed = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
     ok = ok && (net.state = static_cast<uint32_t *>(
-                    dalloc(static_cast<size_t>(p.n_items) * kBatchThreads * kStateWords * 4))) != nullptr;
+                    dalloc(static_cast<size_t>(p.n_items) * kEpilogueThreads * kStateWords * 4))) != nullptr;
     p.n_thr = static_cast<size_t>(batch) * sizes[0];
     ok = ok && (p.d_thr = static_cast<unsigned long long *>(dalloc(p.n_thr * 8))) != nullptr;
     net.rate_thr = p.d_thr;

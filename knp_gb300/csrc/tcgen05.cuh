@@ -142,6 +142,25 @@ __device__ __forceinline__ void st_async_v4(uint32_t remote_addr, float a, float
                  : "memory");
 }
 
+// One arrival (release, CTA scope) on a shared-memory mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// Named barrier `id` over `n` threads (a multiple of 32) that also ANDs a predicate across them, so
+// every participant leaves with the same decision.
+__device__ __forceinline__ bool named_sync_and(uint32_t id, uint32_t n, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"(static_cast<uint32_t>(v)), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
 // Every thread of every CTA in the cluster arrives, then waits for all of them.
 __device__ __forceinline__ void cluster_sync()
 {
