@@ -174,8 +174,11 @@ namespace
 constexpr int kBM = 128, kBN = 32, kBK = 128, kMaxLayers = 4, kMaxItems = 512;
 constexpr int kPairN = 2 * kBN;                 // neurons of a CTA pair's tile; each CTA finalises kBN
 constexpr int kMinStages = 2, kMaxStages = 4;  // operand ring depths the autotuner tries
-constexpr uint32_t kChunkBytes = kBM * kBK * 2;  // one 128 x 128 BF16 chunk
-constexpr uint32_t kSboA = (kBK / 8) * 128;      // row-group stride of a chunk (16 core matrices)
+constexpr uint32_t kAccCols = 2 * kPairN;        // tensor-memory columns of the two accumulators
+constexpr uint32_t kStageCols = kBK / 2;         // tensor-memory columns of one 128 x 128 BF16 operand chunk
+constexpr uint32_t kTmemCols = 512;              // the whole tensor memory (one CTA per SM)
+constexpr size_t kMinDynSmem = size_t(120) << 10;  // keeps a second CTA off the SM (it would wait for tensor memory)
+static_assert(kAccCols + kMaxStages * kStageCols <= kTmemCols, "operand stages exceed tensor memory");
 constexpr uint32_t kChunkWords = kBK / 32;       // bitmap words per sample row and chunk
 constexpr uint32_t kMaxHalfChunks = 8;           // chunks of a K half (bounded by shared memory)
 constexpr uint32_t kRing = 8;                    // bitmap steps kept per layer
@@ -185,7 +188,7 @@ constexpr int kExpandWarps = 4, kEpilogueWarps = 4;  // warps 0-3 expand, 4-7 ep
 constexpr int kIssuerWarp = kExpandWarps + kEpilogueWarps;
 constexpr int kExpandThreads = 32 * kExpandWarps, kEpilogueThreads = 32 * kEpilogueWarps;
 constexpr int kBatchThreads = kExpandThreads + kEpilogueThreads + 32;
-constexpr int kStateWords = 3 * kBN;  // V, refractory counter, spike count of an epilogue thread's neurons
+constexpr int kStateWords = 2 * kBN;  // V and refractory counter of an epilogue thread's neurons
 constexpr size_t kInputSlotBudget = size_t(256) << 20;  // bytes of layer 0's slots per segment
 
 struct BatchedNet
@@ -300,17 +303,6 @@ __device__ __forceinline__ void release_add(unsigned int *counter)
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
 }
 
-// The low 8 bits of x as eight BF16 values 0 or 1.0 (0x3F80), bit i -> element i.
-__device__ __forceinline__ uint4 bf16_bits(uint32_t x)
-{
-    uint4 v;
-    v.x = ((x & 1u) ? 0x3F80u : 0u) | ((x & 2u) ? 0x3F800000u : 0u);
-    v.y = ((x & 4u) ? 0x3F80u : 0u) | ((x & 8u) ? 0x3F800000u : 0u);
-    v.z = ((x & 16u) ? 0x3F80u : 0u) | ((x & 32u) ? 0x3F800000u : 0u);
-    v.w = ((x & 64u) ? 0x3F80u : 0u) | ((x & 128u) ? 0x3F800000u : 0u);
-    return v;
-}
-
 // Roles of the 9 warps: warps 0-3 expand the input bitmaps into the operand ring (one sample row
 // per thread), warps 4-7 run the epilogue (one sample row and the CTA's 32 neurons per thread; warp
 // 4 + w reads tensor-memory lanes 32 w .. 32 w + 31), lane 0 of warp 8 issues the MMAs. Two
@@ -321,7 +313,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t full[kStages];   // stage b expanded (kExpandThreads arrivals)
+    __shared__ __align__(8) uint64_t full[kStages];   // operand stage b written (kExpandThreads arrivals)
     __shared__ __align__(8) uint64_t empty[kStages];  // the MMAs that read stage b have completed (commit)
     __shared__ __align__(8) uint64_t acc_full[2];     // every MMA into accumulator a has completed (commit)
     __shared__ __align__(8) uint64_t acc_empty[2];    // the epilogue has read accumulator a (kEpilogueThreads)
@@ -344,11 +336,10 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t c_lo = kh ? c_mid : 0u, c_hi = kh ? n_chunks_all : c_mid;
     const uint32_t n_chunks = c_hi - c_lo;  // this CTA's chunks (<= kMaxHalfChunks)
     const uint32_t Kw = c_mid * kBK;        // K extent of the weight tile (the larger half)
-    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), kStages operand stages, two
-    // exchange buffers.
+    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), two exchange buffers. Tensor
+    // memory: two accumulators (columns [0, kAccCols)), then kStages operand stages of kStageCols.
     uint8_t *sW = smem;
-    uint8_t *sA = smem + static_cast<size_t>(kPairN) * Kw * 2;
-    uint8_t *sX = sA + static_cast<size_t>(kStages) * kChunkBytes;
+    uint8_t *sX = smem + static_cast<size_t>(kPairN) * Kw * 2;
     const uint32_t sbo_w = (Kw / 8) * 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -363,7 +354,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                                            : __float2bfloat16(0.0f);
         *reinterpret_cast<uint4 *>(sW + tc::core_offset(r, k, 128, sbo_w)) = *reinterpret_cast<uint4 *>(tmp);
     }
-    if (warp == kIssuerWarp) tc::tmem_alloc(&tmem_slot, 2 * kPairN);
+    if (warp == kIssuerWarp) tc::tmem_alloc(&tmem_slot, kTmemCols);
     if (threadIdx.x == 0)
     {
         for (int b = 0; b < kStages; ++b)
@@ -395,12 +386,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     {
         // Expanders: per step, wait until every CTA of layer - 1 (this sample tile) has published
         // step t - 1, load this row's words of the K half, and write each chunk as BF16 0/1 into a
-        // free stage (8 consecutive rows of one 8-input group per quarter warp: conflict-free).
+        // free operand stage in tensor memory (thread = sample row = tensor-memory lane).
         const uint32_t xr = threadIdx.x;
         const uint32_t wp_in = net.wpad[layer - 1];
         const unsigned int *ready_in = layer > 1 ? net.ready + ctr_in : nullptr;
         const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] : 0u;
-        const uint32_t x_off = (xr >> 3) * kSboA + (xr & 7u) * 16u;
+        const uint32_t x_lane = (32u * warp) << 16;
         uint32_t seq = 0;
         bool ok = true;
         for (uint32_t t = t0; t < t1; ++t)
@@ -428,12 +419,23 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 if (c >= n_chunks) break;
                 const uint32_t u = seq + c, b = u % kStages;
                 if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
-                uint8_t *dst = sA + static_cast<size_t>(b) * kChunkBytes + x_off;
+                tc::fence_after_sync();
                 const uint32_t w4[4] = {wv[c].x, wv[c].y, wv[c].z, wv[c].w};
 #pragma unroll
-                for (uint32_t g = 0; g < 16; ++g)
-                    *reinterpret_cast<uint4 *>(dst + g * 128u) = bf16_bits(w4[g >> 2] >> (8u * (g & 3u)));
-                tc::fence_async_smem();
+                for (uint32_t q = 0; q < 4; ++q)
+                {
+                    // Word q holds inputs 32 q .. 32 q + 31 of the chunk: 16 columns of two BF16 each.
+                    uint32_t v[16];
+#pragma unroll
+                    for (uint32_t i = 0; i < 16; ++i)
+                    {
+                        const uint32_t two = w4[q] >> (2u * i);
+                        v[i] = ((two & 1u) ? 0x3F80u : 0u) | ((two & 2u) ? 0x3F800000u : 0u);
+                    }
+                    tc::tmem_st16(tmem + x_lane + kAccCols + b * kStageCols + 16u * q, v);
+                }
+                tc::tmem_wait_st();
+                tc::fence_before_sync();
                 tc::mbar_arrive(&full[b]);
             }
             seq += n_chunks;
@@ -448,14 +450,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint32_t lane_base = (32u * (warp & 3)) << 16;
         float V[kBN];
         uint32_t RC[kBN];
-        int CNT[kBN];
         uint32_t *saved = net.state + (static_cast<size_t>(item) * kEpilogueThreads + et) * kStateWords;
 #pragma unroll
         for (int i = 0; i < kBN; ++i)
         {
             V[i] = t0 ? __uint_as_float(saved[i]) : 0.f;
             RC[i] = t0 ? saved[kBN + i] : 0u;
-            CNT[i] = t0 ? static_cast<int>(saved[2 * kBN + i]) : 0;
         }
         const int li = layer - 1;
         const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
@@ -472,6 +472,10 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         unsigned int *ready_out = producer ? net.ready + ctr_out : nullptr;
         const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
         const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
+        // Output spike counts of the last layer (zeroed before the run), one owner per (sample, neuron).
+        int *count_row = (layer == net.n_layers && erow < net.batch)
+                             ? net.counts + static_cast<size_t>(e_smp) * N + n0
+                             : nullptr;
         const uint32_t peer = tc::cluster_rank() ^ 1u;
         const uint32_t x_peer = tc::mapa(tc::smem_u32(sX), peer);
         const uint32_t xfull_peer[2] = {tc::mapa(tc::smem_u32(&xfull[0]), peer),
@@ -544,7 +548,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                                 V[i] = rst;
                                 RC[i] = per;
                                 mask |= 1u << i;
-                                ++CNT[i];
+                                if (count_row) ++count_row[i];
                             }
                             else
                             {
@@ -588,15 +592,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             {
                 saved[i] = __float_as_uint(V[i]);
                 saved[kBN + i] = RC[i];
-                saved[2 * kBN + i] = static_cast<uint32_t>(CNT[i]);
             }
-        }
-        else if (layer == net.n_layers && erow < net.batch)
-        {
-            // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
-#pragma unroll
-            for (int i = 0; i < kBN; ++i)
-                if (n0 + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + i] = CNT[i];
         }
     }
     else if (lane == 0)
@@ -605,9 +601,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         // of each expanded stage, then one commit for the accumulator. The input slot has been read
         // once every stage of the step is expanded.
         constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
-        // Matrix descriptors of stage 0 and of the weight tile's first K slice; the others follow by
-        // adding byte offsets / 16 to the start-address field.
-        const uint64_t dA0 = tc::smem_desc(tc::smem_u32(sA), 128, kSboA);
+        // Matrix descriptor of the weight tile's first K slice; the others follow by adding byte
+        // offsets / 16 to the start-address field. The A operand is read from tensor memory.
         const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
         unsigned int *consumed_in = layer > 1 ? net.consumed + ctr_in : nullptr;
         uint32_t seq = 0, s = 0;
@@ -622,11 +617,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                 const uint32_t u = seq + c, b = u % kStages;
                 if (!tc::mbar_wait(&full[b], (u / kStages) & 1u, kWaitLimit)) s_fail = 1;
                 tc::fence_after_sync();
-                const uint64_t da = dA0 + b * (kChunkBytes >> 4);
+                const uint32_t ta = tmem + kAccCols + b * kStageCols;
                 const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
                 const uint32_t kc = min(static_cast<uint32_t>(kBK), Kp - (c_lo + c) * kBK);
                 for (uint32_t j = 0; j < kc / 16; ++j)
-                    tc::mma_bf16(tmem + a * kPairN, da + j * 16, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                    tc::mma_bf16_ta(tmem + a * kPairN, ta + j * 8, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
                 tc::commit(&empty[b]);
             }
             seq += n_chunks;
@@ -646,7 +641,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         if (s_events) atomicAdd(net.events, s_events);
     }
     tc::cluster_sync();  // neither CTA leaves while the other may still write into its shared memory
-    if (warp == kIssuerWarp) tc::tmem_dealloc(tmem, 2 * kPairN);
+    if (warp == kIssuerWarp) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 }  // namespace
@@ -702,7 +697,8 @@ const void *kernel_for(int stages)
 
 size_t smem_bytes(const BatchedPlan &p, int stages)
 {
-    return p.w_bytes + static_cast<size_t>(stages) * kChunkBytes + 2 * kXchBytes;
+    (void)stages;  // operand stages live in tensor memory
+    return std::max(p.w_bytes + 2 * kXchBytes, kMinDynSmem);
 }
 
 // Whether a ring of `stages` chunks fits (shared memory, every CTA pair resident at once).
