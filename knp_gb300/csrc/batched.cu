@@ -22,7 +22,7 @@ namespace
 constexpr int kGemmM = 128;
 constexpr int kGemmN = 64;
 constexpr int kGemmK = 64;  // K chunk staged in shared memory
-constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait calls of up to kSuspendNs each
 
 // Stage rows [r0, r0 + rows) x K-chunk [k0, k0 + kGemmK) of a row-major BF16 matrix into the
 // canonical no-swizzle K-major layout (zero outside the matrix).
@@ -188,7 +188,8 @@ constexpr int kExpandWarps = 4, kEpilogueWarps = 4;  // warps 0-3 expand, 4-7 ep
 constexpr int kIssuerWarp = kExpandWarps + kEpilogueWarps;
 constexpr int kExpandThreads = 32 * kExpandWarps, kEpilogueThreads = 32 * kEpilogueWarps;
 constexpr int kBatchThreads = kExpandThreads + kEpilogueThreads + 32;
-constexpr int kStateWords = 2 * kBN;  // V and refractory counter of an epilogue thread's neurons
+constexpr int kStateWords = 3 * kBN;  // V, refractory counter, spike count of an epilogue thread's neurons
+constexpr uint32_t kCntBytes = kBM * kBN * 4;  // last layer's spike counts of a tile, [kBN][kBM] int
 constexpr size_t kInputSlotBudget = size_t(256) << 20;  // bytes of layer 0's slots per segment
 
 struct BatchedNet
@@ -298,6 +299,28 @@ __device__ __forceinline__ bool poll_at_least(const unsigned int *counter, unsig
     return false;
 }
 
+// A counter read ahead of need (relaxed: later memory operations do not wait for it). A value
+// found sufficient is followed by fence_acquire() before the data it guards is touched.
+__device__ __forceinline__ unsigned int load_relaxed(const unsigned int *counter)
+{
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Whether *counter >= target: from a value read ahead if that suffices, else by polling.
+__device__ __forceinline__ bool reached(const unsigned int *counter, unsigned int target, unsigned int seen)
+{
+    if (static_cast<int>(seen - target) >= 0)
+    {
+        fence_acquire();
+        return true;
+    }
+    return poll_at_least(counter, target);
+}
+
 __device__ __forceinline__ void release_add(unsigned int *counter)
 {
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
@@ -336,7 +359,8 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     const uint32_t c_lo = kh ? c_mid : 0u, c_hi = kh ? n_chunks_all : c_mid;
     const uint32_t n_chunks = c_hi - c_lo;  // this CTA's chunks (<= kMaxHalfChunks)
     const uint32_t Kw = c_mid * kBK;        // K extent of the weight tile (the larger half)
-    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), two exchange buffers. Tensor
+    // Shared memory: weight tile [kPairN x Kw] (K-major core matrices), two exchange buffers, the
+    // last layer's spike counts. Tensor
     // memory: two accumulators (columns [0, kAccCols)), then kStages operand stages of kStageCols.
     uint8_t *sW = smem;
     uint8_t *sX = smem + static_cast<size_t>(kPairN) * Kw * 2;
@@ -394,13 +418,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint32_t x_lane = (32u * warp) << 16;
         uint32_t seq = 0;
         bool ok = true;
+        unsigned int ready_seen = 0;  // this step's counter, read during the previous step
         for (uint32_t t = t0; t < t1; ++t)
         {
             if (m0 >= net.act[t]) break;  // sample tiles finish in order: no steps left
             bool go = ok;
             if (threadIdx.x == 0)
                 go = go && !s_fail &&
-                     (!ready_in || t == 0 || poll_at_least(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1)));
+                     (!ready_in || t == 0 || reached(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1), ready_seen));
             if (!tc::named_sync_and(1, kExpandThreads, go))  // the group's decision is uniform
             {
                 s_fail = 1;
@@ -413,14 +438,18 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             uint4 wv[kMaxHalfChunks];
 #pragma unroll
             for (uint32_t c = 0; c < kMaxHalfChunks; ++c) wv[c] = c < n_chunks ? __ldcg(rowp + c) : make_uint4(0, 0, 0, 0);
-#pragma unroll
-            for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
+            if (threadIdx.x == 0 && ready_in && t + 1 < t1) ready_seen = load_relaxed(ready_in + (t + 1) % kRing);
+            // One copy of the chunk body (kept small for the instruction cache); the loaded words
+            // shift down by one chunk per iteration so that every register index stays static.
+#pragma unroll 1
+            for (uint32_t c = 0; c < n_chunks; ++c)
             {
-                if (c >= n_chunks) break;
                 const uint32_t u = seq + c, b = u % kStages;
                 if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
                 tc::fence_after_sync();
-                const uint32_t w4[4] = {wv[c].x, wv[c].y, wv[c].z, wv[c].w};
+                const uint32_t w4[4] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w};
+#pragma unroll
+                for (uint32_t k = 0; k + 1 < kMaxHalfChunks; ++k) wv[k] = wv[k + 1];
 #pragma unroll
                 for (uint32_t q = 0; q < 4; ++q)
                 {
@@ -472,24 +501,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         unsigned int *ready_out = producer ? net.ready + ctr_out : nullptr;
         const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
         const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
-        // Output spike counts of the last layer (zeroed before the run), one owner per (sample, neuron).
-        int *count_row = (layer == net.n_layers && erow < net.batch)
-                             ? net.counts + static_cast<size_t>(e_smp) * N + n0
-                             : nullptr;
+        // Last layer: spike counts in shared memory, neuron-major so that a warp's 32 rows hit 32 banks.
+        int *cnt = layer == net.n_layers ? reinterpret_cast<int *>(sX + 2 * kXchBytes) + er : nullptr;
+        if (cnt)
+#pragma unroll
+            for (int i = 0; i < kBN; ++i) cnt[i * kBM] = t0 ? static_cast<int>(saved[2 * kBN + i]) : 0;
         const uint32_t peer = tc::cluster_rank() ^ 1u;
-        const uint32_t x_peer = tc::mapa(tc::smem_u32(sX), peer);
-        const uint32_t xfull_peer[2] = {tc::mapa(tc::smem_u32(&xfull[0]), peer),
-                                        tc::mapa(tc::smem_u32(&xfull[1]), peer)};
         auto partial = [&](uint32_t col, float *v)
         {
             if (n_chunks == 0)
             {
 #pragma unroll
-                for (int i = 0; i < kBN; ++i) v[i] = 0.0f;
+                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
                 return;
             }
             tc::tmem_ld16(tmem + lane_base + col, v);
-            tc::tmem_ld16(tmem + lane_base + col + 16, v + 16);
         };
         uint32_t s = 0;
         for (uint32_t t = t0; t < t1; ++t)
@@ -497,71 +523,65 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             const uint32_t b_act = net.act[t];
             if (m0 >= b_act) break;
             // Ring slot (t + 1) % kRing was read at steps t + 1 - kRing, t + 1 - 2 kRing, ...: every
-            // consumer must have read it that many times before it is overwritten below.
-            bool room = true;
-            if (et == 0 && producer && t + 1 >= kRing)
-                room = poll_at_least(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1));
+            // consumer must have read it that many times before it is overwritten below (the count
+            // is read now and checked after the update).
+            const bool check_room = et == 0 && producer && t + 1 >= kRing;
+            const unsigned int room_seen = check_room ? load_relaxed(consumed_out + (t + 1) % kRing) : 0u;
             const uint32_t a = s & 1u, ph = (s >> 1) & 1u;
             bool ok = tc::mbar_wait(&acc_full[a], ph, kWaitLimit);
             tc::fence_after_sync();
-            // Hand the partner the columns it finalises (row er, 16-byte slot q of the row stored at
-            // q ^ (er % 8), so that 8 consecutive rows hit different banks), keep ours, release the
-            // accumulator, then add the partner's partial: (K half 0) + (K half 1) on both sides.
+            // Read the accumulator while the tensor cores are idle (the issuer starts the next step's
+            // MMAs once it is released): the partner's columns go straight to the partner (row er,
+            // 16-byte slot q of the row stored at q ^ (er % 8), so that 8 consecutive rows hit
+            // different banks), ours stay in registers. Then our partial + the partner's ((K half 0)
+            // + (K half 1) on both sides) and the LIF update.
             if (et == 0) mbar_arrive_expect_tx(&xfull[a], kXchBytes);
+            const uint32_t row_peer = tc::mapa(tc::smem_u32(sX), peer) + a * kXchBytes + er * (kBN * 4u);
+            const uint32_t xfull_peer = tc::mapa(tc::smem_u32(&xfull[a]), peer);
             float acc[kBN];
             partial(a * kPairN + kBN * (1u - kh), acc);
-            const uint32_t row_peer = x_peer + a * kXchBytes + er * (kBN * 4u);
+            partial(a * kPairN + kBN * (1u - kh) + 16u, acc + 16);
 #pragma unroll
             for (uint32_t q = 0; q < kBN / 4; ++q)
                 tc::st_async_v4(row_peer + ((q ^ (er & 7u)) << 4), acc[4 * q], acc[4 * q + 1], acc[4 * q + 2],
-                                acc[4 * q + 3], xfull_peer[a]);
+                                acc[4 * q + 3], xfull_peer);
             partial(a * kPairN + kBN * kh, acc);
+            partial(a * kPairN + kBN * kh + 16u, acc + 16);
             tc::fence_before_sync();
             tc::mbar_arrive(&acc_empty[a]);
             ok = tc::mbar_wait_cluster(&xfull[a], ph, kWaitLimit) && ok;
             uint32_t mask = 0;
-            if (ok)
+            const uint8_t *row_own = sX + a * kXchBytes + er * (kBN * 4u);
+#pragma unroll
+            for (uint32_t q = 0; q < kBN / 4; ++q)
             {
-                const uint8_t *row_own = sX + a * kXchBytes + er * (kBN * 4u);
+                const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((q ^ (er & 7u)) << 4));
+                const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
-                for (uint32_t q = 0; q < kBN / 4; ++q)
-                {
-                    const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((q ^ (er & 7u)) << 4));
-                    const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        acc[4 * q + e] = kh ? __fadd_rn(pv[e], acc[4 * q + e]) : __fadd_rn(acc[4 * q + e], pv[e]);
-                }
-                if (erow < b_act)
-                {
-#pragma unroll
-                    for (int i = 0; i < kBN; ++i)
-                    {
-                        if (n0 + i >= my_n) break;
-                        // lif_impl.h:33-86: leak and input only outside the refractory period;
-                        // strict '>'; reset to a value.
-                        if (RC[i] == 0u)
-                        {
-                            const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
-                            if (v > thr)
-                            {
-                                V[i] = rst;
-                                RC[i] = per;
-                                mask |= 1u << i;
-                                if (count_row) ++count_row[i];
-                            }
-                            else
-                            {
-                                V[i] = v;
-                            }
-                        }
-                        else
-                        {
-                            --RC[i];
-                        }
-                    }
-                }
+                for (int e = 0; e < 4; ++e)
+                    acc[4 * q + e] = kh ? __fadd_rn(pv[e], acc[4 * q + e]) : __fadd_rn(acc[4 * q + e], pv[e]);
             }
+            // Neurons at or past this sample's size do not exist (never updated, never spike).
+            const uint32_t n_here = (ok && erow < b_act && my_n > n0) ? my_n - n0 : 0u;
+            const uint32_t exists = n_here >= 32u ? 0xFFFFFFFFu : (1u << n_here) - 1u;
+#pragma unroll
+            for (int i = 0; i < kBN; ++i)
+            {
+                // lif_impl.h:33-86: leak and input only outside the refractory period; strict '>';
+                // reset to a value. Branch-free: the lanes are different samples.
+                const bool here = (exists >> i) & 1u;
+                const bool free_ = RC[i] == 0u;
+                const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
+                const bool spike = here && free_ && v > thr;
+                V[i] = spike ? rst : ((here && free_) ? v : V[i]);
+                RC[i] = spike ? per : ((here && !free_) ? RC[i] - 1u : RC[i]);
+                mask |= static_cast<uint32_t>(spike) << i;
+            }
+            if (cnt)
+                for (uint32_t m = mask; m; m &= m - 1u) ++cnt[(__ffs(m) - 1) * kBM];
+            const bool room =
+                !check_room ||
+                reached(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1), room_seen);
             const bool go = ok && room && (et != 0 || !s_fail);
             if (!tc::named_sync_and(2, kEpilogueThreads, go))  // the group's decision is uniform
             {
@@ -592,13 +612,20 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             {
                 saved[i] = __float_as_uint(V[i]);
                 saved[kBN + i] = RC[i];
+                if (cnt) saved[2 * kBN + i] = static_cast<uint32_t>(cnt[i * kBM]);
             }
+        }
+        else if (cnt && erow < net.batch)
+        {
+            // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
+            for (int i = 0; i < kBN; ++i)
+                if (n0 + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + i] = cnt[i * kBM];
         }
     }
     else if (lane == 0)
     {
-        // Issuer: per step, once the epilogue has released accumulator s % 2 (step s - 2), the MMAs
-        // of each expanded stage, then one commit for the accumulator. The input slot has been read
+        // Issuer: per step, once the epilogue has read the previous step's accumulator, the MMAs of
+        // each expanded stage into accumulator s % 2, then one commit for it. The input slot has been read
         // once every stage of the step is expanded.
         constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kPairN);
         // Matrix descriptor of the weight tile's first K slice; the others follow by adding byte
@@ -610,7 +637,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         {
             if (m0 >= net.act[t] || s_fail) break;
             const uint32_t a = s & 1u;
-            if (s >= 2 && !tc::mbar_wait(&acc_empty[a], ((s >> 1) - 1u) & 1u, kWaitLimit)) s_fail = 1;
+            // The epilogue has read the previous step's accumulator (no tensor-memory reads run
+            // beside these MMAs).
+            if (s >= 1 && !tc::mbar_wait(&acc_empty[(s - 1) & 1u], ((s - 1) >> 1) & 1u, kWaitLimit)) s_fail = 1;
             tc::fence_after_sync();
             for (uint32_t c = 0; c < n_chunks; ++c)
             {
@@ -698,7 +727,7 @@ const void *kernel_for(int stages)
 size_t smem_bytes(const BatchedPlan &p, int stages)
 {
     (void)stages;  // operand stages live in tensor memory
-    return std::max(p.w_bytes + 2 * kXchBytes, kMinDynSmem);
+    return std::max(p.w_bytes + 2 * kXchBytes + kCntBytes, kMinDynSmem);
 }
 
 // Whether a ring of `stages` chunks fits (shared memory, every CTA pair resident at once).

@@ -114,6 +114,11 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Upper bound of one try_wait's suspension (ns): a waiting thread sleeps instead of spinning, so it
+// does not take issue slots from the other warps of its SM sub-partition; it wakes when the phase
+// completes.
+constexpr uint32_t kSuspendNs = 4096;
+
 // Wait for phase `parity` of the mbarrier to complete; false after `limit` polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit)
 {
@@ -122,10 +127,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(kSuspendNs)
             : "memory");
         if (done) return true;
     }
@@ -141,10 +146,10 @@ __device__ __forceinline__ bool mbar_wait_cluster(uint64_t *mbar, uint32_t parit
     {
         uint32_t done;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(kSuspendNs)
             : "memory");
         if (done) return true;
     }
