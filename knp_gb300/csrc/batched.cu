@@ -155,9 +155,9 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
 // 32 neurons, whose LIF state stays in registers.
 //
 // Spikes travel between layers as bitmaps (one 32-bit word per sample and 32 neurons) in a ring of
-// kRing steps per layer. A consumer expands its K half chunk by chunk into BF16 operand tiles in
-// shared memory (canonical no-swizzle K-major layout) while the tensor cores multiply the previous
-// chunk. There is no grid-wide barrier: per (layer, sample tile, ring slot) counters record how
+// kRing steps per layer. A consumer expands its K half chunk by chunk into BF16 operand chunks in
+// tensor memory (one sample row per lane) while the tensor cores multiply the previous chunk. There
+// is no grid-wide barrier: per (layer, sample tile, ring slot) counters record how
 // many times the layer's CTAs have written the slot (`ready`) and how many times consumer CTAs have
 // read it (`consumed`), so a layer starts step t as soon as every CTA of the layer below has
 // published step t - 1, and overwrites a slot only after every consumer has read it (a layer runs
