@@ -8,7 +8,8 @@ arrays (9 GB) are far larger than L2, so no L2 flush is needed between steps.
 
 value      synaptic events/s with the background schedule already in HBM, CUDA-event timed.
 e2e        the same metric through the C ABI with host buffers: every step the host sends the
-           step's background spikes (pinned host -> device) and reads the population's spikes back.
+           step's background spikes (pinned host -> device) and reads the population's spikes back
+           (bitmap device -> host, expanded to indexes), pipelined one step deep as a caller would.
 roofline   the dominant kernel phase (projection scatter), algorithmic bytes 9 B per synaptic event
            + 8 B per presynaptic spike row, divided by its CUDA-event time measured here.
 cpu_baseline / --impl reference: the CPU oracle (restated single-threaded backend step) on a
@@ -449,17 +450,22 @@ def main():
         b.synchronize()
         ea, _, _ = b.counters()
         h2d = d2h = n_out = 0
+        buf = np.empty(n_neurons, np.uint32)
         t0 = time.perf_counter()
-        for k in range(args.e2e_steps):
-            idx = sched.at(k)
-            b.send_spikes(chan_uid, idx, start + k)
-            h2d += idx.nbytes
-            b.step(1)
-            out = b.spikes(pop_uid, start + k)  # ascending indexes, as in the reference's SpikeMessage
-            b.discard_spikes(start + k + 1)
-            # What crosses to the host is the step's spike bitmap (one bit per neuron), expanded there.
-            d2h += (n_neurons + 31) // 32 * 4
-            n_out += out.size
+        # Pipelined as a caller would: step k + 1 is queued (its input sent) before step k's spikes are
+        # read, so the device runs step k + 1 while the host copies and expands step k's spikes.
+        for k in range(args.e2e_steps + 1):
+            if k < args.e2e_steps:
+                idx = sched.at(k)
+                b.send_spikes(chan_uid, idx, start + k)
+                h2d += idx.nbytes
+                b.step(1)
+            if k > 0:
+                out = b.spikes(pop_uid, start + k - 1, out=buf)  # ascending, as in the reference's SpikeMessage
+                b.discard_spikes(start + k)
+                # What crosses to the host is the step's spike bitmap (one bit per neuron), expanded there.
+                d2h += (n_neurons + 31) // 32 * 4
+                n_out += out.size
         b.synchronize()
         te = time.perf_counter() - t0
         eb, _, _ = b.counters()

@@ -241,10 +241,12 @@ class GB300Backend:
         self._chk(self._lib.knp_gb300_generate_bernoulli_schedule(self._h, T.to_c_uid(sender), n_sources, float(p),
                                                                   first_step, n_steps, seed, stream))
 
-    def spikes(self, pop: bytes, step: int, cap: int | None = None) -> np.ndarray:
-        """Ascending spike indexes of ``pop`` at ``step`` (population must be recorded)."""
+    def spikes(self, pop: bytes, step: int, cap: int | None = None, out: np.ndarray | None = None) -> np.ndarray:
+        """Ascending spike indexes of ``pop`` at ``step`` (population must be recorded). ``out``: a
+        reusable uint32 buffer to expand into (the result is a view of it when it is large enough)."""
         n = self._pops[pop].size if cap is None and pop in self._pops else (cap or 0)
-        out = np.empty(max(n, 1), np.uint32)
+        if out is None or out.dtype != np.uint32 or not out.flags.c_contiguous or out.size < max(n, 1):
+            out = np.empty(max(n, 1), np.uint32)
         cnt = ctypes.c_uint32(0)
         self._chk(self._lib.knp_gb300_read_spikes(self._h, T.to_c_uid(pop), step, out.size, _ptr(out),
                                                   ctypes.byref(cnt)))
@@ -253,6 +255,14 @@ class GB300Backend:
             self._chk(self._lib.knp_gb300_read_spikes(self._h, T.to_c_uid(pop), step, out.size, _ptr(out),
                                                       ctypes.byref(cnt)))
         return out[: cnt.value]
+
+    def spikes_capped(self, pop: bytes, step: int, out: np.ndarray) -> int:
+        """Writes at most ``out.size`` ascending spike indexes of ``pop`` at ``step`` into ``out``
+        (uint32) and returns the step's full spike count."""
+        cnt = ctypes.c_uint32(0)
+        self._chk(self._lib.knp_gb300_read_spikes(self._h, T.to_c_uid(pop), step, out.size, _ptr(out),
+                                                  ctypes.byref(cnt)))
+        return int(cnt.value)
 
     def discard_spikes(self, before_step: int):
         self._chk(self._lib.knp_gb300_discard_spikes(self._h, before_step))

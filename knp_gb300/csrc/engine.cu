@@ -92,6 +92,9 @@ Backend::Backend(int device) : device_(device)
     KNP_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
     KNP_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     KNP_CUDA(cudaEventCreateWithFlags(&pinned_free_, cudaEventDisableTiming));
+    KNP_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+    for (auto &e : step_ev_) KNP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    KNP_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ctl_host_), sizeof(Control), cudaHostAllocDefault));
     ctl_ = arena_.make<Control>(1);
 }
 
@@ -106,6 +109,11 @@ Backend::~Backend()
     if (pinned_) cudaFreeHost(pinned_);
     if (rec_host_) cudaFreeHost(rec_host_);
     if (pinned_free_) cudaEventDestroy(pinned_free_);
+    if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+    for (auto &e : step_ev_)
+        if (e) cudaEventDestroy(e);
+    if (ctl_host_) cudaFreeHost(ctl_host_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -1080,6 +1088,7 @@ void Backend::step(uint64_t n)
         {
             stage_host_inputs();
             KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
+            if (any_recording_) record_step_event(step_);
             ++step_;
             --n;
             continue;
@@ -1097,6 +1106,7 @@ void Backend::step(uint64_t n)
             KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
             ++done;
         }
+        if (any_recording_ && k) record_step_event(step_ + k - 1);
         step_ += k;
         n -= k;
     }
@@ -1195,56 +1205,128 @@ void Backend::alloc_recording(PopulationSlot &p)
     any_recording_ = true;
 }
 
-// Copies the recorded bitmaps of steps [drained_to_, step_) to the host (per step: the bitmap and
-// its spike count); read_spikes expands a step's bitmap into ascending spike indexes, the order of
-// the reference's SpikeMessage (populations_old.h:104-118).
-void Backend::drain_recordings()
+void Backend::record_step_event(uint64_t last_step)
 {
-    const uint64_t steps = step_ - drained_to_;
-    if (steps)
+    const uint64_t slot = last_step % kStepEvents;
+    KNP_CUDA(cudaEventRecord(step_ev_[slot], stream_));
+    step_ev_of_[slot] = last_step + 1;
+}
+
+// Copies the recorded bitmaps of steps [drained_to_, upto) to the host (per step: the bitmap and
+// its spike count); read_spikes expands a step's bitmap into ascending spike indexes, the order of
+// the reference's SpikeMessage (populations_old.h:104-118). When the completion event of step
+// upto - 1 is at hand, the copy waits for that event only (on copy_stream_), so the steps queued
+// after it keep running; otherwise it waits for the whole stream.
+void Backend::drain_recordings(uint64_t upto)
+{
+    upto = std::min(upto, step_);
+    if (upto <= drained_to_) return;
+    const uint64_t steps = upto - drained_to_;
+    const uint64_t ev = (upto - 1) % kStepEvents;
+    const bool by_event = step_ev_of_[ev] == upto;
+    cudaStream_t cs = by_event ? copy_stream_ : stream_;
+    if (by_event) KNP_CUDA(cudaStreamWaitEvent(copy_stream_, step_ev_[ev], 0));
+    size_t need = 0;
+    for (auto &q : pops_)
+        if (q->record && q->rec_bits) need = std::max<size_t>(need, static_cast<size_t>(steps) * q->rec_words);
+    if (need > rec_host_words_)
     {
-        size_t need = 0;
+        KNP_CUDA(cudaStreamSynchronize(copy_stream_));
+        if (rec_host_) KNP_CUDA(cudaFreeHost(rec_host_));
+        rec_host_ = nullptr;
+        size_t cap = 0;
         for (auto &q : pops_)
-            if (q->record && q->rec_bits) need = std::max<size_t>(need, static_cast<size_t>(steps) * q->rec_words);
-        if (need > rec_host_words_)
+            if (q->rec_bits) cap = std::max<size_t>(cap, static_cast<size_t>(q->rec_slots) * q->rec_words);
+        KNP_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&rec_host_), cap * 4, cudaHostAllocDefault));
+        rec_host_words_ = cap;
+    }
+    for (auto &q : pops_)
+    {
+        if (!q->record || !q->rec_bits) continue;
+        // The steps occupy ring slots drained_to_ % slots ... (upto - 1) % slots: one or two spans.
+        const uint64_t first = drained_to_ % q->rec_slots;
+        const uint64_t span1 = std::min<uint64_t>(steps, q->rec_slots - first);
+        const size_t W = q->rec_words;
+        KNP_CUDA(cudaMemcpyAsync(rec_host_, q->rec_bits + first * W, span1 * W * 4, cudaMemcpyDeviceToHost, cs));
+        if (span1 < steps)
+            KNP_CUDA(cudaMemcpyAsync(rec_host_ + span1 * W, q->rec_bits, (steps - span1) * W * 4,
+                                     cudaMemcpyDeviceToHost, cs));
+        KNP_CUDA(cudaStreamSynchronize(cs));
+        for (uint64_t k = 0; k < steps; ++k)
         {
-            KNP_CUDA(cudaStreamSynchronize(stream_));
-            if (rec_host_) KNP_CUDA(cudaFreeHost(rec_host_));
-            rec_host_ = nullptr;
-            size_t cap = 0;
-            for (auto &q : pops_)
-                if (q->rec_bits) cap = std::max<size_t>(cap, static_cast<size_t>(q->rec_slots) * q->rec_words);
-            KNP_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&rec_host_), cap * 4, cudaHostAllocDefault));
-            rec_host_words_ = cap;
+            const uint64_t step = drained_to_ + k;
+            if (step < q->record_from) continue;
+            const uint32_t *bits = rec_host_ + k * W;
+            RecordedStep &r = q->recorded[step];
+            r.bits.assign(bits, bits + W);
+            r.count = 0;
+            for (size_t w = 0; w < W; ++w) r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
         }
-        for (auto &q : pops_)
+    }
+    drained_to_ = upto;
+    // Device error flags as of the drained steps (read on the same stream as the bitmaps).
+    KNP_CUDA(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, cs));
+    KNP_CUDA(cudaStreamSynchronize(cs));
+    if (ctl_host_->error)
+        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(ctl_host_->error) +
+                                                 (ctl_host_->error & kErrLogOverflow ? " (spike recording overflow)" : ""));
+}
+
+namespace
+{
+// Per byte value: its set bits' positions (padded to 8) and their number, for the expansion below.
+struct ByteBits
+{
+    uint8_t pos[256][8];
+    uint8_t cnt[256];
+    ByteBits()
+    {
+        for (int b = 0; b < 256; ++b)
         {
-            if (!q->record || !q->rec_bits) continue;
-            // The steps occupy ring slots drained_to_ % slots ... (step_ - 1) % slots: one or two spans.
-            const uint64_t first = drained_to_ % q->rec_slots;
-            const uint64_t span1 = std::min<uint64_t>(steps, q->rec_slots - first);
-            const size_t W = q->rec_words;
-            KNP_CUDA(cudaMemcpyAsync(rec_host_, q->rec_bits + first * W, span1 * W * 4, cudaMemcpyDeviceToHost,
-                                     stream_));
-            if (span1 < steps)
-                KNP_CUDA(cudaMemcpyAsync(rec_host_ + span1 * W, q->rec_bits, (steps - span1) * W * 4,
-                                         cudaMemcpyDeviceToHost, stream_));
-            KNP_CUDA(cudaStreamSynchronize(stream_));
-            for (uint64_t k = 0; k < steps; ++k)
+            cnt[b] = 0;
+            for (int i = 0; i < 8; ++i) pos[b][i] = 0;
+            for (int i = 0; i < 8; ++i)
+                if (b >> i & 1) pos[b][cnt[b]++] = static_cast<uint8_t>(i);
+        }
+    }
+};
+const ByteBits kByteBits;
+
+// Ascending indexes of the set bits of `bits` (W words) into out[0, cap); returns how many were
+// written. Full words are written as runs, other words a byte at a time from kByteBits.
+uint32_t expand_bits(const uint32_t *bits, size_t W, uint32_t cap, uint32_t *out)
+{
+    uint32_t k = 0;
+    for (size_t w = 0; w < W; ++w)
+    {
+        const uint32_t x = bits[w];
+        if (!x) continue;
+        const uint32_t base = static_cast<uint32_t>(w * 32);
+        if (x == 0xFFFFFFFFu && k + 32 <= cap)
+        {
+            for (uint32_t i = 0; i < 32; ++i) out[k + i] = base + i;
+            k += 32;
+            continue;
+        }
+        for (uint32_t j = 0; j < 4; ++j)
+        {
+            const uint32_t byte = x >> (8 * j) & 0xFFu;
+            if (!byte) continue;
+            const uint32_t c = kByteBits.cnt[byte];
+            if (k + 8 <= cap)
             {
-                const uint64_t step = drained_to_ + k;
-                if (step < q->record_from) continue;
-                const uint32_t *bits = rec_host_ + k * W;
-                RecordedStep &r = q->recorded[step];
-                r.bits.assign(bits, bits + W);
-                r.count = 0;
-                for (size_t w = 0; w < W; ++w) r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
+                for (uint32_t i = 0; i < 8; ++i) out[k + i] = base + 8 * j + kByteBits.pos[byte][i];
+                k += c;
+            }
+            else
+            {
+                for (uint32_t i = 0; i < c && k < cap; ++i) out[k++] = base + 8 * j + kByteBits.pos[byte][i];
             }
         }
     }
-    drained_to_ = step_;
-    check_device_error();
+    return k;
 }
+}  // namespace
 
 void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n)
 {
@@ -1253,15 +1335,13 @@ void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t 
     if (!q) throw Error(KNP_GB300_E_INVALID, "unknown population");
     if (!q->record) throw Error(KNP_GB300_E_STATE, "spike recording is not enabled for this population");
     if (step >= step_) throw Error(KNP_GB300_E_INVALID, "step has not been run yet");
-    if (step >= drained_to_) drain_recordings();
+    if (step >= drained_to_) drain_recordings(step + 1);
     auto it = q->recorded.find(step);
     if (it == q->recorded.end()) throw Error(KNP_GB300_E_INVALID, "spikes of this step were not recorded or were discarded");
     // Ascending indexes straight from the step's bitmap into the caller's buffer.
     const RecordedStep &r = it->second;
     *n = r.count;
-    uint32_t k = 0;
-    for (size_t w = 0; w < r.bits.size() && k < cap; ++w)
-        for (uint32_t x = r.bits[w]; x && k < cap; x &= x - 1) out[k++] = static_cast<uint32_t>(w * 32 + __builtin_ctz(x));
+    expand_bits(r.bits.data(), r.bits.size(), cap, out);
 }
 
 void Backend::discard_spikes(uint64_t before)

@@ -227,7 +227,8 @@ private:
     void enqueue_step();
     void capture_graphs();
     void stage_host_inputs();
-    void drain_recordings();
+    void drain_recordings() { drain_recordings(step_); }
+    void drain_recordings(uint64_t upto);
     void check_device_error();
     void alloc_recording(PopulationSlot &p);
     uint64_t steps_before_drain() const;
@@ -260,6 +261,14 @@ private:
     size_t pinned_bytes_ = 0;
     cudaEvent_t pinned_free_ = nullptr;
     bool any_recording_ = false;
+    // Completion events of recent steps (while spikes are recorded), so that a step's bitmaps can be
+    // copied to the host on copy_stream_ while later steps still run on stream_.
+    static constexpr uint64_t kStepEvents = 16;
+    cudaEvent_t step_ev_[kStepEvents] = {};
+    uint64_t step_ev_of_[kStepEvents] = {};  // the step each event was last recorded after, plus one
+    cudaStream_t copy_stream_ = nullptr;
+    Control *ctl_host_ = nullptr;  // pinned copy of the control block read after a drain
+    void record_step_event(uint64_t last_step);
 };
 
 }  // namespace knp_gb300

@@ -94,6 +94,40 @@ def test_large_sparse_reduced_scale():
     assert b.counters()[0] == oo.events
 
 
+def test_pipelined_spike_reads_and_caps():
+    """A step's spikes read while the next step already runs (its input sent first), into a reused
+    buffer, equal the oracle's; a read capped below the spike count returns its ascending prefix
+    and the full count."""
+    from oracle import oracle as orc
+
+    B = _gpu()
+    net, scheds = N.large_sparse_network(seed=3, n=10_000, fan_in=1000, steps=50)
+    steps = 50
+    o, _ = orc.run(net, scheds, steps)
+    pop = net.populations[0].uid
+    b = B.GB300Backend(0)
+    b.load_network(net)
+    b._init()
+    buf = np.empty(10_000, np.uint32)
+    for k in range(steps + 1):
+        if k < steps:
+            for sc in scheds:
+                idx = sc.at(k)
+                if idx.size:
+                    b.send_spikes(sc.sender, idx, k)
+            b.step(1)
+        if k > 0:
+            t = k - 1
+            exp = o[pop][t]
+            got = b.spikes(pop, t, out=buf)
+            assert np.array_equal(got, exp), f"step {t}"
+            if exp.size > 3:
+                capped = np.full(3, 0xFFFFFFFF, np.uint32)
+                cnt = b.spikes_capped(pop, t, capped)
+                assert cnt == exp.size and np.array_equal(capped, exp[:3])
+    b.close()
+
+
 @pytest.mark.parametrize("fraction", [0.0, 0.05, 0.3, -1.0])
 def test_gather_direction_bit_exact(fraction):
     """Steps delivered by the gather kernel (spike share >= fraction; 0 = every step with a spike,
