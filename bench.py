@@ -285,6 +285,40 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
     }
 
 
+def stdp_measure(device: int):
+    """STDP learning config (200 samples x 100 steps: 784 rate-coded inputs -> 800 resource-STDP
+    BLIFAT through all-to-all additive STDP, all-to-all lateral inhibition), input schedule resident
+    on the device, all 20,000 steps timed with CUDA events. The final plastic weights are compared
+    (CRC32) with the fixture the reference-header oracle wrote for the same config."""
+    import zlib
+
+    from knp_gb300 import backend as B
+    from knp_gb300 import network as Nw
+
+    steps = 20_000
+    net, scheds = Nw.stdp_network(seed=3, samples=200, steps_per_sample=100)
+    b = B.GB300Backend(device)
+    b.load_network(net, record=[])
+    b._init()
+    for sc in scheds:
+        b.load_spike_schedule(sc)
+    ms = b.step_timed(steps)
+    events, spikes, updates = b.counters()
+    w = b.read_weights(net.projections[0].uid)
+    b.close()
+    crc = zlib.crc32(w.tobytes())
+    fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "stdp_full.json")
+    with open(fixture) as f:
+        expect = json.load(f)
+    return {
+        "workload": "stdp: 784 -> 800 additive STDP (tau 20) + 800 x 800 lateral inhibition, 200 samples x 100 steps",
+        "value": events / (ms / 1e3), "unit": UNIT, "ms_total": ms, "us_per_step": ms / steps * 1e3,
+        "events": int(events), "spikes": int(spikes), "neuron_updates_per_s": updates / (ms / 1e3),
+        "weights_crc32": crc, "weights_match_reference_oracle": bool(crc == expect["weights_crc"]),
+        "events_match_reference_oracle": bool(int(events) == expect["events"]),
+    }
+
+
 def bptt_measure(device: int, iters: int = 10, warmup: int = 3):
     """Surrogate-gradient BPTT training step (LIF 784-512-512-10, batch 128, T 32, decay 0.9,
     threshold 1, fast-sigmoid slope 25, membrane checkpoint every 8 steps): forward + backward +
@@ -349,9 +383,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--profile-steps", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the batched dense and BPTT measurements")
-    ap.add_argument("--form", default="all", choices=["all", "batched", "bptt"],
-                    help="measure only the batched dense form or only the BPTT step (profiling runs)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched dense, BPTT and STDP measurements")
+    ap.add_argument("--form", default="all", choices=["all", "batched", "bptt", "stdp"],
+                    help="measure one form alone: the batched dense form, the BPTT step or the STDP config (profiling runs)")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     ap.add_argument("--pull-threshold", type=float, default=0.1,
@@ -363,7 +397,7 @@ def main():
     if args.form != "all":
         # One form alone (profiling runs): prints that form's measurement as one JSON line.
         local = int(os.environ.get("LOCAL_RANK", "0"))
-        out = batched_dense_measure(local) if args.form == "batched" else bptt_measure(local)
+        out = {"batched": batched_dense_measure, "bptt": bptt_measure, "stdp": stdp_measure}[args.form](local)
         print(json.dumps({"form": args.form, **out}))
         return
 
@@ -479,10 +513,11 @@ def main():
         cpu = cpu_baseline_sample()
     b.close()
 
-    batched = bp = None
+    batched = bp = stdp = None
     if rank == 0 and not args.no_forms:
         batched = batched_dense_measure(local)
         bp = bptt_measure(local)
+        stdp = stdp_measure(local)
 
     if rank == 0:
         line = {
@@ -508,6 +543,7 @@ def main():
             "build_s": t_build,
             "batched_dense": batched,
             "bptt": bp,
+            "stdp": stdp,
         }
         print(json.dumps(line))
     if dist is not None:
