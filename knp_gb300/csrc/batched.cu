@@ -184,11 +184,12 @@ constexpr uint32_t kMaxHalfChunks = 8;           // chunks of a K half (bounded 
 constexpr uint32_t kRing = 8;                    // bitmap steps kept per layer
 constexpr uint32_t kXchBytes = kBM * kBN * 4;    // one exchange buffer: [kBM][kBN] FP32 partial sums
 constexpr uint32_t kPollLimit = 1u << 22;        // polls of a cross-CTA counter before giving up
-constexpr int kExpandWarps = 4, kEpilogueWarps = 4;  // warps 0-3 expand, 4-7 epilogue, 8 issues
+constexpr int kExpandWarps = 4, kEpilogueWarps = 8;  // warps 0-3 expand, 4-11 epilogue, 12 issues
 constexpr int kIssuerWarp = kExpandWarps + kEpilogueWarps;
 constexpr int kExpandThreads = 32 * kExpandWarps, kEpilogueThreads = 32 * kEpilogueWarps;
 constexpr int kBatchThreads = kExpandThreads + kEpilogueThreads + 32;
-constexpr int kStateWords = 3 * kBN;  // V, refractory counter, spike count of an epilogue thread's neurons
+constexpr int kEN = 16;                  // neurons per epilogue thread (two threads per sample row)
+constexpr int kStateWords = 3 * kEN;  // V, refractory counter, spike count of an epilogue thread's neurons
 constexpr uint32_t kCntBytes = kBM * kBN * 4;  // last layer's spike counts of a tile, [kBN][kBM] int
 constexpr size_t kInputSlotBudget = size_t(256) << 20;  // bytes of layer 0's slots per segment
 
@@ -326,11 +327,10 @@ __device__ __forceinline__ void release_add(unsigned int *counter)
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
 }
 
-// Roles of the 9 warps: warps 0-3 expand the input bitmaps into the operand ring (one sample row
-// per thread), warps 4-7 run the epilogue (one sample row and the CTA's 32 neurons per thread; warp
-// 4 + w reads tensor-memory lanes 32 w .. 32 w + 31), lane 0 of warp 8 issues the MMAs. Two
-// accumulators in tensor memory let the MMAs of step s + 1 run while the epilogue of step s
-// exchanges partial sums and updates the neurons.
+// Roles of the 13 warps: warps 0-3 expand the input bitmaps into the operand ring (one sample row
+// per thread), warps 4-11 run the epilogue (one sample row and 16 of the CTA's 32 neurons per
+// thread), lane 0 of warp 12 issues the MMAs. Two accumulators in tensor memory let the MMAs of
+// step s + 1 run while the epilogue of step s exchanges partial sums and updates the neurons.
 template <int kStages>
 __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNet net, uint32_t t0, uint32_t t1)
 {
@@ -343,6 +343,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     __shared__ __align__(8) uint64_t xfull[2];        // the partner's partial sums of a step have landed
     __shared__ unsigned long long s_events;
     __shared__ int s_fail;  // some role gave up on a wait (each group reads it through one thread)
+    __shared__ uint32_t s_half[2][2][kBM];  // [step parity][neuron half][row]: epilogue spike masks
     const uint32_t item = blockIdx.x;
     const int layer = net.item_layer[item];  // 1..L
     const uint32_t m_tile = net.item_m[item];
@@ -472,19 +473,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     }
     else if (warp < kExpandWarps + kEpilogueWarps)
     {
-        // Epilogue: thread (warp 4 + w, lane) owns sample row er = 32 w + lane of the tile and the
-        // CTA's 32 neurons, keeping their LIF state in registers.
-        const uint32_t et = threadIdx.x - kExpandThreads;
-        const uint32_t er = et, erow = m0 + er;
+        // Epilogue: thread (warp 4 + w, lane) owns sample row er = 32 (w % 4) + lane of the tile and
+        // the CTA's neurons cb .. cb + 15 (cb = 16 (w / 4)), keeping their LIF state in registers;
+        // warp 4 + w reads tensor-memory lanes 32 (w % 4) .. + 31.
+        const uint32_t et = threadIdx.x - kExpandThreads, ew = et >> 5;
+        const uint32_t er = 32u * (ew & 3u) + lane, erow = m0 + er;
+        const uint32_t cb = kEN * (ew >> 2);
         const uint32_t lane_base = (32u * (warp & 3)) << 16;
-        float V[kBN];
-        uint32_t RC[kBN];
+        float V[kEN];
+        uint32_t RC[kEN];
         uint32_t *saved = net.state + (static_cast<size_t>(item) * kEpilogueThreads + et) * kStateWords;
 #pragma unroll
-        for (int i = 0; i < kBN; ++i)
+        for (int i = 0; i < kEN; ++i)
         {
             V[i] = t0 ? __uint_as_float(saved[i]) : 0.f;
-            RC[i] = t0 ? saved[kBN + i] : 0u;
+            RC[i] = t0 ? saved[kEN + i] : 0u;
         }
         const int li = layer - 1;
         const float leak = net.leak[li], thr = net.thr[li], rst = net.reset[li];
@@ -502,21 +505,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const unsigned int *consumed_out = producer ? net.consumed + ctr_out : nullptr;
         const uint32_t need_out = producer ? net.n_cta[layer + 1] : 0u;
         // Last layer: spike counts in shared memory, neuron-major so that a warp's 32 rows hit 32 banks.
-        int *cnt = layer == net.n_layers ? reinterpret_cast<int *>(sX + 2 * kXchBytes) + er : nullptr;
+        int *cnt = layer == net.n_layers ? reinterpret_cast<int *>(sX + 2 * kXchBytes) + cb * kBM + er : nullptr;
         if (cnt)
 #pragma unroll
-            for (int i = 0; i < kBN; ++i) cnt[i * kBM] = t0 ? static_cast<int>(saved[2 * kBN + i]) : 0;
+            for (int i = 0; i < kEN; ++i) cnt[i * kBM] = t0 ? static_cast<int>(saved[2 * kEN + i]) : 0;
         const uint32_t peer = tc::cluster_rank() ^ 1u;
-        auto partial = [&](uint32_t col, float *v)
-        {
-            if (n_chunks == 0)
-            {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
-                return;
-            }
-            tc::tmem_ld16(tmem + lane_base + col, v);
-        };
+        // Neurons at or past this sample's size do not exist (never updated, never spike).
+        const uint32_t n_here = my_n > n0 + cb ? my_n - n0 - cb : 0u;
+        const uint32_t exists = n_here >= 16u ? 0xFFFFu : (1u << n_here) - 1u;
         uint32_t s = 0;
         for (uint32_t t = t0; t < t1; ++t)
         {
@@ -538,38 +534,39 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (et == 0) mbar_arrive_expect_tx(&xfull[a], kXchBytes);
             const uint32_t row_peer = tc::mapa(tc::smem_u32(sX), peer) + a * kXchBytes + er * (kBN * 4u);
             const uint32_t xfull_peer = tc::mapa(tc::smem_u32(&xfull[a]), peer);
-            float acc[kBN];
-            partial(a * kPairN + kBN * (1u - kh), acc);
-            partial(a * kPairN + kBN * (1u - kh) + 16u, acc + 16);
+            float acc[kEN];
+            if (n_chunks)
+                tc::tmem_ld16(tmem + lane_base + a * kPairN + kBN * (1u - kh) + cb, acc);
+            else
 #pragma unroll
-            for (uint32_t q = 0; q < kBN / 4; ++q)
-                tc::st_async_v4(row_peer + ((q ^ (er & 7u)) << 4), acc[4 * q], acc[4 * q + 1], acc[4 * q + 2],
-                                acc[4 * q + 3], xfull_peer);
-            partial(a * kPairN + kBN * kh, acc);
-            partial(a * kPairN + kBN * kh + 16u, acc + 16);
+                for (int i = 0; i < kEN; ++i) acc[i] = 0.0f;
+#pragma unroll
+            for (uint32_t q = 0; q < kEN / 4; ++q)
+                tc::st_async_v4(row_peer + ((((cb >> 2) + q) ^ (er & 7u)) << 4), acc[4 * q], acc[4 * q + 1],
+                                acc[4 * q + 2], acc[4 * q + 3], xfull_peer);
+            if (n_chunks)
+                tc::tmem_ld16(tmem + lane_base + a * kPairN + kBN * kh + cb, acc);
             tc::fence_before_sync();
             tc::mbar_arrive(&acc_empty[a]);
             ok = tc::mbar_wait_cluster(&xfull[a], ph, kWaitLimit) && ok;
-            uint32_t mask = 0;
             const uint8_t *row_own = sX + a * kXchBytes + er * (kBN * 4u);
 #pragma unroll
-            for (uint32_t q = 0; q < kBN / 4; ++q)
+            for (uint32_t q = 0; q < kEN / 4; ++q)
             {
-                const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((q ^ (er & 7u)) << 4));
+                const float4 p4 = *reinterpret_cast<const float4 *>(row_own + ((((cb >> 2) + q) ^ (er & 7u)) << 4));
                 const float pv[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
                     acc[4 * q + e] = kh ? __fadd_rn(pv[e], acc[4 * q + e]) : __fadd_rn(acc[4 * q + e], pv[e]);
             }
-            // Neurons at or past this sample's size do not exist (never updated, never spike).
-            const uint32_t n_here = (ok && erow < b_act && my_n > n0) ? my_n - n0 : 0u;
-            const uint32_t exists = n_here >= 32u ? 0xFFFFFFFFu : (1u << n_here) - 1u;
+            const uint32_t live = (ok && erow < b_act) ? exists : 0u;
+            uint32_t mask = 0;  // this thread's spikes, bit i = neuron cb + i
 #pragma unroll
-            for (int i = 0; i < kBN; ++i)
+            for (int i = 0; i < kEN; ++i)
             {
                 // lif_impl.h:33-86: leak and input only outside the refractory period; strict '>';
                 // reset to a value. Branch-free: the lanes are different samples.
-                const bool here = (exists >> i) & 1u;
+                const bool here = (live >> i) & 1u;
                 const bool free_ = RC[i] == 0u;
                 const float v = __fadd_rn(__fmul_rn(V[i], leak), acc[i]);
                 const bool spike = here && free_ && v > thr;
@@ -579,6 +576,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             }
             if (cnt)
                 for (uint32_t m = mask; m; m &= m - 1u) ++cnt[(__ffs(m) - 1) * kBM];
+            s_half[a][ew >> 2][er] = mask;
             const bool room =
                 !check_room ||
                 reached(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1), room_seen);
@@ -590,14 +588,16 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             }
             ++s;
             my_events += static_cast<unsigned long long>(__popc(mask)) * my_fan_out;
-            if ((n0 >> 5) < wn)  // the second half of a tile may lie past N
+            // The row's word (both halves) is written by the thread of the first half.
+            if (cb == 0 && (n0 >> 5) < wn)  // the second half of a tile may lie past N
             {
+                const uint32_t word = s_half[a][0][er] | (s_half[a][1][er] << kEN);
                 if (producer)
                     out_bits[((static_cast<size_t>((t + 1) % kRing) * m_tiles + m_tile) * kBM + er) * wp_out +
-                             (n0 >> 5)] = mask;
+                             (n0 >> 5)] = word;
                 if (net.record && erow < b_act)
                     net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(e_smp) * wn + (n0 >> 5)] =
-                        mask;
+                        word;
             }
             if (producer)
             {
@@ -608,18 +608,18 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         if (t1 < net.t_max)
         {
 #pragma unroll
-            for (int i = 0; i < kBN; ++i)
+            for (int i = 0; i < kEN; ++i)
             {
                 saved[i] = __float_as_uint(V[i]);
-                saved[kBN + i] = RC[i];
-                if (cnt) saved[2 * kBN + i] = static_cast<uint32_t>(cnt[i * kBM]);
+                saved[kEN + i] = RC[i];
+                if (cnt) saved[2 * kEN + i] = static_cast<uint32_t>(cnt[i * kBM]);
             }
         }
         else if (cnt && erow < net.batch)
         {
             // Output spike counts of the last layer: each (sample, neuron) is owned by one thread.
-            for (int i = 0; i < kBN; ++i)
-                if (n0 + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + i] = cnt[i * kBM];
+            for (int i = 0; i < kEN; ++i)
+                if (n0 + cb + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + cb + i] = cnt[i * kBM];
         }
     }
     else if (lane == 0)
@@ -737,7 +737,7 @@ bool variant_fits(const BatchedPlan &p, int stages)
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     const size_t smem = smem_bytes(p, stages);
-    if (smem + 2048 > static_cast<size_t>(smem_max)) return false;  // 2 KB: the kernel's static shared memory
+    if (smem + 4096 > static_cast<size_t>(smem_max)) return false;  // 4 KB: the kernel's static shared memory
     const void *k = kernel_for(stages);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess)
         return false;
