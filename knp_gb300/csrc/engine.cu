@@ -1260,7 +1260,12 @@ void Backend::drain_recordings(uint64_t upto)
             RecordedStep &r = q->recorded[step];
             r.bits.assign(bits, bits + W);
             r.count = 0;
-            for (size_t w = 0; w < W; ++w) r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
+            r.block_prefix.resize((W + kExpandBlockWords - 1) / kExpandBlockWords);
+            for (size_t w = 0; w < W; ++w)
+            {
+                if (w % kExpandBlockWords == 0) r.block_prefix[w / kExpandBlockWords] = r.count;
+                r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
+            }
         }
     }
     drained_to_ = upto;
@@ -1292,17 +1297,19 @@ struct ByteBits
 };
 const ByteBits kByteBits;
 
-// Ascending indexes of the set bits of `bits` (W words) into out[0, cap); returns how many were
-// written. Full words are written as runs, other words a byte at a time from kByteBits.
-uint32_t expand_bits(const uint32_t *bits, size_t W, uint32_t cap, uint32_t *out)
+// Ascending indexes of the set bits of words [w0, w1) of `bits` into out[k0, end), end = min(the
+// range's last index + 1, cap): full words are written as runs, other words a byte at a time from
+// kByteBits (eight entries at once where they stay below `end`, so a range never writes into the
+// next range's part of `out`).
+void expand_bits(const uint32_t *bits, size_t w0, size_t w1, uint32_t k0, uint32_t end, uint32_t *out)
 {
-    uint32_t k = 0;
-    for (size_t w = 0; w < W; ++w)
+    uint32_t k = k0;
+    for (size_t w = w0; w < w1 && k < end; ++w)
     {
         const uint32_t x = bits[w];
         if (!x) continue;
         const uint32_t base = static_cast<uint32_t>(w * 32);
-        if (x == 0xFFFFFFFFu && k + 32 <= cap)
+        if (x == 0xFFFFFFFFu && k + 32 <= end)
         {
             for (uint32_t i = 0; i < 32; ++i) out[k + i] = base + i;
             k += 32;
@@ -1313,20 +1320,74 @@ uint32_t expand_bits(const uint32_t *bits, size_t W, uint32_t cap, uint32_t *out
             const uint32_t byte = x >> (8 * j) & 0xFFu;
             if (!byte) continue;
             const uint32_t c = kByteBits.cnt[byte];
-            if (k + 8 <= cap)
+            if (k + 8 <= end)
             {
                 for (uint32_t i = 0; i < 8; ++i) out[k + i] = base + 8 * j + kByteBits.pos[byte][i];
                 k += c;
             }
             else
             {
-                for (uint32_t i = 0; i < c && k < cap; ++i) out[k++] = base + 8 * j + kByteBits.pos[byte][i];
+                for (uint32_t i = 0; i < c && k < end; ++i) out[k++] = base + 8 * j + kByteBits.pos[byte][i];
             }
         }
     }
-    return k;
 }
 }  // namespace
+
+ExpandPool::ExpandPool(unsigned workers)
+{
+    for (unsigned i = 0; i < workers; ++i) threads_.emplace_back([this] { work(); });
+}
+
+ExpandPool::~ExpandPool()
+{
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        stop_ = true;
+    }
+    go_.notify_all();
+    for (auto &t : threads_) t.join();
+}
+
+void ExpandPool::drain_tasks()
+{
+    for (unsigned i = next_.fetch_add(1); i < n_tasks_; i = next_.fetch_add(1)) (*fn_)(i);
+}
+
+void ExpandPool::work()
+{
+    uint64_t seen = 0;
+    for (;;)
+    {
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            go_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+        }
+        drain_tasks();
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            if (--busy_ == 0) done_.notify_one();
+        }
+    }
+}
+
+void ExpandPool::run(unsigned n_tasks, const std::function<void(unsigned)> &fn)
+{
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        fn_ = &fn;
+        n_tasks_ = n_tasks;
+        next_.store(0);
+        busy_ = static_cast<unsigned>(threads_.size());
+        ++gen_;
+    }
+    go_.notify_all();
+    drain_tasks();
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [&] { return busy_ == 0; });
+}
 
 void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n)
 {
@@ -1341,7 +1402,30 @@ void Backend::read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t 
     // Ascending indexes straight from the step's bitmap into the caller's buffer.
     const RecordedStep &r = it->second;
     *n = r.count;
-    expand_bits(r.bits.data(), r.bits.size(), cap, out);
+    const size_t W = r.bits.size();
+    const unsigned blocks = static_cast<unsigned>(r.block_prefix.size());
+    // Large steps are expanded in parallel, one block of words per task (its offset is known).
+    if (r.count >= (1u << 16) && blocks > 1)
+    {
+        if (!expand_pool_)
+        {
+            const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
+            expand_pool_ = std::make_unique<ExpandPool>(std::min(7u, hc > 1 ? hc - 1 : 1u));
+        }
+        const std::function<void(unsigned)> task = [&](unsigned b)
+        {
+            const uint32_t k0 = r.block_prefix[b];
+            const uint32_t k1 = b + 1 < blocks ? r.block_prefix[b + 1] : r.count;
+            if (k0 >= cap) return;
+            const size_t w0 = static_cast<size_t>(b) * kExpandBlockWords;
+            expand_bits(r.bits.data(), w0, std::min(W, w0 + kExpandBlockWords), k0, std::min(k1, cap), out);
+        };
+        expand_pool_->run(blocks, task);
+    }
+    else
+    {
+        expand_bits(r.bits.data(), 0, W, 0, std::min(r.count, cap), out);
+    }
 }
 
 void Backend::discard_spikes(uint64_t before)

@@ -8,9 +8,14 @@
 // end-of-step kernel. Internal SpikeMessages / SynapticImpactMessages never leave the device.
 #pragma once
 
+#include <atomic>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <memory>
 #include <set>
 #include <stdexcept>
@@ -72,10 +77,39 @@ private:
     size_t bytes_ = 0;
 };
 
+// Words of a recorded bitmap per block of the parallel expansion.
+constexpr size_t kExpandBlockWords = 4096;
+
 struct RecordedStep
 {
     std::vector<uint32_t> bits;  // bit i of word i / 32: neuron i fired
     uint32_t count = 0;
+    std::vector<uint32_t> block_prefix;  // spikes before each block of kExpandBlockWords words
+};
+
+// Host worker threads for large bitmap expansions: run(n, fn) calls fn(0 .. n - 1) on the workers
+// and the calling thread and returns once all calls are done. One run at a time (the backend is not
+// reentrant).
+class ExpandPool
+{
+public:
+    explicit ExpandPool(unsigned workers);
+    ~ExpandPool();
+    void run(unsigned n_tasks, const std::function<void(unsigned)> &fn);
+    unsigned workers() const { return static_cast<unsigned>(threads_.size()); }
+
+private:
+    void work();
+    void drain_tasks();
+    std::vector<std::thread> threads_;
+    std::mutex m_;
+    std::condition_variable go_, done_;
+    const std::function<void(unsigned)> *fn_ = nullptr;
+    unsigned n_tasks_ = 0;
+    std::atomic<unsigned> next_{0};
+    unsigned busy_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
 };
 
 struct PopulationSlot
@@ -267,6 +301,7 @@ private:
     cudaEvent_t step_ev_[kStepEvents] = {};
     uint64_t step_ev_of_[kStepEvents] = {};  // the step each event was last recorded after, plus one
     cudaStream_t copy_stream_ = nullptr;
+    std::unique_ptr<ExpandPool> expand_pool_;  // created on the first large spike read
     Control *ctl_host_ = nullptr;  // pinned copy of the control block read after a drain
     void record_step_event(uint64_t last_step);
 };
