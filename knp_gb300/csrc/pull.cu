@@ -228,10 +228,44 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
             const size_t q = q0 + qi;
             const uint32_t len = g.slice_len[q];
             if (len == 0) continue;
-            const long long base = g.slice_ptr[q] + lane;
-            float sum = 0.0f;
-            for (uint32_t k0 = 0; k0 < len; k0 += kDepth)
+            // Entry k of this lane's list is at slice_ptr + 32 k + lane (a warp load reads 128
+            // consecutive bytes). Full rounds of kDepth entries run without bounds checks; an absent
+            // spike adds +0.0, which leaves the sum unchanged (the sum is never -0.0: it starts at
+            // +0.0 and a round-to-nearest sum is -0.0 only if both terms are).
+            const long long off = g.slice_ptr[q] + lane;
+            const uint32_t *pk = g.packed + off;
+            const uint16_t *ph = kForm == kHalf ? g.w16 + off : nullptr;
+            const float *pf = kForm == kFull ? g.w + off : nullptr;
+            auto value = [&](uint32_t pn, float wi) -> float
             {
+                if (kForm == kDict)
+                {
+                    wi = s_tab[pn >> 24];
+                    pn &= 0xFFFFFFu;
+                }
+                return ((bm[pn >> 5] >> (pn & 31)) & 1u) ? wi : 0.0f;
+            };
+            float sum = 0.0f;
+            uint32_t k0 = 0;
+            for (; k0 + kDepth <= len; k0 += kDepth)
+            {
+                const size_t o = static_cast<size_t>(k0) * kPullSlice;
+                uint32_t pre[kDepth];
+                float w[kDepth];
+#pragma unroll
+                for (int i = 0; i < kDepth; ++i)
+                {
+                    pre[i] = __ldcs(pk + o + i * kPullSlice);
+                    w[i] = 0.0f;
+                    if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(ph + o + i * kPullSlice)));
+                    if (kForm == kFull) w[i] = __ldcs(pf + o + i * kPullSlice);
+                }
+#pragma unroll
+                for (int i = 0; i < kDepth; ++i) sum = __fadd_rn(sum, value(pre[i], w[i]));
+            }
+            if (k0 < len)
+            {
+                const size_t o = static_cast<size_t>(k0) * kPullSlice;
                 uint32_t pre[kDepth];
                 float w[kDepth];
 #pragma unroll
@@ -241,24 +275,14 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
                     w[i] = 0.0f;
                     if (k0 + i < len)
                     {
-                        const long long e = base + static_cast<long long>(k0 + i) * kPullSlice;
-                        pre[i] = __ldcs(g.packed + e);
-                        if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(g.w16 + e)));
-                        if (kForm == kFull) w[i] = __ldcs(g.w + e);
+                        pre[i] = __ldcs(pk + o + i * kPullSlice);
+                        if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(ph + o + i * kPullSlice)));
+                        if (kForm == kFull) w[i] = __ldcs(pf + o + i * kPullSlice);
                     }
                 }
 #pragma unroll
                 for (int i = 0; i < kDepth; ++i)
-                {
-                    uint32_t pn = pre[i];
-                    float wi = w[i];
-                    if (kForm == kDict)
-                    {
-                        wi = s_tab[pn >> 24];
-                        pn &= 0xFFFFFFu;
-                    }
-                    if ((bm[pn >> 5] >> (pn & 31)) & 1u) sum = __fadd_rn(sum, wi);
-                }
+                    if (k0 + i < len) sum = __fadd_rn(sum, value(pre[i], w[i]));
             }
             // This lane's target: one owner per (delay, target), so a plain add.
             const uint32_t t = g.perm[q * kPullSlice + lane];
