@@ -20,6 +20,7 @@
 #include <cstdint>
 
 #include <cuda_runtime.h>
+#include <utility>
 
 namespace knp_gb300
 {
@@ -420,5 +421,34 @@ __host__ __device__ inline long long uniform_int(unsigned long long key, unsigne
     const unsigned long long span = static_cast<unsigned long long>(hi - lo + 1);
     return static_cast<long long>((r * span) >> 32) + lo;
 }
+
+// Programmatic dependent launch of a step's kernels: each kernel is launched while its predecessor
+// on the stream still runs, waits at its first instruction until the predecessor has completed and
+// its memory is visible (so every kernel still sees the whole previous kernel's results), then lets
+// its own successor start launching. Only the launch latency between kernels is overlapped.
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_begin()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args &&...args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+#endif
 
 }  // namespace knp_gb300

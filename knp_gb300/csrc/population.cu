@@ -272,6 +272,7 @@ __device__ __forceinline__ void resource_step(
 template <bool kFixed>
 __global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ctl)
 {
+    pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t q = blockIdx.x * kBlock + threadIdx.x;
     const uint32_t i0 = q * 4;
@@ -389,6 +390,7 @@ __global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ct
 
 __global__ void __launch_bounds__(kBlock) lif_kernel(LifDev p, Control *ctl)
 {
+    pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t q = blockIdx.x * kBlock + threadIdx.x;
     const uint32_t i0 = q * 4;
@@ -469,16 +471,16 @@ void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s)
     const uint32_t quads = (p.n + 3) / 4;
     const uint32_t grid = (quads + kBlock - 1) / kBlock;
     if (p.ring.fixed)
-        blifat_kernel<true><<<grid, kBlock, 0, s>>>(p, ctl);
+        launch_pdl(blifat_kernel<true>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
     else
-        blifat_kernel<false><<<grid, kBlock, 0, s>>>(p, ctl);
+        launch_pdl(blifat_kernel<false>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
 }
 
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s)
 {
     const uint32_t quads = (p.n + 3) / 4;
     const uint32_t grid = (quads + kBlock - 1) / kBlock;
-    lif_kernel<<<grid, kBlock, 0, s>>>(p, ctl);
+    launch_pdl(lif_kernel, dim3(grid), dim3(kBlock), 0, s, p, ctl);
 }
 
 void launch_apply_impacts(

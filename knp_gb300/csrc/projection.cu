@@ -79,6 +79,7 @@ __device__ __forceinline__ void deliver(
 template <bool kFixed, bool kUniformExc>
 __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Control *ctl)
 {
+    pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t slot_base = static_cast<uint32_t>(t % p.ring.slots);
     const int lane = threadIdx.x & 31;
@@ -191,16 +192,16 @@ void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStrea
     if (p.ring.fixed)
     {
         if (uexc)
-            projection_kernel<true, true><<<grid, 256, 0, s>>>(p, ctl);
+            launch_pdl(projection_kernel<true, true>, dim3(grid), dim3(256), 0, s, p, ctl);
         else
-            projection_kernel<true, false><<<grid, 256, 0, s>>>(p, ctl);
+            launch_pdl(projection_kernel<true, false>, dim3(grid), dim3(256), 0, s, p, ctl);
     }
     else
     {
         if (uexc)
-            projection_kernel<false, true><<<grid, 256, 0, s>>>(p, ctl);
+            launch_pdl(projection_kernel<false, true>, dim3(grid), dim3(256), 0, s, p, ctl);
         else
-            projection_kernel<false, false><<<grid, 256, 0, s>>>(p, ctl);
+            launch_pdl(projection_kernel<false, false>, dim3(grid), dim3(256), 0, s, p, ctl);
     }
 }
 

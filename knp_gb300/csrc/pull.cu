@@ -185,6 +185,7 @@ enum WeightForm
 template <int kForm>
 __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev p, Control *ctl)
 {
+    pdl_begin();
     extern __shared__ uint4 smem_u4[];
     __shared__ uint32_t s_next;  // next slice of the current delay to hand out
     __shared__ float s_tab[256];
@@ -334,11 +335,11 @@ void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t 
 {
     const size_t smem = gather_smem_bytes(p.pull, grid);
     if (p.pull.wtab)
-        gather_kernel<kDict><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+        launch_pdl(gather_kernel<kDict>, dim3(grid), dim3(kGatherThreads), smem, s, p, ctl);
     else if (p.pull.w16)
-        gather_kernel<kHalf><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+        launch_pdl(gather_kernel<kHalf>, dim3(grid), dim3(kGatherThreads), smem, s, p, ctl);
     else
-        gather_kernel<kFull><<<grid, kGatherThreads, smem, s>>>(p, ctl);
+        launch_pdl(gather_kernel<kFull>, dim3(grid), dim3(kGatherThreads), smem, s, p, ctl);
 }
 
 cudaError_t set_gather_smem(size_t bytes)

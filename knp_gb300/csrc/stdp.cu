@@ -24,6 +24,7 @@ namespace
 
 __global__ void stdp_append_kernel(StdpDev d, SpikeSource src, int both_lists, Control *ctl)
 {
+    pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t *idx;
     uint32_t cnt;
@@ -77,6 +78,7 @@ __global__ void stdp_append_kernel(StdpDev d, SpikeSource src, int both_lists, C
 // One warp per touched column.
 __global__ void stdp_modify_kernel(StdpDev d, Control *ctl)
 {
+    pdl_begin();
     const int lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -120,6 +122,7 @@ __global__ void stdp_modify_kernel(StdpDev d, Control *ctl)
 
 __global__ void step_end_kernel(StepEnd e, uint32_t n_spike_counts, Control *ctl)
 {
+    pdl_begin();
     __shared__ unsigned long long spikes;
     if (threadIdx.x == 0) spikes = 0;
     __syncthreads();
@@ -142,7 +145,7 @@ void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Contr
 {
     const int threads = 256;
     const int blocks = static_cast<int>((d.n_cols + threads - 1) / threads);
-    stdp_append_kernel<<<blocks > 0 ? blocks : 1, threads, 0, s>>>(d, src, both_lists, ctl);
+    launch_pdl(stdp_append_kernel, dim3(blocks > 0 ? blocks : 1), dim3(threads), 0, s, d, src, both_lists, ctl);
 }
 
 void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s)
@@ -150,14 +153,14 @@ void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s)
     const int threads = 256;
     int blocks = static_cast<int>((static_cast<uint64_t>(d.n_cols) * 32 + threads - 1) / threads);
     if (blocks > 1216) blocks = 1216;
-    stdp_modify_kernel<<<blocks > 0 ? blocks : 1, threads, 0, s>>>(d, ctl);
+    launch_pdl(stdp_modify_kernel, dim3(blocks > 0 ? blocks : 1), dim3(threads), 0, s, d, ctl);
 }
 
 // Zeroes this step's counters (adding the population spike counts to the spike total) and advances
 // the device step number.
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s)
 {
-    step_end_kernel<<<1, 256, 0, s>>>(e, e.n_spike_counts, ctl);
+    launch_pdl(step_end_kernel, dim3(1), dim3(256), 0, s, e, e.n_spike_counts, ctl);
 }
 
 }  // namespace knp_gb300
