@@ -141,8 +141,12 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
             return;
         }
     }
-    for (uint32_t j = warp; j < total; j += n_warps)
+    // Few spikes for many warps: each row is split over F warps (warp f of a row takes its 128-synapse
+    // rounds f, f + F, ...), so one long row does not serialise the step.
+    const uint32_t F = total ? max(1u, min(8u, n_warps / total)) : 1u;
+    for (uint32_t it = warp; it < total * F; it += n_warps)
     {
+        const uint32_t j = it / F, f = it - j * F;
         uint32_t jj = j;
         int k = 0;
         while (jj >= cnt[k])
@@ -154,9 +158,9 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
         if (pre >= p.n_rows) continue;  // no synapses from this neuron
         const int64_t a = p.row_ptr[pre];
         const int64_t b = p.row_ptr[pre + 1];
-        events += static_cast<unsigned long long>(b - a);
-        int64_t e = a + lane;
-        for (; e + 96 < b; e += 128)
+        if (f == 0) events += static_cast<unsigned long long>(b - a);
+        int64_t e = a + 128 * static_cast<int64_t>(f) + lane;
+        for (; e + 96 < b; e += 128 * static_cast<int64_t>(F))
         {
             int32_t c[4];
             float w[4];
@@ -173,6 +177,7 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
 #pragma unroll
             for (int u = 0; u < 4; ++u) deliver<kFixed, kUniformExc>(p, slot_base, e + 32 * u, c[u], w[u], d[u], ty[u]);
         }
+        // The last, partial round of this warp (the next one would start past b).
         for (; e < b; e += 32)
         {
             const int ty = kUniformExc ? 0 : (p.type ? __ldg(p.type + e) : p.uniform_type);
