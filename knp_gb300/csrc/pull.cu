@@ -175,6 +175,16 @@ __global__ void to_half_kernel(const float *w, uint64_t n, uint16_t *out)
         out[i] = __half_as_ushort(__float2half_rn(w[i]));
 }
 
+// Hint: bring [p, p + bytes) into L2 (16-byte aligned address and size; no completion to wait for).
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Slices ahead of the one a warp takes whose entries it asks L2 to fetch (about one round of the
+// block's warps): by the time a warp takes that slice its loads hit L2 instead of DRAM.
+constexpr uint32_t kPrefetchAhead = 32;
+
 enum WeightForm
 {
     kDict = 0,  // 8-bit dictionary index in the top bits of the packed entry
@@ -226,6 +236,18 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
             if (lane == 0) qi = atomicAdd(&s_next, 1u);
             qi = __shfl_sync(0xffffffffu, qi, 0);
             if (qi >= n_q) break;
+            if (lane == 0 && qi + kPrefetchAhead < n_q)
+            {
+                const size_t qa = q0 + qi + kPrefetchAhead;
+                const uint32_t la = g.slice_len[qa];
+                if (la)
+                {
+                    // Slices start on 32-entry boundaries; one slice is len x 32 entries.
+                    prefetch_l2(g.packed + g.slice_ptr[qa], la * kPullSlice * 4u);
+                    if (kForm == kHalf) prefetch_l2(g.w16 + g.slice_ptr[qa], la * kPullSlice * 2u);
+                    if (kForm == kFull) prefetch_l2(g.w + g.slice_ptr[qa], la * kPullSlice * 4u);
+                }
+            }
             const size_t q = q0 + qi;
             const uint32_t len = g.slice_len[q];
             if (len == 0) continue;
