@@ -235,7 +235,25 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
             uint32_t qi = 0;
             if (lane == 0) qi = atomicAdd(&s_next, 1u);
             qi = __shfl_sync(0xffffffffu, qi, 0);
-            if (qi >= n_q) break;
+            if (qi >= n_q)
+            {
+                // The first kPrefetchAhead warps to run out prefetch the first slices of the next
+                // delay (those no earlier slice's prefetch covered).
+                const uint32_t r = qi - n_q;
+                if (lane == 0 && r < kPrefetchAhead && r < n_q && d < g.max_delay && d < tn &&
+                    g.pulled[static_cast<uint32_t>((tn - d - 1) % g.hist_slots)])
+                {
+                    const size_t qa = (static_cast<size_t>(d) * g.n_windows + w0) * kPullSlicesPerWindow + r;
+                    const uint32_t la = g.slice_len[qa];
+                    if (la)
+                    {
+                        prefetch_l2(g.packed + g.slice_ptr[qa], la * kPullSlice * 4u);
+                        if (kForm == kHalf) prefetch_l2(g.w16 + g.slice_ptr[qa], la * kPullSlice * 2u);
+                        if (kForm == kFull) prefetch_l2(g.w + g.slice_ptr[qa], la * kPullSlice * 4u);
+                    }
+                }
+                break;
+            }
             if (lane == 0 && qi + kPrefetchAhead < n_q)
             {
                 const size_t qa = q0 + qi + kPrefetchAhead;
