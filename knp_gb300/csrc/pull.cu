@@ -181,9 +181,10 @@ __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Slices ahead of the one a warp takes whose entries it asks L2 to fetch (about one round of the
-// block's warps): by the time a warp takes that slice its loads hit L2 instead of DRAM.
-constexpr uint32_t kPrefetchAhead = 32;
+// Slices ahead of the one a warp takes whose entries it asks L2 to fetch: by the time a warp takes
+// that slice its loads hit L2 instead of DRAM (full-size step: 8 and 16 give 0.80 ms, 32 0.81 ms,
+// 64 0.84 ms).
+constexpr uint32_t kPrefetchAhead = 16;
 
 enum WeightForm
 {
