@@ -270,7 +270,7 @@ __device__ __forceinline__ void resource_step(
 }
 
 template <bool kFixed>
-__global__ void __launch_bounds__(kBlock) blifat_kernel(BlifatDev p, Control *ctl)
+__global__ void __launch_bounds__(kBlock, 3) blifat_kernel(BlifatDev p, Control *ctl)
 {
     pdl_begin();
     const unsigned long long t = ctl->step;
