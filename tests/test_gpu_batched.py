@@ -186,3 +186,29 @@ def test_batched_segments_give_identical_results():
         np.testing.assert_array_equal(c2, c1)
         for layer in r1:
             np.testing.assert_array_equal(r2[layer], r1[layer])
+
+
+def test_batched_full_config_identical_across_depths_and_repeats():
+    """The full dense config (256 samples, 784-1000-1000-10: several chunks per K half, two sample
+    tiles, layers running ahead of each other on the ring counters) gives bit-identical spike
+    records, counts and event totals at every operand-ring depth and on repeated runs; a counting
+    error in the inter-layer step protocol shows up here as run-to-run differences."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(seed=4)
+    ref = None
+    for stages in (2, 3, 4):
+        plan = BT.BatchedPlan(cfg, record=True, stages=stages)
+        try:
+            for _ in range(2):
+                ev, _ = plan.run()
+                got = (ev, plan.counts(), plan.record())
+                if ref is None:
+                    ref = got
+                    continue
+                assert got[0] == ref[0]
+                np.testing.assert_array_equal(got[1], ref[1])
+                for layer in ref[2]:
+                    np.testing.assert_array_equal(got[2][layer], ref[2][layer])
+        finally:
+            plan.close()
