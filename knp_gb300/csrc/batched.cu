@@ -419,27 +419,48 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint32_t x_lane = (32u * warp) << 16;
         uint32_t seq = 0;
         bool ok = true;
-        unsigned int ready_seen = 0;  // this step's counter, read during the previous step
+        unsigned int ready_seen = 0;  // the next step's counter, read early in this step
+        auto row_words = [&](uint32_t t) -> const uint4 *
+        {
+            const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
+            return reinterpret_cast<const uint4 *>(
+                net.bits[layer - 1] + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
+                static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords);
+        };
+        uint4 wv[kMaxHalfChunks];  // this step's words
+        uint4 wn[kMaxHalfChunks];  // the next step's words, when they could be loaded during this step
+        bool have_next = false;
         for (uint32_t t = t0; t < t1; ++t)
         {
             if (m0 >= net.act[t]) break;  // sample tiles finish in order: no steps left
             bool go = ok;
             if (threadIdx.x == 0)
                 go = go && !s_fail &&
-                     (!ready_in || t == 0 || reached(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1), ready_seen));
+                     (have_next || !ready_in || t == 0 ||
+                      reached(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1), ready_seen));
             if (!tc::named_sync_and(1, kExpandThreads, go))  // the group's decision is uniform
             {
                 s_fail = 1;
                 break;
             }
-            const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
-            const uint4 *rowp = reinterpret_cast<const uint4 *>(
-                net.bits[layer - 1] + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
-                static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords);
-            uint4 wv[kMaxHalfChunks];
+            if (have_next)
+            {
 #pragma unroll
-            for (uint32_t c = 0; c < kMaxHalfChunks; ++c) wv[c] = c < n_chunks ? __ldcg(rowp + c) : make_uint4(0, 0, 0, 0);
-            if (threadIdx.x == 0 && ready_in && t + 1 < t1) ready_seen = load_relaxed(ready_in + (t + 1) % kRing);
+                for (uint32_t c = 0; c < kMaxHalfChunks; ++c) wv[c] = wn[c];
+            }
+            else
+            {
+                const uint4 *rowp = row_words(t);
+#pragma unroll
+                for (uint32_t c = 0; c < kMaxHalfChunks; ++c)
+                    wv[c] = c < n_chunks ? __ldcg(rowp + c) : make_uint4(0, 0, 0, 0);
+            }
+            have_next = false;
+            const bool can_next = t + 1 < t1 && m0 < net.act[t + 1];  // uniform
+            if (threadIdx.x == 0 && ready_in && can_next) ready_seen = load_relaxed(ready_in + (t + 1) % kRing);
+            // After chunk `c_ask`, the next step's words are loaded (to be used next step) if layer - 1
+            // has already published that step, so their L2 round trip overlaps this step's chunks.
+            const uint32_t c_ask = n_chunks > 1 ? 1u : 0u;
             // One copy of the chunk body (kept small for the instruction cache); the loaded words
             // shift down by one chunk per iteration so that every register index stays static.
 #pragma unroll 1
@@ -454,19 +475,34 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
 #pragma unroll
                 for (uint32_t q = 0; q < 4; ++q)
                 {
-                    // Word q holds inputs 32 q .. 32 q + 31 of the chunk: 16 columns of two BF16 each.
+                    // Word q holds inputs 32 q .. 32 q + 31 of the chunk: 16 columns of two BF16 each,
+                    // bits (2 i, 2 i + 1) -> column i = 1.0 or 0 in its low and high halves.
                     uint32_t v[16];
 #pragma unroll
-                    for (uint32_t i = 0; i < 16; ++i)
-                    {
-                        const uint32_t two = w4[q] >> (2u * i);
-                        v[i] = ((two & 1u) ? 0x3F80u : 0u) | ((two & 2u) ? 0x3F800000u : 0u);
-                    }
+                    for (uint32_t i = 0; i < 16; ++i) v[i] = (((w4[q] >> (2u * i) & 3u) * 0x8001u) & 0x10001u) * 0x3F80u;
                     tc::tmem_st16(tmem + x_lane + kAccCols + b * kStageCols + 16u * q, v);
                 }
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
                 tc::mbar_arrive(&full[b]);
+                if (c == c_ask && can_next)
+                {
+                    bool nx = true;
+                    if (threadIdx.x == 0 && ready_in)
+                    {
+                        const unsigned int target = need_in * (t / kRing + 1);
+                        nx = static_cast<int>(ready_seen - target) >= 0;
+                        if (nx) fence_acquire();
+                    }
+                    have_next = tc::named_sync_and(1, kExpandThreads, nx);
+                    if (have_next)
+                    {
+                        const uint4 *rown = row_words(t + 1);
+#pragma unroll
+                        for (uint32_t c2 = 0; c2 < kMaxHalfChunks; ++c2)
+                            wn[c2] = c2 < n_chunks ? __ldcg(rown + c2) : make_uint4(0, 0, 0, 0);
+                    }
+                }
             }
             seq += n_chunks;
         }
