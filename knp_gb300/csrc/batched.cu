@@ -235,11 +235,32 @@ struct BatchedNet
     uint8_t item_k[kMaxItems];   // K half = rank in the cluster: items 2i and 2i + 1 are one tile
 };
 
-// Per (sample, input): the 53-bit threshold that the input draw is compared with.
+// Per (sample, input): the 53-bit threshold that the input draw is compared with, rate * 2^53
+// truncated, computed exactly from the FP32 rate's fields (no FP64 on the device): m * 2^(e - 97)
+// for a normal rate in (0, 1) with 24-bit significand m and biased exponent e; 0 for rates <= 0,
+// subnormal or NaN; 2^53 (every draw is below it) for rates >= 1.
 __global__ void rate_threshold_kernel(const float *rates, unsigned long long *thr, size_t n)
 {
     const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) thr[i] = static_cast<unsigned long long>(static_cast<double>(rates[i]) * 9007199254740992.0);
+    if (i >= n) return;
+    const uint32_t bits = __float_as_uint(rates[i]);
+    const uint32_t e = (bits >> 23) & 0xFFu;
+    unsigned long long v = 0;
+    if ((bits >> 31) == 0u && e != 0u && e != 0xFFu)
+    {
+        const unsigned long long m = (bits & 0x7FFFFFu) | 0x800000u;
+        if (e >= 127u)
+            v = 1ull << 53;
+        else if (e >= 97u)
+            v = m << (e - 97u);
+        else if (97u - e < 64u)
+            v = m >> (97u - e);
+    }
+    else if ((bits >> 31) == 0u && e == 0xFFu && (bits & 0x7FFFFFu) == 0u)
+    {
+        v = 1ull << 53;  // +infinity
+    }
+    thr[i] = v;
 }
 
 // Layer 0's slots of the segment [t0, t1): slot j = the input spikes drawn at step t0 + j - 1, one

@@ -72,7 +72,7 @@ __global__ void fan_in_gather_kernel(
         const uint64_t i = perm[e];
         col_out[e] = static_cast<int32_t>(i % n_post);
         const long long k = uniform_int(key_w, i, k_lo, k_hi);
-        w_out[e] = static_cast<float>(static_cast<double>(k) / 256.0);
+        w_out[e] = static_cast<float>(k) * (1.0f / 256.0f);  // k / 256, one rounding (exact for |k| < 2^24)
         delay_out[e] = static_cast<uint8_t>(uniform_int(key_d, i, d_lo, d_hi));
     }
 }

@@ -250,7 +250,7 @@ __device__ __forceinline__ void resource_step(
         else
         {
             const unsigned long long diff_u = t - r.first_isi_spike[i] - isi_max;
-            const float diff = static_cast<float>(static_cast<double>(diff_u));
+            const float diff = __ull2float_rn(diff_u);
             const float m = fmaxf(__fsub_rn(2.0f, __fdiv_rn(diff, static_cast<float>(isi_max))), -1.0f);
             st = __fadd_rn(st, __fmul_rn(__fmul_rn(c, dopa), m));
         }
