@@ -220,7 +220,7 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
     cfg = BT.dense_config(seed=4)
     # Prepared once (ring depth autotuned), each run one CUDA-graph launch.
     plan = BT.BatchedPlan(cfg, autotune=True, device=device)
-    stages, tuned = plan.info()
+    stages, ring, tuned = plan.info()
     for _ in range(warmup):
         plan.run()
     times, events = [], 0
@@ -281,7 +281,8 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
         "dtype": "bf16 x bf16 -> fp32", "l2": "flushed (256 MB write) before each timed run",
         "launch": "one CUDA graph per batch (state memsets, input thresholds, input spike bitmaps drawn ahead, "
                   "persistent kernel of CTA-pair clusters)",
-        "autotuned_ring_depth": stages, "autotune_ms": tuned,
+        "autotuned_ring_depth": stages, "autotuned_layer_ring_steps": ring,
+        "autotune_ms": {f"depth{d}_ring{r}": v for (d, r), v in tuned.items()},
     }
 
 

@@ -338,9 +338,10 @@ KNP_GB300_API int knp_gb300_batched_lif_run(
  *                 l (<= sizes[l]); inputs and neurons beyond it do not exist for that sample (never
  *                 spike, carry no events). NULL: every sample has the full sizes (uneven network
  *                 instances over shared weights, or inputs of uneven width).
- *   autotune      > 0: each operand ring depth that fits (2..4 chunks of 32 KB) is run twice at
- *                 creation and the fastest kept; < 0: depth -autotune; 0: the deepest that fits. The
- *                 depth does not change any result.
+ *   autotune      > 0: each operand ring depth that fits (2..4 chunks of 32 KB) with each layer
+ *                 ring length (4, 8, 16 steps) is run twice at creation and the fastest pair kept;
+ *                 < 0: depth -autotune (layer rings of 8); 0: the deepest that fits. Neither choice
+ *                 changes any result.
  *   segment_steps non-zero: at most this many steps per persistent launch (0: as many as a 256 MB
  *                 buffer of pre-drawn input spike bitmaps holds); segments do not change any result.
  * The device buffers (weights, rates, counts, record) must stay valid for the plan's life; their
@@ -361,8 +362,14 @@ KNP_GB300_API int knp_gb300_batched_plan_create(
 /** Runs the prepared batch once: *events (host) synaptic events, *ms device time of the graph launch. */
 KNP_GB300_API int knp_gb300_batched_plan_run(knp_gb300_batched_plan *plan, uint64_t *events, float *ms);
 
-/** The ring depth in use and, after autotuning, the time of each depth tried (tune_ms[3] for depths 2, 3, 4; 0 = not tried). */
-KNP_GB300_API int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, float *tune_ms);
+/**
+ * The operand ring depth and the layer ring length (steps a layer may hold; it runs at most that
+ * many minus 2 steps ahead of the next layer) in use, and, after autotuning, the time of each pair
+ * tried: tune_ms[9], index 3 * r + (depth - 2) for layer rings of 4, 8, 16 steps (r = 0, 1, 2) and
+ * depths 2, 3, 4; 0 = not tried.
+ */
+KNP_GB300_API int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, int *ring_steps,
+                                              float *tune_ms);
 
 KNP_GB300_API void knp_gb300_batched_plan_destroy(knp_gb300_batched_plan *plan);
 

@@ -84,7 +84,8 @@ def lib():
         "knp_gb300_batched_plan_create": ([c_int, p, p, p, p, p, p, u32, p, p, p, u64, p, p, c_int, u32, p,
                                            ctypes.POINTER(p)], c_int),
         "knp_gb300_batched_plan_run": ([p, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_float)], c_int),
-        "knp_gb300_batched_plan_info": ([p, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_float)], c_int),
+        "knp_gb300_batched_plan_info": ([p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_float)],
+                                        c_int),
         "knp_gb300_batched_plan_destroy": ([p], None),
         "knp_gb300_synchronize": ([p], c_int),
         "knp_gb300_stream": ([p, ctypes.POINTER(p)], c_int),

@@ -86,8 +86,8 @@ def uneven_config(seed: int = 8, batch: int = 40, sizes=(96, 128, 64, 10), t_lo:
 
 class BatchedPlan:
     """A batch prepared on the device (knp_gb300_batched_plan_create) and run as one CUDA-graph
-    launch per ``run()``; with ``autotune`` the operand ring depth is chosen by timing each depth,
-    ``stages`` fixes it (0: the deepest that fits)."""
+    launch per ``run()``; with ``autotune`` the operand ring depth and the layer ring length are
+    chosen by timing each pair, ``stages`` fixes the depth (0: the deepest that fits)."""
 
     def __init__(self, cfg: BatchedConfig, record: bool = False, autotune: bool = False, device: int = 0,
                  segment_steps: int = 0, stages: int = 0):
@@ -134,11 +134,14 @@ class BatchedPlan:
         return int(events.value), float(ms.value)
 
     def info(self):
-        """(ring depth in use, {depth: ms of the autotuning run})."""
+        """(operand ring depth, layer ring length, {(depth, ring length): ms of the autotuning run})."""
         st = ctypes.c_int(0)
-        t = (ctypes.c_float * 3)()
-        _capi.check(self._lib.knp_gb300_batched_plan_info(self._h, ctypes.byref(st), t))
-        return st.value, {d: float(t[d - 2]) for d in (2, 3, 4) if t[d - 2] > 0}
+        ring = ctypes.c_int(0)
+        t = (ctypes.c_float * 9)()
+        _capi.check(self._lib.knp_gb300_batched_plan_info(self._h, ctypes.byref(st), ctypes.byref(ring), t))
+        tuned = {(d, r): float(t[3 * ri + d - 2]) for ri, r in enumerate((4, 8, 16)) for d in (2, 3, 4)
+                 if t[3 * ri + d - 2] > 0}
+        return st.value, ring.value, tuned
 
     def counts(self) -> np.ndarray:
         return self._counts.cpu().numpy()

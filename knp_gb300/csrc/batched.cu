@@ -155,13 +155,13 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
 // 32 neurons, whose LIF state stays in registers.
 //
 // Spikes travel between layers as bitmaps (one 32-bit word per sample and 32 neurons) in a ring of
-// kRing steps per layer. A consumer expands its K half chunk by chunk into BF16 operand chunks in
+// R steps per layer (R tuned, at most kMaxRing). A consumer expands its K half chunk by chunk into BF16 operand chunks in
 // tensor memory (one sample row per lane) while the tensor cores multiply the previous chunk. There
 // is no grid-wide barrier: per (layer, sample tile, ring slot) counters record how
 // many times the layer's CTAs have written the slot (`ready`) and how many times consumer CTAs have
 // read it (`consumed`), so a layer starts step t as soon as every CTA of the layer below has
 // published step t - 1, and overwrites a slot only after every consumer has read it (a layer runs
-// at most kRing - 2 steps ahead of its consumers). Counting per slot matters: CTAs of one layer are
+// at most R - 2 steps ahead of its consumers). Counting per slot matters: CTAs of one layer are
 // not in lockstep, and a sum over all slots would let a fast CTA stand in for a slow one. Input spikes do not depend on the network, so
 // a separate kernel draws them ahead of the run (layer 0's slots hold every step of a segment; long
 // runs are cut into segments, the LIF state saved and restored between them). Samples are processed
@@ -181,7 +181,9 @@ constexpr size_t kMinDynSmem = size_t(120) << 10;  // keeps a second CTA off the
 static_assert(kAccCols + kMaxStages * kStageCols <= kTmemCols, "operand stages exceed tensor memory");
 constexpr uint32_t kChunkWords = kBK / 32;       // bitmap words per sample row and chunk
 constexpr uint32_t kMaxHalfChunks = 8;           // chunks of a K half (bounded by shared memory)
-constexpr uint32_t kRing = 8;                    // bitmap steps kept per layer
+constexpr uint32_t kMaxRing = 16;                // bitmap steps kept per layer at most (counter stride)
+constexpr uint32_t kRingChoices[3] = {4, 8, 16};   // ring lengths the autotuner tries
+constexpr uint32_t kDefaultRing = 8;
 constexpr uint32_t kXchBytes = kBM * kBN * 4;    // one exchange buffer: [kBM][kBN] FP32 partial sums
 constexpr uint32_t kPollLimit = 1u << 22;        // polls of a cross-CTA counter before giving up
 constexpr int kExpandWarps = 4, kEpilogueWarps = 8;  // warps 0-3 expand, 4-11 epilogue, 12 issues
@@ -216,11 +218,12 @@ struct BatchedNet
     uint32_t t_max;
     // bits[l]: spikes of layer l as layer l + 1's input, [slot][m tile][kBM][wpad[l]] words (bit j of
     // word w = neuron 32 w + j, words past words[l] zero). Layer 0: slot j of a segment starting at
-    // step t0 = input drawn at step t0 + j - 1 (nothing before step 0). Layers >= 1: kRing slots,
-    // slot (t + 1) % kRing written at step t.
+    // step t0 = input drawn at step t0 + j - 1 (nothing before step 0). Layers >= 1: ring slots,
+    // slot (t + 1) % ring written at step t.
     uint32_t *bits[kMaxLayers];
-    unsigned int *ready;     // [kMaxLayers + 1][m_tiles][kRing]: writes of layer l's slot by its CTAs
-    unsigned int *consumed;  // [kMaxLayers + 1][m_tiles][kRing]: reads of layer l's slot by layer l + 1's CTAs
+    uint32_t ring;           // steps kept per layer ring (3 .. kMaxRing)
+    unsigned int *ready;     // [kMaxLayers + 1][m_tiles][kMaxRing]: writes of layer l's slot by its CTAs
+    unsigned int *consumed;  // [kMaxLayers + 1][m_tiles][kMaxRing]: reads of layer l's slot by layer l + 1's CTAs
     uint32_t *state;         // [n_items][kEpilogueThreads][kStateWords]: LIF state between segments
     int *counts;             // [batch][size[L]] by sample
     uint32_t *record;        // [t_max][sum_l batch * words[l]] by sample, or null
@@ -423,8 +426,9 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     tc::fence_after_sync();
     const uint32_t tmem = tmem_slot;
     const uint32_t m_tiles = net.m_tiles;
-    const size_t ctr_in = (static_cast<size_t>(layer - 1) * m_tiles + m_tile) * kRing;
-    const size_t ctr_out = (static_cast<size_t>(layer) * m_tiles + m_tile) * kRing;
+    const uint32_t R = net.ring;
+    const size_t ctr_in = (static_cast<size_t>(layer - 1) * m_tiles + m_tile) * kMaxRing;
+    const size_t ctr_out = (static_cast<size_t>(layer) * m_tiles + m_tile) * kMaxRing;
     const bool producer = layer < net.n_layers;
     unsigned long long my_events = 0;
 
@@ -443,7 +447,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         unsigned int ready_seen = 0;  // the next step's counter, read early in this step
         auto row_words = [&](uint32_t t) -> const uint4 *
         {
-            const uint32_t slot = layer == 1 ? t - t0 : t % kRing;
+            const uint32_t slot = layer == 1 ? t - t0 : t % R;
             return reinterpret_cast<const uint4 *>(
                 net.bits[layer - 1] + (static_cast<size_t>(slot) * m_tiles + m_tile) * kBM * wp_in +
                 static_cast<size_t>(xr) * wp_in + c_lo * kChunkWords);
@@ -458,7 +462,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (threadIdx.x == 0)
                 go = go && !s_fail &&
                      (have_next || !ready_in || t == 0 ||
-                      reached(ready_in + t % kRing, need_in * ((t - 1) / kRing + 1), ready_seen));
+                      reached(ready_in + t % R, need_in * ((t - 1) / R + 1), ready_seen));
             if (!tc::named_sync_and(1, kExpandThreads, go))  // the group's decision is uniform
             {
                 s_fail = 1;
@@ -478,7 +482,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             }
             have_next = false;
             const bool can_next = t + 1 < t1 && m0 < net.act[t + 1];  // uniform
-            if (threadIdx.x == 0 && ready_in && can_next) ready_seen = load_relaxed(ready_in + (t + 1) % kRing);
+            if (threadIdx.x == 0 && ready_in && can_next) ready_seen = load_relaxed(ready_in + (t + 1) % R);
             // After chunk `c_ask`, the next step's words are loaded (to be used next step) if layer - 1
             // has already published that step, so their L2 round trip overlaps this step's chunks.
             const uint32_t c_ask = n_chunks > 1 ? 1u : 0u;
@@ -511,7 +515,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     bool nx = true;
                     if (threadIdx.x == 0 && ready_in)
                     {
-                        const unsigned int target = need_in * (t / kRing + 1);
+                        const unsigned int target = need_in * (t / R + 1);
                         nx = static_cast<int>(ready_seen - target) >= 0;
                         if (nx) fence_acquire();
                     }
@@ -575,11 +579,11 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         {
             const uint32_t b_act = net.act[t];
             if (m0 >= b_act) break;
-            // Ring slot (t + 1) % kRing was read at steps t + 1 - kRing, t + 1 - 2 kRing, ...: every
+            // Ring slot (t + 1) % R was read at steps t + 1 - R, t + 1 - 2 R, ...: every
             // consumer must have read it that many times before it is overwritten below (the count
             // is read now and checked after the update).
-            const bool check_room = et == 0 && producer && t + 1 >= kRing;
-            const unsigned int room_seen = check_room ? load_relaxed(consumed_out + (t + 1) % kRing) : 0u;
+            const bool check_room = et == 0 && producer && t + 1 >= R;
+            const unsigned int room_seen = check_room ? load_relaxed(consumed_out + (t + 1) % R) : 0u;
             const uint32_t a = s & 1u, ph = (s >> 1) & 1u;
             bool ok = tc::mbar_wait(&acc_full[a], ph, kWaitLimit);
             tc::fence_after_sync();
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             s_half[a][ew >> 2][er] = mask;
             const bool room =
                 !check_room ||
-                reached(consumed_out + (t + 1) % kRing, need_out * ((t + 1 - kRing) / kRing + 1), room_seen);
+                reached(consumed_out + (t + 1) % R, need_out * ((t + 1 - R) / R + 1), room_seen);
             const bool go = ok && room && (et != 0 || !s_fail);
             if (!tc::named_sync_and(2, kEpilogueThreads, go))  // the group's decision is uniform
             {
@@ -650,7 +654,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             {
                 const uint32_t word = s_half[a][0][er] | (s_half[a][1][er] << kEN);
                 if (producer)
-                    out_bits[((static_cast<size_t>((t + 1) % kRing) * m_tiles + m_tile) * kBM + er) * wp_out +
+                    out_bits[((static_cast<size_t>((t + 1) % R) * m_tiles + m_tile) * kBM + er) * wp_out +
                              (n0 >> 5)] = word;
                 if (net.record && erow < b_act)
                     net.record[t * net.rec_stride + net.rec_off[layer] + static_cast<size_t>(e_smp) * wn + (n0 >> 5)] =
@@ -659,7 +663,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (producer)
             {
                 tc::named_sync_and(2, kEpilogueThreads, true);
-                if (et == 0) release_add(ready_out + (t + 1) % kRing);
+                if (et == 0) release_add(ready_out + (t + 1) % R);
             }
         }
         if (t1 < net.t_max)
@@ -712,7 +716,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             }
             seq += n_chunks;
             tc::commit(&acc_full[a]);
-            if (consumed_in) release_add(consumed_in + t % kRing);
+            if (consumed_in) release_add(consumed_in + t % R);
             ++s;
         }
         // Let the MMAs still in flight finish (bounded) before the tensor memory is released.
@@ -753,7 +757,7 @@ struct BatchedPlan
     cudaGraphExec_t exec = nullptr;
     int stages = 0;
     bool cooperative = true;  // cluster launch with the cooperative attribute (cleared if refused)
-    float tune_ms[kMaxStages + 1] = {};
+    float tune_ms[3][kMaxStages + 1] = {};  // [ring choice][operand ring depth] of the autotuning runs
 
     ~BatchedPlan()
     {
@@ -1082,11 +1086,11 @@ int batched_plan_create(
     ok = ok && (net.bits[0] = static_cast<uint32_t *>(dalloc(p.seg_steps * slot_bytes))) != nullptr;
     for (int l = 1; l < n_layers && ok; ++l)
     {
-        const size_t bytes = static_cast<size_t>(kRing) * m_tiles * kBM * net.wpad[l] * 4;
+        const size_t bytes = static_cast<size_t>(kMaxRing) * m_tiles * kBM * net.wpad[l] * 4;
         ok = (net.bits[l] = static_cast<uint32_t *>(dalloc(bytes))) != nullptr;
         p.zero.emplace_back(net.bits[l], bytes);
     }
-    const size_t n_counters = static_cast<size_t>(kMaxLayers + 1) * m_tiles * kRing;
+    const size_t n_counters = static_cast<size_t>(kMaxLayers + 1) * m_tiles * kMaxRing;
     ok = ok && (net.ready = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
     ok = ok && (net.consumed = static_cast<unsigned int *>(dalloc(n_counters * 4))) != nullptr;
     ok = ok && (net.state = static_cast<uint32_t *>(
@@ -1117,24 +1121,32 @@ int batched_plan_create(
     if (record) p.zero.emplace_back(record, static_cast<size_t>(net.t_max) * off * 4);
 
     cudaError_t err = cudaSuccess;
+    net.ring = kDefaultRing;
     if (autotune)
     {
+        // Schedule choices that leave every result bit-identical: the operand ring depth and the
+        // length of the layer rings (how far a layer may run ahead of the next).
         float best_ms = 0.f;
-        for (int stg = kMinStages; stg <= kMaxStages; ++stg)
-        {
-            if (!variant_fits(p, stg)) continue;
-            float t = 0.f;
-            err = prepare(p, stg, true, &t);
-            if (err == cudaSuccess) err = launch_timed(p, &t);
-            if (err != cudaSuccess) break;
-            p.tune_ms[stg] = t;
-            if (!best_ms || t < best_ms)
+        uint32_t best_ring = kDefaultRing;
+        for (int ri = 0; ri < 3 && err == cudaSuccess; ++ri)
+            for (int stg = kMinStages; stg <= kMaxStages; ++stg)
             {
-                best_ms = t;
-                best = stg;
+                if (!variant_fits(p, stg)) continue;
+                net.ring = kRingChoices[ri];
+                float t = 0.f;
+                err = prepare(p, stg, true, &t);
+                if (err == cudaSuccess) err = launch_timed(p, &t);
+                if (err != cudaSuccess) break;
+                p.tune_ms[ri][stg] = t;
+                if (!best_ms || t < best_ms)
+                {
+                    best_ms = t;
+                    best = stg;
+                    best_ring = kRingChoices[ri];
+                }
             }
-        }
-        if (err == cudaSuccess && p.stages != best) err = capture(p, best);
+        net.ring = best_ring;
+        if (err == cudaSuccess) err = capture(p, best);
     }
     else
     {
@@ -1170,11 +1182,14 @@ int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, 
     return 0;
 }
 
-void batched_plan_info(const BatchedPlan *p, int *stages, float *tune_ms)
+void batched_plan_info(const BatchedPlan *p, int *stages, int *ring_steps, float *tune_ms)
 {
     if (stages) *stages = p->stages;
+    if (ring_steps) *ring_steps = static_cast<int>(p->net.ring);
     if (tune_ms)
-        for (int i = kMinStages; i <= kMaxStages; ++i) tune_ms[i - kMinStages] = p->tune_ms[i];
+        for (int ri = 0; ri < 3; ++ri)
+            for (int i = kMinStages; i <= kMaxStages; ++i)
+                tune_ms[ri * (kMaxStages - kMinStages + 1) + (i - kMinStages)] = p->tune_ms[ri][i];
 }
 
 void batched_plan_destroy(BatchedPlan *p) { delete p; }

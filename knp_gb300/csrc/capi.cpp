@@ -39,7 +39,7 @@ int batched_plan_create(
     const float *rates, unsigned long long key, int *counts, uint32_t *record, int autotune, uint32_t segment_steps,
     cudaStream_t s, BatchedPlan **out, const char **why);
 int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, const char **why);
-void batched_plan_info(const BatchedPlan *p, int *stages, float *tune_ms);
+void batched_plan_info(const BatchedPlan *p, int *stages, int *ring_steps, float *tune_ms);
 void batched_plan_destroy(BatchedPlan *p);
 }  // namespace knp_gb300
 
@@ -439,14 +439,14 @@ int knp_gb300_batched_plan_run(knp_gb300_batched_plan *plan, uint64_t *events, f
     return batched_status(rc, why);
 }
 
-int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, float *tune_ms)
+int knp_gb300_batched_plan_info(const knp_gb300_batched_plan *plan, int *stages, int *ring_steps, float *tune_ms)
 {
     if (!plan || !plan->impl)
     {
         g_error = "plan is null";
         return KNP_GB300_E_INVALID;
     }
-    knp_gb300::batched_plan_info(plan->impl, stages, tune_ms);
+    knp_gb300::batched_plan_info(plan->impl, stages, ring_steps, tune_ms);
     return KNP_GB300_OK;
 }
 

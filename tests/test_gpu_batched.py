@@ -134,8 +134,8 @@ def test_batched_plan_graph_runs_repeat_exactly():
     cfg = BT.dense_config(seed=10, batch=130, sizes=(200, 160, 96, 10), t_lo=20, t_hi=40, rate_max=0.3)
     plan = BT.BatchedPlan(cfg, record=True, autotune=True)
     try:
-        stages, tuned = plan.info()
-        assert stages in (2, 3, 4) and stages in tuned
+        stages, ring, tuned = plan.info()
+        assert stages in (2, 3, 4) and ring in (4, 8, 16) and (stages, ring) in tuned
         ev1, ms1 = plan.run()
         c1, r1 = plan.counts(), plan.record()
         ev2, ms2 = plan.run()
