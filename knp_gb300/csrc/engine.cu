@@ -727,6 +727,7 @@ void Backend::build_projection(ProjectionSlot &p)
         {
             src.idx = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
             src.count = counters_ + q->counter_index;
+            src.n = q->n;
         }
         else
         {

@@ -153,6 +153,7 @@ struct SpikeSource
     const uint32_t *idx;          // population spike list (null for a channel)
     const uint32_t *count;        // population spike count
     const ChannelDev *channel;    // channel descriptor (null for a population)
+    uint32_t n;                   // population size (0 for a channel)
 };
 
 // Gather ("pull") form of a projection. A step whose spike count reaches `threshold` is not
@@ -173,7 +174,7 @@ constexpr int kPullSlicesPerWindow = kPullWindow / kPullSlice;
 struct PullDev
 {
     uint32_t *bitmap;       // [hist_slots][words] spikes of pulled steps
-    uint32_t *pulled;       // [hist_slots] 1 if that step was pulled
+    uint32_t *pulled;       // [hist_slots] 1 if that step was pulled, 2 if every presynaptic neuron fired
     uint32_t hist_slots;    // max_delay + 1
     uint32_t words;         // ceil(n_rows / 32), rounded up to 4
     uint32_t threshold;     // minimum spike count for pulling a step

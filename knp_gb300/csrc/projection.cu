@@ -112,8 +112,11 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
         // Direction choice for this step's spikes (the same in every block: it depends only on the
         // spike count). A pulled step only records its spikes; gather_kernel delivers them.
         const bool pull = total >= p.pull.threshold;
+        // Every presynaptic neuron fired (one population source, whose spike indexes are distinct
+        // and below its size): the gather then needs no bitmap and tests no bit for this step.
+        const bool full = pull && p.n_src == 1 && !p.src[0].channel && p.src[0].n && total >= p.src[0].n;
         const uint32_t sl = static_cast<uint32_t>(t % p.pull.hist_slots);
-        if (blockIdx.x == 0 && threadIdx.x == 0) p.pull.pulled[sl] = pull ? 1u : 0u;
+        if (blockIdx.x == 0 && threadIdx.x == 0) p.pull.pulled[sl] = pull ? (full ? 2u : 1u) : 0u;
         if (pull)
         {
             uint32_t *bm = p.pull.bitmap + static_cast<size_t>(sl) * p.pull.words;
@@ -129,7 +132,7 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
                 }
                 const uint32_t pre = idx[k][jj];
                 if (pre >= p.n_rows) continue;
-                atomicOr(bm + (pre >> 5), 1u << (pre & 31));
+                if (!full) atomicOr(bm + (pre >> 5), 1u << (pre & 31));
                 events += static_cast<unsigned long long>(p.row_ptr[pre + 1] - p.row_ptr[pre]);
             }
             // Per-thread counts: reduce over the warp, then the block.

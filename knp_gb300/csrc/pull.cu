@@ -11,6 +11,7 @@
 // delta_impl.h:78-79), added in another order, which is exact for the FP32 ring (dyadic weights);
 // populations with the fixed-point ring never use this form.
 #include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -217,15 +218,20 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
     {
         const unsigned long long s = tn - d;
         const uint32_t sl = static_cast<uint32_t>(s % g.hist_slots);
-        if (!g.pulled[sl]) continue;
+        const uint32_t pflag = g.pulled[sl];
+        if (!pflag) continue;
+        const bool all = pflag == 2u;  // every presynaptic neuron fired at step s: no bitmap needed
         if (!any)
         {
             for (uint32_t i = threadIdx.x; i < n_acc; i += blockDim.x) acc[i] = 0.0f;
             any = true;
         }
         __syncthreads();  // the previous bitmap is no longer read
-        const uint4 *src = reinterpret_cast<const uint4 *>(g.bitmap + static_cast<size_t>(sl) * g.words);
-        for (uint32_t i = threadIdx.x; i < g.words / 4; i += blockDim.x) smem_u4[i] = src[i];
+        if (!all)
+        {
+            const uint4 *src = reinterpret_cast<const uint4 *>(g.bitmap + static_cast<size_t>(sl) * g.words);
+            for (uint32_t i = threadIdx.x; i < g.words / 4; i += blockDim.x) smem_u4[i] = src[i];
+        }
         if (threadIdx.x == 0) s_next = 0;
         __syncthreads();
         const size_t q0 = (static_cast<size_t>(d - 1) * g.n_windows + w0) * kPullSlicesPerWindow;
@@ -278,54 +284,63 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
             const uint32_t *pk = g.packed + off;
             const uint16_t *ph = kForm == kHalf ? g.w16 + off : nullptr;
             const float *pf = kForm == kFull ? g.w + off : nullptr;
-            auto value = [&](uint32_t pn, float wi) -> float
+            // Two copies of the walk: with the bit test, and without it for a step in which every
+            // presynaptic neuron fired (the test would always pass).
+            auto walk = [&](auto all_tag) -> float
             {
-                if (kForm == kDict)
+                constexpr bool kAll = decltype(all_tag)::value;
+                auto value = [&](uint32_t pn, float wi) -> float
                 {
-                    wi = s_tab[pn >> 24];
-                    pn &= 0xFFFFFFu;
-                }
-                return ((bm[pn >> 5] >> (pn & 31)) & 1u) ? wi : 0.0f;
-            };
-            float sum = 0.0f;
-            uint32_t k0 = 0;
-            for (; k0 + kDepth <= len; k0 += kDepth)
-            {
-                const size_t o = static_cast<size_t>(k0) * kPullSlice;
-                uint32_t pre[kDepth];
-                float w[kDepth];
-#pragma unroll
-                for (int i = 0; i < kDepth; ++i)
+                    if (kForm == kDict)
+                    {
+                        wi = s_tab[pn >> 24];
+                        pn &= 0xFFFFFFu;
+                    }
+                    if (kAll) return wi;
+                    return ((bm[pn >> 5] >> (pn & 31)) & 1u) ? wi : 0.0f;
+                };
+                float sum = 0.0f;
+                uint32_t k0 = 0;
+                for (; k0 + kDepth <= len; k0 += kDepth)
                 {
-                    pre[i] = __ldcs(pk + o + i * kPullSlice);
-                    w[i] = 0.0f;
-                    if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(ph + o + i * kPullSlice)));
-                    if (kForm == kFull) w[i] = __ldcs(pf + o + i * kPullSlice);
-                }
+                    const size_t o = static_cast<size_t>(k0) * kPullSlice;
+                    uint32_t pre[kDepth];
+                    float w[kDepth];
 #pragma unroll
-                for (int i = 0; i < kDepth; ++i) sum = __fadd_rn(sum, value(pre[i], w[i]));
-            }
-            if (k0 < len)
-            {
-                const size_t o = static_cast<size_t>(k0) * kPullSlice;
-                uint32_t pre[kDepth];
-                float w[kDepth];
-#pragma unroll
-                for (int i = 0; i < kDepth; ++i)
-                {
-                    pre[i] = 0u;
-                    w[i] = 0.0f;
-                    if (k0 + i < len)
+                    for (int i = 0; i < kDepth; ++i)
                     {
                         pre[i] = __ldcs(pk + o + i * kPullSlice);
+                        w[i] = 0.0f;
                         if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(ph + o + i * kPullSlice)));
                         if (kForm == kFull) w[i] = __ldcs(pf + o + i * kPullSlice);
                     }
-                }
 #pragma unroll
-                for (int i = 0; i < kDepth; ++i)
-                    if (k0 + i < len) sum = __fadd_rn(sum, value(pre[i], w[i]));
-            }
+                    for (int i = 0; i < kDepth; ++i) sum = __fadd_rn(sum, value(pre[i], w[i]));
+                }
+                if (k0 < len)
+                {
+                    const size_t o = static_cast<size_t>(k0) * kPullSlice;
+                    uint32_t pre[kDepth];
+                    float w[kDepth];
+#pragma unroll
+                    for (int i = 0; i < kDepth; ++i)
+                    {
+                        pre[i] = 0u;
+                        w[i] = 0.0f;
+                        if (k0 + i < len)
+                        {
+                            pre[i] = __ldcs(pk + o + i * kPullSlice);
+                            if (kForm == kHalf) w[i] = __half2float(__ushort_as_half(__ldcs(ph + o + i * kPullSlice)));
+                            if (kForm == kFull) w[i] = __ldcs(pf + o + i * kPullSlice);
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < kDepth; ++i)
+                        if (k0 + i < len) sum = __fadd_rn(sum, value(pre[i], w[i]));
+                }
+                return sum;
+            };
+            const float sum = all ? walk(std::true_type{}) : walk(std::false_type{});
             // This lane's target: one owner per (delay, target), so a plain add.
             const uint32_t t = g.perm[q * kPullSlice + lane];
             if (sum != 0.0f) acc[(qi / kPullSlicesPerWindow) * kPullWindow + t] += sum;
