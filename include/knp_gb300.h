@@ -233,8 +233,10 @@ KNP_GB300_API int knp_gb300_get_step(const knp_gb300_backend *b, uint64_t *step)
 /**
  * Spike indexes (ascending) that population `pop` emitted at step `step`, which must be among the
  * steps run since recording was enabled and not yet discarded. Writes min(count, cap) indexes and
- * the full count to *n. Replaces: receiving the population's SpikeMessage of that step on a
- * subscribed endpoint (single_thread_cpu_test.cpp:85, tests_messaging_common.h:48-56).
+ * the full count to *n. Waits only for step `step` itself: later steps already queued keep running
+ * on the device while the step's bitmap is copied and expanded (a caller can queue step k + 1 before
+ * reading step k). Replaces: receiving the population's SpikeMessage of that step on a subscribed
+ * endpoint (single_thread_cpu_test.cpp:85, tests_messaging_common.h:48-56).
  */
 KNP_GB300_API int knp_gb300_read_spikes(
     knp_gb300_backend *b, knp_uid pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n);
