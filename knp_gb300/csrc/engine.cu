@@ -833,7 +833,9 @@ void Backend::build_pull(ProjectionSlot &p)
     g.bitmap = arena_.make<uint32_t>(static_cast<size_t>(g.hist_slots) * g.words);
     g.pulled = arena_.make<uint32_t>(g.hist_slots);
     g.threshold = static_cast<uint32_t>(std::max(1.0, std::ceil(p.pull_fraction * p.n_rows)));
-    KNP_CUDA(set_gather_smem(std::max<size_t>(smem, 48 * 1024)));
+    // 32 copies of the weight dictionary (one per bank) when shared memory has room for them.
+    if (g.wtab && smem + static_cast<size_t>(g.n_tab) * 32 * 4 + 2048 <= static_cast<size_t>(smem_max)) g.tab_rep = 1;
+    KNP_CUDA(set_gather_smem(std::max<size_t>(gather_smem_bytes(g, grid), 48 * 1024)));
     p.dev.pull = g;
     p.pull = true;
 }

@@ -187,6 +187,9 @@ struct PullDev
     const uint32_t *packed;      // presynaptic neuron of each entry (| weight index << 24 with wtab)
     const float *wtab;           // [256] weight dictionary (entry 0 is +0.0), used when the projection has at
                                  // most 256 distinct weights and fewer than 2^24 presynaptic neurons; else null
+    uint32_t n_tab;              // dictionary entries in use
+    uint32_t tab_rep;            // 1: the gather keeps 32 copies of the dictionary in shared memory (entry
+                                 // i of lane l at 32 i + l: conflict-free lookups); 0: one copy
     const float *w;              // FP32 weights (negated for inhibitory current), or null
     const uint16_t *w16;         // FP16 bit patterns, used when every weight is exactly an FP16 value
     uint64_t padded_entries;     // entries of packed / w

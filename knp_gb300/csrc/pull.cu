@@ -202,11 +202,17 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
     __shared__ uint32_t s_next;  // next slice of the current delay to hand out
     __shared__ float s_tab[256];
     const PullDev &g = p.pull;
-    if (kForm == kDict)
-        for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) s_tab[i] = g.wtab[i];
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem_u4);
     float *acc = reinterpret_cast<float *>(bm + g.words);
     const uint32_t G = gridDim.x;
+    float *rep = acc + static_cast<size_t>((g.n_windows + G - 1) / G) * kPullWindow;  // after the largest acc
+    if (kForm == kDict)
+    {
+        if (g.tab_rep)
+            for (uint32_t i = threadIdx.x; i < g.n_tab * 32u; i += blockDim.x) rep[i] = g.wtab[i >> 5];
+        else
+            for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) s_tab[i] = g.wtab[i];
+    }
     const uint32_t w0 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x) * g.n_windows / G);
     const uint32_t w1 = static_cast<uint32_t>(static_cast<uint64_t>(blockIdx.x + 1) * g.n_windows / G);
     const uint32_t n_acc = (w1 - w0) * kPullWindow;
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1) gather_kernel(ProjectionDev
                 {
                     if (kForm == kDict)
                     {
-                        wi = s_tab[pn >> 24];
+                        wi = g.tab_rep ? rep[((pn >> 24) << 5) + lane] : s_tab[pn >> 24];
                         pn &= 0xFFFFFFu;
                     }
                     if (kAll) return wi;
@@ -384,7 +390,8 @@ int bits_for(uint64_t max_key)
 size_t gather_smem_bytes(const PullDev &p, int grid)
 {
     const uint64_t windows_per_block = (p.n_windows + grid - 1) / grid;
-    return static_cast<size_t>(p.words) * 4 + windows_per_block * kPullWindow * 4;
+    return static_cast<size_t>(p.words) * 4 + windows_per_block * kPullWindow * 4 +
+           (p.tab_rep ? static_cast<size_t>(p.n_tab) * 32 * 4 : 0);
 }
 
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s)
@@ -579,6 +586,7 @@ cudaError_t build_pull_layout(
     out.perm = perm;
     out.packed = packed;
     out.wtab = wtab;
+    out.n_tab = wtab ? static_cast<uint32_t>(h_uniq) : 0u;
     out.w = w32;
     out.w16 = w16;
     out.padded_entries = n_entries;
