@@ -323,7 +323,7 @@ KNP_GB300_API int knp_gb300_bf16_gemm_tn(
  * weights (device, d_weights[l] = [sizes[l + 1]][sizes[l]] row-major) with FP32 accumulation in tensor
  * memory. Sample b runs steps[b] (host array) steps; its input i spikes at step t iff
  * rand64(stream_key(seed, 5), (t * batch + b) * sizes[0] + i) >> 11 < d_rates[b][i] * 2^53 (the
- * generator of knp_gb300/network.py). Outputs: d_counts[batch][sizes[n_layers]] (device, int32) output
+ * generator of knp_gb300/network.py; a rate below 0 or NaN never fires, 1 or above always). Outputs: d_counts[batch][sizes[n_layers]] (device, int32) output
  * spike counts; optional d_record (device, uint32) with every layer's spike bitmap of every step,
  * laid out [max(steps)][layer 0..n_layers][batch][ceil(sizes[l] / 32)]; *events (host) synaptic events
  * (spikes x fan-out of their layer); *ms (host) device time of the run. Synchronous.

@@ -64,7 +64,9 @@ def input_spikes(cfg: BatchedConfig, b: int, t: int) -> np.ndarray:
     n0 = cfg.sizes[0]
     key = N.stream_key(cfg.seed, N.S_INPUT)
     ctr = (np.uint64(t) * np.uint64(cfg.batch) + np.uint64(b)) * np.uint64(n0) + np.arange(n0, dtype=np.uint64)
-    thr = (cfg.rates[b].astype(np.float64) * float(1 << 53)).astype(np.uint64)
+    # A rate is a probability: below 0 (or NaN) never, 1 or above always.
+    r = np.clip(np.nan_to_num(cfg.rates[b].astype(np.float64), nan=0.0), 0.0, 1.0)
+    thr = (r * float(1 << 53)).astype(np.uint64)
     idx = np.nonzero((N.rand64(key, ctr) >> np.uint64(11)) < thr)[0].astype(np.uint32)
     if cfg.sample_sizes is not None:
         idx = idx[idx < cfg.sample_sizes[0][b]]

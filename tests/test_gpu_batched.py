@@ -212,3 +212,19 @@ def test_batched_full_config_identical_across_depths_and_repeats():
                     np.testing.assert_array_equal(got[2][layer], ref[2][layer])
         finally:
             plan.close()
+
+
+def test_batched_input_rates_at_the_edges():
+    """Input draws for rates at and beyond the ends of [0, 1] (negative, NaN, subnormal, 1, above 1,
+    infinity) equal the host restatement: never below 0 or for NaN, always at 1 and above."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(seed=13, batch=6, sizes=(64, 32, 10), t_lo=5, t_hi=9, rate_max=0.5)
+    edge = np.array([0.0, -0.5, np.nan, 1e-40, 1.0, 1.5, np.inf, 0.999999], np.float32)
+    cfg.rates[:, :edge.size] = edge
+    counts, rec, events, ms = BT.run(cfg, record=True)
+    for s in range(cfg.batch):
+        for t in range(int(cfg.steps[s])):
+            got = BT.spikes_from_bits(rec[0][t, s], cfg.sizes[0])
+            np.testing.assert_array_equal(got, BT.input_spikes(cfg, s, t))
+            assert {4, 5, 6} <= set(got.tolist()) and not ({0, 1, 2, 3} & set(got.tolist()))
