@@ -303,7 +303,12 @@ def stdp_measure(device: int):
     b._init()
     for sc in scheds:
         b.load_spike_schedule(sc)
-    ms = b.step_timed(steps)
+    # The first 200 steps run phase by phase (CUDA events between the phases), the rest as the
+    # normal step graphs, timed; together they are the config's 20,000 steps.
+    n_prof = 200
+    ph = b.profile_phases(n_prof) / n_prof
+    e0, _, _ = b.counters()
+    ms = b.step_timed(steps - n_prof)
     events, spikes, updates = b.counters()
     w = b.read_weights(net.projections[0].uid)
     b.close()
@@ -313,8 +318,10 @@ def stdp_measure(device: int):
         expect = json.load(f)
     return {
         "workload": "stdp: 784 -> 800 additive STDP (tau 20) + 800 x 800 lateral inhibition, 200 samples x 100 steps",
-        "value": events / (ms / 1e3), "unit": UNIT, "ms_total": ms, "us_per_step": ms / steps * 1e3,
-        "events": int(events), "spikes": int(spikes), "neuron_updates_per_s": updates / (ms / 1e3),
+        "value": (events - e0) / (ms / 1e3), "unit": UNIT, "timed_steps": steps - n_prof, "ms_timed": ms,
+        "us_per_step": ms / (steps - n_prof) * 1e3,
+        "phase_us_per_step": {k: float(v) * 1e3 for k, v in zip(("population", "projection", "stdp", "step_end"), ph)},
+        "events": int(events), "spikes": int(spikes),
         "weights_crc32": crc, "weights_match_reference_oracle": bool(crc == expect["weights_crc"]),
         "events_match_reference_oracle": bool(int(events) == expect["events"]),
     }
