@@ -800,7 +800,7 @@ int Backend::gather_grid(const ProjectionSlot &p) const
 }
 
 // The gather form is built for large delta projections fed by one population into an FP32 ring,
-// when the device has room for a second (6 or 8 B / synapse) copy of the synapses and the build's
+// when the device has room for a second (4, 6 or 8 B / synapse) copy of the synapses and the build's
 // temporaries.
 void Backend::build_pull(ProjectionSlot &p)
 {
