@@ -535,7 +535,7 @@ def main():
             "config": {"workload": "large_sparse_plain", "neurons": n_neurons, "fan_in": args.fan_in,
                        "synapses": n_neurons * args.fan_in,
                        "delays": "1..20", "weights": "k/256, k in [-16,48]", "p_background": P_BG,
-                       "l2": "inputs larger than L2 (9 GB synapse arrays), no flush",
+                       "l2": "inputs larger than L2 (4 GB gather layout, 9 GB CSR), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "pull_threshold": args.pull_threshold},
             "neuron_updates_per_s": n_neurons * world * args.steps / t,
