@@ -117,6 +117,13 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
         const bool full = pull && p.n_src == 1 && !p.src[0].channel && p.src[0].n && total >= p.src[0].n;
         const uint32_t sl = static_cast<uint32_t>(t % p.pull.hist_slots);
         if (blockIdx.x == 0 && threadIdx.x == 0) p.pull.pulled[sl] = pull ? (full ? 2u : 1u) : 0u;
+        if (full)
+        {
+            // Every row fired: the step's events are all the synapses, and the bitmap stays unused.
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                atomicAdd(&ctl->events_total, static_cast<unsigned long long>(p.row_ptr[p.n_rows] - p.row_ptr[0]));
+            return;
+        }
         if (pull)
         {
             uint32_t *bm = p.pull.bitmap + static_cast<size_t>(sl) * p.pull.words;
@@ -132,7 +139,7 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
                 }
                 const uint32_t pre = idx[k][jj];
                 if (pre >= p.n_rows) continue;
-                if (!full) atomicOr(bm + (pre >> 5), 1u << (pre & 31));
+                atomicOr(bm + (pre >> 5), 1u << (pre & 31));
                 events += static_cast<unsigned long long>(p.row_ptr[pre + 1] - p.row_ptr[pre]);
             }
             // Per-thread counts: reduce over the warp, then the block.
