@@ -295,16 +295,19 @@ def stdp_measure(device: int):
 
     from knp_gb300 import backend as B
     from knp_gb300 import network as Nw
+    from knp_gb300 import types as T
 
     steps = 20_000
     net, scheds = Nw.stdp_network(seed=3, samples=200, steps_per_sample=100)
     b = B.GB300Backend(device)
     b.load_network(net, record=[])
     b._init()
+    fused = b.fused
     for sc in scheds:
         b.load_spike_schedule(sc)
-    # The first 200 steps run phase by phase (CUDA events between the phases), the rest as the
-    # normal step graphs, timed; together they are the config's 20,000 steps.
+    # The first 200 steps run phase by phase (per-phase kernels with CUDA events between the
+    # phases), the rest as normal steps (the fused step kernel at this size), timed; together they
+    # are the config's 20,000 steps.
     n_prof = 200
     ph = b.profile_phases(n_prof) / n_prof
     e0, _, _ = b.counters()
@@ -312,6 +315,17 @@ def stdp_measure(device: int):
     events, spikes, updates = b.counters()
     w = b.read_weights(net.projections[0].uid)
     b.close()
+    # The per-phase step graphs on the same config, for comparison (first 2,000 steps, timed after
+    # 100 untimed ones).
+    bp = B.GB300Backend(device)
+    bp.load_network(net, record=[])
+    bp.set_step_mode(T.STEP_PHASES)
+    bp._init()
+    for sc in scheds:
+        bp.load_spike_schedule(sc)
+    bp.step(100)
+    ms_phases = bp.step_timed(1900)
+    bp.close()
     crc = zlib.crc32(w.tobytes())
     fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "stdp_full.json")
     with open(fixture) as f:
@@ -320,6 +334,8 @@ def stdp_measure(device: int):
         "workload": "stdp: 784 -> 800 additive STDP (tau 20) + 800 x 800 lateral inhibition, 200 samples x 100 steps",
         "value": (events - e0) / (ms / 1e3), "unit": UNIT, "timed_steps": steps - n_prof, "ms_timed": ms,
         "us_per_step": ms / (steps - n_prof) * 1e3,
+        "step_kernel": "fused step kernel (one CTA cluster)" if fused else "per-phase kernels",
+        "phases_us_per_step": ms_phases / 1900 * 1e3,
         "phase_us_per_step": {k: float(v) * 1e3 for k, v in zip(("population", "projection", "stdp", "step_end"), ph)},
         "events": int(events), "spikes": int(spikes),
         "weights_crc32": crc, "weights_match_reference_oracle": bool(crc == expect["weights_crc"]),

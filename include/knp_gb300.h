@@ -54,6 +54,14 @@ typedef enum knp_gb300_accumulator
     KNP_GB300_ACC_FIXED64 = 2 /* int64 fixed point (2^-40): order-independent, exact for |w| >= 2^-17 */
 } knp_gb300_accumulator;
 
+/** How a step is executed (results are the same in every mode). */
+typedef enum knp_gb300_step_mode
+{
+    KNP_GB300_STEP_AUTO = 0,   /* fused when the network qualifies (see knp_gb300_set_step_mode), else phases */
+    KNP_GB300_STEP_PHASES = 1, /* one kernel per phase (population, projection, STDP, end of step) in CUDA graphs */
+    KNP_GB300_STEP_FUSED = 2   /* one kernel (one CTA cluster) runs whole steps; init fails if the network does not qualify */
+} knp_gb300_step_mode;
+
 /** Message text of the last failed call on this thread (never NULL). */
 KNP_GB300_API const char *knp_gb300_last_error(void);
 
@@ -146,6 +154,19 @@ KNP_GB300_API int knp_gb300_set_accumulator(knp_gb300_backend *b, knp_uid pop_ui
  * the reference's delivery loop (delta_impl.h:65-107) is a scatter only.
  */
 KNP_GB300_API int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid proj_uid, double fraction);
+
+/**
+ * Step execution mode (before init). The fused mode runs every phase of a step, and many steps per
+ * launch, in one thread-block cluster (up to 8 CTAs) with cluster barriers between the phases; it
+ * takes networks of at most 16384 neurons and 2^22 synapses whose projections have no gather form.
+ * AUTO (the default) picks it for such networks. No reference counterpart: the reference's step driver is
+ * SingleThreadedCPUBackend::_step (knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:89-141),
+ * whose phase order both modes keep.
+ */
+KNP_GB300_API int knp_gb300_set_step_mode(knp_gb300_backend *b, int mode);
+
+/** 1 when init chose the fused step kernel, else 0 (after init). */
+KNP_GB300_API int knp_gb300_step_fused(const knp_gb300_backend *b, int *fused);
 
 /**
  * Enable or disable per-step spike recording of a population (SpikeMessages that an output

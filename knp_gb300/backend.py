@@ -143,6 +143,18 @@ class GB300Backend:
         (negative: always scatter)."""
         self._chk(self._lib.knp_gb300_set_pull_threshold(self._h, T.to_c_uid(proj_uid), float(fraction)))
 
+    def set_step_mode(self, mode: int):
+        """Step execution (before init): T.STEP_AUTO, T.STEP_PHASES (a kernel per phase) or
+        T.STEP_FUSED (one cluster kernel per run of steps; small networks only)."""
+        self._chk(self._lib.knp_gb300_set_step_mode(self._h, int(mode)))
+
+    @property
+    def fused(self) -> bool:
+        """True when init chose the fused step kernel."""
+        v = ctypes.c_int(0)
+        self._chk(self._lib.knp_gb300_step_fused(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     def record_spikes(self, pop_uid: bytes, enable: bool = True):
         self._chk(self._lib.knp_gb300_record_spikes(self._h, T.to_c_uid(pop_uid), int(enable)))
         (self._recorded.add if enable else self._recorded.discard)(pop_uid)
@@ -312,7 +324,7 @@ class GB300Backend:
 
 
 def run(net: N.Network, schedules, n_steps: int, record=None, device: int = 0, device_schedule: bool = False,
-        on_step=None, accumulator=None):
+        on_step=None, accumulator=None, step_mode=None):
     """Run a network for ``n_steps`` steps through the C ABI. Input schedules are sent as host
     messages step by step (``device_schedule=False``) or uploaded once to device memory. Returns
     ({pop uid: [per-step ascending spike arrays]}, backend)."""
@@ -321,6 +333,8 @@ def run(net: N.Network, schedules, n_steps: int, record=None, device: int = 0, d
     if accumulator is not None:
         for p in net.populations:
             b.set_accumulator(p.uid, accumulator)
+    if step_mode is not None:
+        b.set_step_mode(step_mode)
     b._init()
     rec = [p.uid for p in net.populations] if record is None else record
     if device_schedule:

@@ -183,6 +183,19 @@ int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid proj_uid, double 
     return guarded([&] { b->impl.set_pull_threshold(U(proj_uid), fraction); });
 }
 
+int knp_gb300_set_step_mode(knp_gb300_backend *b, int mode)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.set_step_mode(mode); });
+}
+
+int knp_gb300_step_fused(const knp_gb300_backend *b, int *fused)
+{
+    if (!b || !fused) return null_handle();
+    *fused = b->impl.fused() ? 1 : 0;
+    return KNP_GB300_OK;
+}
+
 int knp_gb300_record_spikes(knp_gb300_backend *b, knp_uid pop_uid, int enable)
 {
     if (!b) return null_handle();

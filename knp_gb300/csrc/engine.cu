@@ -806,6 +806,7 @@ void Backend::build_pull(ProjectionSlot &p)
 {
     PopulationSlot *post = find_pop(p.post_uid);
     if (p.pull_fraction < 0 || p.kind != KNP_SYNAPSE_DELTA || !post || p.n_syn < (1u << 20)) return;
+    if (step_mode_ == KNP_GB300_STEP_FUSED) return;  // the fused step kernel scatters every step
     if (p.dev.n_src != 1 || p.dev.src[0].channel) return;
     const RingView &rg = post->ring;
     if (rg.fixed || (rg.forced && p.dev.forcing)) return;
@@ -866,6 +867,12 @@ void Backend::init()
 {
     require_not_init("init");
     KNP_CUDA(cudaSetDevice(device_));
+    if (step_mode_ == KNP_GB300_STEP_FUSED)
+    {
+        std::string why;
+        if (!small_net_eligible(why))
+            throw Error(KNP_GB300_E_INVALID, "the fused step kernel does not take this network: " + why);
+    }
     for (auto &p : projs_)
     {
         if (!p->post_uid.is_null() && !find_pop(p->post_uid))
@@ -932,8 +939,96 @@ void Backend::init()
         std::vector<float>().swap(p->weight);
         if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) std::vector<uint32_t>().swap(p->post);
     }
+    std::string why;
+    fused_ = step_mode_ == KNP_GB300_STEP_FUSED || (step_mode_ == KNP_GB300_STEP_AUTO && small_net_eligible(why));
     initialized_ = true;
     capture_graphs();
+}
+
+void Backend::set_step_mode(int mode)
+{
+    require_not_init("set_step_mode");
+    if (mode != KNP_GB300_STEP_AUTO && mode != KNP_GB300_STEP_PHASES && mode != KNP_GB300_STEP_FUSED)
+        throw Error(KNP_GB300_E_INVALID, "unknown step mode");
+    step_mode_ = mode;
+}
+
+// The fused kernel is one cluster of at most 8 CTAs: it pays off while a step is a few microseconds
+// of work, and it has no gather form (in AUTO mode a projection with a gather layout keeps the per-phase kernels; the
+// FUSED mode builds no gather layout).
+bool Backend::small_net_eligible(std::string &why) const
+{
+    uint64_t neurons = 0, syn = 0;
+    for (auto &q : pops_) neurons += q->n;
+    for (auto &p : projs_)
+    {
+        syn += p->n_syn;
+        if (p->pull)
+        {
+            why = "a projection has a gather layout";
+            return false;
+        }
+    }
+    if (neurons > kSmallMaxNeurons)
+    {
+        why = "more than " + std::to_string(kSmallMaxNeurons) + " neurons";
+        return false;
+    }
+    if (syn > kSmallMaxSynapses)
+    {
+        why = "more than " + std::to_string(kSmallMaxSynapses) + " synapses";
+        return false;
+    }
+    return true;
+}
+
+// Uploads the device descriptors of the fused kernel (again after a change of recording).
+void Backend::build_small_net()
+{
+    std::vector<SmallPop> pops;
+    for (auto &q : pops_)
+    {
+        SmallPop sp{};
+        sp.kind = q->kind == KNP_NEURON_LIF ? kSmallLif : kSmallBlifat;
+        sp.blifat = q->bdev;
+        sp.lif = q->ldev;
+        pops.push_back(sp);
+    }
+    std::vector<ProjectionDev> projs;
+    std::vector<SmallStdp> rules;
+    for (auto &p : projs_)
+    {
+        if (p->dev.n_src) projs.push_back(p->dev);
+        if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
+        if (p->stdp_sources.size() > static_cast<size_t>(kMaxSources))
+            throw Error(KNP_GB300_E_INVALID, "too many STDP populations for one projection");
+        SmallStdp r{};
+        r.d = p->stdp;
+        for (auto &[src, both] : p->stdp_sources)
+        {
+            r.src[r.n_src] = src;
+            r.both[r.n_src] = both;
+            ++r.n_src;
+        }
+        rules.push_back(r);
+    }
+    small_cluster_ = small_net_cluster();
+    if (!small_.pops)
+    {
+        small_.pops = arena_.make<SmallPop>(std::max<size_t>(pops.size(), 1));
+        small_.projs = arena_.make<ProjectionDev>(std::max<size_t>(projs.size(), 1));
+        small_.stdp = arena_.make<SmallStdp>(std::max<size_t>(rules.size(), 1));
+    }
+    small_.n_pops = static_cast<uint32_t>(pops.size());
+    small_.n_projs = static_cast<uint32_t>(projs.size());
+    small_.n_stdp = static_cast<uint32_t>(rules.size());
+    small_.end = StepEnd{counters_, n_counters_, n_spike_counters_};
+    KNP_CUDA(cudaMemcpy(const_cast<SmallPop *>(small_.pops), pops.data(), pops.size() * sizeof(SmallPop),
+                        cudaMemcpyHostToDevice));
+    KNP_CUDA(cudaMemcpy(const_cast<ProjectionDev *>(small_.projs), projs.data(), projs.size() * sizeof(ProjectionDev),
+                        cudaMemcpyHostToDevice));
+    KNP_CUDA(cudaMemcpy(const_cast<SmallStdp *>(small_.stdp), rules.data(), rules.size() * sizeof(SmallStdp),
+                        cudaMemcpyHostToDevice));
 }
 
 // ------------------------------------------------------------------------------------ stepping
@@ -977,6 +1072,11 @@ void Backend::capture_graphs()
     if (graph1_) cudaGraphExecDestroy(graph1_);
     if (graphK_) cudaGraphExecDestroy(graphK_);
     graph1_ = graphK_ = nullptr;
+    if (fused_)
+    {
+        build_small_net();
+        return;
+    }
     for (int which = 0; which < 2; ++which)
     {
         cudaGraph_t g = nullptr;
@@ -1090,7 +1190,11 @@ void Backend::step(uint64_t n)
         if (host_inputs)
         {
             stage_host_inputs();
-            KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
+            if (fused_)
+                KNP_CUDA(launch_small_net(small_, ctl_, 1, small_cluster_, stream_));
+            else
+                KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
+            KNP_CUDA(cudaGetLastError());
             if (any_recording_) record_step_event(step_);
             ++step_;
             --n;
@@ -1099,6 +1203,13 @@ void Backend::step(uint64_t n)
         uint64_t k = n;
         if (any_recording_) k = std::min<uint64_t>(k, steps_before_drain());
         uint64_t done = 0;
+        while (fused_ && done < k)
+        {
+            const uint64_t m = std::min<uint64_t>(k - done, kSmallMaxStepsPerLaunch);
+            KNP_CUDA(launch_small_net(small_, ctl_, static_cast<uint32_t>(m), small_cluster_, stream_));
+            KNP_CUDA(cudaGetLastError());
+            done += m;
+        }
         while (k - done >= kGraphSteps)
         {
             KNP_CUDA(cudaGraphLaunch(graphK_, stream_));

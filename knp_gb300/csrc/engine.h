@@ -216,6 +216,8 @@ public:
     void subscribe(const Uid &receiver, const Uid &sender);
     void set_accumulator(const Uid &pop, int mode);
     void set_pull_threshold(const Uid &proj, double fraction);
+    void set_step_mode(int mode);
+    bool fused() const { return fused_; }
     void record_spikes(const Uid &pop, bool enable);
     void init();
 
@@ -259,6 +261,8 @@ private:
     int gather_grid(const ProjectionSlot &p) const;
     void wire();
     void enqueue_step();
+    bool small_net_eligible(std::string &why) const;
+    void build_small_net();
     void capture_graphs();
     void stage_host_inputs();
     void drain_recordings() { drain_recordings(step_); }
@@ -290,6 +294,14 @@ private:
     uint64_t updates_before_init_ = 0;
     cudaGraphExec_t graph1_ = nullptr, graphK_ = nullptr;
     static constexpr uint64_t kGraphSteps = 16;
+    // Fused step kernel for small networks (small_net.cu: one CTA cluster runs whole steps), chosen at init.
+    int step_mode_ = 0;  // knp_gb300_step_mode
+    bool fused_ = false;
+    SmallNet small_{};
+    int small_cluster_ = 1;  // CTAs of the fused kernel's cluster
+    static constexpr uint64_t kSmallMaxNeurons = 16384;
+    static constexpr uint64_t kSmallMaxSynapses = 1ull << 22;
+    static constexpr uint64_t kSmallMaxStepsPerLaunch = 1ull << 16;
     // pinned staging for host-sent messages
     void *pinned_ = nullptr;
     size_t pinned_bytes_ = 0;

@@ -244,6 +244,35 @@ struct StepEnd
     uint32_t n_spike_counts;  // the first n_spike_counts counters are population spike counts
 };
 
+// A small network run by the fused step kernel (small_net.cu): device arrays of its populations,
+// its projections (none with a gather layout) and its STDP rules, in step order.
+enum SmallPopKind : int
+{
+    kSmallBlifat = 0,
+    kSmallLif = 1,
+};
+struct SmallPop
+{
+    int kind;
+    BlifatDev blifat;
+    LifDev lif;
+};
+struct SmallStdp
+{
+    StdpDev d;
+    uint32_t n_src;
+    SpikeSource src[kMaxSources];
+    int both[kMaxSources];  // the source fills both histories (STDPAndSpike)
+};
+struct SmallNet
+{
+    const SmallPop *pops;
+    const ProjectionDev *projs;
+    const SmallStdp *stdp;
+    uint32_t n_pops, n_projs, n_stdp;
+    StepEnd end;
+};
+
 // ---------------------------------------------------------------- launchers (stream-ordered)
 void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s);
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
@@ -251,6 +280,11 @@ void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStrea
 void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
 void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
+// Runs n_steps whole steps of a small network in one launch of one cluster of `cluster` CTAs
+// (advances Control::step). small_net_cluster() is the largest cluster size (8, 4, 2 or 1) the
+// device can schedule for it.
+int small_net_cluster();
+cudaError_t launch_small_net(const SmallNet &net, Control *ctl, uint32_t n_steps, int cluster, cudaStream_t s);
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 size_t gather_smem_bytes(const PullDev &p, int grid);
 // Builds the gather layout of a projection from its CSR and fills `out`; the buffers go to `bufs`.

@@ -1,0 +1,437 @@
+// Device-side per-neuron code of the population kernels, shared by the per-phase kernels
+// (population.cu) and the fused small-network step kernel (small_net.cu). A thread steps 4
+// consecutive neurons (float4 / 16-byte loads of state and input-ring slots); a block compacts its
+// threads' spike masks into the population's spike list.
+//
+// BLIFAT arithmetic follows the reference per-neuron functions
+//   calculate_pre_impact_single_neuron_state_impl   blifat_impl.h:31-47 (resource-STDP: :50-65)
+//   impact_neuron_impl                              blifat_impl.h:68-107 (impacts pre-summed in the ring)
+//   calculate_post_impact_single_neuron_state_impl  blifat_impl.h:110-168
+//   resource-STDP neuron training without resource synapses  blifat_stdp.h:35-172, training/stdp.h:88-186
+// (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/impl/populations/...), with FP32
+// state. LIF follows lif_impl.h:33-86. Every floating-point operation is an explicit
+// round-to-nearest intrinsic, so the compiler cannot contract it into an FMA.
+#pragma once
+
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace knp_gb300
+{
+namespace
+{
+
+__device__ __forceinline__ float pf(const ParamF &p, uint32_t i) { return p.a ? p.a[i] : p.u; }
+__device__ __forceinline__ uint32_t pu(const ParamU &p, uint32_t i) { return p.a ? p.a[i] : p.u; }
+
+__device__ __forceinline__ float4 ld4(const float *p, uint32_t i) { return *reinterpret_cast<const float4 *>(p + i); }
+__device__ __forceinline__ void st4(float *p, uint32_t i, float4 v) { *reinterpret_cast<float4 *>(p + i) = v; }
+__device__ __forceinline__ uint4 ld4u(const uint32_t *p, uint32_t i) { return *reinterpret_cast<const uint4 *>(p + i); }
+__device__ __forceinline__ void st4u(uint32_t *p, uint32_t i, uint4 v) { *reinterpret_cast<uint4 *>(p + i) = v; }
+__device__ __forceinline__ float &at(float4 &v, int k) { return reinterpret_cast<float *>(&v)[k]; }
+__device__ __forceinline__ uint32_t &at(uint4 &v, int k) { return reinterpret_cast<uint32_t *>(&v)[k]; }
+
+// Append this thread's spikes (bit k of mask = neuron i0 + k) to list[*count ...] with one atomic
+// per block; indexes stay ascending within a block. With a recording slot `rec` (rec_words words),
+// also writes the step's spike bitmap: the 8 lanes of an aligned lane group cover 32 consecutive
+// neurons, so OR-ing their 4-bit masks gives one whole word, stored by the group's first lane.
+// Every thread of the block calls this (threads past the population with mask 0).
+template <int kThreads>
+__device__ __forceinline__ void emit_spikes(
+    uint32_t mask, uint32_t i0, uint32_t *list, uint32_t *count, uint32_t *rec, uint32_t rec_words)
+{
+    __shared__ uint32_t warp_tot[kThreads / 32];
+    __shared__ uint32_t block_base;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    if (rec)
+    {
+        uint32_t v = mask << (4 * (lane & 7));
+        v |= __shfl_xor_sync(0xffffffffu, v, 1);
+        v |= __shfl_xor_sync(0xffffffffu, v, 2);
+        v |= __shfl_xor_sync(0xffffffffu, v, 4);
+        const uint32_t word = i0 >> 5;
+        if ((lane & 7) == 0 && word < rec_words) rec[word] = v;
+    }
+    const uint32_t c = __popc(mask);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        uint32_t run = 0;
+        for (int w = 0; w < kThreads / 32; ++w)
+        {
+            const uint32_t x = warp_tot[w];
+            warp_tot[w] = run;
+            run += x;
+        }
+        block_base = run ? atomicAdd(count, run) : 0u;
+    }
+    __syncthreads();
+    if (!c) return;
+    uint32_t pos = block_base + warp_tot[warp] + incl - c;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (mask & (1u << k)) list[pos++] = i0 + k;
+}
+
+__device__ __forceinline__ uint32_t *record_slot(uint32_t *rec_bits, uint32_t rec_words, uint32_t rec_slots,
+                                                 unsigned long long t)
+{
+    return rec_bits ? rec_bits + static_cast<size_t>(t % rec_slots) * rec_words : nullptr;
+}
+
+struct NeuronState
+{
+    float V, V_pre, thr_dyn, trace, g, dopa, add_thr;
+    uint32_t ns, phase;
+    long long block;
+};
+
+// One BLIFAT neuron for one step. `acc` is this step's summed EXCITATORY - INHIBITORY_CURRENT input
+// (FP32 ring) and (acc_hi, acc_lo) the same in two-word fixed point (fixed ring).
+template <bool kFixed>
+__device__ __forceinline__ bool blifat_step(
+    const BlifatDev &p, uint32_t i, unsigned long long t, NeuronState &s, float acc, long long acc_hi,
+    long long acc_lo, float g_in, float d_in)
+{
+    const uint32_t f = p.flags;
+    const bool res = f & kResource;
+    // ---- pre-impact (blifat_impl.h:31-65)
+    if (f & kLiveRefract) s.ns = (s.ns == 0xFFFFFFFFu) ? 0u : (s.ns >= 0xFFFFFFFEu ? 0xFFFFFFFEu : s.ns + 1u);
+    if (f & kLiveThrDyn) s.thr_dyn = __fmul_rn(s.thr_dyn, pf(p.thr_decay, i));
+    if (f & kLiveTrace) s.trace = __fmul_rn(s.trace, pf(p.trace_decay, i));
+    if (f & kLiveG) s.g = __fmul_rn(s.g, pf(p.g_decay, i));
+    if (res) s.dopa = 0.0f;
+    s.V = (f & kLiveVRead) ? __fmul_rn(s.V, pf(p.v_decay, i)) : 0.0f;
+    if ((f & kLiveBurst) && s.phase == 1u)
+    {
+        if (!res) s.phase = 0u;
+        s.V = __fadd_rn(s.V, pf(p.reflexive, i));
+    }
+    s.V_pre = s.V;
+    // ---- impacts (blifat_impl.h:68-107), pre-summed per channel
+    // Fixed point: the exact potential as vh * 2^-8 + vl * 2^-48; the spike test compares it with the
+    // threshold exactly, and the stored potential is its correctly rounded FP32 value.
+    long long vh = 0, vl = 0;
+    bool fx_ok = false;
+    if (kFixed)
+    {
+        vh = acc_hi;
+        vl = acc_lo;
+        fx_normalize(vh, vl);
+        if (s.V_pre != 0.0f)
+        {
+            long long ph, pl;
+            fx_split(s.V_pre, ph, pl);
+            vh += ph;
+            vl += pl;
+            fx_normalize(vh, vl);
+        }
+        fx_ok = true;
+        s.V = fx_to_float(vh, vl);
+    }
+    else
+    {
+        s.V = __fadd_rn(s.V, acc);
+    }
+    if (f & kLiveG) s.g = __fadd_rn(s.g, g_in);
+    if (f & kLiveDopa) s.dopa = __fadd_rn(s.dopa, d_in);
+    // ---- post-impact (blifat_impl.h:119-168)
+    if (f & kLiveBlock)
+    {
+        if (s.block <= 0)
+        {
+            s.V = s.V_pre;
+            fx_ok = false;
+        }
+        if (s.block < 0)
+        {
+            ++s.block;
+            if (s.block == 0) s.block = 0x7FFFFFFFFFFFFFFFll;
+        }
+        else if (s.block > 0)
+        {
+            --s.block;
+        }
+    }
+    if (f & kLiveG)
+    {
+        const float e = pf(p.e_inh, i);
+        if (s.g < 1.0f)
+            s.V = __fsub_rn(s.V, __fmul_rn(__fsub_rn(s.V, e), s.g));
+        else
+            s.V = e;
+        fx_ok = false;
+    }
+    const float thr_total = __fadd_rn(__fadd_rn(pf(p.thr, i), s.thr_dyn), s.add_thr);
+    const bool ref_ok = (f & kLiveRefract) ? (s.ns > pu(p.t_ref, i)) : (t > 0);
+    bool above;
+    if (kFixed && fx_ok)
+    {
+        long long th, tl;
+        fx_split(thr_total, th, tl);
+        above = vh > th || (vh == th && vl >= tl);
+    }
+    else
+    {
+        above = s.V >= thr_total;
+    }
+    const bool spike = ref_ok && above;
+    if (spike)
+    {
+        if (f & kLiveThrDyn) s.thr_dyn = __fadd_rn(s.thr_dyn, pf(p.thr_inc, i));
+        if (f & kLiveTrace) s.trace = __fadd_rn(s.trace, pf(p.trace_inc, i));
+        s.V = pf(p.v_reset, i);
+        if (f & kLiveBurst) s.phase = pu(p.burst_period, i);
+        s.ns = (f & kLiveRefract) ? 0u : static_cast<uint32_t>(t);
+    }
+    const float vmin = pf(p.v_min, i);
+    if (s.V < vmin) s.V = vmin;
+    return spike;
+}
+
+// Resource-STDP neuron bookkeeping with no resource-STDP synapses (blifat_stdp.h:35-172).
+__device__ __forceinline__ void resource_step(
+    const BlifatDev &p, uint32_t i, unsigned long long t, bool spike, bool forced, float dopa, float &add_thr)
+{
+    const ResourceDev &r = p.res;
+    int32_t status = r.isi_status[i];
+    const uint32_t isi_max = pu(r.isi_max, i);
+    if (spike)
+    {
+        // process_spiking_neurons_impl (blifat_stdp.h:43-67) + update_isi (training/stdp.h:88-126).
+        r.last_spike_step[i] = t;
+        if (forced)
+        {
+            status = 0;  // is_forced
+        }
+        else
+        {
+            const unsigned long long last = r.last_step[i];
+            switch (status)
+            {
+                case 3:  // not_in_period
+                case 0:  // is_forced
+                    status = 1;
+                    r.first_isi_spike[i] = t;
+                    break;
+                case 1:  // period_started
+                    if (last - t < isi_max) status = 2;
+                    break;
+                default:  // period_continued
+                    if (last - t >= isi_max || dopa != 0.0f)
+                    {
+                        status = 1;
+                        r.first_isi_spike[i] = t;
+                    }
+                    break;
+            }
+            r.last_step[i] = t;
+        }
+        if (status == 1) r.stability[i] = __fsub_rn(r.stability[i], pf(r.stability_change_at_isi, i));
+        add_thr = __fmul_rn(0.0f, pf(r.add_thr_coef, i));
+    }
+    // do_dopamine_plasticity_impl (blifat_stdp.h:106-155), no connected synapses.
+    if (dopa > 0.0f || (dopa < 0.0f && status != 0))
+    {
+        float st = r.stability[i];
+        const float c = pf(r.stability_change_param, i);
+        if (forced || dopa < 0.0f)
+        {
+            st = __fsub_rn(st, __fmul_rn(dopa, c));
+            st = fmaxf(st, 0.0f);
+        }
+        else
+        {
+            const unsigned long long diff_u = t - r.first_isi_spike[i] - isi_max;
+            const float diff = __ull2float_rn(diff_u);
+            const float m = fmaxf(__fsub_rn(2.0f, __fdiv_rn(diff, static_cast<float>(isi_max))), -1.0f);
+            st = __fadd_rn(st, __fmul_rn(__fmul_rn(c, dopa), m));
+        }
+        r.stability[i] = st;
+    }
+    // renormalize_resource (training/stdp.h:152-186), no connected synapses.
+    if (p.flags & kLiveRenorm)
+    {
+        if (!(t - r.last_step[i] <= isi_max && status != 0))
+        {
+            const float fr = r.free_resource[i];
+            if (!(fabsf(fr) < pf(r.resource_threshold, i))) r.free_resource[i] = 0.0f;
+        }
+    }
+    r.isi_status[i] = status;
+    r.is_forced[i] = forced ? 1 : 0;
+}
+
+// Steps neurons i0 .. i0 + 3 of a BLIFAT population (those below n) at step t and returns their spike
+// mask (bit k = neuron i0 + k fired).
+template <bool kFixed>
+__device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned long long t, uint32_t i0)
+{
+    const uint32_t f = p.flags;
+    uint32_t mask = 0;
+    if (i0 < p.n)
+    {
+        const RingView &rg = p.ring;
+        const uint32_t slot = static_cast<uint32_t>(t % rg.slots);
+        const size_t ro = static_cast<size_t>(slot) * rg.pitch + i0;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        long long acc_hi[4] = {0, 0, 0, 0}, acc_lo[4] = {0, 0, 0, 0};
+        if (kFixed)
+        {
+            longlong2 *a = reinterpret_cast<longlong2 *>(rg.v64 + ro);
+            longlong2 *b = reinterpret_cast<longlong2 *>(rg.v64lo + ro);
+            const longlong2 x = a[0], y = a[1], xl = b[0], yl = b[1];
+            acc_hi[0] = x.x;
+            acc_hi[1] = x.y;
+            acc_hi[2] = y.x;
+            acc_hi[3] = y.y;
+            acc_lo[0] = xl.x;
+            acc_lo[1] = xl.y;
+            acc_lo[2] = yl.x;
+            acc_lo[3] = yl.y;
+            a[0] = a[1] = b[0] = b[1] = make_longlong2(0, 0);
+        }
+        else
+        {
+            acc = ld4(rg.v32, ro);
+            st4(rg.v32, ro, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
+        float4 gin = make_float4(0.f, 0.f, 0.f, 0.f), din = gin;
+        if (rg.g)
+        {
+            gin = ld4(rg.g, ro);
+            st4(rg.g, ro, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
+        if (rg.dopa)
+        {
+            din = ld4(rg.dopa, ro);
+            st4(rg.dopa, ro, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
+        uint32_t forced_bits = 0;
+        if (rg.forced)
+        {
+            uint32_t *wp = rg.forced + static_cast<size_t>(slot) * rg.words + (i0 >> 5);
+            forced_bits = (*wp >> (i0 & 31)) & 0xFu;
+            if (forced_bits) atomicAnd(wp, ~(0xFu << (i0 & 31)));
+        }
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 V = (f & kLiveVRead) ? ld4(p.V, i0) : z;
+        float4 thr_dyn = (f & kLiveThrDyn) ? ld4(p.thr_dyn, i0) : z;
+        float4 trace = (f & kLiveTrace) ? ld4(p.trace, i0) : z;
+        float4 g = (f & kLiveG) ? ld4(p.g, i0) : z;
+        float4 dopa = ((f & kLiveDopa) && !(f & kResource)) ? ld4(p.dopa, i0) : z;
+        float4 add_thr = (f & kLiveAddThr) ? ld4(p.add_thr, i0) : z;
+        uint4 ns = (f & kLiveRefract) ? ld4u(p.n_since, i0) : make_uint4(0, 0, 0, 0);
+        uint4 phase = (f & kLiveBurst) ? ld4u(p.burst_phase, i0) : make_uint4(0, 0, 0, 0);
+        float4 vpre;
+        const uint4 ns_old = ns;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const uint32_t i = i0 + k;
+            if (i >= p.n) break;
+            NeuronState s;
+            s.V = at(V, k);
+            s.thr_dyn = at(thr_dyn, k);
+            s.trace = at(trace, k);
+            s.g = at(g, k);
+            s.dopa = at(dopa, k);
+            s.add_thr = at(add_thr, k);
+            s.ns = at(ns, k);
+            s.phase = at(phase, k);
+            s.block = (f & kLiveBlock) ? p.blocking[i] : 0;
+            const bool spike = blifat_step<kFixed>(p, i, t, s, at(acc, k), acc_hi[k], acc_lo[k], at(gin, k), at(din, k));
+            if (spike) mask |= 1u << k;
+            if (f & kResource)
+                resource_step(p, i, t, spike, (forced_bits >> k) & 1u, s.dopa, s.add_thr);
+            at(V, k) = s.V;
+            at(vpre, k) = s.V_pre;
+            at(thr_dyn, k) = s.thr_dyn;
+            at(trace, k) = s.trace;
+            at(g, k) = s.g;
+            at(dopa, k) = s.dopa;
+            at(add_thr, k) = s.add_thr;
+            at(ns, k) = s.ns;
+            at(phase, k) = s.phase;
+            if (f & kLiveBlock) p.blocking[i] = s.block;
+        }
+        // Padding lanes beyond n write their (unused) slots too; the arrays are padded to n_pad.
+        st4(p.V, i0, V);
+        if (f & kLiveVPre) st4(p.V_pre, i0, vpre);
+        if (f & kLiveThrDyn) st4(p.thr_dyn, i0, thr_dyn);
+        if (f & kLiveTrace) st4(p.trace, i0, trace);
+        if (f & kLiveG) st4(p.g, i0, g);
+        if ((f & kLiveDopa) || (f & kResource)) st4(p.dopa, i0, dopa);
+        if ((f & kLiveAddThr) || (f & kResource)) st4(p.add_thr, i0, add_thr);
+        if (f & kLiveRefract)
+            st4u(p.n_since, i0, ns);
+        else if (mask)
+        {
+            // Lazy refractory tracking: record the step of the last spike.
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (mask & (1u << k)) p.n_since[i0 + k] = at(ns, k);
+        }
+        (void)ns_old;
+        if (f & kLiveBurst) st4u(p.burst_phase, i0, phase);
+    }
+    return mask;
+}
+
+// Steps neurons i0 .. i0 + 3 of a LIF population at step t; returns their spike mask.
+__device__ __forceinline__ uint32_t lif_quad(const LifDev &p, unsigned long long t, uint32_t i0)
+{
+    uint32_t mask = 0;
+    if (i0 < p.n)
+    {
+        const RingView &rg = p.ring;
+        const uint32_t slot = static_cast<uint32_t>(t % rg.slots);
+        const size_t ro = static_cast<size_t>(slot) * rg.pitch + i0;
+        float4 acc = ld4(rg.v32, ro);
+        st4(rg.v32, ro, make_float4(0.f, 0.f, 0.f, 0.f));
+        float4 V = ld4(p.V, i0);
+        uint4 rc = ld4u(p.refract, i0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const uint32_t i = i0 + k;
+            if (i >= p.n) break;
+            float v = at(V, k);
+            uint32_t r = at(rc, k);
+            // lif_impl.h:33-86: leak and impacts only outside the refractory period; strict '>'.
+            if (r == 0u)
+            {
+                v = __fmul_rn(v, pf(p.leak, i));
+                v = __fadd_rn(v, at(acc, k));
+                if (v > pf(p.thr, i))
+                {
+                    v = pf(p.v_reset, i);
+                    r = pu(p.refract_period, i);
+                    mask |= 1u << k;
+                }
+            }
+            else
+            {
+                --r;
+            }
+            at(V, k) = v;
+            at(rc, k) = r;
+        }
+        st4(p.V, i0, V);
+        st4u(p.refract, i0, rc);
+    }
+    return mask;
+}
+
+}  // namespace
+}  // namespace knp_gb300

@@ -1,0 +1,177 @@
+// Fused step kernel for small networks: one thread-block cluster runs whole steps of every
+// population, projection and STDP rule of a backend, `n_steps` steps per launch, with the phases of
+// a step separated by cluster barriers instead of kernel boundaries.
+//
+// A step of the per-phase path is five to six dependent launches (population, scatter per
+// projection, STDP append and modify, end of step); below ~10^4 neurons each phase is a few
+// microseconds of latency and the launches, not the work, set the step time. Here the phases run
+// in the order of the single-threaded backend's step (backend.cpp:89-141 of the reference:
+// populations, then projections, then the STDP rules, then the end of step) inside one cluster of
+// up to 8 CTAs on 8 SMs (enough warps to keep the scatter's dependent loads of many rows in flight),
+// so no phase waits for a launch and no wait spins: every ordering is a hardware cluster barrier
+// (barrier.cluster arrive.release / wait.acquire, which also orders the CTAs' global-memory
+// accesses) or a block barrier.
+//
+// The per-neuron, per-synapse and per-column code is the per-phase kernels' own (population_dev.cuh,
+// projection_dev.cuh, stdp_dev.cuh), and the cluster walks the same device layout, so results are
+// those of the per-phase path. Only projections without a gather layout take part (the host selects
+// this kernel only then).
+#include <cstdint>
+
+#include "kernels.h"
+#include "population_dev.cuh"
+#include "projection_dev.cuh"
+#include "stdp_dev.cuh"
+#include "tcgen05.cuh"
+
+namespace knp_gb300
+{
+namespace
+{
+
+constexpr int kSmallThreads = 512;
+constexpr uint32_t kSmallWarps = kSmallThreads / 32;
+
+template <bool kFixed, bool kUniformExc>
+__device__ __forceinline__ unsigned long long scatter_one(const ProjectionDev &p, unsigned long long t, uint32_t warp,
+                                                          uint32_t n_warps, int lane)
+{
+    const uint32_t *idx[kMaxSources];
+    uint32_t cnt[kMaxSources];
+    const uint32_t total = resolve_sources(p, t, idx, cnt);
+    const uint32_t slot_base = static_cast<uint32_t>(t % p.ring.slots);
+    return scatter_rows<kFixed, kUniformExc>(p, slot_base, idx, cnt, total, warp, n_warps, lane);
+}
+
+// Launched as one cluster of C CTAs (C = cluster size, 1 to 8); every thread of the cluster passes
+// the same sequence of cluster barriers (all loop bounds below are the same in every thread).
+__global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet net, Control *ctl, uint32_t n_steps)
+{
+    __shared__ unsigned long long s_spikes;
+    const int lane = threadIdx.x & 31;
+    const uint32_t C = gridDim.x;
+    const uint32_t rank = blockIdx.x;
+    const uint32_t gthread = rank * kSmallThreads + threadIdx.x, n_threads = C * kSmallThreads;
+    const uint32_t gwarp = gthread >> 5, n_warps = C * kSmallWarps;
+    if (threadIdx.x == 0) s_spikes = 0;
+    unsigned long long t = ctl->step;
+    unsigned long long events = 0;
+    // Every CTA has read the step number before CTA 0 may advance it (at the end).
+    tc::cluster_sync();
+    for (uint32_t s = 0; s < n_steps; ++s, ++t)
+    {
+        // Populations (each pass of the cluster covers 4 * n_threads neurons; each CTA compacts
+        // its own spikes into the list).
+        for (uint32_t k = 0; k < net.n_pops; ++k)
+        {
+            const SmallPop &q = net.pops[k];
+            if (q.kind == kSmallLif)
+            {
+                const LifDev &p = q.lif;
+                for (uint32_t base = 0; base < p.n; base += 4 * n_threads)
+                {
+                    const uint32_t i0 = base + 4 * gthread;
+                    const uint32_t mask = lif_quad(p, t, i0);
+                    emit_spikes<kSmallThreads>(mask, i0, p.spikes, p.spike_count,
+                                               record_slot(p.rec_bits, p.rec_words, p.rec_slots, t), p.rec_words);
+                }
+            }
+            else
+            {
+                const BlifatDev &p = q.blifat;
+                for (uint32_t base = 0; base < p.n; base += 4 * n_threads)
+                {
+                    const uint32_t i0 = base + 4 * gthread;
+                    const uint32_t mask = p.ring.fixed ? blifat_quad<true>(p, t, i0) : blifat_quad<false>(p, t, i0);
+                    emit_spikes<kSmallThreads>(mask, i0, p.spikes, p.spike_count,
+                                               record_slot(p.rec_bits, p.rec_words, p.rec_slots, t), p.rec_words);
+                }
+            }
+        }
+        tc::cluster_sync();
+        // Projections: every warp of the cluster walks its share of each projection's spike rows.
+        for (uint32_t k = 0; k < net.n_projs; ++k)
+        {
+            const ProjectionDev &p = net.projs[k];
+            if (p.n_src == 0) continue;
+            const bool uexc = !p.type && p.uniform_type == 0;
+            unsigned long long ev;
+            if (p.ring.fixed)
+                ev = uexc ? scatter_one<true, true>(p, t, gwarp, n_warps, lane)
+                          : scatter_one<true, false>(p, t, gwarp, n_warps, lane);
+            else
+                ev = uexc ? scatter_one<false, true>(p, t, gwarp, n_warps, lane)
+                          : scatter_one<false, false>(p, t, gwarp, n_warps, lane);
+            events += ev;
+        }
+        tc::cluster_sync();
+        // STDP rules: the sources' appends in order, then the weight update of full columns.
+        for (uint32_t k = 0; k < net.n_stdp; ++k)
+        {
+            const SmallStdp &r = net.stdp[k];
+            for (uint32_t j = 0; j < r.n_src; ++j)
+            {
+                stdp_append_range(r.d, r.src[j], r.both[j], t, gthread, n_threads);
+                tc::cluster_sync();
+            }
+            stdp_modify_range(r.d, gwarp, n_warps, lane);
+        }
+        if (net.n_stdp) tc::cluster_sync();
+        // End of step: spike counts into the total, this step's counters zeroed.
+        for (uint32_t k = gthread; k < net.end.n_zero_u32; k += n_threads)
+        {
+            if (k < net.end.n_spike_counts) atomicAdd(&s_spikes, static_cast<unsigned long long>(net.end.zero_u32[k]));
+            net.end.zero_u32[k] = 0;
+        }
+        tc::cluster_sync();
+    }
+    if (lane == 0 && events) atomicAdd(&ctl->events_total, events);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_spikes) atomicAdd(&ctl->spikes_total, s_spikes);
+    if (rank == 0 && threadIdx.x == 0) ctl->step = t;
+}
+
+}  // namespace
+
+int small_net_cluster()
+{
+    static int c = [] {
+        cudaLaunchConfig_t cfg{};
+        cfg.blockDim = dim3(kSmallThreads);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        for (int size = 8; size > 1; size /= 2)
+        {
+            cfg.gridDim = dim3(size);
+            attr[0].val.clusterDim.x = size;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveClusters(&n, small_net_kernel, &cfg) == cudaSuccess && n > 0) return size;
+            cudaGetLastError();
+        }
+        return 1;
+    }();
+    return c;
+}
+
+cudaError_t launch_small_net(const SmallNet &net, Control *ctl, uint32_t n_steps, int cluster, cudaStream_t s)
+{
+    if (!n_steps) return cudaSuccess;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(kSmallThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, small_net_kernel, net, ctl, n_steps);
+}
+
+}  // namespace knp_gb300

@@ -16,6 +16,7 @@
 #include <cstdint>
 
 #include "kernels.h"
+#include "stdp_dev.cuh"
 
 namespace knp_gb300
 {
@@ -25,99 +26,15 @@ namespace
 __global__ void stdp_append_kernel(StdpDev d, SpikeSource src, int both_lists, Control *ctl)
 {
     pdl_begin();
-    const unsigned long long t = ctl->step;
-    const uint32_t *idx;
-    uint32_t cnt;
-    if (src.channel)
-    {
-        const ChannelDev &c = *src.channel;
-        if (t >= c.first_step && t - c.first_step < c.n_steps)
-        {
-            const unsigned long long k = t - c.first_step;
-            idx = c.idx + c.offsets[k];
-            cnt = static_cast<uint32_t>(c.offsets[k + 1] - c.offsets[k]);
-        }
-        else
-        {
-            return;
-        }
-    }
-    else
-    {
-        idx = src.idx;
-        cnt = *src.count;
-    }
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
-    {
-        const uint32_t col = idx[k];
-        if (col >= d.n_cols) continue;
-        const uint32_t tt = static_cast<uint32_t>(t);
-        uint32_t c = d.post_cnt[col];
-        if (c < d.period)
-        {
-            d.post_hist[static_cast<size_t>(col) * d.period + c] = tt;
-            d.post_cnt[col] = c + 1;
-        }
-        if (both_lists)
-        {
-            c = d.pre_cnt[col];
-            if (c < d.period)
-            {
-                d.pre_hist[static_cast<size_t>(col) * d.period + c] = tt;
-                d.pre_cnt[col] = c + 1;
-            }
-        }
-        if (d.touched_stamp[col] != t + 1)
-        {
-            d.touched_stamp[col] = t + 1;
-            d.touched[atomicAdd(d.touched_count, 1u)] = col;
-        }
-    }
+    stdp_append_range(d, src, both_lists, ctl->step, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // One warp per touched column.
 __global__ void stdp_modify_kernel(StdpDev d, Control *ctl)
 {
     pdl_begin();
-    const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t n = *d.touched_count;
-    for (uint32_t k = warp; k < n; k += n_warps)
-    {
-        const uint32_t col = d.touched[k];
-        if (d.pre_cnt[col] < d.period || d.post_cnt[col] < d.period) continue;
-        float wj = 0.0f;
-        if (lane == 0)
-        {
-            const uint32_t *pre = d.pre_hist + static_cast<size_t>(col) * d.period;
-            const uint32_t *post = d.post_hist + static_cast<size_t>(col) * d.period;
-            for (uint32_t a = 0; a < d.period; ++a)
-            {
-                const uint32_t tf = pre[a];
-                for (uint32_t b = 0; b < d.period; ++b)
-                {
-                    const uint32_t tn = post[b];
-                    if (tn < tf) continue;  // term is exactly +0
-                    const uint32_t diff = tn - tf;
-                    if (diff < d.table_len) wj = __fadd_rn(wj, d.table[diff]);
-                }
-            }
-        }
-        wj = __shfl_sync(0xffffffffu, wj, 0);
-        const long long a = d.col_ptr[col], b = d.col_ptr[col + 1];
-        for (long long e = a + lane; e < b; e += 32)
-        {
-            const uint64_t pos = d.col_pos[e];
-            d.w[pos] = __fadd_rn(d.w[pos], wj);
-        }
-        __syncwarp();
-        if (lane == 0)
-        {
-            d.pre_cnt[col] = 0;
-            d.post_cnt[col] = 0;
-        }
-    }
+    stdp_modify_range(d, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5,
+                      threadIdx.x & 31);
 }
 
 __global__ void step_end_kernel(StepEnd e, uint32_t n_spike_counts, Control *ctl)

@@ -21,12 +21,18 @@ def _gpu():
     return B
 
 
-def run_both(net, scheds, steps, record=None, device_schedule=False, on_step=None):
+# Step modes: AUTO takes the fused step kernel (one CTA cluster) for the small networks of these tests;
+# PHASES keeps the per-phase kernels (population, scatter, STDP, end of step) for the same network.
+MODES = {"auto": T.STEP_AUTO, "phases": T.STEP_PHASES}
+
+
+def run_both(net, scheds, steps, record=None, device_schedule=False, on_step=None, step_mode=None):
     from oracle import oracle as orc
 
     B = _gpu()
     g, b = B.run(net, scheds, steps, record=record, device_schedule=device_schedule,
-                 on_step=None if on_step is None else (lambda be, t: on_step(be, t, "gpu")))
+                 on_step=None if on_step is None else (lambda be, t: on_step(be, t, "gpu")),
+                 step_mode=None if step_mode is None else MODES[step_mode])
     o, oo = orc.run(net, scheds, steps, record=record,
                     on_step=None if on_step is None else (lambda be, t: on_step(be, t, "oracle")))
     return g, b, o, oo
@@ -57,11 +63,13 @@ def assert_same_state(b, oo, pop, rtol=0.0):
         np.testing.assert_array_equal(gext["free_synaptic_resource"], oext["free_synaptic_resource"])
 
 
+@pytest.mark.parametrize("mode", ["auto", "phases"])
 @pytest.mark.parametrize("kind", ["delta", "stdp", "stdp_resource_neuron"])
-def test_smallest_network_golden(kind):
+def test_smallest_network_golden(kind, mode):
     """knp/tests/backend/single_thread_cpu_test.cpp:54-176 through the C ABI."""
     net, sched = N.smallest_network(kind)
-    g, b, o, oo = run_both(net, sched, 20)
+    g, b, o, oo = run_both(net, sched, 20, step_mode=mode)
+    assert b.fused == (mode == "auto")
     pop = net.populations[0].uid
     assert [t for t, s in enumerate(g[pop]) if s.size] == GOLDEN
     assert_same_spikes(g, o)
@@ -72,12 +80,14 @@ def test_smallest_network_golden(kind):
     assert_same_state(b, oo, pop)
 
 
+@pytest.mark.parametrize("mode", ["auto", "phases"])
 @pytest.mark.parametrize("device_schedule", [False, True])
-def test_small_network_bit_exact(device_schedule):
+def test_small_network_bit_exact(device_schedule, mode):
     """Plain small config: 1000 BLIFAT, 100 Bernoulli inputs, all-to-all input and p=0.1 recurrent
     projections with dyadic weights, 1000 steps: spikes bit-exact every step."""
     net, sched = N.small_network(seed=1, steps=1000)
-    g, b, o, oo = run_both(net, sched, 1000, device_schedule=device_schedule)
+    g, b, o, oo = run_both(net, sched, 1000, device_schedule=device_schedule, step_mode=mode)
+    assert b.fused == (mode == "auto")
     assert_same_spikes(g, o)
     assert_same_state(b, oo, net.populations[0].uid)
     ev, sp, upd = b.counters()
@@ -343,10 +353,12 @@ def test_device_bernoulli_schedule_matches_host():
         np.testing.assert_array_equal(b1.spikes(pop, t), o[pop][t])
 
 
-def test_stdp_reduced():
+@pytest.mark.parametrize("mode", ["auto", "phases"])
+def test_stdp_reduced(mode):
     """STDP config with 10 samples x 100 steps: spikes bit-exact, weights bit-exact."""
     net, sched = N.stdp_network(seed=3, samples=10, steps_per_sample=100)
-    g, b, o, oo = run_both(net, sched, 1000)
+    g, b, o, oo = run_both(net, sched, 1000, step_mode=mode)
+    assert b.fused == (mode == "auto")
     assert_same_spikes(g, o)
     for pr in net.projections:
         np.testing.assert_array_equal(b.read_weights(pr.uid), oo.weights(pr.uid))
@@ -419,7 +431,8 @@ def test_external_impacts_and_channels():
     del rng
 
 
-def test_delay_zero_and_inhibitory_types():
+@pytest.mark.parametrize("mode", ["auto", "phases"])
+def test_delay_zero_and_inhibitory_types(mode):
     """Delay-0 synapses create events that are never delivered; INHIBITORY_CURRENT subtracts."""
     n = 64
     pop = N.Population(T.uid_from_int(11), T.BLIFAT, T.blifat_defaults(n))
@@ -432,13 +445,14 @@ def test_delay_zero_and_inhibitory_types():
     pr = N.Projection(T.uid_from_int(12), T.DELTA, T.NULL_UID, pop.uid, pre, post, w, d, ty)
     net = N.Network([pop], [pr], [(pr.uid, chan)])
     sched = N.bernoulli_schedule(chan, 3, 8, 40, 0.5)
-    g, b, o, oo = run_both(net, [sched], 40)
+    g, b, o, oo = run_both(net, [sched], 40, step_mode=mode)
     assert_same_spikes(g, o)
     assert b.counters()[0] == oo.events
     assert_same_state(b, oo, pop.uid)
 
 
-def test_stdp_only_and_multiple_sources():
+@pytest.mark.parametrize("mode", ["auto", "phases"])
+def test_stdp_only_and_multiple_sources(mode):
     """An STDP projection whose presynaptic population is also an STDP-only population: its spikes
     are emptied before propagation (additive_stdp.h:162-166) and never update weights."""
     n = 32
@@ -455,7 +469,7 @@ def test_stdp_only_and_multiple_sources():
                            stdp_populations={a.uid: T.STDP_ONLY, c.uid: T.STDP_AND_SPIKE})
     net = N.Network([a, c], [drive, plastic], [(drive.uid, chan)])
     sched = N.bernoulli_schedule(chan, 4, n, 80, 0.3)
-    g, b, o, oo = run_both(net, [sched], 80)
+    g, b, o, oo = run_both(net, [sched], 80, step_mode=mode)
     assert_same_spikes(g, o)
     np.testing.assert_array_equal(b.read_weights(plastic.uid), oo.weights(plastic.uid))
 
@@ -546,3 +560,39 @@ def test_errors_are_reported():
         b._init()
     with pytest.raises(KnpGb300Error):
         b.step(1)
+
+
+def test_step_mode_selection_and_recording_change():
+    """Step modes: an unknown mode and a fused mode forced on a network above the fused kernel's
+    size are refused; a recording switched on mid-run under the fused kernel (its descriptors
+    uploaded again) gives the oracle's spikes from that step on."""
+    from oracle import oracle as orc
+    from knp_gb300 import backend as B
+    from knp_gb300._capi import KnpGb300Error
+
+    b = B.GB300Backend()
+    with pytest.raises(KnpGb300Error):
+        b.set_step_mode(7)
+    big = N.Population(T.uid_from_int(41), T.BLIFAT, T.blifat_defaults(20_000))
+    b.load_populations([big])
+    b.set_step_mode(T.STEP_FUSED)
+    with pytest.raises(KnpGb300Error):
+        b._init()
+
+    net, sched = N.small_network(seed=5, steps=100)
+    pop = net.populations[0].uid
+    o, _ = orc.run(net, sched, 100)
+    b = B.GB300Backend()
+    b.load_network(net, record=[])
+    b.set_step_mode(T.STEP_FUSED)
+    b._init()
+    assert b.fused
+    with pytest.raises(KnpGb300Error):
+        b.set_step_mode(T.STEP_PHASES)
+    for s in sched:
+        b.load_spike_schedule(s)
+    b.step(50)
+    b.record_spikes(pop, True)
+    b.step(50)
+    for t in range(50, 100):
+        np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t])
