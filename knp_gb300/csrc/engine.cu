@@ -982,53 +982,78 @@ bool Backend::small_net_eligible(std::string &why) const
     return true;
 }
 
-// Uploads the device descriptors of the fused kernel (again after a change of recording).
+// Uploads the device descriptors of the fused kernel (again after a change of recording): set 0
+// with the per-step counters of the per-phase kernels, set 1 the same with a second counter array.
 void Backend::build_small_net()
 {
-    std::vector<SmallPop> pops;
-    for (auto &q : pops_)
-    {
-        SmallPop sp{};
-        sp.kind = q->kind == KNP_NEURON_LIF ? kSmallLif : kSmallBlifat;
-        sp.blifat = q->bdev;
-        sp.lif = q->ldev;
-        pops.push_back(sp);
-    }
-    std::vector<ProjectionDev> projs;
-    std::vector<SmallStdp> rules;
-    for (auto &p : projs_)
-    {
-        if (p->dev.n_src) projs.push_back(p->dev);
-        if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
-        if (p->stdp_sources.size() > static_cast<size_t>(kMaxSources))
-            throw Error(KNP_GB300_E_INVALID, "too many STDP populations for one projection");
-        SmallStdp r{};
-        r.d = p->stdp;
-        for (auto &[src, both] : p->stdp_sources)
-        {
-            r.src[r.n_src] = src;
-            r.both[r.n_src] = both;
-            ++r.n_src;
-        }
-        rules.push_back(r);
-    }
     small_cluster_ = small_net_cluster();
-    if (!small_.pops)
+    if (!counters_alt_) counters_alt_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
+    for (int set = 0; set < 2; ++set)
     {
-        small_.pops = arena_.make<SmallPop>(std::max<size_t>(pops.size(), 1));
-        small_.projs = arena_.make<ProjectionDev>(std::max<size_t>(projs.size(), 1));
-        small_.stdp = arena_.make<SmallStdp>(std::max<size_t>(rules.size(), 1));
+        uint32_t *base = set ? counters_alt_ : counters_;
+        auto cnt = [&](const uint32_t *c) -> uint32_t * {
+            if (c >= counters_ && c < counters_ + n_counters_) return base + (c - counters_);
+            return const_cast<uint32_t *>(c);
+        };
+        std::vector<SmallPop> pops;
+        for (auto &q : pops_)
+        {
+            SmallPop sp{};
+            sp.kind = q->kind == KNP_NEURON_LIF ? kSmallLif : kSmallBlifat;
+            sp.blifat = q->bdev;
+            sp.lif = q->ldev;
+            sp.blifat.spike_count = cnt(sp.blifat.spike_count);
+            sp.lif.spike_count = cnt(sp.lif.spike_count);
+            pops.push_back(sp);
+        }
+        std::vector<ProjectionDev> projs;
+        std::vector<SmallStdp> rules;
+        for (auto &p : projs_)
+        {
+            if (p->dev.n_src)
+            {
+                ProjectionDev d = p->dev;
+                for (int k = 0; k < d.n_src; ++k) d.src[k].count = cnt(d.src[k].count);
+                projs.push_back(d);
+            }
+            if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
+            if (p->stdp_sources.size() > static_cast<size_t>(kMaxSources))
+                throw Error(KNP_GB300_E_INVALID, "too many STDP populations for one projection");
+            SmallStdp r{};
+            r.d = p->stdp;
+            r.d.touched_count = cnt(r.d.touched_count);
+            for (auto &[src, both] : p->stdp_sources)
+            {
+                r.src[r.n_src] = src;
+                r.src[r.n_src].count = cnt(src.count);
+                r.both[r.n_src] = both;
+                ++r.n_src;
+            }
+            rules.push_back(r);
+        }
+        if (!small_.pops[0])
+        {
+            small_.n_pops = static_cast<uint32_t>(pops.size());
+            small_.n_projs = static_cast<uint32_t>(projs.size());
+            small_.n_stdp = static_cast<uint32_t>(rules.size());
+            SmallPop *dp = arena_.make<SmallPop>(2 * std::max<size_t>(pops.size(), 1));
+            ProjectionDev *dj = arena_.make<ProjectionDev>(2 * std::max<size_t>(projs.size(), 1));
+            SmallStdp *ds = arena_.make<SmallStdp>(2 * std::max<size_t>(rules.size(), 1));
+            for (int k = 0; k < 2; ++k)
+            {
+                small_.pops[k] = dp + k * std::max<size_t>(pops.size(), 1);
+                small_.projs[k] = dj + k * std::max<size_t>(projs.size(), 1);
+                small_.stdp[k] = ds + k * std::max<size_t>(rules.size(), 1);
+            }
+        }
+        small_.end[set] = StepEnd{base, n_counters_, n_spike_counters_};
+        KNP_CUDA(cudaMemcpy(const_cast<SmallPop *>(small_.pops[set]), pops.data(), pops.size() * sizeof(SmallPop),
+                            cudaMemcpyHostToDevice));
+        KNP_CUDA(cudaMemcpy(const_cast<ProjectionDev *>(small_.projs[set]), projs.data(),
+                            projs.size() * sizeof(ProjectionDev), cudaMemcpyHostToDevice));
+        KNP_CUDA(cudaMemcpy(const_cast<SmallStdp *>(small_.stdp[set]), rules.data(), rules.size() * sizeof(SmallStdp),
+                            cudaMemcpyHostToDevice));
     }
-    small_.n_pops = static_cast<uint32_t>(pops.size());
-    small_.n_projs = static_cast<uint32_t>(projs.size());
-    small_.n_stdp = static_cast<uint32_t>(rules.size());
-    small_.end = StepEnd{counters_, n_counters_, n_spike_counters_};
-    KNP_CUDA(cudaMemcpy(const_cast<SmallPop *>(small_.pops), pops.data(), pops.size() * sizeof(SmallPop),
-                        cudaMemcpyHostToDevice));
-    KNP_CUDA(cudaMemcpy(const_cast<ProjectionDev *>(small_.projs), projs.data(), projs.size() * sizeof(ProjectionDev),
-                        cudaMemcpyHostToDevice));
-    KNP_CUDA(cudaMemcpy(const_cast<SmallStdp *>(small_.stdp), rules.data(), rules.size() * sizeof(SmallStdp),
-                        cudaMemcpyHostToDevice));
 }
 
 // ------------------------------------------------------------------------------------ stepping

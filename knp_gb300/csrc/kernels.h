@@ -264,13 +264,17 @@ struct SmallStdp
     SpikeSource src[kMaxSources];
     int both[kMaxSources];  // the source fills both histories (STDPAndSpike)
 };
+// Two descriptor sets that differ only in their per-step counters (spike counts, STDP touched
+// counts): step t uses set t & 1, so the counters of step t - 1 are read and zeroed while step t
+// runs, and a step needs no end-of-step phase. Set 0 uses the per-phase kernels' counters; both
+// sets are zero between launches.
 struct SmallNet
 {
-    const SmallPop *pops;
-    const ProjectionDev *projs;
-    const SmallStdp *stdp;
+    const SmallPop *pops[2];
+    const ProjectionDev *projs[2];
+    const SmallStdp *stdp[2];
     uint32_t n_pops, n_projs, n_stdp;
-    StepEnd end;
+    StepEnd end[2];
 };
 
 // ---------------------------------------------------------------- launchers (stream-ordered)

@@ -6,7 +6,7 @@
 // projection, STDP append and modify, end of step); below ~10^4 neurons each phase is a few
 // microseconds of latency and the launches, not the work, set the step time. Here the phases run
 // in the order of the single-threaded backend's step (backend.cpp:89-141 of the reference:
-// populations, then projections, then the STDP rules, then the end of step) inside one cluster of
+// populations, then projections, then the STDP rules) inside one cluster of
 // up to 8 CTAs on 8 SMs (enough warps to keep the scatter's dependent loads of many rows in flight),
 // so no phase waits for a launch and no wait spins: every ordering is a hardware cluster barrier
 // (barrier.cluster arrive.release / wait.acquire, which also orders the CTAs' global-memory
@@ -43,8 +43,21 @@ __device__ __forceinline__ unsigned long long scatter_one(const ProjectionDev &p
     return scatter_rows<kFixed, kUniformExc>(p, slot_base, idx, cnt, total, warp, n_warps, lane);
 }
 
+// Reads (into the CTA's spike total) and zeroes the per-step counters of one descriptor set.
+__device__ __forceinline__ void retire_counters(const StepEnd &e, uint32_t gthread, uint32_t n_threads,
+                                                unsigned long long *spikes)
+{
+    for (uint32_t k = gthread; k < e.n_zero_u32; k += n_threads)
+    {
+        const uint32_t v = e.zero_u32[k];
+        if (k < e.n_spike_counts && v) atomicAdd(spikes, static_cast<unsigned long long>(v));
+        if (v) e.zero_u32[k] = 0;
+    }
+}
+
 // Launched as one cluster of C CTAs (C = cluster size, 1 to 8); every thread of the cluster passes
 // the same sequence of cluster barriers (all loop bounds below are the same in every thread).
+// A step is: populations | projections | STDP rules, with a cluster barrier after each phase.
 __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet net, Control *ctl, uint32_t n_steps)
 {
     __shared__ unsigned long long s_spikes;
@@ -60,11 +73,18 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
     tc::cluster_sync();
     for (uint32_t s = 0; s < n_steps; ++s, ++t)
     {
+        // Descriptor set of this step (selects, not a dynamic index into the parameter block).
+        const bool odd = t & 1u;
+        const SmallPop *pops = odd ? net.pops[1] : net.pops[0];
+        const ProjectionDev *projs = odd ? net.projs[1] : net.projs[0];
+        const SmallStdp *rules = odd ? net.stdp[1] : net.stdp[0];
+        // The previous step's counters (the other set) are no longer read by anyone.
+        retire_counters(odd ? net.end[0] : net.end[1], gthread, n_threads, &s_spikes);
         // Populations (each pass of the cluster covers 4 * n_threads neurons; each CTA compacts
         // its own spikes into the list).
         for (uint32_t k = 0; k < net.n_pops; ++k)
         {
-            const SmallPop &q = net.pops[k];
+            const SmallPop &q = pops[k];
             if (q.kind == kSmallLif)
             {
                 const LifDev &p = q.lif;
@@ -92,7 +112,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
         // Projections: every warp of the cluster walks its share of each projection's spike rows.
         for (uint32_t k = 0; k < net.n_projs; ++k)
         {
-            const ProjectionDev &p = net.projs[k];
+            const ProjectionDev &p = projs[k];
             if (p.n_src == 0) continue;
             const bool uexc = !p.type && p.uniform_type == 0;
             unsigned long long ev;
@@ -105,26 +125,30 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
             events += ev;
         }
         tc::cluster_sync();
-        // STDP rules: the sources' appends in order, then the weight update of full columns.
-        for (uint32_t k = 0; k < net.n_stdp; ++k)
+        // STDP rules: a one-source rule appends and updates in one pass; otherwise the sources'
+        // appends in order, then the weight update of the touched columns that are full.
+        if (net.n_stdp)
         {
-            const SmallStdp &r = net.stdp[k];
-            for (uint32_t j = 0; j < r.n_src; ++j)
+            for (uint32_t k = 0; k < net.n_stdp; ++k)
             {
-                stdp_append_range(r.d, r.src[j], r.both[j], t, gthread, n_threads);
-                tc::cluster_sync();
+                const SmallStdp &r = rules[k];
+                if (r.n_src == 1 && !r.src[0].channel)
+                {
+                    stdp_append_update_range(r.d, r.src[0], r.both[0], t, gthread, n_threads);
+                    continue;
+                }
+                for (uint32_t j = 0; j < r.n_src; ++j)
+                {
+                    stdp_append_range(r.d, r.src[j], r.both[j], t, gthread, n_threads);
+                    tc::cluster_sync();
+                }
+                stdp_modify_range(r.d, gwarp, n_warps, lane);
             }
-            stdp_modify_range(r.d, gwarp, n_warps, lane);
+            tc::cluster_sync();
         }
-        if (net.n_stdp) tc::cluster_sync();
-        // End of step: spike counts into the total, this step's counters zeroed.
-        for (uint32_t k = gthread; k < net.end.n_zero_u32; k += n_threads)
-        {
-            if (k < net.end.n_spike_counts) atomicAdd(&s_spikes, static_cast<unsigned long long>(net.end.zero_u32[k]));
-            net.end.zero_u32[k] = 0;
-        }
-        tc::cluster_sync();
     }
+    // The last step's counters: both sets are zero between launches.
+    retire_counters(((t - 1) & 1u) ? net.end[1] : net.end[0], gthread, n_threads, &s_spikes);
     if (lane == 0 && events) atomicAdd(&ctl->events_total, events);
     __syncthreads();
     if (threadIdx.x == 0 && s_spikes) atomicAdd(&ctl->spikes_total, s_spikes);
