@@ -36,3 +36,31 @@ def test_binding_loads_and_reports_errors_without_gpu(lib_path):
 
 def test_library_is_built_for_sm_103a_only():
     assert kb.GENCODE == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_python_constants_match_header_enums():
+    """Every enumerator of the ABI headers has the same value in knp_gb300.types, and every declared
+    entry point has a ctypes signature in the binding."""
+    import os
+    import re
+
+    from knp_gb300 import types as T
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    prefixes = [("KNP_GB300_STEP_", "STEP_"), ("KNP_GB300_ACC_", "ACC_"), ("KNP_OUT_", ""), ("KNP_NEURON_", ""),
+                ("KNP_SYNAPSE_", ""), ("KNP_STDP_", "STDP_"), ("KNP_ISI_", "ISI_")]
+    seen = 0
+    for hdr in ("knp_gb300.h", "knp_gb300_types.h"):
+        with open(os.path.join(root, "include", hdr)) as f:
+            text = f.read()
+        for name, value in re.findall(r"\b(KNP_[A-Z0-9_]+)\s*=\s*(-?\d+)", text):
+            for c_prefix, py_prefix in prefixes:
+                if name.startswith(c_prefix):
+                    py = py_prefix + name[len(c_prefix):]
+                    assert getattr(T, py) == int(value), (name, py)
+                    seen += 1
+                    break
+    assert seen >= 20
+    lib = _capi.lib()
+    unbound = [s for s in _capi.exported_symbols() if getattr(lib, s).argtypes is None]
+    assert not unbound, unbound
