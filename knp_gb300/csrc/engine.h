@@ -1,11 +1,13 @@
 // Host runtime of the GB300 KNP backend: owns device memory, builds the device network at init,
-// records the step as a CUDA graph, stages external messages and drains spike recordings.
+// records the step as CUDA graphs of per-phase kernels (or, for small networks, launches the fused
+// step kernel), stages external messages and drains spike recordings.
 //
 // The step order is the single-threaded backend's (knp/backends/cpu/cpu-single-threaded-backend/
 // impl/backend.cpp:89-141): all populations (consume this step's ring slot, emit spikes), then all
 // projections (scatter this step's spikes into future ring slots), then additive-STDP updates
 // (after the scatter, as modify_weights follows impact construction in delta_impl.h:63-111), then the
-// end-of-step kernel. Internal SpikeMessages / SynapticImpactMessages never leave the device.
+// end-of-step kernel (per-phase path). Internal SpikeMessages / SynapticImpactMessages never leave
+// the device.
 #pragma once
 
 #include <atomic>
