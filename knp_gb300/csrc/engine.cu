@@ -1331,8 +1331,7 @@ void Backend::check_device_error()
     KNP_CUDA(cudaMemcpyAsync(&c, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, stream_));
     KNP_CUDA(cudaStreamSynchronize(stream_));
     if (c.error)
-        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(c.error) +
-                                                 (c.error & kErrLogOverflow ? " (spike recording overflow)" : ""));
+        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(c.error));
 }
 
 void Backend::alloc_recording(PopulationSlot &p)
@@ -1412,8 +1411,7 @@ void Backend::drain_recordings(uint64_t upto)
     KNP_CUDA(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, cs));
     KNP_CUDA(cudaStreamSynchronize(cs));
     if (ctl_host_->error)
-        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(ctl_host_->error) +
-                                                 (ctl_host_->error & kErrLogOverflow ? " (spike recording overflow)" : ""));
+        throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(ctl_host_->error));
 }
 
 namespace

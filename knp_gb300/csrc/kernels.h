@@ -28,20 +28,13 @@ namespace knp_gb300
 constexpr int kFxLoBits = 40;  // fixed-point input: value = hi * 2^-8 + lo * 2^-48
 constexpr int kMaxSources = 8;
 
-// Bits of Control::error.
-enum DeviceError : uint32_t
-{
-    kErrLogOverflow = 1u << 0,
-    kErrHistory = 1u << 1,
-};
-
 // Device-resident step control block (one per backend).
 struct Control
 {
     unsigned long long step;          // step being executed
     unsigned long long events_total;  // synaptic events (impacts created) since init
     unsigned long long spikes_total;  // spikes since init
-    unsigned int error;               // sticky DeviceError bits
+    unsigned int error;               // sticky error bits a kernel can report through; checked by the host
     unsigned int pad;
 };
 
