@@ -983,17 +983,32 @@ bool Backend::small_net_eligible(std::string &why) const
 }
 
 // Uploads the device descriptors of the fused kernel (again after a change of recording): set 0
-// with the per-step counters of the per-phase kernels, set 1 the same with a second counter array.
+// with the per-step counters and spike lists of the per-phase kernels, set 1 the same with a second
+// counter array and a second spike list per population.
 void Backend::build_small_net()
 {
     small_cluster_ = small_net_cluster();
-    if (!counters_alt_) counters_alt_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
+    if (!counters_alt_)
+    {
+        counters_alt_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
+        for (auto &q : pops_)
+        {
+            const uint32_t *list = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+            spikes_alt_.emplace_back(list, arena_.make<uint32_t>(std::max<uint32_t>(q->n_pad, 4), false));
+        }
+    }
     for (int set = 0; set < 2; ++set)
     {
         uint32_t *base = set ? counters_alt_ : counters_;
         auto cnt = [&](const uint32_t *c) -> uint32_t * {
             if (c >= counters_ && c < counters_ + n_counters_) return base + (c - counters_);
             return const_cast<uint32_t *>(c);
+        };
+        auto list = [&](const uint32_t *l) -> uint32_t * {
+            if (set && l)
+                for (auto &[a, b] : spikes_alt_)
+                    if (a == l) return b;
+            return const_cast<uint32_t *>(l);
         };
         std::vector<SmallPop> pops;
         for (auto &q : pops_)
@@ -1004,6 +1019,8 @@ void Backend::build_small_net()
             sp.lif = q->ldev;
             sp.blifat.spike_count = cnt(sp.blifat.spike_count);
             sp.lif.spike_count = cnt(sp.lif.spike_count);
+            sp.blifat.spikes = list(sp.blifat.spikes);
+            sp.lif.spikes = list(sp.lif.spikes);
             pops.push_back(sp);
         }
         std::vector<ProjectionDev> projs;
@@ -1013,7 +1030,11 @@ void Backend::build_small_net()
             if (p->dev.n_src)
             {
                 ProjectionDev d = p->dev;
-                for (int k = 0; k < d.n_src; ++k) d.src[k].count = cnt(d.src[k].count);
+                for (int k = 0; k < d.n_src; ++k)
+                {
+                    d.src[k].count = cnt(d.src[k].count);
+                    d.src[k].idx = list(d.src[k].idx);
+                }
                 projs.push_back(d);
             }
             if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA || p->n_syn == 0 || p->stdp_sources.empty()) continue;
@@ -1026,6 +1047,7 @@ void Backend::build_small_net()
             {
                 r.src[r.n_src] = src;
                 r.src[r.n_src].count = cnt(src.count);
+                r.src[r.n_src].idx = list(src.idx);
                 r.both[r.n_src] = both;
                 ++r.n_src;
             }

@@ -302,6 +302,7 @@ private:
     SmallNet small_{};
     int small_cluster_ = 1;  // CTAs of the fused kernel's cluster
     uint32_t *counters_alt_ = nullptr;  // the fused kernel's second set of per-step counters
+    std::vector<std::pair<const uint32_t *, uint32_t *>> spikes_alt_;  // spike list -> its second copy
     static constexpr uint64_t kSmallMaxNeurons = 16384;
     static constexpr uint64_t kSmallMaxSynapses = 1ull << 22;
     static constexpr uint64_t kSmallMaxStepsPerLaunch = 1ull << 16;

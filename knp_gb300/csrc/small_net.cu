@@ -55,9 +55,40 @@ __device__ __forceinline__ void retire_counters(const StepEnd &e, uint32_t gthre
     }
 }
 
+// The STDP rules of step t (descriptor set of step t): a one-source rule appends and updates in one
+// pass; otherwise the sources' appends in order, then the weight update of the touched columns that
+// are full. `thread` / `warp` are this thread's ids rotated by half the cluster, so that the rules'
+// work lands on other SMs than the first neurons' population work it runs beside.
+__device__ __forceinline__ void stdp_rules(const SmallStdp *rules, uint32_t n_rules, unsigned long long t,
+                                           uint32_t thread, uint32_t n_threads, int lane)
+{
+    const uint32_t warp = thread >> 5, n_warps = n_threads >> 5;
+    for (uint32_t k = 0; k < n_rules; ++k)
+    {
+        const SmallStdp &r = rules[k];
+        if (r.n_src == 1 && !r.src[0].channel)
+        {
+            stdp_append_update_range(r.d, r.src[0], r.both[0], t, thread, n_threads);
+            continue;
+        }
+        for (uint32_t j = 0; j < r.n_src; ++j)
+        {
+            stdp_append_range(r.d, r.src[j], r.both[j], t, thread, n_threads);
+            tc::cluster_sync();
+        }
+        stdp_modify_range(r.d, warp, n_warps, lane);
+    }
+}
+
 // Launched as one cluster of C CTAs (C = cluster size, 1 to 8); every thread of the cluster passes
 // the same sequence of cluster barriers (all loop bounds below are the same in every thread).
-// A step is: populations | projections | STDP rules, with a cluster barrier after each phase.
+// Step t is two phases, each closed by a cluster barrier:
+//   A: the populations of step t, beside the STDP rules of step t - 1 (they read step t - 1's spike
+//      lists and counters, the other descriptor set, and change weights no one reads in phase A);
+//   B: the projections of step t (reading the weights after step t - 1's STDP update, as the
+//      reference's order requires), beside the retirement of step t - 1's counters.
+// A launch ends with the STDP rules of its last step, so both descriptor sets' counters are zero and
+// every update is done between launches.
 __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet net, Control *ctl, uint32_t n_steps)
 {
     __shared__ unsigned long long s_spikes;
@@ -66,6 +97,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
     const uint32_t rank = blockIdx.x;
     const uint32_t gthread = rank * kSmallThreads + threadIdx.x, n_threads = C * kSmallThreads;
     const uint32_t gwarp = gthread >> 5, n_warps = C * kSmallWarps;
+    const uint32_t sthread = (gthread + n_threads / 2) % n_threads;
     if (threadIdx.x == 0) s_spikes = 0;
     unsigned long long t = ctl->step;
     unsigned long long events = 0;
@@ -73,13 +105,12 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
     tc::cluster_sync();
     for (uint32_t s = 0; s < n_steps; ++s, ++t)
     {
-        // Descriptor set of this step (selects, not a dynamic index into the parameter block).
+        // Descriptor sets of this step and of the previous one (selects, not a dynamic index into
+        // the parameter block).
         const bool odd = t & 1u;
         const SmallPop *pops = odd ? net.pops[1] : net.pops[0];
         const ProjectionDev *projs = odd ? net.projs[1] : net.projs[0];
-        const SmallStdp *rules = odd ? net.stdp[1] : net.stdp[0];
-        // The previous step's counters (the other set) are no longer read by anyone.
-        retire_counters(odd ? net.end[0] : net.end[1], gthread, n_threads, &s_spikes);
+        // ---- phase A
         // Populations (each pass of the cluster covers 4 * n_threads neurons; each CTA compacts
         // its own spikes into the list).
         for (uint32_t k = 0; k < net.n_pops; ++k)
@@ -108,7 +139,12 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
                 }
             }
         }
+        // The STDP rules of step t - 1 (done by the previous launch for its first step).
+        if (s > 0 && net.n_stdp) stdp_rules(odd ? net.stdp[0] : net.stdp[1], net.n_stdp, t - 1, sthread, n_threads, lane);
         tc::cluster_sync();
+        // ---- phase B
+        // Step t - 1's counters are no longer read by anyone.
+        retire_counters(odd ? net.end[0] : net.end[1], gthread, n_threads, &s_spikes);
         // Projections: every warp of the cluster walks its share of each projection's spike rows.
         for (uint32_t k = 0; k < net.n_projs; ++k)
         {
@@ -125,30 +161,15 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
             events += ev;
         }
         tc::cluster_sync();
-        // STDP rules: a one-source rule appends and updates in one pass; otherwise the sources'
-        // appends in order, then the weight update of the touched columns that are full.
-        if (net.n_stdp)
-        {
-            for (uint32_t k = 0; k < net.n_stdp; ++k)
-            {
-                const SmallStdp &r = rules[k];
-                if (r.n_src == 1 && !r.src[0].channel)
-                {
-                    stdp_append_update_range(r.d, r.src[0], r.both[0], t, gthread, n_threads);
-                    continue;
-                }
-                for (uint32_t j = 0; j < r.n_src; ++j)
-                {
-                    stdp_append_range(r.d, r.src[j], r.both[j], t, gthread, n_threads);
-                    tc::cluster_sync();
-                }
-                stdp_modify_range(r.d, gwarp, n_warps, lane);
-            }
-            tc::cluster_sync();
-        }
     }
-    // The last step's counters: both sets are zero between launches.
-    retire_counters(((t - 1) & 1u) ? net.end[1] : net.end[0], gthread, n_threads, &s_spikes);
+    // The last step's STDP rules, then its counters: both sets are zero between launches.
+    const bool last_odd = (t - 1) & 1u;
+    if (net.n_stdp)
+    {
+        stdp_rules(last_odd ? net.stdp[1] : net.stdp[0], net.n_stdp, t - 1, sthread, n_threads, lane);
+        tc::cluster_sync();
+    }
+    retire_counters(last_odd ? net.end[1] : net.end[0], gthread, n_threads, &s_spikes);
     if (lane == 0 && events) atomicAdd(&ctl->events_total, events);
     __syncthreads();
     if (threadIdx.x == 0 && s_spikes) atomicAdd(&ctl->spikes_total, s_spikes);
