@@ -258,9 +258,9 @@ struct SmallStdp
     int both[kMaxSources];  // the source fills both histories (STDPAndSpike)
 };
 // Two descriptor sets that differ only in their per-step counters (spike counts, STDP touched
-// counts): step t uses set t & 1, so the counters of step t - 1 are read and zeroed while step t
-// runs, and a step needs no end-of-step phase. Set 0 uses the per-phase kernels' counters; both
-// sets are zero between launches.
+// counts) and population spike lists: step t uses set t & 1, so step t - 1's STDP rules can read its
+// spikes, and its counters can be zeroed, while step t runs; a step needs no end-of-step phase. Set 0
+// uses the per-phase kernels' counters and lists; both sets' counters are zero between launches.
 struct SmallNet
 {
     const SmallPop *pops[2];

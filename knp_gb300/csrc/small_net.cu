@@ -4,13 +4,14 @@
 //
 // A step of the per-phase path is five to six dependent launches (population, scatter per
 // projection, STDP append and modify, end of step); below ~10^4 neurons each phase is a few
-// microseconds of latency and the launches, not the work, set the step time. Here the phases run
-// in the order of the single-threaded backend's step (backend.cpp:89-141 of the reference:
-// populations, then projections, then the STDP rules) inside one cluster of
-// up to 8 CTAs on 8 SMs (enough warps to keep the scatter's dependent loads of many rows in flight),
-// so no phase waits for a launch and no wait spins: every ordering is a hardware cluster barrier
-// (barrier.cluster arrive.release / wait.acquire, which also orders the CTAs' global-memory
-// accesses) or a block barrier.
+// microseconds of latency and the launches, not the work, set the step time. Here a step is two
+// phases inside one cluster of up to 8 CTAs on 8 SMs (enough warps to keep the scatter's dependent
+// loads of many rows in flight): the populations of step t beside the STDP rules of step t - 1,
+// then the projections of step t. That keeps the order of the single-threaded backend's step
+// (backend.cpp:89-141 of the reference: populations, projections, then the STDP rules, whose
+// weights the next step's projections read) for every datum, and no wait spins: every ordering is a
+// hardware cluster barrier (barrier.cluster arrive.release / wait.acquire, which also orders the
+// CTAs' global-memory accesses) or a block barrier.
 //
 // The per-neuron, per-synapse and per-column code is the per-phase kernels' own (population_dev.cuh,
 // projection_dev.cuh, stdp_dev.cuh), and the cluster walks the same device layout, so results are
