@@ -968,6 +968,11 @@ bool Backend::small_net_eligible(std::string &why) const
             why = "a projection has a gather layout";
             return false;
         }
+        if (p->stdp_pops.size() > static_cast<size_t>(kMaxSources))
+        {
+            why = "a projection has more than " + std::to_string(kMaxSources) + " STDP populations";
+            return false;
+        }
     }
     if (neurons > kSmallMaxNeurons)
     {
@@ -1238,7 +1243,10 @@ void Backend::step(uint64_t n)
         {
             stage_host_inputs();
             if (fused_)
+            {
+                if (!small_.pops[0]) throw Error(KNP_GB300_E_STATE, "the fused step kernel was not set up");
                 KNP_CUDA(launch_small_net(small_, ctl_, 1, small_cluster_, stream_));
+            }
             else
                 KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
             KNP_CUDA(cudaGetLastError());
@@ -1250,6 +1258,7 @@ void Backend::step(uint64_t n)
         uint64_t k = n;
         if (any_recording_) k = std::min<uint64_t>(k, steps_before_drain());
         uint64_t done = 0;
+        if (fused_ && !small_.pops[0]) throw Error(KNP_GB300_E_STATE, "the fused step kernel was not set up");
         while (fused_ && done < k)
         {
             const uint64_t m = std::min<uint64_t>(k - done, kSmallMaxStepsPerLaunch);
