@@ -158,7 +158,8 @@ KNP_GB300_API int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid pro
 /**
  * Step execution mode (before init). The fused mode runs every phase of a step, and many steps per
  * launch, in one thread-block cluster (up to 8 CTAs) with cluster barriers between the phases; it
- * takes networks of at most 16384 neurons and 2^22 synapses whose projections have no gather form.
+ * takes networks of at most 16384 neurons and 2^22 synapses whose projections have no gather form
+ * and at most 8 STDP populations each.
  * AUTO (the default) picks it for such networks. No reference counterpart: the reference's step driver is
  * SingleThreadedCPUBackend::_step (knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:89-141),
  * whose phase order both modes keep.
