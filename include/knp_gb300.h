@@ -57,9 +57,11 @@ typedef enum knp_gb300_accumulator
 /** How a step is executed (results are the same in every mode). */
 typedef enum knp_gb300_step_mode
 {
-    KNP_GB300_STEP_AUTO = 0,   /* fused when the network qualifies (see knp_gb300_set_step_mode), else phases */
+    KNP_GB300_STEP_AUTO = 0,   /* fused, else grid, when the network qualifies (see knp_gb300_set_step_mode), else phases */
     KNP_GB300_STEP_PHASES = 1, /* one kernel per phase (population, projection, STDP, end of step) in CUDA graphs */
-    KNP_GB300_STEP_FUSED = 2   /* one kernel (one CTA cluster) runs whole steps; init fails if the network does not qualify */
+    KNP_GB300_STEP_FUSED = 2,  /* one kernel (one CTA cluster) runs whole steps; init fails if the network does not qualify */
+    KNP_GB300_STEP_GRID = 3    /* one persistent cooperative kernel (one CTA per SM) runs whole steps, gather
+                                  form included; init fails if the network does not qualify */
 } knp_gb300_step_mode;
 
 /** Message text of the last failed call on this thread (never NULL). */
@@ -159,15 +161,22 @@ KNP_GB300_API int knp_gb300_set_pull_threshold(knp_gb300_backend *b, knp_uid pro
  * Step execution mode (before init). The fused mode runs every phase of a step, and many steps per
  * launch, in one thread-block cluster (up to 8 CTAs) with cluster barriers between the phases; it
  * takes networks of at most 16384 neurons and 2^22 synapses whose projections have no gather form
- * and at most 8 STDP populations each.
- * AUTO (the default) picks it for such networks. No reference counterpart: the reference's step driver is
+ * and at most 8 STDP populations each. The grid mode runs every phase of a step, and many steps per
+ * launch, in one cooperative launch of one 1024-thread CTA per SM with bounded grid barriers
+ * between the phases (gather form included); it takes networks whose projections have at most 8 STDP
+ * populations each, with at most 8 gather-form projections whose shared memory fits one CTA.
+ * AUTO (the default) picks the fused mode for networks it takes, else the grid mode for networks it
+ * takes, else the per-phase kernels. No reference counterpart: the reference's step driver is
  * SingleThreadedCPUBackend::_step (knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:89-141),
- * whose phase order both modes keep.
+ * whose phase order every mode keeps.
  */
 KNP_GB300_API int knp_gb300_set_step_mode(knp_gb300_backend *b, int mode);
 
 /** 1 when init chose the fused step kernel, else 0 (after init). */
 KNP_GB300_API int knp_gb300_step_fused(const knp_gb300_backend *b, int *fused);
+
+/** The step mode init chose: KNP_GB300_STEP_PHASES, _FUSED or _GRID (after init). */
+KNP_GB300_API int knp_gb300_step_kernel(const knp_gb300_backend *b, int *mode);
 
 /**
  * Enable or disable per-step spike recording of a population (SpikeMessages that an output
@@ -219,11 +228,15 @@ KNP_GB300_API int knp_gb300_generate_bernoulli_schedule(
  * first_step + t sends d_idx[d_offsets[t] : d_offsets[t + 1]] (ascending), the same spikes the
  * allocating generator produces for (seed, stream). *n_idx (host) receives the number of spikes.
  * It calls no cudaMalloc, cudaFree or allocating library routine: its scratch is one fixed device
- * array of 2^18 + 1 int64 counters that every GPU loading the library keeps until process exit, so
- * n_steps * ceil(n_sources / 4096) must not exceed 262144 and n_steps 65535 (else
- * KNP_GB300_E_INVALID). If capacity is too small it returns KNP_GB300_E_INVALID with the needed
- * count in *n_idx and writes nothing to d_idx. The first call on a device looks up the scratch
- * array's device address with that device current; make that first call before any stream capture.
+ * array of 2^18 + 1 int64 counters (2 MiB) that every GPU it runs on keeps until process exit, so
+ * n_steps * ceil(n_sources / 4096) must not exceed 262144 and n_steps 65535, and p must be finite
+ * (else KNP_GB300_E_INVALID with *n_idx = 0). If capacity is too small it returns
+ * KNP_GB300_E_INVALID with the needed count (non-zero) in *n_idx and writes nothing to d_idx.
+ * Set-up: the CUDA runtime loads device code and __device__ arrays lazily, and that load allocates
+ * device memory. The first call in a CUDA context (per device, with that device current; again after
+ * cudaDeviceReset) therefore loads this entry point's kernels and its scratch array (2 MiB) and looks
+ * up the array's address: make that first call (any valid call) during set-up, where allocation is
+ * allowed and no stream capture is active. Later calls in the same context allocate nothing.
  * Every call shares the scratch and finds the previous call's contents (each call rewrites every
  * counter it reads); calls that overlap on the GPU race and must be serialised by the caller. The
  * call waits for its own stream (`stream`, a cudaStream_t; NULL: legacy default stream) once, to read

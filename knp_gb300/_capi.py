@@ -57,6 +57,7 @@ def lib():
         "knp_gb300_set_pull_threshold": ([p, U, ctypes.c_double], c_int),
         "knp_gb300_set_step_mode": ([p, c_int], c_int),
         "knp_gb300_step_fused": ([p, ctypes.POINTER(c_int)], c_int),
+        "knp_gb300_step_kernel": ([p, ctypes.POINTER(c_int)], c_int),
         "knp_gb300_init": ([p], c_int),
         "knp_gb300_send_spikes": ([p, U, u64, u32, p], c_int),
         "knp_gb300_load_spike_schedule": ([p, U, u64, u64, p, p], c_int),

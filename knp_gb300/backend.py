@@ -144,8 +144,9 @@ class GB300Backend:
         self._chk(self._lib.knp_gb300_set_pull_threshold(self._h, T.to_c_uid(proj_uid), float(fraction)))
 
     def set_step_mode(self, mode: int):
-        """Step execution (before init): T.STEP_AUTO, T.STEP_PHASES (a kernel per phase) or
-        T.STEP_FUSED (one cluster kernel per run of steps; small networks only)."""
+        """Step execution (before init): T.STEP_AUTO, T.STEP_PHASES (a kernel per phase),
+        T.STEP_FUSED (one cluster kernel per run of steps; small networks only) or T.STEP_GRID (one
+        persistent cooperative kernel of one CTA per SM per run of steps)."""
         self._chk(self._lib.knp_gb300_set_step_mode(self._h, int(mode)))
 
     @property
@@ -154,6 +155,13 @@ class GB300Backend:
         v = ctypes.c_int(0)
         self._chk(self._lib.knp_gb300_step_fused(self._h, ctypes.byref(v)))
         return bool(v.value)
+
+    @property
+    def step_kernel(self) -> int:
+        """The step mode init chose: T.STEP_PHASES, T.STEP_FUSED or T.STEP_GRID."""
+        v = ctypes.c_int(0)
+        self._chk(self._lib.knp_gb300_step_kernel(self._h, ctypes.byref(v)))
+        return int(v.value)
 
     def record_spikes(self, pop_uid: bytes, enable: bool = True):
         self._chk(self._lib.knp_gb300_record_spikes(self._h, T.to_c_uid(pop_uid), int(enable)))

@@ -196,6 +196,13 @@ int knp_gb300_step_fused(const knp_gb300_backend *b, int *fused)
     return KNP_GB300_OK;
 }
 
+int knp_gb300_step_kernel(const knp_gb300_backend *b, int *mode)
+{
+    if (!b || !mode) return null_handle();
+    *mode = b->impl.step_kernel();
+    return KNP_GB300_OK;
+}
+
 int knp_gb300_record_spikes(knp_gb300_backend *b, knp_uid pop_uid, int enable)
 {
     if (!b) return null_handle();

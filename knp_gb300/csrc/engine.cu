@@ -102,6 +102,13 @@ Backend::~Backend()
 {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    if (persisting_l2_)
+    {
+        // The ring's lines go back to normal eviction and the L2 set-aside to its previous size, so
+        // that later work in this process gets the whole L2 again.
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persisting_before_);
+    }
     if (graph1_) cudaGraphExecDestroy(graph1_);
     if (graphK_) cudaGraphExecDestroy(graphK_);
     for (auto &c : channels_)
@@ -941,6 +948,15 @@ void Backend::init()
     }
     std::string why;
     fused_ = step_mode_ == KNP_GB300_STEP_FUSED || (step_mode_ == KNP_GB300_STEP_AUTO && small_net_eligible(why));
+    grid_ = false;
+    if (!fused_ && (step_mode_ == KNP_GB300_STEP_GRID || step_mode_ == KNP_GB300_STEP_AUTO))
+    {
+        std::string why_grid;
+        grid_ = grid_net_eligible(why_grid);
+        if (!grid_ && step_mode_ == KNP_GB300_STEP_GRID)
+            throw Error(KNP_GB300_E_INVALID, "the grid step kernel does not take this network: " + why_grid);
+        if (grid_) setup_ring_window();
+    }
     initialized_ = true;
     capture_graphs();
 }
@@ -948,7 +964,8 @@ void Backend::init()
 void Backend::set_step_mode(int mode)
 {
     require_not_init("set_step_mode");
-    if (mode != KNP_GB300_STEP_AUTO && mode != KNP_GB300_STEP_PHASES && mode != KNP_GB300_STEP_FUSED)
+    if (mode != KNP_GB300_STEP_AUTO && mode != KNP_GB300_STEP_PHASES && mode != KNP_GB300_STEP_FUSED &&
+        mode != KNP_GB300_STEP_GRID)
         throw Error(KNP_GB300_E_INVALID, "unknown step mode");
     step_mode_ = mode;
 }
@@ -985,6 +1002,93 @@ bool Backend::small_net_eligible(std::string &why) const
         return false;
     }
     return true;
+}
+
+// The grid kernel runs any network of the per-phase path whose STDP projections have at most
+// kMaxSources STDP populations, with at most kMaxGridPull gather-form projections, when one
+// 1024-thread CTA per SM fits with the gather form's shared memory and the device takes
+// cooperative launches.
+bool Backend::grid_net_eligible(std::string &why)
+{
+    int coop = 0;
+    KNP_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device_));
+    if (!coop)
+    {
+        why = "the device does not take cooperative launches";
+        return false;
+    }
+    size_t smem = 0;
+    uint32_t n_pull = 0;
+    for (auto &p : projs_)
+    {
+        if (p->stdp_pops.size() > static_cast<size_t>(kMaxSources))
+        {
+            why = "a projection has more than " + std::to_string(kMaxSources) + " STDP populations";
+            return false;
+        }
+        if (p->pull && p->dev.n_src)
+        {
+            ++n_pull;
+            smem = std::max(smem, grid_net_smem(p->dev.pull, sm_count_));
+        }
+    }
+    if (n_pull > static_cast<uint32_t>(kMaxGridPull))
+    {
+        why = "more than " + std::to_string(kMaxGridPull) + " gather-form projections";
+        return false;
+    }
+    const int ctas = grid_net_ctas(smem);
+    if (ctas <= 0)
+    {
+        why = "one CTA per SM does not fit (shared memory " + std::to_string(smem) + " B)";
+        return false;
+    }
+    grid_ctas_ = ctas;
+    grid_smem_ = smem;
+    return true;
+}
+
+// Keeps the largest FP32 input ring in L2 during the grid kernel's launches: the scatter's atomics
+// land there, while the synapse arrays stream through with evict-first loads. Uses the device's
+// set-aside for persisting accesses (a limit of this process's context).
+void Backend::setup_ring_window()
+{
+    ring_window_ = cudaAccessPolicyWindow{};
+    const RingView *best = nullptr;
+    size_t best_bytes = 0;
+    for (auto &q : pops_)
+    {
+        const RingView &rg = q->kind == KNP_NEURON_LIF ? q->ldev.ring : q->bdev.ring;
+        const size_t bytes = rg.v32 ? static_cast<size_t>(rg.slots) * rg.pitch * 4 : 0;
+        if (bytes > best_bytes)
+        {
+            best_bytes = bytes;
+            best = &rg;
+        }
+    }
+    if (!best || best_bytes < (size_t(4) << 20)) return;
+    int max_persist = 0, max_window = 0;
+    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, device_) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, device_) != cudaSuccess ||
+        max_persist <= 0 || max_window <= 0)
+    {
+        cudaGetLastError();
+        return;
+    }
+    const size_t window = std::min(best_bytes, static_cast<size_t>(max_window));
+    const size_t set_aside = std::min(window, static_cast<size_t>(max_persist));
+    if (cudaDeviceGetLimit(&persisting_before_, cudaLimitPersistingL2CacheSize) != cudaSuccess ||
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::max(set_aside, persisting_before_)) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return;
+    }
+    persisting_l2_ = true;
+    ring_window_.base_ptr = best->v32;
+    ring_window_.num_bytes = window;
+    ring_window_.hitRatio = static_cast<float>(static_cast<double>(set_aside) / static_cast<double>(window));
+    ring_window_.hitProp = cudaAccessPropertyPersisting;
+    ring_window_.missProp = cudaAccessPropertyStreaming;
 }
 
 // Uploads the device descriptors of the fused kernel (again after a change of recording): set 0
@@ -1030,10 +1134,12 @@ void Backend::build_small_net()
         }
         std::vector<ProjectionDev> projs;
         std::vector<SmallStdp> rules;
+        small_pull_.clear();
         for (auto &p : projs_)
         {
             if (p->dev.n_src)
             {
+                if (p->pull) small_pull_.push_back(static_cast<uint32_t>(projs.size()));
                 ProjectionDev d = p->dev;
                 for (int k = 0; k < d.n_src; ++k)
                 {
@@ -1124,9 +1230,16 @@ void Backend::capture_graphs()
     if (graph1_) cudaGraphExecDestroy(graph1_);
     if (graphK_) cudaGraphExecDestroy(graphK_);
     graph1_ = graphK_ = nullptr;
-    if (fused_)
+    if (fused_ || grid_)
     {
         build_small_net();
+        if (grid_)
+        {
+            grid_net_.net = small_;
+            if (!grid_net_.barrier) grid_net_.barrier = arena_.make<unsigned long long>(1);
+            grid_net_.n_pull = static_cast<uint32_t>(small_pull_.size());
+            for (size_t k = 0; k < small_pull_.size(); ++k) grid_net_.pull[k] = small_pull_[k];
+        }
         return;
     }
     for (int which = 0; which < 2; ++which)
@@ -1242,10 +1355,13 @@ void Backend::step(uint64_t n)
         if (host_inputs)
         {
             stage_host_inputs();
-            if (fused_)
+            if (fused_ || grid_)
             {
                 if (!small_.pops[0]) throw Error(KNP_GB300_E_STATE, "the fused step kernel was not set up");
-                KNP_CUDA(launch_small_net(small_, ctl_, 1, small_cluster_, stream_));
+                if (grid_)
+                    KNP_CUDA(launch_grid_net(grid_net_, ctl_, 1, grid_ctas_, grid_smem_, &ring_window_, stream_));
+                else
+                    KNP_CUDA(launch_small_net(small_, ctl_, 1, small_cluster_, stream_));
             }
             else
                 KNP_CUDA(cudaGraphLaunch(graph1_, stream_));
@@ -1258,11 +1374,15 @@ void Backend::step(uint64_t n)
         uint64_t k = n;
         if (any_recording_) k = std::min<uint64_t>(k, steps_before_drain());
         uint64_t done = 0;
-        if (fused_ && !small_.pops[0]) throw Error(KNP_GB300_E_STATE, "the fused step kernel was not set up");
-        while (fused_ && done < k)
+        if ((fused_ || grid_) && !small_.pops[0]) throw Error(KNP_GB300_E_STATE, "the fused step kernel was not set up");
+        while ((fused_ || grid_) && done < k)
         {
             const uint64_t m = std::min<uint64_t>(k - done, kSmallMaxStepsPerLaunch);
-            KNP_CUDA(launch_small_net(small_, ctl_, static_cast<uint32_t>(m), small_cluster_, stream_));
+            if (grid_)
+                KNP_CUDA(launch_grid_net(grid_net_, ctl_, static_cast<uint32_t>(m), grid_ctas_, grid_smem_, &ring_window_,
+                                         stream_));
+            else
+                KNP_CUDA(launch_small_net(small_, ctl_, static_cast<uint32_t>(m), small_cluster_, stream_));
             KNP_CUDA(cudaGetLastError());
             done += m;
         }

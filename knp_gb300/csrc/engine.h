@@ -220,6 +220,7 @@ public:
     void set_pull_threshold(const Uid &proj, double fraction);
     void set_step_mode(int mode);
     bool fused() const { return fused_; }
+    int step_kernel() const { return fused_ ? KNP_GB300_STEP_FUSED : (grid_ ? KNP_GB300_STEP_GRID : KNP_GB300_STEP_PHASES); }
     void record_spikes(const Uid &pop, bool enable);
     void init();
 
@@ -264,7 +265,9 @@ private:
     void wire();
     void enqueue_step();
     bool small_net_eligible(std::string &why) const;
+    bool grid_net_eligible(std::string &why);
     void build_small_net();
+    void setup_ring_window();
     void capture_graphs();
     void stage_host_inputs();
     void drain_recordings() { drain_recordings(step_); }
@@ -306,6 +309,17 @@ private:
     static constexpr uint64_t kSmallMaxNeurons = 16384;
     static constexpr uint64_t kSmallMaxSynapses = 1ull << 22;
     static constexpr uint64_t kSmallMaxStepsPerLaunch = 1ull << 16;
+    // Persistent grid step kernel (grid_net.cu: one cooperative launch of one CTA per SM runs whole
+    // steps), chosen at init for networks the fused kernel does not take.
+    bool grid_ = false;
+    GridNet grid_net_{};
+    std::vector<uint32_t> small_pull_;  // indices (into the fused descriptor sets' projections) with a gather layout
+    int grid_ctas_ = 0;
+    size_t grid_smem_ = 0;
+    // L2 access policy of the grid kernel's launches: the largest FP32 input ring kept persisting.
+    cudaAccessPolicyWindow ring_window_{};
+    bool persisting_l2_ = false;
+    size_t persisting_before_ = 0;  // the context's set-aside before this backend changed it (restored at destroy)
     // pinned staging for host-sent messages
     void *pinned_ = nullptr;
     size_t pinned_bytes_ = 0;

@@ -38,6 +38,9 @@ struct Control
     unsigned int pad;
 };
 
+// Bits of Control::error.
+constexpr unsigned int kErrGridBarrier = 1u << 0;  // a grid barrier of the persistent grid kernel gave up
+
 struct RingView
 {
     uint32_t n;      // neurons
@@ -270,6 +273,18 @@ struct SmallNet
     StepEnd end[2];
 };
 
+// A network run by the persistent grid step kernel (grid_net.cu): the fused kernel's descriptor
+// sets, plus the projections with a gather layout (indices into net.projs) and the grid barrier's
+// arrival counter (zeroed before every launch).
+constexpr int kMaxGridPull = 8;
+struct GridNet
+{
+    SmallNet net;
+    unsigned long long *barrier;
+    uint32_t n_pull;
+    uint32_t pull[kMaxGridPull];
+};
+
 // ---------------------------------------------------------------- launchers (stream-ordered)
 void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s);
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
@@ -282,6 +297,14 @@ void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);
 // device can schedule for it.
 int small_net_cluster();
 cudaError_t launch_small_net(const SmallNet &net, Control *ctl, uint32_t n_steps, int cluster, cudaStream_t s);
+// Runs n_steps whole steps of a network in one cooperative launch of `ctas` CTAs (advances
+// Control::step). grid_net_ctas(smem) is the CTA count (one per SM) when the kernel fits with `smem`
+// bytes of dynamic shared memory, else 0; grid_net_smem is the shared memory a gather projection
+// needs in it. `window` (may be null): L2 access policy of the launch (persisting input ring).
+int grid_net_ctas(size_t smem);
+size_t grid_net_smem(const PullDev &p, int ctas);
+cudaError_t launch_grid_net(const GridNet &g, Control *ctl, uint32_t n_steps, int ctas, size_t smem,
+                            const cudaAccessPolicyWindow *window, cudaStream_t s);
 void launch_gather(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 size_t gather_smem_bytes(const PullDev &p, int grid);
 // Builds the gather layout of a projection from its CSR and fills `out`; the buffers go to `bufs`.

@@ -27,7 +27,7 @@ DELTA, ADDITIVE_STDP_DELTA = range(2)
 STDP_ONLY, STDP_AND_SPIKE = range(2)
 # knp_gb300_accumulator (input-ring accumulation of a population)
 ACC_AUTO, ACC_FP32, ACC_FIXED64 = range(3)
-STEP_AUTO, STEP_PHASES, STEP_FUSED = range(3)  # knp_gb300_step_mode
+STEP_AUTO, STEP_PHASES, STEP_FUSED, STEP_GRID = range(4)  # knp_gb300_step_mode
 # knp_isi_status (stdp_synaptic_resource_rule.h:46-66)
 ISI_IS_FORCED, ISI_PERIOD_STARTED, ISI_PERIOD_CONTINUED, ISI_NOT_IN_PERIOD = range(4)
 

@@ -21,9 +21,10 @@ def _gpu():
     return B
 
 
-# Step modes: AUTO takes the fused step kernel (one CTA cluster) for the small networks of these tests;
-# PHASES keeps the per-phase kernels (population, scatter, STDP, end of step) for the same network.
-MODES = {"auto": T.STEP_AUTO, "phases": T.STEP_PHASES}
+# Step modes: AUTO takes the fused step kernel (one CTA cluster) for the small networks of these tests
+# and the persistent grid kernel for the larger ones; PHASES keeps the per-phase kernels (population,
+# scatter, STDP, end of step); GRID forces the persistent grid kernel (one CTA per SM).
+MODES = {"auto": T.STEP_AUTO, "phases": T.STEP_PHASES, "grid": T.STEP_GRID}
 
 
 def run_both(net, scheds, steps, record=None, device_schedule=False, on_step=None, step_mode=None):
@@ -63,7 +64,7 @@ def assert_same_state(b, oo, pop, rtol=0.0):
         np.testing.assert_array_equal(gext["free_synaptic_resource"], oext["free_synaptic_resource"])
 
 
-@pytest.mark.parametrize("mode", ["auto", "phases"])
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 @pytest.mark.parametrize("kind", ["delta", "stdp", "stdp_resource_neuron"])
 def test_smallest_network_golden(kind, mode):
     """knp/tests/backend/single_thread_cpu_test.cpp:54-176 through the C ABI."""
@@ -80,7 +81,7 @@ def test_smallest_network_golden(kind, mode):
     assert_same_state(b, oo, pop)
 
 
-@pytest.mark.parametrize("mode", ["auto", "phases"])
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 @pytest.mark.parametrize("device_schedule", [False, True])
 def test_small_network_bit_exact(device_schedule, mode):
     """Plain small config: 1000 BLIFAT, 100 Bernoulli inputs, all-to-all input and p=0.1 recurrent
@@ -138,10 +139,12 @@ def test_pipelined_spike_reads_and_caps():
     b.close()
 
 
+@pytest.mark.parametrize("mode", ["auto", "phases"])
 @pytest.mark.parametrize("fraction", [0.0, 0.05, 0.3, -1.0])
-def test_gather_direction_bit_exact(fraction):
+def test_gather_direction_bit_exact(fraction, mode):
     """Steps delivered by the gather kernel (spike share >= fraction; 0 = every step with a spike,
-    -1 = never) give the same spike trains as the oracle, through the ramp into saturated firing."""
+    -1 = never) give the same spike trains as the oracle, through the ramp into saturated firing,
+    with the persistent grid kernel (AUTO at this size) and with the per-phase kernels."""
     from knp_gb300 import backend as B
     from oracle import oracle as orc
 
@@ -150,7 +153,9 @@ def test_gather_direction_bit_exact(fraction):
     b = B.GB300Backend()
     b.load_network(net)
     b.set_pull_threshold(rec.uid, fraction)
+    b.set_step_mode(MODES[mode])
     b._init()
+    assert b.step_kernel == (T.STEP_GRID if mode == "auto" else T.STEP_PHASES)
     for t in range(70):
         idx = sched[0].at(t)
         if idx.size:
@@ -353,7 +358,7 @@ def test_device_bernoulli_schedule_matches_host():
         np.testing.assert_array_equal(b1.spikes(pop, t), o[pop][t])
 
 
-@pytest.mark.parametrize("mode", ["auto", "phases"])
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 def test_stdp_reduced(mode):
     """STDP config with 10 samples x 100 steps: spikes bit-exact, weights bit-exact."""
     net, sched = N.stdp_network(seed=3, samples=10, steps_per_sample=100)
@@ -431,7 +436,7 @@ def test_external_impacts_and_channels():
     del rng
 
 
-@pytest.mark.parametrize("mode", ["auto", "phases"])
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 def test_delay_zero_and_inhibitory_types(mode):
     """Delay-0 synapses create events that are never delivered; INHIBITORY_CURRENT subtracts."""
     n = 64
@@ -451,7 +456,7 @@ def test_delay_zero_and_inhibitory_types(mode):
     assert_same_state(b, oo, pop.uid)
 
 
-@pytest.mark.parametrize("mode", ["auto", "phases"])
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 def test_stdp_only_and_multiple_sources(mode):
     """An STDP projection whose presynaptic population is also an STDP-only population: its spikes
     are emptied before propagation (additive_stdp.h:162-166) and never update weights."""
@@ -564,8 +569,8 @@ def test_errors_are_reported():
 
 def test_step_mode_selection_and_recording_change():
     """Step modes: an unknown mode and a fused mode forced on a network above the fused kernel's
-    size are refused; a recording switched on mid-run under the fused kernel (its descriptors
-    uploaded again) gives the oracle's spikes from that step on."""
+    size are refused; a recording switched on mid-run under the fused kernel or the grid kernel
+    (their descriptors uploaded again) gives the oracle's spikes from that step on."""
     from oracle import oracle as orc
     from knp_gb300 import backend as B
     from knp_gb300._capi import KnpGb300Error
@@ -589,6 +594,20 @@ def test_step_mode_selection_and_recording_change():
     assert b.fused
     with pytest.raises(KnpGb300Error):
         b.set_step_mode(T.STEP_PHASES)
+    for s in sched:
+        b.load_spike_schedule(s)
+    b.step(50)
+    b.record_spikes(pop, True)
+    b.step(50)
+    for t in range(50, 100):
+        np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t])
+    b.close()
+    # The same under the persistent grid kernel (forced at this size).
+    b = B.GB300Backend()
+    b.load_network(net, record=[])
+    b.set_step_mode(T.STEP_GRID)
+    b._init()
+    assert b.step_kernel == T.STEP_GRID and not b.fused
     for s in sched:
         b.load_spike_schedule(s)
     b.step(50)
