@@ -4,6 +4,7 @@
 // contiguous), tcgen05.mma kind::f16 with the accumulator in tensor memory. Used to validate the
 // tcgen05 encodings and as a library GEMM of spike matrices.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdint>
 #include <memory>
 #include <vector>
@@ -230,7 +231,9 @@ struct BatchedNet
     unsigned long long rec_off[kMaxLayers + 1];
     unsigned long long rec_stride;
     unsigned long long *events;
-    unsigned int *err;
+    unsigned int *err;       // bit 0: a wait gave up; bit 1: launched without the 2-CTA cluster shape
+    uint32_t poll_limit;     // polls of a cross-CTA ring counter before a wait gives up
+    uint32_t stall;          // failure test: consumers wait for this many more producer CTAs than exist
     uint32_t n_items;
     uint16_t item_layer[kMaxItems];
     uint16_t item_m[kMaxItems];
@@ -312,14 +315,46 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t b
                  : "memory");
 }
 
-// Polls (acquire, bounded) until *counter >= target; false on timeout.
-__device__ __forceinline__ bool poll_at_least(const unsigned int *counter, unsigned int target)
+// Whether this CTA (its shared failure flag) or any CTA of the launch (the error word) has given up.
+__device__ __forceinline__ bool failed(const volatile int *flag, const unsigned int *gerr)
 {
-    for (uint32_t i = 0; i < kPollLimit; ++i)
+    return *flag != 0 || *reinterpret_cast<const volatile unsigned int *>(gerr) != 0u;
+}
+
+// Polls (acquire, bounded) until *counter >= target; false after `limit` polls or once a failure has
+// been reported (checked every 64 polls).
+__device__ __forceinline__ bool poll_at_least(const unsigned int *counter, unsigned int target, uint32_t limit,
+                                              const volatile int *flag, const unsigned int *gerr)
+{
+    for (uint32_t i = 0; i < limit; ++i)
     {
         unsigned int cur;
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(counter) : "memory");
         if (static_cast<int>(cur - target) >= 0) return true;
+        if ((i & 63u) == 63u && failed(flag, gerr)) return false;
+    }
+    return false;
+}
+
+// mbar_wait that also gives up as soon as a failure has been reported (checked after each poll).
+__device__ __forceinline__ bool wait_or_fail(uint64_t *mbar, uint32_t parity, const volatile int *flag,
+                                             const unsigned int *gerr)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    {
+        if (tc::mbar_try_wait(mbar, parity)) return true;
+        if (failed(flag, gerr)) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool wait_cluster_or_fail(uint64_t *mbar, uint32_t parity, const volatile int *flag,
+                                                     const unsigned int *gerr)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    {
+        if (tc::mbar_try_wait_cluster(mbar, parity)) return true;
+        if (failed(flag, gerr)) return false;
     }
     return false;
 }
@@ -336,14 +371,15 @@ __device__ __forceinline__ unsigned int load_relaxed(const unsigned int *counter
 __device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // Whether *counter >= target: from a value read ahead if that suffices, else by polling.
-__device__ __forceinline__ bool reached(const unsigned int *counter, unsigned int target, unsigned int seen)
+__device__ __forceinline__ bool reached(const unsigned int *counter, unsigned int target, unsigned int seen,
+                                        uint32_t limit, const volatile int *flag, const unsigned int *gerr)
 {
     if (static_cast<int>(seen - target) >= 0)
     {
         fence_acquire();
         return true;
     }
-    return poll_at_least(counter, target);
+    return poll_at_least(counter, target, limit, flag, gerr);
 }
 
 __device__ __forceinline__ void release_add(unsigned int *counter)
@@ -365,9 +401,20 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
     __shared__ __align__(8) uint64_t acc_full[2];     // every MMA into accumulator a has completed (commit)
     __shared__ __align__(8) uint64_t acc_empty[2];    // the epilogue has read accumulator a (kEpilogueThreads)
     __shared__ __align__(8) uint64_t xfull[2];        // the partner's partial sums of a step have landed
+    __shared__ __align__(8) uint64_t drain;           // every MMA this CTA issued has completed (teardown)
     __shared__ unsigned long long s_events;
     __shared__ int s_fail;  // some role gave up on a wait (each group reads it through one thread)
     __shared__ uint32_t s_half[2][2][kBM];  // [step parity][neuron half][row]: epilogue spike masks
+    // Exchange bookkeeping for the teardown: steps whose partial sums this CTA sent to its partner,
+    // exchange phases it received, phases it armed; the partner's sent count (written by the partner).
+    __shared__ uint32_t s_sent, s_recv, s_armed, s_peer_sent;
+    // A launch without the two-CTA cluster shape (every CTA sees the same count) stops here, before
+    // any access to a partner's shared memory.
+    if (tc::cluster_nctarank() != 2u)
+    {
+        if (threadIdx.x == 0) atomicOr(net.err, 2u);
+        return;
+    }
     const uint32_t item = blockIdx.x;
     const int layer = net.item_layer[item];  // 1..L
     const uint32_t m_tile = net.item_m[item];
@@ -417,8 +464,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             tc::mbar_init(&acc_empty[a], kEpilogueThreads);
             tc::mbar_init(&xfull[a], 1);
         }
+        tc::mbar_init(&drain, 1);
         s_events = 0;
-        s_fail = 0;
+        // A failure reported by an earlier segment of the run: this launch steps nothing (but keeps
+        // the teardown protocol with its partner).
+        s_fail = *reinterpret_cast<volatile unsigned int *>(net.err) != 0u ? 1 : 0;
+        s_sent = s_recv = s_armed = s_peer_sent = 0;
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -440,7 +491,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint32_t xr = threadIdx.x;
         const uint32_t wp_in = net.wpad[layer - 1];
         const unsigned int *ready_in = layer > 1 ? net.ready + ctr_in : nullptr;
-        const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] : 0u;
+        const uint32_t need_in = layer > 1 ? net.n_cta[layer - 1] + net.stall : 0u;
         const uint32_t x_lane = (32u * warp) << 16;
         uint32_t seq = 0;
         bool ok = true;
@@ -462,10 +513,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (threadIdx.x == 0)
                 go = go && !s_fail &&
                      (have_next || !ready_in || t == 0 ||
-                      reached(ready_in + t % R, need_in * ((t - 1) / R + 1), ready_seen));
+                      reached(ready_in + t % R, need_in * ((t - 1) / R + 1), ready_seen, net.poll_limit, &s_fail,
+                              net.err));
             if (!tc::named_sync_and(1, kExpandThreads, go))  // the group's decision is uniform
             {
                 s_fail = 1;
+                atomicOr(net.err, 1u);
                 break;
             }
             if (have_next)
@@ -492,24 +545,36 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             for (uint32_t c = 0; c < n_chunks; ++c)
             {
                 const uint32_t u = seq + c, b = u % kStages;
-                if (u >= kStages && !tc::mbar_wait(&empty[b], ((u / kStages) - 1u) & 1u, kWaitLimit)) ok = false;
+                if (ok && u >= kStages && !wait_or_fail(&empty[b], ((u / kStages) - 1u) & 1u, &s_fail, net.err))
+                {
+                    // The stage may still be read by MMAs: it is not written, and the failure stops
+                    // the issuer (which waits on this stage) and, at the next step, this group.
+                    ok = false;
+                    s_fail = 1;
+                    atomicOr(net.err, 1u);
+                }
                 tc::fence_after_sync();
                 const uint32_t w4[4] = {wv[0].x, wv[0].y, wv[0].z, wv[0].w};
 #pragma unroll
                 for (uint32_t k = 0; k + 1 < kMaxHalfChunks; ++k) wv[k] = wv[k + 1];
-#pragma unroll
-                for (uint32_t q = 0; q < 4; ++q)
+                // tcgen05.st is warp-collective: a warp writes only if all its lanes may.
+                if (__all_sync(0xffffffffu, ok))
                 {
-                    // Word q holds inputs 32 q .. 32 q + 31 of the chunk: 16 columns of two BF16 each,
-                    // bits (2 i, 2 i + 1) -> column i = 1.0 or 0 in its low and high halves.
-                    uint32_t v[16];
 #pragma unroll
-                    for (uint32_t i = 0; i < 16; ++i) v[i] = (((w4[q] >> (2u * i) & 3u) * 0x8001u) & 0x10001u) * 0x3F80u;
-                    tc::tmem_st16(tmem + x_lane + kAccCols + b * kStageCols + 16u * q, v);
+                    for (uint32_t q = 0; q < 4; ++q)
+                    {
+                        // Word q holds inputs 32 q .. 32 q + 31 of the chunk: 16 columns of two BF16
+                        // each, bits (2 i, 2 i + 1) -> column i = 1.0 or 0 in its low and high halves.
+                        uint32_t v[16];
+#pragma unroll
+                        for (uint32_t i = 0; i < 16; ++i)
+                            v[i] = (((w4[q] >> (2u * i) & 3u) * 0x8001u) & 0x10001u) * 0x3F80u;
+                        tc::tmem_st16(tmem + x_lane + kAccCols + b * kStageCols + 16u * q, v);
+                    }
+                    tc::tmem_wait_st();
+                    tc::fence_before_sync();
+                    tc::mbar_arrive(&full[b]);
                 }
-                tc::tmem_wait_st();
-                tc::fence_before_sync();
-                tc::mbar_arrive(&full[b]);
                 if (c == c_ask && can_next)
                 {
                     bool nx = true;
@@ -574,7 +639,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         // Neurons at or past this sample's size do not exist (never updated, never spike).
         const uint32_t n_here = my_n > n0 + cb ? my_n - n0 - cb : 0u;
         const uint32_t exists = n_here >= 16u ? 0xFFFFu : (1u << n_here) - 1u;
-        uint32_t s = 0;
+        uint32_t s = 0, sent = 0, armed = 0;
         for (uint32_t t = t0; t < t1; ++t)
         {
             const uint32_t b_act = net.act[t];
@@ -585,7 +650,15 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             const bool check_room = et == 0 && producer && t + 1 >= R;
             const unsigned int room_seen = check_room ? load_relaxed(consumed_out + (t + 1) % R) : 0u;
             const uint32_t a = s & 1u, ph = (s >> 1) & 1u;
-            bool ok = tc::mbar_wait(&acc_full[a], ph, kWaitLimit);
+            // A failed accumulator wait stops the group before it reads tensor memory that MMAs may
+            // still write, and before it sends its partner anything for this step.
+            if (!tc::named_sync_and(2, kEpilogueThreads, wait_or_fail(&acc_full[a], ph, &s_fail, net.err)))
+            {
+                s_fail = 1;
+                atomicOr(net.err, 1u);
+                break;
+            }
+            bool ok = true;
             tc::fence_after_sync();
             // Read the accumulator while the tensor cores are idle (the issuer starts the next step's
             // MMAs once it is released): the partner's columns go straight to the partner (row er,
@@ -593,6 +666,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             // different banks), ours stay in registers. Then our partial + the partner's ((K half 0)
             // + (K half 1) on both sides) and the LIF update.
             if (et == 0) mbar_arrive_expect_tx(&xfull[a], kXchBytes);
+            armed = s + 1;
             const uint32_t row_peer = tc::mapa(tc::smem_u32(sX), peer) + a * kXchBytes + er * (kBN * 4u);
             const uint32_t xfull_peer = tc::mapa(tc::smem_u32(&xfull[a]), peer);
             float acc[kEN];
@@ -605,11 +679,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             for (uint32_t q = 0; q < kEN / 4; ++q)
                 tc::st_async_v4(row_peer + ((((cb >> 2) + q) ^ (er & 7u)) << 4), acc[4 * q], acc[4 * q + 1],
                                 acc[4 * q + 2], acc[4 * q + 3], xfull_peer);
+            sent = s + 1;
             if (n_chunks)
                 tc::tmem_ld16(tmem + lane_base + a * kPairN + kBN * kh + cb, acc);
             tc::fence_before_sync();
             tc::mbar_arrive(&acc_empty[a]);
-            ok = tc::mbar_wait_cluster(&xfull[a], ph, kWaitLimit) && ok;
+            ok = wait_cluster_or_fail(&xfull[a], ph, &s_fail, net.err) && ok;
             const uint8_t *row_own = sX + a * kXchBytes + er * (kBN * 4u);
 #pragma unroll
             for (uint32_t q = 0; q < kEN / 4; ++q)
@@ -638,13 +713,14 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             if (cnt)
                 for (uint32_t m = mask; m; m &= m - 1u) ++cnt[(__ffs(m) - 1) * kBM];
             s_half[a][ew >> 2][er] = mask;
-            const bool room =
-                !check_room ||
-                reached(consumed_out + (t + 1) % R, need_out * ((t + 1 - R) / R + 1), room_seen);
+            const bool room = !check_room || reached(consumed_out + (t + 1) % R, need_out * ((t + 1 - R) / R + 1),
+                                                     room_seen, net.poll_limit, &s_fail, net.err);
             const bool go = ok && room && (et != 0 || !s_fail);
             if (!tc::named_sync_and(2, kEpilogueThreads, go))  // the group's decision is uniform
             {
                 s_fail = 1;
+                atomicOr(net.err, 1u);
+                if (ok) ++s;  // this step's exchange phase completed in every thread
                 break;
             }
             ++s;
@@ -682,6 +758,12 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
             for (int i = 0; i < kEN; ++i)
                 if (n0 + cb + i < N) net.counts[static_cast<size_t>(e_smp) * N + n0 + cb + i] = cnt[i * kBM];
         }
+        if (et == 0)
+        {
+            s_sent = sent;
+            s_recv = s;
+            s_armed = armed;
+        }
     }
     else if (lane == 0)
     {
@@ -694,18 +776,28 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
         const uint64_t dW0 = tc::smem_desc(tc::smem_u32(sW), 128, sbo_w);
         unsigned int *consumed_in = layer > 1 ? net.consumed + ctr_in : nullptr;
         uint32_t seq = 0, s = 0;
-        for (uint32_t t = t0; t < t1; ++t)
+        bool stop = false;
+        for (uint32_t t = t0; t < t1 && !stop; ++t)
         {
             if (m0 >= net.act[t] || s_fail) break;
             const uint32_t a = s & 1u;
             // The epilogue has read the previous step's accumulator (no tensor-memory reads run
             // beside these MMAs).
-            if (s >= 1 && !tc::mbar_wait(&acc_empty[(s - 1) & 1u], ((s - 1) >> 1) & 1u, kWaitLimit)) s_fail = 1;
+            if (s >= 1 && !wait_or_fail(&acc_empty[(s - 1) & 1u], ((s - 1) >> 1) & 1u, &s_fail, net.err))
+            {
+                stop = true;
+                break;
+            }
             tc::fence_after_sync();
             for (uint32_t c = 0; c < n_chunks; ++c)
             {
                 const uint32_t u = seq + c, b = u % kStages;
-                if (!tc::mbar_wait(&full[b], (u / kStages) & 1u, kWaitLimit)) s_fail = 1;
+                // A stage that was not written is not multiplied: the run stops here.
+                if (!wait_or_fail(&full[b], (u / kStages) & 1u, &s_fail, net.err))
+                {
+                    stop = true;
+                    break;
+                }
                 tc::fence_after_sync();
                 const uint32_t ta = tmem + kAccCols + b * kStageCols;
                 const uint64_t db = dW0 + c * ((kBK / 8 * 128) >> 4);
@@ -714,16 +806,49 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batched_lif_kernel(BatchedNe
                     tc::mma_bf16_ta(tmem + a * kPairN, ta + j * 8, db + j * 16, idesc, (c > 0 || j > 0) ? 1u : 0u);
                 tc::commit(&empty[b]);
             }
+            if (stop) break;
             seq += n_chunks;
             tc::commit(&acc_full[a]);
             if (consumed_in) release_add(consumed_in + t % R);
             ++s;
         }
-        // Let the MMAs still in flight finish (bounded) before the tensor memory is released.
-        if (s) tc::mbar_wait(&acc_full[(s - 1) & 1u], ((s - 1) >> 1) & 1u, kWaitLimit);
+        if (stop)
+        {
+            s_fail = 1;
+            atomicOr(net.err, 1u);
+        }
+        // Every MMA this thread issued completes (bounded wait) before the tensor memory is released;
+        // a drain that does not finish is reported too.
+        tc::commit(&drain);
+        if (!tc::mbar_wait(&drain, 0, kWaitLimit))
+        {
+            s_fail = 1;
+            atomicOr(net.err, 1u);
+        }
     }
     if (my_events) atomicAdd(&s_events, my_events);
     tc::fence_before_sync();
+    __syncthreads();
+    // Exchange drain: each CTA tells its partner how many steps of partial sums it sent, then waits
+    // (bounded) until every one of them has landed in its own shared memory, so that no store of the
+    // partner is in flight into this CTA when it leaves (after a failure the loops end at different
+    // steps).
+    const bool xthread = threadIdx.x == static_cast<unsigned>(kExpandThreads);  // the first epilogue thread
+    if (xthread) tc::st_cluster_u32(tc::mapa(tc::smem_u32(&s_peer_sent), tc::cluster_rank() ^ 1u), s_sent);
+    tc::cluster_sync();
+    if (xthread)
+    {
+        const uint32_t peer_sent = s_peer_sent;
+        for (uint32_t q = s_recv; q < peer_sent; ++q)
+        {
+            if (q >= s_armed) mbar_arrive_expect_tx(&xfull[q & 1u], kXchBytes);
+            if (!tc::mbar_wait_cluster(&xfull[q & 1u], (q >> 1) & 1u, kWaitLimit))
+            {
+                s_fail = 1;
+                atomicOr(net.err, 1u);
+            }
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0)
     {
@@ -951,6 +1076,12 @@ int batched_plan_create(
         *why = "could not create the plan's stream";
         return -3;
     }
+    // Failure test (KNP_GB300_BATCHED_STALL=1): every consumer layer waits for one producer CTA more
+    // than exists, so its first ring wait runs out (after a short poll limit) and the run ends with
+    // the error word set instead of results.
+    const char *stall = std::getenv("KNP_GB300_BATCHED_STALL");
+    net.stall = (stall && stall[0] == '1') ? 1u : 0u;
+    net.poll_limit = net.stall ? (1u << 16) : kPollLimit;
     net.n_layers = n_layers;
     for (int l = 0; l <= n_layers; ++l)
     {
@@ -1176,7 +1307,8 @@ int batched_plan_run(BatchedPlan *p, unsigned long long *events_out, float *ms, 
     }
     if (kerr)
     {
-        *why = "a tensor-core completion wait, the pair exchange or a layer's step counter wait timed out";
+        *why = (kerr & 2u) ? "the batched kernel ran without its two-CTA cluster shape"
+                           : "a tensor-core completion wait, the pair exchange or a layer's step counter wait timed out";
         return -4;
     }
     return 0;

@@ -137,6 +137,45 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// One poll of mbar_wait (suspends for at most kSuspendNs); true if the phase has completed.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity), "r"(kSuspendNs)
+        : "memory");
+    return done != 0;
+}
+
+// One poll of mbar_wait_cluster.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *mbar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity), "r"(kSuspendNs)
+        : "memory");
+    return done != 0;
+}
+
+// 32-bit store into the shared memory of another CTA of the cluster (address from mapa).
+__device__ __forceinline__ void st_cluster_u32(uint32_t remote_addr, uint32_t v)
+{
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(remote_addr), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_nctarank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
 // As mbar_wait, with cluster-scope acquire: for phases completed by another CTA of the cluster
 // (st.async with complete_tx into this CTA's shared memory).
 __device__ __forceinline__ bool mbar_wait_cluster(uint64_t *mbar, uint32_t parity, uint32_t limit)

@@ -7,6 +7,9 @@ KNP sources are present). Run from the repository root:
 Each case stores, per step, the spike count and the CRC32 of the ascending spike indexes of the
 network's first population, the total synaptic event count, and CRC32s of final projection weights.
 
+`python tests/golden/make_golden.py --batched` writes tests/golden/batched_oracle.json: per (layer,
+sample) spike digests of a small dense batched config run as one block-diagonal LIF network.
+
 `python tests/golden/make_golden.py --full` also writes tests/golden/stdp_full.json for the full STDP
 learning config (200 samples x 100 steps; about two minutes of CPU): per sample the spike count and
 a CRC32 over that sample's per-step digests, the final plastic weights' CRC32, and every 613th final
@@ -65,10 +68,48 @@ def full_stdp():
     print("stdp_full", "spikes", sum(s.size for s in res[pop]), "events", o.events)
 
 
+BATCHED = {"seed": 9, "batch": 8, "sizes": [128, 160, 128, 10], "t_lo": 20, "t_hi": 60, "rate_max": 0.3}
+
+
+def batched_oracle():
+    """Per (layer, sample) of a small dense batched config run as one block-diagonal LIF network by
+    the reference-header oracle: each step's spike count and CRC32 of the sample's ascending
+    neuron indexes."""
+    from knp_gb300 import batched as BT
+
+    cfg = BT.dense_config(**BATCHED)
+    net, sched = BT.plain_network(cfg)
+    res, _ = orc.run(net, [sched], int(cfg.steps.max()), which="reference")
+    layers = []
+    for l in range(1, len(cfg.sizes)):
+        n = cfg.sizes[l]
+        uid = net.populations[l - 1].uid
+        for s in range(cfg.batch):
+            counts, crcs = [], []
+            for t in range(int(cfg.steps[s])):
+                idx = res[uid][t].astype(np.int64)
+                mine = (idx[(idx // n) == s] % n).astype(np.uint32)
+                counts.append(int(mine.size))
+                crcs.append(zlib.crc32(np.ascontiguousarray(mine).tobytes()))
+            layers.append({"layer": l, "sample": s, "counts": counts, "crcs": crcs})
+    out = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "config": BATCHED, "layers": layers}
+    with open(os.path.join(ROOT, "tests", "golden", "batched_oracle.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    print("batched_oracle", "spikes", sum(sum(c["counts"]) for c in layers))
+
+
+def knp_reference_dir():
+    """The KNP sources: $KNP_REF, else a `reference` directory beside this repository."""
+    return os.environ.get("KNP_REF") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def main():
-    orc.build("reference", knp_ref=os.environ.get("KNP_REF", "/root/reference"))
+    orc.build("reference", knp_ref=knp_reference_dir())
     if "--full" in sys.argv:
         full_stdp()
+        return
+    if "--batched" in sys.argv:
+        batched_oracle()
         return
     out = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "cases": []}
     for name, builder, kwargs, steps, wproj in CASES:

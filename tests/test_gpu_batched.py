@@ -228,3 +228,50 @@ def test_batched_input_rates_at_the_edges():
             got = BT.spikes_from_bits(rec[0][t, s], cfg.sizes[0])
             np.testing.assert_array_equal(got, BT.input_spikes(cfg, s, t))
             assert {4, 5, 6} <= set(got.tolist()) and not ({0, 1, 2, 3} & set(got.tolist()))
+
+
+def test_batched_ring_wait_timeout_reports_an_error(monkeypatch):
+    """Failure detection: with KNP_GB300_BATCHED_STALL=1 every consumer layer waits for one producer
+    CTA more than exists, a step counter that nothing ever raises. Its bounded wait (a short poll
+    limit in this mode) gives up, every other wait of the launch stops on the reported failure, the
+    CTA pairs drain their in-flight MMAs and partial-sum stores and free their tensor memory, and the
+    run returns the device-error status instead of hanging. A plan created afterwards on the same
+    device gives the same results as a run before the failure."""
+    from knp_gb300 import batched as BT
+    from knp_gb300._capi import KnpGb300Error
+
+    cfg = BT.dense_config(seed=10, batch=130, sizes=(200, 160, 96, 10), t_lo=20, t_hi=40, rate_max=0.3)
+    c0, r0, ev0, _ = BT.run(cfg, record=True)
+    monkeypatch.setenv("KNP_GB300_BATCHED_STALL", "1")
+    plan = BT.BatchedPlan(cfg, record=True, stages=2)  # a fixed ring depth: no tuning runs at creation
+    try:
+        with pytest.raises(KnpGb300Error) as err:
+            plan.run()
+        assert err.value.code == -4  # KNP_GB300_E_DEVICE_FLAG
+    finally:
+        plan.close()
+    monkeypatch.delenv("KNP_GB300_BATCHED_STALL")
+    c1, r1, ev1, _ = BT.run(cfg, record=True)
+    assert ev1 == ev0
+    np.testing.assert_array_equal(c1, c0)
+    for layer in r0:
+        np.testing.assert_array_equal(r1[layer], r0[layer])
+
+
+def test_batched_dense_config_against_fp64_oracle():
+    """The full batched dense config (256 samples, 784-1000-1000-10, T in [50, 200], BF16 weights,
+    FP32 accumulation on the tensor cores) against the FP64 oracle (oracle/batched_fp64.py: the
+    reference LIF semantics of lif_impl.h:33-86 in exact arithmetic, pinned to the reference-header
+    oracle on the CPU) over every sample's own steps: the input spikes are identical, and at most
+    0.1% of (sample, neuron, step) of layers 1-3 differ."""
+    from knp_gb300 import batched as BT
+    from oracle import batched_fp64 as BF
+
+    cfg = BT.dense_config(seed=4)
+    _, rec, _, _ = BT.run(cfg, record=True)
+    fp = BF.run_fp64(cfg)
+    m0, t0 = BF.mismatch(fp, rec, cfg, layers=[0])
+    assert m0 == 0 and t0 > 0
+    m, t = BF.mismatch(fp, rec, cfg)
+    print(f"batched tcgen05 form vs FP64 oracle: {m} of {t} (sample, neuron, step) differ ({m / t:.2e})")
+    assert m <= 0.001 * t, (m, t)
