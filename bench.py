@@ -3,17 +3,25 @@
 Workload (one GPU): 1,000,000 BLIFAT neurons (reference defaults), fixed fan-in 1000 from uniform
 random presynaptic sources (1e9 delta synapses; int32 index, FP32 weight k/256 with k in [-16, 48],
 u8 delay in 1..20), Bernoulli background drive p = 0.005 per neuron per step through a one-to-one
-projection (w = 1.0, delay 1). A step is one simulation step of the whole network. The synapse
-arrays (9 GB) are far larger than L2, so no L2 flush is needed between steps.
+projection (w = 1.0, delay 1). A step is one simulation step of the whole network; the network
+ramps up from the background rate and, after about 30 steps, every neuron fires every step. The
+synapse arrays (9 GB) are far larger than L2, so no L2 flush is needed between steps.
 
-value      synaptic events/s with the background schedule already in HBM, CUDA-event timed.
-e2e        the same metric through the C ABI with host buffers: every step the host sends the
-           step's background spikes (pinned host -> device) and reads the population's spikes back
-           (bitmap device -> host, expanded to indexes), pipelined one step deep as a caller would.
-roofline   the dominant kernel phase (projection scatter), algorithmic bytes 9 B per synaptic event
-           + 8 B per presynaptic spike row, divided by its CUDA-event time measured here.
-cpu_baseline / --impl reference: the CPU oracle (restated single-threaded backend step) on a
-           bounded sample: the same configuration at 1/100 scale.
+Every figure of the main line describes the same steps: W untimed warm-up steps, then the K timed
+steps W..W+K-1 (with the defaults, the sparse ramp: a few thousand spikes per step, scattered).
+value      synaptic events/s of the K steps with the background schedule already in HBM, timed with
+           CUDA events on the backend's stream (in grid mode the K steps are one launch).
+roofline   the same launch: algorithmic bytes (9 B per synaptic event + 32 B per neuron update + 8 B
+           per spike row) over its CUDA-event time, against the measured HBM copy bandwidth.
+e2e        the same K steps through the C ABI with host buffers, on a fresh backend that ran the W
+           warm-up steps first: every step the host sends the step's background spikes (pinned host ->
+           device) and reads the population's spikes back (bitmap device -> host, expanded to indexes),
+           pipelined one step deep as a caller would; its event count equals value's.
+cpu_baseline / --impl reference: the restated CPU backend (single-threaded, and the multi-threaded
+           backend's structure on all host threads) on the same step window of the config at 1/100
+           scale.
+Extra blocks: a saturated window of the same run, the per-phase kernels on the timed window, and the
+batched dense, BPTT and STDP forms.
 """
 from __future__ import annotations
 
@@ -124,60 +132,70 @@ def build_large(b, n=N, fan_in=FAN_IN):
     return pop_uid, chan_uid
 
 
-def cpu_baseline_sample(target_s: float = 15.0):
-    """Restated single-threaded oracle on the large sparse config at 1/100 scale (10k neurons,
-    fan-in 1000): events/s of its step loop."""
+def large_backend(device, n, fan_in, pull_threshold, mode=None):
+    """The large sparse network on the GPU backend, initialised (step mode `mode`, default AUTO)."""
+    from knp_gb300 import backend as B
+    from knp_gb300 import types as T
+
+    b = B.GB300Backend(device)
+    pop_uid, chan_uid = build_large(b, n=n, fan_in=fan_in)
+    b.set_pull_threshold(T.uid_from_int(SEED * 100 + 2), pull_threshold)
+    if mode is not None:
+        b.set_step_mode(mode)
+    b._init()
+    return b, pop_uid, chan_uid
+
+
+def window_oracle(which_step: str, n: int, warmup: int, steps: int, target_s: float, threads: int = 1):
+    """The restated CPU backend (single-threaded step, or the multi-threaded backend's structure on
+    `threads` threads) on the large sparse config at 1/100 scale, over the same step window as the
+    GPU measurement: `warmup` steps untimed, then up to `steps` timed (stopping after target_s)."""
     from knp_gb300 import network as Nw
     from oracle import oracle as orc
 
-    n = 10_000
-    steps = 200
-    net, sched = Nw.large_sparse_network(seed=SEED, n=n, fan_in=FAN_IN, steps=steps)
+    net, sched = Nw.large_sparse_network(seed=SEED, n=n, fan_in=FAN_IN, steps=warmup + steps)
     o = orc.OracleNet("restated")
     o.load(net)
-    t0 = time.perf_counter()
-    done = 0
-    for t in range(steps):
+
+    def one(t):
         idx = sched[0].at(t)
         if idx.size:
             o.send_spikes(sched[0].sender, idx, t)
-        o.step()
+        if which_step == "mt":
+            o.step_mt(threads)
+        else:
+            o.step()
+
+    for t in range(warmup):
+        one(t)
+    e0 = o.events
+    t0 = time.perf_counter()
+    done = 0
+    for t in range(warmup, warmup + steps):
+        one(t)
         done += 1
         if time.perf_counter() - t0 > target_s:
             break
     dt = time.perf_counter() - t0
-    return {"value": o.events / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"large sparse config at 1/100 scale ({n} neurons, fan-in {FAN_IN}), {done} steps, "
-                      f"{o.events} events, {dt:.1f} s, restated single-threaded backend step"}
+    ev = o.events - e0
+    what = (f"restated multi-threaded backend step on {threads} threads" if which_step == "mt"
+            else "restated single-threaded backend step")
+    return {"value": ev / dt, "unit": UNIT, "cores": threads if which_step == "mt" else 1, "kind": "port",
+            "sample": f"large sparse config at 1/100 scale ({n} neurons, fan-in {FAN_IN}), steps {warmup}.."
+                      f"{warmup + done - 1} (the GPU's timed window; {warmup} untimed before), {ev} events, "
+                      f"{dt:.2f} s, {what}"}
 
 
-def reference_mt_sample(target_s: float = 30.0):
+def cpu_baseline_sample(warmup: int, steps: int, target_s: float = 20.0):
+    """Restated single-threaded oracle on the GPU's step window, large sparse config at 1/100 scale."""
+    return window_oracle("st", 10_000, warmup, steps, target_s)
+
+
+def reference_mt_sample(warmup: int, steps: int, target_s: float = 30.0):
     """The reference multi-threaded CPU backend's step structure (restated in the oracle library:
-    1000-neuron parts, O(S) synapse scan per step in 1000-synapse parts) on all host threads, on
-    the large sparse config at 1/100 scale: events/s of its step loop."""
-    from knp_gb300 import network as Nw
-    from oracle import oracle as orc
-
-    n = 10_000
-    steps = 200
-    threads = os.cpu_count() or 1
-    net, sched = Nw.large_sparse_network(seed=SEED, n=n, fan_in=FAN_IN, steps=steps)
-    o = orc.OracleNet("restated")
-    o.load(net)
-    t0 = time.perf_counter()
-    done = 0
-    for t in range(steps):
-        idx = sched[0].at(t)
-        if idx.size:
-            o.send_spikes(sched[0].sender, idx, t)
-        o.step_mt(threads)
-        done += 1
-        if time.perf_counter() - t0 > target_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": o.events / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"large sparse config at 1/100 scale ({n} neurons, fan-in {FAN_IN}), {done} steps, "
-                      f"{o.events} events, {dt:.1f} s, restated multi-threaded backend step on {threads} threads"}
+    1000-neuron parts, O(S) synapse scan per step in 1000-synapse parts) on all host threads, on the
+    GPU's step window of the large sparse config at 1/100 scale."""
+    return window_oracle("mt", 10_000, warmup, steps, target_s, threads=os.cpu_count() or 1)
 
 
 def replica_totals(t_s: float, events: int, device: str = "cpu"):
@@ -232,6 +250,12 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
     plan.close()
     ms_b = statistics.median(times)
     _, rec, _, _ = BT.run(cfg, record=True, device=device)
+    # Checker (outside every timed region): the FP64 oracle of every sample (reference LIF semantics
+    # in exact arithmetic), against the batched form's record.
+    from oracle import batched_fp64 as BF
+
+    fp64 = BF.run_fp64(cfg)
+    m64, t64 = BF.mismatch(fp64, rec, cfg)
 
     # Plain FP32 path on the same samples.
     t_build = time.perf_counter()
@@ -251,32 +275,38 @@ def batched_dense_measure(device: int, reps: int = 5, warmup: int = 3):
     e1, _, _ = b.counters()
     ev_p = e1 - e0
 
-    # Spike mismatch between the two forms.
+    # Spike mismatch between the two forms, and of the plain path against the FP64 oracle.
     live = np.arange(t_max)[:, None] < cfg.steps[None, :].astype(np.int64)  # [t, sample]
     mism = total = 0
     pops = [p for p in b._pops]
+    plain_rec = {0: rec[0]}
     for layer in range(1, len(cfg.sizes)):
         n = cfg.sizes[layer]
         words = (n + 31) // 32
         uid = pops[layer - 1]
+        plain_rec[layer] = np.zeros((t_max, cfg.batch, words), np.uint32)
         for t in range(t_max):
             idx = b.spikes(uid, t).astype(np.int64)
-            bm = np.zeros((cfg.batch, words), np.uint32)
+            bm = plain_rec[layer][t]
             s, j = idx // n, idx % n
             np.bitwise_or.at(bm, (s, j >> 5), (np.uint32(1) << (j & 31).astype(np.uint32)))
             diff = (bm ^ rec[layer][t]) & np.where(live[t][:, None], np.uint32(0xFFFFFFFF), np.uint32(0))
             mism += int(np.unpackbits(diff.view(np.uint8)).sum())
             total += int(live[t].sum()) * n
     b.close()
+    mp64, tp64 = BF.mismatch(fp64, plain_rec, cfg)
     flops = 2.0 * float(sum(int(cfg.steps.sum()) * a * c for a, c in zip(cfg.sizes[:-1], cfg.sizes[1:])))
     return {
         "workload": "batched_dense: 256 LIF samples 784-1000-1000-10, T in [50,200], inputs rate U[0,0.2], "
                     "weights N(0,1/fan_in) as BF16, FP32 accumulation, one persistent launch",
         "value": events / (ms_b / 1e3), "unit": UNIT, "ms_per_run": ms_b, "events_per_run": events,
         "plain_fp32_path": {"value": ev_p / (ms_p / 1e3), "unit": UNIT, "ms_per_run": ms_p, "events_per_run": ev_p,
-                            "build_s": t_build},
+                            "build_s": t_build, "mismatch_vs_fp64_oracle": mp64 / max(tp64, 1)},
         "speedup_vs_plain": (events / ms_b) / (ev_p / ms_p),
         "spike_mismatch": mism / max(total, 1), "compared": total,
+        "mismatch_vs_fp64_oracle": m64 / max(t64, 1), "compared_fp64": t64,
+        "fp64_oracle": "oracle/batched_fp64.py: reference LIF semantics (lif_impl.h:33-86) in FP64 over every "
+                       "sample's own steps; pinned to the reference-header oracle on a smaller batch",
         "tensor": {"dense_flops_per_run": flops, "achieved_tflops": flops / (ms_b / 1e3) / 1e12},
         "dtype": "bf16 x bf16 -> fp32", "l2": "flushed (256 MB write) before each timed run",
         "launch": "one CUDA graph per batch (state memsets, input thresholds, input spike bitmaps drawn ahead, "
@@ -387,33 +417,81 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = reference_mt_sample(target_s=max(5.0, min(60.0, 0.5 * args.steps)))
+    cb = reference_mt_sample(args.warmup, args.steps, target_s=max(10.0, min(60.0, 3.0 * args.steps)))
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
-            "config": {"workload": "large_sparse_plain at 1/100 scale on the host CPU (reference multi-threaded "
-                                   "backend structure)", "neurons": 10_000, "fan_in": FAN_IN, "p_background": P_BG},
+            "config": {"workload": f"large_sparse_plain, steps {args.warmup}..{args.warmup + args.steps - 1} "
+                                   "(the GPU arm's timed window), at 1/100 scale on the host CPU (reference "
+                                   "multi-threaded backend structure)",
+                       "neurons": 10_000, "fan_in": FAN_IN, "p_background": P_BG},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
+def algorithmic_bytes(events, neuron_updates, rows):
+    """Bytes of the measurement plan: 9 B per synaptic event (int32 target + FP32 weight + u8 delay),
+    32 B per neuron update, 8 B per spike row walked (a row_ptr pair)."""
+    return 9.0 * events + 32.0 * neuron_updates + 8.0 * rows
+
+
+def e2e_window(device, n, fan_in, pull, chan_seed, warmup, steps, sched):
+    """The timed window through the C ABI with host buffers: a fresh backend runs steps 0..warmup-1
+    untimed, then each timed step sends that step's background spikes from host memory (pinned
+    staging, host -> device), runs the step, and reads the population's previous step back (spike
+    bitmap device -> host, expanded to ascending indexes), pipelined one step deep as a caller would."""
+    b, pop_uid, chan_uid = large_backend(device, n, fan_in, pull)
+    b.record_spikes(pop_uid, True)
+    buf = np.empty(n, np.uint32)
+    for t in range(warmup):
+        b.send_spikes(chan_uid, sched.at(t), t)
+        b.step(1)
+    b.spikes(pop_uid, warmup - 1, out=buf)
+    b.discard_spikes(warmup)
+    b.synchronize()
+    ea, _, _ = b.counters()
+    h2d = d2h = n_out = 0
+    t0 = time.perf_counter()
+    for k in range(steps + 1):
+        if k < steps:
+            idx = sched.at(warmup + k)
+            b.send_spikes(chan_uid, idx, warmup + k)
+            h2d += idx.nbytes
+            b.step(1)
+        if k > 0:
+            out = b.spikes(pop_uid, warmup + k - 1, out=buf)  # ascending, as in the reference's SpikeMessage
+            b.discard_spikes(warmup + k)
+            d2h += (n + 31) // 32 * 4  # the step's spike bitmap crosses to the host, expanded there
+            n_out += out.size
+    b.synchronize()
+    te = time.perf_counter() - t0
+    eb, _, _ = b.counters()
+    launches = b.step_kernel
+    b.close()
+    return {"value": (eb - ea) / te, "unit": UNIT, "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+            "steps": f"{warmup}..{warmup + steps - 1}", "ms_per_step": te / steps * 1e3,
+            "spikes_returned_per_step": n_out / steps, "events": int(eb - ea), "step_kernel": launches}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=100)
-    ap.add_argument("--profile-steps", type=int, default=50)
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched dense, BPTT and STDP measurements")
+    ap.add_argument("--no-extra-windows", action="store_true",
+                    help="skip the saturated window and the per-phase kernels on the timed window")
     ap.add_argument("--form", default="all", choices=["all", "batched", "bptt", "stdp"],
                     help="measure one form alone: the batched dense form, the BPTT step or the STDP config (profiling runs)")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     ap.add_argument("--pull-threshold", type=float, default=0.1,
                     help="spike share above which a step is gathered instead of scattered (-1: scatter only)")
+    ap.add_argument("--step-mode", default="auto", choices=["auto", "phases", "grid"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -436,137 +514,120 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
 
-    from knp_gb300 import backend as B
     from knp_gb300 import network as Nw
-
-    b = B.GB300Backend(local)
-    t_build = time.perf_counter()
-    n_neurons = args.neurons
-    pop_uid, chan_uid = build_large(b, n=n_neurons, fan_in=args.fan_in)
     from knp_gb300 import types as T
 
-    b.set_pull_threshold(T.uid_from_int(SEED * 100 + 2), args.pull_threshold)
-    b._init()
-    total_steps = args.warmup + args.steps + args.profile_steps
-    b.generate_bernoulli_schedule(chan_uid, n_neurons, P_BG, 0, total_steps, seed=SEED + 1000 * rank)
+    modes = {"auto": None, "phases": T.STEP_PHASES, "grid": T.STEP_GRID}
+    n_neurons, W, K = args.neurons, args.warmup, args.steps
+    sat0, sat_steps = max(W + K, 40), 20  # a window of saturated steps (every neuron fires every step)
+    total_steps = sat0 + sat_steps
+    chan_seed = SEED + 1000 * rank
+    t_build = time.perf_counter()
+    b, pop_uid, chan_uid = large_backend(local, n_neurons, args.fan_in, args.pull_threshold, modes[args.step_mode])
+    b.generate_bernoulli_schedule(chan_uid, n_neurons, P_BG, 0, total_steps, seed=chan_seed)
     t_build = time.perf_counter() - t_build
+    step_kernel = b.step_kernel
+    # The same background spikes on the host (the device generator's restatement): their count per
+    # step gives the spike rows of the one-to-one projection; the e2e run sends them from host memory.
+    sched = Nw.bernoulli_schedule(chan_uid, chan_seed, n_neurons, total_steps, P_BG)
 
-    b.step(args.warmup)
+    b.step(W)
     b.synchronize()
     if dist is not None:
         dist.barrier()
     ev0, sp0, _ = b.counters()
     with Clocks(local) as clk:
-        ms = b.step_timed(args.steps)
+        ms = b.step_timed(K)
     ev1, sp1, _ = b.counters()
     t, events_all = replica_totals(ms / 1e3, ev1 - ev0, f"cuda:{local}" if dist is not None else "cpu")
-    events = ev1 - ev0
-    spikes = sp1 - sp0
+    events, spikes = ev1 - ev0, sp1 - sp0
     value = events_all / t
-
-    # Live per-phase timing of the same steps (kernels launched one by one, CUDA events between phases).
-    args.profile_steps = max(args.profile_steps, 1)
-    e0, s0, _ = b.counters()
-    ph = b.profile_phases(args.profile_steps)
-    e1, s1, _ = b.counters()
-    p_events = (e1 - e0) / args.profile_steps
-    p_spikes = (s1 - s0) / args.profile_steps
+    bg_rows = int(sched.offsets[W + K] - sched.offsets[W])
+    # Roofline of the timed launch: in grid mode the K steps are one launch of the persistent step
+    # kernel, timed by the CUDA events around it on the backend's stream.
     hbm, src = peaks()
-    proj_ms = ph[1] / args.profile_steps
-    pop_ms = ph[0] / args.profile_steps
-    # Spike rows walked per step: population spikes through the recurrent projection + background
-    # spikes through the one-to-one projection (each a row_ptr pair).
-    bg_per_step = P_BG * n_neurons
-    proj_bytes = 9.0 * p_events + 8.0 * (p_spikes + bg_per_step)
-    pop_bytes = 32.0 * n_neurons
-    dominant = "projection" if proj_ms >= pop_ms else "population"
-    a_bytes, a_ms = (proj_bytes, proj_ms) if dominant == "projection" else (pop_bytes, pop_ms)
-    achieved = a_bytes / (a_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": f"{dominant} phase", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": src,
-                # DRAM bytes (read + write) of one saturated gather launch, measured with ncu on the
-                # same configuration at 200k neurons (677.2 MB read + 3.05 MB written for 2e8
-                # synapses), scaled by the synapse count; a step of the timed region that scatters
-                # moves far less. The gather layout holds 4 B per synapse (presynaptic index and an
-                # 8-bit weight-dictionary index; target and delay are implied by the position), so
-                # the bytes actually moved are below the 9 B per event counted as algorithmic.
-                "traffic": GATHER_DRAM_BYTES_PER_SYNAPSE * n_neurons * args.fan_in,
-                "traffic_per": "saturated gathered step (ncu at 200k neurons, scaled by synapses)",
-                # The same traffic over the projection phase of the profiled (saturated) steps.
-                "traffic_frac": GATHER_DRAM_BYTES_PER_SYNAPSE * n_neurons * args.fan_in / (proj_ms / 1e3) / 1e9 / hbm,
-                "phase_ms_per_step": {"population": pop_ms, "projection": proj_ms,
-                                      "stdp": ph[2] / args.profile_steps, "step_end": ph[3] / args.profile_steps},
-                "algorithmic_bytes_per_step": {"projection": proj_bytes, "population": pop_bytes},
-                "whole_step_hbm_frac": (proj_bytes + pop_bytes) / (ms / args.steps / 1e3) / 1e9 / hbm}
+    a_bytes = algorithmic_bytes(events, n_neurons * K, spikes + bg_rows)
+    achieved = a_bytes / (ms / 1e3) / 1e9
+    kernel_name = {T.STEP_GRID: f"grid_net_kernel (persistent step kernel, one launch of {K} steps)",
+                   T.STEP_PHASES: "whole step (per-phase kernels in CUDA graphs)",
+                   T.STEP_FUSED: "small_net_kernel"}[step_kernel]
+    roofline = {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": src, "steps": f"{W}..{W + K - 1}",
+                "launch_ms": ms, "algorithmic_bytes_per_launch": a_bytes,
+                "bytes_model": "9 B per synaptic event + 32 B per neuron update + 8 B per spike row",
+                "traffic": None}
+    per_step_share = spikes / (n_neurons * K)
+    regime = "sparse (every step below the pull threshold: scattered)" if per_step_share < args.pull_threshold \
+        else "mixed or saturated"
 
-    # End to end through the C ABI with host buffers.
+    extra = {}
+    if rank == 0 and not args.no_extra_windows:
+        # Saturated window of the same run (every neuron fires every step; steps gathered).
+        b.step(sat0 - (W + K))
+        s0, q0, _ = b.counters()
+        ms_sat = b.step_timed(sat_steps)
+        s1, q1, _ = b.counters()
+        rows_sat = (q1 - q0) + int(sched.offsets[sat0 + sat_steps] - sched.offsets[sat0])
+        ab = algorithmic_bytes(s1 - s0, n_neurons * sat_steps, rows_sat)
+        extra["saturated_window"] = {
+            "steps": f"{sat0}..{sat0 + sat_steps - 1}", "value": (s1 - s0) / (ms_sat / 1e3), "unit": UNIT,
+            "ms_per_step": ms_sat / sat_steps, "firing_rate": (q1 - q0) / (n_neurons * sat_steps),
+            "effective_frac": ab / (ms_sat / 1e3) / 1e9 / hbm,
+            "note": "effective: the plan's 9 B per event over the step time; the gather layout moves 4 B per "
+                    "synapse (dictionary weights, target and delay implied), so this can exceed 1"}
+        # The per-phase kernels on the same timed window (for comparison with the persistent kernel).
+        if step_kernel == T.STEP_GRID:
+            bp, _, cp = large_backend(local, n_neurons, args.fan_in, args.pull_threshold, T.STEP_PHASES)
+            bp.generate_bernoulli_schedule(cp, n_neurons, P_BG, 0, W + K, seed=chan_seed)
+            bp.step(W)
+            e0p, _, _ = bp.counters()
+            ms_p = bp.step_timed(K)
+            e1p, _, _ = bp.counters()
+            bp.close()
+            extra["per_phase_kernels_same_window"] = {
+                "value": (e1p - e0p) / (ms_p / 1e3), "unit": UNIT, "ms_per_step": ms_p / K,
+                "same_events": bool(e1p - e0p == events)}
+    b.close()
+
     e2e = None
-    if rank == 0 and args.e2e_steps > 0:
-        start = b.get_step()
-        sched = Nw.bernoulli_schedule(chan_uid, SEED + 7, n_neurons, args.e2e_steps, P_BG, step0=start)
-        b.record_spikes(pop_uid, True)
-        b.synchronize()
-        ea, _, _ = b.counters()
-        h2d = d2h = n_out = 0
-        buf = np.empty(n_neurons, np.uint32)
-        t0 = time.perf_counter()
-        # Pipelined as a caller would: step k + 1 is queued (its input sent) before step k's spikes are
-        # read, so the device runs step k + 1 while the host copies and expands step k's spikes.
-        for k in range(args.e2e_steps + 1):
-            if k < args.e2e_steps:
-                idx = sched.at(k)
-                b.send_spikes(chan_uid, idx, start + k)
-                h2d += idx.nbytes
-                b.step(1)
-            if k > 0:
-                out = b.spikes(pop_uid, start + k - 1, out=buf)  # ascending, as in the reference's SpikeMessage
-                b.discard_spikes(start + k)
-                # What crosses to the host is the step's spike bitmap (one bit per neuron), expanded there.
-                d2h += (n_neurons + 31) // 32 * 4
-                n_out += out.size
-        b.synchronize()
-        te = time.perf_counter() - t0
-        eb, _, _ = b.counters()
-        e2e = {"value": (eb - ea) / te, "unit": UNIT, "h2d_bytes_per_step": h2d / args.e2e_steps,
-               "d2h_bytes_per_step": d2h / args.e2e_steps, "steps": args.e2e_steps,
-               "ms_per_step": te / args.e2e_steps * 1e3, "spikes_returned_per_step": n_out / args.e2e_steps}
-        b.record_spikes(pop_uid, False)
+    if rank == 0 and not args.no_e2e:
+        e2e = e2e_window(local, n_neurons, args.fan_in, args.pull_threshold, chan_seed, W, K, sched)
+        e2e["same_events_as_value"] = bool(e2e["events"] == events)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample()
-    b.close()
+        cpu = cpu_baseline_sample(W, K)
 
-    batched = bp = stdp = None
+    batched = bp_ = stdp = None
     if rank == 0 and not args.no_forms:
         batched = batched_dense_measure(local)
-        bp = bptt_measure(local)
+        bp_ = bptt_measure(local)
         stdp = stdp_measure(local)
 
     if rank == 0:
+        launches = (K + 65535) // 65536 if step_kernel in (T.STEP_GRID, T.STEP_FUSED) else 5 * K
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded counter-based generator)",
-            "config": {"workload": "large_sparse_plain", "neurons": n_neurons, "fan_in": args.fan_in,
-                       "synapses": n_neurons * args.fan_in,
+            "config": {"workload": f"large_sparse_plain, steps {W}..{W + K - 1}: {regime}",
+                       "neurons": n_neurons, "fan_in": args.fan_in, "synapses": n_neurons * args.fan_in,
                        "delays": "1..20", "weights": "k/256, k in [-16,48]", "p_background": P_BG,
-                       "l2": "inputs larger than L2 (4 GB gather layout, 9 GB CSR), no flush",
+                       "l2": "inputs larger than L2 (9 GB CSR, 4 GB gather layout), no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "pull_threshold": args.pull_threshold},
-            "neuron_updates_per_s": n_neurons * world * args.steps / t,
-            "firing_rate": spikes / (n_neurons * args.steps),
-            "events_per_step": events / args.steps,
+                       "pull_threshold": args.pull_threshold, "step_mode": args.step_mode},
+            "neuron_updates_per_s": n_neurons * world * K / t,
+            "firing_rate": per_step_share,
+            "events_per_step": events / K,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            # Per step: the population kernel, one scatter kernel per projection (recurrent and
-            # background), the gather kernel of the recurrent projection, the end-of-step kernel.
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": launches,
             "clocks": clk.summary(),
             "build_s": t_build,
+            **extra,
             "batched_dense": batched,
-            "bptt": bp,
+            "bptt": bp_,
             "stdp": stdp,
         }
         print(json.dumps(line))

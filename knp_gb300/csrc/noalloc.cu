@@ -13,9 +13,18 @@
 // the process exits. Every call shares it and finds the last call's contents there; the kernels
 // rewrite every cell they read before reading it. Calls that overlap on the GPU (two streams, or
 // two threads) race on the scratch and must be serialised by the caller.
+//
+// Set-up: the CUDA runtime loads a module's device code and its __device__ arrays lazily, on first
+// use, and that load allocates device memory. So the first call in a CUDA context (per device, and
+// again after cudaDeviceReset, which replaces the context) loads this file's kernels and scratch array
+// and looks up the array's device address, with that device current; a caller makes that first call
+// during its own set-up, outside stream capture. Later calls in the same context reuse the address
+// and allocate nothing.
+#include <cmath>
 #include <cstdint>
 #include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -129,11 +138,48 @@ __global__ void na_step_offsets_kernel(const long long *chunk_offs, uint32_t chu
         step_offs[t] = chunk_offs[t * chunks];  // t == n_steps reads the total at counts[n_cells]
 }
 
-// Device address of the scratch array, looked up once per device with that device current.
+// Identity of the current CUDA context (unique in the process, never reused), through the driver
+// entry point cuCtxGetId; 0 if it cannot be read (the set-up then runs on every call, which stays
+// correct: a lookup in a loaded context allocates nothing).
+unsigned long long current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess)
+        {
+            get_current = reinterpret_cast<GetCurrent>(a);
+            get_id = reinterpret_cast<GetId>(b);
+        }
+        cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of the scratch array in the current context of `device` (which is current). The
+// first call in a context loads this file's kernels (cudaFuncGetAttributes makes the runtime load
+// them now rather than at their first launch) and the array, and looks up its address.
 long long *scratch_address(int device, cudaError_t &err)
 {
+    struct Slot
+    {
+        unsigned long long ctx = 0;
+        long long *addr = nullptr;
+    };
     static std::mutex m;
-    static long long *addr[64] = {};
+    static Slot slots[64];
     std::lock_guard<std::mutex> l(m);
     err = cudaSuccess;
     if (device < 0 || device >= 64)
@@ -141,14 +187,26 @@ long long *scratch_address(int device, cudaError_t &err)
         err = cudaErrorInvalidDevice;
         return nullptr;
     }
-    if (!addr[device])
+    // Before the runtime's first use of the device no context is current (id 0): the set-up below
+    // then runs and makes the primary context current.
+    const unsigned long long ctx = current_context_id();
+    Slot &s = slots[device];
+    if (s.addr && ctx != 0 && s.ctx == ctx) return s.addr;
+    cudaFuncAttributes fa{};
+    const void *kernels[] = {reinterpret_cast<const void *>(na_count_kernel), reinterpret_cast<const void *>(na_scan_kernel),
+                             reinterpret_cast<const void *>(na_write_kernel),
+                             reinterpret_cast<const void *>(na_step_offsets_kernel)};
+    for (const void *k : kernels)
     {
-        void *p = nullptr;
-        err = cudaGetSymbolAddress(&p, g_schedule_scratch);
+        err = cudaFuncGetAttributes(&fa, k);
         if (err != cudaSuccess) return nullptr;
-        addr[device] = static_cast<long long *>(p);
     }
-    return addr[device];
+    void *p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_schedule_scratch);
+    if (err != cudaSuccess) return nullptr;
+    s.ctx = current_context_id();
+    s.addr = static_cast<long long *>(p);
+    return s.addr;
 }
 
 }  // namespace
@@ -159,7 +217,13 @@ int bernoulli_schedule_noalloc(
     uint32_t n_sources, double p, uint64_t first_step, uint64_t n_steps, uint64_t seed, uint64_t stream,
     long long *d_offsets, uint32_t *d_idx, uint64_t capacity, uint64_t *n_idx, cudaStream_t s, const char **why)
 {
-    if (!d_offsets || !n_idx || (capacity && !d_idx))
+    if (!n_idx)
+    {
+        *why = "null n_idx";
+        return -1;
+    }
+    *n_idx = 0;  // every argument error leaves 0 here; only the capacity error reports a count
+    if (!d_offsets || (capacity && !d_idx))
     {
         *why = "null buffer";
         return -1;
@@ -167,6 +231,11 @@ int bernoulli_schedule_noalloc(
     if (n_steps == 0 || n_sources == 0)
     {
         *why = "n_steps and n_sources must be positive";
+        return -1;
+    }
+    if (!std::isfinite(p))
+    {
+        *why = "p must be a finite number";
         return -1;
     }
     if (n_steps > 65535)

@@ -81,8 +81,41 @@ def test_noalloc_schedule_rejects_sizes_beyond_its_scratch():
         1024 * 4096, 0.01, 0, 1000, 1, N.S_INPUT, ctypes.c_void_p(offs.data_ptr()), ctypes.c_void_p(idx.data_ptr()),
         16, ctypes.byref(n), None)
     assert rc == -1 and b"scratch" in lib.knp_gb300_last_error()
+    assert n.value == 0  # argument errors report no count
     # Capacity too small: the needed count comes back, nothing is written.
     rc = lib.knp_gb300_generate_bernoulli_schedule_noalloc(
         N_SRC, P, 0, STEPS, SEED, N.S_INPUT, ctypes.c_void_p(offs.data_ptr()), ctypes.c_void_p(idx.data_ptr()),
         16, ctypes.byref(n), None)
     assert rc == -1 and n.value > 16
+    # A probability that is not a finite number is refused (and reports no count).
+    rc = lib.knp_gb300_generate_bernoulli_schedule_noalloc(
+        N_SRC, float("nan"), 0, STEPS, SEED, N.S_INPUT, ctypes.c_void_p(offs.data_ptr()),
+        ctypes.c_void_p(idx.data_ptr()), 16, ctypes.byref(n), None)
+    assert rc == -1 and n.value == 0 and b"finite" in lib.knp_gb300_last_error()
+
+
+def test_noalloc_schedule_later_calls_allocate_no_device_memory():
+    """After the first call in a process (which loads the entry point's kernels and scratch array),
+    a later call leaves the device's free memory unchanged."""
+    import torch
+
+    from knp_gb300 import _capi
+
+    lib = _capi.lib()
+    offs = torch.empty(STEPS + 1, dtype=torch.int64, device="cuda")
+    idx = torch.empty(40_000, dtype=torch.int32, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n = ctypes.c_uint64(0)
+
+    def call():
+        rc = lib.knp_gb300_generate_bernoulli_schedule_noalloc(
+            N_SRC, P, 0, STEPS, SEED, N.S_INPUT, ctypes.c_void_p(offs.data_ptr()), ctypes.c_void_p(idx.data_ptr()),
+            idx.numel(), ctypes.byref(n), stream)
+        assert rc == 0, lib.knp_gb300_last_error()
+        torch.cuda.synchronize()
+
+    call()  # set-up call
+    free_before, _ = torch.cuda.mem_get_info()
+    call()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
