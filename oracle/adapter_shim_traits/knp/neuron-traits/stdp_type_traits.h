@@ -1,0 +1,9 @@
+// TEST INFRASTRUCTURE — stand-in for knp/neuron-traits-library/include/knp/neuron-traits/stdp_type_traits.h.
+#pragma once
+#include "blifat.h"
+#include "stdp_synaptic_resource_rule.h"
+
+namespace knp::neuron_traits
+{
+using SynapticResourceSTDPBLIFATNeuron = SynapticResourceSTDPNeuron<BLIFATNeuron>;
+}  // namespace knp::neuron_traits
