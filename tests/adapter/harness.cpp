@@ -67,13 +67,13 @@ int run_golden(const std::string &kind)
     if (kind == "resource")
     {
         GB300Backend::ResourceBLIFATPopulation pop(
-            [](size_t) { return std::optional<nt::neuron_parameters<nt::SynapticResourceSTDPBLIFATNeuron>>({}); }, 1);
+            [](size_t) { return std::make_optional(nt::neuron_parameters<nt::SynapticResourceSTDPBLIFATNeuron>{}); }, 1);
         pop_uid = pop.get_uid();
         pops.emplace_back(pop);
     }
     else
     {
-        GB300Backend::BLIFATPopulation pop([](size_t) { return std::optional<nt::neuron_parameters<nt::BLIFATNeuron>>({}); },
+        GB300Backend::BLIFATPopulation pop([](size_t) { return std::make_optional(nt::neuron_parameters<nt::BLIFATNeuron>{}); },
                                            1);
         pop_uid = pop.get_uid();
         pops.emplace_back(pop);
@@ -149,7 +149,7 @@ int run_golden(const std::string &kind)
 int run_impacts()
 {
     GB300Backend backend;
-    GB300Backend::LIFPopulation pop([](size_t) { return std::optional<nt::neuron_parameters<nt::LIFNeuron>>({}); }, 1);
+    GB300Backend::LIFPopulation pop([](size_t) { return std::make_optional(nt::neuron_parameters<nt::LIFNeuron>{}); }, 1);
     const UID pop_uid = pop.get_uid();
     backend.load_all_populations({pop});
     backend.load_all_projections({});
