@@ -403,13 +403,22 @@ def bptt_measure(device: int, iters: int = 10, warmup: int = 3):
         loss = it()
     e1.record()
     torch.cuda.synchronize(dev)
+    bptt.check_gemm_errors(dev)
     ms = e0.elapsed_time(e1) / iters
     layers = [(784, 512), (512, 512), (512, 10)]
     tb = 32 * 128
-    # Forward GEMMs, recomputed input GEMMs in the backward, weight and input gradients.
-    flops = 2.0 * tb * sum(a * c for a, c in layers) * 4
+    # Algorithmic: forward GEMMs, recomputed inputs, weight and input gradients (4 per layer, no
+    # input gradient for the first layer). Executed on the tensor cores: the two gradient GEMMs carry
+    # dI as two BF16 terms (K doubled).
+    fwd = 2.0 * tb * sum(a * c for a, c in layers)
+    first = 2.0 * tb * layers[0][0] * layers[0][1]
+    flops = fwd * 4 - first
+    executed = fwd * 2 + 2 * (fwd * 2 - first)
     return {"workload": "bptt: LIF 784-512-512-10, batch 128, T 32, checkpoint 8", "ms_per_iter": ms,
             "gemm_flops_per_iter": flops, "achieved_tflops": flops / (ms / 1e3) / 1e12,
+            "tensor_flops_executed_per_iter": executed,
+            "gemm": "tcgen05 BF16 (knp_gb300_bf16_gemm_tn, pipelined 128x128 tiles), FP32 accumulation; "
+                    "gradients as BF16 hi + lo",
             "loss": float(loss.item())}
 
 

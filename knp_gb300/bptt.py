@@ -7,6 +7,16 @@ products exact in FP32, FP32 accumulation); the LIF recurrence over T and its ba
 hand-written kernels of knp_gb300/csrc/bptt.cu behind ``LIFLayerFn`` (torch.autograd.Function).
 The forward keeps the membrane state only every ``checkpoint`` steps; the backward recomputes each
 segment. The reference has no gradient-based training; this form has no counterpart there.
+
+Every contraction runs on the library's tcgen05 BF16 GEMM (knp_gb300_bf16_gemm_tn, FP32 accumulation
+in tensor memory): the forward and recomputed inputs take the 0/1 spikes and the BF16 weights
+directly (exact operands); the weight and input gradients carry the FP32 surrogate gradients dI as
+two BF16 terms, dI = hi + lo with hi = bf16(dI) and lo = bf16(dI - hi), concatenated along K, so
+each product is exact in FP32 and dI is represented to 2^-17 relative. The sigmoid-relaxed forward
+(a verification mode whose recurrence amplifies input errors about 1e5-fold) has continuous layer
+outputs: there every layer input and dI are split into three BF16 terms, which hold every normal
+FP32 value exactly (8 + 8 + 8 significand bits), so each contraction equals an FP32 GEMM with exact
+products.
 """
 from __future__ import annotations
 
@@ -32,20 +42,65 @@ def bf16_values(w: torch.Tensor) -> torch.Tensor:
     return w.to(torch.bfloat16).to(torch.float32)
 
 
-def _mm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
-    """FP32 GEMM with IEEE FP32 arithmetic (no TF32 rounding of the operands)."""
-    cm = torch.backends.cuda.matmul
-    prev = cm.allow_tf32
-    prev_p = getattr(cm, "fp32_precision", None)
-    cm.allow_tf32 = False
-    if prev_p is not None:
-        cm.fp32_precision = "ieee"
-    try:
-        return a @ b
-    finally:
-        if prev_p is not None:
-            cm.fp32_precision = prev_p
-        cm.allow_tf32 = prev
+_ERR = {}
+
+
+def _err_word(device) -> torch.Tensor:
+    """Device error word of the GEMMs on `device` (bit 0: a tensor-core completion wait timed out)."""
+    key = str(device)
+    if key not in _ERR:
+        _ERR[key] = torch.zeros(1, dtype=torch.int32, device=device)
+    return _ERR[key]
+
+
+def check_gemm_errors(device="cuda"):
+    """Raises if a GEMM of this module reported a timeout on `device` (one device-to-host read)."""
+    e = _err_word(torch.device(device))
+    if int(e.item()) != 0:
+        e.zero_()
+        raise RuntimeError("a tcgen05 GEMM completion wait timed out")
+
+
+def _pad_k(x: torch.Tensor, mult: int = 8) -> torch.Tensor:
+    """Zero columns up to a multiple of `mult` (the pipelined GEMM wants 16-byte rows)."""
+    k = x.shape[1]
+    kp = (k + mult - 1) // mult * mult
+    return x if kp == k else torch.nn.functional.pad(x, (0, kp - k))
+
+
+def gemm_tn(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """D[M, N] = A[M, K] @ B[N, K]^T (FP32) on the tcgen05 tensor cores; a and b are BF16, row-major."""
+    assert a.dtype == torch.bfloat16 and b.dtype == torch.bfloat16 and a.shape[1] == b.shape[1]
+    a = _pad_k(a.contiguous())
+    b = _pad_k(b.contiguous())
+    M, K = a.shape
+    N = b.shape[0]
+    d = torch.empty((M, N), device=a.device, dtype=torch.float32)
+    _capi.check(_capi.lib().knp_gb300_bf16_gemm_tn(_p(a), _p(b), _p(d), M, N, K, _p(_err_word(a.device)), _stream()))
+    return d
+
+
+def bf16_terms(x: torch.Tensor, n: int):
+    """n BF16 tensors whose FP32 sum is x: term k is bf16 of x minus the terms before it. n = 1 for
+    values that are BF16 already (0/1 spikes, BF16 weights); n = 2 leaves O(2^-17 |x|); n = 3 is exact
+    for normal FP32 values."""
+    terms, rest = [], x.float()
+    for k in range(n):
+        t = rest.to(torch.bfloat16)
+        terms.append(t)
+        if k + 1 < n:
+            rest = rest - t.to(torch.float32)
+    return terms
+
+
+def gemm_terms(a_terms, b_terms) -> torch.Tensor:
+    """(sum a_i) @ (sum b_j)^T as one GEMM: every pair (a_i, b_j) concatenated along K, each part padded
+    to 16-byte rows."""
+    pairs = [(a, b) for a in a_terms for b in b_terms]
+    if len(pairs) == 1:
+        return gemm_tn(*pairs[0])
+    return gemm_tn(torch.cat([_pad_k(a.contiguous()) for a, _ in pairs], 1),
+                   torch.cat([_pad_k(b.contiguous()) for _, b in pairs], 1))
 
 
 class LIFLayerFn(torch.autograd.Function):
@@ -55,32 +110,35 @@ class LIFLayerFn(torch.autograd.Function):
     def forward(ctx, s_in, w_master, beta: float, theta: float, checkpoint: int, relaxed: bool, k: float):
         T, B, n_in = s_in.shape
         n_out = w_master.shape[1]
-        wb = bf16_values(w_master)
+        wb = w_master.to(torch.bfloat16)  # [n_in, n_out]
         s_in = s_in.contiguous()
-        I = _mm(s_in.reshape(T * B, n_in), wb).reshape(T, B, n_out).contiguous()
+        s_terms = bf16_terms(s_in.reshape(T * B, n_in), 3 if relaxed else 1)  # 0/1 spikes are exact
+        I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()
         S = torch.empty_like(I)
         ckpt = torch.empty(((T + checkpoint - 1) // checkpoint, B, n_out), device=I.device, dtype=torch.float32)
         _capi.check(_capi.lib().knp_gb300_lif_scan_forward(
             _p(I), _p(S), _p(ckpt), T, B * n_out, beta, theta, checkpoint, int(relaxed), k, _stream()))
-        ctx.save_for_backward(s_in, wb, ckpt)
-        ctx.cfg = (beta, theta, checkpoint, relaxed, k)
+        ctx.save_for_backward(wb, ckpt, *s_terms)
+        ctx.cfg = (T, B, beta, theta, checkpoint, relaxed, k)
         return S
 
     @staticmethod
     def backward(ctx, dS):
-        s_in, wb, ckpt = ctx.saved_tensors
-        beta, theta, checkpoint, relaxed, k = ctx.cfg
-        T, B, n_in = s_in.shape
-        n_out = wb.shape[1]
-        flat_in = s_in.reshape(T * B, n_in)
-        I = _mm(flat_in, wb).reshape(T, B, n_out).contiguous()  # recomputed, not stored
+        wb, ckpt, *s_terms = ctx.saved_tensors
+        T, B, beta, theta, checkpoint, relaxed, k = ctx.cfg
+        n_in, n_out = wb.shape
+        I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()  # recomputed, not stored
         dS = dS.contiguous()
         dI = torch.empty_like(I)
         _capi.check(_capi.lib().knp_gb300_lif_scan_backward(
             _p(I), _p(ckpt), _p(dS), _p(dI), T, B * n_out, beta, theta, checkpoint, int(relaxed), k, _stream()))
-        flat_dI = dI.reshape(T * B, n_out)
-        dW = _mm(flat_in.t(), flat_dI)
-        ds_in = _mm(flat_dI, wb.t()).reshape(T, B, n_in) if ctx.needs_input_grad[0] else None
+        d_terms = bf16_terms(dI.reshape(T * B, n_out), 3 if relaxed else 2)
+        # dW[n_in, n_out] = S^T dI: K = T B per (S term, dI term) pair.
+        dW = gemm_terms([s.t() for s in s_terms], [d.t() for d in d_terms])
+        ds_in = None
+        if ctx.needs_input_grad[0]:
+            # ds_in[TB, n_in] = dI W^T, W as [n_in, n_out]: K = n_out per dI term.
+            ds_in = gemm_terms(d_terms, [wb]).reshape(T, B, n_in)
         return ds_in, dW, None, None, None, None, None
 
 

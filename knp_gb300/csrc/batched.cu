@@ -1,8 +1,8 @@
 // Batched form on 5th-generation tensor cores.
 //
-// bf16_gemm_tn: D[M x N] (FP32) = A[M x K] * B[N x K]^T with BF16 operands (row-major, K
-// contiguous), tcgen05.mma kind::f16 with the accumulator in tensor memory. Used to validate the
-// tcgen05 encodings and as a library GEMM of spike matrices.
+// bf16_gemm_tn_simple: D[M x N] (FP32) = A[M x K] * B[N x K]^T with BF16 operands (row-major, K
+// contiguous), tcgen05.mma kind::f16 with the accumulator in tensor memory, single stage; the
+// pipelined GEMM is gemm.cu.
 #include <algorithm>
 #include <cstdlib>
 #include <cstdint>
@@ -125,7 +125,9 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(
 
 }  // namespace
 
-int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, cudaStream_t s)
+// The single-stage GEMM: any K and alignment (bf16_gemm_tn in gemm.cu takes it for shapes the
+// pipelined kernel does not).
+int bf16_gemm_tn_simple(const void *A, const void *B, float *D, int M, int N, int K, unsigned int *d_err, cudaStream_t s)
 {
     if (M < 1 || N < 1 || K < 1 || !A || !B || !D || !d_err) return -1;
     dim3 grid((M + kGemmM - 1) / kGemmM, (N + kGemmN - 1) / kGemmN);
