@@ -108,8 +108,12 @@ KNP_GB300_API int knp_gb300_read_lif_population(knp_gb300_backend *b, knp_uid po
  * (weight[i], delay[i], out_type[i]) from presynaptic neuron pre[i] to postsynaptic neuron post[i].
  * kind: KNP_SYNAPSE_DELTA or KNP_SYNAPSE_ADDITIVE_STDP_DELTA (tau_plus/tau_minus required, uniform
  * per projection). out_type may be NULL (all EXCITATORY). pre_uid may be the all-zero UID (the
- * projection then receives spikes only through knp_gb300_subscribe). KNP_OUT_BLOCKING is rejected:
- * its last-writer-wins effect depends on message order. Replaces: load_projections /
+ * projection then receives spikes only through knp_gb300_subscribe). KNP_OUT_BLOCKING synapses are
+ * taken in delta projections (not in additive-STDP ones) of backends with at most 62 projections: of
+ * the BLOCKING impacts a neuron receives in a step, the last one in the reference's message order
+ * (projection load order; within a projection, larger delays first, then ascending spike index and
+ * synapse order; external messages last) sets its total blocking period (blifat_impl.h:86).
+ * Replaces: load_projections /
  * load_all_projections for Projection<DeltaSynapse> and Projection<AdditiveSTDPDeltaSynapse>
  * (backend.h:206; core backend.h:137; impl/backend.cpp:158-178).
  */
@@ -249,7 +253,8 @@ KNP_GB300_API int knp_gb300_generate_bernoulli_schedule_noalloc(
 /**
  * Send an external SynapticImpactMessage to population `receiver` (impacts post_idx[i], value[i],
  * out_type[i] (NULL = EXCITATORY)); applied at the next step, after impacts of the backend's own
- * projections. Replaces: MessageEndpoint::send_message of a SynapticImpactMessage
+ * projections (so a BLOCKING impact here overrides theirs, and within one step the last message's last
+ * BLOCKING impact on a neuron counts). Replaces: MessageEndpoint::send_message of a SynapticImpactMessage
  *   (knp/tests/framework/lif_test.cpp:78-86).
  */
 KNP_GB300_API int knp_gb300_send_impacts(

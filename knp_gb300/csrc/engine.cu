@@ -234,9 +234,10 @@ void Backend::load_projection(
         p->type.assign(type, type + n_syn);
         for (uint8_t t : p->type)
         {
-            if (t == KNP_OUT_BLOCKING)
-                throw Error(KNP_GB300_E_INVALID,
-                            "BLOCKING synapses are not supported: their effect depends on message order");
+            // A BLOCKING impact carries the synapse's weight at the spike; an additive-STDP weight can
+            // change before the impact arrives, so BLOCKING synapses are taken in delta projections.
+            if (t == KNP_OUT_BLOCKING && kind != KNP_SYNAPSE_DELTA)
+                throw Error(KNP_GB300_E_INVALID, "BLOCKING synapses are supported in delta projections only");
             if (t > KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
         }
         if (std::all_of(p->type.begin(), p->type.end(), [&](uint8_t t) { return t == p->type[0]; }) && n_syn)
@@ -362,7 +363,7 @@ void Backend::build_population(PopulationSlot &p)
     const uint32_t n = p.n, np = p.n_pad;
     // Incoming projections decide ring length, accumulator mode and the live input channels.
     uint32_t slots = 1;
-    bool dyadic = true, stdp_in = false, g_in = false, d_in = false, forcing_exc = false;
+    bool dyadic = true, stdp_in = false, g_in = false, d_in = false, forcing_exc = false, blk_in = false;
     for (auto &pr : projs_)
     {
         if (!(pr->post_uid == p.uid)) continue;
@@ -374,6 +375,7 @@ void Backend::build_population(PopulationSlot &p)
         { return has_type ? std::find(pr->type.begin(), pr->type.end(), t) != pr->type.end() : t == 0; };
         g_in = g_in || any_type(KNP_OUT_INHIBITORY_CONDUCTANCE);
         d_in = d_in || any_type(KNP_OUT_DOPAMINE);
+        blk_in = blk_in || any_type(KNP_OUT_BLOCKING);
         if (pr->kind == KNP_SYNAPSE_DELTA && any_type(KNP_OUT_EXCITATORY)) forcing_exc = true;
     }
     if (p.has_external_impacts) g_in = d_in = forcing_exc = true;
@@ -404,6 +406,14 @@ void Backend::build_population(PopulationSlot &p)
     {
         if (g_in) rg.g = arena_.make<float>(cells);
         if (d_in) rg.dopa = arena_.make<float>(cells);
+        if (blk_in || p.has_external_impacts)
+        {
+            // BLOCKING keys per (slot, neuron); the weight table by projection load order is filled once
+            // every projection's CSR exists (init).
+            rg.blk = arena_.make<unsigned long long>(cells);
+            rg.blk_w = arena_.make<const float *>(std::max<size_t>(projs_.size(), 1));
+            if (p.has_external_impacts) rg.blk_ext = arena_.make<long long>(np);
+        }
         if (res && forcing_exc)
         {
             rg.words = (np + 31) / 32;
@@ -511,6 +521,7 @@ void Backend::build_population(PopulationSlot &p)
             }))
         f |= kLiveRefract;
     if (d_in) f |= kLiveDopa;
+    if (rg.blk) f |= kLiveBlock;
     if (f & (kLiveBlock | kLiveVRead | kLiveBurst)) f |= kLiveVPre;
     if (res)
     {
@@ -721,6 +732,8 @@ void Backend::build_projection(ProjectionSlot &p)
     d.type = p.type_d;
     d.uniform_type = p.type.size() == 1 ? p.type[0] : 0;
     d.forcing = p.kind == KNP_SYNAPSE_DELTA ? 1 : 0;  // is_forced(): stdp_dispatcher.h:54-58, additive_stdp.h:199-203
+    for (size_t k = 0; k < projs_.size(); ++k)
+        if (projs_[k].get() == &p) d.order = static_cast<uint32_t>(k);
     if (post) d.ring = post->ring;
     // Spike sources: every subscribed sender, except STDP-only populations whose messages the
     // projection empties before propagating them (additive_stdp.h:162-166).
@@ -915,6 +928,11 @@ void Backend::init()
             for (uint32_t v : p->post)
                 if (v >= post->n) throw Error(KNP_GB300_E_INVALID, "postsynaptic index out of the target population");
     }
+    if (projs_.size() > 62)
+        for (auto &p : projs_)
+            for (uint8_t ty : p->type)
+                if (ty == KNP_OUT_BLOCKING)
+                    throw Error(KNP_GB300_E_INVALID, "BLOCKING synapses need a backend of at most 62 projections");
     wire();
     // Per-step counters: population spike counts, then STDP touched counts.
     n_spike_counters_ = static_cast<uint32_t>(pops_.size());
@@ -938,6 +956,16 @@ void Backend::init()
     uint32_t ci = n_spike_counters_;
     for (auto &p : projs_)
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) p->stdp.touched_count = counters_ + ci++;
+    // BLOCKING weight tables: entry k is the CSR weight array of the projection loaded k-th.
+    for (auto &q : pops_)
+    {
+        if (!q->ring.blk) continue;
+        std::vector<const float *> tab(std::max<size_t>(projs_.size(), 1), nullptr);
+        for (size_t k = 0; k < projs_.size(); ++k)
+            if (projs_[k]->post_uid == q->uid) tab[k] = projs_[k]->w;
+        KNP_CUDA(cudaMemcpy(const_cast<const float **>(q->ring.blk_w), tab.data(), tab.size() * sizeof(const float *),
+                            cudaMemcpyHostToDevice));
+    }
     // Host copies of the synapse arrays are no longer needed, except what readback and STDP use.
     for (auto &p : projs_)
     {
@@ -1806,13 +1834,29 @@ void Backend::send_impacts(
     {
         if (post[i] >= q->n) throw Error(KNP_GB300_E_INVALID, "impact postsynaptic index out of range");
         const uint8_t t = type ? type[i] : 0;
-        if (t == KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "BLOCKING impacts are not supported");
         if (t > KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
         if (q->kind == KNP_NEURON_LIF && t > KNP_OUT_INHIBITORY_CURRENT)
             throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
         m.post.push_back(post[i]);
         m.value.push_back(value[i]);
         m.type.push_back(t);
+    }
+    // Of several BLOCKING impacts on one neuron only the last one in the message counts
+    // (blifat_impl.h:86): the earlier ones are dropped here, so the device writes each target once.
+    std::map<uint32_t, size_t> last_blk;
+    for (size_t i = 0; i < m.type.size(); ++i)
+        if (m.type[i] == KNP_OUT_BLOCKING) last_blk[m.post[i]] = i;
+    if (!last_blk.empty())
+    {
+        PendingImpacts r{receiver, forcing, {}, {}, {}};
+        for (size_t i = 0; i < m.type.size(); ++i)
+        {
+            if (m.type[i] == KNP_OUT_BLOCKING && last_blk[m.post[i]] != i) continue;
+            r.post.push_back(m.post[i]);
+            r.value.push_back(m.value[i]);
+            r.type.push_back(m.type[i]);
+        }
+        m = std::move(r);
     }
     pending_impacts_.push_back(std::move(m));
 }

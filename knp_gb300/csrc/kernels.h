@@ -54,7 +54,29 @@ struct RingView
     float *dopa;       // dopamine input, or null
     uint32_t *forced;  // forcing bitmap [slots][words], or null
     uint32_t words;
+    // BLOCKING impacts (last writer in message order wins), or null: per (slot, neuron) the largest
+    // key blocking_key() of the impacts arriving at that step; blk_w[order] is the weight array (CSR
+    // order) of the projection with load order `order`, blk_ext[neuron] the value of this step's last
+    // external BLOCKING impact (key kBlkExternal << kBlkOrderShift).
+    unsigned long long *blk;
+    const float *const *blk_w;
+    long long *blk_ext;
 };
+
+// Key of a BLOCKING impact: the reference applies the impacts of a step in message order and the last
+// one sets the blocking period (blifat_impl.h:86). Messages arrive in projection load order, then
+// the external messages; within a projection's message, impacts of earlier source steps (larger
+// delays) come first, then by ascending spike index and synapse order, which is the CSR position.
+constexpr int kBlkOrderShift = 58;
+constexpr int kBlkDelayShift = 50;
+constexpr unsigned long long kBlkExternal = 63;  // external SynapticImpactMessages come last
+constexpr unsigned long long kBlkPosMask = (1ull << kBlkDelayShift) - 1;
+__host__ __device__ inline unsigned long long blocking_key(uint32_t order, uint32_t delay, long long csr_pos)
+{
+    return (static_cast<unsigned long long>(order + 1) << kBlkOrderShift) |
+           (static_cast<unsigned long long>(255u - delay) << kBlkDelayShift) |
+           (static_cast<unsigned long long>(csr_pos) & kBlkPosMask);
+}
 
 // Liveness flags of a BLIFAT population: a field that is not live keeps a value that follows from
 // its initial value alone and is neither read nor written per step.
@@ -210,6 +232,7 @@ struct ProjectionDev
     const uint8_t *type;  // per-synapse output type, or null (uniform_type)
     int uniform_type;
     int forcing;  // impacts of this projection carry is_forcing (plain delta projections)
+    uint32_t order;  // load order among the backend's projections (message order of BLOCKING impacts)
     RingView ring;
     int n_src;
     SpikeSource src[kMaxSources];

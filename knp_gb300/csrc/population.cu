@@ -59,6 +59,12 @@ __global__ void apply_impacts_kernel(
         atomicAdd(ring.g + o, w);
     else if (ty == 3 && ring.dopa)
         atomicAdd(ring.dopa + o, w);
+    else if (ty == 4 && ring.blk)
+    {
+        // The host keeps only each target's last external BLOCKING impact of the step.
+        ring.blk_ext[i] = static_cast<long long>(w);
+        atomicMax(ring.blk + o, kBlkExternal << kBlkOrderShift);
+    }
 }
 
 }  // namespace

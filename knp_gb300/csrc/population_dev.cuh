@@ -350,6 +350,19 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
             s.ns = at(ns, k);
             s.phase = at(phase, k);
             s.block = (f & kLiveBlock) ? p.blocking[i] : 0;
+            if ((f & kLiveBlock) && rg.blk)
+            {
+                // The step's last BLOCKING impact sets the period (impact phase, blifat_impl.h:86).
+                const unsigned long long key = rg.blk[ro + k];
+                if (key)
+                {
+                    rg.blk[ro + k] = 0ull;
+                    const unsigned long long order = key >> kBlkOrderShift;
+                    s.block = order == kBlkExternal
+                                  ? rg.blk_ext[i]
+                                  : static_cast<long long>(rg.blk_w[order - 1][key & kBlkPosMask]);
+                }
+            }
             const bool spike = blifat_step<kFixed>(p, i, t, s, at(acc, k), acc_hi[k], acc_lo[k], at(gin, k), at(din, k));
             if (spike) mask |= 1u << k;
             if (f & kResource)

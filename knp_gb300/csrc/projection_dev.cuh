@@ -71,6 +71,10 @@ __device__ __forceinline__ void deliver(
     {
         if (p.ring.dopa) atomicAdd(p.ring.dopa + o, w);
     }
+    else if (ty == 4)
+    {
+        if (p.ring.blk) atomicMax(p.ring.blk + o, blocking_key(p.order, d, e));
+    }
 }
 
 // Sources of projection p at step t: idx[k] / cnt[k] for source k (unused entries empty); returns

@@ -305,3 +305,45 @@ def smallest_network(kind: str = "delta"):
             idx.append(0)
         offs[t + 1] = len(idx)
     return net, [SpikeSchedule(chan_uid, offs, np.array(idx, np.uint32))]
+
+
+def blocking_network(seed: int = 12, n: int = 400, n_in: int = 100, steps: int = 300):
+    """BLOCKING synapses (blifat_impl.h:86: the step's last BLOCKING impact in message order sets the
+    neuron's total blocking period) beside excitatory drive: n BLIFAT neurons (defaults); channel A ->
+    excitatory projection (p 0.2, w k/256 with k in [0, 96], delays 1..3); channel B -> BLOCKING
+    projection (p 0.05 plus repeated (pre, post) pairs, weights from {-3, -1.5, 2, 4.7, -6.2, 1}, delays
+    1..4); a recurrent excitatory projection (p 0.05, k in [-32, 64], delays 1..5) and a recurrent
+    BLOCKING projection (p 0.01, weights -2 or 3, delays 1..2). Inputs: A Bernoulli 0.1, B 0.05. The
+    population also takes external impact messages from channel uid_from_int(1203)."""
+    rng = np.random.default_rng(seed)
+    pop_uid = T.uid_from_int(1200)
+    pop = Population(pop_uid, T.BLIFAT, T.blifat_defaults(n))
+    chan_a, chan_b, chan_ext = T.uid_from_int(1201), T.uid_from_int(1202), T.uid_from_int(1203)
+
+    def rand_proj(uid, pre_uid, n_pre, p, weights_fn, d_lo, d_hi, out, extra_pairs=0):
+        pre, post = np.nonzero(rng.random((n_pre, n)) < p)
+        if extra_pairs:
+            k = rng.integers(0, pre.size, extra_pairs)
+            pre = np.concatenate([pre, pre[k]])
+            post = np.concatenate([post, post[k]])
+        w = np.asarray(weights_fn(pre.size), np.float32)
+        d = rng.integers(d_lo, d_hi + 1, pre.size).astype(np.uint32)
+        return Projection(uid, T.DELTA, pre_uid, pop_uid, pre.astype(np.uint32), post.astype(np.uint32), w, d,
+                          out_type=np.full(pre.size, out, np.uint8))
+
+    blk_w = np.float32([-3, -1.5, 2, 4.7, -6.2, 1])
+    projs = [
+        rand_proj(T.uid_from_int(1210), T.NULL_UID, n_in, 0.2, lambda s: rng.integers(0, 97, s) / 256.0, 1, 3,
+                  T.EXCITATORY),
+        rand_proj(T.uid_from_int(1211), T.NULL_UID, n_in, 0.05, lambda s: blk_w[rng.integers(0, blk_w.size, s)], 1, 4,
+                  T.BLOCKING, extra_pairs=200),
+        rand_proj(T.uid_from_int(1212), pop_uid, n, 0.05, lambda s: rng.integers(-32, 65, s) / 256.0, 1, 5,
+                  T.EXCITATORY),
+        rand_proj(T.uid_from_int(1213), pop_uid, n, 0.01, lambda s: np.where(rng.random(s) < 0.5, -2.0, 3.0), 1, 2,
+                  T.BLOCKING),
+    ]
+    net = Network([pop], projs, [(T.uid_from_int(1210), chan_a), (T.uid_from_int(1211), chan_b),
+                                 (pop_uid, chan_ext)])
+    return net, [bernoulli_schedule(chan_a, seed, n_in, steps, 0.1),
+                 bernoulli_schedule(chan_b, seed, n_in, steps, 0.05, stream=S_INPUT + 50)]
+

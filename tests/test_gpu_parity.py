@@ -615,3 +615,37 @@ def test_step_mode_selection_and_recording_change():
     b.step(50)
     for t in range(50, 100):
         np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t])
+
+
+@pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
+def test_blocking_synapses_and_impacts(mode):
+    """BLOCKING synapses (blifat_impl.h:86): of a step's BLOCKING impacts on a neuron the last in the
+    reference's message order sets its total blocking period (projection load order, then larger
+    delays first, then spike and synapse order; external messages last). Repeated (pre, post) pairs,
+    recurrent BLOCKING synapses and external BLOCKING impacts (two messages in one step, repeated
+    targets within a message) against the oracle: spikes every step and the blocking periods."""
+    net, scheds = N.blocking_network(seed=12, steps=200)
+    pop = net.populations[0].uid
+    ext = T.uid_from_int(1203)
+    rng = np.random.default_rng(5)
+    plan = {}
+    for t in range(3, 200, 7):
+        post = rng.integers(0, 400, 12).astype(np.uint32)
+        post[5] = post[2]  # a repeated target within the message
+        vals = rng.choice(np.float32([-4, -1, 2, 3.5, 6, 0.75]), 12).astype(np.float32)
+        types = rng.choice(np.uint8([T.BLOCKING, T.EXCITATORY]), 12, p=[0.7, 0.3]).astype(np.uint8)
+        plan[t] = [(post, vals, types)]
+        if t % 2:
+            plan[t].append((post[:4].copy(), np.float32([5, -2, 1, -7]), np.full(4, T.BLOCKING, np.uint8)))
+
+    def on_step(be, t, which):
+        for post, vals, types in plan.get(t, []):
+            be.send_impacts(ext, pop, post, vals, types, True)
+
+    g, b, o, oo = run_both(net, scheds, 200, on_step=on_step, step_mode=mode)
+    assert_same_spikes(g, o)
+    gs, _ = b.read_population(pop)
+    os_, _ = oo.blifat(pop)
+    np.testing.assert_array_equal(gs["total_blocking_period"], os_["total_blocking_period"])
+    assert (os_["total_blocking_period"] != np.iinfo(np.int64).max).sum() > 20
+    assert b.counters()[0] == oo.events

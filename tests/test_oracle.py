@@ -152,3 +152,17 @@ def test_struct_layouts():
     d = T.blifat_defaults(2)
     assert d["n_time_steps_since_last_firing"][0] == np.iinfo(np.uint64).max
     assert d["total_blocking_period"][0] == np.iinfo(np.int64).max
+
+
+@pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
+def test_restated_oracle_matches_reference_headers_blocking(oracle_lib):
+    """BLOCKING synapses (blifat_impl.h:86, last writer in message order): the restated oracle gives the
+    reference headers' spikes and blocking periods."""
+    net, scheds = N.blocking_network(seed=12, steps=120)
+    pop = net.populations[0].uid
+    a, oa = orc.run(net, scheds, 120, which="restated")
+    b, ob = orc.run(net, scheds, 120, which="reference")
+    for t, (x, y) in enumerate(zip(a[pop], b[pop])):
+        np.testing.assert_array_equal(x, y, err_msg=f"step {t}")
+    np.testing.assert_array_equal(oa.blifat(pop)[0]["total_blocking_period"], ob.blifat(pop)[0]["total_blocking_period"])
+    assert (oa.blifat(pop)[0]["total_blocking_period"] != np.iinfo(np.int64).max).sum() > 20
