@@ -9,6 +9,9 @@
  *   knp_resource_stdp_state   <- neuron_parameters<SynapticResourceSTDPNeuron<N>> extra fields,
  *                                knp/neuron-traits-library/include/knp/neuron-traits/stdp_synaptic_resource_rule.h:70-192
  *   knp_isi_status            <- ISIPeriodType, stdp_synaptic_resource_rule.h:46-66
+ *   knp_resource_synapse      <- STDPSynapticResourceRule, knp/synapse-traits-library/include/knp/synapse-traits/stdp_synaptic_resource_rule.h:45-89
+ *   knp_lif_neuron            <- neuron_parameters<LIFNeuron>, knp/neuron-traits-library/include/knp/neuron-traits/lif.h:84-118
+ *   knp_altai_neuron          <- neuron_parameters<AltAILIF>, knp/neuron-traits-library/include/knp/neuron-traits/altai_lif.h:164-335
  *   knp_stdp_processing       <- Projection<STDP<...>>::SharedSynapseParameters::ProcessingType, knp/core-library/include/knp/core/projection.h:139-150
  */
 #ifndef KNP_GB300_TYPES_H
@@ -41,14 +44,17 @@ typedef enum knp_neuron_kind
 {
     KNP_NEURON_BLIFAT = 0,
     KNP_NEURON_RESOURCE_STDP_BLIFAT = 1,
-    KNP_NEURON_LIF = 2
+    KNP_NEURON_LIF = 2,
+    KNP_NEURON_ALTAI_LIF = 3,
+    KNP_NEURON_RESOURCE_STDP_ALTAI_LIF = 4
 } knp_neuron_kind;
 
 /** Synapse model of a projection. */
 typedef enum knp_synapse_kind
 {
     KNP_SYNAPSE_DELTA = 0,
-    KNP_SYNAPSE_ADDITIVE_STDP_DELTA = 1
+    KNP_SYNAPSE_ADDITIVE_STDP_DELTA = 1,
+    KNP_SYNAPSE_RESOURCE_STDP_DELTA = 2
 } knp_synapse_kind;
 
 /** How an STDP projection treats spikes of one of its STDP populations. */
@@ -126,6 +132,24 @@ typedef struct knp_resource_stdp_state
 } knp_resource_stdp_state;
 
 /**
+ * Rule state of a synaptic-resource STDP delta synapse (synapse_parameters<
+ * SynapticResourceSTDPDeltaSynapse>::rule_, knp/synapse-traits-library/include/knp/synapse-traits/
+ * stdp_synaptic_resource_rule.h:45-89), field for field. 40 bytes.
+ */
+typedef struct knp_resource_synapse
+{
+    float synaptic_resource;              /* default 0 */
+    float w_min;                          /* default 0 */
+    float w_max;                          /* default 1 */
+    float d_u;                            /* default 0 */
+    uint32_t dopamine_plasticity_period;  /* default 0 */
+    uint32_t had_hebbian_update;          /* bool */
+    uint64_t last_spike_step;             /* default 0 */
+    uint32_t has_contributed;             /* bool */
+    uint32_t pad_;
+} knp_resource_synapse;
+
+/**
  * LIF neuron parameters and state, field for field as neuron_parameters<LIFNeuron>
  * (knp/neuron-traits-library/include/knp/neuron-traits/lif.h:84-118). 24 bytes.
  */
@@ -139,6 +163,31 @@ typedef struct knp_lif_neuron
     uint32_t refract_period;
 } knp_lif_neuron;
 
+/**
+ * AltAI-LIF neuron parameters and state, field for field and in the same layout as
+ * neuron_parameters<AltAILIF> (knp/neuron-traits-library/include/knp/neuron-traits/altai_lif.h:
+ * 164-335; bools as bytes). 48 bytes. A KNP_NEURON_RESOURCE_STDP_ALTAI_LIF population keeps a
+ * knp_resource_stdp_state beside each neuron, as the BLIFAT variant does.
+ */
+typedef struct knp_altai_neuron
+{
+    uint8_t is_diff;                         /* default 0 */
+    uint8_t is_reset;                        /* default 1 */
+    uint8_t leak_rev;                        /* default 1 */
+    uint8_t saturate;                        /* default 1 */
+    uint8_t do_not_save;                     /* default 0 */
+    uint8_t pad0_[3];
+    float potential;
+    float pre_impact_potential;
+    uint16_t activation_threshold;           /* default 1 */
+    uint16_t negative_activation_threshold;  /* default 30000 */
+    int16_t potential_leak;                  /* default 0 */
+    uint16_t potential_reset_value;          /* default 0 */
+    double dopamine_value;
+    double additional_threshold;
+    int64_t activity_time;                   /* default 0 */
+} knp_altai_neuron;
+
 #ifdef __cplusplus
 }
 #endif
@@ -147,6 +196,8 @@ typedef struct knp_lif_neuron
 static_assert(sizeof(knp_lif_neuron) == 24, "knp_lif_neuron layout");
 static_assert(sizeof(knp_blifat_neuron) == 192, "knp_blifat_neuron layout");
 static_assert(sizeof(knp_resource_stdp_state) == 72, "knp_resource_stdp_state layout");
+static_assert(sizeof(knp_resource_synapse) == 40, "knp_resource_synapse layout");
+static_assert(sizeof(knp_altai_neuron) == 48, "knp_altai_neuron layout");
 #endif
 
 #endif /* KNP_GB300_TYPES_H */

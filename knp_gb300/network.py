@@ -71,8 +71,8 @@ S_PRE, S_WEIGHT, S_DELAY, S_EXISTS, S_INPUT, S_IMAGE = range(1, 7)
 class Population:
     uid: bytes
     kind: int
-    neurons: np.ndarray  # BLIFAT_DTYPE or LIF_DTYPE
-    resource: np.ndarray | None = None  # RESOURCE_DTYPE for RESOURCE_STDP_BLIFAT
+    neurons: np.ndarray  # BLIFAT_DTYPE, LIF_DTYPE or ALTAI_DTYPE
+    resource: np.ndarray | None = None  # RESOURCE_DTYPE for the resource-STDP kinds
 
     @property
     def size(self) -> int:
@@ -93,6 +93,8 @@ class Projection:
     tau_plus: np.ndarray | None = None  # float32, additive STDP only
     tau_minus: np.ndarray | None = None
     stdp_populations: dict = field(default_factory=dict)  # uid -> STDP_ONLY / STDP_AND_SPIKE
+    rule: np.ndarray | None = None  # RESOURCE_SYNAPSE_DTYPE, resource-STDP synapses only
+    locked: bool = True  # resource-STDP: weights start locked (projection.h:384-396)
 
     @property
     def size(self) -> int:
@@ -295,6 +297,26 @@ def smallest_network(kind: str = "delta"):
         loop = Projection(loop_uid, T.ADDITIVE_STDP_DELTA, pop_uid, pop_uid, one, one, np.ones(1, np.float32),
                           np.full(1, 6, np.uint32), tau_plus=np.ones(1, np.float32), tau_minus=np.ones(1, np.float32),
                           stdp_populations={pop_uid: T.STDP_AND_SPIKE})
+    elif kind in ("resource_stdp", "resource_stdp_altai"):
+        # single_thread_cpu_test.cpp:179-355: synaptic-resource STDP synapses (input rule {resource 0,
+        # w_min 1, w_max 2, d_u 0.1}, loop rule {0, 1, 2}) onto one resource-STDP neuron (BLIFAT or
+        # AltAI-LIF; synaptic resource threshold 1, free resource 2, isi_max 0), learning started.
+        res = T.resource_defaults(1)
+        res["synaptic_resource_threshold"] = 1.0
+        res["free_synaptic_resource"] = 2.0
+        res["isi_max"] = 0
+        if kind == "resource_stdp":
+            pop = Population(pop_uid, T.RESOURCE_STDP_BLIFAT, T.blifat_defaults(1), res)
+        else:
+            pop = Population(pop_uid, T.RESOURCE_STDP_ALTAI_LIF, T.altai_defaults(1), res)
+        rule_in = T.resource_synapse_defaults(1)
+        rule_in["w_min"], rule_in["w_max"], rule_in["d_u"] = 1.0, 2.0, np.float32(0.1)
+        rule_loop = T.resource_synapse_defaults(1)
+        rule_loop["w_min"], rule_loop["w_max"] = 1.0, 2.0
+        inp = Projection(in_uid, T.RESOURCE_STDP_DELTA, T.NULL_UID, pop_uid, one, one, np.ones(1, np.float32),
+                         np.ones(1, np.uint32), rule=rule_in, locked=False)
+        loop = Projection(loop_uid, T.RESOURCE_STDP_DELTA, pop_uid, pop_uid, one, one, np.ones(1, np.float32),
+                          np.full(1, 6, np.uint32), rule=rule_loop, locked=False)
     else:
         raise ValueError(kind)
     net = Network([pop], [inp, loop], [(in_uid, chan_uid)])
@@ -346,4 +368,156 @@ def blocking_network(seed: int = 12, n: int = 400, n_in: int = 100, steps: int =
                                  (pop_uid, chan_ext)])
     return net, [bernoulli_schedule(chan_a, seed, n_in, steps, 0.1),
                  bernoulli_schedule(chan_b, seed, n_in, steps, 0.05, stream=S_INPUT + 50)]
+
+
+def _aligned(n_pre: int, n_post: int):
+    """The reference's aligned synapse generator (synapse_generators.h:94-120): max(n_pre, n_post)
+    synapses; the larger side is indexed by the synapse index, the other by index / pack size."""
+    i = np.arange(max(n_pre, n_post), dtype=np.uint32)
+    if n_pre >= n_post:
+        return i, i // np.uint32(n_pre // n_post)
+    return i // np.uint32(n_post // n_pre), i
+
+
+def resource_stdp_network(seed: int = 21, samples: int = 20, n_in: int = 784, per_column: int = 20,
+                          classes: int = 10, potential_decay: float = 0.0, steps_per_sample: int = 15,
+                          active_steps: int = 10, label_step: int = 11):
+    """A network shaped like the reference's mnist-learn BLIFAT model (examples/mnist-learn/models/
+    blifat/construct_network.cpp:64-223, hyperparameters.h:35-117) on synthetic blob images: an
+    image channel (n_in) -> all-to-all SynapticResourceSTDPDeltaSynapse projection (w_min -0.253, w_max
+    0.0924, dopamine plasticity period 10, resource from weight 0) -> INPUT (classes * per_column
+    resource-STDP BLIFAT neurons: threshold 8.571, d_h -0.177, dopamine plasticity time 10, threshold
+    coefficient 0.218, isi_max 10, min potential 0, stability change 0.05, drain 27) -> OUTPUT (classes)
+    -> GATE (classes) by aligned delta projections (w 10; BLOCKING -10 output -> gate), the label
+    channel -> INPUT (DOPAMINE 0.18, delay 3; EXCITATORY -30, delay 4) and -> GATE (10), GATE -> INPUT
+    (10). Image pixels spike with p = 0.2 * intensity on the first `active_steps` steps of each
+    `steps_per_sample`-step sample; the label neuron (sample index mod classes) spikes at step
+    `label_step` of the sample (spike_generators.cpp: the 11th of 15 steps). The input neurons'
+    potential decay is a parameter (mnist-learn uses 2/3; the default 0 keeps every FP32 potential
+    exact). The framework-level winner-take-all is not part of the backend and not modelled.
+    Learning is on (every projection unlocked)."""
+    n = classes * per_column
+    uid = lambda k: T.uid_from_int(seed * 1000 + k)
+    in_uid, out_uid, gate_uid = uid(1), uid(2), uid(3)
+    raster_chan, label_chan = uid(10), uid(11)
+    nn = T.blifat_defaults(n)
+    nn["activation_threshold"] = np.float32(8.571)
+    nn["potential_decay"] = potential_decay
+    nn["min_potential"] = 0.0
+    res = T.resource_defaults(n)
+    res["d_h"] = np.float32(-0.177)
+    res["dopamine_plasticity_time"] = 10
+    res["synapse_sum_threshold_coefficient"] = np.float32(0.218)
+    res["isi_max"] = 10
+    res["stability_change_parameter"] = np.float32(0.05)
+    res["resource_drain_coefficient"] = 27
+    default = T.blifat_defaults(classes)
+    default["activation_threshold"] = np.float32(8.571)
+    pops = [Population(in_uid, T.RESOURCE_STDP_BLIFAT, nn, res),
+            Population(out_uid, T.RESOURCE_STDP_BLIFAT, default, T.resource_defaults(classes)),
+            Population(gate_uid, T.RESOURCE_STDP_BLIFAT, default.copy(), T.resource_defaults(classes))]
+    w_min, w_max = np.float32(-0.253), np.float32(0.0924)
+    diff, over = np.float32(w_max - w_min), np.float32(np.float32(0.0) - w_min)
+    r0 = np.float32(float(over) * float(diff) / (float(diff) - float(over)))  # resource_from_weight(0, ...)
+    i = np.arange(n_in * n, dtype=np.uint64)
+    rule = T.resource_synapse_defaults(i.size)
+    rule["synaptic_resource"] = r0
+    rule["w_min"], rule["w_max"] = w_min, w_max
+    rule["dopamine_plasticity_period"] = 10
+    projs = [Projection(uid(20), T.RESOURCE_STDP_DELTA, T.NULL_UID, in_uid,
+                        pre=(i % np.uint64(n_in)).astype(np.uint32), post=(i // np.uint64(n_in)).astype(np.uint32),
+                        weight=np.zeros(i.size, np.float32), delay=np.ones(i.size, np.uint32), rule=rule, locked=False)]
+
+    def aligned(k, pre_uid, n_pre, post_uid, n_post, w, d, ty):
+        pre, post = _aligned(n_pre, n_post)
+        return Projection(uid(k), T.DELTA, pre_uid, post_uid, pre, post, np.full(pre.size, w, np.float32),
+                          np.full(pre.size, d, np.uint32), out_type=np.full(pre.size, ty, np.uint8))
+
+    projs += [aligned(21, T.NULL_UID, classes, in_uid, n, 0.18, 3, T.DOPAMINE),
+              aligned(22, in_uid, n, out_uid, classes, 10.0, 1, T.EXCITATORY),
+              aligned(23, out_uid, classes, gate_uid, classes, -10.0, 1, T.BLOCKING),
+              aligned(24, T.NULL_UID, classes, gate_uid, classes, 10.0, 1, T.EXCITATORY),
+              aligned(25, gate_uid, classes, in_uid, n, 10.0, 1, T.EXCITATORY),
+              aligned(26, T.NULL_UID, classes, in_uid, n, -30.0, 4, T.EXCITATORY)]
+    subs = [(uid(20), raster_chan)] + [(uid(k), label_chan) for k in (21, 24, 26)]
+    net = Network(pops, projs, subs)
+    images = blob_images(seed, samples)[:, :n_in]
+    key = stream_key(seed, S_INPUT)
+    total = samples * steps_per_sample
+    offs, loffs = np.zeros(total + 1, np.int64), np.zeros(total + 1, np.int64)
+    chunks, labels = [], []
+    src = np.arange(n_in, dtype=np.uint64)
+    for t in range(total):
+        m, local = divmod(t, steps_per_sample)
+        idx = np.zeros(0, np.uint32)
+        if local < active_steps:
+            thr = (0.2 * images[m] * float(1 << 53)).astype(np.uint64)
+            r = rand64(key, np.uint64(t) * np.uint64(n_in) + src) >> np.uint64(11)
+            idx = np.nonzero(r < thr)[0].astype(np.uint32)
+        chunks.append(idx)
+        offs[t + 1] = offs[t] + idx.size
+        if local == label_step:
+            labels.append(m % classes)
+        loffs[t + 1] = len(labels)
+    return net, [SpikeSchedule(raster_chan, offs, np.concatenate(chunks)),
+                 SpikeSchedule(label_chan, loffs, np.array(labels, np.uint32))]
+
+
+def resource_stdp_mixed_network(seed: int = 23, n: int = 300, n_in: int = 100, n_plain: int = 50, steps: int = 300):
+    """Every path of the resource-STDP training on one network: n resource-STDP BLIFAT neurons with
+    per-neuron ISI, Hebbian, dopamine, threshold-coefficient, drain and renormalisation parameters;
+    channel X (n_in) -> resource-STDP projection (p 0.2, per-synapse resource, weight bounds, d_u,
+    dopamine period, delays 1..4; unlocked); a recurrent resource-STDP projection (p 0.03, delays
+    1..3; loaded locked); channel F -> forcing delta projection (EXCITATORY 2.0, aligned); channel D ->
+    DOPAMINE delta projection (+-0.3, aligned); and channel X -> a resource-STDP projection into a
+    plain BLIFAT population (not trained; its synapses still record spike steps). Inputs: X
+    Bernoulli 0.05, F 0.01, D 0.02 per source and step."""
+    rng = np.random.default_rng(seed)
+    uid = lambda k: T.uid_from_int(seed * 1000 + k)
+    a_uid, b_uid = uid(1), uid(2)
+    cx, cf, cd = uid(10), uid(11), uid(12)
+    res = T.resource_defaults(n)
+    pick = lambda vals: np.asarray(vals)[rng.integers(0, len(vals), n)]
+    res["isi_max"] = pick([0, 1, 3, 8])
+    res["d_h"] = pick(np.float32([0.5, 1.0, -0.2]))
+    res["stability_change_at_isi"] = np.float32(0.25)
+    res["stability_change_parameter"] = np.float32(0.1)
+    res["dopamine_plasticity_time"] = pick([1, 5])
+    res["synapse_sum_threshold_coefficient"] = pick(np.float32([0.0, 0.01, 0.05]))
+    res["resource_drain_coefficient"] = pick([0, 3])
+    res["synaptic_resource_threshold"] = pick(np.float32([T.FLT_MAX, 0.5, 2.0]))
+    res["free_synaptic_resource"] = pick(np.float32([1.0, 0.0, 3.0]))
+    pops = [Population(a_uid, T.RESOURCE_STDP_BLIFAT, T.blifat_defaults(n), res),
+            Population(b_uid, T.BLIFAT, T.blifat_defaults(n_plain))]
+
+    def rule_for(size, lo_choices, hi_choices):
+        r = T.resource_synapse_defaults(size)
+        r["synaptic_resource"] = (rng.integers(0, 64, size) / 32.0).astype(np.float32)
+        r["w_min"] = np.asarray(lo_choices, np.float32)[rng.integers(0, len(lo_choices), size)]
+        r["w_max"] = np.asarray(hi_choices, np.float32)[rng.integers(0, len(hi_choices), size)]
+        r["d_u"] = np.float32([0.0, 0.01])[rng.integers(0, 2, size)]
+        r["dopamine_plasticity_period"] = np.array([0, 2, 5])[rng.integers(0, 3, size)]
+        return r
+
+    def random_proj(k, pre_uid, n_pre, post_uid, n_post, p, d_hi, lo, hi, locked):
+        pre, post = np.nonzero(rng.random((n_pre, n_post)) < p)
+        rule = rule_for(pre.size, lo, hi)
+        w = (rng.integers(-64, 64, pre.size) / 64.0).astype(np.float32)
+        return Projection(uid(k), T.RESOURCE_STDP_DELTA, pre_uid, post_uid, pre.astype(np.uint32),
+                          post.astype(np.uint32), w, rng.integers(1, d_hi + 1, pre.size).astype(np.uint32), rule=rule,
+                          locked=locked)
+
+    x_proj = random_proj(20, T.NULL_UID, n_in, a_uid, n, 0.2, 4, [0.0, -0.5], [1.0, 2.0], False)
+    rec = random_proj(21, a_uid, n, a_uid, n, 0.03, 3, [-0.5], [0.5], True)
+    one = np.arange(n, dtype=np.uint32)
+    force = Projection(uid(22), T.DELTA, T.NULL_UID, a_uid, one, one, np.full(n, 2.0, np.float32), np.ones(n, np.uint32))
+    dopa = Projection(uid(23), T.DELTA, T.NULL_UID, a_uid, one, one,
+                      np.where(one % 3 == 0, -0.3, 0.3).astype(np.float32), np.ones(n, np.uint32),
+                      out_type=np.full(n, T.DOPAMINE, np.uint8))
+    plain = random_proj(24, T.NULL_UID, n_in, b_uid, n_plain, 0.2, 2, [0.0], [1.0], False)
+    net = Network(pops, [x_proj, rec, force, dopa, plain],
+                  [(uid(20), cx), (uid(24), cx), (uid(22), cf), (uid(23), cd)])
+    return net, [bernoulli_schedule(cx, seed, n_in, steps, 0.05, stream=S_INPUT),
+                 bernoulli_schedule(cf, seed, n, steps, 0.01, stream=S_INPUT + 100),
+                 bernoulli_schedule(cd, seed, n, steps, 0.02, stream=S_INPUT + 200)]
 

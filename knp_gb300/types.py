@@ -20,9 +20,9 @@ FLT_MAX = float(np.finfo(np.float32).max)
 # knp_output_type (output_types.h:36-62)
 EXCITATORY, INHIBITORY_CURRENT, INHIBITORY_CONDUCTANCE, DOPAMINE, BLOCKING = range(5)
 # knp_neuron_kind
-BLIFAT, RESOURCE_STDP_BLIFAT, LIF = range(3)
+BLIFAT, RESOURCE_STDP_BLIFAT, LIF, ALTAI_LIF, RESOURCE_STDP_ALTAI_LIF = range(5)
 # knp_synapse_kind
-DELTA, ADDITIVE_STDP_DELTA = range(2)
+DELTA, ADDITIVE_STDP_DELTA, RESOURCE_STDP_DELTA = range(3)
 # knp_stdp_processing (projection.h:139-150)
 STDP_ONLY, STDP_AND_SPIKE = range(2)
 # knp_gb300_accumulator (input-ring accumulation of a population)
@@ -85,6 +85,45 @@ RESOURCE_DTYPE = np.dtype(
 )
 assert RESOURCE_DTYPE.itemsize == 72
 
+# knp_resource_synapse: the rule state of one SynapticResourceSTDPDeltaSynapse
+# (stdp_synaptic_resource_rule.h:45-89)
+RESOURCE_SYNAPSE_DTYPE = np.dtype(
+    [
+        ("synaptic_resource", "<f4"),
+        ("w_min", "<f4"),
+        ("w_max", "<f4"),
+        ("d_u", "<f4"),
+        ("dopamine_plasticity_period", "<u4"),
+        ("had_hebbian_update", "<u4"),
+        ("last_spike_step", "<u8"),
+        ("has_contributed", "<u4"),
+        ("pad_", "<u4"),
+    ]
+)
+assert RESOURCE_SYNAPSE_DTYPE.itemsize == 40
+
+# knp_altai_neuron: neuron_parameters<AltAILIF> (altai_lif.h:164-335)
+ALTAI_DTYPE = np.dtype(
+    [
+        ("is_diff", "u1"),
+        ("is_reset", "u1"),
+        ("leak_rev", "u1"),
+        ("saturate", "u1"),
+        ("do_not_save", "u1"),
+        ("pad0_", "u1", (3,)),
+        ("potential", "<f4"),
+        ("pre_impact_potential", "<f4"),
+        ("activation_threshold", "<u2"),
+        ("negative_activation_threshold", "<u2"),
+        ("potential_leak", "<i2"),
+        ("potential_reset_value", "<u2"),
+        ("dopamine_value", "<f8"),
+        ("additional_threshold", "<f8"),
+        ("activity_time", "<i8"),
+    ]
+)
+assert ALTAI_DTYPE.itemsize == 48
+
 LIF_DTYPE = np.dtype(
     [
         ("potential", "<f4"),
@@ -119,6 +158,32 @@ def resource_defaults(n: int) -> np.ndarray:
     a["d_h"] = 1.0
     a["isi_status"] = ISI_NOT_IN_PERIOD
     return a
+
+
+def resource_synapse_defaults(n: int) -> np.ndarray:
+    """``n`` resource-STDP synapse rules with the reference defaults (stdp_synaptic_resource_rule.h:45-89)."""
+    a = np.zeros(n, dtype=RESOURCE_SYNAPSE_DTYPE)
+    a["w_max"] = 1.0
+    return a
+
+
+def altai_defaults(n: int) -> np.ndarray:
+    """``n`` AltAI-LIF neurons with the reference defaults (altai_lif.h:50-157)."""
+    a = np.zeros(n, dtype=ALTAI_DTYPE)
+    a["is_reset"] = 1
+    a["leak_rev"] = 1
+    a["saturate"] = 1
+    a["activation_threshold"] = 1
+    a["negative_activation_threshold"] = 30000
+    return a
+
+
+def is_altai(kind: int) -> bool:
+    return kind in (ALTAI_LIF, RESOURCE_STDP_ALTAI_LIF)
+
+
+def is_resource(kind: int) -> bool:
+    return kind in (RESOURCE_STDP_BLIFAT, RESOURCE_STDP_ALTAI_LIF)
 
 
 def lif_defaults(n: int) -> np.ndarray:

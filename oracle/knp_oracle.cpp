@@ -99,10 +99,19 @@ struct Population
     std::vector<knp_blifat_neuron> blifat;
     std::vector<knp_resource_stdp_state> res;
     std::vector<knp_lif_neuron> lif;
+    std::vector<knp_altai_neuron> altai;
     std::vector<uint32_t> last_spikes;
     std::unordered_set<Uid, UidHash> impact_senders;  // impact-message subscription
     std::vector<ImpactMessage> inbox;
-    size_t size() const { return kind == KNP_NEURON_LIF ? lif.size() : blifat.size(); }
+    size_t size() const
+    {
+        return kind == KNP_NEURON_LIF ? lif.size() : is_altai() ? altai.size() : blifat.size();
+    }
+    bool is_altai() const { return kind == KNP_NEURON_ALTAI_LIF || kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF; }
+    bool is_resource() const
+    {
+        return kind == KNP_NEURON_RESOURCE_STDP_BLIFAT || kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF;
+    }
 };
 
 struct Synapse
@@ -116,6 +125,7 @@ struct Synapse
     std::vector<uint64_t> post_times;
     uint32_t pre;
     uint32_t post;
+    knp_resource_synapse rule{};  // synaptic-resource STDP rule state
 };
 
 struct Projection
@@ -127,6 +137,7 @@ struct Projection
     std::vector<Synapse> syn;
     std::vector<std::vector<size_t>> by_pre;
     std::vector<std::vector<size_t>> by_post;
+    bool locked = true;  // is_locked() (projection.h:384-396); only resource-STDP training reads it
     std::unordered_map<Uid, int, UidHash> stdp_pops;
     std::unordered_set<Uid, UidHash> spike_senders;  // spike-message subscription
     std::vector<SpikeMessage> inbox;
@@ -331,12 +342,12 @@ bool blifat_post_impact(knp_blifat_neuron &n)
 }
 
 // ------------------------------------------- resource-STDP neuron training (blifat_stdp.h:35-172)
-// The GB300 backend supports no SynapticResourceSTDPDeltaSynapse projection, so the list of
-// "working projections" (populations_old.h:207-209) is always empty and only the neuron-side
-// bookkeeping runs: ISI status, stability, additional threshold, dopamine-driven stability and the
-// free-resource renormalisation.
+// The population's training over the unlocked SynapticResourceSTDPDeltaSynapse projections into it:
+// ISI status, stability, additional threshold, Hebbian and dopamine changes of the synaptic
+// resource, free-resource renormalisation and the weights that follow from the resource.
 
-int update_isi(knp_resource_stdp_state &r, const knp_blifat_neuron &n, uint64_t step)  // training/stdp.h:88-126
+template <class Neuron>
+int update_isi(knp_resource_stdp_state &r, const Neuron &n, uint64_t step)  // training/stdp.h:88-126
 {
     if (r.is_being_forced)
     {
@@ -368,26 +379,103 @@ int update_isi(knp_resource_stdp_state &r, const knp_blifat_neuron &n, uint64_t 
     return r.isi_status;
 }
 
-void train_resource_population(Population &pop, const std::vector<uint32_t> &spikes, uint64_t step)
+// recalculate_synapse_weights (training/stdp.h:40-52).
+void recalc_weight(Synapse &s)
 {
-    // process_spiking_neurons_impl (blifat_stdp.h:35-103) with no connected synapses.
+    const float syn_w = std::max(s.rule.synaptic_resource, 0.F);
+    const float weight_diff = s.rule.w_max - s.rule.w_min;
+    s.weight = s.rule.w_min + weight_diff * syn_w / (weight_diff + syn_w);
+}
+
+// min(2^-stability, 1) as the reference evaluates it: std::pow(2, -stability) in double, then float.
+float resource_factor(float stability) { return std::min(static_cast<float>(std::pow(2, -stability)), 1.F); }
+
+// The SynapticResourceSTDPDeltaSynapse projections into a population that are not locked, in the
+// backend's projection order (populations_old.h:57-83, 207-209).
+std::vector<Projection *> working_projections(or_net &net, const Population &pop)
+{
+    std::vector<Projection *> out;
+    for (auto &p : net.projs)
+        if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA && p->post_uid == pop.uid && !p->locked) out.push_back(p.get());
+    return out;
+}
+
+// get_all_connected_synapses (training/stdp.h:55-72): synapses into neuron i, projection by projection.
+std::vector<Synapse *> connected(const std::vector<Projection *> &working, uint32_t i)
+{
+    std::vector<Synapse *> out;
+    for (Projection *p : working)
+        for (size_t si : p->find_by_post(i)) out.push_back(&p->syn[si]);
+    return out;
+}
+
+bool is_point_in_interval(uint64_t a, uint64_t b, uint64_t point)  // training/stdp.h:129-133
+{
+    if (a > b) std::swap(a, b);
+    return a <= point && point <= b;
+}
+
+// train_population_impl (blifat_stdp.h:158-172): process_spiking_neurons_impl (:35-103),
+// do_dopamine_plasticity_impl (:106-155), renormalize_resource (training/stdp.h:152-186). The
+// AltAI-LIF variant (altai/altai_stdp.h) is the same computation on the AltAI neuron's dopamine value
+// and additional threshold.
+template <class Neuron>
+void train_resource_population(or_net &net, Population &pop, std::vector<Neuron> &neurons,
+                               const std::vector<uint32_t> &spikes, uint64_t step)
+{
+    const std::vector<Projection *> working = working_projections(net, pop);
     for (uint32_t i : spikes)
     {
-        auto &n = pop.blifat[i];
+        auto &n = neurons[i];
         auto &r = pop.res[i];
+        const std::vector<Synapse *> syns = connected(working, i);
         r.last_spike_step = step;
         update_isi(r, n, step);
         if (KNP_ISI_PERIOD_STARTED == r.isi_status) r.stability -= r.stability_change_at_isi;
         n.additional_threshold = 0.0;
+        for (Synapse *s : syns)
+        {
+            n.additional_threshold += s->weight * (s->weight > 0);
+            const bool had_spike =
+                is_point_in_interval(step - s->rule.dopamine_plasticity_period, step, s->rule.last_spike_step + s->delay - 1);
+            if (KNP_ISI_PERIOD_CONTINUED != r.isi_status || had_spike) s->rule.has_contributed = had_spike;
+        }
         n.additional_threshold *= r.synapse_sum_threshold_coefficient;
+        if (r.isi_status != KNP_ISI_PERIOD_CONTINUED)
+            for (Synapse *s : syns) s->rule.had_hebbian_update = 0;
+        if (r.isi_status != KNP_ISI_IS_FORCED)
+        {
+            for (Synapse *s : syns)
+            {
+                s->rule.synaptic_resource -= s->rule.d_u;
+                r.free_synaptic_resource += s->rule.d_u;
+                if (s->rule.has_contributed && !s->rule.had_hebbian_update)
+                {
+                    const float d_h = r.d_h * resource_factor(r.stability);
+                    s->rule.synaptic_resource += d_h;
+                    r.free_synaptic_resource -= d_h;
+                    s->rule.had_hebbian_update = 1;
+                }
+            }
+        }
+        for (Synapse *s : syns) recalc_weight(*s);
     }
-    // do_dopamine_plasticity_impl (blifat_stdp.h:106-155).
-    for (size_t i = 0; i < pop.blifat.size(); ++i)
+    for (uint32_t i = 0; i < neurons.size(); ++i)
     {
-        auto &n = pop.blifat[i];
+        auto &n = neurons[i];
         auto &r = pop.res[i];
         if (n.dopamine_value > 0.0 || (n.dopamine_value < 0.0 && r.isi_status != KNP_ISI_IS_FORCED))
         {
+            const std::vector<Synapse *> syns = connected(working, i);
+            for (Synapse *s : syns)
+            {
+                if (step - r.last_spike_step <= r.dopamine_plasticity_time && s->rule.has_contributed)
+                {
+                    const float resource_change = n.dopamine_value * resource_factor(r.stability);
+                    s->rule.synaptic_resource += resource_change;
+                    r.free_synaptic_resource -= resource_change;
+                }
+            }
             if (r.is_being_forced || n.dopamine_value < 0)
             {
                 r.stability -= n.dopamine_value * r.stability_change_parameter;
@@ -400,15 +488,19 @@ void train_resource_population(Population &pop, const std::vector<uint32_t> &spi
                 r.stability += r.stability_change_parameter * n.dopamine_value *
                                std::max(dopamine_constant - difference / r.isi_max, -1.0);
             }
+            for (Synapse *s : syns) recalc_weight(*s);
         }
     }
-    // renormalize_resource (training/stdp.h:152-186).
-    for (size_t i = 0; i < pop.blifat.size(); ++i)
+    for (uint32_t i = 0; i < neurons.size(); ++i)
     {
         auto &r = pop.res[i];
         if (step - r.last_step <= r.isi_max && r.isi_status != KNP_ISI_IS_FORCED) continue;
         if (std::fabs(r.free_synaptic_resource) < r.synaptic_resource_threshold) continue;
+        const std::vector<Synapse *> syns = connected(working, i);
+        const float add_resource_value = r.free_synaptic_resource / (syns.size() + r.resource_drain_coefficient);
+        for (Synapse *s : syns) s->rule.synaptic_resource += add_resource_value;
         r.free_synaptic_resource = 0.0F;
+        for (Synapse *s : syns) recalc_weight(*s);
     }
 }
 
@@ -452,6 +544,77 @@ bool lif_post_impact(knp_lif_neuron &n)
     return false;
 }
 
+// ---------------------------------------------------------- AltAI-LIF (altai/altai_impl.h:33-168)
+
+void altai_pre_impact(knp_altai_neuron &n, knp_resource_stdp_state *r)
+{
+    n.potential = n.do_not_save ? static_cast<float>(n.potential_reset_value) : std::round(n.potential);
+    if (r)
+    {
+        n.dopamine_value = 0.0;
+        r->is_being_forced = 0;
+    }
+    n.pre_impact_potential = n.potential;
+}
+
+void altai_impact(knp_altai_neuron &n, const Impact &imp)
+{
+    switch (imp.type)
+    {
+        case KNP_OUT_EXCITATORY:
+            n.potential += imp.value;
+            break;
+        case KNP_OUT_INHIBITORY_CURRENT:
+            n.potential -= imp.value;
+            break;
+        case KNP_OUT_DOPAMINE:
+            n.dopamine_value += imp.value;
+            break;
+        case KNP_OUT_BLOCKING:
+            // A blocking impact replaces the activity time unless it has the same sign and a smaller
+            // magnitude (signs of the values as doubles).
+            if (std::signbit(static_cast<double>(n.activity_time)) != std::signbit(static_cast<double>(imp.value)) ||
+                std::abs(n.activity_time) <= std::abs(imp.value))
+                n.activity_time = static_cast<int64_t>(imp.value);
+            break;
+        default:
+            throw std::runtime_error("Unhandled synapse type.");
+    }
+}
+
+bool altai_post_impact(knp_altai_neuron &n)
+{
+    const int sign = (n.leak_rev && n.potential < 0) ? -1 : 1;
+    n.potential += n.potential_leak * sign;
+    bool spiked = false;
+    if (n.activity_time > 0)
+        --n.activity_time;
+    else if (n.activity_time < 0)
+        ++n.activity_time;
+    if (n.activity_time == 0) n.activity_time = std::numeric_limits<int64_t>::max();
+    bool was_reset = false;
+    if (n.potential >= n.activation_threshold + n.additional_threshold)
+    {
+        if (n.activity_time > 0) spiked = true;
+        if (n.is_diff) n.potential -= n.activation_threshold + n.additional_threshold;
+        if (n.is_reset)
+        {
+            n.potential = n.potential_reset_value;
+            was_reset = true;
+        }
+    }
+    if (n.potential <= -static_cast<float>(n.negative_activation_threshold) && !was_reset)
+    {
+        if (n.saturate)
+            n.potential = -static_cast<float>(n.negative_activation_threshold);
+        else if (n.is_reset)
+            n.potential = -n.potential_reset_value;
+        else if (n.is_diff)
+            n.potential += n.negative_activation_threshold;
+    }
+    return spiked;
+}
+
 // ------------------------------------------------------------------ one population step
 
 void check_impacts(const Population &pop, const std::vector<ImpactMessage> &msgs)
@@ -461,39 +624,69 @@ void check_impacts(const Population &pop, const std::vector<ImpactMessage> &msgs
             if (imp.post >= pop.size()) throw std::runtime_error("Impact postsynaptic index out of range.");
 }
 
+// Per-neuron phases of any population kind.
+void pre_impact(Population &q, size_t i)
+{
+    switch (q.kind)
+    {
+        case KNP_NEURON_LIF:
+            lif_pre_impact(q.lif[i]);
+            break;
+        case KNP_NEURON_RESOURCE_STDP_BLIFAT:
+            resource_blifat_pre_impact(q.blifat[i], q.res[i]);
+            break;
+        case KNP_NEURON_ALTAI_LIF:
+            altai_pre_impact(q.altai[i], nullptr);
+            break;
+        case KNP_NEURON_RESOURCE_STDP_ALTAI_LIF:
+            altai_pre_impact(q.altai[i], &q.res[i]);
+            break;
+        default:
+            blifat_pre_impact(q.blifat[i]);
+    }
+}
+
+void impact(Population &q, const Impact &imp, bool is_forcing)
+{
+    if (q.kind == KNP_NEURON_LIF)
+    {
+        lif_impact(q.lif[imp.post], imp);
+        return;
+    }
+    if (q.is_altai())
+        altai_impact(q.altai[imp.post], imp);
+    else
+        blifat_impact(q.blifat[imp.post], imp);
+    if (q.is_resource() && imp.type == KNP_OUT_EXCITATORY) q.res[imp.post].is_being_forced |= is_forcing ? 1u : 0u;
+}
+
+bool post_impact(Population &q, size_t i)
+{
+    if (q.kind == KNP_NEURON_LIF) return lif_post_impact(q.lif[i]);
+    if (q.is_altai()) return altai_post_impact(q.altai[i]);
+    return blifat_post_impact(q.blifat[i]);
+}
+
+void train(or_net &net, Population &q, uint64_t step)
+{
+    if (q.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT) train_resource_population(net, q, q.blifat, q.last_spikes, step);
+    if (q.kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF) train_resource_population(net, q, q.altai, q.last_spikes, step);
+}
+
 // calculate_any_population / calculate_resource_stdp_population (populations_old.h:104-121, 195-217).
-void calculate_population(Population &pop, uint64_t step)
+void calculate_population(or_net &net, Population &pop, uint64_t step)
 {
     std::vector<ImpactMessage> msgs = std::move(pop.inbox);
     pop.inbox.clear();
     check_impacts(pop, msgs);
     pop.last_spikes.clear();
-    if (pop.kind == KNP_NEURON_LIF)
-    {
-        for (auto &n : pop.lif) lif_pre_impact(n);
-        for (auto &m : msgs)
-            for (auto &imp : m.impacts) lif_impact(pop.lif[imp.post], imp);
-        for (uint32_t i = 0; i < pop.lif.size(); ++i)
-            if (lif_post_impact(pop.lif[i])) pop.last_spikes.push_back(i);
-        return;
-    }
-    const bool res = pop.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT;
-    for (size_t i = 0; i < pop.blifat.size(); ++i)
-    {
-        if (res)
-            resource_blifat_pre_impact(pop.blifat[i], pop.res[i]);
-        else
-            blifat_pre_impact(pop.blifat[i]);
-    }
+    const size_t n = pop.size();
+    for (size_t i = 0; i < n; ++i) pre_impact(pop, i);
     for (auto &m : msgs)
-        for (auto &imp : m.impacts)
-        {
-            blifat_impact(pop.blifat[imp.post], imp);
-            if (res && imp.type == KNP_OUT_EXCITATORY) pop.res[imp.post].is_being_forced |= m.is_forcing ? 1u : 0u;
-        }
-    for (uint32_t i = 0; i < pop.blifat.size(); ++i)
-        if (blifat_post_impact(pop.blifat[i])) pop.last_spikes.push_back(i);
-    if (res) train_resource_population(pop, pop.last_spikes, step);
+        for (auto &imp : m.impacts) impact(pop, imp, m.is_forcing);
+    for (uint32_t i = 0; i < n; ++i)
+        if (post_impact(pop, i)) pop.last_spikes.push_back(i);
+    train(net, pop, step);
 }
 
 // --------------------------------------------------------- additive STDP (additive_stdp.h:42-196)
@@ -562,12 +755,15 @@ bool calculate_projection(or_net &net, Projection &proj, uint64_t step, ImpactMe
     std::vector<SpikeMessage> msgs = std::move(proj.inbox);
     proj.inbox.clear();
     const bool stdp = proj.kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA;
+    const bool resource = proj.kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA;
     if (stdp) stdp_init_projection(proj, msgs);
     for (auto &msg : msgs)
         for (uint32_t spiked : msg.idx)
             for (size_t si : proj.find_by_pre(spiked))
             {
-                const Synapse &s = proj.syn[si];
+                Synapse &s = proj.syn[si];
+                // init_synapse (synaptic_resource_stdp.h:36-41): the step of the presynaptic spike.
+                if (resource) s.rule.last_spike_step = step;
                 // The message is sent on step N - 1 and received on step N.
                 const uint64_t future_step = s.delay + step - 1;
                 Impact imp{si, s.weight, s.type, s.pre, s.post};
@@ -579,9 +775,9 @@ bool calculate_projection(or_net &net, Projection &proj, uint64_t step, ImpactMe
                 }
                 else
                 {
-                    // is_forced(): true for plain delta projections, false for additive STDP
-                    // (stdp_dispatcher.h:54-58, additive_stdp.h:199-203).
-                    ImpactMessage m{proj.uid, step, proj.pre_uid, proj.post_uid, !stdp, {imp}};
+                    // is_forced(): true for plain delta projections, false for additive and resource
+                    // STDP (stdp_dispatcher.h:54-58, additive_stdp.h:199-203, synaptic_resource_stdp.h:58-62).
+                    ImpactMessage m{proj.uid, step, proj.pre_uid, proj.post_uid, proj.kind == KNP_SYNAPSE_DELTA, {imp}};
                     proj.future.emplace(future_step, std::move(m));
                 }
             }
@@ -631,6 +827,29 @@ int or_add_blifat_population(
     return 0;
 }
 
+int or_add_altai_population(
+    or_net *net, knp_uid uid, int kind, uint32_t n, const knp_altai_neuron *neurons, const knp_resource_stdp_state *ext)
+{
+    if (kind != KNP_NEURON_ALTAI_LIF && kind != KNP_NEURON_RESOURCE_STDP_ALTAI_LIF) return fail("bad neuron kind");
+    if (kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF && !ext) return fail("resource-STDP population needs ext state");
+    auto p = std::make_unique<Population>();
+    p->uid = Uid{uid};
+    p->kind = kind;
+    p->altai.assign(neurons, neurons + n);
+    if (kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF) p->res.assign(ext, ext + n);
+    net->pops.push_back(std::move(p));
+    return 0;
+}
+
+int or_read_altai(const or_net *net, knp_uid pop, knp_altai_neuron *out, knp_resource_stdp_state *ext)
+{
+    const Population *q = net->find_pop(Uid{pop});
+    if (!q || !q->is_altai()) return fail("unknown AltAI population");
+    std::copy(q->altai.begin(), q->altai.end(), out);
+    if (ext && !q->res.empty()) std::copy(q->res.begin(), q->res.end(), ext);
+    return 0;
+}
+
 int or_add_lif_population(or_net *net, knp_uid uid, uint32_t n, const knp_lif_neuron *neurons)
 {
     auto p = std::make_unique<Population>();
@@ -646,7 +865,8 @@ int or_add_projection(
     const uint32_t *pre_idx, const uint32_t *post_idx, const float *weight, const uint32_t *delay,
     const uint8_t *out_type, const float *tau_plus, const float *tau_minus)
 {
-    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) return fail("bad synapse kind");
+    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA && kind != KNP_SYNAPSE_RESOURCE_STDP_DELTA)
+        return fail("bad synapse kind");
     auto p = std::make_unique<Projection>();
     p->uid = Uid{uid};
     p->kind = kind;
@@ -675,6 +895,36 @@ int or_add_projection(
         p->by_post[p->syn[i].post].push_back(i);
     }
     net->projs.push_back(std::move(p));
+    return 0;
+}
+
+int or_add_resource_projection(
+    or_net *net, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre_idx,
+    const uint32_t *post_idx, const float *weight, const uint32_t *delay, const uint8_t *out_type,
+    const knp_resource_synapse *rule, int locked)
+{
+    if (n_syn && !rule) return fail("resource-STDP synapses need their rule state");
+    const int rc = or_add_projection(net, uid, KNP_SYNAPSE_RESOURCE_STDP_DELTA, pre_uid, post_uid, n_syn, pre_idx,
+                                     post_idx, weight, delay, out_type, nullptr, nullptr);
+    if (rc) return rc;
+    Projection &p = *net->projs.back();
+    for (uint64_t i = 0; i < n_syn; ++i) p.syn[i].rule = rule[i];
+    p.locked = locked != 0;
+    return 0;
+}
+
+int or_set_learning(or_net *net, int on)
+{
+    // start_learning / stop_learning unlock / lock every projection (cpu-single-threaded/backend.h:315-332).
+    for (auto &p : net->projs) p->locked = on == 0;
+    return 0;
+}
+
+int or_read_resource_synapses(const or_net *net, knp_uid proj, knp_resource_synapse *out)
+{
+    const Projection *p = net->find_proj(Uid{proj});
+    if (!p || p->kind != KNP_SYNAPSE_RESOURCE_STDP_DELTA) return fail("unknown resource-STDP projection");
+    for (size_t i = 0; i < p->syn.size(); ++i) out[i] = p->syn[i].rule;
     return 0;
 }
 
@@ -756,7 +1006,7 @@ int or_step(or_net *net)
             std::vector<SpikeMessage> sent;
             for (auto &q : net->pops)
             {
-                calculate_population(*q, step);
+                calculate_population(*net, *q, step);
                 if (!q->last_spikes.empty()) sent.push_back(SpikeMessage{q->uid, step, q->last_spikes});
             }
             for (auto &m : sent)  // Route #2.
@@ -817,15 +1067,7 @@ int or_step_mt(or_net *net, int threads)
                         [&q, a, n, part]
                         {
                             const size_t b = std::min(a + part, n);
-                            for (size_t i = a; i < b; ++i)
-                            {
-                                if (q.kind == KNP_NEURON_LIF)
-                                    lif_pre_impact(q.lif[i]);
-                                else if (q.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT)
-                                    resource_blifat_pre_impact(q.blifat[i], q.res[i]);
-                                else
-                                    blifat_pre_impact(q.blifat[i]);
-                            }
+                            for (size_t i = a; i < b; ++i) pre_impact(q, i);
                         });
             }
             pool.join();
@@ -835,17 +1077,7 @@ int or_step_mt(or_net *net, int threads)
                     {
                         Population &q = *net->pops[k];
                         for (auto &m : msgs[k])
-                            for (auto &imp : m.impacts)
-                            {
-                                if (q.kind == KNP_NEURON_LIF)
-                                {
-                                    lif_impact(q.lif[imp.post], imp);
-                                    continue;
-                                }
-                                blifat_impact(q.blifat[imp.post], imp);
-                                if (q.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT && imp.type == KNP_OUT_EXCITATORY)
-                                    q.res[imp.post].is_being_forced |= m.is_forcing ? 1u : 0u;
-                            }
+                            for (auto &imp : m.impacts) impact(q, imp, m.is_forcing);
                     });
             pool.join();
             for (auto &qp : net->pops)
@@ -860,9 +1092,7 @@ int or_step_mt(or_net *net, int threads)
                             const size_t b = std::min(a + part, n);
                             for (size_t i = a; i < b; ++i)
                             {
-                                const bool s = q.kind == KNP_NEURON_LIF ? lif_post_impact(q.lif[i])
-                                                                        : blifat_post_impact(q.blifat[i]);
-                                if (s) local.push_back(static_cast<uint32_t>(i));
+                                if (post_impact(q, i)) local.push_back(static_cast<uint32_t>(i));
                             }
                             std::lock_guard<std::mutex> l(merge);
                             q.last_spikes.insert(q.last_spikes.end(), local.begin(), local.end());
@@ -872,7 +1102,7 @@ int or_step_mt(or_net *net, int threads)
             std::vector<SpikeMessage> sent;
             for (auto &q : net->pops)
             {
-                if (q->kind == KNP_NEURON_RESOURCE_STDP_BLIFAT) train_resource_population(*q, q->last_spikes, step);
+                train(*net, *q, step);
                 if (!q->last_spikes.empty()) sent.push_back(SpikeMessage{q->uid, step, q->last_spikes});
             }
             for (auto &m : sent)
@@ -954,7 +1184,7 @@ int or_read_spikes(const or_net *net, knp_uid pop, uint32_t cap, uint32_t *out, 
 int or_read_blifat(const or_net *net, knp_uid pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext)
 {
     const Population *q = net->find_pop(Uid{pop});
-    if (!q || q->kind == KNP_NEURON_LIF) return fail("unknown BLIFAT population");
+    if (!q || q->kind == KNP_NEURON_LIF || q->is_altai()) return fail("unknown BLIFAT population");
     std::copy(q->blifat.begin(), q->blifat.end(), out);
     if (ext && !q->res.empty()) std::copy(q->res.begin(), q->res.end(), ext);
     return 0;

@@ -38,6 +38,10 @@ int or_add_blifat_population(
 
 /** Add a LIF population (kind 2). */
 int or_add_lif_population(or_net *net, knp_uid uid, uint32_t n, const knp_lif_neuron *neurons);
+/* AltAI-LIF populations (kind KNP_NEURON_ALTAI_LIF, or KNP_NEURON_RESOURCE_STDP_ALTAI_LIF with ext). */
+int or_add_altai_population(
+    or_net *net, knp_uid uid, int kind, uint32_t n, const knp_altai_neuron *neurons, const knp_resource_stdp_state *ext);
+int or_read_altai(const or_net *net, knp_uid pop, knp_altai_neuron *out, knp_resource_stdp_state *ext);
 
 /**
  * Add a projection. kind: knp_synapse_kind. pre_uid may be all-zero (no presynaptic population).
@@ -50,6 +54,15 @@ int or_add_projection(
 
 /** Register `pop_uid` in an STDP projection's stdp_populations_ map. */
 int or_set_stdp_population(or_net *net, knp_uid proj_uid, knp_uid pop_uid, int processing);
+/* SynapticResourceSTDPDeltaSynapse projection: the rule state of every synapse and the projection's
+ * lock flag (a projection starts locked; start_learning unlocks every projection). */
+int or_add_resource_projection(
+    or_net *net, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre_idx,
+    const uint32_t *post_idx, const float *weight, const uint32_t *delay, const uint8_t *out_type,
+    const knp_resource_synapse *rule, int locked);
+/* start_learning (on = 1) / stop_learning (on = 0). */
+int or_set_learning(or_net *net, int on);
+int or_read_resource_synapses(const or_net *net, knp_uid proj, knp_resource_synapse *out);
 
 /** Extra subscription of `receiver` (projection or population) to messages of `sender`. */
 int or_subscribe(or_net *net, knp_uid receiver, knp_uid sender);

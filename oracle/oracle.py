@@ -73,6 +73,11 @@ def _load(which: str):
             "or_read_lif": ([p, U, p], ctypes.c_int),
             "or_read_weights": ([p, U, p], ctypes.c_int),
             "or_event_count": ([p], ctypes.c_uint64),
+            "or_add_resource_projection": ([p, U, U, U, ctypes.c_uint64, p, p, p, p, p, p, ctypes.c_int], ctypes.c_int),
+            "or_set_learning": ([p, ctypes.c_int], ctypes.c_int),
+            "or_read_resource_synapses": ([p, U, p], ctypes.c_int),
+            "or_add_altai_population": ([p, U, ctypes.c_int, ctypes.c_uint32, p, p], ctypes.c_int),
+            "or_read_altai": ([p, U, p, p], ctypes.c_int),
         }
         if which == "restated":
             sig["or_step_mt"] = ([p, ctypes.c_int], ctypes.c_int)
@@ -125,6 +130,10 @@ class OracleNet:
             neurons = np.ascontiguousarray(pop.neurons)
             if pop.kind == T.LIF:
                 self._chk(self.lib.or_add_lif_population(self.h, T.to_c_uid(pop.uid), n, _ptr(neurons)))
+            elif T.is_altai(pop.kind):
+                res = None if pop.resource is None else np.ascontiguousarray(pop.resource)
+                self._chk(self.lib.or_add_altai_population(self.h, T.to_c_uid(pop.uid), pop.kind, n, _ptr(neurons),
+                                                           _ptr(res)))
             else:
                 res = None if pop.resource is None else np.ascontiguousarray(pop.resource)
                 self._chk(self.lib.or_add_blifat_population(self.h, T.to_c_uid(pop.uid), pop.kind, n, _ptr(neurons),
@@ -136,6 +145,13 @@ class OracleNet:
                     None if pr.tau_plus is None else np.ascontiguousarray(pr.tau_plus, np.float32),
                     None if pr.tau_minus is None else np.ascontiguousarray(pr.tau_minus, np.float32)]
             self._sizes[pr.uid] = (pr.kind, pr.size)
+            if pr.kind == T.RESOURCE_STDP_DELTA:
+                rule = np.ascontiguousarray(pr.rule if pr.rule is not None else T.resource_synapse_defaults(pr.size))
+                self._chk(self.lib.or_add_resource_projection(self.h, T.to_c_uid(pr.uid), T.to_c_uid(pr.pre_uid),
+                                                              T.to_c_uid(pr.post_uid), pr.size,
+                                                              *[_ptr(a) for a in arrs[:5]], _ptr(rule),
+                                                              int(pr.locked)))
+                continue
             self._chk(self.lib.or_add_projection(self.h, T.to_c_uid(pr.uid), pr.kind, T.to_c_uid(pr.pre_uid),
                                                  T.to_c_uid(pr.post_uid), pr.size, *[_ptr(a) for a in arrs]))
             for pop_uid, ptype in pr.stdp_populations.items():
@@ -184,6 +200,22 @@ class OracleNet:
         ext = np.empty(n, T.RESOURCE_DTYPE) if kind == T.RESOURCE_STDP_BLIFAT else None
         self._chk(self.lib.or_read_blifat(self.h, T.to_c_uid(pop), _ptr(out), _ptr(ext)))
         return out, ext
+
+    def altai(self, pop: bytes):
+        kind, n = self._sizes[pop]
+        out = np.empty(n, T.ALTAI_DTYPE)
+        ext = np.empty(n, T.RESOURCE_DTYPE) if kind == T.RESOURCE_STDP_ALTAI_LIF else None
+        self._chk(self.lib.or_read_altai(self.h, T.to_c_uid(pop), _ptr(out), _ptr(ext)))
+        return out, ext
+
+    def set_learning(self, on: bool):
+        """Backend::start_learning / stop_learning: unlock / lock the weights of every projection."""
+        self._chk(self.lib.or_set_learning(self.h, int(on)))
+
+    def resource_synapses(self, proj: bytes) -> np.ndarray:
+        out = np.empty(self._sizes[proj][1], T.RESOURCE_SYNAPSE_DTYPE)
+        self._chk(self.lib.or_read_resource_synapses(self.h, T.to_c_uid(proj), _ptr(out)))
+        return out
 
     def lif(self, pop: bytes):
         out = np.empty(self._sizes[pop][1], T.LIF_DTYPE)

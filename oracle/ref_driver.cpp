@@ -5,10 +5,12 @@
 // write golden fixtures. It includes, unmodified, from the reference tree:
 //   cpu-library/impl/populations/blifat/blifat_impl.h (+ blifat_stdp.h, training/stdp.h)
 //   cpu-library/impl/populations/lif/lif_impl.h
+//   cpu-library/impl/populations/altai/altai_impl.h (+ altai_stdp.h)
 //   cpu-library/impl/projections/delta/delta_impl.h (+ additive_stdp.h, synaptic_resource_stdp.h)
 // with the neuron/synapse trait headers, against the small shim in oracle/ref_shim/. Message routing
 // follows knp/backends/cpu/cpu-single-threaded-backend/impl/backend.cpp:89-141 exactly as in
 // knp_oracle.cpp; everything that touches a neuron or a synapse is the reference's code.
+#include <knp/backends/cpu-library/impl/populations/altai/altai_impl.h>
 #include <knp/backends/cpu-library/impl/populations/blifat/blifat_impl.h>
 #include <knp/backends/cpu-library/impl/populations/lif/lif_impl.h>
 #include <knp/backends/cpu-library/impl/projections/delta/delta_impl.h>
@@ -33,6 +35,8 @@ using LifParams = nt::neuron_parameters<nt::LIFNeuron>;
 using DeltaProj = kc::Projection<st::DeltaSynapse>;
 using AddStdpProj = kc::Projection<st::AdditiveSTDPDeltaSynapse>;
 using ResStdpProj = kc::Projection<st::SynapticResourceSTDPDeltaSynapse>;
+using AltaiParams = nt::neuron_parameters<nt::AltAILIF>;
+using ResAltaiParams = nt::neuron_parameters<nt::SynapticResourceSTDPAltAILIFNeuron>;
 
 namespace
 {
@@ -134,7 +138,8 @@ ResBlifatParams to_ref(const knp_blifat_neuron &a, const knp_resource_stdp_state
     return b;
 }
 
-knp_resource_stdp_state res_from_ref(const ResBlifatParams &b)
+template <class P>
+knp_resource_stdp_state res_from_ref(const P &b)
 {
     knp_resource_stdp_state r{};
     r.synapse_sum_threshold_coefficient = b.synapse_sum_threshold_coefficient_;
@@ -155,12 +160,74 @@ knp_resource_stdp_state res_from_ref(const ResBlifatParams &b)
     return r;
 }
 
+AltaiParams to_ref(const knp_altai_neuron &a)
+{
+    AltaiParams b;
+    b.is_diff_ = a.is_diff != 0;
+    b.is_reset_ = a.is_reset != 0;
+    b.leak_rev_ = a.leak_rev != 0;
+    b.saturate_ = a.saturate != 0;
+    b.do_not_save_ = a.do_not_save != 0;
+    b.potential_ = a.potential;
+    b.pre_impact_potential_ = a.pre_impact_potential;
+    b.activation_threshold_ = a.activation_threshold;
+    b.negative_activation_threshold_ = a.negative_activation_threshold;
+    b.potential_leak_ = a.potential_leak;
+    b.potential_reset_value_ = a.potential_reset_value;
+    b.dopamine_value_ = a.dopamine_value;
+    b.additional_threshold_ = a.additional_threshold;
+    b.activity_time_ = a.activity_time;
+    return b;
+}
+
+knp_altai_neuron from_ref(const AltaiParams &b)
+{
+    knp_altai_neuron a{};
+    a.is_diff = b.is_diff_ ? 1 : 0;
+    a.is_reset = b.is_reset_ ? 1 : 0;
+    a.leak_rev = b.leak_rev_ ? 1 : 0;
+    a.saturate = b.saturate_ ? 1 : 0;
+    a.do_not_save = b.do_not_save_ ? 1 : 0;
+    a.potential = b.potential_;
+    a.pre_impact_potential = b.pre_impact_potential_;
+    a.activation_threshold = b.activation_threshold_;
+    a.negative_activation_threshold = b.negative_activation_threshold_;
+    a.potential_leak = b.potential_leak_;
+    a.potential_reset_value = b.potential_reset_value_;
+    a.dopamine_value = b.dopamine_value_;
+    a.additional_threshold = b.additional_threshold_;
+    a.activity_time = b.activity_time_;
+    return a;
+}
+
+// The resource-STDP extension of a neuron of either base type.
+template <class P>
+void res_to_ref(P &b, const knp_resource_stdp_state &r)
+{
+    b.synapse_sum_threshold_coefficient_ = r.synapse_sum_threshold_coefficient;
+    b.dopamine_plasticity_time_ = r.dopamine_plasticity_time;
+    b.free_synaptic_resource_ = r.free_synaptic_resource;
+    b.synaptic_resource_threshold_ = r.synaptic_resource_threshold;
+    b.resource_drain_coefficient_ = r.resource_drain_coefficient;
+    b.stability_ = r.stability;
+    b.stability_change_parameter_ = r.stability_change_parameter;
+    b.stability_change_at_isi_ = r.stability_change_at_isi;
+    b.isi_max_ = r.isi_max;
+    b.d_h_ = r.d_h;
+    b.isi_status_ = static_cast<nt::ISIPeriodType>(r.isi_status);
+    b.last_step_ = r.last_step;
+    b.last_spike_step_ = r.last_spike_step;
+    b.first_isi_spike_ = r.first_isi_spike;
+    b.is_being_forced_ = r.is_being_forced != 0;
+}
+
 struct Pop
 {
     kc::UID uid;
     int kind;
     std::variant<kc::Population<nt::BLIFATNeuron>, kc::Population<nt::SynapticResourceSTDPBLIFATNeuron>,
-                 kc::Population<nt::LIFNeuron>>
+                 kc::Population<nt::LIFNeuron>, kc::Population<nt::AltAILIF>,
+                 kc::Population<nt::SynapticResourceSTDPAltAILIFNeuron>>
         pop;
     std::unordered_set<kc::UID, kc::uid_hash> impact_senders;
     std::vector<msg::SynapticImpactMessage> inbox;
@@ -170,7 +237,7 @@ struct Pop
 struct Proj
 {
     kc::UID uid;
-    std::variant<DeltaProj, AddStdpProj> proj;
+    std::variant<DeltaProj, AddStdpProj, ResStdpProj> proj;
     std::unordered_set<kc::UID, kc::uid_hash> spike_senders;
     std::vector<msg::SpikeMessage> inbox;
     knp::backends::cpu::projections::MessageQueue future;
@@ -207,6 +274,7 @@ namespace
 {
 namespace bl = knp::backends::cpu::populations::impl::blifat;
 namespace li = knp::backends::cpu::populations::impl::lif;
+namespace al = knp::backends::cpu::populations::impl::altai;
 namespace de = knp::backends::cpu::projections::impl::delta;
 
 template <class PopT, class Pre, class Imp, class Post>
@@ -227,7 +295,18 @@ void run_population(Pop &p, PopT &pop, Pre pre, Imp imp, Post post)
         if (post(pop[i])) p.last_spikes.push_back(static_cast<uint32_t>(i));
 }
 
-void step_population(Pop &p, uint64_t step)
+// populations_old.h:57-83, 207-209: the unlocked SynapticResourceSTDPDeltaSynapse projections into
+// population `uid`, in projection order.
+std::vector<std::reference_wrapper<ResStdpProj>> working_projections(or_net &net, const kc::UID &uid)
+{
+    std::vector<std::reference_wrapper<ResStdpProj>> working;
+    for (auto &q : net.projs)
+        if (auto *rp = std::get_if<ResStdpProj>(&q->proj))
+            if (rp->get_postsynaptic() == uid && !rp->is_locked()) working.emplace_back(*rp);
+    return working;
+}
+
+void step_population(or_net &net, Pop &p, uint64_t step)
 {
     if (auto *b = std::get_if<kc::Population<nt::BLIFATNeuron>>(&p.pop))
     {
@@ -242,10 +321,26 @@ void step_population(Pop &p, uint64_t step)
             p, *r, [](ResBlifatParams &n) { bl::calculate_pre_impact_single_neuron_state_impl(n); },
             [](ResBlifatParams &n, const msg::SynapticImpact &i, bool f) { bl::impact_neuron_impl(n, i, f); },
             [](ResBlifatParams &n) { return bl::calculate_post_impact_single_neuron_state_impl(n); });
-        // populations_old.h:207-209: no SynapticResourceSTDPDeltaSynapse projection is loaded.
-        std::vector<std::reference_wrapper<ResStdpProj>> working;
+        auto working = working_projections(net, p.uid);
         msg::SpikeMessage out{{p.uid, step}, {p.last_spikes.begin(), p.last_spikes.end()}};
         bl::train_population_impl(*r, working, out, step);
+    }
+    else if (auto *a = std::get_if<kc::Population<nt::AltAILIF>>(&p.pop))
+    {
+        run_population(
+            p, *a, [](AltaiParams &n) { al::calculate_pre_impact_single_neuron_state_impl(n); },
+            [](AltaiParams &n, const msg::SynapticImpact &i, bool f) { al::impact_neuron_impl(n, i, f); },
+            [](AltaiParams &n) { return al::calculate_post_impact_single_neuron_state_impl(n); });
+    }
+    else if (auto *ra = std::get_if<kc::Population<nt::SynapticResourceSTDPAltAILIFNeuron>>(&p.pop))
+    {
+        run_population(
+            p, *ra, [](ResAltaiParams &n) { al::calculate_pre_impact_single_neuron_state_impl(n); },
+            [](ResAltaiParams &n, const msg::SynapticImpact &i, bool f) { al::impact_neuron_impl(n, i, f); },
+            [](ResAltaiParams &n) { return al::calculate_post_impact_single_neuron_state_impl(n); });
+        auto working = working_projections(net, p.uid);
+        msg::SpikeMessage out{{p.uid, step}, {p.last_spikes.begin(), p.last_spikes.end()}};
+        al::train_population_impl(*ra, working, out, step);
     }
     else
     {
@@ -388,6 +483,120 @@ int or_add_projection(
     return 0;
 }
 
+int or_add_resource_projection(
+    or_net *net, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre_idx,
+    const uint32_t *post_idx, const float *weight, const uint32_t *delay, const uint8_t *out_type,
+    const knp_resource_synapse *rule, int locked)
+{
+    if (n_syn && !rule) return fail("resource-STDP synapses need their rule state");
+    auto p = std::make_unique<Proj>();
+    p->uid = to_uid(uid);
+    std::vector<ResStdpProj::Synapse> v;
+    for (uint64_t i = 0; i < n_syn; ++i)
+    {
+        st::synapse_parameters<st::SynapticResourceSTDPDeltaSynapse> s;
+        s.weight_ = weight[i];
+        s.delay_ = delay[i];
+        s.output_type_ = static_cast<st::OutputType>(out_type ? out_type[i] : 0);
+        s.rule_.synaptic_resource_ = rule[i].synaptic_resource;
+        s.rule_.w_min_ = rule[i].w_min;
+        s.rule_.w_max_ = rule[i].w_max;
+        s.rule_.d_u_ = rule[i].d_u;
+        s.rule_.dopamine_plasticity_period_ = rule[i].dopamine_plasticity_period;
+        s.rule_.last_spike_step_ = rule[i].last_spike_step;
+        s.rule_.had_hebbian_update_ = rule[i].had_hebbian_update != 0;
+        s.rule_.has_contributed_ = rule[i].has_contributed != 0;
+        v.emplace_back(s, pre_idx[i], post_idx[i]);
+    }
+    ResStdpProj proj(p->uid, to_uid(pre_uid), to_uid(post_uid), std::move(v));
+    if (locked)
+        proj.lock_weights();
+    else
+        proj.unlock_weights();
+    p->proj = std::move(proj);
+    net->projs.push_back(std::move(p));
+    return 0;
+}
+
+int or_set_learning(or_net *net, int on)
+{
+    for (auto &p : net->projs)
+        std::visit([on](auto &proj) { on ? proj.unlock_weights() : proj.lock_weights(); }, p->proj);
+    return 0;
+}
+
+int or_read_resource_synapses(const or_net *net, knp_uid proj, knp_resource_synapse *out)
+{
+    const Proj *p = net->find_proj(to_uid(proj));
+    const auto *r = p ? std::get_if<ResStdpProj>(&p->proj) : nullptr;
+    if (!r) return fail("unknown resource-STDP projection");
+    for (size_t i = 0; i < r->size(); ++i)
+    {
+        const auto &rule = std::get<kc::synapse_data>((*r)[i]).rule_;
+        knp_resource_synapse s{};
+        s.synaptic_resource = rule.synaptic_resource_;
+        s.w_min = rule.w_min_;
+        s.w_max = rule.w_max_;
+        s.d_u = rule.d_u_;
+        s.dopamine_plasticity_period = rule.dopamine_plasticity_period_;
+        s.had_hebbian_update = rule.had_hebbian_update_ ? 1u : 0u;
+        s.last_spike_step = rule.last_spike_step_;
+        s.has_contributed = rule.has_contributed_ ? 1u : 0u;
+        out[i] = s;
+    }
+    return 0;
+}
+
+int or_add_altai_population(
+    or_net *net, knp_uid uid, int kind, uint32_t n, const knp_altai_neuron *neurons, const knp_resource_stdp_state *ext)
+{
+    auto p = std::make_unique<Pop>();
+    p->uid = to_uid(uid);
+    p->kind = kind;
+    if (kind == KNP_NEURON_ALTAI_LIF)
+    {
+        std::vector<AltaiParams> v;
+        for (uint32_t i = 0; i < n; ++i) v.push_back(to_ref(neurons[i]));
+        p->pop = kc::Population<nt::AltAILIF>(p->uid, std::move(v));
+    }
+    else if (kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF && ext)
+    {
+        std::vector<ResAltaiParams> v;
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            ResAltaiParams b{to_ref(neurons[i])};
+            res_to_ref(b, ext[i]);
+            v.push_back(b);
+        }
+        p->pop = kc::Population<nt::SynapticResourceSTDPAltAILIFNeuron>(p->uid, std::move(v));
+    }
+    else
+        return fail("bad neuron kind");
+    net->pops.push_back(std::move(p));
+    return 0;
+}
+
+int or_read_altai(const or_net *net, knp_uid pop, knp_altai_neuron *out, knp_resource_stdp_state *ext)
+{
+    Pop *p = net->find_pop(to_uid(pop));
+    if (!p) return fail("unknown population");
+    if (auto *a = std::get_if<kc::Population<nt::AltAILIF>>(&p->pop))
+    {
+        for (size_t i = 0; i < a->size(); ++i) out[i] = from_ref((*a)[i]);
+        return 0;
+    }
+    if (auto *ra = std::get_if<kc::Population<nt::SynapticResourceSTDPAltAILIFNeuron>>(&p->pop))
+    {
+        for (size_t i = 0; i < ra->size(); ++i)
+        {
+            out[i] = from_ref(static_cast<const AltaiParams &>((*ra)[i]));
+            if (ext) ext[i] = res_from_ref((*ra)[i]);
+        }
+        return 0;
+    }
+    return fail("unknown AltAI population");
+}
+
 int or_set_stdp_population(or_net *net, knp_uid proj_uid, knp_uid pop_uid, int processing)
 {
     Proj *p = net->find_proj(to_uid(proj_uid));
@@ -473,7 +682,7 @@ int or_step(or_net *net)
             std::vector<msg::SpikeMessage> sent;
             for (auto &q : net->pops)
             {
-                step_population(*q, step);
+                step_population(*net, *q, step);
                 if (!q->last_spikes.empty())
                     sent.push_back(msg::SpikeMessage{{q->uid, step}, {q->last_spikes.begin(), q->last_spikes.end()}});
             }

@@ -26,6 +26,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from knp_gb300 import network as N  # noqa: E402
+from knp_gb300 import types as T  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
 CASES = [
@@ -35,7 +36,43 @@ CASES = [
     ("small_seed1_1000", "small_network", {"seed": 1, "steps": 1000}, 1000, []),
     ("large_sparse_n2000", "large_sparse_network", {"seed": 2, "n": 2000, "fan_in": 200, "steps": 100}, 100, []),
     ("stdp_3samples", "stdp_network", {"seed": 3, "samples": 3, "steps_per_sample": 100}, 300, [0, 1]),
+    ("smallest_resource_stdp", "smallest_network", {"kind": "resource_stdp"}, 20, [0, 1]),
+    ("smallest_resource_stdp_altai", "smallest_network", {"kind": "resource_stdp_altai"}, 20, [0, 1]),
+    ("resource_mnist_shaped", "resource_stdp_network", {"samples": 8}, 120, [0]),
+    ("resource_mixed", "resource_stdp_mixed_network", {"steps": 300}, 300, [0, 1, 4]),
 ]
+# Learning switches of a case: {step: on}, applied before that step (stop_learning / start_learning).
+LEARNING = {"resource_mixed": {150: False, 200: True}}
+
+
+def learning_switch(switches):
+    """An oracle.run on_step callback that applies {step: on} learning switches."""
+    def on_step(o, t):
+        if t in switches:
+            o.set_learning(switches[t])
+    return on_step
+
+
+def canonical(a):
+    """Bytes of an array with every FP32 / FP64 NaN replaced by one quiet NaN, so that digests do not
+    depend on the NaN payloads of the machine (x86 and Arm produce different default NaNs)."""
+    a = np.array(a, copy=True)
+    if a.dtype.names:
+        for f in a.dtype.names:
+            if a.dtype[f] in (np.float32, np.float64):
+                a[f] = np.where(np.isnan(a[f]), a.dtype[f].type(np.nan), a[f])
+        return a.tobytes()
+    if a.dtype in (np.float32, np.float64):
+        a = np.where(np.isnan(a), a.dtype.type(np.nan), a).astype(a.dtype)
+    return a.tobytes()
+
+
+def population_state(o, pop):
+    """(neurons, resource extension or None) of a population of any kind from an oracle."""
+    kind = o._sizes[pop.uid][0]
+    if T.is_altai(kind):
+        return o.altai(pop.uid)
+    return o.blifat(pop.uid)
 
 
 def digest(trains):
@@ -114,11 +151,22 @@ def main():
     out = {"source": "oracle/_ref/libknp_ref.so (KNP reference headers + shim)", "cases": []}
     for name, builder, kwargs, steps, wproj in CASES:
         net, sched = getattr(N, builder)(**kwargs)
-        res, o = orc.run(net, sched, steps, which="reference")
+        switches = LEARNING.get(name, {})
+        res, o = orc.run(net, sched, steps, which="reference", on_step=learning_switch(switches) if switches else None)
         pop = net.populations[0].uid
         case = {"name": name, "builder": builder, "kwargs": kwargs, "steps": steps,
                 "digest": digest(res[pop]), "events": o.events}
-        if wproj:
+        if switches:
+            case["learning"] = {str(k): v for k, v in switches.items()}
+        resource = [k for k, pr in enumerate(net.projections) if pr.kind == T.RESOURCE_STDP_DELTA]
+        if resource:
+            # Digests over NaN-canonical bytes: weights, rule state and the first population's state.
+            case["weights_crc"] = {str(k): zlib.crc32(canonical(o.weights(net.projections[k].uid))) for k in wproj}
+            case["rules_crc"] = {str(k): zlib.crc32(canonical(o.resource_synapses(net.projections[k].uid)))
+                                 for k in resource}
+            neurons, ext = population_state(o, net.populations[0])
+            case["state_crc"] = zlib.crc32(canonical(neurons) + (b"" if ext is None else canonical(ext)))
+        elif wproj:
             case["weights_crc"] = {str(k): zlib.crc32(o.weights(net.projections[k].uid).tobytes()) for k in wproj}
         out["cases"].append(case)
         print(name, "spikes", sum(s.size for s in res[pop]), "events", o.events)

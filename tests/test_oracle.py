@@ -79,6 +79,8 @@ def test_oracle_lif_known_answers(oracle_lib):
 def test_oracle_against_golden_fixtures(oracle_lib):
     """Spike digests written by tests/golden/make_golden.py from the reference-header oracle."""
     for case in load_golden("spike_digests.json")["cases"]:
+        if "rules_crc" in case:
+            continue  # resource-STDP cases: test_oracle_resource_stdp_fixtures
         net, sched = N.__dict__[case["builder"]](**case["kwargs"])
         out, o = orc.run(net, sched, case["steps"])
         pop = net.populations[0].uid
@@ -166,3 +168,71 @@ def test_restated_oracle_matches_reference_headers_blocking(oracle_lib):
         np.testing.assert_array_equal(x, y, err_msg=f"step {t}")
     np.testing.assert_array_equal(oa.blifat(pop)[0]["total_blocking_period"], ob.blifat(pop)[0]["total_blocking_period"])
     assert (oa.blifat(pop)[0]["total_blocking_period"] != np.iinfo(np.int64).max).sum() > 20
+
+
+@pytest.mark.parametrize("kind", ["resource_stdp", "resource_stdp_altai"])
+def test_oracle_resource_stdp_golden(oracle_lib, kind):
+    """knp/tests/backend/single_thread_cpu_test.cpp:179-355 (SynapticResourceSTDPDeltaSynapse
+    projections onto a resource-STDP BLIFAT or AltAI-LIF neuron, learning started): the expected spike
+    steps, and the loop projection's weight changes."""
+    net, sched = N.smallest_network(kind)
+    out, o = orc.run(net, sched, 20)
+    pop = net.populations[0].uid
+    assert [t for t, s in enumerate(out[pop]) if s.size] == GOLDEN
+    assert o.weights(net.projections[1].uid)[0] != 1.0
+
+
+def test_oracle_resource_stdp_fixtures(oracle_lib):
+    """The resource-STDP cases of the fixture (written from the reference-header oracle): weights,
+    synapse rule state and neuron state digests, with the learning switches of each case."""
+    from tests.golden.make_golden import canonical, learning_switch, population_state
+
+    cases = [c for c in load_golden("spike_digests.json")["cases"] if "rules_crc" in c]
+    assert len(cases) == 4
+    for case in cases:
+        net, sched = N.__dict__[case["builder"]](**case["kwargs"])
+        switches = {int(k): v for k, v in case.get("learning", {}).items()}
+        out, o = orc.run(net, sched, case["steps"], on_step=learning_switch(switches) if switches else None)
+        pop = net.populations[0].uid
+        assert spike_digest(out[pop]) == case["digest"], case["name"]
+        for k, crc in case["rules_crc"].items():
+            assert zlib.crc32(canonical(o.resource_synapses(net.projections[int(k)].uid))) == crc, (case["name"], k)
+        for k, crc in case["weights_crc"].items():
+            assert zlib.crc32(canonical(o.weights(net.projections[int(k)].uid))) == crc, (case["name"], k)
+        neurons, ext = population_state(o, net.populations[0])
+        assert zlib.crc32(canonical(neurons) + (b"" if ext is None else canonical(ext))) == case["state_crc"], case["name"]
+        assert o.events == case["events"], case["name"]
+
+
+def _same_runs(net, sched, steps, switches=None):
+    from tests.golden.make_golden import canonical, learning_switch, population_state
+
+    cb = learning_switch(switches) if switches else None
+    a, oa = orc.run(net, sched, steps, which="restated", on_step=cb)
+    b, ob = orc.run(net, sched, steps, which="reference", on_step=cb)
+    for p in net.populations:
+        assert spike_digest(a[p.uid]) == spike_digest(b[p.uid])
+        (sa, ea), (sb, eb) = population_state(oa, p), population_state(ob, p)
+        assert canonical(sa) == canonical(sb)
+        assert (ea is None and eb is None) or canonical(ea) == canonical(eb)
+    for pr in net.projections:
+        assert canonical(oa.weights(pr.uid)) == canonical(ob.weights(pr.uid))
+        if pr.kind == T.RESOURCE_STDP_DELTA:
+            assert canonical(oa.resource_synapses(pr.uid)) == canonical(ob.resource_synapses(pr.uid))
+    assert oa.events == ob.events
+    return oa
+
+
+@pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
+def test_restated_oracle_matches_reference_headers_resource_stdp(oracle_lib):
+    """Resource-STDP training (blifat_stdp.h:35-172, training/stdp.h:40-186) on the mnist-learn-shaped
+    network and on the mixed network with learning switched off and on again: the restated oracle
+    gives the reference headers' spikes, neuron state, weights and synapse rule state."""
+    net, sched = N.resource_stdp_network(samples=12)
+    o = _same_runs(net, sched, 180)
+    assert np.count_nonzero(o.weights(net.projections[0].uid)) > 1000
+    net, sched = N.resource_stdp_mixed_network(steps=300)
+    o = _same_runs(net, sched, 300, {150: False, 200: True})
+    rules = o.resource_synapses(net.projections[0].uid)
+    assert rules["had_hebbian_update"].sum() > 100 and rules["has_contributed"].sum() > 100
+
