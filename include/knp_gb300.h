@@ -123,6 +123,28 @@ KNP_GB300_API int knp_gb300_load_projection(
     const uint8_t *out_type, const float *tau_plus, const float *tau_minus);
 
 /**
+ * Load a projection of `n_syn` SynapticResourceSTDPDeltaSynapse synapses (synaptic-resource STDP,
+ * stdp_synaptic_resource_rule.h:45-89): synapse i is (weight[i], delay[i], out_type[i], rule[i]) from
+ * pre[i] to post[i], as knp_gb300_load_projection; `locked` is the projection's is_locked()
+ * (projection.h:384-396; a projection starts locked). The synapses deliver impacts like delta
+ * synapses with is_forcing false (synaptic_resource_stdp.h:58-62), record the step of every
+ * presynaptic spike (init_synapse, :36-41), and while unlocked are trained by their postsynaptic
+ * resource-STDP BLIFAT population at the end of its step (blifat_stdp.h:35-172: Hebbian and
+ * dopamine changes of the synaptic resource, free-resource renormalisation, weights recalculated
+ * from the resource). out_type may not hold KNP_OUT_BLOCKING. A backend with such projections runs
+ * the per-phase step (KNP_GB300_STEP_PHASES). Replaces: load_projections for
+ * Projection<SynapticResourceSTDPDeltaSynapse> (cpu-single-threaded-backend/impl/backend.cpp:158-178).
+ */
+KNP_GB300_API int knp_gb300_load_resource_stdp_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre,
+    const uint32_t *post, const float *weight, const uint32_t *delay, const uint8_t *out_type,
+    const knp_resource_synapse *rule, int locked);
+
+/** Read back the rule state of a resource-STDP projection's synapses in the order they were loaded.
+ * Replaces: get_network_data projection range for Projection<SynapticResourceSTDPDeltaSynapse>. */
+KNP_GB300_API int knp_gb300_read_resource_synapses(knp_gb300_backend *b, knp_uid proj, knp_resource_synapse *out);
+
+/**
  * Generate, on the device, a delta projection with fixed fan-in: synapse i has post = i % n_post,
  * pre = uniform [0, n_pre), weight = k/256 with k uniform in [k_lo, k_hi], delay uniform in
  * [d_lo, d_hi], drawn from the counter-based generator keyed by (seed, stream). Equivalent to
@@ -299,10 +321,11 @@ KNP_GB300_API int knp_gb300_read_weights(knp_gb300_backend *b, knp_uid proj, flo
 KNP_GB300_API int knp_gb300_projection_size(const knp_gb300_backend *b, knp_uid proj, uint64_t *n);
 
 /**
- * Unlock / lock projection weights. Replaces: start_learning / stop_learning
- * (cpu-single-threaded-backend/include/.../backend.h:315-332). As in the reference, additive-STDP
- * weight updates ignore the lock (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/impl/
- * projections/training/stdp/additive_stdp.h:173-196); the flag is kept for get/set symmetry.
+ * Unlock / lock the weights of every loaded projection. Replaces: start_learning / stop_learning
+ * (cpu-single-threaded-backend/include/.../backend.h:315-332). As in the reference, only
+ * resource-STDP training reads the lock (populations_old.h:57-83 keeps unlocked projections);
+ * additive-STDP weight updates ignore it (knp/backends/cpu/cpu-library/include/knp/backends/
+ * cpu-library/impl/projections/training/stdp/additive_stdp.h:173-196).
  */
 KNP_GB300_API int knp_gb300_start_learning(knp_gb300_backend *b);
 KNP_GB300_API int knp_gb300_stop_learning(knp_gb300_backend *b);

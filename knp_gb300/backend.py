@@ -99,13 +99,21 @@ class GB300Backend:
 
     def load_projections(self, projections):
         for pr in projections:
-            if pr.kind not in (T.DELTA, T.ADDITIVE_STDP_DELTA):
+            if pr.kind not in (T.DELTA, T.ADDITIVE_STDP_DELTA, T.RESOURCE_STDP_DELTA):
                 raise TypeError("Type is not supported.")
             arrs = [np.ascontiguousarray(pr.pre, np.uint32), np.ascontiguousarray(pr.post, np.uint32),
                     np.ascontiguousarray(pr.weight, np.float32), np.ascontiguousarray(pr.delay, np.uint32),
                     None if pr.out_type is None else np.ascontiguousarray(pr.out_type, np.uint8),
                     None if pr.tau_plus is None else np.ascontiguousarray(pr.tau_plus, np.float32),
                     None if pr.tau_minus is None else np.ascontiguousarray(pr.tau_minus, np.float32)]
+            if pr.kind == T.RESOURCE_STDP_DELTA:
+                rule = np.ascontiguousarray(pr.rule if pr.rule is not None else T.resource_synapse_defaults(pr.size),
+                                            T.RESOURCE_SYNAPSE_DTYPE)
+                self._chk(self._lib.knp_gb300_load_resource_stdp_projection(
+                    self._h, T.to_c_uid(pr.uid), T.to_c_uid(pr.pre_uid), T.to_c_uid(pr.post_uid), pr.size,
+                    *[_ptr(a) for a in arrs[:5]], _ptr(rule), int(pr.locked)))
+                self._projs[pr.uid] = pr
+                continue
             self._chk(self._lib.knp_gb300_load_projection(
                 self._h, T.to_c_uid(pr.uid), pr.kind, T.to_c_uid(pr.pre_uid), T.to_c_uid(pr.post_uid), pr.size,
                 *[_ptr(a) for a in arrs]))
@@ -307,6 +315,14 @@ class GB300Backend:
         self._chk(self._lib.knp_gb300_read_weights(self._h, T.to_c_uid(uid), _ptr(out)))
         return out
 
+    def read_resource_synapses(self, uid: bytes) -> np.ndarray:
+        """Rule state of a resource-STDP projection's synapses, in load order (RESOURCE_SYNAPSE_DTYPE)."""
+        n = ctypes.c_uint64(0)
+        self._chk(self._lib.knp_gb300_projection_size(self._h, T.to_c_uid(uid), ctypes.byref(n)))
+        out = np.empty(n.value, T.RESOURCE_SYNAPSE_DTYPE)
+        self._chk(self._lib.knp_gb300_read_resource_synapses(self._h, T.to_c_uid(uid), _ptr(out)))
+        return out
+
     def get_network_data(self):
         """Copies of the loaded populations and projections with the device's current state and
         weights (get_network.cpp:80-93)."""
@@ -322,6 +338,8 @@ class GB300Backend:
                 continue
             q = copy.copy(pr)
             q.weight = self.read_weights(uid)
+            if pr.kind == T.RESOURCE_STDP_DELTA:
+                q.rule = self.read_resource_synapses(uid)
             projs.append(q)
         return pops, projs
 

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libknp_gb300.so")
-SOURCES = ["population.cu", "projection.cu", "pull.cu", "bptt.cu", "batched.cu", "gemm.cu", "stdp.cu", "small_net.cu", "grid_net.cu", "generate.cu", "noalloc.cu", "engine.cu", "capi.cpp"]
+SOURCES = ["population.cu", "resource.cu", "projection.cu", "pull.cu", "bptt.cu", "batched.cu", "gemm.cu", "stdp.cu", "small_net.cu", "grid_net.cu", "generate.cu", "noalloc.cu", "engine.cu", "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden",
           "-I", CSRC, "-I", os.path.join(os.path.dirname(HERE), "include")]

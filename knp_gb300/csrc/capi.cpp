@@ -141,6 +141,9 @@ int knp_gb300_load_projection(
     return guarded(
         [&]
         {
+            if (kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA)
+                throw knp_gb300::Error(KNP_GB300_E_INVALID,
+                                       "resource-STDP projections are loaded with knp_gb300_load_resource_stdp_projection");
             b->impl.load_projection(U(uid), kind, U(pre_uid), U(post_uid), n_syn, pre, post, weight, delay, out_type,
                                     tau_plus, tau_minus);
         });
@@ -295,6 +298,26 @@ int knp_gb300_read_blifat_population(
 {
     if (!b || !out) return null_handle();
     return guarded([&] { b->impl.read_blifat(U(pop), out, ext); });
+}
+
+int knp_gb300_load_resource_stdp_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre,
+    const uint32_t *post, const float *weight, const uint32_t *delay, const uint8_t *out_type,
+    const knp_resource_synapse *rule, int locked)
+{
+    if (!b) return null_handle();
+    return guarded(
+        [&]
+        {
+            b->impl.load_resource_projection(U(uid), U(pre_uid), U(post_uid), n_syn, pre, post, weight, delay, out_type,
+                                             rule, locked != 0);
+        });
+}
+
+int knp_gb300_read_resource_synapses(knp_gb300_backend *b, knp_uid proj, knp_resource_synapse *out)
+{
+    if (!b || !out) return null_handle();
+    return guarded([&] { b->impl.read_resource_synapses(U(proj), out); });
 }
 
 int knp_gb300_read_weights(knp_gb300_backend *b, knp_uid proj, float *out)

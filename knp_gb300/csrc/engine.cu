@@ -212,7 +212,7 @@ void Backend::load_projection(
     const float *tau_minus)
 {
     require_not_init("load_projection");
-    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA)
+    if (kind != KNP_SYNAPSE_DELTA && kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA && kind != KNP_SYNAPSE_RESOURCE_STDP_DELTA)
         throw Error(KNP_GB300_E_INVALID, "unsupported synapse kind " + std::to_string(kind));
     if (n_syn && (!pre || !post || !w || !delay)) throw Error(KNP_GB300_E_INVALID, "null synapse array");
     if (n_syn > 0xFFFFFFFFull) throw Error(KNP_GB300_E_INVALID, "more than 2^32-1 synapses in one projection");
@@ -259,6 +259,40 @@ void Backend::load_projection(
                 throw Error(KNP_GB300_E_INVALID, "STDP time constants must be uniform within a projection");
     }
     projs_.push_back(std::move(p));
+}
+
+void Backend::load_resource_projection(
+    const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn, const uint32_t *pre, const uint32_t *post,
+    const float *w, const uint32_t *delay, const uint8_t *type, const knp_resource_synapse *rule, bool locked)
+{
+    if (n_syn && !rule) throw Error(KNP_GB300_E_INVALID, "resource-STDP synapses need their rule state");
+    load_projection(uid, KNP_SYNAPSE_RESOURCE_STDP_DELTA, pre_uid, post_uid, n_syn, pre, post, w, delay, type, nullptr,
+                    nullptr);
+    ProjectionSlot *p = projs_.back().get();
+    p->rule.assign(rule, rule + n_syn);
+    p->locked = locked;
+}
+
+void Backend::set_learning(bool on)
+{
+    // start_learning / stop_learning unlock / lock every projection (cpu-single-threaded/backend.h:
+    // 315-332); only resource-STDP training reads the lock.
+    learning_ = on;
+    for (auto &p : projs_) p->locked = !on;
+    if (initialized_) upload_locks();
+}
+
+void Backend::upload_locks()
+{
+    for (auto &q : pops_)
+    {
+        if (!q->res_locked) continue;
+        for (size_t k = 0; k < q->res_projs.size(); ++k) q->res_locked_host[k] = q->res_projs[k]->locked ? 1u : 0u;
+        // Ordered with the steps on the stream; the host vector outlives the copy.
+        KNP_CUDA(cudaMemcpyAsync(q->res_locked, q->res_locked_host.data(), q->res_locked_host.size() * 4,
+                                 cudaMemcpyHostToDevice, stream_));
+        KNP_CUDA(cudaStreamSynchronize(stream_));
+    }
 }
 
 void Backend::generate_fixed_fan_in(
@@ -369,7 +403,7 @@ void Backend::build_population(PopulationSlot &p)
         if (!(pr->post_uid == p.uid)) continue;
         slots = std::max(slots, pr->max_delay);
         dyadic = dyadic && pr->dyadic;
-        stdp_in = stdp_in || pr->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA;
+        stdp_in = stdp_in || pr->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA || pr->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA;
         const bool has_type = !pr->type.empty();
         auto any_type = [&](uint8_t t)
         { return has_type ? std::find(pr->type.begin(), pr->type.end(), t) != pr->type.end() : t == 0; };
@@ -414,6 +448,10 @@ void Backend::build_population(PopulationSlot &p)
             rg.blk_w = arena_.make<const float *>(std::max<size_t>(projs_.size(), 1));
             if (p.has_external_impacts) rg.blk_ext = arena_.make<long long>(np);
         }
+        if (fixed && res)
+            for (auto &pr : projs_)
+                if (pr->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA && pr->post_uid == p.uid && !rg.nf)
+                    rg.nf = arena_.make<uint32_t>(cells / 4);
         if (res && forcing_exc)
         {
             rg.words = (np + 31) / 32;
@@ -523,9 +561,14 @@ void Backend::build_population(PopulationSlot &p)
     if (d_in) f |= kLiveDopa;
     if (rg.blk) f |= kLiveBlock;
     if (f & (kLiveBlock | kLiveVRead | kLiveBurst)) f |= kLiveVPre;
+    bool res_syn = false;
+    if (res)
+        for (auto &pr : projs_)
+            if (pr->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA && pr->post_uid == p.uid) res_syn = true;
     if (res)
     {
         f |= kResource | kLiveAddThr;
+        if (res_syn) f |= kResSyn;
         for (uint32_t i = 0; i < n; ++i)
             if (!(std::fabs(p.init_res[i].free_synaptic_resource) < p.init_res[i].synaptic_resource_threshold))
                 f |= kLiveRenorm;
@@ -640,12 +683,28 @@ void Backend::build_population(PopulationSlot &p)
         r.resource_threshold = rpf([](const R &x) { return x.synaptic_resource_threshold; });
         r.stability_change_param = rpf([](const R &x) { return x.stability_change_parameter; });
         r.stability_change_at_isi = rpf([](const R &x) { return x.stability_change_at_isi; });
+        r.d_h = rpf([](const R &x) { return x.d_h; });
+        auto rpu = [&](auto get) -> ParamU
         {
-            ParamU x{nullptr, n ? rr[0].isi_max : 0u};
+            ParamU x{nullptr, n ? get(rr[0]) : 0u};
             bool uni = true;
-            for (uint32_t i = 1; i < n && uni; ++i) uni = rr[i].isi_max == x.u;
-            if (!uni) x.a = upload_u([&](uint32_t i) { return rr[i].isi_max; });
-            r.isi_max = x;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = get(rr[i]) == x.u;
+            if (!uni) x.a = upload_u([&](uint32_t i) { return get(rr[i]); });
+            return x;
+        };
+        r.isi_max = rpu([](const R &x) { return x.isi_max; });
+        r.dopamine_time = rpu([](const R &x) { return x.dopamine_plasticity_time; });
+        r.drain = rpu([](const R &x) { return x.resource_drain_coefficient; });
+        if (f & kResSyn)
+        {
+            // FP64 additional threshold and the training kernel's work list; the synapse arrays
+            // follow once every projection's CSR exists (build_resource_synapses).
+            std::vector<double> a(np, 0.0);
+            for (uint32_t i = 0; i < n; ++i) a[i] = nn[i].additional_threshold;
+            d.syn.add_thr = arena_.make<double>(np);
+            KNP_CUDA(cudaMemcpy(d.syn.add_thr, a.data(), np * 8, cudaMemcpyHostToDevice));
+            d.syn.work = arena_.make<uint32_t>(np);
+            d.syn.work_count = counters_ + p.work_counter_index;
         }
     }
     d.spikes = spikes;
@@ -812,6 +871,111 @@ void Backend::build_stdp(ProjectionSlot &p)
     }
 }
 
+// The resource-STDP projections into population q, concatenated in load order: each projection's
+// CSR weights, delays and last-spike steps become a slice of the population's arrays (its scatter
+// reads and writes them there), its rule state is uploaded in CSR order, and the column index lists
+// every neuron's synapses in get_all_connected_synapses order (training/stdp.h:55-72: projection
+// order, then the synapse index within the projection).
+void Backend::build_resource_synapses(PopulationSlot &q)
+{
+    for (auto &p : projs_)
+        if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA && p->post_uid == q.uid) q.res_projs.push_back(p.get());
+    if (q.res_projs.empty()) return;
+    if (q.res_projs.size() > 255)
+        throw Error(KNP_GB300_E_INVALID, "more than 255 resource-STDP projections into one population");
+    uint64_t total = 0;
+    for (ProjectionSlot *p : q.res_projs) total += p->n_syn;
+    const size_t T = std::max<uint64_t>(total, 1);
+    ResSynDev &y = q.res_syn;
+    y.w = arena_.make<float>(T, false);
+    y.resource = arena_.make<float>(T, false);
+    float *w_min = arena_.make<float>(T, false), *w_max = arena_.make<float>(T, false), *d_u = arena_.make<float>(T, false);
+    uint32_t *period = arena_.make<uint32_t>(T, false);
+    y.last_spike = arena_.make<unsigned long long>(T, false);
+    y.flags = arena_.make<uint8_t>(T, false);
+    uint8_t *delay = arena_.make<uint8_t>(T, false);
+    y.w_min = w_min;
+    y.w_max = w_max;
+    y.d_u = d_u;
+    y.period = period;
+    y.delay = delay;
+    std::vector<long long> col_ptr(static_cast<size_t>(q.n) + 1, 0);
+    std::vector<std::vector<uint32_t>> inv(q.res_projs.size());  // loaded index -> CSR position
+    uint64_t off = 0;
+    for (size_t k = 0; k < q.res_projs.size(); ++k)
+    {
+        ProjectionSlot &p = *q.res_projs[k];
+        const uint64_t S = p.n_syn;
+        p.res_pop = &q;
+        p.res_offset = off;
+        if (S)
+        {
+            std::vector<uint32_t> perm(S);
+            KNP_CUDA(cudaMemcpy(perm.data(), p.perm, S * 4, cudaMemcpyDeviceToHost));
+            inv[k].resize(S);
+            for (uint64_t e = 0; e < S; ++e) inv[k][perm[e]] = static_cast<uint32_t>(e);
+            std::vector<float> res(S), lo(S), hi(S), du(S);
+            std::vector<uint32_t> per(S);
+            std::vector<unsigned long long> ls(S);
+            std::vector<uint8_t> fl(S);
+            for (uint64_t e = 0; e < S; ++e)
+            {
+                const knp_resource_synapse &r = p.rule[perm[e]];
+                res[e] = r.synaptic_resource;
+                lo[e] = r.w_min;
+                hi[e] = r.w_max;
+                du[e] = r.d_u;
+                per[e] = r.dopamine_plasticity_period;
+                ls[e] = r.last_spike_step;
+                fl[e] = static_cast<uint8_t>((r.had_hebbian_update ? 1u : 0u) | (r.has_contributed ? 2u : 0u));
+            }
+            KNP_CUDA(cudaMemcpy(y.resource + off, res.data(), S * 4, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(w_min + off, lo.data(), S * 4, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(w_max + off, hi.data(), S * 4, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(d_u + off, du.data(), S * 4, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(period + off, per.data(), S * 4, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(y.last_spike + off, ls.data(), S * 8, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(y.flags + off, fl.data(), S, cudaMemcpyHostToDevice));
+            KNP_CUDA(cudaMemcpy(y.w + off, p.w, S * 4, cudaMemcpyDeviceToDevice));
+            KNP_CUDA(cudaMemcpy(delay + off, p.delay_d, S, cudaMemcpyDeviceToDevice));
+            for (uint64_t i = 0; i < S; ++i) ++col_ptr[p.post[i] + 1];
+        }
+        arena_.release(p.w);
+        arena_.release(p.delay_d);
+        p.w = y.w + off;
+        p.delay_d = delay + off;
+        p.dev.w = p.w;
+        p.dev.delay = p.delay_d;
+        p.dev.last_spike = y.last_spike + off;
+        off += S;
+    }
+    for (uint32_t i = 0; i < q.n; ++i) col_ptr[i + 1] += col_ptr[i];
+    std::vector<unsigned long long> col_pos(T, 0);
+    std::vector<long long> fill(col_ptr.begin(), col_ptr.end() - 1);
+    for (size_t k = 0; k < q.res_projs.size(); ++k)
+    {
+        const ProjectionSlot &p = *q.res_projs[k];
+        for (uint64_t i = 0; i < p.n_syn; ++i)
+            col_pos[fill[p.post[i]]++] = (static_cast<unsigned long long>(k) << kResSlotShift) | (p.res_offset + inv[k][i]);
+    }
+    auto *cp = arena_.make<long long>(col_ptr.size(), false);
+    auto *cpos = arena_.make<unsigned long long>(T, false);
+    KNP_CUDA(cudaMemcpy(cp, col_ptr.data(), col_ptr.size() * 8, cudaMemcpyHostToDevice));
+    KNP_CUDA(cudaMemcpy(cpos, col_pos.data(), T * 8, cudaMemcpyHostToDevice));
+    y.col_ptr = cp;
+    y.col_pos = cpos;
+    q.res_locked_host.assign(q.res_projs.size(), 0u);
+    q.res_locked = arena_.make<uint32_t>(q.res_projs.size());
+    y.locked = q.res_locked;
+    if (q.bdev.flags & kResSyn)
+    {
+        y.add_thr = q.bdev.syn.add_thr;
+        y.work = q.bdev.syn.work;
+        y.work_count = q.bdev.syn.work_count;
+        q.bdev.syn = y;
+    }
+}
+
 cudaError_t set_gather_smem(size_t bytes);
 
 int Backend::gather_grid(const ProjectionSlot &p) const
@@ -923,7 +1087,7 @@ void Backend::init()
                 if (p->post[i] < post->n) colsum[p->post[i]] += std::fabs(p->weight[i]);
             for (double v : colsum) dy = dy && v < 32768.0;
         }
-        p->dyadic = dy;
+        p->dyadic = dy && p->kind != KNP_SYNAPSE_RESOURCE_STDP_DELTA;  // resource-STDP weights change
         if (post)
             for (uint32_t v : p->post)
                 if (v >= post->n) throw Error(KNP_GB300_E_INVALID, "postsynaptic index out of the target population");
@@ -939,6 +1103,9 @@ void Backend::init()
     n_counters_ = n_spike_counters_;
     for (auto &p : projs_)
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) ++n_counters_;
+    // Work-list counts of the resource-STDP training, one per population that may need one.
+    for (auto &q : pops_)
+        if (q->kind == KNP_NEURON_RESOURCE_STDP_BLIFAT) q->work_counter_index = n_counters_++;
     counters_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
     for (uint32_t i = 0; i < pops_.size(); ++i) pops_[i]->counter_index = i;
     neurons_total_ = 0;
@@ -953,6 +1120,8 @@ void Backend::init()
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) build_stdp(*p);
         build_pull(*p);
     }
+    for (auto &q : pops_) build_resource_synapses(*q);
+    upload_locks();
     uint32_t ci = n_spike_counters_;
     for (auto &p : projs_)
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) p->stdp.touched_count = counters_ + ci++;
@@ -973,6 +1142,7 @@ void Backend::init()
         std::vector<uint32_t>().swap(p->delay);
         std::vector<float>().swap(p->weight);
         if (p->kind != KNP_SYNAPSE_ADDITIVE_STDP_DELTA) std::vector<uint32_t>().swap(p->post);
+        if (p->res_pop) std::vector<knp_resource_synapse>().swap(p->rule);
     }
     std::string why;
     fused_ = step_mode_ == KNP_GB300_STEP_FUSED || (step_mode_ == KNP_GB300_STEP_AUTO && small_net_eligible(why));
@@ -1008,6 +1178,11 @@ bool Backend::small_net_eligible(std::string &why) const
     for (auto &p : projs_)
     {
         syn += p->n_syn;
+        if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA)
+        {
+            why = "resource-STDP projections are trained between the per-phase kernels";
+            return false;
+        }
         if (p->pull)
         {
             why = "a projection has a gather layout";
@@ -1049,6 +1224,11 @@ bool Backend::grid_net_eligible(std::string &why)
     uint32_t n_pull = 0;
     for (auto &p : projs_)
     {
+        if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA)
+        {
+            why = "resource-STDP projections are trained between the per-phase kernels";
+            return false;
+        }
         if (p->stdp_pops.size() > static_cast<size_t>(kMaxSources))
         {
             why = "a projection has more than " + std::to_string(kMaxSources) + " STDP populations";
@@ -1219,15 +1399,26 @@ void Backend::build_small_net()
 
 // ------------------------------------------------------------------------------------ stepping
 
+// One population's step: its kernel, then (resource-STDP populations with resource-STDP synapses)
+// the training that ends the population's step in the reference (populations_old.h:207-209).
+void Backend::launch_population(const PopulationSlot &q)
+{
+    if (q.kind == KNP_NEURON_LIF)
+    {
+        launch_lif(q.ldev, ctl_, stream_);
+        return;
+    }
+    launch_blifat(q.bdev, ctl_, stream_);
+    if (q.bdev.flags & kResSyn)
+    {
+        const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((q.n + 7) / 8, 4ull * sm_count_));
+        launch_resource_train(q.bdev, static_cast<int>(blocks), ctl_, stream_);
+    }
+}
+
 void Backend::enqueue_step()
 {
-    for (auto &q : pops_)
-    {
-        if (q->kind == KNP_NEURON_LIF)
-            launch_lif(q->ldev, ctl_, stream_);
-        else
-            launch_blifat(q->bdev, ctl_, stream_);
-    }
+    for (auto &q : pops_) launch_population(*q);
     for (auto &p : projs_)
     {
         if (p->dev.n_src == 0) continue;
@@ -1462,13 +1653,7 @@ void Backend::profile_phases(uint64_t n, float *ms)
     {
         if (any_recording_ && steps_before_drain() == 0) drain_recordings();
         KNP_CUDA(cudaEventRecord(ev[0], stream_));
-        for (auto &q : pops_)
-        {
-            if (q->kind == KNP_NEURON_LIF)
-                launch_lif(q->ldev, ctl_, stream_);
-            else
-                launch_blifat(q->bdev, ctl_, stream_);
-        }
+        for (auto &q : pops_) launch_population(*q);
         KNP_CUDA(cudaEventRecord(ev[1], stream_));
         for (auto &p : projs_)
         {
@@ -1917,7 +2102,13 @@ void Backend::read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_s
         auto v = getf(d.dopa);
         for (uint32_t i = 0; i < n; ++i) out[i].dopamine_value = v[i];
     }
-    if (d.add_thr)
+    if (f & kResSyn)
+    {
+        std::vector<double> v(n);
+        if (n) KNP_CUDA(cudaMemcpy(v.data(), d.syn.add_thr, n * 8, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < n; ++i) out[i].additional_threshold = v[i];
+    }
+    else if (d.add_thr)
     {
         auto v = getf(d.add_thr);
         for (uint32_t i = 0; i < n; ++i) out[i].additional_threshold = v[i];
@@ -2015,6 +2206,49 @@ void Backend::read_weights(const Uid &proj, float *out)
     std::vector<uint32_t> perm(p->n_syn);
     if (p->n_syn) KNP_CUDA(cudaMemcpy(perm.data(), p->perm, p->n_syn * 4, cudaMemcpyDeviceToHost));
     for (uint64_t e = 0; e < p->n_syn; ++e) out[perm[e]] = w[e];
+}
+
+void Backend::read_resource_synapses(const Uid &proj, knp_resource_synapse *out)
+{
+    ProjectionSlot *p = find_proj(proj);
+    if (!p || p->kind != KNP_SYNAPSE_RESOURCE_STDP_DELTA)
+        throw Error(KNP_GB300_E_INVALID, "unknown resource-STDP projection");
+    const uint64_t S = p->n_syn;
+    if (!initialized_ || !p->res_pop)
+    {
+        // Not trained and not scattered (no target population on this backend): the loaded state.
+        std::copy(p->rule.begin(), p->rule.end(), out);
+        return;
+    }
+    if (!S) return;
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    const ResSynDev &y = p->res_pop->res_syn;
+    const uint64_t off = p->res_offset;
+    std::vector<float> res(S), lo(S), hi(S), du(S);
+    std::vector<uint32_t> per(S), perm(S);
+    std::vector<unsigned long long> ls(S);
+    std::vector<uint8_t> fl(S);
+    KNP_CUDA(cudaMemcpy(res.data(), y.resource + off, S * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(lo.data(), y.w_min + off, S * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(hi.data(), y.w_max + off, S * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(du.data(), y.d_u + off, S * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(per.data(), y.period + off, S * 4, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(ls.data(), y.last_spike + off, S * 8, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(fl.data(), y.flags + off, S, cudaMemcpyDeviceToHost));
+    KNP_CUDA(cudaMemcpy(perm.data(), p->perm, S * 4, cudaMemcpyDeviceToHost));
+    for (uint64_t e = 0; e < S; ++e)
+    {
+        knp_resource_synapse r{};
+        r.synaptic_resource = res[e];
+        r.w_min = lo[e];
+        r.w_max = hi[e];
+        r.d_u = du[e];
+        r.dopamine_plasticity_period = per[e];
+        r.had_hebbian_update = fl[e] & 1u;
+        r.last_spike_step = ls[e];
+        r.has_contributed = (fl[e] >> 1) & 1u;
+        out[perm[e]] = r;
+    }
 }
 
 uint64_t Backend::projection_size(const Uid &proj) const

@@ -114,6 +114,8 @@ private:
     bool stop_ = false;
 };
 
+struct ProjectionSlot;
+
 struct PopulationSlot
 {
     Uid uid;
@@ -137,6 +139,13 @@ struct PopulationSlot
     // recorded spikes drained to the host: per step, the spike bitmap and its count
     std::map<uint64_t, RecordedStep> recorded;
     uint64_t record_from = 0;
+    // SynapticResourceSTDPDeltaSynapse projections into this population (load order) and their
+    // concatenated synapse arrays; the training runs for resource-STDP BLIFAT populations.
+    std::vector<ProjectionSlot *> res_projs;
+    ResSynDev res_syn{};
+    uint32_t *res_locked = nullptr;  // device copy of the projections' lock flags
+    std::vector<uint32_t> res_locked_host;
+    uint32_t work_counter_index = 0;
 };
 
 struct ProjectionSlot
@@ -174,6 +183,12 @@ struct ProjectionSlot
     ProjectionDev dev{};
     StdpDev stdp{};
     std::vector<std::pair<SpikeSource, int>> stdp_sources;  // (source, both lists)
+    // resource-STDP synapses: rule state in load order (host copy until init, and for projections
+    // with no target population on this backend), lock flag, slice of the target's arrays
+    std::vector<knp_resource_synapse> rule;
+    bool locked = true;
+    PopulationSlot *res_pop = nullptr;
+    uint64_t res_offset = 0;
 };
 
 struct Channel
@@ -211,6 +226,10 @@ public:
     void load_projection(const Uid &uid, int kind, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn,
                          const uint32_t *pre, const uint32_t *post, const float *w, const uint32_t *delay,
                          const uint8_t *type, const float *tau_plus, const float *tau_minus);
+    void load_resource_projection(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint64_t n_syn,
+                                  const uint32_t *pre, const uint32_t *post, const float *w, const uint32_t *delay,
+                                  const uint8_t *type, const knp_resource_synapse *rule, bool locked);
+    void read_resource_synapses(const Uid &proj, knp_resource_synapse *out);
     void generate_fixed_fan_in(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint32_t n_pre, uint32_t n_post,
                                uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed,
                                uint64_t stream);
@@ -245,7 +264,7 @@ public:
     uint64_t projection_size(const Uid &proj) const;
     void counters(uint64_t *events, uint64_t *spikes, uint64_t *updates);
     void synchronize();
-    void set_learning(bool on) { learning_ = on; }
+    void set_learning(bool on);
     cudaStream_t stream() const { return stream_; }
 
 private:
@@ -261,9 +280,12 @@ private:
     void build_projection(ProjectionSlot &p);
     void build_stdp(ProjectionSlot &p);
     void build_pull(ProjectionSlot &p);
+    void build_resource_synapses(PopulationSlot &q);
+    void upload_locks();
     int gather_grid(const ProjectionSlot &p) const;
     void wire();
     void enqueue_step();
+    void launch_population(const PopulationSlot &q);
     bool small_net_eligible(std::string &why) const;
     bool grid_net_eligible(std::string &why);
     void build_small_net();

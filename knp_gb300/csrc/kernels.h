@@ -61,6 +61,10 @@ struct RingView
     unsigned long long *blk;
     const float *const *blk_w;
     long long *blk_ext;
+    // Non-finite EXCITATORY / INHIBITORY_CURRENT impacts (trained resource-STDP weights can become NaN
+    // or infinite), or null: one byte per (slot, neuron), packed four to a word, bit 0 NaN, bit 1 +inf,
+    // bit 2 -inf; such impacts are not added to the fixed-point sum.
+    uint32_t *nf;
 };
 
 // Key of a BLOCKING impact: the reference applies the impacts of a step in message order and the last
@@ -94,6 +98,7 @@ enum BlifatFlags : uint32_t
     kResource = 1u << 9,      // synaptic-resource-STDP neuron bookkeeping
     kLiveRenorm = 1u << 10,   // free-resource renormalisation can fire
     kLiveAddThr = 1u << 11,   // additional threshold differs from 0 somewhere
+    kResSyn = 1u << 12,       // resource-STDP neurons with SynapticResourceSTDPDeltaSynapse projections
 };
 
 // One parameter: a broadcast value, or a per-neuron array when `a` is not null.
@@ -116,8 +121,32 @@ struct ResourceDev
     float *stability, *free_resource;
     uint8_t *is_forced;  // is_being_forced_ of the last step
     // parameters
-    ParamF add_thr_coef, resource_threshold, stability_change_param, stability_change_at_isi;
-    ParamU isi_max;
+    ParamF add_thr_coef, resource_threshold, stability_change_param, stability_change_at_isi, d_h;
+    ParamU isi_max, dopamine_time, drain;
+};
+
+// SynapticResourceSTDPDeltaSynapse synapses into one population: the synapses of all its
+// resource-STDP projections, concatenated in projection load order, each projection's CSR range
+// one slice (the projection's scatter reads its weights and writes last_spike there). Synapse
+// state is the rule of stdp_synaptic_resource_rule.h:45-89.
+constexpr int kResSlotShift = 56;  // col_pos entries: projection slot << 56 | position
+struct ResSynDev
+{
+    float *w;                        // weight_
+    float *resource;                 // synaptic_resource_
+    const float *w_min, *w_max, *d_u;
+    const uint32_t *period;          // dopamine_plasticity_period_
+    unsigned long long *last_spike;  // last_spike_step_
+    uint8_t *flags;                  // bit 0 had_hebbian_update_, bit 1 has_contributed_
+    const uint8_t *delay;
+    // By postsynaptic neuron, in get_all_connected_synapses order (projection load order, then
+    // synapse index): entries col_pos[col_ptr[i] .. col_ptr[i + 1]).
+    const long long *col_ptr;
+    const unsigned long long *col_pos;
+    const uint32_t *locked;          // [slot] 1: the projection's weights are locked (not trained)
+    uint32_t *work;                  // non-spiking neurons with dopamine or renormalisation work this step
+    uint32_t *work_count;            // this step (a per-step counter)
+    double *add_thr;                 // additional_threshold_, FP64 as the reference keeps it
 };
 
 struct BlifatDev
@@ -132,6 +161,7 @@ struct BlifatDev
     ParamF thr, thr_decay, thr_inc, trace_decay, trace_inc, g_decay, v_decay, reflexive, e_inh, v_reset, v_min;
     ParamU t_ref, burst_period;
     ResourceDev res;
+    ResSynDev syn;  // kResSyn only
     // outputs
     uint32_t *spikes;
     uint32_t *spike_count;  // this step
@@ -232,6 +262,7 @@ struct ProjectionDev
     const uint8_t *type;  // per-synapse output type, or null (uniform_type)
     int uniform_type;
     int forcing;  // impacts of this projection carry is_forcing (plain delta projections)
+    unsigned long long *last_spike;  // resource-STDP synapses: last_spike_step_ per CSR position, or null
     uint32_t order;  // load order among the backend's projections (message order of BLOCKING impacts)
     RingView ring;
     int n_src;
@@ -310,6 +341,7 @@ struct GridNet
 
 // ---------------------------------------------------------------- launchers (stream-ordered)
 void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s);
+void launch_resource_train(const BlifatDev &p, int blocks, Control *ctl, cudaStream_t s);
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
 void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
@@ -434,6 +466,101 @@ __host__ __device__ inline void fx_normalize(long long &hi, long long &lo)
 {
     hi += lo >> kFxLoBits;
     lo &= (1ll << kFxLoBits) - 1;
+}
+
+// The smallest two-word fixed-point value (hi * 2^-8 + lo * 2^-48, 0 <= lo < 2^40) that is >= x,
+// for comparing an exact fixed-point sum V with an FP64 threshold: V >= x iff (V.hi, V.lo) >= (hi, lo)
+// lexicographically. NaN and +inf give a value no sum reaches, -inf one every sum reaches;
+// |x| >= 2^54 saturates as fx_split does.
+__host__ __device__ inline void fx_ceil64(double x, long long &hi, long long &lo)
+{
+    unsigned long long b;
+    static_assert(sizeof(double) == sizeof(unsigned long long), "64-bit double");
+#ifdef __CUDA_ARCH__
+    b = static_cast<unsigned long long>(__double_as_longlong(x));
+#else
+    __builtin_memcpy(&b, &x, 8);
+#endif
+    const bool neg = (b >> 63) != 0;
+    const int ex = static_cast<int>((b >> 52) & 0x7FFu);
+    unsigned long long m = b & ((1ull << 52) - 1);
+    if (ex == 0x7FF)
+    {
+        if (neg && m == 0)
+        {
+            hi = -0x7FFFFFFFFFFFFFFFll - 1;
+            lo = 0;
+        }
+        else
+        {
+            hi = 0x7FFFFFFFFFFFFFFFll;
+            lo = 1ll << kFxLoBits;
+        }
+        return;
+    }
+    int e = -1074;
+    if (ex != 0)
+    {
+        m |= 1ull << 52;
+        e = ex - 1075;
+    }
+    const unsigned long long mask = (1ull << kFxLoBits) - 1;
+    const int s = e + 48;  // |x| * 2^48 = m * 2^s
+    // C = ceil(|x| * 2^48) for x > 0, floor(|x| * 2^48) for x < 0 (then negated), as H * 2^40 + L.
+    unsigned long long H = 0, L = 0;
+    if (s >= 0)
+    {
+        if (s <= 10)
+        {
+            const unsigned long long v = m << s;  // < 2^63
+            H = v >> kFxLoBits;
+            L = v & mask;
+        }
+        else if (s < kFxLoBits)
+        {
+            H = m >> (kFxLoBits - s);
+            L = (m << s) & mask;  // the low 40 bits survive the shift's wrap
+        }
+        else if (s - kFxLoBits <= 9)
+        {
+            H = m << (s - kFxLoBits);  // < 2^62
+        }
+        else
+        {
+            H = 1ull << 62;
+        }
+    }
+    else
+    {
+        const int r = -s;
+        unsigned long long q = 0, rem = m;
+        if (r < 64)
+        {
+            q = m >> r;
+            rem = m & ((1ull << r) - 1);
+        }
+        if (!neg && rem) ++q;
+        H = q >> kFxLoBits;
+        L = q & mask;
+    }
+    if (neg)
+    {
+        if (L)
+        {
+            hi = -static_cast<long long>(H) - 1;
+            lo = static_cast<long long>((1ull << kFxLoBits) - L);
+        }
+        else
+        {
+            hi = -static_cast<long long>(H);
+            lo = 0;
+        }
+    }
+    else
+    {
+        hi = static_cast<long long>(H);
+        lo = static_cast<long long>(L);
+    }
 }
 
 #ifdef __CUDACC__

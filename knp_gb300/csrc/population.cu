@@ -13,13 +13,13 @@ namespace
 
 constexpr int kBlock = 256;
 
-template <bool kFixed>
+template <bool kFixed, bool kRS>
 __global__ void __launch_bounds__(kBlock, 3) blifat_kernel(BlifatDev p, Control *ctl)
 {
     pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t i0 = (blockIdx.x * kBlock + threadIdx.x) * 4;
-    const uint32_t mask = blifat_quad<kFixed>(p, t, i0);
+    const uint32_t mask = blifat_quad<kFixed, kRS>(p, t, i0);
     emit_spikes<kBlock>(mask, i0, p.spikes, p.spike_count, record_slot(p.rec_bits, p.rec_words, p.rec_slots, t),
                         p.rec_words);
 }
@@ -73,10 +73,13 @@ void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s)
 {
     const uint32_t quads = (p.n + 3) / 4;
     const uint32_t grid = (quads + kBlock - 1) / kBlock;
-    if (p.ring.fixed)
-        launch_pdl(blifat_kernel<true>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
+    // Resource-STDP synapses always feed a fixed-point ring.
+    if (p.flags & kResSyn)
+        launch_pdl(blifat_kernel<true, true>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
+    else if (p.ring.fixed)
+        launch_pdl(blifat_kernel<true, false>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
     else
-        launch_pdl(blifat_kernel<false>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
+        launch_pdl(blifat_kernel<false, false>, dim3(grid), dim3(kBlock), 0, s, p, ctl);
 }
 
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s)

@@ -94,14 +94,16 @@ struct NeuronState
     float V, V_pre, thr_dyn, trace, g, dopa, add_thr;
     uint32_t ns, phase;
     long long block;
+    double add64;  // kResSyn: the FP64 additional threshold
 };
 
 // One BLIFAT neuron for one step. `acc` is this step's summed EXCITATORY - INHIBITORY_CURRENT input
-// (FP32 ring) and (acc_hi, acc_lo) the same in two-word fixed point (fixed ring).
-template <bool kFixed>
+// (FP32 ring) and (acc_hi, acc_lo) the same in two-word fixed point (fixed ring). kRS: a kResSyn
+// population (separate instantiation, so that other populations carry none of its code).
+template <bool kFixed, bool kRS = false>
 __device__ __forceinline__ bool blifat_step(
     const BlifatDev &p, uint32_t i, unsigned long long t, NeuronState &s, float acc, long long acc_hi,
-    long long acc_lo, float g_in, float d_in)
+    long long acc_lo, float g_in, float d_in, uint32_t nf = 0)
 {
     const uint32_t f = p.flags;
     const bool res = f & kResource;
@@ -111,7 +113,10 @@ __device__ __forceinline__ bool blifat_step(
     if (f & kLiveTrace) s.trace = __fmul_rn(s.trace, pf(p.trace_decay, i));
     if (f & kLiveG) s.g = __fmul_rn(s.g, pf(p.g_decay, i));
     if (res) s.dopa = 0.0f;
-    s.V = (f & kLiveVRead) ? __fmul_rn(s.V, pf(p.v_decay, i)) : 0.0f;
+    if (kRS && !(f & kLiveVRead))
+        s.V = isfinite(s.V) ? 0.0f : __int_as_float(0x7FC00000);  // V * 0: NaN for a NaN or infinite V
+    else
+        s.V = (f & kLiveVRead) ? __fmul_rn(s.V, pf(p.v_decay, i)) : 0.0f;
     if ((f & kLiveBurst) && s.phase == 1u)
     {
         if (!res) s.phase = 0u;
@@ -138,6 +143,18 @@ __device__ __forceinline__ bool blifat_step(
         }
         fx_ok = true;
         s.V = fx_to_float(vh, vl);
+        if (kRS && (nf || !isfinite(s.V_pre)))
+        {
+            // A non-finite term makes the FP64 sum non-finite: NaN if any term is NaN or both infinities
+            // occur, else the infinity.
+            const bool pinf = (nf & 2u) || s.V_pre == __int_as_float(0x7F800000);
+            const bool ninf = (nf & 4u) || s.V_pre == __int_as_float(0xFF800000);
+            if ((nf & 1u) || isnan(s.V_pre) || (pinf && ninf))
+                s.V = __int_as_float(0x7FC00000);
+            else
+                s.V = pinf ? __int_as_float(0x7F800000) : __int_as_float(0xFF800000);
+            fx_ok = false;
+        }
     }
     else
     {
@@ -175,7 +192,24 @@ __device__ __forceinline__ bool blifat_step(
     const float thr_total = __fadd_rn(__fadd_rn(pf(p.thr, i), s.thr_dyn), s.add_thr);
     const bool ref_ok = (f & kLiveRefract) ? (s.ns > pu(p.t_ref, i)) : (t > 0);
     bool above;
-    if (kFixed && fx_ok)
+    if (kRS)
+    {
+        // The additional threshold of trained synapses is an FP64 sum: compare in FP64, exactly
+        // against the fixed-point potential.
+        const double thr64 =
+            __dadd_rn(__dadd_rn(static_cast<double>(pf(p.thr, i)), static_cast<double>(s.thr_dyn)), s.add64);
+        if (kFixed && fx_ok)
+        {
+            long long th, tl;
+            fx_ceil64(thr64, th, tl);
+            above = vh > th || (vh == th && vl >= tl);
+        }
+        else
+        {
+            above = static_cast<double>(s.V) >= thr64;
+        }
+    }
+    else if (kFixed && fx_ok)
     {
         long long th, tl;
         fx_split(thr_total, th, tl);
@@ -199,8 +233,60 @@ __device__ __forceinline__ bool blifat_step(
     return spike;
 }
 
-// Resource-STDP neuron bookkeeping with no resource-STDP synapses (blifat_stdp.h:35-172).
-__device__ __forceinline__ void resource_step(
+// update_isi (training/stdp.h:88-126) of a neuron that spiked at step t: its new ISI status
+// (0 is_forced, 1 period_started, 2 period_continued, 3 not_in_period). The step differences are
+// unsigned, as in the reference.
+__device__ __forceinline__ int32_t update_isi(
+    int32_t status, bool forced, float dopa, uint32_t isi_max, unsigned long long t, unsigned long long &last_step,
+    unsigned long long &first_isi_spike)
+{
+    if (forced) return 0;  // last_step_ is not updated
+    switch (status)
+    {
+        case 3:
+        case 0:
+            status = 1;
+            first_isi_spike = t;
+            break;
+        case 1:
+            if (last_step - t < isi_max) status = 2;
+            break;
+        default:
+            if (last_step - t >= isi_max || dopa != 0.0f)
+            {
+                status = 1;
+                first_isi_spike = t;
+            }
+            break;
+    }
+    last_step = t;
+    return status;
+}
+
+// The dopamine change of stability (blifat_stdp.h:138-150). The reference's dopamine value and
+// intermediates are FP64 and the stored stability FP32: the same operations here.
+__device__ __noinline__ float dopamine_stability(
+    float stability, float dopa, float change_param, bool forced, unsigned long long t,
+    unsigned long long first_isi_spike, uint32_t isi_max)
+{
+    if (forced || dopa < 0.0f)
+    {
+        const float st = __double2float_rn(
+            __dsub_rn(static_cast<double>(stability), __dmul_rn(static_cast<double>(dopa), static_cast<double>(change_param))));
+        return st < 0.0f ? 0.0f : st;  // std::max(stability, 0.0F)
+    }
+    // std::fabs of the unsigned difference, converted to double.
+    const double difference = __ull2double_rn(t - first_isi_spike - isi_max);
+    const double q = __dsub_rn(2.0, __ddiv_rn(difference, static_cast<double>(isi_max)));
+    const double m = q < -1.0 ? -1.0 : q;  // std::max(q, -1.0)
+    const double inc = __dmul_rn(__dmul_rn(static_cast<double>(change_param), static_cast<double>(dopa)), m);
+    return __double2float_rn(__dadd_rn(static_cast<double>(stability), inc));
+}
+
+// Resource-STDP neuron bookkeeping with no resource-STDP synapses (blifat_stdp.h:35-172). Returns
+// whether the dopamine change of stability is due; the caller applies it (dopamine_stability) once
+// the neuron's other state is stored, which keeps the rare FP64 path off the step's registers.
+__device__ __forceinline__ bool resource_step(
     const BlifatDev &p, uint32_t i, unsigned long long t, bool spike, bool forced, float dopa, float &add_thr)
 {
     const ResourceDev &r = p.res;
@@ -208,57 +294,18 @@ __device__ __forceinline__ void resource_step(
     const uint32_t isi_max = pu(r.isi_max, i);
     if (spike)
     {
-        // process_spiking_neurons_impl (blifat_stdp.h:43-67) + update_isi (training/stdp.h:88-126).
+        // process_spiking_neurons_impl (blifat_stdp.h:43-67) + update_isi.
         r.last_spike_step[i] = t;
-        if (forced)
-        {
-            status = 0;  // is_forced
-        }
-        else
-        {
-            const unsigned long long last = r.last_step[i];
-            switch (status)
-            {
-                case 3:  // not_in_period
-                case 0:  // is_forced
-                    status = 1;
-                    r.first_isi_spike[i] = t;
-                    break;
-                case 1:  // period_started
-                    if (last - t < isi_max) status = 2;
-                    break;
-                default:  // period_continued
-                    if (last - t >= isi_max || dopa != 0.0f)
-                    {
-                        status = 1;
-                        r.first_isi_spike[i] = t;
-                    }
-                    break;
-            }
-            r.last_step[i] = t;
-        }
+        unsigned long long last = r.last_step[i], first = r.first_isi_spike[i];
+        status = update_isi(status, forced, dopa, isi_max, t, last, first);
+        r.last_step[i] = last;
+        r.first_isi_spike[i] = first;
         if (status == 1) r.stability[i] = __fsub_rn(r.stability[i], pf(r.stability_change_at_isi, i));
         add_thr = __fmul_rn(0.0f, pf(r.add_thr_coef, i));
     }
-    // do_dopamine_plasticity_impl (blifat_stdp.h:106-155), no connected synapses.
-    if (dopa > 0.0f || (dopa < 0.0f && status != 0))
-    {
-        float st = r.stability[i];
-        const float c = pf(r.stability_change_param, i);
-        if (forced || dopa < 0.0f)
-        {
-            st = __fsub_rn(st, __fmul_rn(dopa, c));
-            st = fmaxf(st, 0.0f);
-        }
-        else
-        {
-            const unsigned long long diff_u = t - r.first_isi_spike[i] - isi_max;
-            const float diff = __ull2float_rn(diff_u);
-            const float m = fmaxf(__fsub_rn(2.0f, __fdiv_rn(diff, static_cast<float>(isi_max))), -1.0f);
-            st = __fadd_rn(st, __fmul_rn(__fmul_rn(c, dopa), m));
-        }
-        r.stability[i] = st;
-    }
+    // do_dopamine_plasticity_impl (blifat_stdp.h:106-155), no connected synapses: only stability
+    // changes, and the renormalisation below does not read it.
+    const bool dopamine = dopa > 0.0f || (dopa < 0.0f && status != 0);
     // renormalize_resource (training/stdp.h:152-186), no connected synapses.
     if (p.flags & kLiveRenorm)
     {
@@ -270,11 +317,30 @@ __device__ __forceinline__ void resource_step(
     }
     r.isi_status[i] = status;
     r.is_forced[i] = forced ? 1 : 0;
+    return dopamine;
+}
+
+// kResSyn populations: the training kernel (resource.cu) runs the whole neuron-side training after
+// the population step. Here the step's forcing flag is stored, and a neuron that did not spike is
+// listed for the training kernel when it has dopamine or renormalisation work (the spike list
+// holds the others); a neuron with neither is left unchanged by the training.
+__device__ __forceinline__ void resource_mark(const BlifatDev &p, uint32_t i, unsigned long long t, bool spike,
+                                              bool forced, float dopa)
+{
+    const ResourceDev &r = p.res;
+    r.is_forced[i] = forced ? 1 : 0;
+    if (spike) return;
+    const int32_t status = r.isi_status[i];
+    bool need = dopa > 0.0f || (dopa < 0.0f && status != 0);
+    if (!need)
+        need = !(t - r.last_step[i] <= pu(r.isi_max, i) && status != 0) &&
+               !(fabsf(r.free_resource[i]) < pf(r.resource_threshold, i));
+    if (need) p.syn.work[atomicAdd(p.syn.work_count, 1u)] = i;
 }
 
 // Steps neurons i0 .. i0 + 3 of a BLIFAT population (those below n) at step t and returns their spike
 // mask (bit k = neuron i0 + k fired).
-template <bool kFixed>
+template <bool kFixed, bool kRS = false>
 __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned long long t, uint32_t i0)
 {
     const uint32_t f = p.flags;
@@ -325,7 +391,14 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
             if (forced_bits) atomicAnd(wp, ~(0xFu << (i0 & 31)));
         }
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 V = (f & kLiveVRead) ? ld4(p.V, i0) : z;
+        float4 V = (kRS || (f & kLiveVRead)) ? ld4(p.V, i0) : z;
+        uint32_t nf_bits = 0;  // kRS: the four neurons' non-finite impact bytes
+        if (kRS && rg.nf)
+        {
+            uint32_t *wp = rg.nf + (ro >> 2);
+            nf_bits = *wp;
+            if (nf_bits) *wp = 0u;
+        }
         float4 thr_dyn = (f & kLiveThrDyn) ? ld4(p.thr_dyn, i0) : z;
         float4 trace = (f & kLiveTrace) ? ld4(p.trace, i0) : z;
         float4 g = (f & kLiveG) ? ld4(p.g, i0) : z;
@@ -335,6 +408,7 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
         uint4 phase = (f & kLiveBurst) ? ld4u(p.burst_phase, i0) : make_uint4(0, 0, 0, 0);
         float4 vpre;
         const uint4 ns_old = ns;
+        uint32_t dopamine_due = 0;  // neurons whose dopamine stability change follows the loop
 #pragma unroll
         for (int k = 0; k < 4; ++k)
         {
@@ -350,6 +424,7 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
             s.ns = at(ns, k);
             s.phase = at(phase, k);
             s.block = (f & kLiveBlock) ? p.blocking[i] : 0;
+            s.add64 = kRS ? p.syn.add_thr[i] : 0.0;
             if ((f & kLiveBlock) && rg.blk)
             {
                 // The step's last BLOCKING impact sets the period (impact phase, blifat_impl.h:86).
@@ -363,10 +438,13 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
                                   : static_cast<long long>(rg.blk_w[order - 1][key & kBlkPosMask]);
                 }
             }
-            const bool spike = blifat_step<kFixed>(p, i, t, s, at(acc, k), acc_hi[k], acc_lo[k], at(gin, k), at(din, k));
+            const bool spike = blifat_step<kFixed, kRS>(p, i, t, s, at(acc, k), acc_hi[k], acc_lo[k], at(gin, k), at(din, k),
+                                                        (nf_bits >> (8 * k)) & 0xFFu);
             if (spike) mask |= 1u << k;
-            if (f & kResource)
-                resource_step(p, i, t, spike, (forced_bits >> k) & 1u, s.dopa, s.add_thr);
+            if (kRS)
+                resource_mark(p, i, t, spike, (forced_bits >> k) & 1u, s.dopa);
+            else if ((f & kResource) && resource_step(p, i, t, spike, (forced_bits >> k) & 1u, s.dopa, s.add_thr))
+                dopamine_due |= 1u << k;
             at(V, k) = s.V;
             at(vpre, k) = s.V_pre;
             at(thr_dyn, k) = s.thr_dyn;
@@ -397,6 +475,13 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
         }
         (void)ns_old;
         if (f & kLiveBurst) st4u(p.burst_phase, i0, phase);
+        for (; dopamine_due; dopamine_due &= dopamine_due - 1)
+        {
+            const uint32_t k = __ffs(dopamine_due) - 1, i = i0 + k;
+            const ResourceDev &r = p.res;
+            r.stability[i] = dopamine_stability(r.stability[i], at(dopa, k), pf(r.stability_change_param, i),
+                                                (forced_bits >> k) & 1u, t, r.first_isi_spike[i], pu(r.isi_max, i));
+        }
     }
     return mask;
 }

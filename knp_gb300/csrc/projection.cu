@@ -78,6 +78,24 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
         }
     }
     events = scatter_rows<kFixed, kUniformExc>(p, slot_base, idx, cnt, total, warp, n_warps, lane);
+    if (p.last_spike)
+    {
+        // Resource-STDP synapses: init_synapse (synaptic_resource_stdp.h:36-41, called per synapse of
+        // a spiking row in delta_impl.h:75) records the step of the presynaptic spike.
+        for (uint32_t j = warp; j < total; j += n_warps)
+        {
+            uint32_t jj = j;
+            int k = 0;
+            while (jj >= cnt[k])
+            {
+                jj -= cnt[k];
+                ++k;
+            }
+            const uint32_t pre = idx[k][jj];
+            if (pre >= p.n_rows) continue;
+            for (int64_t e = p.row_ptr[pre] + lane; e < p.row_ptr[pre + 1]; e += 32) p.last_spike[e] = t;
+        }
+    }
     if (lane == 0 && events) atomicAdd(&block_events, events);
     __syncthreads();
     if (threadIdx.x == 0 && block_events) atomicAdd(&ctl->events_total, block_events);

@@ -55,6 +55,12 @@ __device__ __forceinline__ void deliver(
     if (kUniformExc || ty == 0 || ty == 1)
     {
         if (!kUniformExc && ty == 1) w = -w;
+        if (kFixed && p.ring.nf && !isfinite(w))
+        {
+            const uint32_t bit = isnan(w) ? 1u : (w > 0.0f ? 2u : 4u);
+            atomicOr(p.ring.nf + (o >> 2), bit << (8 * (o & 3)));
+            return;
+        }
         if (kFixed)
             fx_atomic_add(p.ring.v64, p.ring.v64lo, o, w);
         else
