@@ -161,6 +161,35 @@ void resource_from_c(const knp_resource_stdp_state &c, ResourceParams &n)
     n.first_isi_spike_ = c.first_isi_spike;
 }
 
+// The rule state of one SynapticResourceSTDPDeltaSynapse (stdp_synaptic_resource_rule.h:45-89).
+template <class Rule>
+knp_resource_synapse rule_to_c(const Rule &r)
+{
+    knp_resource_synapse c{};
+    c.synaptic_resource = r.synaptic_resource_;
+    c.w_min = r.w_min_;
+    c.w_max = r.w_max_;
+    c.d_u = r.d_u_;
+    c.dopamine_plasticity_period = r.dopamine_plasticity_period_;
+    c.had_hebbian_update = r.had_hebbian_update_ ? 1u : 0u;
+    c.last_spike_step = r.last_spike_step_;
+    c.has_contributed = r.has_contributed_ ? 1u : 0u;
+    return c;
+}
+
+template <class Rule>
+void rule_from_c(const knp_resource_synapse &c, Rule &r)
+{
+    r.synaptic_resource_ = c.synaptic_resource;
+    r.w_min_ = c.w_min;
+    r.w_max_ = c.w_max;
+    r.d_u_ = c.d_u;
+    r.dopamine_plasticity_period_ = c.dopamine_plasticity_period;
+    r.had_hebbian_update_ = c.had_hebbian_update != 0u;
+    r.last_spike_step_ = c.last_spike_step;
+    r.has_contributed_ = c.has_contributed != 0u;
+}
+
 knp_lif_neuron lif_to_c(const nt::neuron_parameters<nt::LIFNeuron> &n)
 {
     knp_lif_neuron c{};
@@ -244,7 +273,7 @@ std::vector<std::string> GB300Backend::get_supported_neurons() const
 
 std::vector<std::string> GB300Backend::get_supported_synapses() const
 {
-    return {"DeltaSynapse", "AdditiveSTDPDeltaSynapse"};
+    return {"DeltaSynapse", "AdditiveSTDPDeltaSynapse", "SynapticResourceSTDPDeltaSynapse"};
 }
 
 std::vector<size_t> GB300Backend::get_supported_population_indexes() const
@@ -254,7 +283,7 @@ std::vector<size_t> GB300Backend::get_supported_population_indexes() const
 
 std::vector<size_t> GB300Backend::get_supported_projection_indexes() const
 {
-    return indexes_in<knp::core::AllProjectionsVariant, DeltaProjection, AdditiveSTDPProjection>();
+    return indexes_in<knp::core::AllProjectionsVariant, DeltaProjection, AdditiveSTDPProjection, ResourceSTDPProjection>();
 }
 
 void GB300Backend::load_all_populations(const std::vector<knp::core::AllPopulationsVariant> &populations)
@@ -305,9 +334,19 @@ void GB300Backend::load_projections(const std::vector<ProjectionVariants> &proje
 
 std::vector<std::unique_ptr<knp::core::Device>> GB300Backend::get_devices() const { return {}; }
 
-void GB300Backend::stop_learning() { check(knp_gb300_stop_learning(handle()), "knp_gb300_stop_learning"); }
+void GB300Backend::stop_learning()
+{
+    check(knp_gb300_stop_learning(handle()), "knp_gb300_stop_learning");
+    learning_known_ = true;
+    learning_ = false;
+}
 
-void GB300Backend::start_learning() { check(knp_gb300_start_learning(handle()), "knp_gb300_start_learning"); }
+void GB300Backend::start_learning()
+{
+    check(knp_gb300_start_learning(handle()), "knp_gb300_start_learning");
+    learning_known_ = true;
+    learning_ = true;
+}
 
 void GB300Backend::_init()
 {
@@ -356,6 +395,7 @@ void GB300Backend::_init()
                 std::vector<uint32_t> pre(n), post(n), delay(n);
                 std::vector<float> w(n), tp, tm;
                 std::vector<uint8_t> type(n);
+                std::vector<knp_resource_synapse> rule;
                 for (size_t i = 0; i < n; ++i)
                 {
                     const auto &s = proj[i];
@@ -370,14 +410,26 @@ void GB300Backend::_init()
                         tp.push_back(p.rule_.tau_plus_);
                         tm.push_back(p.rule_.tau_minus_);
                     }
+                    if constexpr (std::is_same_v<T, ResourceSTDPProjection>) rule.push_back(rule_to_c(p.rule_));
                 }
+                const knp_uid uid = to_c(proj.get_uid());
+                if constexpr (std::is_same_v<T, ResourceSTDPProjection>)
+                {
+                    check(knp_gb300_load_resource_stdp_projection(h_, uid, to_c(proj.get_presynaptic()),
+                                                                  to_c(proj.get_postsynaptic()), n, pre.data(), post.data(),
+                                                                  w.data(), delay.data(), type.data(), rule.data(),
+                                                                  proj.is_locked() ? 1 : 0),
+                          "knp_gb300_load_resource_stdp_projection");
+                }
+                else
+                {
                 constexpr int kind =
                     std::is_same_v<T, AdditiveSTDPProjection> ? KNP_SYNAPSE_ADDITIVE_STDP_DELTA : KNP_SYNAPSE_DELTA;
-                const knp_uid uid = to_c(proj.get_uid());
                 check(knp_gb300_load_projection(h_, uid, kind, to_c(proj.get_presynaptic()), to_c(proj.get_postsynaptic()), n,
                                                 pre.data(), post.data(), w.data(), delay.data(), type.data(),
                                                 tp.empty() ? nullptr : tp.data(), tm.empty() ? nullptr : tm.data()),
                       "knp_gb300_load_projection");
+                }
                 if constexpr (std::is_same_v<T, AdditiveSTDPProjection>)
                 {
                     using Processing = typename T::SharedSynapseParameters::ProcessingType;
@@ -495,12 +547,28 @@ knp::core::Backend::DataRanges GB300Backend::get_network_data() const
         std::visit(
             [this, &projs](const auto &proj)
             {
+                using T = std::decay_t<decltype(proj)>;
                 auto copy = proj;
                 if (initialized_ && proj.size())
                 {
                     std::vector<float> w(proj.size());
                     check(knp_gb300_read_weights(h_, to_c(proj.get_uid()), w.data()), "knp_gb300_read_weights");
                     for (size_t i = 0; i < w.size(); ++i) std::get<knp::core::synapse_data>(copy[i]).weight_ = w[i];
+                    if constexpr (std::is_same_v<T, ResourceSTDPProjection>)
+                    {
+                        std::vector<knp_resource_synapse> r(proj.size());
+                        check(knp_gb300_read_resource_synapses(h_, to_c(proj.get_uid()), r.data()),
+                              "knp_gb300_read_resource_synapses");
+                        for (size_t i = 0; i < r.size(); ++i) rule_from_c(r[i], std::get<knp::core::synapse_data>(copy[i]).rule_);
+                    }
+                }
+                // start_learning / stop_learning lock or unlock every projection.
+                if (learning_known_)
+                {
+                    if (learning_)
+                        copy.unlock_weights();
+                    else
+                        copy.lock_weights();
                 }
                 projs.emplace_back(std::move(copy));
             },

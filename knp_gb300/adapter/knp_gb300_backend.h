@@ -11,7 +11,8 @@
  * export line is the only Boost-dependent line and is compiled only where Boost is available.
  *
  * It keeps the single-threaded backend's behaviour: the same supported neuron and synapse types
- * (BLIFAT, synaptic-resource-STDP BLIFAT, LIF; delta and additive-STDP delta), the same message
+ * (BLIFAT, synaptic-resource-STDP BLIFAT, LIF; delta, additive-STDP delta and synaptic-resource-STDP
+ * delta), the same message
  * semantics on the backend's bus (SpikeMessages sent to a projection's UID reach that projection
  * at the next step; SynapticImpactMessages sent to a population's UID are applied at the next
  * step; each population that spiked sends its SpikeMessage {population UID, step, ascending
@@ -48,9 +49,10 @@ public:
     using LIFPopulation = knp::core::Population<knp::neuron_traits::LIFNeuron>;
     using DeltaProjection = knp::core::Projection<knp::synapse_traits::DeltaSynapse>;
     using AdditiveSTDPProjection = knp::core::Projection<knp::synapse_traits::AdditiveSTDPDeltaSynapse>;
+    using ResourceSTDPProjection = knp::core::Projection<knp::synapse_traits::SynapticResourceSTDPDeltaSynapse>;
     /** The population and projection types this backend runs (the single-threaded backend's set). */
     using PopulationVariants = std::variant<BLIFATPopulation, ResourceBLIFATPopulation, LIFPopulation>;
-    using ProjectionVariants = std::variant<DeltaProjection, AdditiveSTDPProjection>;
+    using ProjectionVariants = std::variant<DeltaProjection, AdditiveSTDPProjection, ResourceSTDPProjection>;
 
     /** A backend on CUDA device `device`; the device backend (knp_gb300_create) is created at first
      * use (init, or a learning switch), so constructing and loading need no GPU. */
@@ -80,7 +82,8 @@ public:
     void start_learning() override;
 
     /** Copies of the loaded populations and projections with their current state read back from the
-     * GPU (neuron state; projection weights in the loaded synapse order). The additive-STDP spike
+     * GPU (neuron state; projection weights in the loaded synapse order; the rule state of
+     * synaptic-resource-STDP synapses; the lock flag of every projection). The additive-STDP spike
      * time lists of a synapse keep their loaded contents: the GPU keeps one history per
      * postsynaptic neuron, not per synapse. */
     [[nodiscard]] DataRanges get_network_data() const override;
@@ -104,6 +107,8 @@ private:
     std::vector<PopulationVariants> populations_;
     std::vector<ProjectionVariants> projections_;
     bool initialized_ = false;
+    // The last start_learning / stop_learning: every projection's lock flag follows it.
+    bool learning_known_ = false, learning_ = false;
     // External messages reach the C ABI through one input channel per projection (spikes) and one
     // per population (impacts), subscribed at _init.
     std::unordered_map<knp::core::UID, knp::core::UID, knp::core::uid_hash> spike_channel_, impact_channel_;

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include <knp/core/core.h>
+#include <knp/neuron-traits/altai_lif.h>
 #include <knp/neuron-traits/blifat.h>
 #include <knp/neuron-traits/lif.h>
 #include <knp/neuron-traits/stdp_type_traits.h>
@@ -54,5 +55,6 @@ private:
 
 using AllPopulationsVariant = std::variant<
     Population<neuron_traits::BLIFATNeuron>, Population<neuron_traits::SynapticResourceSTDPBLIFATNeuron>,
+    Population<neuron_traits::AltAILIF>, Population<neuron_traits::SynapticResourceSTDPAltAILIFNeuron>,
     Population<neuron_traits::LIFNeuron>>;
 }  // namespace knp::core

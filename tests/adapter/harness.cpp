@@ -9,7 +9,12 @@
 // get_network_data. Prints "steps: ..." (steps with output), "weights: ..." (loop and input weights
 // after 20 steps, from get_network_data) and "ok".
 //
-// Usage: harness delta|stdp|resource|impacts
+// The resource_stdp case is single_thread_cpu_test.cpp:179-264: SynapticResourceSTDPDeltaSynapse input
+// (rule {0, 1, 2, 0.1}) and loop (rule {0, 1, 2}, delay 6) projections onto one resource-STDP BLIFAT
+// neuron (synaptic resource threshold 1, free resource 2, isi_max 0), start_learning after _init;
+// it also prints the loop synapse's rule state from get_network_data ("rule: ...").
+//
+// Usage: harness delta|stdp|resource|resource_stdp|impacts|unsupported
 #include <cstdio>
 #include <cstring>
 #include <optional>
@@ -23,6 +28,18 @@ using knp::core::UID;
 using knp::core::messaging::SpikeMessage;
 namespace nt = knp::neuron_traits;
 namespace st = knp::synapse_traits;
+
+// Inside lambdas (which cannot return the harness's status): record the failure.
+static bool failed = false;
+#define EXPECT_VOID(c)                                                            \
+    do                                                                            \
+    {                                                                             \
+        if (!(c))                                                                 \
+        {                                                                         \
+            std::fprintf(stderr, "check failed: %s (line %d)\n", #c, __LINE__); \
+            failed = true;                                                        \
+        }                                                                         \
+    } while (0)
 
 #define EXPECT(c)                                                  \
     do                                                             \
@@ -60,11 +77,27 @@ int run_golden(const std::string &kind)
     EXPECT(backend.plasticity_supported());
     EXPECT(backend.get_supported_neurons().size() == 3);
     EXPECT(backend.get_supported_population_indexes().size() == 3);
-    EXPECT(backend.get_supported_projection_indexes().size() == 2);
+    EXPECT(backend.get_supported_projection_indexes().size() == 3);
+    EXPECT(backend.get_supported_synapses().size() == 3);
 
     std::vector<knp::core::AllPopulationsVariant> pops;
     UID pop_uid;
-    if (kind == "resource")
+    if (kind == "resource_stdp")
+    {
+        GB300Backend::ResourceBLIFATPopulation pop(
+            [](size_t)
+            {
+                nt::neuron_parameters<nt::SynapticResourceSTDPBLIFATNeuron> n{};
+                n.synaptic_resource_threshold_ = 1;
+                n.free_synaptic_resource_ = 2;
+                n.isi_max_ = 0;
+                return std::make_optional(n);
+            },
+            1);
+        pop_uid = pop.get_uid();
+        pops.emplace_back(pop);
+    }
+    else if (kind == "resource")
     {
         GB300Backend::ResourceBLIFATPopulation pop(
             [](size_t) { return std::make_optional(nt::neuron_parameters<nt::SynapticResourceSTDPBLIFATNeuron>{}); }, 1);
@@ -89,6 +122,33 @@ int run_golden(const std::string &kind)
         projs.emplace_back(input);
         projs.emplace_back(loop);
     }
+    else if (kind == "resource_stdp")
+    {
+        using RP = GB300Backend::ResourceSTDPProjection;
+        auto make = [](const UID &pre, const UID &post, uint32_t d, float d_u)
+        {
+            return RP(pre, post,
+                      [d, d_u](size_t) -> std::optional<RP::Synapse>
+                      {
+                          RP::SynapseParameters p{};
+                          p.weight_ = 1.0f;
+                          p.delay_ = d;
+                          p.output_type_ = st::OutputType::EXCITATORY;
+                          p.rule_.synaptic_resource_ = 0;
+                          p.rule_.w_min_ = 1;
+                          p.rule_.w_max_ = 2;
+                          p.rule_.d_u_ = d_u;
+                          return RP::Synapse{p, 0, 0};
+                      },
+                      1);
+        };
+        auto input = make(UID{false}, pop_uid, 1, 0.1f);
+        auto loop = make(pop_uid, pop_uid, 6, 0.0f);
+        input_uid = input.get_uid();
+        loop_uid = loop.get_uid();
+        projs.emplace_back(input);
+        projs.emplace_back(loop);
+    }
     else
     {
         auto input = one_synapse<GB300Backend::AdditiveSTDPProjection>(UID{false}, pop_uid, 1.0f, 1, 2);
@@ -103,6 +163,7 @@ int run_golden(const std::string &kind)
     backend.load_all_populations(pops);
     backend.load_all_projections(projs);
     backend._init();
+    if (kind == "resource_stdp") backend.start_learning();
     auto endpoint = backend.get_message_bus().create_endpoint();
     const UID in_channel_uid, out_channel_uid;
     backend.subscribe<SpikeMessage>(input_uid, {in_channel_uid});
@@ -132,8 +193,26 @@ int run_golden(const std::string &kind)
     for (auto &it = *data.projection_range.first; it != *data.projection_range.second; ++it)
     {
         ++n_proj;
-        std::visit([&weights](const auto &p) { weights.push_back(std::get<knp::core::synapse_data>(p[0]).weight_); }, *it);
+        std::visit(
+            [&](const auto &p)
+            {
+                using T = std::decay_t<decltype(p)>;
+                weights.push_back(std::get<knp::core::synapse_data>(p[0]).weight_);
+                if constexpr (std::is_same_v<T, GB300Backend::ResourceSTDPProjection>)
+                {
+                    EXPECT_VOID(!p.is_locked());
+                    if (p.get_uid() == loop_uid)
+                    {
+                        const auto &r = std::get<knp::core::synapse_data>(p[0]).rule_;
+                        std::printf("rule: %.9g %llu %d %d\n", r.synaptic_resource_,
+                                    static_cast<unsigned long long>(r.last_spike_step_), r.had_hebbian_update_ ? 1 : 0,
+                                    r.has_contributed_ ? 1 : 0);
+                    }
+                }
+            },
+            *it);
     }
+    EXPECT(!failed);
     for (auto &it = *data.population_range.first; it != *data.population_range.second; ++it)
     {
         ++n_pop;
@@ -183,11 +262,11 @@ int main(int argc, char **argv)
         {
             // A type the backend does not take is refused as load_from_container refuses it.
             GB300Backend backend;
-            knp::core::Projection<st::SynapticResourceSTDPDeltaSynapse> p(
-                UID{false}, UID{false}, [](size_t) { return std::nullopt; }, 0);
+            knp::core::Population<nt::AltAILIF> p(
+                [](size_t) { return std::make_optional(nt::neuron_parameters<nt::AltAILIF>{}); }, 1);
             try
             {
-                backend.load_all_projections({p});
+                backend.load_all_populations({p});
             }
             catch (const std::runtime_error &e)
             {

@@ -27,7 +27,8 @@ def _parse(out):
     return steps, weights
 
 
-@pytest.mark.parametrize("case,kind", [("delta", "delta"), ("stdp", "stdp"), ("resource", "stdp_resource_neuron")])
+@pytest.mark.parametrize("case,kind", [("delta", "delta"), ("stdp", "stdp"), ("resource", "stdp_resource_neuron"),
+                                       ("resource_stdp", "resource_stdp")])
 def test_adapter_golden_network_through_the_bus(harness, case, kind):
     from oracle import oracle as orc
 
