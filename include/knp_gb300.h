@@ -104,6 +104,28 @@ KNP_GB300_API int knp_gb300_load_lif_population(knp_gb300_backend *b, knp_uid ui
 KNP_GB300_API int knp_gb300_read_lif_population(knp_gb300_backend *b, knp_uid pop, knp_lif_neuron *out);
 
 /**
+ * Load an AltAI-LIF population: kind KNP_NEURON_ALTAI_LIF, or KNP_NEURON_RESOURCE_STDP_ALTAI_LIF with
+ * `ext` (the resource-STDP extension, trained like the BLIFAT variant: altai/altai_stdp.h). Semantics
+ * of altai/altai_impl.h:33-168: the potential is rounded (or reset when do_not_save) before the
+ * impacts, leak with optional sign reversal, activity time counted towards INT64_MAX, threshold
+ * crossing with difference or reset, negative threshold with saturation. Impacts of a step are summed
+ * exactly and rounded once, which is the reference's impact-by-impact FP32 sum whenever its partial
+ * sums are exact (integer or dyadic weights); BLOCKING impacts are applied in the reference's message
+ * order (at most 2048 per population and step, else KNP_GB300_E_DEVICE_FLAG). INHIBITORY_CONDUCTANCE
+ * impacts are refused, as the reference throws on them. Populations of these kinds run the per-phase
+ * step. Replaces: load_populations for Population<AltAILIF> and
+ * Population<SynapticResourceSTDPAltAILIFNeuron> (cpu-single-threaded-backend/impl/backend.cpp:144-186).
+ */
+KNP_GB300_API int knp_gb300_load_altai_population(
+    knp_gb300_backend *b, knp_uid uid, int kind, uint32_t n, const knp_altai_neuron *neurons,
+    const knp_resource_stdp_state *ext);
+
+/** Read back an AltAI-LIF population's neurons (and their resource-STDP extension when `ext` is not
+ * NULL). Replaces: get_network_data population range for the AltAI-LIF kinds. */
+KNP_GB300_API int knp_gb300_read_altai_population(
+    knp_gb300_backend *b, knp_uid pop, knp_altai_neuron *out, knp_resource_stdp_state *ext);
+
+/**
  * Load a projection of `n_syn` synapses given in the reference's synapse order: synapse i is
  * (weight[i], delay[i], out_type[i]) from presynaptic neuron pre[i] to postsynaptic neuron post[i].
  * kind: KNP_SYNAPSE_DELTA or KNP_SYNAPSE_ADDITIVE_STDP_DELTA (tau_plus/tau_minus required, uniform

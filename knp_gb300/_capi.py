@@ -71,6 +71,8 @@ def lib():
         "knp_gb300_discard_spikes": ([p, u64], c_int),
         "knp_gb300_read_blifat_population": ([p, U, p, p], c_int),
         "knp_gb300_read_weights": ([p, U, p], c_int),
+        "knp_gb300_load_altai_population": ([p, U, c_int, ctypes.c_uint32, p, p], c_int),
+        "knp_gb300_read_altai_population": ([p, U, p, p], c_int),
         "knp_gb300_load_resource_stdp_projection": ([p, U, U, U, u64, p, p, p, p, p, p, c_int], c_int),
         "knp_gb300_read_resource_synapses": ([p, U, p], c_int),
         "knp_gb300_projection_size": ([p, U, ctypes.POINTER(u64)], c_int),

@@ -87,6 +87,13 @@ class GB300Backend:
                                                                   _ptr(neurons)))
                 self._pops[pop.uid] = pop
                 continue
+            if T.is_altai(pop.kind):
+                neurons = np.ascontiguousarray(pop.neurons, dtype=T.ALTAI_DTYPE)
+                res = None if pop.resource is None else np.ascontiguousarray(pop.resource, dtype=T.RESOURCE_DTYPE)
+                self._chk(self._lib.knp_gb300_load_altai_population(
+                    self._h, T.to_c_uid(pop.uid), pop.kind, pop.size, _ptr(neurons), _ptr(res)))
+                self._pops[pop.uid] = pop
+                continue
             if pop.kind not in (T.BLIFAT, T.RESOURCE_STDP_BLIFAT):
                 raise TypeError("Type is not supported.")
             neurons = np.ascontiguousarray(pop.neurons, dtype=T.BLIFAT_DTYPE)
@@ -297,7 +304,13 @@ class GB300Backend:
 
     # ------------------------------------------------------------------ readback (backend.h:420)
     def read_population(self, uid: bytes):
+        """(neurons, resource-STDP extension or None) of a BLIFAT or AltAI-LIF population."""
         pop = self._pops[uid]
+        if T.is_altai(pop.kind):
+            out = np.empty(pop.size, T.ALTAI_DTYPE)
+            ext = np.empty(pop.size, T.RESOURCE_DTYPE) if pop.kind == T.RESOURCE_STDP_ALTAI_LIF else None
+            self._chk(self._lib.knp_gb300_read_altai_population(self._h, T.to_c_uid(uid), _ptr(out), _ptr(ext)))
+            return out, ext
         out = np.empty(pop.size, T.BLIFAT_DTYPE)
         ext = np.empty(pop.size, T.RESOURCE_DTYPE) if pop.kind == T.RESOURCE_STDP_BLIFAT else None
         self._chk(self._lib.knp_gb300_read_blifat_population(self._h, T.to_c_uid(uid), _ptr(out), _ptr(ext)))

@@ -132,6 +132,20 @@ int knp_gb300_read_lif_population(knp_gb300_backend *b, knp_uid pop, knp_lif_neu
     return guarded([&] { b->impl.read_lif(U(pop), out); });
 }
 
+int knp_gb300_load_altai_population(
+    knp_gb300_backend *b, knp_uid uid, int kind, uint32_t n, const knp_altai_neuron *neurons,
+    const knp_resource_stdp_state *ext)
+{
+    if (!b) return null_handle();
+    return guarded([&] { b->impl.load_altai(U(uid), kind, n, neurons, ext); });
+}
+
+int knp_gb300_read_altai_population(knp_gb300_backend *b, knp_uid pop, knp_altai_neuron *out, knp_resource_stdp_state *ext)
+{
+    if (!b || !out) return null_handle();
+    return guarded([&] { b->impl.read_altai(U(pop), out, ext); });
+}
+
 int knp_gb300_load_projection(
     knp_gb300_backend *b, knp_uid uid, int kind, knp_uid pre_uid, knp_uid post_uid, uint64_t n_syn, const uint32_t *pre,
     const uint32_t *post, const float *weight, const uint32_t *delay, const uint8_t *out_type, const float *tau_plus,

@@ -192,6 +192,26 @@ void Backend::load_blifat(
     pops_.push_back(std::move(p));
 }
 
+void Backend::load_altai(
+    const Uid &uid, int kind, uint32_t n, const knp_altai_neuron *neurons, const knp_resource_stdp_state *ext)
+{
+    require_not_init("load_altai_population");
+    if (kind != KNP_NEURON_ALTAI_LIF && kind != KNP_NEURON_RESOURCE_STDP_ALTAI_LIF)
+        throw Error(KNP_GB300_E_INVALID, "unsupported neuron kind " + std::to_string(kind));
+    if (kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF && !ext)
+        throw Error(KNP_GB300_E_INVALID, "a resource-STDP population needs its knp_resource_stdp_state array");
+    if (!neurons && n) throw Error(KNP_GB300_E_INVALID, "null neuron array");
+    if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    auto p = std::make_unique<PopulationSlot>();
+    p->uid = uid;
+    p->kind = kind;
+    p->n = n;
+    p->n_pad = round_up(std::max<uint32_t>(n, 1), 4);
+    p->init_altai.assign(neurons, neurons + n);
+    if (kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF) p->init_res.assign(ext, ext + n);
+    pops_.push_back(std::move(p));
+}
+
 void Backend::load_lif(const Uid &uid, uint32_t n, const knp_lif_neuron *neurons)
 {
     require_not_init("load_lif_population");
@@ -352,13 +372,14 @@ void Backend::record_spikes(const Uid &pop, bool enable)
         if (enable && !p->rec_bits)
         {
             alloc_recording(*p);
-            p->bdev.rec_words = p->ldev.rec_words = p->rec_words;
-            p->bdev.rec_slots = p->ldev.rec_slots = p->rec_slots;
+            p->bdev.rec_words = p->ldev.rec_words = p->adev.rec_words = p->rec_words;
+            p->bdev.rec_slots = p->ldev.rec_slots = p->adev.rec_slots = p->rec_slots;
         }
         p->record = enable;
         p->record_from = step_;
         p->bdev.rec_bits = enable ? p->rec_bits : nullptr;
         p->ldev.rec_bits = enable ? p->rec_bits : nullptr;
+        p->adev.rec_bits = enable ? p->rec_bits : nullptr;
         capture_graphs();
         return;
     }
@@ -435,8 +456,28 @@ void Backend::build_population(PopulationSlot &p)
     }
     else
         rg.v32 = arena_.make<float>(cells);
-    const bool res = p.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT;
-    if (p.kind != KNP_NEURON_LIF)
+    const bool res = p.kind == KNP_NEURON_RESOURCE_STDP_BLIFAT || p.kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF;
+    if (p.is_altai())
+    {
+        if (d_in) rg.dopa = arena_.make<float>(cells);
+        if (blk_in || p.has_external_impacts)
+        {
+            // Every BLOCKING impact of a step, kept as an ordered event.
+            rg.bev_cap = 2048;
+            const size_t ev = static_cast<size_t>(slots) * rg.bev_cap;
+            rg.bev_key = arena_.make<unsigned long long>(ev, false);
+            rg.bev_val = arena_.make<float>(ev, false);
+            rg.bev_tgt = arena_.make<uint32_t>(ev, false);
+            rg.bev_count = arena_.make<uint32_t>(slots);
+        }
+        if (fixed) rg.nf = arena_.make<uint32_t>(cells / 4);
+        if (res && forcing_exc)
+        {
+            rg.words = (np + 31) / 32;
+            rg.forced = arena_.make<uint32_t>(static_cast<size_t>(slots) * rg.words);
+        }
+    }
+    else if (p.kind != KNP_NEURON_LIF)
     {
         if (g_in) rg.g = arena_.make<float>(cells);
         if (d_in) rg.dopa = arena_.make<float>(cells);
@@ -466,6 +507,98 @@ void Backend::build_population(PopulationSlot &p)
     {
         alloc_recording(p);
         p.record_from = 0;
+    }
+
+    if (p.is_altai())
+    {
+        AltaiDev &d = p.adev;
+        const auto &nn = p.init_altai;
+        d.n = n;
+        d.n_pad = np;
+        d.flags = (res ? kResource : 0u) | (rg.dopa ? kLiveDopa : 0u);
+        auto upload = [&](auto get, auto *dst)
+        {
+            using V = std::remove_pointer_t<decltype(dst)>;
+            std::vector<V> a(np, V{});
+            for (uint32_t i = 0; i < n; ++i) a[i] = get(i);
+            V *dp = arena_.make<V>(np);
+            KNP_CUDA(cudaMemcpy(dp, a.data(), np * sizeof(V), cudaMemcpyHostToDevice));
+            return dp;
+        };
+        auto param_u = [&](auto get) -> ParamU
+        {
+            ParamU r{nullptr, n ? static_cast<uint32_t>(get(0)) : 0u};
+            bool uni = true;
+            for (uint32_t i = 1; i < n && uni; ++i) uni = static_cast<uint32_t>(get(i)) == r.u;
+            if (!uni) r.a = upload([&](uint32_t i) { return static_cast<uint32_t>(get(i)); }, static_cast<uint32_t *>(nullptr));
+            return r;
+        };
+        d.V = upload([&](uint32_t i) { return nn[i].potential; }, static_cast<float *>(nullptr));
+        d.V_pre = upload([&](uint32_t i) { return nn[i].pre_impact_potential; }, static_cast<float *>(nullptr));
+        d.activity = upload([&](uint32_t i) { return static_cast<long long>(nn[i].activity_time); },
+                            static_cast<long long *>(nullptr));
+        d.add_thr = upload([&](uint32_t i) { return nn[i].additional_threshold; }, static_cast<double *>(nullptr));
+        d.dopa = (rg.dopa || res)
+                     ? upload([&](uint32_t i) { return static_cast<float>(nn[i].dopamine_value); }, static_cast<float *>(nullptr))
+                     : nullptr;
+        d.cfg = param_u(
+            [&](uint32_t i)
+            {
+                const knp_altai_neuron &x = nn[i];
+                return (x.is_diff ? kAltaiDiff : 0u) | (x.is_reset ? kAltaiReset : 0u) | (x.leak_rev ? kAltaiLeakRev : 0u) |
+                       (x.saturate ? kAltaiSaturate : 0u) | (x.do_not_save ? kAltaiNoSave : 0u);
+            });
+        d.thr = param_u([&](uint32_t i) { return nn[i].activation_threshold; });
+        d.neg_thr = param_u([&](uint32_t i) { return nn[i].negative_activation_threshold; });
+        d.reset = param_u([&](uint32_t i) { return nn[i].potential_reset_value; });
+        d.leak = param_u([&](uint32_t i) { return static_cast<uint32_t>(static_cast<int32_t>(nn[i].potential_leak)); });
+        if (res)
+        {
+            ResourceDev &r = d.res;
+            const auto &rr = p.init_res;
+            using R = knp_resource_stdp_state;
+            auto up64 = [&](auto get)
+            { return upload([&](uint32_t i) { return static_cast<unsigned long long>(get(rr[i])); },
+                            static_cast<unsigned long long *>(nullptr)); };
+            auto rpf = [&](auto get) -> ParamF
+            {
+                ParamF x{nullptr, n ? get(rr[0]) : 0.f};
+                bool uni = true;
+                for (uint32_t i = 1; i < n && uni; ++i) uni = get(rr[i]) == x.u;
+                if (!uni) x.a = upload([&](uint32_t i) { return get(rr[i]); }, static_cast<float *>(nullptr));
+                return x;
+            };
+            auto rpu = [&](auto get) -> ParamU { return param_u([&](uint32_t i) { return get(rr[i]); }); };
+            r.isi_status = reinterpret_cast<int32_t *>(
+                upload([&](uint32_t i) { return static_cast<uint32_t>(rr[i].isi_status); }, static_cast<uint32_t *>(nullptr)));
+            r.last_step = up64([](const R &x) { return x.last_step; });
+            r.last_spike_step = up64([](const R &x) { return x.last_spike_step; });
+            r.first_isi_spike = up64([](const R &x) { return x.first_isi_spike; });
+            r.stability = upload([&](uint32_t i) { return rr[i].stability; }, static_cast<float *>(nullptr));
+            r.free_resource = upload([&](uint32_t i) { return rr[i].free_synaptic_resource; }, static_cast<float *>(nullptr));
+            r.is_forced = upload([&](uint32_t i) { return static_cast<uint8_t>(rr[i].is_being_forced ? 1 : 0); },
+                                 static_cast<uint8_t *>(nullptr));
+            r.add_thr_coef = rpf([](const R &x) { return x.synapse_sum_threshold_coefficient; });
+            r.resource_threshold = rpf([](const R &x) { return x.synaptic_resource_threshold; });
+            r.stability_change_param = rpf([](const R &x) { return x.stability_change_parameter; });
+            r.stability_change_at_isi = rpf([](const R &x) { return x.stability_change_at_isi; });
+            r.d_h = rpf([](const R &x) { return x.d_h; });
+            r.isi_max = rpu([](const R &x) { return x.isi_max; });
+            r.dopamine_time = rpu([](const R &x) { return x.dopamine_plasticity_time; });
+            r.drain = rpu([](const R &x) { return x.resource_drain_coefficient; });
+            // Training kernel's work list and FP64 additional threshold (shared with the neuron state);
+            // the synapse arrays follow in build_resource_synapses.
+            d.syn.add_thr = d.add_thr;
+            d.syn.work = arena_.make<uint32_t>(np);
+            d.syn.work_count = counters_ + p.work_counter_index;
+        }
+        d.spikes = spikes;
+        d.spike_count = count;
+        d.rec_bits = p.record ? p.rec_bits : nullptr;
+        d.rec_words = p.rec_words;
+        d.rec_slots = p.rec_slots;
+        d.ring = rg;
+        return;
     }
 
     if (p.kind == KNP_NEURON_LIF)
@@ -804,7 +937,7 @@ void Backend::build_projection(ProjectionSlot &p)
         SpikeSource src{};
         if (PopulationSlot *q = find_pop(s))
         {
-            src.idx = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+            src.idx = q->spike_list();
             src.count = counters_ + q->counter_index;
             src.n = q->n;
         }
@@ -865,7 +998,7 @@ void Backend::build_stdp(ProjectionSlot &p)
         auto it = p.stdp_pops.find(q->uid);
         if (it == p.stdp_pops.end()) continue;
         SpikeSource src{};
-        src.idx = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+        src.idx = q->spike_list();
         src.count = counters_ + q->counter_index;
         p.stdp_sources.emplace_back(src, it->second == KNP_STDP_AND_SPIKE ? 1 : 0);
     }
@@ -880,7 +1013,15 @@ void Backend::build_resource_synapses(PopulationSlot &q)
 {
     for (auto &p : projs_)
         if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA && p->post_uid == q.uid) q.res_projs.push_back(p.get());
-    if (q.res_projs.empty()) return;
+    if (q.res_projs.empty())
+    {
+        if (q.kind != KNP_NEURON_RESOURCE_STDP_ALTAI_LIF) return;
+        // A resource-STDP AltAI-LIF population always runs the training kernel: no synapses.
+        ResSynDev y = q.adev.syn;
+        y.col_ptr = arena_.make<long long>(static_cast<size_t>(q.n) + 1);
+        q.adev.syn = y;
+        return;
+    }
     if (q.res_projs.size() > 255)
         throw Error(KNP_GB300_E_INVALID, "more than 255 resource-STDP projections into one population");
     uint64_t total = 0;
@@ -974,6 +1115,13 @@ void Backend::build_resource_synapses(PopulationSlot &q)
         y.work_count = q.bdev.syn.work_count;
         q.bdev.syn = y;
     }
+    if (q.kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF)
+    {
+        y.add_thr = q.adev.syn.add_thr;
+        y.work = q.adev.syn.work;
+        y.work_count = q.adev.syn.work_count;
+        q.adev.syn = y;
+    }
 }
 
 cudaError_t set_gather_smem(size_t bytes);
@@ -1062,6 +1210,10 @@ void Backend::init()
         if (!p->post_uid.is_null() && !find_pop(p->post_uid))
             throw Error(KNP_GB300_E_INVALID, "projection targets a population that is not loaded");
         PopulationSlot *post = find_pop(p->post_uid);
+        if (post && post->is_altai())
+            for (uint8_t t : p->type)
+                if (t == KNP_OUT_INHIBITORY_CONDUCTANCE)
+                    throw Error(KNP_GB300_E_INVALID, "AltAI-LIF neurons take no inhibitory-conductance impacts");
         if (post && post->kind == KNP_NEURON_LIF)
             for (uint8_t t : p->type)
                 if (t > KNP_OUT_INHIBITORY_CURRENT)
@@ -1105,7 +1257,8 @@ void Backend::init()
         if (p->kind == KNP_SYNAPSE_ADDITIVE_STDP_DELTA && p->n_syn) ++n_counters_;
     // Work-list counts of the resource-STDP training, one per population that may need one.
     for (auto &q : pops_)
-        if (q->kind == KNP_NEURON_RESOURCE_STDP_BLIFAT) q->work_counter_index = n_counters_++;
+        if (q->kind == KNP_NEURON_RESOURCE_STDP_BLIFAT || q->kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF)
+            q->work_counter_index = n_counters_++;
     counters_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
     for (uint32_t i = 0; i < pops_.size(); ++i) pops_[i]->counter_index = i;
     neurons_total_ = 0;
@@ -1175,6 +1328,12 @@ bool Backend::small_net_eligible(std::string &why) const
 {
     uint64_t neurons = 0, syn = 0;
     for (auto &q : pops_) neurons += q->n;
+    for (auto &q : pops_)
+        if (q->is_altai())
+        {
+            why = "AltAI-LIF populations run on the per-phase kernels";
+            return false;
+        }
     for (auto &p : projs_)
     {
         syn += p->n_syn;
@@ -1222,6 +1381,12 @@ bool Backend::grid_net_eligible(std::string &why)
     }
     size_t smem = 0;
     uint32_t n_pull = 0;
+    for (auto &q : pops_)
+        if (q->is_altai())
+        {
+            why = "AltAI-LIF populations run on the per-phase kernels";
+            return false;
+        }
     for (auto &p : projs_)
     {
         if (p->kind == KNP_SYNAPSE_RESOURCE_STDP_DELTA)
@@ -1266,7 +1431,7 @@ void Backend::setup_ring_window()
     size_t best_bytes = 0;
     for (auto &q : pops_)
     {
-        const RingView &rg = q->kind == KNP_NEURON_LIF ? q->ldev.ring : q->bdev.ring;
+        const RingView &rg = q->input_ring();
         const size_t bytes = rg.v32 ? static_cast<size_t>(rg.slots) * rg.pitch * 4 : 0;
         if (bytes > best_bytes)
         {
@@ -1310,7 +1475,7 @@ void Backend::build_small_net()
         counters_alt_ = arena_.make<uint32_t>(std::max<uint32_t>(n_counters_, 1));
         for (auto &q : pops_)
         {
-            const uint32_t *list = q->kind == KNP_NEURON_LIF ? q->ldev.spikes : q->bdev.spikes;
+            const uint32_t *list = q->spike_list();
             spikes_alt_.emplace_back(list, arena_.make<uint32_t>(std::max<uint32_t>(q->n_pad, 4), false));
         }
     }
@@ -1408,11 +1573,24 @@ void Backend::launch_population(const PopulationSlot &q)
         launch_lif(q.ldev, ctl_, stream_);
         return;
     }
+    if (q.is_altai())
+    {
+        if (q.adev.ring.bev_key) launch_altai_blocking(q.adev, ctl_, stream_);
+        launch_altai(q.adev, ctl_, stream_);
+        if (q.adev.flags & kResource)
+        {
+            const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((q.n + 7) / 8, 4ull * sm_count_));
+            const TrainView v{q.adev.res, q.adev.syn, q.adev.dopa, q.adev.spikes, q.adev.spike_count};
+            launch_resource_train(v, static_cast<int>(blocks), ctl_, stream_);
+        }
+        return;
+    }
     launch_blifat(q.bdev, ctl_, stream_);
     if (q.bdev.flags & kResSyn)
     {
         const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>((q.n + 7) / 8, 4ull * sm_count_));
-        launch_resource_train(q.bdev, static_cast<int>(blocks), ctl_, stream_);
+        const TrainView v{q.bdev.res, q.bdev.syn, q.bdev.dopa, q.bdev.spikes, q.bdev.spike_count};
+        launch_resource_train(v, static_cast<int>(blocks), ctl_, stream_);
     }
 }
 
@@ -1538,6 +1716,7 @@ void Backend::stage_host_inputs()
         c->pending.clear();
         c->has_pending = false;
     }
+    std::map<PopulationSlot *, uint32_t> ext_seq;
     for (auto &m : pending_impacts_)
     {
         PopulationSlot *q = find_pop(m.receiver);
@@ -1550,8 +1729,11 @@ void Backend::stage_host_inputs()
         KNP_CUDA(cudaMemcpyAsync(dpost, stage(m.post.data(), n * 4), n * 4, cudaMemcpyHostToDevice, stream_));
         KNP_CUDA(cudaMemcpyAsync(dval, stage(m.value.data(), n * 4), n * 4, cudaMemcpyHostToDevice, stream_));
         KNP_CUDA(cudaMemcpyAsync(dtype, stage(m.type.data(), n), n, cudaMemcpyHostToDevice, stream_));
-        const RingView &rg = q->kind == KNP_NEURON_LIF ? q->ldev.ring : q->bdev.ring;
-        launch_apply_impacts(rg, dpost, dval, dtype, m.forcing ? 1 : 0, n, ctl_, stream_);
+        // External impacts on a population are numbered in message order within the step (the order of
+        // an AltAI-LIF population's BLOCKING events).
+        const uint32_t seq = ext_seq[q];
+        ext_seq[q] += n;
+        launch_apply_impacts(q->input_ring(), dpost, dval, dtype, m.forcing ? 1 : 0, n, seq, ctl_, stream_);
         KNP_CUDA(cudaGetLastError());
         KNP_CUDA(cudaStreamSynchronize(stream_));
         arena_.release(dpost);
@@ -2022,14 +2204,17 @@ void Backend::send_impacts(
         if (t > KNP_OUT_BLOCKING) throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
         if (q->kind == KNP_NEURON_LIF && t > KNP_OUT_INHIBITORY_CURRENT)
             throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
+        if (q->is_altai() && t == KNP_OUT_INHIBITORY_CONDUCTANCE)
+            throw Error(KNP_GB300_E_INVALID, "unhandled synapse type");
         m.post.push_back(post[i]);
         m.value.push_back(value[i]);
         m.type.push_back(t);
     }
     // Of several BLOCKING impacts on one neuron only the last one in the message counts
     // (blifat_impl.h:86): the earlier ones are dropped here, so the device writes each target once.
+    // (AltAI-LIF neurons apply every BLOCKING impact in order: all are kept.)
     std::map<uint32_t, size_t> last_blk;
-    for (size_t i = 0; i < m.type.size(); ++i)
+    for (size_t i = 0; i < m.type.size() && !q->is_altai(); ++i)
         if (m.type[i] == KNP_OUT_BLOCKING) last_blk[m.post[i]] = i;
     if (!last_blk.empty())
     {
@@ -2051,7 +2236,7 @@ void Backend::send_impacts(
 void Backend::read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext)
 {
     PopulationSlot *q = find_pop(pop);
-    if (!q || q->kind == KNP_NEURON_LIF) throw Error(KNP_GB300_E_INVALID, "unknown BLIFAT population");
+    if (!q || q->kind == KNP_NEURON_LIF || q->is_altai()) throw Error(KNP_GB300_E_INVALID, "unknown BLIFAT population");
     const uint32_t n = q->n;
     std::copy(q->init_blifat.begin(), q->init_blifat.end(), out);
     if (ext && !q->init_res.empty()) std::copy(q->init_res.begin(), q->init_res.end(), ext);
@@ -2206,6 +2391,62 @@ void Backend::read_weights(const Uid &proj, float *out)
     std::vector<uint32_t> perm(p->n_syn);
     if (p->n_syn) KNP_CUDA(cudaMemcpy(perm.data(), p->perm, p->n_syn * 4, cudaMemcpyDeviceToHost));
     for (uint64_t e = 0; e < p->n_syn; ++e) out[perm[e]] = w[e];
+}
+
+void Backend::read_altai(const Uid &pop, knp_altai_neuron *out, knp_resource_stdp_state *ext)
+{
+    PopulationSlot *q = find_pop(pop);
+    if (!q || !q->is_altai()) throw Error(KNP_GB300_E_INVALID, "unknown AltAI-LIF population");
+    const uint32_t n = q->n;
+    std::copy(q->init_altai.begin(), q->init_altai.end(), out);
+    if (ext && !q->init_res.empty()) std::copy(q->init_res.begin(), q->init_res.end(), ext);
+    if (!initialized_ || step_ == 0 || n == 0) return;
+    KNP_CUDA(cudaStreamSynchronize(stream_));
+    const AltaiDev &d = q->adev;
+    auto get = [&](const auto *p)
+    {
+        using V = std::remove_const_t<std::remove_pointer_t<decltype(p)>>;
+        std::vector<V> v(n);
+        KNP_CUDA(cudaMemcpy(v.data(), p, n * sizeof(V), cudaMemcpyDeviceToHost));
+        return v;
+    };
+    auto V = get(d.V);
+    auto Vp = get(d.V_pre);
+    auto act = get(d.activity);
+    auto add = get(d.add_thr);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        out[i].potential = V[i];
+        out[i].pre_impact_potential = Vp[i];
+        out[i].activity_time = act[i];
+        out[i].additional_threshold = add[i];
+    }
+    if (d.dopa)
+    {
+        auto v = get(d.dopa);
+        for (uint32_t i = 0; i < n; ++i) out[i].dopamine_value = v[i];
+    }
+    if (ext && (d.flags & kResource))
+    {
+        const ResourceDev &r = d.res;
+        auto st = get(r.isi_status);
+        auto stab = get(r.stability);
+        auto fr = get(r.free_resource);
+        auto ls = get(r.last_step);
+        auto lss = get(r.last_spike_step);
+        auto fis = get(r.first_isi_spike);
+        auto forced = get(r.is_forced);
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            ext[i].isi_status = st[i];
+            ext[i].stability = stab[i];
+            ext[i].free_synaptic_resource = fr[i];
+            ext[i].last_step = ls[i];
+            ext[i].last_spike_step = lss[i];
+            ext[i].first_isi_spike = fis[i];
+            ext[i].is_being_forced = forced[i];
+        }
+    }
 }
 
 void Backend::read_resource_synapses(const Uid &proj, knp_resource_synapse *out)

@@ -124,12 +124,18 @@ struct PopulationSlot
     std::vector<knp_blifat_neuron> init_blifat;
     std::vector<knp_resource_stdp_state> init_res;
     std::vector<knp_lif_neuron> init_lif;
+    std::vector<knp_altai_neuron> init_altai;
     int acc_request = KNP_GB300_ACC_AUTO;
     bool record = false;
     std::set<Uid> impact_senders;
     // device
     BlifatDev bdev{};
     LifDev ldev{};
+    AltaiDev adev{};
+    bool is_altai() const { return kind == KNP_NEURON_ALTAI_LIF || kind == KNP_NEURON_RESOURCE_STDP_ALTAI_LIF; }
+    // this step's spike list of the population, whatever its kind
+    uint32_t *spike_list() const { return kind == KNP_NEURON_LIF ? ldev.spikes : is_altai() ? adev.spikes : bdev.spikes; }
+    const RingView &input_ring() const { return kind == KNP_NEURON_LIF ? ldev.ring : is_altai() ? adev.ring : bdev.ring; }
     RingView ring{};
     uint32_t counter_index = 0;
     // spike recording: ring of rec_slots per-step bitmaps on the device (see BlifatDev)
@@ -259,6 +265,9 @@ public:
     void discard_spikes(uint64_t before);
     void read_blifat(const Uid &pop, knp_blifat_neuron *out, knp_resource_stdp_state *ext);
     void load_lif(const Uid &uid, uint32_t n, const knp_lif_neuron *neurons);
+    void load_altai(const Uid &uid, int kind, uint32_t n, const knp_altai_neuron *neurons,
+                    const knp_resource_stdp_state *ext);
+    void read_altai(const Uid &pop, knp_altai_neuron *out, knp_resource_stdp_state *ext);
     void read_lif(const Uid &pop, knp_lif_neuron *out);
     void read_weights(const Uid &proj, float *out);
     uint64_t projection_size(const Uid &proj) const;

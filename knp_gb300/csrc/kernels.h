@@ -40,6 +40,7 @@ struct Control
 
 // Bits of Control::error.
 constexpr unsigned int kErrGridBarrier = 1u << 0;  // a grid barrier of the persistent grid kernel gave up
+constexpr unsigned int kErrBlockingEvents = 1u << 1;  // more BLOCKING impacts on an AltAI population in a step than kept
 
 struct RingView
 {
@@ -65,6 +66,14 @@ struct RingView
     // or infinite), or null: one byte per (slot, neuron), packed four to a word, bit 0 NaN, bit 1 +inf,
     // bit 2 -inf; such impacts are not added to the fixed-point sum.
     uint32_t *nf;
+    // BLOCKING impacts on an AltAI-LIF population, or null: every impact of a step kept as an event
+    // (key blocking_key(), value, target) in its slot's list of bev_cap entries; the population's
+    // blocking kernel applies them in key order (altai_impl.h:74-83 depends on their order).
+    unsigned long long *bev_key;
+    float *bev_val;
+    uint32_t *bev_tgt;
+    uint32_t *bev_count;  // [slots]
+    uint32_t bev_cap;
 };
 
 // Key of a BLOCKING impact: the reference applies the impacts of a step in message order and the last
@@ -184,6 +193,46 @@ struct LifDev
     uint32_t *rec_bits;  // spike recording ring, as for BlifatDev
     uint32_t rec_words, rec_slots;
     RingView ring;
+};
+
+// AltAI-LIF population (altai_lif.h:164-335, altai_impl.h:33-168): FP32 potential, integer
+// thresholds, leak and reset, FP64 additional threshold (written by resource-STDP training), int64
+// activity time. cfg bits per neuron: kAltaiDiff, kAltaiReset, kAltaiLeakRev, kAltaiSaturate,
+// kAltaiNoSave.
+enum AltaiCfg : uint32_t
+{
+    kAltaiDiff = 1u << 0,
+    kAltaiReset = 1u << 1,
+    kAltaiLeakRev = 1u << 2,
+    kAltaiSaturate = 1u << 3,
+    kAltaiNoSave = 1u << 4,
+};
+struct AltaiDev
+{
+    uint32_t n, n_pad;
+    uint32_t flags;  // kResource, kResSyn, kLiveDopa
+    float *V, *V_pre;
+    long long *activity;
+    ParamU cfg, thr, neg_thr, reset, leak;  // leak: the int16 value's int32 bits
+    float *dopa;
+    double *add_thr;
+    ResourceDev res;
+    ResSynDev syn;
+    uint32_t *spikes;
+    uint32_t *spike_count;
+    uint32_t *rec_bits;  // spike recording ring, as for BlifatDev
+    uint32_t rec_words, rec_slots;
+    RingView ring;
+};
+
+// What the resource-STDP training kernel reads and writes of a population of either base type.
+struct TrainView
+{
+    ResourceDev res;
+    ResSynDev syn;
+    const float *dopa;
+    const uint32_t *spikes;
+    const uint32_t *spike_count;
 };
 
 // External spike schedule of one sender channel (device-resident window).
@@ -341,7 +390,9 @@ struct GridNet
 
 // ---------------------------------------------------------------- launchers (stream-ordered)
 void launch_blifat(const BlifatDev &p, Control *ctl, cudaStream_t s);
-void launch_resource_train(const BlifatDev &p, int blocks, Control *ctl, cudaStream_t s);
+void launch_resource_train(const TrainView &p, int blocks, Control *ctl, cudaStream_t s);
+void launch_altai(const AltaiDev &p, Control *ctl, cudaStream_t s);
+void launch_altai_blocking(const AltaiDev &p, Control *ctl, cudaStream_t s);
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
 void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
 void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
@@ -369,9 +420,11 @@ size_t gather_smem_bytes(const PullDev &p, int grid);
 cudaError_t build_pull_layout(
     uint64_t n_syn, uint32_t n_rows, uint32_t n_post, const long long *row_ptr, const int32_t *col, const float *w,
     const uint8_t *delay, bool negate, PullDev &out, PullBuffers &bufs, cudaStream_t s);
+// seq_base: the message-order index of the first impact among this step's external impacts on the
+// population (AltAI-LIF BLOCKING events are ordered by it).
 void launch_apply_impacts(
     const RingView &ring, const uint32_t *post, const float *value, const uint8_t *type, int forcing, uint32_t n,
-    Control *ctl, cudaStream_t s);
+    uint32_t seq_base, Control *ctl, cudaStream_t s);
 
 // Network construction on the device.
 cudaError_t build_csr(

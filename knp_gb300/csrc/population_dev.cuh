@@ -487,6 +487,148 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
 }
 
 // Steps neurons i0 .. i0 + 3 of a LIF population at step t; returns their spike mask.
+// AltAI-LIF neurons i0 .. i0 + 3 (altai_impl.h:33-168) at step t; returns their spike mask. The
+// impact sum is exact (FP32 ring of dyadic weights or fixed point) and rounded once, which equals the
+// reference's FP32 sum taken impact by impact whenever its partial sums are exact (integer weights,
+// as AltAI hardware uses, or dyadic ones). BLOCKING impacts were applied to the activity time by
+// the population's blocking kernel before this step's kernel.
+template <bool kFixed>
+__device__ __forceinline__ uint32_t altai_quad(const AltaiDev &p, unsigned long long t, uint32_t i0)
+{
+    const uint32_t f = p.flags;
+    uint32_t mask = 0;
+    if (i0 >= p.n) return 0;
+    const RingView &rg = p.ring;
+    const uint32_t slot = static_cast<uint32_t>(t % rg.slots);
+    const size_t ro = static_cast<size_t>(slot) * rg.pitch + i0;
+    uint32_t forced_bits = 0;
+    if (rg.forced)
+    {
+        uint32_t *wp = rg.forced + static_cast<size_t>(slot) * rg.words + (i0 >> 5);
+        forced_bits = (*wp >> (i0 & 31)) & 0xFu;
+        if (forced_bits) atomicAnd(wp, ~(0xFu << (i0 & 31)));
+    }
+    uint32_t nf_bits = 0;
+    if (rg.nf)
+    {
+        uint32_t *wp = rg.nf + (ro >> 2);
+        nf_bits = *wp;
+        if (nf_bits) *wp = 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const uint32_t i = i0 + k;
+        if (i >= p.n) break;
+        const uint32_t cfg = pu(p.cfg, i);
+        // ---- pre-impact: the potential rounded (std::round: half away from zero) or reset.
+        float V = (cfg & kAltaiNoSave) ? static_cast<float>(pu(p.reset, i)) : roundf(p.V[i]);
+        const float v_pre = V;
+        float dopa = 0.0f;
+        // ---- impacts
+        bool finite_sum = true;
+        if (kFixed)
+        {
+            long long vh = rg.v64[ro + k], vl = rg.v64lo[ro + k];
+            rg.v64[ro + k] = 0;
+            rg.v64lo[ro + k] = 0;
+            fx_normalize(vh, vl);
+            if (isfinite(V))
+            {
+                if (V != 0.0f)
+                {
+                    long long ph, pl;
+                    fx_split(V, ph, pl);
+                    vh += ph;
+                    vl += pl;
+                    fx_normalize(vh, vl);
+                }
+                V = fx_to_float(vh, vl);
+            }
+            else
+            {
+                finite_sum = false;
+            }
+        }
+        else
+        {
+            V = __fadd_rn(V, rg.v32[ro + k]);
+            rg.v32[ro + k] = 0.0f;
+        }
+        const uint32_t nf = (nf_bits >> (8 * k)) & 0xFFu;
+        if (nf || !finite_sum)
+        {
+            const bool pinf = (nf & 2u) || v_pre == __int_as_float(0x7F800000);
+            const bool ninf = (nf & 4u) || v_pre == __int_as_float(0xFF800000);
+            if ((nf & 1u) || isnan(v_pre) || (pinf && ninf))
+                V = __int_as_float(0x7FC00000);
+            else
+                V = pinf ? __int_as_float(0x7F800000) : __int_as_float(0xFF800000);
+        }
+        if (rg.dopa)
+        {
+            dopa = rg.dopa[ro + k];
+            rg.dopa[ro + k] = 0.0f;
+        }
+        // The resource-STDP variant clears the dopamine value at pre-impact; the plain one keeps adding.
+        if (!(f & kResource) && p.dopa) dopa = __fadd_rn(p.dopa[i], dopa);
+        // ---- post-impact
+        const int32_t leak = static_cast<int32_t>(pu(p.leak, i));
+        const int sign = ((cfg & kAltaiLeakRev) && V < 0.0f) ? -1 : 1;
+        V = __fadd_rn(V, static_cast<float>(leak * sign));
+        long long act = p.activity[i];
+        if (act > 0)
+            --act;
+        else if (act < 0)
+            ++act;
+        if (act == 0) act = 0x7FFFFFFFFFFFFFFFll;
+        const double thr = __dadd_rn(static_cast<double>(pu(p.thr, i)), p.add_thr[i]);
+        bool spike = false, was_reset = false;
+        if (static_cast<double>(V) >= thr)
+        {
+            if (act > 0) spike = true;
+            if (cfg & kAltaiDiff) V = __double2float_rn(__dsub_rn(static_cast<double>(V), thr));
+            if (cfg & kAltaiReset)
+            {
+                V = static_cast<float>(pu(p.reset, i));
+                was_reset = true;
+            }
+        }
+        const float neg = static_cast<float>(pu(p.neg_thr, i));
+        if (V <= -neg && !was_reset)
+        {
+            if (cfg & kAltaiSaturate)
+                V = -neg;
+            else if (cfg & kAltaiReset)
+                V = static_cast<float>(-static_cast<int32_t>(pu(p.reset, i)));
+            else if (cfg & kAltaiDiff)
+                V = __fadd_rn(V, neg);
+        }
+        p.V[i] = V;
+        p.V_pre[i] = v_pre;
+        p.activity[i] = act;
+        if (p.dopa) p.dopa[i] = dopa;
+        if (f & kResource)
+        {
+            // The resource-STDP training kernel runs the neuron-side training; list this neuron for it.
+            const ResourceDev &r = p.res;
+            const bool forced = (forced_bits >> k) & 1u;
+            r.is_forced[i] = forced ? 1 : 0;
+            if (!spike)
+            {
+                const int32_t status = r.isi_status[i];
+                bool need = dopa > 0.0f || (dopa < 0.0f && status != 0);
+                if (!need)
+                    need = !(t - r.last_step[i] <= pu(r.isi_max, i) && status != 0) &&
+                           !(fabsf(r.free_resource[i]) < pf(r.resource_threshold, i));
+                if (need) p.syn.work[atomicAdd(p.syn.work_count, 1u)] = i;
+            }
+        }
+        if (spike) mask |= 1u << k;
+    }
+    return mask;
+}
+
 __device__ __forceinline__ uint32_t lif_quad(const LifDev &p, unsigned long long t, uint32_t i0)
 {
     uint32_t mask = 0;

@@ -79,7 +79,23 @@ __device__ __forceinline__ void deliver(
     }
     else if (ty == 4)
     {
-        if (p.ring.blk) atomicMax(p.ring.blk + o, blocking_key(p.order, d, e));
+        if (p.ring.blk)
+        {
+            atomicMax(p.ring.blk + o, blocking_key(p.order, d, e));
+        }
+        else if (p.ring.bev_key)
+        {
+            // AltAI-LIF target: keep the impact as an event of its slot (the overflow is detected by
+            // the blocking kernel from the count).
+            const uint32_t k = atomicAdd(p.ring.bev_count + slot, 1u);
+            if (k < p.ring.bev_cap)
+            {
+                const size_t q = static_cast<size_t>(slot) * p.ring.bev_cap + k;
+                p.ring.bev_key[q] = blocking_key(p.order, d, e);
+                p.ring.bev_val[q] = w;
+                p.ring.bev_tgt[q] = static_cast<uint32_t>(c);
+            }
+        }
     }
 }
 

@@ -1,6 +1,7 @@
-// Neuron-side training of resource-STDP BLIFAT populations over their SynapticResourceSTDPDeltaSynapse
-// projections, after the population step and before the projections (the population's step in
-// populations_old.h:195-217 ends with train_population):
+// Neuron-side training of resource-STDP BLIFAT and AltAI-LIF populations over their
+// SynapticResourceSTDPDeltaSynapse projections, after the population step and before the
+// projections (the population's step in populations_old.h:195-217 ends with train_population; the
+// AltAI-LIF training of altai/altai_stdp.h is the same computation):
 //   process_spiking_neurons_impl (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/impl/
 //     populations/blifat/blifat_stdp.h:35-103) for every neuron that spiked,
 //   do_dopamine_plasticity_impl (:106-155) and renormalize_resource (impl/populations/training/
@@ -66,7 +67,7 @@ __device__ __forceinline__ bool working_synapse(const ResSynDev &y, long long e,
     return y.locked[ent >> kResSlotShift] == 0u;
 }
 
-__device__ void train_neuron(const BlifatDev &p, uint32_t i, unsigned long long t, bool spiked, int lane)
+__device__ void train_neuron(const TrainView &p, uint32_t i, unsigned long long t, bool spiked, int lane)
 {
     const ResourceDev &r = p.res;
     const ResSynDev &y = p.syn;
@@ -198,7 +199,7 @@ __device__ void train_neuron(const BlifatDev &p, uint32_t i, unsigned long long 
     }
 }
 
-__global__ void __launch_bounds__(kTrainThreads) resource_train_kernel(BlifatDev p, Control *ctl)
+__global__ void __launch_bounds__(kTrainThreads) resource_train_kernel(TrainView p, Control *ctl)
 {
     pdl_begin();
     const unsigned long long t = ctl->step;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(kTrainThreads) resource_train_kernel(BlifatDev
 
 }  // namespace
 
-void launch_resource_train(const BlifatDev &p, int blocks, Control *ctl, cudaStream_t s)
+void launch_resource_train(const TrainView &p, int blocks, Control *ctl, cudaStream_t s)
 {
     launch_pdl(resource_train_kernel, dim3(blocks > 0 ? blocks : 1), dim3(kTrainThreads), 0, s, p, ctl);
 }

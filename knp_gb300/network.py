@@ -521,3 +521,49 @@ def resource_stdp_mixed_network(seed: int = 23, n: int = 300, n_in: int = 100, n
                  bernoulli_schedule(cf, seed, n, steps, 0.01, stream=S_INPUT + 100),
                  bernoulli_schedule(cd, seed, n, steps, 0.02, stream=S_INPUT + 200)]
 
+
+def altai_network(seed: int = 31, n: int = 200, n_in: int = 80, steps: int = 200):
+    """AltAI-LIF neurons (altai_impl.h:33-168) with every option: per-neuron is_diff / is_reset /
+    leak_rev / saturate / do_not_save, thresholds 20..60, negative thresholds 10..100, leaks -3..3,
+    resets 0..5. Channel A -> excitatory/inhibitory delta projection (p 0.3, integer weights -8..16,
+    delays 1..4); a recurrent delta projection (p 0.05, integer weights -6..10, delays 1..3); channel B
+    -> BLOCKING projection (p 0.05 plus repeated pairs, weights from {-3, -1, 2, 4, 5, -6}, delays
+    1..2); channel D -> DOPAMINE (aligned, 0.5). Integer weights keep every FP32 partial sum exact, so
+    the order of the reference's impact-by-impact sum does not matter. External impacts may be sent
+    from channel uid 3103. Inputs: A Bernoulli 0.1, B 0.03, D 0.02."""
+    rng = np.random.default_rng(seed)
+    uid = lambda k: T.uid_from_int(3100 + k)
+    pop_uid = uid(0)
+    a = T.altai_defaults(n)
+    for f in ("is_diff", "is_reset", "leak_rev", "saturate", "do_not_save"):
+        a[f] = rng.random(n) < (0.1 if f == "do_not_save" else 0.5)
+    a["activation_threshold"] = rng.integers(20, 61, n)
+    a["negative_activation_threshold"] = rng.integers(10, 101, n)
+    a["potential_leak"] = rng.integers(-3, 4, n)
+    a["potential_reset_value"] = rng.integers(0, 6, n)
+    pop = Population(pop_uid, T.ALTAI_LIF, a)
+
+    def rand_proj(k, pre_uid, n_pre, p, wfn, d_lo, d_hi, types, extra=0):
+        pre, post = np.nonzero(rng.random((n_pre, n)) < p)
+        if extra:
+            j = rng.integers(0, pre.size, extra)
+            pre, post = np.concatenate([pre, pre[j]]), np.concatenate([post, post[j]])
+        ty = np.asarray(types, np.uint8)[rng.integers(0, len(types), pre.size)]
+        return Projection(uid(k), T.DELTA, pre_uid, pop_uid, pre.astype(np.uint32), post.astype(np.uint32),
+                          np.asarray(wfn(pre.size), np.float32), rng.integers(d_lo, d_hi + 1, pre.size).astype(np.uint32),
+                          out_type=ty)
+
+    blk = np.float32([-3, -1, 2, 4, 5, -6])
+    one = np.arange(n, dtype=np.uint32)
+    projs = [
+        rand_proj(10, T.NULL_UID, n_in, 0.3, lambda s: rng.integers(-8, 17, s), 1, 4, [T.EXCITATORY, T.INHIBITORY_CURRENT]),
+        rand_proj(11, pop_uid, n, 0.05, lambda s: rng.integers(-6, 11, s), 1, 3, [T.EXCITATORY]),
+        rand_proj(12, T.NULL_UID, n_in, 0.05, lambda s: blk[rng.integers(0, blk.size, s)], 1, 2, [T.BLOCKING], extra=100),
+        Projection(uid(13), T.DELTA, T.NULL_UID, pop_uid, one, one, np.full(n, 0.5, np.float32), np.ones(n, np.uint32),
+                   out_type=np.full(n, T.DOPAMINE, np.uint8)),
+    ]
+    net = Network([pop], projs, [(uid(10), uid(20)), (uid(12), uid(21)), (uid(13), uid(22)), (pop_uid, uid(3))])
+    return net, [bernoulli_schedule(uid(20), seed, n_in, steps, 0.1),
+                 bernoulli_schedule(uid(21), seed, n_in, steps, 0.03, stream=S_INPUT + 60),
+                 bernoulli_schedule(uid(22), seed, n, steps, 0.02, stream=S_INPUT + 70)]
+

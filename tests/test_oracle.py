@@ -236,3 +236,73 @@ def test_restated_oracle_matches_reference_headers_resource_stdp(oracle_lib):
     rules = o.resource_synapses(net.projections[0].uid)
     assert rules["had_hebbian_update"].sum() > 100 and rules["has_contributed"].sum() > 100
 
+
+
+def _run_altai(neuron, steps, impacts=(), n=1, index=0):
+    """knp/tests/framework/altai_lif_test.cpp:45-95: AltAI neurons, one external EXCITATORY impact per
+    step to neuron `index`; the potential is read before each step."""
+    pop_uid, in_uid = T.uid_from_int(601), T.uid_from_int(602)
+    neurons = np.repeat(neuron, n)
+    net = N.Network([N.Population(pop_uid, T.ALTAI_LIF, neurons)], [], [(pop_uid, in_uid)])
+    o = orc.OracleNet("restated")
+    o.load(net)
+    pots, spikes = [], []
+    for t in range(steps):
+        if t < len(impacts):
+            o.send_impacts(in_uid, pop_uid, [index], [impacts[t]], [T.EXCITATORY], True)
+        pots.append(int(np.int16(o.altai(pop_uid)[0]["potential"][index])))
+        o.step()
+        if index in o.spikes(pop_uid):
+            spikes.append(t)
+    return pots, spikes
+
+
+ALTAI_KATS = [
+    # altai_lif_test.cpp:97-190: (fields, steps, impacts, n, index, potentials, spikes)
+    ({"activation_threshold": 200, "potential_leak": -25, "potential": 100, "leak_rev": 1}, 10, (), 3, 2,
+     [100, 75, 50, 25, 0, -25, 0, -25, 0, -25], []),
+    ({"activation_threshold": 200, "negative_activation_threshold": (-200) % 65536, "potential_leak": -25,
+      "potential": 100, "leak_rev": 0}, 10, (), 1, 0, [100, 75, 50, 25, 0, -25, -50, -75, -100, -125], []),
+    ({"potential": 100, "activation_threshold": 200, "negative_activation_threshold": 60, "potential_leak": -50,
+      "leak_rev": 0, "saturate": 1}, 10, (), 1, 0, [100, 50, 0, -50, -60, -60, -60, -60, -60, -60], []),
+    ({"potential_leak": 50, "activation_threshold": 110}, 10, (), 1, 0, [0, 50, 100, 0, 50, 100, 0, 50, 100, 0], [2, 5, 8]),
+    ({"potential_leak": -30, "activation_threshold": 100}, 10, (130, 50, 50, 50, 50, 0, 100, 80, 80, 80), 5, 3,
+     [0, 0, 20, 40, 60, 80, 50, 0, 50, 0], [0, 6, 8]),
+]
+
+
+@pytest.mark.parametrize("case", range(len(ALTAI_KATS)))
+def test_oracle_altai_known_answers(oracle_lib, case):
+    """Expected potentials and spike steps of knp/tests/framework/altai_lif_test.cpp."""
+    fields, steps, impacts, n, index, pots, spikes = ALTAI_KATS[case]
+    neuron = T.altai_defaults(1)
+    for k, v in fields.items():
+        neuron[k] = v
+    assert _run_altai(neuron, steps, impacts, n, index) == (pots, spikes)
+
+
+@pytest.mark.skipif(not orc.available("reference"), reason="reference-header oracle not built (no KNP sources)")
+def test_restated_oracle_matches_reference_headers_altai(oracle_lib):
+    """AltAI-LIF populations (altai_impl.h:33-168, including the order-dependent BLOCKING rule and
+    external impacts) and the resource-STDP AltAI golden network: the restated oracle gives the
+    reference headers' spikes and neuron state."""
+    from tests.golden.make_golden import canonical
+
+    net, scheds = N.altai_network(steps=150)
+    pop = net.populations[0].uid
+    rng = np.random.default_rng(2)
+
+    def ext(o, t):
+        if t % 9 == 4:
+            post = rng.integers(0, 200, 10).astype(np.uint32)
+            o.send_impacts(T.uid_from_int(3103), pop, post, rng.choice(np.float32([-5, 3, 7, -2]), 10),
+                           rng.choice(np.uint8([T.BLOCKING, T.EXCITATORY, T.DOPAMINE]), 10), True)
+
+    rng_state = rng.bit_generator.state
+    a, oa = orc.run(net, scheds, 150, which="restated", on_step=ext)
+    rng.bit_generator.state = rng_state
+    b, ob = orc.run(net, scheds, 150, which="reference", on_step=ext)
+    assert spike_digest(a[pop]) == spike_digest(b[pop])
+    assert canonical(oa.altai(pop)[0]) == canonical(ob.altai(pop)[0])
+    assert sum(s.size for s in a[pop]) > 200
+    assert (oa.altai(pop)[0]["activity_time"] != np.iinfo(np.int64).max).sum() > 5
