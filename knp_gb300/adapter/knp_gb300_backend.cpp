@@ -119,8 +119,8 @@ void from_c(const knp_blifat_neuron &c, nt::neuron_parameters<nt::BLIFATNeuron> 
     n.random_number_generator_state_ = c.random_number_generator_state;
 }
 
-using ResourceParams = nt::neuron_parameters<nt::SynapticResourceSTDPBLIFATNeuron>;
-
+// The resource-STDP extension of a neuron of either base type (stdp_synaptic_resource_rule.h:70-192).
+template <class ResourceParams>
 knp_resource_stdp_state resource_to_c(const ResourceParams &n)
 {
     knp_resource_stdp_state c{};
@@ -142,6 +142,7 @@ knp_resource_stdp_state resource_to_c(const ResourceParams &n)
     return c;
 }
 
+template <class ResourceParams>
 void resource_from_c(const knp_resource_stdp_state &c, ResourceParams &n)
 {
     n.synapse_sum_threshold_coefficient_ = c.synapse_sum_threshold_coefficient;
@@ -188,6 +189,44 @@ void rule_from_c(const knp_resource_synapse &c, Rule &r)
     r.had_hebbian_update_ = c.had_hebbian_update != 0u;
     r.last_spike_step_ = c.last_spike_step;
     r.has_contributed_ = c.has_contributed != 0u;
+}
+
+knp_altai_neuron altai_to_c(const nt::neuron_parameters<nt::AltAILIF> &n)
+{
+    knp_altai_neuron c{};
+    c.is_diff = n.is_diff_ ? 1 : 0;
+    c.is_reset = n.is_reset_ ? 1 : 0;
+    c.leak_rev = n.leak_rev_ ? 1 : 0;
+    c.saturate = n.saturate_ ? 1 : 0;
+    c.do_not_save = n.do_not_save_ ? 1 : 0;
+    c.potential = n.potential_;
+    c.pre_impact_potential = n.pre_impact_potential_;
+    c.activation_threshold = n.activation_threshold_;
+    c.negative_activation_threshold = n.negative_activation_threshold_;
+    c.potential_leak = n.potential_leak_;
+    c.potential_reset_value = n.potential_reset_value_;
+    c.dopamine_value = n.dopamine_value_;
+    c.additional_threshold = n.additional_threshold_;
+    c.activity_time = n.activity_time_;
+    return c;
+}
+
+void altai_from_c(const knp_altai_neuron &c, nt::neuron_parameters<nt::AltAILIF> &n)
+{
+    n.is_diff_ = c.is_diff != 0;
+    n.is_reset_ = c.is_reset != 0;
+    n.leak_rev_ = c.leak_rev != 0;
+    n.saturate_ = c.saturate != 0;
+    n.do_not_save_ = c.do_not_save != 0;
+    n.potential_ = c.potential;
+    n.pre_impact_potential_ = c.pre_impact_potential;
+    n.activation_threshold_ = c.activation_threshold;
+    n.negative_activation_threshold_ = c.negative_activation_threshold;
+    n.potential_leak_ = c.potential_leak;
+    n.potential_reset_value_ = c.potential_reset_value;
+    n.dopamine_value_ = c.dopamine_value;
+    n.additional_threshold_ = c.additional_threshold;
+    n.activity_time_ = c.activity_time;
 }
 
 knp_lif_neuron lif_to_c(const nt::neuron_parameters<nt::LIFNeuron> &n)
@@ -268,7 +307,8 @@ void GB300Backend::check(int rc, const char *what) const
 
 std::vector<std::string> GB300Backend::get_supported_neurons() const
 {
-    return {"BLIFATNeuron", "SynapticResourceSTDPBLIFATNeuron", "LIFNeuron"};
+    return {"BLIFATNeuron", "SynapticResourceSTDPBLIFATNeuron", "AltAILIF", "SynapticResourceSTDPAltAILIFNeuron",
+            "LIFNeuron"};
 }
 
 std::vector<std::string> GB300Backend::get_supported_synapses() const
@@ -278,7 +318,8 @@ std::vector<std::string> GB300Backend::get_supported_synapses() const
 
 std::vector<size_t> GB300Backend::get_supported_population_indexes() const
 {
-    return indexes_in<knp::core::AllPopulationsVariant, BLIFATPopulation, ResourceBLIFATPopulation, LIFPopulation>();
+    return indexes_in<knp::core::AllPopulationsVariant, BLIFATPopulation, ResourceBLIFATPopulation, AltAIPopulation,
+                      ResourceAltAIPopulation, LIFPopulation>();
 }
 
 std::vector<size_t> GB300Backend::get_supported_projection_indexes() const
@@ -363,6 +404,20 @@ void GB300Backend::_init()
                     std::vector<knp_lif_neuron> c;
                     for (const auto &x : pop) c.push_back(lif_to_c(x));
                     check(knp_gb300_load_lif_population(h_, uid, n, c.data()), "knp_gb300_load_lif_population");
+                }
+                else if constexpr (std::is_same_v<T, AltAIPopulation> || std::is_same_v<T, ResourceAltAIPopulation>)
+                {
+                    std::vector<knp_altai_neuron> c;
+                    std::vector<knp_resource_stdp_state> ext;
+                    for (const auto &x : pop)
+                    {
+                        c.push_back(altai_to_c(static_cast<const nt::neuron_parameters<nt::AltAILIF> &>(x)));
+                        if constexpr (std::is_same_v<T, ResourceAltAIPopulation>) ext.push_back(resource_to_c(x));
+                    }
+                    constexpr int kind = std::is_same_v<T, ResourceAltAIPopulation> ? KNP_NEURON_RESOURCE_STDP_ALTAI_LIF
+                                                                                    : KNP_NEURON_ALTAI_LIF;
+                    check(knp_gb300_load_altai_population(h_, uid, kind, n, c.data(), ext.empty() ? nullptr : ext.data()),
+                          "knp_gb300_load_altai_population");
                 }
                 else
                 {
@@ -525,6 +580,18 @@ knp::core::Backend::DataRanges GB300Backend::get_network_data() const
                         std::vector<knp_lif_neuron> c(pop.size());
                         check(knp_gb300_read_lif_population(h_, uid, c.data()), "knp_gb300_read_lif_population");
                         for (size_t i = 0; i < c.size(); ++i) lif_from_c(c[i], copy[i]);
+                    }
+                    else if constexpr (std::is_same_v<T, AltAIPopulation> || std::is_same_v<T, ResourceAltAIPopulation>)
+                    {
+                        std::vector<knp_altai_neuron> c(pop.size());
+                        std::vector<knp_resource_stdp_state> ext(std::is_same_v<T, ResourceAltAIPopulation> ? pop.size() : 0);
+                        check(knp_gb300_read_altai_population(h_, uid, c.data(), ext.empty() ? nullptr : ext.data()),
+                              "knp_gb300_read_altai_population");
+                        for (size_t i = 0; i < c.size(); ++i)
+                        {
+                            altai_from_c(c[i], static_cast<nt::neuron_parameters<nt::AltAILIF> &>(copy[i]));
+                            if constexpr (std::is_same_v<T, ResourceAltAIPopulation>) resource_from_c(ext[i], copy[i]);
+                        }
                     }
                     else
                     {

@@ -11,8 +11,8 @@
  * export line is the only Boost-dependent line and is compiled only where Boost is available.
  *
  * It keeps the single-threaded backend's behaviour: the same supported neuron and synapse types
- * (BLIFAT, synaptic-resource-STDP BLIFAT, LIF; delta, additive-STDP delta and synaptic-resource-STDP
- * delta), the same message
+ * (BLIFAT, AltAI-LIF and their synaptic-resource-STDP variants, LIF; delta, additive-STDP delta and
+ * synaptic-resource-STDP delta), the same message
  * semantics on the backend's bus (SpikeMessages sent to a projection's UID reach that projection
  * at the next step; SynapticImpactMessages sent to a population's UID are applied at the next
  * step; each population that spiked sends its SpikeMessage {population UID, step, ascending
@@ -24,6 +24,7 @@
 #include <knp/core/backend.h>
 #include <knp/core/population.h>
 #include <knp/core/projection.h>
+#include <knp/neuron-traits/altai_lif.h>
 #include <knp/neuron-traits/blifat.h>
 #include <knp/neuron-traits/lif.h>
 #include <knp/neuron-traits/stdp_type_traits.h>
@@ -47,11 +48,14 @@ public:
     using BLIFATPopulation = knp::core::Population<knp::neuron_traits::BLIFATNeuron>;
     using ResourceBLIFATPopulation = knp::core::Population<knp::neuron_traits::SynapticResourceSTDPBLIFATNeuron>;
     using LIFPopulation = knp::core::Population<knp::neuron_traits::LIFNeuron>;
+    using AltAIPopulation = knp::core::Population<knp::neuron_traits::AltAILIF>;
+    using ResourceAltAIPopulation = knp::core::Population<knp::neuron_traits::SynapticResourceSTDPAltAILIFNeuron>;
     using DeltaProjection = knp::core::Projection<knp::synapse_traits::DeltaSynapse>;
     using AdditiveSTDPProjection = knp::core::Projection<knp::synapse_traits::AdditiveSTDPDeltaSynapse>;
     using ResourceSTDPProjection = knp::core::Projection<knp::synapse_traits::SynapticResourceSTDPDeltaSynapse>;
     /** The population and projection types this backend runs (the single-threaded backend's set). */
-    using PopulationVariants = std::variant<BLIFATPopulation, ResourceBLIFATPopulation, LIFPopulation>;
+    using PopulationVariants = std::variant<BLIFATPopulation, ResourceBLIFATPopulation, AltAIPopulation,
+                                            ResourceAltAIPopulation, LIFPopulation>;
     using ProjectionVariants = std::variant<DeltaProjection, AdditiveSTDPProjection, ResourceSTDPProjection>;
 
     /** A backend on CUDA device `device`; the device backend (knp_gb300_create) is created at first
