@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
                 for (uint32_t base = 0; base < p.n; base += 4 * n_threads)
                 {
                     const uint32_t i0 = base + 4 * gthread;
-                    const uint32_t mask = p.ring.fixed ? blifat_quad<true>(p, t, i0) : blifat_quad<false>(p, t, i0);
+                    const uint32_t mask = blifat_quad_any(p, t, i0);
                     emit_spikes<kGridThreads>(mask, i0, p.spikes, p.spike_count,
                                               record_slot(p.rec_bits, p.rec_words, p.rec_slots, t), p.rec_words);
                 }
@@ -286,17 +286,19 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
         // ---- phase C: gathers completing step t + 1's input (every projection with a gather
         // layout clears its next bitmap slot here even when nothing was pulled).
         bool need = false;
-        for (uint32_t k = 0; k < g.n_pull; ++k) need = need || gather_needed(projs[g.pull[k]].pull, t + 1);
-        need = __syncthreads_or(need) != 0;  // one decision per block (it gates a barrier)
-        for (uint32_t k = 0; k < g.n_pull; ++k) grid_gather(projs[g.pull[k]], t + 1, grid_smem);
-        if (need)
+        for (uint32_t k = 0; k < g.n_pull; ++k) need = gather_needed_block(projs[g.pull[k]].pull, t + 1) || need;
+        if (!need)
         {
-            target += G;
-            if (!grid_sync(g.barrier, ctl, target))
-            {
-                ok = false;
-                break;
-            }
+            // Nothing was pulled in the gathers' delay window: only the next bitmap slots are cleared.
+            for (uint32_t k = 0; k < g.n_pull; ++k) clear_bitmap_slot(projs[g.pull[k]].pull, t + 1, blockIdx.x, G);
+            continue;
+        }
+        for (uint32_t k = 0; k < g.n_pull; ++k) grid_gather(projs[g.pull[k]], t + 1, grid_smem);
+        target += G;
+        if (!grid_sync(g.barrier, ctl, target))
+        {
+            ok = false;
+            break;
         }
     }
     if (!ok)

@@ -19,7 +19,8 @@ __global__ void __launch_bounds__(kBlock, 3) blifat_kernel(BlifatDev p, Control 
     pdl_begin();
     const unsigned long long t = ctl->step;
     const uint32_t i0 = (blockIdx.x * kBlock + threadIdx.x) * 4;
-    const uint32_t mask = blifat_quad<kFixed, kRS>(p, t, i0);
+    const uint32_t mask =
+        (!kFixed && !kRS && p.flags == 0u) ? blifat_quad_lean(p, t, i0) : blifat_quad<kFixed, kRS>(p, t, i0);
     emit_spikes<kBlock>(mask, i0, p.spikes, p.spike_count, record_slot(p.rec_bits, p.rec_words, p.rec_slots, t),
                         p.rec_words);
 }

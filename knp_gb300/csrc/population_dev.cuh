@@ -487,6 +487,54 @@ __device__ __forceinline__ uint32_t blifat_quad(const BlifatDev &p, unsigned lon
 }
 
 // Steps neurons i0 .. i0 + 3 of a LIF population at step t; returns their spike mask.
+// blifat_quad for a population whose every state field is lazy (flags 0: no potential,
+// threshold, trace, conductance or dopamine dynamics, no bursting or blocking, refractory period 0
+// with the default counter, no additional threshold — the reference's default BLIFAT neuron) and an
+// FP32 input ring. blifat_step then reduces to: the potential is +0 plus this step's input sum, a
+// spike iff the step is not step 0 and the potential reaches the threshold, the reset, and the
+// min-potential clamp; the same operations in the same order, so results are identical.
+__device__ __forceinline__ uint32_t blifat_quad_lean(const BlifatDev &p, unsigned long long t, uint32_t i0)
+{
+    uint32_t mask = 0;
+    if (i0 < p.n)
+    {
+        const RingView &rg = p.ring;
+        const uint32_t slot = static_cast<uint32_t>(t % rg.slots);
+        const size_t ro = static_cast<size_t>(slot) * rg.pitch + i0;
+        float4 acc = ld4(rg.v32, ro);
+        st4(rg.v32, ro, make_float4(0.f, 0.f, 0.f, 0.f));
+        float4 V = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            const uint32_t i = i0 + k;
+            if (i >= p.n) break;
+            float v = __fadd_rn(0.0f, at(acc, k));
+            const float thr_total = __fadd_rn(__fadd_rn(pf(p.thr, i), 0.0f), 0.0f);
+            if (t > 0 && v >= thr_total)
+            {
+                mask |= 1u << k;
+                v = pf(p.v_reset, i);
+                p.n_since[i] = static_cast<uint32_t>(t);  // lazy refractory tracking: the step of the spike
+            }
+            const float vmin = pf(p.v_min, i);
+            if (v < vmin) v = vmin;
+            at(V, k) = v;
+        }
+        st4(p.V, i0, V);
+    }
+    return mask;
+}
+
+// The BLIFAT quad step of any plain population (no resource-STDP synapses) for the fused and grid
+// kernels.
+__device__ __forceinline__ uint32_t blifat_quad_any(const BlifatDev &p, unsigned long long t, uint32_t i0)
+{
+    if (p.ring.fixed) return blifat_quad<true>(p, t, i0);
+    if (p.flags == 0u) return blifat_quad_lean(p, t, i0);
+    return blifat_quad<false>(p, t, i0);
+}
+
 // AltAI-LIF neurons i0 .. i0 + 3 (altai_impl.h:33-168) at step t; returns their spike mask. The
 // impact sum is exact (FP32 ring of dyadic weights or fixed point) and rounded once, which equals the
 // reference's FP32 sum taken impact by impact whenever its partial sums are exact (integer weights,

@@ -62,6 +62,27 @@ __device__ __forceinline__ bool gather_needed(const PullDev &g, unsigned long lo
     return false;
 }
 
+// gather_needed for a whole block (every thread calls it; one flag per thread, the same answer in
+// every thread of the block).
+__device__ __forceinline__ bool gather_needed_block(const PullDev &g, unsigned long long tn)
+{
+    bool need = false;
+    for (uint32_t d = 1 + threadIdx.x; d <= g.max_delay && d <= tn; d += blockDim.x)
+        need = need || g.pulled[static_cast<uint32_t>((tn - d) % g.hist_slots)] != 0u;
+    return __syncthreads_or(need) != 0;
+}
+
+// Clears block `block`'s share (of G) of the bitmap slot that the scatter kernel of step tn will
+// fill; it holds step tn - hist_slots, which no gather reads any more.
+__device__ __forceinline__ void clear_bitmap_slot(const PullDev &g, unsigned long long tn, uint32_t block, uint32_t G)
+{
+    const uint32_t sl_next = static_cast<uint32_t>(tn % g.hist_slots);
+    uint32_t *dst = g.bitmap + static_cast<size_t>(sl_next) * g.words;
+    const uint32_t b0 = static_cast<uint32_t>(static_cast<uint64_t>(block) * g.words / G);
+    const uint32_t b1 = static_cast<uint32_t>(static_cast<uint64_t>(block + 1) * g.words / G);
+    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) dst[i] = 0u;
+}
+
 // Block `block` of G gather blocks completes the input of step tn (every thread of the block calls
 // it; it contains block barriers), and clears its share of the bitmap slot that step tn's spikes
 // will be recorded in. smem_u4: gather_smem_for(p.pull, G) bytes of dynamic shared memory.
@@ -71,6 +92,7 @@ __device__ __forceinline__ void gather_block(const ProjectionDev &p, unsigned lo
 {
     __shared__ uint32_t s_next;  // next slice of the current delay to hand out
     __shared__ float s_tab[256];
+    __shared__ uint8_t s_pflag[256];  // pulled flag of step tn - d, d = 1 .. max_delay (max_delay <= 255)
     const PullDev &g = p.pull;
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem_u4);
     float *acc = reinterpret_cast<float *>(bm + g.words);
@@ -86,13 +108,16 @@ __device__ __forceinline__ void gather_block(const ProjectionDev &p, unsigned lo
     const uint32_t w1 = static_cast<uint32_t>(static_cast<uint64_t>(block + 1) * g.n_windows / G);
     const uint32_t n_acc = (w1 - w0) * kPullWindow;
     const int lane = threadIdx.x & 31;
+    for (uint32_t d = 1 + threadIdx.x; d <= g.max_delay; d += blockDim.x)
+        s_pflag[d] = d <= tn ? static_cast<uint8_t>(g.pulled[static_cast<uint32_t>((tn - d) % g.hist_slots)]) : 0;
+    __syncthreads();
 
     bool any = false;
     for (uint32_t d = 1; d <= g.max_delay && d <= tn; ++d)
     {
         const unsigned long long s = tn - d;
         const uint32_t sl = static_cast<uint32_t>(s % g.hist_slots);
-        const uint32_t pflag = g.pulled[sl];
+        const uint32_t pflag = s_pflag[d];
         if (!pflag) continue;
         const bool all = pflag == 2u;  // every presynaptic neuron fired at step s: no bitmap needed
         if (!any)
@@ -231,13 +256,7 @@ __device__ __forceinline__ void gather_block(const ProjectionDev &p, unsigned lo
             if (j < g.n_post && acc[i] != 0.0f) ring[j] = __fadd_rn(ring[j], acc[i]);
         }
     }
-    // Clear the bitmap slot that the scatter kernel of step tn will fill; it holds step
-    // tn - hist_slots, which no gather reads any more.
-    const uint32_t sl_next = static_cast<uint32_t>(tn % g.hist_slots);
-    uint32_t *dst = g.bitmap + static_cast<size_t>(sl_next) * g.words;
-    const uint32_t b0 = static_cast<uint32_t>(static_cast<uint64_t>(block) * g.words / G);
-    const uint32_t b1 = static_cast<uint32_t>(static_cast<uint64_t>(block + 1) * g.words / G);
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) dst[i] = 0u;
+    clear_bitmap_slot(g, tn, block, G);
 }
 
 }  // namespace

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1) small_net_kernel(SmallNet ne
                 for (uint32_t base = 0; base < p.n; base += 4 * n_threads)
                 {
                     const uint32_t i0 = base + 4 * gthread;
-                    const uint32_t mask = p.ring.fixed ? blifat_quad<true>(p, t, i0) : blifat_quad<false>(p, t, i0);
+                    const uint32_t mask = blifat_quad_any(p, t, i0);
                     emit_spikes<kSmallThreads>(mask, i0, p.spikes, p.spike_count,
                                                record_slot(p.rec_bits, p.rec_words, p.rec_slots, t), p.rec_words);
                 }
