@@ -357,6 +357,23 @@ def stdp_measure(device: int):
     ms_phases = bp.step_timed(1900)
     bp.close()
     crc = zlib.crc32(w.tobytes())
+    # The single-threaded CPU baseline on the same config: the oracle (restated single-threaded
+    # backend step, one host thread) over the first samples, about 10-20 s of CPU work.
+    from oracle import oracle as orc
+
+    o = orc.OracleNet("restated")
+    o.load(net)
+    t0, cpu_steps = time.perf_counter(), 0
+    while cpu_steps < 2000 and (cpu_steps < 100 or time.perf_counter() - t0 < 10.0):
+        for sc in scheds:
+            idx = sc.at(cpu_steps)
+            if idx.size:
+                o.send_spikes(sc.sender, idx, cpu_steps)
+        o.step()
+        cpu_steps += 1
+    cpu_s = time.perf_counter() - t0
+    cpu_events = o.events
+    o.close()
     fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "stdp_full.json")
     with open(fixture) as f:
         expect = json.load(f)
@@ -368,6 +385,9 @@ def stdp_measure(device: int):
         "phases_us_per_step": ms_phases / 1900 * 1e3,
         "phase_us_per_step": {k: float(v) * 1e3 for k, v in zip(("population", "projection", "stdp", "step_end"), ph)},
         "events": int(events), "spikes": int(spikes),
+        "cpu_baseline": {"value": cpu_events / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"the first {cpu_steps} steps of the same config on the oracle (restated "
+                                   "single-threaded backend step), host-sent inputs"},
         "weights_crc32": crc, "weights_match_reference_oracle": bool(crc == expect["weights_crc"]),
         "events_match_reference_oracle": bool(int(events) == expect["events"]),
     }
