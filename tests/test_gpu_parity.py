@@ -553,9 +553,11 @@ def test_errors_are_reported():
     b = B.GB300Backend()
     pop = N.Population(T.uid_from_int(31), T.BLIFAT, T.blifat_defaults(4))
     b.load_populations([pop])
-    bad = N.Projection(T.uid_from_int(32), T.DELTA, T.NULL_UID, pop.uid, np.zeros(1, np.uint32),
+    # BLOCKING synapses are taken in delta projections only (an STDP weight may change in flight).
+    bad = N.Projection(T.uid_from_int(32), T.ADDITIVE_STDP_DELTA, T.NULL_UID, pop.uid, np.zeros(1, np.uint32),
                        np.zeros(1, np.uint32), np.ones(1, np.float32), np.ones(1, np.uint32),
-                       out_type=np.array([T.BLOCKING], np.uint8))
+                       out_type=np.array([T.BLOCKING], np.uint8), tau_plus=np.full(1, 2.0, np.float32),
+                       tau_minus=np.full(1, 2.0, np.float32))
     with pytest.raises(KnpGb300Error):
         b.load_projections([bad])
     oob = N.Projection(T.uid_from_int(33), T.DELTA, T.NULL_UID, pop.uid, np.zeros(1, np.uint32),
