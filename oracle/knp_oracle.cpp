@@ -230,6 +230,9 @@ struct or_net
     uint64_t step = 0;
     uint64_t events = 0;
     bool initialized = false;
+    // The network as built by or_init, for or_reset (repeated timing windows of the CPU baseline).
+    std::vector<Population> pops0;
+    std::vector<Projection> projs0;
 
     Population *find_pop(const Uid &u) const
     {
@@ -965,6 +968,29 @@ int or_init(or_net *net)
         if (Population *q = net->find_pop(recv)) q->impact_senders.insert(send);
     }
     net->initialized = true;
+    net->pops0.clear();
+    net->projs0.clear();
+    return 0;
+}
+
+int or_snapshot(or_net *net)
+{
+    net->pops0.clear();
+    net->projs0.clear();
+    for (auto &p : net->pops) net->pops0.push_back(*p);
+    for (auto &p : net->projs) net->projs0.push_back(*p);
+    return 0;
+}
+
+int or_reset(or_net *net)
+{
+    if (net->pops0.size() != net->pops.size()) return fail("no snapshot to reset to");
+    for (size_t i = 0; i < net->pops.size(); ++i) *net->pops[i] = net->pops0[i];
+    for (size_t i = 0; i < net->projs.size(); ++i) *net->projs[i] = net->projs0[i];
+    net->ext_spikes.clear();
+    net->ext_impacts.clear();
+    net->step = 0;
+    net->events = 0;
     return 0;
 }
 

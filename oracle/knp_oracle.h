@@ -69,6 +69,10 @@ int or_subscribe(or_net *net, knp_uid receiver, knp_uid sender);
 
 /** Build the reference's subscriptions (knp/backends/cpu/cpu-library/include/knp/backends/cpu-library/init.h:93-110). */
 int or_init(or_net *net);
+/* Timing support (restated oracle only): or_snapshot keeps a copy of the network as it is now, and
+ * or_reset returns the network to that copy (step 0, no messages in flight). */
+int or_snapshot(or_net *net);
+int or_reset(or_net *net);
 
 /** An external SpikeMessage {sender, send_time, indexes}, delivered at the next step. */
 int or_send_spikes(or_net *net, knp_uid sender, uint64_t send_time, uint32_t n, const uint32_t *idx);

@@ -81,6 +81,8 @@ def _load(which: str):
         }
         if which == "restated":
             sig["or_step_mt"] = ([p, ctypes.c_int], ctypes.c_int)
+            sig["or_snapshot"] = ([p], ctypes.c_int)
+            sig["or_reset"] = ([p], ctypes.c_int)
         for name, (args, res) in sig.items():
             f = getattr(lib, name)
             f.argtypes = args
@@ -174,6 +176,14 @@ class OracleNet:
 
     def step(self):
         self._chk(self.lib.or_step(self.h))
+
+    def snapshot(self):
+        """Keep a copy of the network as it is now (restated oracle)."""
+        self._chk(self.lib.or_snapshot(self.h))
+
+    def reset(self):
+        """Return to the snapshot: step 0, no messages in flight (restated oracle)."""
+        self._chk(self.lib.or_reset(self.h))
 
     def step_mt(self, threads: int):
         """One step with the reference multi-threaded backend's structure (timing only)."""
