@@ -57,6 +57,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def bf16_peak():
+    """Dense BF16 burst peak (TFLOP/s) measured with cuBLAS on this GPU model, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 class Clocks:
     """nvidia-smi sampler (SM clock, max clock, throttle reasons) running during the timed region."""
 
@@ -417,17 +426,23 @@ def bptt_measure(device: int, iters: int = 10, warmup: int = 3):
         opt.step()
         return loss
 
-    for _ in range(warmup):
-        it()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(iters):
-        loss = it()
-    e1.record()
-    torch.cuda.synchronize(dev)
-    bptt.check_gemm_errors(dev)
-    ms = e0.elapsed_time(e1) / iters
+    def timed(step):
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            out = step()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        bptt.check_gemm_errors(dev)
+        return e0.elapsed_time(e1) / iters, float(out.item())
+
+    ms_eager, _ = timed(it)
+    # The same iteration captured as one CUDA graph (the eager loop is bound by ~70 launches from Python).
+    graphed = bptt.GraphedTrainStep(model, opt, x, labels)
+    ms, loss = timed(graphed)
     layers = [(784, 512), (512, 512), (512, 10)]
     tb = 32 * 128
     # Algorithmic: forward GEMMs, recomputed inputs, weight and input gradients (4 per layer, no
@@ -438,11 +453,72 @@ def bptt_measure(device: int, iters: int = 10, warmup: int = 3):
     flops = fwd * 4 - first
     executed = fwd * 2 + 2 * (fwd * 2 - first)
     return {"workload": "bptt: LIF 784-512-512-10, batch 128, T 32, checkpoint 8", "ms_per_iter": ms,
+            "execution": "one CUDA graph per iteration (forward, backward, SGD step)", "ms_per_iter_eager": ms_eager,
             "gemm_flops_per_iter": flops, "achieved_tflops": flops / (ms / 1e3) / 1e12,
             "tensor_flops_executed_per_iter": executed,
-            "gemm": "tcgen05 BF16 (knp_gb300_bf16_gemm_tn, pipelined 128x128 tiles), FP32 accumulation; "
-                    "gradients as BF16 hi + lo",
-            "loss": float(loss.item())}
+            "gemm": "tcgen05 BF16 (knp_gb300_bf16_gemm_tn: TMA-fed 128x128 tiles, 128-byte swizzle, split K "
+                    "when tiles are few), FP32 accumulation; gradients as BF16 hi + lo",
+            "loss": loss}
+
+
+GEMM_SHAPES = [(4096, 512, 784), (784, 512, 8192), (512, 512, 8192), (4096, 784, 1024), (8192, 8192, 8192)]
+
+
+def gemm_measure(device: int, shapes=None, reps: int = 20):
+    """The tcgen05 BF16 GEMM (D = A B^T, FP32 accumulation) alone on the BPTT step's shapes and one
+    large square, through the C ABI: `reps` calls captured in one CUDA graph (so the time is the
+    kernels', not Python's), replayed 3 times untimed then once timed with CUDA events; achieved
+    TFLOP/s against the measured cuBLAS BF16 burst peak."""
+    import ctypes
+
+    import torch
+
+    from knp_gb300 import _capi
+
+    dev = torch.device(f"cuda:{device}")
+    torch.cuda.set_device(dev)
+    peak, peak_source = bf16_peak()
+    lib = _capi.lib()
+    out = []
+    for M, N, K in shapes or GEMM_SHAPES:
+        g = torch.Generator(device="cpu").manual_seed(M + N + K)
+        a = (torch.rand(M, K, generator=g) < 0.2).to(torch.bfloat16).to(dev)
+        b = torch.randn(N, K, generator=g).to(torch.bfloat16).to(dev)
+        d = torch.empty(M, N, device=dev, dtype=torch.float32)
+        err = torch.zeros(1, device=dev, dtype=torch.int32)
+
+        def call():
+            _capi.check(lib.knp_gb300_bf16_gemm_tn(
+                ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(d.data_ptr()), M, N, K,
+                ctypes.c_void_p(err.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            call()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for _ in range(reps):
+                call()
+        for _ in range(3):
+            graph.replay()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        graph.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        if int(err.item()) != 0:
+            raise RuntimeError("a tcgen05 GEMM completion wait timed out")
+        max_err = float((d - a.float() @ b.float().t()).abs().max().item())
+        tf = 2.0 * M * N * K / (us * 1e-6) / 1e12
+        out.append({"M": M, "N": N, "K": K, "us": us, "tflops": tf, "frac": tf / peak, "max_abs_err_vs_fp32": max_err})
+        del graph
+    return {"workload": "bf16 GEMM D = A B^T (A 0/1 spikes, B normal), FP32 accumulation, "
+                        f"{reps} calls per CUDA graph, L2-resident operands",
+            "peak_tflops": peak, "peak_source": peak_source + " cuBLAS bf16 burst", "shapes": out}
 
 
 def run_reference(args):
@@ -517,8 +593,10 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched dense, BPTT and STDP measurements")
     ap.add_argument("--no-extra-windows", action="store_true",
                     help="skip the saturated window and the per-phase kernels on the timed window")
-    ap.add_argument("--form", default="all", choices=["all", "batched", "bptt", "stdp"],
-                    help="measure one form alone: the batched dense form, the BPTT step or the STDP config (profiling runs)")
+    ap.add_argument("--form", default="all", choices=["all", "batched", "bptt", "stdp", "gemm"],
+                    help="measure one form alone: the batched dense form, the BPTT step, the STDP config or the "
+                         "tcgen05 GEMM (profiling runs)")
+    ap.add_argument("--gemm-shape", default=None, help="M,N,K: the GEMM form on this shape alone")
     ap.add_argument("--neurons", type=int, default=N, help="population size (profiling cases only)")
     ap.add_argument("--fan-in", type=int, default=FAN_IN, help="fan-in (profiling cases only)")
     ap.add_argument("--pull-threshold", type=float, default=0.1,
@@ -531,7 +609,11 @@ def main():
     if args.form != "all":
         # One form alone (profiling runs): prints that form's measurement as one JSON line.
         local = int(os.environ.get("LOCAL_RANK", "0"))
-        out = {"batched": batched_dense_measure, "bptt": bptt_measure, "stdp": stdp_measure}[args.form](local)
+        if args.form == "gemm":
+            shapes = [tuple(int(v) for v in args.gemm_shape.split(","))] if args.gemm_shape else None
+            out = gemm_measure(local, shapes)
+        else:
+            out = {"batched": batched_dense_measure, "bptt": bptt_measure, "stdp": stdp_measure}[args.form](local)
         print(json.dumps({"form": args.form, **out}))
         return
 

@@ -165,6 +165,37 @@ def loss_fn(counts, labels):
     return torch.nn.functional.cross_entropy(counts, labels)
 
 
+class GraphedTrainStep:
+    """One training iteration (forward, loss, backward, optimizer step) on the static tensors ``x`` and
+    ``labels``, captured once as a CUDA graph and replayed by ``__call__``; the iteration's ~70
+    kernels then cost one launch. New data is copied into ``x`` / ``labels`` in place. The optimizer
+    must be graph-safe (SGD; Adam with ``capturable=True``). Warm-up iterations run on a side stream
+    first, as torch's graph capture asks."""
+
+    def __init__(self, model: torch.nn.Module, opt: torch.optim.Optimizer, x: torch.Tensor, labels: torch.Tensor,
+                 warmup: int = 3):
+        self.x, self.labels = x, labels
+        side = torch.cuda.Stream(device=x.device)
+        side.wait_stream(torch.cuda.current_stream(x.device))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                opt.zero_grad(set_to_none=True)
+                loss_fn(model(x), labels).backward()
+                opt.step()
+        torch.cuda.current_stream(x.device).wait_stream(side)
+        opt.zero_grad(set_to_none=True)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = loss_fn(model(x), labels)
+            self.loss.backward()
+            opt.step()
+
+    def __call__(self) -> torch.Tensor:
+        """Replays the iteration on torch's current stream; returns the (static) loss tensor."""
+        self.graph.replay()
+        return self.loss
+
+
 def make_batch(T=32, B=128, n_in=784, n_classes=10, max_rate=0.3, seed=0, device="cuda"):
     """Bernoulli input spikes with per-(sample, input) rate uniform in [0, max_rate]; random labels."""
     g = torch.Generator(device="cpu").manual_seed(seed)

@@ -9,8 +9,21 @@
 // of later chunks overlap the MMAs of earlier ones. The same four warps then read the accumulator
 // (tcgen05.ld, one row per thread) and store it. Every wait is bounded: a timeout sets bit 0 of
 // *err, stops the loops, drains the issued MMAs (bounded) and frees the tensor memory.
+//
+// When K is a multiple of 8, the chunks are loaded by TMA instead (gemm_tma_kernel): each operand is
+// described to the TMA unit as a 2-D tensor (K, rows) whose 64 x 128 box (128 bytes of K per row)
+// lands in shared memory in the 128-byte swizzled K-major layout the MMA reads directly; one thread
+// issues the two copies of a stage and the stage's mbarrier counts their bytes; rows and K past the
+// matrix edge arrive as zeros. Tiles are few when M and N are small and K large (weight gradients):
+// the K range is then split over up to 16 CTAs per tile, each writing its partial tile to a
+// workspace, and a second kernel adds the partials in split order, so results
+// do not depend on scheduling.
+#include <algorithm>
 #include <cstdint>
+#include <map>
+#include <mutex>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -203,6 +216,221 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_pipe_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, kBN);
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMA load of the 2-D box at (x, y) of `map` into shared memory at `dst`, completing its bytes on the
+// mbarrier's transaction count.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc::smem_u32(mbar))
+        : "memory");
+}
+
+constexpr int kTmaStages = 6;
+constexpr int kTmaThreads = 128;
+constexpr uint32_t kTmaSmem = kTmaStages * kStageBytes + 1024;  // + alignment slack
+
+// One 128 x 128 tile of D (or of split blockIdx.z's partial, into `out` with row stride N) over
+// chunks [blockIdx.z * cps, min(nk, (blockIdx.z + 1) * cps)). Warp 0 lane 0 issues the TMA copies,
+// warp 1 lane 0 the MMAs; all four warps read the accumulator back.
+__global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
+    const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *__restrict__ out, int M,
+    int N, int K, int cps, size_t split_stride, unsigned int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], acc_full, drain;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int nk = (K + kBK - 1) / kBK;
+    const int c0 = blockIdx.z * cps, c1 = min(nk, c0 + cps);
+    float *dst = out + blockIdx.z * split_stride;
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, kBN);
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < kTmaStages; ++s)
+        {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(&acc_full, 1);
+        tc::mbar_init(&drain, 1);
+        s_fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t base = (tc::smem_u32(smem) + 1023u) & ~1023u;  // TMA boxes on 1024-byte boundaries
+
+    if (warp == 0 && lane == 0)
+    {
+        int issued = 0;
+        for (int c = c0; c < c1; ++c)
+        {
+            const int i = c - c0, s = i % kTmaStages;
+            if (i >= kTmaStages && !wait_or_fail(&empty[s], ((i / kTmaStages) - 1) & 1, &s_fail))
+            {
+                s_fail = 1;
+                break;
+            }
+            const uint32_t sa = base + s * kStageBytes;
+            mbar_expect_tx(&full[s], kStageBytes);
+            tma_load_2d(sa, &ta, c * kBK, m0, &full[s]);
+            tma_load_2d(sa + kTileBytes, &tb, c * kBK, n0, &full[s]);
+            issued = i + 1;
+        }
+        // Copies still in flight after a failed wait land before the CTA leaves (bounded).
+        for (int i = max(0, issued - kTmaStages); i < issued; ++i)
+            if (!tc::mbar_wait(&full[i % kTmaStages], (i / kTmaStages) & 1, kWait)) s_fail = 1;
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+        for (int c = c0; c < c1; ++c)
+        {
+            const int i = c - c0, s = i % kTmaStages;
+            if (!wait_or_fail(&full[s], (i / kTmaStages) & 1, &s_fail))
+            {
+                s_fail = 1;
+                break;
+            }
+            tc::fence_after_sync();
+            const uint32_t sa = base + s * kStageBytes, sb = sa + kTileBytes;
+#pragma unroll
+            for (int j = 0; j < kBK / 16; ++j)
+                tc::mma_bf16(tmem, tc::smem_desc_sw128(sa + j * 32, 1024), tc::smem_desc_sw128(sb + j * 32, 1024),
+                             idesc, (i > 0 || j > 0) ? 1u : 0u);
+            tc::commit(&empty[s]);
+        }
+        tc::commit(&acc_full);
+        tc::commit(&drain);
+        if (!tc::mbar_wait(&drain, 0, kWait)) s_fail = 1;
+    }
+    __syncwarp();
+    // Epilogue: thread t reads accumulator lane t (row m0 + t); an empty chunk range leaves zeros.
+    const bool done = c1 <= c0 || wait_or_fail(&acc_full, 0, &s_fail);
+    tc::fence_after_sync();
+    const bool ok = tc::named_sync_and(1, kTmaThreads, done && !s_fail);
+    if (ok)
+    {
+        const int row = m0 + threadIdx.x;
+        const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
+#pragma unroll 1
+        for (int q0 = 0; q0 < kBN; q0 += 16)
+        {
+            float v[16];
+            if (c1 > c0)
+                tc::tmem_ld16(tmem + lane_base + q0, v);
+            else
+                for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+            if (row < M)
+            {
+                float *d = dst + static_cast<size_t>(row) * N + n0 + q0;
+                if (n0 + q0 + 16 <= N && (reinterpret_cast<uintptr_t>(d) & 15u) == 0)
+                {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        reinterpret_cast<float4 *>(d)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+                else
+                {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i)
+                        if (n0 + q0 + i < N) d[i] = v[i];
+                }
+            }
+        }
+    }
+    else if (threadIdx.x == 0)
+    {
+        atomicOr(err, 1u);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kBN);
+}
+
+// D = sum over the splits of ws[z] (split order), n elements.
+__global__ void split_sum_kernel(const float *__restrict__ ws, float *__restrict__ D, size_t n, int splits)
+{
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    {
+        float s = ws[i];
+        for (int z = 1; z < splits; ++z) s = __fadd_rn(s, ws[z * n + i]);
+        D[i] = s;
+    }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled()
+{
+    static EncodeTiled fn = []
+    {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+        {
+            cudaGetLastError();
+            return static_cast<EncodeTiled>(nullptr);
+        }
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+// The (K, rows) view of a row-major [rows][K] BF16 matrix (K a multiple of 8), loaded in 64 x 128
+// boxes with the 128-byte swizzle.
+bool sw128_map(CUtensorMap *map, const void *ptr, int rows, int K)
+{
+    const EncodeTiled fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * 2};
+    const cuuint32_t box[2] = {kBK, kBM};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Stream-ordered pool of the split-K workspaces of device `dev` (memory kept by the pool between
+// calls). Allocating on the call's stream keeps concurrent streams apart and lets a call be captured
+// in a CUDA graph (the allocation becomes a graph memory node).
+cudaMemPool_t split_pool(int dev)
+{
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = pools.find(dev);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return pools[dev] = nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    return pools[dev] = pool;
+}
+
 }  // namespace
 }  // namespace knp_gb300
 
@@ -217,6 +445,47 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
     if (M < 1 || N < 1 || K < 1 || !A || !B || !D || !d_err) return -1;
     const bool aligned = K % 8 == 0 && (reinterpret_cast<uintptr_t>(A) & 15u) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0;
     if (!aligned) return bf16_gemm_tn_simple(A, B, D, M, N, K, d_err, s);
+    CUtensorMap ta, tb;
+    if (sw128_map(&ta, A, M, K) && sw128_map(&tb, B, N, K))
+    {
+        static const cudaError_t attr_tma = cudaFuncSetAttribute(
+            gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem);
+        if (attr_tma != cudaSuccess) return -3;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int tiles_m = (M + kBM - 1) / kBM, tiles_n = (N + kBN - 1) / kBN, tiles = tiles_m * tiles_n;
+        const int nk = (K + kBK - 1) / kBK;
+        // Split K when the tiles leave most SMs idle and each split keeps at least 4 chunks.
+        int splits = 1;
+        if (tiles * 2 <= sms) splits = std::max(1, std::min({16, nk / 4, sms / tiles}));
+        const int cps = (nk + splits - 1) / splits;
+        splits = (nk + cps - 1) / cps;
+        const size_t mn = static_cast<size_t>(M) * N;
+        float *ws = nullptr;
+        if (splits > 1)
+        {
+            const cudaMemPool_t pool = split_pool(dev);
+            if (!pool || cudaMallocFromPoolAsync(reinterpret_cast<void **>(&ws), mn * splits * sizeof(float), pool, s) !=
+                             cudaSuccess)
+            {
+                cudaGetLastError();
+                ws = nullptr;
+                splits = 1;
+            }
+        }
+        const int cps_used = splits > 1 ? cps : nk;
+        dim3 grid(tiles_m, tiles_n, splits);
+        gemm_tma_kernel<<<grid, kTmaThreads, kTmaSmem, s>>>(ta, tb, splits > 1 ? ws : D, M, N, K,
+                                                                              cps_used, splits > 1 ? mn : 0, d_err);
+        if (splits > 1)
+        {
+            const int blocks = static_cast<int>(std::min<size_t>((mn + 255) / 256, 8ull * sms));
+            split_sum_kernel<<<blocks, 256, 0, s>>>(ws, D, mn, splits);
+            cudaFreeAsync(ws, s);
+        }
+        return cudaGetLastError() == cudaSuccess ? 0 : -3;
+    }
     static const cudaError_t attr =
         cudaFuncSetAttribute(gemm_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStages * kStageBytes);
     if (attr != cudaSuccess) return -3;

@@ -130,9 +130,11 @@ __device__ __forceinline__ unsigned long long scatter_rows(
     const uint32_t (&cnt)[kMaxSources], uint32_t total, uint32_t warp, uint32_t n_warps, int lane)
 {
     unsigned long long events = 0;
-    // Few spikes for many warps: each row is split over F warps (warp f of a row takes its 128-synapse
-    // rounds f, f + F, ...), so one long row does not serialise the step.
-    const uint32_t F = total ? max(1u, min(8u, n_warps / total)) : 1u;
+    // Each row is split over F warps (warp f of a row takes its 128-synapse rounds f, f + F, ...), so
+    // that one long row does not serialise the step and the rows' parts spread evenly over the warps:
+    // about four parts per warp (with whole rows, 1.25 rows per warp would leave a quarter of the warps
+    // a second full row while the rest idle).
+    const uint32_t F = total ? max(1u, min(8u, (4u * n_warps) / total)) : 1u;
     for (uint32_t it = warp; it < total * F; it += n_warps)
     {
         const uint32_t j = it / F, f = it - j * F;

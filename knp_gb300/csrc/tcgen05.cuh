@@ -27,6 +27,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return d;
 }
 
+// Descriptor of a K-major operand in the 128-byte swizzled layout (the one a TMA load with
+// SWIZZLE_128B writes): row r of the tile at r * 128 bytes, its 16-byte chunk j at chunk j ^ (r % 8),
+// 8-row groups `sbo` bytes apart; the tile starts on a 1024-byte boundary, and the K step of an MMA
+// inside the 128-byte row is an offset of the start address.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr, uint32_t sbo)
+{
+    uint64_t d = static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+    d |= 1ull << 16;  // leading offset: unused for swizzled K-major operands
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= 1ull << 46;  // descriptor version of tcgen05
+    d |= 2ull << 61;  // 128-byte swizzle
+    return d;
+}
+
 __device__ __forceinline__ uint32_t core_offset(uint32_t r, uint32_t k, uint32_t lbo, uint32_t sbo)
 {
     return (r >> 3) * sbo + (k >> 3) * lbo + (r & 7u) * 16u + (k & 7u) * 2u;

@@ -26,7 +26,8 @@ def _gemm(a, b):
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 64, 16), (200, 100, 784), (256, 1000, 1000), (37, 10, 1000),
-                                   (300, 260, 8192), (4096, 512, 784), (129, 129, 72), (512, 10, 8200)])
+                                   (300, 260, 8192), (4096, 512, 784), (129, 129, 72), (512, 10, 8200),
+                                   (304, 256, 8192), (512, 64, 4104), (136, 8, 512)])
 def test_bf16_gemm_tn(M, N, K):
     g = torch.Generator(device="cpu").manual_seed(M * 7 + N + K)
     a = (torch.rand(M, K, generator=g) < 0.2).to(torch.bfloat16).cuda()  # 0/1 spike matrix
@@ -34,6 +35,18 @@ def test_bf16_gemm_tn(M, N, K):
     ref = a.float() @ b.float().t()
     d = _gemm(a, b)
     torch.testing.assert_close(d, ref, rtol=1e-5, atol=1e-5)
+
+
+def test_bf16_gemm_tn_split_k_is_deterministic():
+    """Few tiles and a long K take the split-K form; its partial tiles are added in split order, so
+    repeated calls give the same bits."""
+    g = torch.Generator(device="cpu").manual_seed(11)
+    a = torch.randn(256, 8192, generator=g).to(torch.bfloat16).cuda()
+    b = torch.randn(128, 8192, generator=g).to(torch.bfloat16).cuda()
+    d0 = _gemm(a, b)
+    for _ in range(3):
+        assert torch.equal(_gemm(a, b), d0)
+    torch.testing.assert_close(d0, a.float() @ b.float().t(), rtol=1e-5, atol=1e-3)
 
 
 def test_bf16_gemm_tn_dense_values():

@@ -107,3 +107,29 @@ def test_bptt_full_config_runs_and_learns():
         losses.append(loss.item())
     assert all(torch.isfinite(torch.tensor(losses)))
     assert losses[-1] < losses[0], losses
+
+
+def test_graphed_train_step_matches_eager_steps():
+    """GraphedTrainStep (the iteration captured once as a CUDA graph) takes the same SGD steps as the
+    eager loop: after 3 warm-up + 4 replayed iterations the weights and the loss equal those of 7 eager
+    iterations bit for bit (every kernel of the iteration is deterministic, split-K GEMMs included)."""
+    from knp_gb300 import bptt
+
+    x, labels = bptt.make_batch(T=16, B=64, seed=5)
+    eager = bptt.SpikingMLP(sizes=(784, 256, 10), checkpoint=8, seed=4)
+    graphed = bptt.SpikingMLP(sizes=(784, 256, 10), checkpoint=8, seed=4)
+    opt_e = torch.optim.SGD(eager.parameters(), lr=1e-3)
+    opt_g = torch.optim.SGD(graphed.parameters(), lr=1e-3)
+    for _ in range(7):
+        opt_e.zero_grad(set_to_none=True)
+        loss_e = bptt.loss_fn(eager(x), labels)
+        loss_e.backward()
+        opt_e.step()
+    step = bptt.GraphedTrainStep(graphed, opt_g, x, labels, warmup=3)
+    for _ in range(4):
+        loss_g = step()
+    torch.cuda.synchronize()
+    bptt.check_gemm_errors()
+    assert torch.equal(loss_g, loss_e)
+    for a, b in zip(eager.weights, graphed.weights):
+        assert torch.equal(a, b)
