@@ -45,6 +45,7 @@ SEED = 2
 N = 1_000_000
 FAN_IN = 1000
 P_BG = 0.005
+RING_SLOTS = 20  # input ring slots per neuron: the config's largest delay
 GATHER_DRAM_BYTES_PER_SYNAPSE = (677.2e6 + 3.05e6) / 2e8
 
 
@@ -521,6 +522,21 @@ def gemm_measure(device: int, shapes=None, reps: int = 20):
             "peak_tflops": peak, "peak_source": peak_source + " cuBLAS bf16 burst", "shapes": out}
 
 
+def add_rate_ceiling(device: int, n_floats: int, n_adds: int) -> float:
+    """Measured ceiling of the scatter's ring adds: FP32 atomic adds at uniformly random positions of
+    an `n_floats` buffer (knp_gb300_measure_add_rate, about `n_adds` adds per timed launch), adds/s."""
+    import ctypes
+
+    import torch
+
+    from knp_gb300 import _capi
+
+    torch.cuda.set_device(device)
+    rate = ctypes.c_double(0.0)
+    _capi.check(_capi.lib().knp_gb300_measure_add_rate(n_floats, n_adds, ctypes.byref(rate)))
+    return rate.value
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -633,6 +649,8 @@ def main():
 
     modes = {"auto": None, "phases": T.STEP_PHASES, "grid": T.STEP_GRID}
     n_neurons, W, K = args.neurons, args.warmup, args.steps
+    # Ceiling of the scatter's ring adds, measured before any backend holds memory or an L2 set-aside.
+    ceiling = add_rate_ceiling(local, RING_SLOTS * n_neurons, 100_000_000) if rank == 0 else None
     sat0, sat_steps = max(W + K, 40), 20  # a window of saturated steps (every neuron fires every step)
     total_steps = sat0 + sat_steps
     chan_seed = SEED + 1000 * rank
@@ -671,8 +689,12 @@ def main():
                 "bytes_model": "9 B per synaptic event + 32 B per neuron update + 8 B per spike row",
                 "traffic": None}
     per_step_share = spikes / (n_neurons * K)
-    regime = "sparse (every step below the pull threshold: scattered)" if per_step_share < args.pull_threshold \
-        else "mixed or saturated"
+    if args.pull_threshold < 0:
+        regime = "every step scattered (gather direction off)"
+    elif per_step_share < args.pull_threshold:
+        regime = "sparse (every step below the pull threshold: scattered)"
+    else:
+        regime = "mixed or saturated"
 
     extra = {}
     if rank == 0 and not args.no_extra_windows:
@@ -689,6 +711,35 @@ def main():
             "effective_frac": ab / (ms_sat / 1e3) / 1e9 / hbm,
             "note": "effective: the plan's 9 B per event over the step time; the gather layout moves 4 B per "
                     "synapse (dictionary weights, target and delay implied), so this can exceed 1"}
+        # The persistent kernel's own phase times on the same window (global-timer stamps of CTA 0),
+        # each phase against its bound: the population phase streams 32 B per neuron from HBM; the
+        # scatter phase is one random FP32 add per synaptic event into the input rings (84 MB, held
+        # in L2), bounded by the measured rate of such adds.
+        if step_kernel == T.STEP_GRID:
+            bg, _, cg = large_backend(local, n_neurons, args.fan_in, args.pull_threshold, T.STEP_GRID)
+            bg.generate_bernoulli_schedule(cg, n_neurons, P_BG, 0, W + K, seed=chan_seed)
+            bg.step(W)
+            g0, _, _ = bg.counters()
+            us = bg.profile_grid_phases(K)
+            g1, _, _ = bg.counters()
+            bg.close()
+            pop_bytes = 32.0 * n_neurons * K
+            roofline["phases"] = {
+                "us_per_step": {"populations": us[0] / K, "projections": us[1] / K, "gathers": us[2] / K},
+                "same_events": bool(g1 - g0 == events),
+                "populations": {"bound": "hbm", "achieved": pop_bytes / (us[0] * 1e-6) / 1e9, "peak": hbm,
+                                "unit": "GB/s", "frac": pop_bytes / (us[0] * 1e-6) / 1e9 / hbm,
+                                "bytes_model": "32 B per neuron update"},
+                "projections": {"bound": "l2-atomic", "achieved": events / (us[1] * 1e-6), "peak": ceiling,
+                                "unit": "adds/s", "frac": events / (us[1] * 1e-6) / ceiling,
+                                "peak_source": "measured in this run (knp_gb300_measure_add_rate): FP32 atomic "
+                                               "adds at uniformly random positions of a "
+                                               f"{RING_SLOTS * n_neurons * 4 // 10**6} MB buffer (the input rings' "
+                                               "size), 100M adds per launch, measured before the backends were "
+                                               "built (no L2 set-aside), no other traffic"},
+                "whole_step_bound_us": (pop_bytes / (hbm * 1e9) + events / ceiling) * 1e6 / K,
+                "whole_step_frac": (pop_bytes / (hbm * 1e9) + events / ceiling) / (ms / 1e3),
+            }
         # The per-phase kernels on the same timed window (for comparison with the persistent kernel).
         if step_kernel == T.STEP_GRID:
             bp, _, cp = large_backend(local, n_neurons, args.fan_in, args.pull_threshold, T.STEP_PHASES)

@@ -371,6 +371,24 @@ KNP_GB300_API int knp_gb300_step_timed(knp_gb300_backend *b, uint64_t n_steps, f
  */
 KNP_GB300_API int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms);
 
+/**
+ * Runs n_steps normal steps (knp_gb300_step; results equal its own) on a backend that steps with the
+ * persistent grid kernel (KNP_GB300_E_STATE otherwise, or with host messages pending), timing each
+ * step's phases on the device's global timer: us[0] populations (and the previous step's STDP
+ * rules), us[1] projections (scatter, or spike bitmaps of gathered steps), us[2] gathers and
+ * bitmap clearing; each summed over the steps, a phase ending when every CTA has finished it.
+ * A measurement aid beside knp_gb300_step_timed (no reference counterpart).
+ */
+KNP_GB300_API int knp_gb300_profile_grid_phases(knp_gb300_backend *b, uint64_t n_steps, double *us);
+
+/**
+ * Measures, on the current device, the rate of FP32 atomic adds at uniformly random positions of an
+ * n_floats buffer (0 < n_floats < 2^32) (about n_adds adds, three timed launches after one warm-up): the ceiling of the
+ * scatter's ring adds when n_floats is the input rings' size. A measurement aid for the scatter's
+ * roofline (no reference counterpart). Allocates and frees the buffer; synchronous.
+ */
+KNP_GB300_API int knp_gb300_measure_add_rate(uint64_t n_floats, uint64_t n_adds, double *adds_per_s);
+
 /*
  * Differentiation form (no reference counterpart: KNP has no gradient-based training). LIF layer
  * recurrence over T steps for BN = batch x neurons independent neurons, device buffers laid out

@@ -214,6 +214,13 @@ class GB300Backend:
         self._chk(self._lib.knp_gb300_profile_phases(self._h, n, ms))
         return np.array(list(ms), dtype=np.float64)
 
+    def profile_grid_phases(self, n: int):
+        """Device microseconds of (populations, projections, gathers) summed over ``n`` normal steps
+        of the persistent grid kernel, from the kernel's own global-timer stamps."""
+        us = (ctypes.c_double * 3)()
+        self._chk(self._lib.knp_gb300_profile_grid_phases(self._h, n, us))
+        return np.array(list(us), dtype=np.float64)
+
     def get_step(self) -> int:
         s = ctypes.c_uint64(0)
         self._chk(self._lib.knp_gb300_get_step(self._h, ctypes.byref(s)))

@@ -378,6 +378,12 @@ int knp_gb300_profile_phases(knp_gb300_backend *b, uint64_t n_steps, float *ms)
     return guarded([&] { b->impl.profile_phases(n_steps, ms); });
 }
 
+int knp_gb300_profile_grid_phases(knp_gb300_backend *b, uint64_t n_steps, double *us)
+{
+    if (!b || !us) return null_handle();
+    return guarded([&] { b->impl.profile_grid_phases(n_steps, us); });
+}
+
 int knp_gb300_lif_scan_forward(
     const float *I, float *S, float *ckpt, int T, int64_t BN, float beta, float theta, int K, int relaxed, float k,
     void *stream)
@@ -419,6 +425,19 @@ int knp_gb300_generate_bernoulli_schedule_noalloc(
     if (rc == 0) return KNP_GB300_OK;
     g_error = why;
     return rc == -3 ? KNP_GB300_E_CUDA : KNP_GB300_E_INVALID;
+}
+
+int knp_gb300_measure_add_rate(uint64_t n_floats, uint64_t n_adds, double *adds_per_s)
+{
+    if (!adds_per_s || n_floats == 0 || n_floats > 0xFFFFFFFFull || n_adds == 0)
+    {
+        g_error = "n_floats (below 2^32) and n_adds must be positive, adds_per_s not null";
+        return KNP_GB300_E_INVALID;
+    }
+    const char *why = "";
+    if (knp_gb300::measure_add_rate(n_floats, n_adds, adds_per_s, &why) == 0) return KNP_GB300_OK;
+    g_error = why;
+    return KNP_GB300_E_CUDA;
 }
 
 int knp_gb300_bf16_gemm_tn(

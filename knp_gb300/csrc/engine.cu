@@ -1820,6 +1820,42 @@ float Backend::step_timed(uint64_t n)
     return ms;
 }
 
+void Backend::profile_grid_phases(uint64_t n, double *us)
+{
+    require_init("profile_grid_phases");
+    KNP_CUDA(cudaSetDevice(device_));
+    if (!grid_) throw Error(KNP_GB300_E_STATE, "the backend does not step with the persistent grid kernel");
+    bool host_inputs = !pending_impacts_.empty();
+    for (auto &c : channels_) host_inputs = host_inputs || c->has_pending;
+    if (host_inputs) throw Error(KNP_GB300_E_STATE, "profile_grid_phases does not stage host messages");
+    unsigned long long *acc = nullptr;
+    KNP_CUDA(cudaMalloc(&acc, 3 * sizeof(unsigned long long)));
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t err = cudaMemsetAsync(acc, 0, sizeof(h), stream_);
+    if (err == cudaSuccess)
+    {
+        grid_net_.phase_ns = acc;
+        try
+        {
+            step(n);
+        }
+        catch (...)
+        {
+            grid_net_.phase_ns = nullptr;
+            cudaStreamSynchronize(stream_);
+            cudaFree(acc);
+            throw;
+        }
+        grid_net_.phase_ns = nullptr;
+        err = cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, stream_);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(stream_);
+    }
+    cudaFree(acc);
+    KNP_CUDA(err);
+    check_device_error();
+    for (int k = 0; k < 3; ++k) us[k] = static_cast<double>(h[k]) * 1e-3;
+}
+
 void Backend::profile_phases(uint64_t n, float *ms)
 {
     require_init("profile_phases");

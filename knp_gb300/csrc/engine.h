@@ -260,6 +260,7 @@ public:
     void step(uint64_t n);
     float step_timed(uint64_t n);
     void profile_phases(uint64_t n, float *ms);
+    void profile_grid_phases(uint64_t n, double *us);
     uint64_t current_step() const { return step_; }
     void read_spikes(const Uid &pop, uint64_t step, uint32_t cap, uint32_t *out, uint32_t *n);
     void discard_spikes(uint64_t before);

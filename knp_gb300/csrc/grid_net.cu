@@ -10,11 +10,12 @@
 //   A: the populations of step t beside the STDP rules of step t - 1;
 //   B: the projections of step t (scatter of the spike rows into the input rings, or, for a step
 //      whose spike count reaches a projection's pull threshold, its spike bitmap), beside the
-//      retirement of step t - 1's per-step counters;
-//   C: for projections with a gather layout, the gather that completes step t + 1's input from the
-//      bitmaps of earlier steps, and the clearing of the bitmap slot step t + 1 will fill.
-// A grid barrier follows phase A and phase B; one follows phase C only when a gather had work (its
-// ring writes are the next step's input). This keeps the order of the
+//      retirement of step t - 1's per-step counters and the clearing of the bitmap slot step t + 1
+//      will fill;
+//   C: only when a step of a gather's delay window was pulled (every CTA takes the same decision in
+//      phase B), the gathers that complete step t + 1's input from the bitmaps of earlier steps.
+// A grid barrier follows phase A and phase B, and phase C when it runs (its ring writes are the next
+// step's input). This keeps the order of the
 // single-threaded backend's step (backend.cpp:89-141 of the reference) for every datum, as the
 // per-phase kernels do. The per-neuron, per-synapse and per-column code is theirs
 // (population_dev.cuh, projection_dev.cuh, pull_dev.cuh, stdp_dev.cuh) over the same device layout
@@ -95,6 +96,24 @@ __device__ __forceinline__ bool grid_sync(unsigned long long *bar, Control *ctl,
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// Whether a step of the gather's delay window for step t + 1 (t + 1 - d, d = 1 .. max_delay) was
+// pulled: step t from its spike count (the rule of project()), earlier steps from their flags.
+// Every thread of the CTA may call it; threads share the flag reads.
+__device__ __forceinline__ bool pull_window_active(const ProjectionDev &p, unsigned long long t)
+{
+    const PullDev &g = p.pull;
+    if (threadIdx.x == 0 && p.n_src != 0)
+    {
+        const uint32_t *idx[kMaxSources];
+        uint32_t cnt[kMaxSources];
+        if (resolve_sources(p, t, idx, cnt) >= g.threshold) return true;
+    }
+    bool need = false;
+    for (uint32_t d = 2 + threadIdx.x; d <= g.max_delay && d <= t + 1; d += blockDim.x)
+        need = need || g.pulled[static_cast<uint32_t>((t + 1 - d) % g.hist_slots)] != 0u;
+    return need;
 }
 
 // One projection's work of step t over the whole grid: the pull decision and bitmap (gather form),
@@ -213,9 +232,19 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
     // Every CTA has read the step number before CTA 0 may advance it (at the end).
     target += G;
     ok = grid_sync(g.barrier, ctl, target);
+    // Phase timer state in shared memory (read by one thread), not in registers held across the loop.
+    __shared__ unsigned long long ts, acc[3];
+    const bool timer = g.phase_ns && blockIdx.x == 0 && threadIdx.x == 0;
+    if (timer) ts = acc[0] = acc[1] = acc[2] = 0;
     uint32_t s = 0;
     for (; ok && s < n_steps; ++s, ++t)
     {
+        if (timer)
+        {
+            const unsigned long long now = global_ns();
+            if (s > 0) acc[2] += now - ts;  // phase C of the previous step
+            ts = now;
+        }
         const bool odd = t & 1u;
         const SmallPop *pops = odd ? net.pops[1] : net.pops[0];
         const ProjectionDev *projs = odd ? net.projs[1] : net.projs[0];
@@ -260,6 +289,12 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
             ok = false;
             break;
         }
+        if (timer)
+        {
+            const unsigned long long now = global_ns();
+            acc[0] += now - ts;
+            ts = now;
+        }
         // ---- phase B: step t - 1's counters are no longer read; projections of step t.
         retire(odd ? net.end[0] : net.end[1], gthread, n_threads, &s_spikes);
         for (uint32_t k = 0; k < net.n_projs; ++k)
@@ -274,6 +309,18 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
                 events += uexc ? project<false, true>(p, t, gthread, n_threads, gwarp, n_warps, lane)
                                : project<false, false>(p, t, gthread, n_threads, gwarp, n_warps, lane);
         }
+        // Gathers complete step t + 1's input when a step of their delay window was pulled: every CTA
+        // takes the same decision from this step's spike counts (the pulled flag of step t is being
+        // written in this phase) and the flags of earlier steps. The bitmap slot step t + 1 fills
+        // holds step t - max_delay, which the last gathers (of step t - 1) have read.
+        bool need = false;
+        for (uint32_t k = 0; k < g.n_pull; ++k)
+        {
+            const ProjectionDev &p = projs[g.pull[k]];
+            clear_bitmap_slot(p.pull, t + 1, blockIdx.x, G);
+            need = need || pull_window_active(p, t);
+        }
+        need = __syncthreads_or(need) != 0;
         // The scatter's writes (slots t + 1 .. t + D) are complete before step t + 1's populations
         // read slot t + 1, and the step's bitmaps before the gathers read them.
         target += G;
@@ -282,17 +329,14 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
             ok = false;
             break;
         }
-        if (g.n_pull == 0) continue;
-        // ---- phase C: gathers completing step t + 1's input (every projection with a gather
-        // layout clears its next bitmap slot here even when nothing was pulled).
-        bool need = false;
-        for (uint32_t k = 0; k < g.n_pull; ++k) need = gather_needed_block(projs[g.pull[k]].pull, t + 1) || need;
-        if (!need)
+        if (timer)
         {
-            // Nothing was pulled in the gathers' delay window: only the next bitmap slots are cleared.
-            for (uint32_t k = 0; k < g.n_pull; ++k) clear_bitmap_slot(projs[g.pull[k]].pull, t + 1, blockIdx.x, G);
-            continue;
+            const unsigned long long now = global_ns();
+            acc[1] += now - ts;
+            ts = now;
         }
+        if (!need) continue;
+        // ---- phase C: gathers completing step t + 1's input.
         for (uint32_t k = 0; k < g.n_pull; ++k) grid_gather(projs[g.pull[k]], t + 1, grid_smem);
         target += G;
         if (!grid_sync(g.barrier, ctl, target))
@@ -305,6 +349,11 @@ __global__ void __launch_bounds__(kGridThreads, 1) grid_net_kernel(GridNet g, Co
     {
         // A barrier gave up: the host reads kErrGridBarrier; nothing further is stepped.
         return;
+    }
+    if (timer)
+    {
+        if (s > 0) acc[2] += global_ns() - ts;
+        for (int k = 0; k < 3; ++k) g.phase_ns[k] += acc[k];
     }
     // The last step's STDP rules, then its counters: both sets are zero between launches.
     const bool last_odd = (t - 1) & 1u;

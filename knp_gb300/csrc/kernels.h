@@ -384,6 +384,9 @@ struct GridNet
 {
     SmallNet net;
     unsigned long long *barrier;
+    // Optional (nullptr: off): CTA 0 adds the global-timer nanoseconds of phase A, B and C of every
+    // step it runs to phase_ns[0..2] (each phase up to the exit of the barrier that ends it).
+    unsigned long long *phase_ns;
     uint32_t n_pull;
     uint32_t pull[kMaxGridPull];
 };
@@ -395,6 +398,9 @@ void launch_altai(const AltaiDev &p, Control *ctl, cudaStream_t s);
 void launch_altai_blocking(const AltaiDev &p, Control *ctl, cudaStream_t s);
 void launch_lif(const LifDev &p, Control *ctl, cudaStream_t s);
 void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s);
+// Device rate (adds per second) of FP32 atomic adds at uniformly random positions of an n-float
+// buffer, over about `adds` adds (three timed launches after one warm-up); 0, or -3 with *why.
+int measure_add_rate(uint64_t n, uint64_t adds, double *rate, const char **why);
 void launch_stdp_append(const StdpDev &d, SpikeSource src, int both_lists, Control *ctl, cudaStream_t s);
 void launch_stdp_modify(const StdpDev &d, Control *ctl, cudaStream_t s);
 void launch_step_end(const StepEnd &e, Control *ctl, cudaStream_t s);

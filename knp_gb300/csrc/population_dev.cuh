@@ -64,16 +64,20 @@ __device__ __forceinline__ void emit_spikes(
     }
     if (lane == 31) warp_tot[warp] = incl;
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (warp == 0)
     {
-        uint32_t run = 0;
-        for (int w = 0; w < kThreads / 32; ++w)
+        // Exclusive scan of the warps' totals on warp 0's lanes, one block-wide reservation.
+        const uint32_t x = lane < kThreads / 32 ? warp_tot[lane] : 0u;
+        uint32_t run = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            const uint32_t x = warp_tot[w];
-            warp_tot[w] = run;
-            run += x;
+            const uint32_t v = __shfl_up_sync(0xffffffffu, run, o);
+            if (lane >= o) run += v;
         }
-        block_base = run ? atomicAdd(count, run) : 0u;
+        const uint32_t all = __shfl_sync(0xffffffffu, run, 31);
+        if (lane < kThreads / 32) warp_tot[lane] = run - x;
+        if (lane == 0) block_base = all ? atomicAdd(count, all) : 0u;
     }
     __syncthreads();
     if (!c) return;

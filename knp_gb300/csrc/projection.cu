@@ -6,6 +6,7 @@
 // Work distribution: persistent grid; each warp takes whole spike rows (row-major over the
 // concatenated spike lists of all sources) and its 32 lanes stream the row's col / weight / delay
 // arrays with coalesced loads, 4 synapses per lane in flight.
+#include <algorithm>
 #include <cstdint>
 
 #include "kernels.h"
@@ -101,7 +102,62 @@ __global__ void __launch_bounds__(256) projection_kernel(ProjectionDev p, Contro
     if (threadIdx.x == 0 && block_events) atomicAdd(&ctl->events_total, block_events);
 }
 
+// Random FP32 adds of 1/256 into buf[0, n), n < 2^32: thread g's i-th add goes to position
+// floor(h * n / 2^32) of the 32-bit hash h = mix64(seed, g, i) (a multiply, not a division).
+__global__ void add_rate_kernel(float *buf, uint32_t n, uint32_t per, unsigned long long seed)
+{
+    const unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x;
+    for (uint32_t i = 0; i < per; ++i)
+    {
+        const uint32_t h = static_cast<uint32_t>(mix64(seed ^ (g * 0x9E3779B97F4A7C15ull + i)));
+        atomicAdd(buf + __umulhi(h, n), 1.0f / 256.0f);
+    }
+}
+
 }  // namespace
+
+int measure_add_rate(uint64_t n, uint64_t adds, double *rate, const char **why)
+{
+    int device = 0, sms = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (err != cudaSuccess)
+    {
+        *why = cudaGetErrorString(err);
+        return -3;
+    }
+    const uint32_t threads = 512, blocks = 4u * static_cast<uint32_t>(sms);
+    const uint64_t all = static_cast<uint64_t>(threads) * blocks;
+    const uint32_t per = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(adds / all, 1u << 20)));
+    float *buf = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    float ms = 0.f;
+    err = cudaMalloc(&buf, n * sizeof(float));
+    if (err == cudaSuccess) err = cudaMemset(buf, 0, n * sizeof(float));
+    if (err == cudaSuccess) err = cudaEventCreate(&a);
+    if (err == cudaSuccess) err = cudaEventCreate(&b);
+    if (err == cudaSuccess)
+    {
+        const uint32_t n32 = static_cast<uint32_t>(n);
+        add_rate_kernel<<<blocks, threads>>>(buf, n32, per, 1);  // warm-up: the buffer's lines in L2
+        cudaEventRecord(a);
+        for (int r = 0; r < 3; ++r) add_rate_kernel<<<blocks, threads>>>(buf, n32, per, 2 + r);
+        cudaEventRecord(b);
+        err = cudaEventSynchronize(b);
+        if (err == cudaSuccess) err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (buf) cudaFree(buf);
+    if (err != cudaSuccess)
+    {
+        *why = cudaGetErrorString(err);
+        return -3;
+    }
+    *rate = 3.0 * static_cast<double>(all) * per / (static_cast<double>(ms) * 1e-3);
+    return 0;
+}
 
 void launch_projection(const ProjectionDev &p, Control *ctl, int grid, cudaStream_t s)
 {

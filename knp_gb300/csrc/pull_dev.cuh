@@ -62,16 +62,6 @@ __device__ __forceinline__ bool gather_needed(const PullDev &g, unsigned long lo
     return false;
 }
 
-// gather_needed for a whole block (every thread calls it; one flag per thread, the same answer in
-// every thread of the block).
-__device__ __forceinline__ bool gather_needed_block(const PullDev &g, unsigned long long tn)
-{
-    bool need = false;
-    for (uint32_t d = 1 + threadIdx.x; d <= g.max_delay && d <= tn; d += blockDim.x)
-        need = need || g.pulled[static_cast<uint32_t>((tn - d) % g.hist_slots)] != 0u;
-    return __syncthreads_or(need) != 0;
-}
-
 // Clears block `block`'s share (of G) of the bitmap slot that the scatter kernel of step tn will
 // fill; it holds step tn - hist_slots, which no gather reads any more.
 __device__ __forceinline__ void clear_bitmap_slot(const PullDev &g, unsigned long long tn, uint32_t block, uint32_t G)

@@ -32,6 +32,13 @@ def test_binding_loads_and_reports_errors_without_gpu(lib_path):
     # Null handles are rejected before any CUDA call.
     assert lib.knp_gb300_step(None, 1) == -1
     assert b"null" in lib.knp_gb300_last_error()
+    assert lib.knp_gb300_profile_grid_phases(None, 1, None) == -1
+    # Invalid sizes of the add-rate probe are refused before any CUDA call.
+    import ctypes
+
+    rate = ctypes.c_double(0.0)
+    assert lib.knp_gb300_measure_add_rate(0, 10, ctypes.byref(rate)) != 0
+    assert b"positive" in lib.knp_gb300_last_error()
 
 
 def test_library_is_built_for_sm_103a_only():

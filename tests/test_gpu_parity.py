@@ -619,6 +619,52 @@ def test_step_mode_selection_and_recording_change():
         np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t])
 
 
+def test_profile_grid_phases():
+    """knp_gb300_profile_grid_phases: normal steps of the persistent grid kernel (the oracle's spikes)
+    with a positive time for the population and projection phases; refused on a per-phase backend."""
+    from oracle import oracle as orc
+    from knp_gb300 import backend as B
+    from knp_gb300._capi import KnpGb300Error
+
+    net, sched = N.small_network(seed=5, steps=100)
+    pop = net.populations[0].uid
+    o, _ = orc.run(net, sched, 100)
+    b = B.GB300Backend()
+    b.load_network(net)
+    b.set_step_mode(T.STEP_GRID)
+    b._init()
+    for s in sched:
+        b.load_spike_schedule(s)
+    b.step(10)
+    us = b.profile_grid_phases(90)
+    assert us[0] > 0 and us[1] > 0 and us[2] >= 0
+    for t in range(100):
+        np.testing.assert_array_equal(b.spikes(pop, t), o[pop][t])
+    b.close()
+    b = B.GB300Backend()
+    b.load_network(net)
+    b.set_step_mode(T.STEP_PHASES)
+    b._init()
+    with pytest.raises(KnpGb300Error):
+        b.profile_grid_phases(1)
+
+
+def test_measure_add_rate():
+    """knp_gb300_measure_add_rate: a positive, finite rate of random FP32 atomic adds (L2-resident
+    and DRAM-sized buffers)."""
+    import ctypes
+
+    from knp_gb300 import _capi
+
+    lib = _capi.lib()
+    rates = []
+    for n in (1 << 20, 1 << 26):
+        r = ctypes.c_double(0.0)
+        assert lib.knp_gb300_measure_add_rate(n, 1 << 24, ctypes.byref(r)) == 0, lib.knp_gb300_last_error()
+        assert np.isfinite(r.value) and r.value > 1e9
+        rates.append(r.value)
+
+
 @pytest.mark.parametrize("mode", ["auto", "phases", "grid"])
 def test_blocking_synapses_and_impacts(mode):
     """BLOCKING synapses (blifat_impl.h:86): of a step's BLOCKING impacts on a neuron the last in the
