@@ -179,6 +179,25 @@ KNP_GB300_API int knp_gb300_generate_fixed_fan_in_projection(
     uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream);
 
 /**
+ * Generate, on the device, a delta projection by one of the reference's synapse generators
+ * (knp_generator_kind: all_to_all, aligned (the larger size a multiple of the smaller), exclusive
+ * (equal sizes), one_to_one (equal sizes), FixedProbability with
+ * `probability`, FixedNumberPost and FixedNumberPre with `count` synapses; `count` and
+ * `probability` are ignored by the other kinds). Synapse i connects the pair the generator's index
+ * rule gives (FixedProbability: the i-th kept all_to_all pair in index order, each pair kept when
+ * its draw is below the probability); the random choices, weights (k/256, k uniform in
+ * [k_lo, k_hi]) and delays (uniform in [d_lo, d_hi]) are counter-based draws keyed by (seed,
+ * stream), so one seed gives one projection, where the reference draws from std::mt19937 seeded
+ * by std::random_device. knp_gb300/network.py:generated_synapses gives the same synapses on the
+ * host. Replaces: Projection construction from those generators
+ * (knp/base-framework/include/knp/framework/projection/synapse_generators.h:58-457).
+ */
+KNP_GB300_API int knp_gb300_generate_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, int kind, uint32_t n_pre, uint32_t n_post,
+    uint64_t count, double probability, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed,
+    uint64_t stream);
+
+/**
  * Register `pop_uid` in an STDP projection's stdp_populations_ map with processing type
  * KNP_STDP_ONLY or KNP_STDP_AND_SPIKE. Replaces: writing
  * Projection<STDP<...>>::get_shared_parameters().stdp_populations_ (knp/core-library/include/knp/core/projection.h:133-164).

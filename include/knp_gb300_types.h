@@ -57,6 +57,21 @@ typedef enum knp_synapse_kind
     KNP_SYNAPSE_RESOURCE_STDP_DELTA = 2
 } knp_synapse_kind;
 
+/**
+ * Rule of a device-generated projection (knp_gb300_generate_projection); each is the index -> pair
+ * rule of one generator of knp/base-framework/include/knp/framework/projection/synapse_generators.h.
+ */
+typedef enum knp_generator_kind
+{
+    KNP_GEN_ALL_TO_ALL = 0,          /* all_to_all (:59-69): pre = i % n_pre, post = i / n_pre */
+    KNP_GEN_ALIGNED = 1,             /* aligned (:93-120) */
+    KNP_GEN_EXCLUSIVE = 2,           /* exclusive (:139-154): all pairs but pre == post */
+    KNP_GEN_ONE_TO_ONE = 3,          /* one_to_one (:172-178) */
+    KNP_GEN_FIXED_PROBABILITY = 4,   /* FixedProbability (:259-300): all_to_all pairs kept with a probability */
+    KNP_GEN_FIXED_NUMBER_POST = 5,   /* FixedNumberPost (:352-388): pre = i % n_pre, post uniform */
+    KNP_GEN_FIXED_NUMBER_PRE = 6     /* FixedNumberPre (:409-445): pre uniform, post = i % n_post */
+} knp_generator_kind;
+
 /** How an STDP projection treats spikes of one of its STDP populations. */
 typedef enum knp_stdp_processing
 {

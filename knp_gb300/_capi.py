@@ -50,6 +50,8 @@ def lib():
         "knp_gb300_read_lif_population": ([p, U, p], c_int),
         "knp_gb300_load_projection": ([p, U, c_int, U, U, u64, p, p, p, p, p, p, p], c_int),
         "knp_gb300_generate_fixed_fan_in_projection": ([p, U, U, U, u32, u32, u32, i32, i32, u32, u32, u64, u64], c_int),
+        "knp_gb300_generate_projection": ([p, U, U, U, c_int, u32, u32, u64, ctypes.c_double, i32, i32, u32, u32, u64, u64],
+                                          c_int),
         "knp_gb300_set_stdp_population": ([p, U, U, c_int], c_int),
         "knp_gb300_subscribe": ([p, U, U], c_int),
         "knp_gb300_set_accumulator": ([p, U, c_int], c_int),

@@ -139,6 +139,15 @@ class GB300Backend:
             d_lo, d_hi, seed, stream))
         self._projs[uid] = None
 
+    def generate_projection(self, uid, pre_uid, post_uid, kind, n_pre, n_post, k_lo, k_hi, d_lo, d_hi, seed, stream,
+                            count=0, probability=0.0):
+        """Device-side construction of a delta projection by one of the reference's synapse generators
+        (kind: types.GEN_*; see network.generated_synapses for the synapses it gives)."""
+        self._chk(self._lib.knp_gb300_generate_projection(
+            self._h, T.to_c_uid(uid), T.to_c_uid(pre_uid), T.to_c_uid(post_uid), kind, n_pre, n_post, count,
+            probability, k_lo, k_hi, d_lo, d_hi, seed, stream))
+        self._projs[uid] = None
+
     def remove_projections(self, uids):
         """As in the single-threaded backend (backend.h:287): no effect."""
 

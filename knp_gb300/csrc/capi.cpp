@@ -171,8 +171,23 @@ int knp_gb300_generate_fixed_fan_in_projection(
     return guarded(
         [&]
         {
-            b->impl.generate_fixed_fan_in(U(uid), U(pre_uid), U(post_uid), n_pre, n_post, fan_in, k_lo, k_hi, d_lo,
-                                          d_hi, seed, stream);
+            b->impl.generate_projection(U(uid), U(pre_uid), U(post_uid), KNP_GEN_FIXED_NUMBER_PRE, n_pre, n_post,
+                                        static_cast<uint64_t>(n_post) * fan_in, 0.0, k_lo, k_hi, d_lo, d_hi, seed,
+                                        stream);
+        });
+}
+
+int knp_gb300_generate_projection(
+    knp_gb300_backend *b, knp_uid uid, knp_uid pre_uid, knp_uid post_uid, int kind, uint32_t n_pre, uint32_t n_post,
+    uint64_t count, double probability, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed,
+    uint64_t stream)
+{
+    if (!b) return null_handle();
+    return guarded(
+        [&]
+        {
+            b->impl.generate_projection(U(uid), U(pre_uid), U(post_uid), kind, n_pre, n_post, count, probability, k_lo,
+                                        k_hi, d_lo, d_hi, seed, stream);
         });
 }
 

@@ -315,16 +315,87 @@ void Backend::upload_locks()
     }
 }
 
-void Backend::generate_fixed_fan_in(
-    const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint32_t n_pre, uint32_t n_post, uint32_t fan_in,
-    int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream)
+static_assert(kGenAllToAll == KNP_GEN_ALL_TO_ALL && kGenAligned == KNP_GEN_ALIGNED && kGenExclusive == KNP_GEN_EXCLUSIVE &&
+                  kGenOneToOne == KNP_GEN_ONE_TO_ONE && kGenFixedProbability == KNP_GEN_FIXED_PROBABILITY &&
+                  kGenFixedNumberPost == KNP_GEN_FIXED_NUMBER_POST && kGenFixedNumberPre == KNP_GEN_FIXED_NUMBER_PRE,
+              "generator kinds of the C ABI");
+
+GenSpec Backend::gen_spec(const ProjectionSlot &p, const unsigned long long *cand) const
 {
-    require_not_init("generate_fixed_fan_in_projection");
-    const uint64_t n_syn = static_cast<uint64_t>(n_post) * fan_in;
-    if (n_syn > 0xFFFFFFFFull) throw Error(KNP_GB300_E_INVALID, "more than 2^32-1 synapses in one projection");
-    if (k_lo > k_hi || d_lo > d_hi || d_hi > 255 || n_pre == 0)
+    GenSpec g{};
+    g.kind = p.gen.kind;
+    g.n_pre = p.gen.n_pre;
+    g.n_post = p.gen.n_post;
+    g.k_lo = p.gen.k_lo;
+    g.k_hi = p.gen.k_hi;
+    g.d_lo = p.gen.d_lo;
+    g.d_hi = p.gen.d_hi;
+    g.key_pre = stream_key(p.gen.seed, p.gen.stream + 1);
+    g.key_w = stream_key(p.gen.seed, p.gen.stream + 2);
+    g.key_d = stream_key(p.gen.seed, p.gen.stream + 3);
+    g.key_post = stream_key(p.gen.seed, p.gen.stream + 4);
+    g.cand = cand;
+    return g;
+}
+
+void Backend::generate_projection(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, int kind, uint32_t n_pre,
+                                  uint32_t n_post, uint64_t count, double probability, int32_t k_lo, int32_t k_hi,
+                                  uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream)
+{
+    require_not_init("generate_projection");
+    if (k_lo > k_hi || d_lo > d_hi || d_hi > 255 || n_pre == 0 || n_post == 0)
         throw Error(KNP_GB300_E_INVALID, "bad generator ranges");
     if (find_pop(uid) || find_proj(uid)) throw Error(KNP_GB300_E_INVALID, "duplicate UID");
+    uint64_t n_syn = 0, in_degree = 0;
+    unsigned long long thr = 0;
+    switch (kind)
+    {
+        case KNP_GEN_ALL_TO_ALL:
+            n_syn = static_cast<uint64_t>(n_pre) * n_post;
+            in_degree = n_pre;
+            break;
+        case KNP_GEN_ALIGNED:
+            // The larger size a multiple of the smaller (else the reference's rule makes indexes past
+            // the smaller population).
+            if (std::max(n_pre, n_post) % std::min(n_pre, n_post) != 0)
+                throw Error(KNP_GB300_E_INVALID, "aligned: the larger population size must be a multiple of the smaller");
+            n_syn = std::max(n_pre, n_post);
+            in_degree = n_pre >= n_post ? n_pre / n_post : 1;
+            break;
+        case KNP_GEN_EXCLUSIVE:
+            if (n_pre != n_post || n_pre < 2)
+                throw Error(KNP_GB300_E_INVALID, "exclusive: equal population sizes of at least 2");
+            n_syn = static_cast<uint64_t>(n_pre) * (n_pre - 1);
+            in_degree = n_pre - 1;
+            break;
+        case KNP_GEN_ONE_TO_ONE:
+            if (n_pre != n_post) throw Error(KNP_GB300_E_INVALID, "one_to_one: equal population sizes");
+            n_syn = n_pre;
+            in_degree = 1;
+            break;
+        case KNP_GEN_FIXED_PROBABILITY:
+        {
+            if (!(probability >= 0.0 && probability <= 1.0))
+                throw Error(KNP_GB300_E_INVALID, "connection probability outside [0, 1]");
+            const uint64_t n_cand = static_cast<uint64_t>(n_pre) * n_post;
+            thr = static_cast<unsigned long long>(probability * 9007199254740992.0);
+            KNP_CUDA(cudaSetDevice(device_));
+            KNP_CUDA(gen_candidates(n_cand, thr, stream_key(seed, stream + 5), nullptr, &n_syn, stream_));
+            in_degree = n_pre;
+            break;
+        }
+        case KNP_GEN_FIXED_NUMBER_POST:
+            n_syn = count;
+            in_degree = count;
+            break;
+        case KNP_GEN_FIXED_NUMBER_PRE:
+            n_syn = count;
+            in_degree = (count + n_post - 1) / n_post;
+            break;
+        default:
+            throw Error(KNP_GB300_E_INVALID, "unknown generator kind");
+    }
+    if (n_syn > 0xFFFFFFFFull) throw Error(KNP_GB300_E_INVALID, "more than 2^32-1 synapses in one projection");
     auto p = std::make_unique<ProjectionSlot>();
     p->uid = uid;
     p->kind = KNP_SYNAPSE_DELTA;
@@ -332,7 +403,17 @@ void Backend::generate_fixed_fan_in(
     p->post_uid = post_uid;
     p->n_syn = n_syn;
     p->generated = true;
-    p->gen = {n_pre, n_post, fan_in, k_lo, k_hi, d_lo, d_hi, seed, stream};
+    p->gen.kind = kind;
+    p->gen.n_pre = n_pre;
+    p->gen.n_post = n_post;
+    p->gen.in_degree = static_cast<uint32_t>(std::min<uint64_t>(in_degree, 0xFFFFFFFFull));
+    p->gen.k_lo = k_lo;
+    p->gen.k_hi = k_hi;
+    p->gen.d_lo = d_lo;
+    p->gen.d_hi = d_hi;
+    p->gen.seed = seed;
+    p->gen.stream = stream;
+    p->gen.prob_threshold = thr;
     projs_.push_back(std::move(p));
 }
 
@@ -857,11 +938,20 @@ void Backend::build_projection(ProjectionSlot &p)
     uint32_t *d_post = nullptr, *d_delay = nullptr;
     float *d_w = nullptr;
     uint8_t *d_type = nullptr;
+    unsigned long long *cand = nullptr;  // FixedProbability: the kept pairs, until the gather
     if (p.generated)
     {
         p.n_rows = p.gen.n_pre;
+        if (p.gen.kind == KNP_GEN_FIXED_PROBABILITY)
+        {
+            cand = arena_.make<unsigned long long>(std::max<uint64_t>(S, 1), false);
+            uint64_t kept = 0;
+            KNP_CUDA(gen_candidates(static_cast<uint64_t>(p.gen.n_pre) * p.gen.n_post, p.gen.prob_threshold,
+                                    stream_key(p.gen.seed, p.gen.stream + 5), cand, &kept, stream_));
+            if (kept != S) throw Error(KNP_GB300_E_CUDA, "generated pair count changed");
+        }
         d_key = arena_.make<uint32_t>(S, false);
-        launch_gen_fixed_fan_in_keys(S, p.gen.n_pre, stream_key(p.gen.seed, p.gen.stream + 1), d_key, stream_);
+        launch_gen_keys(gen_spec(p, cand), S, d_key, stream_);
     }
     else
     {
@@ -893,9 +983,7 @@ void Backend::build_projection(ProjectionSlot &p)
     p.delay_d = arena_.make<uint8_t>(S, false);
     if (p.generated)
     {
-        launch_gen_fixed_fan_in_gather(S, perm, p.gen.n_post, p.gen.k_lo, p.gen.k_hi, p.gen.d_lo, p.gen.d_hi,
-                                       stream_key(p.gen.seed, p.gen.stream + 2), stream_key(p.gen.seed, p.gen.stream + 3),
-                                       p.col, p.w, p.delay_d, stream_);
+        launch_gen_gather(gen_spec(p, cand), S, perm, p.col, p.w, p.delay_d, stream_);
     }
     else
     {
@@ -906,6 +994,7 @@ void Backend::build_projection(ProjectionSlot &p)
     KNP_CUDA(cudaStreamSynchronize(stream_));
     arena_.release(temp);
     arena_.release(d_key);
+    if (cand) arena_.release(cand);
     if (d_post) arena_.release(d_post);
     if (d_delay) arena_.release(d_delay);
     if (d_w) arena_.release(d_w);
@@ -1222,7 +1311,7 @@ void Backend::init()
         {
             p->max_delay = p->gen.d_hi;
             const double kmax = std::max(std::abs(p->gen.k_lo), std::abs(p->gen.k_hi));
-            p->dyadic = static_cast<double>(p->gen.fan_in) * kmax / 256.0 < 32768.0;
+            p->dyadic = static_cast<double>(p->gen.in_degree) * kmax / 256.0 < 32768.0;
             if (post && p->gen.n_post > post->n)
                 throw Error(KNP_GB300_E_INVALID, "postsynaptic index out of the target population");
             continue;

@@ -167,10 +167,13 @@ struct ProjectionSlot
     bool generated = false;
     struct
     {
-        uint32_t n_pre, n_post, fan_in;
+        int kind;  // GenKind
+        uint32_t n_pre, n_post;
+        uint32_t in_degree;  // largest number of synapses into one postsynaptic neuron (a bound)
         int32_t k_lo, k_hi;
         uint32_t d_lo, d_hi;
         uint64_t seed, stream;
+        unsigned long long prob_threshold;  // FixedProbability: 53-bit draw below it keeps a pair
     } gen{};
     std::map<Uid, int> stdp_pops;
     std::set<Uid> spike_senders;
@@ -236,9 +239,9 @@ public:
                                   const uint32_t *pre, const uint32_t *post, const float *w, const uint32_t *delay,
                                   const uint8_t *type, const knp_resource_synapse *rule, bool locked);
     void read_resource_synapses(const Uid &proj, knp_resource_synapse *out);
-    void generate_fixed_fan_in(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, uint32_t n_pre, uint32_t n_post,
-                               uint32_t fan_in, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi, uint64_t seed,
-                               uint64_t stream);
+    void generate_projection(const Uid &uid, const Uid &pre_uid, const Uid &post_uid, int kind, uint32_t n_pre,
+                             uint32_t n_post, uint64_t count, double probability, int32_t k_lo, int32_t k_hi,
+                             uint32_t d_lo, uint32_t d_hi, uint64_t seed, uint64_t stream);
     void set_stdp_population(const Uid &proj, const Uid &pop, int processing);
     void subscribe(const Uid &receiver, const Uid &sender);
     void set_accumulator(const Uid &pop, int mode);
@@ -288,6 +291,7 @@ private:
 
     void build_population(PopulationSlot &p);
     void build_projection(ProjectionSlot &p);
+    GenSpec gen_spec(const ProjectionSlot &p, const unsigned long long *cand) const;
     void build_stdp(ProjectionSlot &p);
     void build_pull(ProjectionSlot &p);
     void build_resource_synapses(PopulationSlot &q);

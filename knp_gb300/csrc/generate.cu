@@ -1,6 +1,7 @@
 // Network construction on the device: presynaptic-major CSR build (stable radix sort of synapse
 // indexes by presynaptic neuron, so a row keeps the reference's synapse order) and the counter-based
 // generators shared with knp_gb300/network.py (fixed fan-in projection, Bernoulli spike schedule).
+#include <algorithm>
 #include <cstdint>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -55,25 +56,134 @@ __global__ void gather_kernel(
     }
 }
 
-__global__ void fan_in_keys_kernel(uint64_t n, uint32_t n_pre, unsigned long long key_pre, uint32_t *pre_out)
+// Presynaptic and postsynaptic neuron of generated synapse i (synapse_generators.h:59-69 all_to_all,
+// :93-120 aligned, :139-154 exclusive, :172-178 one_to_one, :259-300 FixedProbability,
+// :352-388 FixedNumberPost, :409-445 FixedNumberPre).
+__device__ __forceinline__ void gen_pair(const GenSpec &g, uint64_t i, uint32_t &pre, uint32_t &post)
+{
+    switch (g.kind)
+    {
+        case kGenAllToAll:
+            pre = static_cast<uint32_t>(i % g.n_pre);
+            post = static_cast<uint32_t>(i / g.n_pre);
+            break;
+        case kGenAligned:
+            if (g.n_pre >= g.n_post)
+            {
+                pre = static_cast<uint32_t>(i);
+                post = static_cast<uint32_t>(i / (g.n_pre / g.n_post));
+            }
+            else
+            {
+                post = static_cast<uint32_t>(i);
+                pre = static_cast<uint32_t>(i / (g.n_post / g.n_pre));
+            }
+            break;
+        case kGenExclusive:
+        {
+            pre = static_cast<uint32_t>(i / (g.n_pre - 1));
+            const uint32_t to = static_cast<uint32_t>(i % (g.n_pre - 1));
+            post = to >= pre ? to + 1 : to;
+            break;
+        }
+        case kGenOneToOne:
+            pre = post = static_cast<uint32_t>(i);
+            break;
+        case kGenFixedProbability:
+        {
+            const unsigned long long c = g.cand[i];
+            pre = static_cast<uint32_t>(c % g.n_pre);
+            post = static_cast<uint32_t>(c / g.n_pre);
+            break;
+        }
+        case kGenFixedNumberPost:
+            pre = static_cast<uint32_t>(i % g.n_pre);
+            post = static_cast<uint32_t>(uniform_int(g.key_post, i, 0, static_cast<long long>(g.n_post) - 1));
+            break;
+        default:  // kGenFixedNumberPre
+            pre = static_cast<uint32_t>(uniform_int(g.key_pre, i, 0, static_cast<long long>(g.n_pre) - 1));
+            post = static_cast<uint32_t>(i % g.n_post);
+            break;
+    }
+}
+
+__global__ void gen_keys_kernel(GenSpec g, uint64_t n, uint32_t *pre_out)
 {
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        pre_out[i] = static_cast<uint32_t>(uniform_int(key_pre, i, 0, static_cast<long long>(n_pre) - 1));
+    {
+        uint32_t pre, post;
+        gen_pair(g, i, pre, post);
+        pre_out[i] = pre;
+    }
 }
 
-__global__ void fan_in_gather_kernel(
-    uint64_t n, const uint32_t *perm, uint32_t n_post, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi,
-    unsigned long long key_w, unsigned long long key_d, int32_t *col_out, float *w_out, uint8_t *delay_out)
+__global__ void gen_gather_kernel(GenSpec g, uint64_t n, const uint32_t *perm, int32_t *col_out, float *w_out,
+                                  uint8_t *delay_out)
 {
     for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < n;
          e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
     {
         const uint64_t i = perm[e];
-        col_out[e] = static_cast<int32_t>(i % n_post);
-        const long long k = uniform_int(key_w, i, k_lo, k_hi);
-        w_out[e] = static_cast<float>(k) * (1.0f / 256.0f);  // k / 256, one rounding (exact for |k| < 2^24)
-        delay_out[e] = static_cast<uint8_t>(uniform_int(key_d, i, d_lo, d_hi));
+        uint32_t pre, post;
+        gen_pair(g, i, pre, post);
+        col_out[e] = static_cast<int32_t>(post);
+        w_out[e] = static_cast<float>(uniform_int(g.key_w, i, g.k_lo, g.k_hi)) * (1.0f / 256.0f);
+        delay_out[e] = static_cast<uint8_t>(uniform_int(g.key_d, i, g.d_lo, g.d_hi));
+    }
+}
+
+constexpr uint32_t kCandChunk = 8192;  // candidate pairs per chunk
+
+// counts[c] = kept candidates of chunk c; one block per chunk (grid-strided).
+__global__ void cand_count_kernel(uint64_t n_cand, unsigned long long threshold, unsigned long long key,
+                                  uint64_t chunks, unsigned long long *counts)
+{
+    __shared__ unsigned int tot;
+    for (uint64_t c = blockIdx.x; c < chunks; c += gridDim.x)
+    {
+        if (threadIdx.x == 0) tot = 0;
+        __syncthreads();
+        unsigned int mine = 0;
+        const uint64_t lo = c * kCandChunk, hi = min(n_cand, lo + kCandChunk);
+        for (uint64_t x = lo + threadIdx.x; x < hi; x += blockDim.x) mine += (rand64(key, x) >> 11) < threshold;
+        atomicAdd(&tot, mine);
+        __syncthreads();
+        if (threadIdx.x == 0) counts[c] = tot;
+        __syncthreads();
+    }
+}
+
+// Writes chunk c's kept candidates in ascending order from offs[c] (exclusive prefix of counts).
+__global__ void cand_write_kernel(uint64_t n_cand, unsigned long long threshold, unsigned long long key,
+                                  uint64_t chunks, const unsigned long long *offs, unsigned long long *out)
+{
+    __shared__ unsigned int warp_tot[32];
+    __shared__ unsigned long long base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+    for (uint64_t c = blockIdx.x; c < chunks; c += gridDim.x)
+    {
+        if (threadIdx.x == 0) base = offs[c];
+        __syncthreads();
+        const uint64_t lo = c * kCandChunk, hi = min(n_cand, lo + kCandChunk);
+        for (uint64_t x0 = lo; x0 < hi; x0 += blockDim.x)
+        {
+            const uint64_t x = x0 + threadIdx.x;
+            const bool hit = x < hi && (rand64(key, x) >> 11) < threshold;
+            const unsigned int b = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) warp_tot[warp] = __popc(b);
+            __syncthreads();
+            unsigned int before = 0, all = 0;
+            for (int w = 0; w < n_warps; ++w)
+            {
+                if (w < warp) before += warp_tot[w];
+                all += warp_tot[w];
+            }
+            if (hit) out[base + before + __popc(b & ((1u << lane) - 1u))] = x;
+            __syncthreads();
+            if (threadIdx.x == 0) base += all;
+            __syncthreads();
+        }
     }
 }
 
@@ -206,19 +316,54 @@ void launch_gather_synapses(
                                                   type_out);
 }
 
-void launch_gen_fixed_fan_in_keys(
-    uint64_t n_syn, uint32_t n_pre, unsigned long long key_pre, uint32_t *pre_out, cudaStream_t s)
+void launch_gen_keys(const GenSpec &g, uint64_t n_syn, uint32_t *pre_out, cudaStream_t s)
 {
-    fan_in_keys_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, n_pre, key_pre, pre_out);
+    gen_keys_kernel<<<grid_for(n_syn), 256, 0, s>>>(g, n_syn, pre_out);
 }
 
-void launch_gen_fixed_fan_in_gather(
-    uint64_t n_syn, const uint32_t *perm, uint32_t n_post, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi,
-    unsigned long long key_w, unsigned long long key_d, int32_t *col_out, float *w_out, uint8_t *delay_out,
-    cudaStream_t s)
+void launch_gen_gather(const GenSpec &g, uint64_t n_syn, const uint32_t *perm, int32_t *col_out, float *w_out,
+                       uint8_t *delay_out, cudaStream_t s)
 {
-    fan_in_gather_kernel<<<grid_for(n_syn), 256, 0, s>>>(n_syn, perm, n_post, k_lo, k_hi, d_lo, d_hi, key_w, key_d,
-                                                         col_out, w_out, delay_out);
+    gen_gather_kernel<<<grid_for(n_syn), 256, 0, s>>>(g, n_syn, perm, col_out, w_out, delay_out);
+}
+
+cudaError_t gen_candidates(uint64_t n_cand, unsigned long long threshold, unsigned long long key,
+                           unsigned long long *out, uint64_t *n_kept, cudaStream_t s)
+{
+    const uint64_t chunks = (n_cand + kCandChunk - 1) / kCandChunk;
+    *n_kept = 0;
+    if (!chunks) return cudaSuccess;
+    unsigned long long *counts = nullptr, *offs = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    const int blocks = static_cast<int>(std::min<uint64_t>(chunks, 1u << 16));
+    cudaError_t err = cudaMallocAsync(&counts, (chunks + 1) * sizeof(unsigned long long), s);
+    if (err == cudaSuccess) err = cudaMallocAsync(&offs, (chunks + 1) * sizeof(unsigned long long), s);
+    if (err == cudaSuccess) err = cudaMemsetAsync(counts + chunks, 0, sizeof(unsigned long long), s);
+    if (err == cudaSuccess)
+    {
+        cand_count_kernel<<<blocks, 256, 0, s>>>(n_cand, threshold, key, chunks, counts);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess)
+        err = cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, counts, offs, static_cast<int64_t>(chunks + 1), s);
+    if (err == cudaSuccess) err = cudaMallocAsync(&tmp, tmp_bytes, s);
+    if (err == cudaSuccess)
+        err = cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, counts, offs, static_cast<int64_t>(chunks + 1), s);
+    unsigned long long total = 0;
+    if (err == cudaSuccess) err = cudaMemcpyAsync(&total, offs + chunks, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err == cudaSuccess && out && total)
+    {
+        cand_write_kernel<<<blocks, 256, 0, s>>>(n_cand, threshold, key, chunks, offs, out);
+        err = cudaGetLastError();
+    }
+    if (tmp) cudaFreeAsync(tmp, s);
+    if (offs) cudaFreeAsync(offs, s);
+    if (counts) cudaFreeAsync(counts, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    *n_kept = total;
+    return err;
 }
 
 // Bernoulli schedule on the device; allocates *d_idx (caller frees with cudaFree) and fills

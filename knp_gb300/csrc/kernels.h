@@ -440,12 +440,40 @@ void launch_iota_u32(uint32_t *out, uint64_t n, cudaStream_t s);
 void launch_gather_synapses(
     uint64_t n_syn, const uint32_t *perm, const uint32_t *post, const float *w, const uint32_t *delay,
     const uint8_t *type, int32_t *col_out, float *w_out, uint8_t *delay_out, uint8_t *type_out, cudaStream_t s);
-void launch_gen_fixed_fan_in_keys(
-    uint64_t n_syn, uint32_t n_pre, unsigned long long key_pre, uint32_t *pre_out, cudaStream_t s);
-void launch_gen_fixed_fan_in_gather(
-    uint64_t n_syn, const uint32_t *perm, uint32_t n_post, int32_t k_lo, int32_t k_hi, uint32_t d_lo, uint32_t d_hi,
-    unsigned long long key_w, unsigned long long key_d, int32_t *col_out, float *w_out, uint8_t *delay_out,
-    cudaStream_t s);
+// Device synapse generators: the index -> (presynaptic, postsynaptic) rules of the reference's
+// synapse_generators.h (all_to_all, aligned, exclusive, one_to_one, FixedProbability,
+// FixedNumberPost, FixedNumberPre), with counter-based draws instead of std::mt19937 so that a seed
+// gives the same projection every time. Synapse i's weight is k/256 (k uniform in [k_lo, k_hi])
+// and its delay uniform in [d_lo, d_hi], drawn from (key_w, i) and (key_d, i).
+enum GenKind : int
+{
+    kGenAllToAll = 0,
+    kGenAligned = 1,
+    kGenExclusive = 2,
+    kGenOneToOne = 3,
+    kGenFixedProbability = 4,
+    kGenFixedNumberPost = 5,
+    kGenFixedNumberPre = 6,
+};
+
+struct GenSpec
+{
+    int kind;
+    uint32_t n_pre, n_post;
+    int32_t k_lo, k_hi;
+    uint32_t d_lo, d_hi;
+    unsigned long long key_pre, key_post, key_w, key_d;
+    const unsigned long long *cand;  // FixedProbability: kept candidate pair indexes (pre + n_pre * post)
+};
+
+void launch_gen_keys(const GenSpec &g, uint64_t n_syn, uint32_t *pre_out, cudaStream_t s);
+void launch_gen_gather(const GenSpec &g, uint64_t n_syn, const uint32_t *perm, int32_t *col_out, float *w_out,
+                       uint8_t *delay_out, cudaStream_t s);
+// Candidate pairs c in [0, n_cand) kept when the 53-bit draw (key, c) is below `threshold`: with
+// out == nullptr only their number (*n_kept); else also written to out[] in ascending order.
+cudaError_t gen_candidates(uint64_t n_cand, unsigned long long threshold, unsigned long long key,
+                           unsigned long long *out, uint64_t *n_kept, cudaStream_t s);
+
 cudaError_t gen_bernoulli_schedule(
     uint32_t n_sources, unsigned long long threshold, unsigned long long key, unsigned long long first_step,
     uint64_t n_steps, long long *d_offsets, uint32_t **d_idx, uint64_t *n_idx, cudaStream_t s);

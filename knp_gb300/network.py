@@ -191,6 +191,47 @@ def fixed_fan_in_pre(key_pre, key_w, key_d, n_pre: int, n_post: int, fan_in: int
     return pre, post, w, d
 
 
+def generated_synapses(kind: int, n_pre: int, n_post: int, k_lo: int, k_hi: int, d_lo: int, d_hi: int, seed: int,
+                       stream: int, count: int = 0, probability: float = 0.0):
+    """The synapses (pre, post, weight, delay), in synapse order, of knp_gb300_generate_projection:
+    synapse i connects the pair of the generator's index rule (synapse_generators.h:58-457), with
+    weight k/256 (k uniform in [k_lo, k_hi]) and delay uniform in [d_lo, d_hi] drawn for i."""
+    key_pre, key_w, key_d = (stream_key(seed, stream + k) for k in (1, 2, 3))
+    key_post, key_prob = stream_key(seed, stream + 4), stream_key(seed, stream + 5)
+    if kind == T.GEN_ALL_TO_ALL:
+        i = np.arange(n_pre * n_post, dtype=np.uint64)
+        pre, post = i % np.uint64(n_pre), i // np.uint64(n_pre)
+    elif kind == T.GEN_ALIGNED:
+        i = np.arange(max(n_pre, n_post), dtype=np.uint64)
+        if n_pre >= n_post:
+            pre, post = i, i // np.uint64(n_pre // n_post)
+        else:
+            pre, post = i // np.uint64(n_post // n_pre), i
+    elif kind == T.GEN_EXCLUSIVE:
+        i = np.arange(n_pre * (n_pre - 1), dtype=np.uint64)
+        pre, to = i // np.uint64(n_pre - 1), i % np.uint64(n_pre - 1)
+        post = np.where(to >= pre, to + np.uint64(1), to)
+    elif kind == T.GEN_ONE_TO_ONE:
+        i = np.arange(n_pre, dtype=np.uint64)
+        pre = post = i
+    elif kind == T.GEN_FIXED_PROBABILITY:
+        c = np.arange(n_pre * n_post, dtype=np.uint64)
+        kept = c[(rand64(key_prob, c) >> np.uint64(11)) < np.uint64(bernoulli_threshold(probability))]
+        i = np.arange(kept.size, dtype=np.uint64)
+        pre, post = kept % np.uint64(n_pre), kept // np.uint64(n_pre)
+    elif kind == T.GEN_FIXED_NUMBER_POST:
+        i = np.arange(count, dtype=np.uint64)
+        pre, post = i % np.uint64(n_pre), uniform_int(key_post, i, 0, n_post - 1)
+    elif kind == T.GEN_FIXED_NUMBER_PRE:
+        i = np.arange(count, dtype=np.uint64)
+        pre, post = uniform_int(key_pre, i, 0, n_pre - 1), i % np.uint64(n_post)
+    else:
+        raise ValueError(f"unknown generator kind {kind}")
+    w = dyadic_weights(key_w, i, k_lo, k_hi)
+    d = uniform_int(key_d, i, d_lo, d_hi).astype(np.uint32)
+    return (np.asarray(pre).astype(np.uint32), np.asarray(post).astype(np.uint32), w, d)
+
+
 LARGE_SEED_STREAM = 30
 
 

@@ -23,6 +23,9 @@ EXCITATORY, INHIBITORY_CURRENT, INHIBITORY_CONDUCTANCE, DOPAMINE, BLOCKING = ran
 BLIFAT, RESOURCE_STDP_BLIFAT, LIF, ALTAI_LIF, RESOURCE_STDP_ALTAI_LIF = range(5)
 # knp_synapse_kind
 DELTA, ADDITIVE_STDP_DELTA, RESOURCE_STDP_DELTA = range(3)
+# Device synapse generators (knp_generator_kind).
+(GEN_ALL_TO_ALL, GEN_ALIGNED, GEN_EXCLUSIVE, GEN_ONE_TO_ONE, GEN_FIXED_PROBABILITY, GEN_FIXED_NUMBER_POST,
+ GEN_FIXED_NUMBER_PRE) = range(7)
 # knp_stdp_processing (projection.h:139-150)
 STDP_ONLY, STDP_AND_SPIKE = range(2)
 # knp_gb300_accumulator (input-ring accumulation of a population)

@@ -262,6 +262,63 @@ def test_device_generated_projection_matches_host_arrays():
     np.testing.assert_array_equal(np.sort(b.read_weights(rec.uid)), np.sort(rec.weight))
 
 
+GEN_CASES = [  # kind, n_pre, n_post, count, probability, k_lo, k_hi (B fires on some steps)
+    (T.GEN_ALL_TO_ALL, 300, 200, 0, 0.0, -8, 40),
+    (T.GEN_ALIGNED, 800, 200, 0, 0.0, 200, 300),
+    (T.GEN_ALIGNED, 200, 800, 0, 0.0, 200, 300),
+    (T.GEN_EXCLUSIVE, 400, 400, 0, 0.0, -4, 32),
+    (T.GEN_ONE_TO_ONE, 500, 500, 0, 0.0, 200, 300),
+    (T.GEN_FIXED_PROBABILITY, 700, 600, 0, 0.05, 32, 256),
+    (T.GEN_FIXED_NUMBER_POST, 600, 500, 30_000, 0.0, 16, 160),
+    (T.GEN_FIXED_NUMBER_PRE, 600, 500, 30_000, 0.0, 16, 160),
+]
+
+
+@pytest.mark.parametrize("case", range(len(GEN_CASES)))
+def test_device_synapse_generators(case):
+    """knp_gb300_generate_projection builds, for every generator kind, the synapses of
+    network.generated_synapses: population A (Bernoulli-driven) projects through the generated
+    projection into population B; both populations' spikes equal the oracle's (which loads the host
+    arrays) step by step, and so does the event count."""
+    from knp_gb300 import backend as B
+    from oracle import oracle as orc
+
+    kind, n_pre, n_post, count, prob, k_lo, k_hi = GEN_CASES[case]
+    seed, stream, steps = 7 + case, 50, 40
+    a_uid, b_uid, g_uid, bg_uid, chan_uid = (T.uid_from_int(9000 + 10 * case + i) for i in range(5))
+    pre, post, w, d = N.generated_synapses(kind, n_pre, n_post, k_lo, k_hi, 1, 8, seed, stream, count=count,
+                                           probability=prob)
+    assert pre.size > 0
+    pa = N.Population(a_uid, T.BLIFAT, T.blifat_defaults(n_pre))
+    pb = N.Population(b_uid, T.BLIFAT, T.blifat_defaults(n_post))
+    ar = np.arange(n_pre, dtype=np.uint32)
+    bg = N.Projection(bg_uid, T.DELTA, T.NULL_UID, a_uid, ar, ar.copy(), np.ones(n_pre, np.float32),
+                      np.ones(n_pre, np.uint32))
+    gp = N.Projection(g_uid, T.DELTA, a_uid, b_uid, pre, post, w, d)
+    net = N.Network([pa, pb], [bg, gp], [(bg_uid, chan_uid)])
+    sched = [N.bernoulli_schedule(chan_uid, seed, n_pre, steps, 0.05)]
+    b = B.GB300Backend()
+    b.load_populations(net.populations)
+    b.load_projections([bg])
+    b.generate_projection(g_uid, a_uid, b_uid, kind, n_pre, n_post, k_lo, k_hi, 1, 8, seed, stream, count=count,
+                          probability=prob)
+    for recv, send in net.subscriptions:
+        b.subscribe(recv, [send])
+    b.record_spikes(a_uid)
+    b.record_spikes(b_uid)
+    b._init()
+    b.load_spike_schedule(sched[0])
+    b.step(steps)
+    o, oo = orc.run(net, sched, steps)
+    for uid in (a_uid, b_uid):
+        for t_ in range(steps):
+            np.testing.assert_array_equal(b.spikes(uid, t_), o[uid][t_], err_msg=f"step {t_}")
+    assert sum(s.size for s in o[b_uid]) > 0
+    assert b.counters()[0] == oo.events
+    np.testing.assert_array_equal(np.sort(b.read_weights(g_uid)), np.sort(w))
+    b.close()
+
+
 def _full_size_run(threshold, n, fan, seed, steps, keep):
     """The large sparse config at full size, synapses and background generated on the device, with
     the given gather threshold. Returns (per-step spike digests, spike masks of the last `keep`

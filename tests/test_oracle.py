@@ -306,3 +306,42 @@ def test_restated_oracle_matches_reference_headers_altai(oracle_lib):
     assert canonical(oa.altai(pop)[0]) == canonical(ob.altai(pop)[0])
     assert sum(s.size for s in a[pop]) > 200
     assert (oa.altai(pop)[0]["activity_time"] != np.iinfo(np.int64).max).sum() > 5
+
+
+def test_generated_synapses_follow_the_reference_index_rules():
+    """network.generated_synapses (the host image of knp_gb300_generate_projection) pairs neurons as
+    the reference's generators do for synapse index i (synapse_generators.h: all_to_all :64-69,
+    aligned :99-118, exclusive :144-152, one_to_one :177-178, FixedProbability :295-299,
+    FixedNumberPost :384-387, FixedNumberPre :442-444), restated here loop by loop."""
+    from knp_gb300 import network as N
+    from knp_gb300 import types as T
+
+    args = dict(k_lo=-8, k_hi=8, d_lo=1, d_hi=6, seed=4, stream=40)
+    pre, post, w, d = N.generated_synapses(T.GEN_ALL_TO_ALL, 7, 5, **args)
+    assert list(zip(pre, post)) == [(i % 7, i // 7) for i in range(35)]
+    for n_pre, n_post in ((12, 4), (3, 9), (6, 6)):
+        pre, post, _, _ = N.generated_synapses(T.GEN_ALIGNED, n_pre, n_post, **args)
+        exp = []
+        for i in range(max(n_pre, n_post)):
+            if n_pre >= n_post:
+                exp.append((i, i // (n_pre // n_post)))
+            else:
+                exp.append((i // (n_post // n_pre), i))
+        assert list(zip(pre, post)) == exp
+    pre, post, _, _ = N.generated_synapses(T.GEN_EXCLUSIVE, 3, 3, **args)
+    assert list(zip(pre, post)) == [(0, 1), (0, 2), (1, 0), (1, 2), (2, 0), (2, 1)]  # the reference's example
+    pre, post, _, _ = N.generated_synapses(T.GEN_ONE_TO_ONE, 9, 9, **args)
+    assert list(pre) == list(post) == list(range(9))
+    pre, post, w, d = N.generated_synapses(T.GEN_FIXED_PROBABILITY, 40, 50, probability=0.1, **args)
+    cand = pre.astype(np.int64) + 40 * post.astype(np.int64)
+    assert np.all(np.diff(cand) > 0) and 120 < pre.size < 280  # kept pairs in index order, ~200 expected
+    pre, post, _, _ = N.generated_synapses(T.GEN_FIXED_NUMBER_POST, 10, 30, count=100, **args)
+    assert list(pre) == [i % 10 for i in range(100)] and post.max() < 30
+    pre, post, w, d = N.generated_synapses(T.GEN_FIXED_NUMBER_PRE, 30, 10, count=100, **args)
+    assert list(post) == [i % 10 for i in range(100)]
+    s = args["stream"]
+    fp = N.fixed_fan_in_pre(N.stream_key(4, s + 1), N.stream_key(4, s + 2), N.stream_key(4, s + 3), 30, 10, 10,
+                            -8, 8, 1, 6)
+    for x, y in zip((pre, post, w, d), fp):
+        np.testing.assert_array_equal(x, y)
+    assert np.all((w * 256 >= -8) & (w * 256 <= 8)) and np.all((d >= 1) & (d <= 6))
