@@ -426,6 +426,16 @@ KNP_GB300_API int knp_gb300_lif_scan_backward(
     const float *I, const float *ckpt, const float *dS, float *dI, int T, int64_t BN, float beta, float theta, int K,
     int relaxed, float k, void *stream);
 
+/**
+ * Differentiation form: a BF16 GEMM operand (K contiguous) from X[R][C] (FP32, or BF16 when x_bf16
+ * != 0; device memory) in one pass. Each output row holds one (mode 0) or two (modes 1, 2) halves of
+ * width P, zero past the copied extent: mode 0 bf16(x); mode 1 bf16(x) twice; mode 2 hi = bf16(x)
+ * and lo = bf16(x - hi) (round to nearest even). transpose == 0: out[R][H P], row r from X's row r
+ * (P >= C, P even); transpose != 0: out[C][H P], row c from X's column c (P >= R). Launch only.
+ */
+KNP_GB300_API int knp_gb300_bf16_operand(const void *X, int x_bf16, int64_t R, int64_t C, int mode, int transpose,
+                                         int64_t P, void *out, void *stream);
+
 /*
  * Batched / precision form (no reference counterpart). D[M x N] (FP32, row-major) = A[M x K] *
  * B[N x K]^T with BF16 operands (row-major, K contiguous, device memory) on the tcgen05 tensor

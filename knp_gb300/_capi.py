@@ -85,6 +85,7 @@ def lib():
         "knp_gb300_profile_phases": ([p, u64, ctypes.POINTER(ctypes.c_float)], c_int),
         "knp_gb300_profile_grid_phases": ([p, u64, ctypes.POINTER(ctypes.c_double)], c_int),
         "knp_gb300_measure_add_rate": ([u64, u64, ctypes.POINTER(ctypes.c_double)], c_int),
+        "knp_gb300_bf16_operand": ([p, c_int, ctypes.c_int64, ctypes.c_int64, c_int, c_int, ctypes.c_int64, p, p], c_int),
         "knp_gb300_lif_scan_forward": ([p, p, p, c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_int, c_int,
                                         ctypes.c_float, p], c_int),
         "knp_gb300_lif_scan_backward": ([p, p, p, p, c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_float, c_int,

@@ -103,6 +103,29 @@ def gemm_terms(a_terms, b_terms) -> torch.Tensor:
                    torch.cat([_pad_k(b.contiguous()) for _, b in pairs], 1))
 
 
+def _round8(n: int) -> int:
+    return (n + 7) // 8 * 8
+
+
+def operand(x: torch.Tensor, mode: int, transpose: bool, width: int) -> torch.Tensor:
+    """BF16 GEMM operand from x[R, C] (FP32 or BF16) by knp_gb300_bf16_operand: rows of one (mode 0)
+    or two (1: the value twice; 2: hi, lo) halves of `width` (zero-padded), from x's rows or, with
+    transpose, from its columns."""
+    x = x.contiguous()
+    R, C = x.shape
+    H = 1 if mode == 0 else 2
+    out = torch.empty((C if transpose else R, H * width), device=x.device, dtype=torch.bfloat16)
+    _capi.check(_capi.lib().knp_gb300_bf16_operand(_p(x), int(x.dtype == torch.bfloat16), R, C, mode, int(transpose),
+                                                   width, _p(out), _stream()))
+    return out
+
+
+# The hard-threshold path builds its GEMM operands with knp_gb300_bf16_operand (one pass per
+# operand: cast, hi/lo split, transpose, concatenation along K and padding); the relaxed path (three
+# BF16 terms of continuous values) keeps the torch composition of bf16_terms / gemm_terms.
+FUSED_OPERANDS = True
+
+
 class LIFLayerFn(torch.autograd.Function):
     """S_out[T, B, N_out] = LIF(S_in[T, B, N_in] @ W) with surrogate-gradient backward."""
 
@@ -110,32 +133,55 @@ class LIFLayerFn(torch.autograd.Function):
     def forward(ctx, s_in, w_master, beta: float, theta: float, checkpoint: int, relaxed: bool, k: float):
         T, B, n_in = s_in.shape
         n_out = w_master.shape[1]
-        wb = w_master.to(torch.bfloat16)  # [n_in, n_out]
         s_in = s_in.contiguous()
-        s_terms = bf16_terms(s_in.reshape(T * B, n_in), 3 if relaxed else 1)  # 0/1 spikes are exact
-        I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()
+        fused = FUSED_OPERANDS and not relaxed
+        if fused:
+            s2d = s_in.reshape(T * B, n_in)
+            a = operand(s2d, 0, False, _round8(n_in))            # [TB, n_in]: 0/1 spikes, exact in BF16
+            wt = operand(w_master, 0, True, _round8(n_in))       # [n_out, n_in]: W^T
+            I = gemm_tn(a, wt).reshape(T, B, n_out)
+            saved = (w_master, s2d, a, wt)
+        else:
+            wb = w_master.to(torch.bfloat16)  # [n_in, n_out]
+            s_terms = bf16_terms(s_in.reshape(T * B, n_in), 3 if relaxed else 1)  # 0/1 spikes are exact
+            I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()
+            saved = (wb, *s_terms)
         S = torch.empty_like(I)
         ckpt = torch.empty(((T + checkpoint - 1) // checkpoint, B, n_out), device=I.device, dtype=torch.float32)
         _capi.check(_capi.lib().knp_gb300_lif_scan_forward(
             _p(I), _p(S), _p(ckpt), T, B * n_out, beta, theta, checkpoint, int(relaxed), k, _stream()))
-        ctx.save_for_backward(wb, ckpt, *s_terms)
-        ctx.cfg = (T, B, beta, theta, checkpoint, relaxed, k)
+        ctx.save_for_backward(ckpt, *saved)
+        ctx.cfg = (T, B, beta, theta, checkpoint, relaxed, k, fused, n_in, n_out)
         return S
 
     @staticmethod
     def backward(ctx, dS):
-        wb, ckpt, *s_terms = ctx.saved_tensors
-        T, B, beta, theta, checkpoint, relaxed, k = ctx.cfg
-        n_in, n_out = wb.shape
-        I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()  # recomputed, not stored
+        ckpt, *saved = ctx.saved_tensors
+        T, B, beta, theta, checkpoint, relaxed, k, fused, n_in, n_out = ctx.cfg
+        if fused:
+            w_master, s2d, a, wt = saved
+            I = gemm_tn(a, wt).reshape(T, B, n_out)  # recomputed, not stored
+        else:
+            wb, *s_terms = saved
+            I = gemm_terms(s_terms, [wb.t().contiguous()]).reshape(T, B, n_out).contiguous()
         dS = dS.contiguous()
         dI = torch.empty_like(I)
         _capi.check(_capi.lib().knp_gb300_lif_scan_backward(
             _p(I), _p(ckpt), _p(dS), _p(dI), T, B * n_out, beta, theta, checkpoint, int(relaxed), k, _stream()))
+        ds_in = None
+        if fused:
+            dI2 = dI.reshape(T * B, n_out)
+            tb = _round8(T * B)
+            # dW[n_in, n_out] = S^T (hi + lo): K = 2 T B, [S^T | S^T] against [hi^T | lo^T].
+            dW = gemm_tn(operand(s2d, 1, True, tb), operand(dI2, 2, True, tb))
+            if ctx.needs_input_grad[0]:
+                # ds_in[TB, n_in] = (hi + lo) W^T: K = 2 n_out, [hi | lo] against [W | W].
+                w2 = _round8(n_out)
+                ds_in = gemm_tn(operand(dI2, 2, False, w2), operand(w_master, 1, False, w2)).reshape(T, B, n_in)
+            return ds_in, dW, None, None, None, None, None
         d_terms = bf16_terms(dI.reshape(T * B, n_out), 3 if relaxed else 2)
         # dW[n_in, n_out] = S^T dI: K = T B per (S term, dI term) pair.
         dW = gemm_terms([s.t() for s in s_terms], [d.t() for d in d_terms])
-        ds_in = None
         if ctx.needs_input_grad[0]:
             # ds_in[TB, n_in] = dI W^T, W as [n_in, n_out]: K = n_out per dI term.
             ds_in = gemm_terms(d_terms, [wb]).reshape(T, B, n_in)

@@ -12,8 +12,10 @@
 //
 // Memory: the forward stores V only at every K-th step (checkpoint c holds the state entering
 // step c*K); the backward recomputes U inside each K-step segment from its checkpoint and I.
+#include <algorithm>
 #include <cstdint>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace knp_gb300
@@ -91,7 +93,92 @@ __global__ void lif_scan_backward_kernel(
     }
 }
 
+// ---- GEMM operand layouts (BF16, K contiguous) built in one pass from an FP32 or BF16 matrix
+// X[R][C]. Each output row holds H halves of width P (P >= the copied extent, the rest zero):
+// mode 0: one half, bf16(x); mode 1: two equal halves, bf16(x); mode 2: two halves hi = bf16(x),
+// lo = bf16(x - hi) (round to nearest even, as torch's conversion), so hi + lo holds x to 2^-17.
+// Row form: out[r][h P + c]; transposed form: out[c][h P + r] (a 32 x 32 tile through shared memory,
+// reads and writes coalesced).
+__device__ __forceinline__ float load_x(const void *X, int x_bf16, long long i)
+{
+    return x_bf16 ? __bfloat162float(static_cast<const __nv_bfloat16 *>(X)[i]) : static_cast<const float *>(X)[i];
+}
+
+__device__ __forceinline__ void halves(float x, int mode, __nv_bfloat16 &h0, __nv_bfloat16 &h1)
+{
+    h0 = __float2bfloat16_rn(x);
+    h1 = mode == 2 ? __float2bfloat16_rn(x - __bfloat162float(h0)) : h0;
+}
+
+// Row form: block (x, y) covers columns [2 (256 x + t), +2) of rows y, y + gridDim.y, ...; a thread
+// stores its two columns as one bf16 pair (P even, so pairs are 4-byte aligned).
+__global__ void operand_rows_kernel(const void *X, int x_bf16, long long R, long long C, int mode, long long P,
+                                    __nv_bfloat16 *out)
+{
+    const int H = mode == 0 ? 1 : 2;
+    const long long c = 2 * (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x);
+    if (c >= P) return;
+    for (long long r = blockIdx.y; r < R; r += gridDim.y)
+    {
+        const __nv_bfloat16 z = __float2bfloat16_rn(0.0f);
+        __nv_bfloat16 a0 = z, a1 = z, b0 = z, b1 = z;
+        if (c < C) halves(load_x(X, x_bf16, r * C + c), mode, a0, a1);
+        if (c + 1 < C) halves(load_x(X, x_bf16, r * C + c + 1), mode, b0, b1);
+        __nv_bfloat16 *o = out + r * H * P + c;
+        *reinterpret_cast<__nv_bfloat162 *>(o) = __halves2bfloat162(a0, b0);
+        if (H == 2) *reinterpret_cast<__nv_bfloat162 *>(o + P) = __halves2bfloat162(a1, b1);
+    }
+}
+
+__global__ void operand_transposed_kernel(const void *X, int x_bf16, long long R, long long C, int mode, long long P,
+                                          __nv_bfloat16 *out)
+{
+    __shared__ float tile[32][33];
+    const int H = mode == 0 ? 1 : 2;
+    const long long r0 = static_cast<long long>(blockIdx.x) * 32, c0 = static_cast<long long>(blockIdx.y) * 32;
+    // Read X[r0 + y][c0 + x] (coalesced along c); rows past R read as zero (the padding).
+    for (int y = threadIdx.y; y < 32; y += blockDim.y)
+    {
+        const long long r = r0 + y, c = c0 + threadIdx.x;
+        tile[y][threadIdx.x] = (r < R && c < C) ? load_x(X, x_bf16, r * C + c) : 0.0f;
+    }
+    __syncthreads();
+    // Write out[c0 + y][h P + r0 + x] (coalesced along r).
+    for (int y = threadIdx.y; y < 32; y += blockDim.y)
+    {
+        const long long c = c0 + y, r = r0 + threadIdx.x;
+        if (c >= C || r >= P) continue;
+        __nv_bfloat16 h0, h1;
+        halves(tile[threadIdx.x][y], mode, h0, h1);
+        out[c * H * P + r] = h0;
+        if (H == 2) out[c * H * P + P + r] = h1;
+    }
+}
+
 }  // namespace
+
+int bf16_operand(const void *X, int x_bf16, long long R, long long C, int mode, int transpose, long long P, void *out,
+                 cudaStream_t s)
+{
+    if (!X || !out || R < 1 || C < 1 || mode < 0 || mode > 2 || P < (transpose ? R : C)) return -1;
+    auto *o = static_cast<__nv_bfloat16 *>(out);
+    if (transpose)
+    {
+        const long long gx = (P + 31) / 32, gy = (C + 31) / 32;
+        if (gx > 0x7FFFFFFFll || gy > 65535) return -1;
+        operand_transposed_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), dim3(32, 8), 0, s>>>(
+            X, x_bf16, R, C, mode, P, o);
+    }
+    else
+    {
+        if (P % 2) return -1;  // pairs of columns
+        const long long gx = (P / 2 + 255) / 256;
+        const unsigned gy = static_cast<unsigned>(std::min<long long>(R, 4096));
+        if (gx > 0x7FFFFFFFll) return -1;
+        operand_rows_kernel<<<dim3(static_cast<unsigned>(gx), gy), 256, 0, s>>>(X, x_bf16, R, C, mode, P, o);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 int lif_scan_forward(
     const float *I, float *S, float *ckpt, int T, long long BN, float beta, float theta, int K, int relaxed, float k,

@@ -15,6 +15,8 @@ int lif_scan_forward(
 int lif_scan_backward(
     const float *I, const float *ckpt, const float *dS, float *dI, int T, long long BN, float beta, float theta, int K,
     int relaxed, float k, cudaStream_t s);
+int bf16_operand(const void *X, int x_bf16, long long R, long long C, int mode, int transpose, long long P, void *out,
+                 cudaStream_t s);
 }  // namespace knp_gb300
 
 namespace knp_gb300
@@ -427,6 +429,15 @@ int knp_gb300_lif_scan_backward(
                                                 static_cast<cudaStream_t>(stream));
     if (rc) g_error = rc == -1 ? "bad sizes (T >= 1, BN >= 1, 1 <= K <= 16)" : "kernel launch failed";
     return rc;
+}
+
+int knp_gb300_bf16_operand(const void *X, int x_bf16, int64_t R, int64_t C, int mode, int transpose, int64_t P,
+                           void *out, void *stream)
+{
+    const int rc = knp_gb300::bf16_operand(X, x_bf16, R, C, mode, transpose, P, out, static_cast<cudaStream_t>(stream));
+    if (rc == 0) return KNP_GB300_OK;
+    g_error = rc == -1 ? "bad operand arguments (sizes >= 1, mode 0..2, P >= the copied extent)" : "kernel launch failed";
+    return rc == -1 ? KNP_GB300_E_INVALID : KNP_GB300_E_CUDA;
 }
 
 int knp_gb300_generate_bernoulli_schedule_noalloc(

@@ -133,3 +133,24 @@ def test_graphed_train_step_matches_eager_steps():
     assert torch.equal(loss_g, loss_e)
     for a, b in zip(eager.weights, graphed.weights):
         assert torch.equal(a, b)
+
+
+def test_fused_operands_equal_the_torch_composition(monkeypatch):
+    """knp_gb300_bf16_operand builds the same GEMM operands as the torch composition (cast, hi/lo
+    split, transposes, concatenation and padding along K): loss and every weight gradient are equal
+    bit for bit, with a layer width that needs padding (10 outputs)."""
+    from knp_gb300 import bptt
+
+    x, labels = bptt.make_batch(T=12, B=41, n_in=200, seed=8)  # T B = 492: K padded to 496
+    grads = []
+    for fused in (True, False):
+        monkeypatch.setattr(bptt, "FUSED_OPERANDS", fused)
+        model = bptt.SpikingMLP(sizes=(200, 136, 10), checkpoint=4, seed=6)
+        loss = bptt.loss_fn(model(x), labels)
+        loss.backward()
+        torch.cuda.synchronize()
+        grads.append((loss.detach().clone(), [w.grad.clone() for w in model.weights]))
+    bptt.check_gemm_errors()
+    assert torch.equal(grads[0][0], grads[1][0])
+    for a, b in zip(grads[0][1], grads[1][1]):
+        assert torch.equal(a, b)
