@@ -36,6 +36,9 @@ __device__ __forceinline__ float surrogate(float x, float k)
     return __fdiv_rn(0.5f * k, d * d);
 }
 
+// One thread per (sample, neuron). A thread's chain of steps is short of parallelism (BN threads, a
+// few warps per SM), so each K-step segment's inputs (and, backward, output gradients) are loaded
+// before the segment's recurrence: up to kMaxSeg independent loads in flight instead of one.
 __global__ void lif_scan_forward_kernel(
     const float *__restrict__ I, float *__restrict__ S, float *__restrict__ ckpt, int T, long long BN, float beta,
     float theta, int K, int relaxed, float k)
@@ -43,13 +46,28 @@ __global__ void lif_scan_forward_kernel(
     const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (i >= BN) return;
     float V = 0.0f;
-    for (int t = 0; t < T; ++t)
+    const int n_seg = (T + K - 1) / K;
+    for (int c = 0; c < n_seg; ++c)
     {
-        if (t % K == 0) ckpt[static_cast<long long>(t / K) * BN + i] = V;
-        const float U = beta * V + I[static_cast<long long>(t) * BN + i];
-        const float s = relaxed ? fast_sigmoid(U - theta, k) : (U > theta ? 1.0f : 0.0f);
-        S[static_cast<long long>(t) * BN + i] = s;
-        V = U - theta * s;
+        const int t0 = c * K;
+        const int t1 = min(T, t0 + K);
+        ckpt[static_cast<long long>(c) * BN + i] = V;
+        float x[kMaxSeg];
+#pragma unroll
+        for (int u = 0; u < kMaxSeg; ++u)
+            if (t0 + u < t1) x[u] = I[static_cast<long long>(t0 + u) * BN + i];
+#pragma unroll
+        for (int u = 0; u < kMaxSeg; ++u)
+        {
+            const int t = t0 + u;
+            if (t < t1)
+            {
+                const float U = beta * V + x[u];
+                const float s = relaxed ? fast_sigmoid(U - theta, k) : (U > theta ? 1.0f : 0.0f);
+                S[static_cast<long long>(t) * BN + i] = s;
+                V = U - theta * s;
+            }
+        }
     }
 }
 
@@ -65,15 +83,21 @@ __global__ void lif_scan_backward_kernel(
     {
         const int t0 = c * K;
         const int t1 = min(T, t0 + K);
-        float U[kMaxSeg];
+        float U[kMaxSeg], g_out[kMaxSeg];
         float V = ckpt[static_cast<long long>(c) * BN + i];
 #pragma unroll
         for (int u = 0; u < kMaxSeg; ++u)
-        {
-            const int t = t0 + u;
-            if (t < t1)
+            if (t0 + u < t1)
             {
-                U[u] = beta * V + I[static_cast<long long>(t) * BN + i];
+                U[u] = I[static_cast<long long>(t0 + u) * BN + i];
+                g_out[u] = dS[static_cast<long long>(t0 + u) * BN + i];
+            }
+#pragma unroll
+        for (int u = 0; u < kMaxSeg; ++u)
+        {
+            if (t0 + u < t1)
+            {
+                U[u] = beta * V + U[u];
                 const float s = relaxed ? fast_sigmoid(U[u] - theta, k) : (U[u] > theta ? 1.0f : 0.0f);
                 V = U[u] - theta * s;
             }
@@ -85,7 +109,7 @@ __global__ void lif_scan_backward_kernel(
             if (t < t1)
             {
                 const float g = surrogate(U[u] - theta, k);
-                const float dU = dS[static_cast<long long>(t) * BN + i] * g + dV * (1.0f - theta * g);
+                const float dU = g_out[u] * g + dV * (1.0f - theta * g);
                 dI[static_cast<long long>(t) * BN + i] = dU;
                 dV = beta * dU;
             }
