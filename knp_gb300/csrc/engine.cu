@@ -2035,9 +2035,11 @@ void Backend::drain_recordings(uint64_t upto)
     const bool by_event = step_ev_of_[ev] == upto;
     cudaStream_t cs = by_event ? copy_stream_ : stream_;
     if (by_event) KNP_CUDA(cudaStreamWaitEvent(copy_stream_, step_ev_[ev], 0));
+    // Every recorded population's bitmaps go to their own span of the pinned buffer, then the
+    // control block; one wait for all of them.
     size_t need = 0;
     for (auto &q : pops_)
-        if (q->record && q->rec_bits) need = std::max<size_t>(need, static_cast<size_t>(steps) * q->rec_words);
+        if (q->record && q->rec_bits) need += static_cast<size_t>(steps) * q->rec_words;
     if (need > rec_host_words_)
     {
         KNP_CUDA(cudaStreamSynchronize(copy_stream_));
@@ -2045,10 +2047,12 @@ void Backend::drain_recordings(uint64_t upto)
         rec_host_ = nullptr;
         size_t cap = 0;
         for (auto &q : pops_)
-            if (q->rec_bits) cap = std::max<size_t>(cap, static_cast<size_t>(q->rec_slots) * q->rec_words);
+            if (q->rec_bits) cap += static_cast<size_t>(q->rec_slots) * q->rec_words;
+        cap = std::max(cap, need);
         KNP_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&rec_host_), cap * 4, cudaHostAllocDefault));
         rec_host_words_ = cap;
     }
+    size_t off = 0;
     for (auto &q : pops_)
     {
         if (!q->record || !q->rec_bits) continue;
@@ -2056,31 +2060,47 @@ void Backend::drain_recordings(uint64_t upto)
         const uint64_t first = drained_to_ % q->rec_slots;
         const uint64_t span1 = std::min<uint64_t>(steps, q->rec_slots - first);
         const size_t W = q->rec_words;
-        KNP_CUDA(cudaMemcpyAsync(rec_host_, q->rec_bits + first * W, span1 * W * 4, cudaMemcpyDeviceToHost, cs));
+        KNP_CUDA(cudaMemcpyAsync(rec_host_ + off, q->rec_bits + first * W, span1 * W * 4, cudaMemcpyDeviceToHost, cs));
         if (span1 < steps)
-            KNP_CUDA(cudaMemcpyAsync(rec_host_ + span1 * W, q->rec_bits, (steps - span1) * W * 4,
+            KNP_CUDA(cudaMemcpyAsync(rec_host_ + off + span1 * W, q->rec_bits, (steps - span1) * W * 4,
                                      cudaMemcpyDeviceToHost, cs));
-        KNP_CUDA(cudaStreamSynchronize(cs));
+        off += static_cast<size_t>(steps) * W;
+    }
+    // Device error flags as of the drained steps (read on the same stream as the bitmaps).
+    KNP_CUDA(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, cs));
+    KNP_CUDA(cudaStreamSynchronize(cs));
+    off = 0;
+    for (auto &q : pops_)
+    {
+        if (!q->record || !q->rec_bits) continue;
+        const size_t W = q->rec_words;
         for (uint64_t k = 0; k < steps; ++k)
         {
             const uint64_t step = drained_to_ + k;
             if (step < q->record_from) continue;
-            const uint32_t *bits = rec_host_ + k * W;
+            const uint32_t *bits = rec_host_ + off + k * W;
             RecordedStep &r = q->recorded[step];
             r.bits.assign(bits, bits + W);
             r.count = 0;
             r.block_prefix.resize((W + kExpandBlockWords - 1) / kExpandBlockWords);
-            for (size_t w = 0; w < W; ++w)
+            // Word pairs (kExpandBlockWords is even, so a block starts on a pair), then an odd last word.
+            size_t w = 0;
+            for (; w + 1 < W; w += 2)
+            {
+                if (w % kExpandBlockWords == 0) r.block_prefix[w / kExpandBlockWords] = r.count;
+                uint64_t pair;
+                std::memcpy(&pair, bits + w, sizeof(pair));
+                r.count += static_cast<uint32_t>(__builtin_popcountll(pair));
+            }
+            if (w < W)
             {
                 if (w % kExpandBlockWords == 0) r.block_prefix[w / kExpandBlockWords] = r.count;
                 r.count += static_cast<uint32_t>(__builtin_popcount(bits[w]));
             }
         }
+        off += static_cast<size_t>(steps) * W;
     }
     drained_to_ = upto;
-    // Device error flags as of the drained steps (read on the same stream as the bitmaps).
-    KNP_CUDA(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Control), cudaMemcpyDeviceToHost, cs));
-    KNP_CUDA(cudaStreamSynchronize(cs));
     if (ctl_host_->error)
         throw Error(KNP_GB300_E_DEVICE_FLAG, "device error flags 0x" + std::to_string(ctl_host_->error));
 }
@@ -2114,13 +2134,19 @@ void expand_bits(const uint32_t *bits, size_t w0, size_t w1, uint32_t k0, uint32
     uint32_t k = k0;
     for (size_t w = w0; w < w1 && k < end; ++w)
     {
-        const uint32_t x = bits[w];
+        uint32_t x = bits[w];
         if (!x) continue;
         const uint32_t base = static_cast<uint32_t>(w * 32);
         if (x == 0xFFFFFFFFu && k + 32 <= end)
         {
             for (uint32_t i = 0; i < 32; ++i) out[k + i] = base + i;
             k += 32;
+            continue;
+        }
+        if (__builtin_popcount(x) <= 4)
+        {
+            // Sparse word (the common case at low firing rates): lowest set bit first.
+            for (; x && k < end; x &= x - 1) out[k++] = base + static_cast<uint32_t>(__builtin_ctz(x));
             continue;
         }
         for (uint32_t j = 0; j < 4; ++j)
