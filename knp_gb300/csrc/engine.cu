@@ -2134,6 +2134,17 @@ void expand_bits(const uint32_t *bits, size_t w0, size_t w1, uint32_t k0, uint32
     uint32_t k = k0;
     for (size_t w = w0; w < w1 && k < end; ++w)
     {
+        // Skip zero word pairs (most words are zero at low firing rates).
+        if (!(w & 1u) && w + 1 < w1)
+        {
+            uint64_t pair;
+            std::memcpy(&pair, bits + w, sizeof(pair));
+            if (!pair)
+            {
+                ++w;
+                continue;
+            }
+        }
         uint32_t x = bits[w];
         if (!x) continue;
         const uint32_t base = static_cast<uint32_t>(w * 32);
