@@ -39,6 +39,15 @@ def test_binding_loads_and_reports_errors_without_gpu(lib_path):
     rate = ctypes.c_double(0.0)
     assert lib.knp_gb300_measure_add_rate(0, 10, ctypes.byref(rate)) != 0
     assert b"positive" in lib.knp_gb300_last_error()
+    # GEMM operand layouts: null buffers, a bad mode and a width below the copied extent are refused
+    # before any launch.
+    assert lib.knp_gb300_bf16_operand(None, 0, 4, 4, 0, 0, 4, None, None) != 0
+    buf = (ctypes.c_float * 16)()
+    out = (ctypes.c_uint16 * 64)()
+    assert lib.knp_gb300_bf16_operand(buf, 0, 4, 4, 3, 0, 4, out, None) != 0
+    assert lib.knp_gb300_bf16_operand(buf, 0, 4, 4, 0, 0, 2, out, None) != 0
+    assert lib.knp_gb300_bf16_operand(buf, 0, 4, 4, 1, 1, 3, out, None) != 0
+    assert b"operand" in lib.knp_gb300_last_error()
 
 
 def test_library_is_built_for_sm_103a_only():

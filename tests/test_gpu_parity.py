@@ -319,6 +319,35 @@ def test_device_synapse_generators(case):
     b.close()
 
 
+def test_device_generator_arguments_are_checked():
+    """knp_gb300_generate_projection refuses what the reference's generators cannot build: an
+    unknown kind, aligned sizes that are not multiples, exclusive and one-to-one with unequal sizes,
+    a probability outside [0, 1], bad weight or delay ranges, a duplicate UID."""
+    from knp_gb300 import backend as B
+    from knp_gb300._capi import KnpGb300Error
+
+    b = B.GB300Backend()
+    pop = N.Population(T.uid_from_int(9901), T.BLIFAT, T.blifat_defaults(100))
+    b.load_populations([pop])
+    u = T.uid_from_int(9902)
+    bad = [dict(kind=9, n_pre=10, n_post=10), dict(kind=T.GEN_ALIGNED, n_pre=10, n_post=4),
+           dict(kind=T.GEN_EXCLUSIVE, n_pre=10, n_post=9), dict(kind=T.GEN_ONE_TO_ONE, n_pre=10, n_post=11),
+           dict(kind=T.GEN_FIXED_PROBABILITY, n_pre=10, n_post=10, probability=1.5),
+           dict(kind=T.GEN_ALL_TO_ALL, n_pre=10, n_post=10, k_lo=5, k_hi=1),
+           dict(kind=T.GEN_ALL_TO_ALL, n_pre=10, n_post=10, d_hi=300)]
+    for a in bad:
+        args = dict(k_lo=0, k_hi=4, d_lo=1, d_hi=4, count=0, probability=0.0)
+        args.update(a)
+        with pytest.raises(KnpGb300Error):
+            b.generate_projection(u, pop.uid, pop.uid, args["kind"], args["n_pre"], args["n_post"], args["k_lo"],
+                                  args["k_hi"], args["d_lo"], args["d_hi"], 1, 2, count=args["count"],
+                                  probability=args["probability"])
+    b.generate_projection(u, pop.uid, pop.uid, T.GEN_ALL_TO_ALL, 100, 100, 0, 4, 1, 4, 1, 2)
+    with pytest.raises(KnpGb300Error):
+        b.generate_projection(u, pop.uid, pop.uid, T.GEN_ALL_TO_ALL, 100, 100, 0, 4, 1, 4, 1, 2)
+    b.close()
+
+
 def _full_size_run(threshold, n, fan, seed, steps, keep):
     """The large sparse config at full size, synapses and background generated on the device, with
     the given gather threshold. Returns (per-step spike digests, spike masks of the last `keep`
