@@ -406,6 +406,18 @@ bool sw128_map(CUtensorMap *map, const void *ptr, int rows, int K)
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The kernel's dynamic shared memory limit raised once per device (a per-device setting).
+template <class Kernel>
+cudaError_t smem_limit_once(Kernel kernel, int bytes, int dev)
+{
+    static std::mutex mu;
+    static std::map<int, cudaError_t> done;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = done.find(dev);
+    if (it != done.end()) return it->second;
+    return done[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 // Stream-ordered pool of the split-K workspaces of device `dev` (memory kept by the pool between
 // calls). Allocating on the call's stream keeps concurrent streams apart and lets a call be captured
 // in a CUDA graph (the allocation becomes a graph memory node).
@@ -448,11 +460,9 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
     CUtensorMap ta, tb;
     if (sw128_map(&ta, A, M, K) && sw128_map(&tb, B, N, K))
     {
-        static const cudaError_t attr_tma = cudaFuncSetAttribute(
-            gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem);
-        if (attr_tma != cudaSuccess) return -3;
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
+        if (smem_limit_once(gemm_tma_kernel, static_cast<int>(kTmaSmem), dev) != cudaSuccess) return -3;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int tiles_m = (M + kBM - 1) / kBM, tiles_n = (N + kBN - 1) / kBN, tiles = tiles_m * tiles_n;
         const int nk = (K + kBK - 1) / kBK;
@@ -486,9 +496,9 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
         }
         return cudaGetLastError() == cudaSuccess ? 0 : -3;
     }
-    static const cudaError_t attr =
-        cudaFuncSetAttribute(gemm_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStages * kStageBytes);
-    if (attr != cudaSuccess) return -3;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (smem_limit_once(gemm_pipe_kernel, static_cast<int>(kStages * kStageBytes), dev) != cudaSuccess) return -3;
     dim3 grid((M + kBM - 1) / kBM, (N + kBN - 1) / kBN);
     gemm_pipe_kernel<<<grid, kThreads, kStages * kStageBytes, s>>>(static_cast<const __nv_bfloat16 *>(A),
                                                                    static_cast<const __nv_bfloat16 *>(B), D, M, N, K, d_err);
