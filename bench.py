@@ -13,6 +13,9 @@ value      synaptic events/s of the K steps with the background schedule already
            CUDA events on the backend's stream (in grid mode the K steps are one launch).
 roofline   the same launch: algorithmic bytes (9 B per synaptic event + 32 B per neuron update + 8 B
            per spike row) over its CUDA-event time, against the measured HBM copy bandwidth.
+           roofline.phases: the window re-run with the kernel's own per-phase timer; the population
+           phase against HBM, the scatter phase against the rate of random FP32 ring adds measured in
+           the same run, and the whole step against the sum of both bounds.
 e2e        the same K steps through the C ABI with host buffers, on a fresh backend that ran the W
            warm-up steps first: every step the host sends the step's background spikes (pinned host ->
            device) and reads the population's spikes back (bitmap device -> host, expanded to indexes),
@@ -21,7 +24,8 @@ cpu_baseline / --impl reference: the restated CPU backend (single-threaded, and 
            backend's structure on all host threads) on the same step window of the config at 1/100
            scale.
 Extra blocks: a saturated window of the same run, the per-phase kernels on the timed window, and the
-batched dense, BPTT and STDP forms.
+batched dense, BPTT and STDP forms. `--form NAME` measures one form alone (`--form gemm`: the tcgen05
+GEMM on the BPTT shapes and 8192^3).
 """
 from __future__ import annotations
 
