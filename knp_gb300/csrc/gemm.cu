@@ -232,27 +232,40 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-constexpr int kTmaStages = 6;
 constexpr int kTmaThreads = 128;
-constexpr uint32_t kTmaSmem = kTmaStages * kStageBytes + 1024;  // + alignment slack
 
-// One 128 x 128 tile of D (or of split blockIdx.z's partial, into `out` with row stride N) over
+// Tile shapes of the TMA-fed kernel: 128 x kTN (kTN = 128, or 256 for large GEMMs: one MMA of
+// N = 256 reads its 8 KB of A per 16-deep step for twice the work, halving shared-memory operand
+// traffic per FLOP). Stages: as many as fit the 227 KB of shared memory.
+template <int kTN>
+struct TmaTile
+{
+    static constexpr uint32_t kBBytes = kTN * kBK * 2;
+    static constexpr uint32_t kStage = kTileBytes + kBBytes;
+    static constexpr int kStages = kTN == 128 ? 6 : 4;
+    static constexpr uint32_t kSmem = kStages * kStage + 1024;  // + alignment slack
+};
+
+// One 128 x kTN tile of D (or of split blockIdx.z's partial, into `out` with row stride N) over
 // chunks [blockIdx.z * cps, min(nk, (blockIdx.z + 1) * cps)). Warp 0 lane 0 issues the TMA copies,
 // warp 1 lane 0 the MMAs; all four warps read the accumulator back.
+template <int kTN>
 __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
     const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, float *__restrict__ out, int M,
     int N, int K, int cps, size_t split_stride, unsigned int *err)
 {
+    using Tile = TmaTile<kTN>;
+    constexpr int kTmaStages = Tile::kStages;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], acc_full, drain;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kTN;
     const int nk = (K + kBK - 1) / kBK;
     const int c0 = blockIdx.z * cps, c1 = min(nk, c0 + cps);
     float *dst = out + blockIdx.z * split_stride;
-    if (warp == 0) tc::tmem_alloc(&tmem_slot, kBN);
+    if (warp == 0) tc::tmem_alloc(&tmem_slot, kTN);
     if (threadIdx.x == 0)
     {
         for (int s = 0; s < kTmaStages; ++s)
@@ -281,8 +294,8 @@ __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
                 s_fail = 1;
                 break;
             }
-            const uint32_t sa = base + s * kStageBytes;
-            mbar_expect_tx(&full[s], kStageBytes);
+            const uint32_t sa = base + s * Tile::kStage;
+            mbar_expect_tx(&full[s], Tile::kStage);
             tma_load_2d(sa, &ta, c * kBK, m0, &full[s]);
             tma_load_2d(sa + kTileBytes, &tb, c * kBK, n0, &full[s]);
             issued = i + 1;
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
     }
     else if (warp == 1 && lane == 0)
     {
-        constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+        constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kTN);
         for (int c = c0; c < c1; ++c)
         {
             const int i = c - c0, s = i % kTmaStages;
@@ -303,7 +316,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
                 break;
             }
             tc::fence_after_sync();
-            const uint32_t sa = base + s * kStageBytes, sb = sa + kTileBytes;
+            const uint32_t sa = base + s * Tile::kStage, sb = sa + kTileBytes;
 #pragma unroll
             for (int j = 0; j < kBK / 16; ++j)
                 tc::mma_bf16(tmem, tc::smem_desc_sw128(sa + j * 32, 1024), tc::smem_desc_sw128(sb + j * 32, 1024),
@@ -324,7 +337,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
         const int row = m0 + threadIdx.x;
         const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
 #pragma unroll 1
-        for (int q0 = 0; q0 < kBN; q0 += 16)
+        for (int q0 = 0; q0 < kTN; q0 += 16)
         {
             float v[16];
             if (c1 > c0)
@@ -355,7 +368,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1) gemm_tma_kernel(
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, kBN);
+    if (warp == 0) tc::tmem_dealloc(tmem, kTN);
 }
 
 // D = sum over the splits of ws[z] (split order), n elements.
@@ -393,29 +406,30 @@ EncodeTiled encode_tiled()
 
 // The (K, rows) view of a row-major [rows][K] BF16 matrix (K a multiple of 8), loaded in 64 x 128
 // boxes with the 128-byte swizzle.
-bool sw128_map(CUtensorMap *map, const void *ptr, int rows, int K)
+bool sw128_map(CUtensorMap *map, const void *ptr, int rows, int K, int box_rows = kBM)
 {
     const EncodeTiled fn = encode_tiled();
     if (!fn) return false;
     const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * 2};
-    const cuuint32_t box[2] = {kBK, kBM};
+    const cuuint32_t box[2] = {kBK, static_cast<cuuint32_t>(box_rows)};
     const cuuint32_t estr[2] = {1, 1};
     return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The kernel's dynamic shared memory limit raised once per device (a per-device setting).
+// The kernel's dynamic shared memory limit raised once per (kernel, device): a per-device setting.
 template <class Kernel>
 cudaError_t smem_limit_once(Kernel kernel, int bytes, int dev)
 {
     static std::mutex mu;
-    static std::map<int, cudaError_t> done;
+    static std::map<std::pair<const void *, int>, cudaError_t> done;
     std::lock_guard<std::mutex> lock(mu);
-    const auto it = done.find(dev);
+    const std::pair<const void *, int> key{reinterpret_cast<const void *>(kernel), dev};
+    const auto it = done.find(key);
     if (it != done.end()) return it->second;
-    return done[dev] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return done[key] = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 // Stream-ordered pool of the split-K workspaces of device `dev` (memory kept by the pool between
@@ -458,14 +472,23 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
     const bool aligned = K % 8 == 0 && (reinterpret_cast<uintptr_t>(A) & 15u) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0;
     if (!aligned) return bf16_gemm_tn_simple(A, B, D, M, N, K, d_err, s);
     CUtensorMap ta, tb;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles_m = (M + kBM - 1) / kBM;
+    const int nk = (K + kBK - 1) / kBK;
+    // 128 x 256 tiles when they alone fill every SM (large GEMMs; no K split then).
+    if (N >= 256 && tiles_m * ((N + 255) / 256) >= sms && sw128_map(&ta, A, M, K) && sw128_map(&tb, B, N, K, 256))
+    {
+        if (smem_limit_once(gemm_tma_kernel<256>, static_cast<int>(TmaTile<256>::kSmem), dev) != cudaSuccess) return -3;
+        dim3 grid(tiles_m, (N + 255) / 256, 1);
+        gemm_tma_kernel<256><<<grid, kTmaThreads, TmaTile<256>::kSmem, s>>>(ta, tb, D, M, N, K, nk, 0, d_err);
+        return cudaGetLastError() == cudaSuccess ? 0 : -3;
+    }
     if (sw128_map(&ta, A, M, K) && sw128_map(&tb, B, N, K))
     {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        if (smem_limit_once(gemm_tma_kernel, static_cast<int>(kTmaSmem), dev) != cudaSuccess) return -3;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int tiles_m = (M + kBM - 1) / kBM, tiles_n = (N + kBN - 1) / kBN, tiles = tiles_m * tiles_n;
-        const int nk = (K + kBK - 1) / kBK;
+        if (smem_limit_once(gemm_tma_kernel<128>, static_cast<int>(TmaTile<128>::kSmem), dev) != cudaSuccess) return -3;
+        const int tiles_n = (N + kBN - 1) / kBN, tiles = tiles_m * tiles_n;
         // Split K when the tiles leave most SMs idle and each split keeps at least 4 chunks.
         int splits = 1;
         if (tiles * 2 <= sms) splits = std::max(1, std::min({16, nk / 4, sms / tiles}));
@@ -486,8 +509,8 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
         }
         const int cps_used = splits > 1 ? cps : nk;
         dim3 grid(tiles_m, tiles_n, splits);
-        gemm_tma_kernel<<<grid, kTmaThreads, kTmaSmem, s>>>(ta, tb, splits > 1 ? ws : D, M, N, K,
-                                                                              cps_used, splits > 1 ? mn : 0, d_err);
+        gemm_tma_kernel<128><<<grid, kTmaThreads, TmaTile<128>::kSmem, s>>>(ta, tb, splits > 1 ? ws : D, M, N, K,
+                                                                          cps_used, splits > 1 ? mn : 0, d_err);
         if (splits > 1)
         {
             const int blocks = static_cast<int>(std::min<size_t>((mn + 255) / 256, 8ull * sms));
@@ -496,8 +519,6 @@ int bf16_gemm_tn(const void *A, const void *B, float *D, int M, int N, int K, un
         }
         return cudaGetLastError() == cudaSuccess ? 0 : -3;
     }
-    int dev = 0;
-    cudaGetDevice(&dev);
     if (smem_limit_once(gemm_pipe_kernel, static_cast<int>(kStages * kStageBytes), dev) != cudaSuccess) return -3;
     dim3 grid((M + kBM - 1) / kBM, (N + kBN - 1) / kBN);
     gemm_pipe_kernel<<<grid, kThreads, kStages * kStageBytes, s>>>(static_cast<const __nv_bfloat16 *>(A),

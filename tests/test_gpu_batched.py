@@ -27,7 +27,8 @@ def _gemm(a, b):
 
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (128, 64, 16), (200, 100, 784), (256, 1000, 1000), (37, 10, 1000),
                                    (300, 260, 8192), (4096, 512, 784), (129, 129, 72), (512, 10, 8200),
-                                   (304, 256, 8192), (512, 64, 4104), (136, 8, 512)])
+                                   (304, 256, 8192), (512, 64, 4104), (136, 8, 512),
+                                   (4864, 1024, 256), (4900, 1000, 200)])  # the last two: 128 x 256 tiles
 def test_bf16_gemm_tn(M, N, K):
     g = torch.Generator(device="cpu").manual_seed(M * 7 + N + K)
     a = (torch.rand(M, K, generator=g) < 0.2).to(torch.bfloat16).cuda()  # 0/1 spike matrix
