@@ -181,7 +181,7 @@ KNP_GB300_API int knp_gb300_generate_fixed_fan_in_projection(
 /**
  * Generate, on the device, a delta projection by one of the reference's synapse generators
  * (knp_generator_kind: all_to_all, aligned (the larger size a multiple of the smaller), exclusive
- * (equal sizes), one_to_one (equal sizes), FixedProbability with
+ * (equal sizes), one_to_one (equal sizes), FixedProbability (at most 2^40 candidate pairs) with
  * `probability`, FixedNumberPost and FixedNumberPre with `count` synapses; `count` and
  * `probability` are ignored by the other kinds). Synapse i connects the pair the generator's index
  * rule gives (FixedProbability: the i-th kept all_to_all pair in index order, each pair kept when

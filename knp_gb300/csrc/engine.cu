@@ -378,6 +378,7 @@ void Backend::generate_projection(const Uid &uid, const Uid &pre_uid, const Uid 
             if (!(probability >= 0.0 && probability <= 1.0))
                 throw Error(KNP_GB300_E_INVALID, "connection probability outside [0, 1]");
             const uint64_t n_cand = static_cast<uint64_t>(n_pre) * n_post;
+            if (n_cand > (1ull << 40)) throw Error(KNP_GB300_E_INVALID, "more than 2^40 candidate pairs");
             thr = static_cast<unsigned long long>(probability * 9007199254740992.0);
             KNP_CUDA(cudaSetDevice(device_));
             KNP_CUDA(gen_candidates(n_cand, thr, stream_key(seed, stream + 5), nullptr, &n_syn, stream_));
