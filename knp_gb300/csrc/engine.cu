@@ -315,9 +315,11 @@ void Backend::upload_locks()
     }
 }
 
-static_assert(kGenAllToAll == KNP_GEN_ALL_TO_ALL && kGenAligned == KNP_GEN_ALIGNED && kGenExclusive == KNP_GEN_EXCLUSIVE &&
-                  kGenOneToOne == KNP_GEN_ONE_TO_ONE && kGenFixedProbability == KNP_GEN_FIXED_PROBABILITY &&
-                  kGenFixedNumberPost == KNP_GEN_FIXED_NUMBER_POST && kGenFixedNumberPre == KNP_GEN_FIXED_NUMBER_PRE,
+static_assert(int(kGenAllToAll) == int(KNP_GEN_ALL_TO_ALL) && int(kGenAligned) == int(KNP_GEN_ALIGNED) &&
+                  int(kGenExclusive) == int(KNP_GEN_EXCLUSIVE) && int(kGenOneToOne) == int(KNP_GEN_ONE_TO_ONE) &&
+                  int(kGenFixedProbability) == int(KNP_GEN_FIXED_PROBABILITY) &&
+                  int(kGenFixedNumberPost) == int(KNP_GEN_FIXED_NUMBER_POST) &&
+                  int(kGenFixedNumberPre) == int(KNP_GEN_FIXED_NUMBER_PRE),
               "generator kinds of the C ABI");
 
 GenSpec Backend::gen_spec(const ProjectionSlot &p, const unsigned long long *cand) const
